@@ -1,0 +1,254 @@
+"""ctypes binding of the C ABI declared in include/beep_gpu.h.
+
+This is the binding a Python caller (or a test) uses; the structures mirror
+the header field for field.  ``Model`` and ``Tables`` keep the numpy arrays
+that back the structures alive for as long as the structures are in use.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+
+_i32p = C.POINTER(C.c_int32)
+_u32p = C.POINTER(C.c_uint32)
+_f64p = C.POINTER(C.c_double)
+
+STATUS = {0: "OK", 1: "BAD_INPUT", 2: "NAN_RATE", 3: "OOM", 4: "TIMEOUT", 5: "DEVICE_ERROR",
+          6: "NO_DEVICE", 7: "COUNT_OVERFLOW"}
+
+FORM_PLAIN_FP64 = 0
+
+
+class ModelDesc(C.Structure):
+    _fields_ = [
+        ("narea", C.c_int32), ("nage", C.c_int32), ("ndemocatpos", C.c_int32), ("nstrain", C.c_int32),
+        ("ncomp", C.c_int32), ("ntrans", C.c_int32),
+        ("ndivision", C.c_int32), ("period", C.c_int32), ("division_per_time", C.c_int32),
+        ("dt", C.c_double), ("popsize", C.c_double),
+        ("trans_from", _i32p), ("trans_to", _i32p), ("infection_trans", C.c_int32), ("democatpos_age", _i32p),
+        ("M_diag", _f64p), ("M_rowptr", _i32p), ("M_to", _i32p), ("M_val", _f64p), ("M_factor", _f64p),
+        ("pop_init", _f64p),
+        ("nobs", C.c_int32),
+        ("obs_sett_i", _i32p), ("obs_sett_f", _i32p), ("obs_value_kind", _i32p), ("obs_value", _f64p),
+        ("obs_model", _i32p), ("obs_sd", _f64p), ("obs_shape", _f64p), ("obs_threshold", _f64p),
+        ("obs_factor", _f64p), ("obs_factor_spline", _i32p), ("obs_cell_ptr", _i32p), ("obs_cells", _i32p),
+    ]
+
+
+class ParamTables(C.Structure):
+    _fields_ = [
+        ("transrate", _f64p), ("susceptibility", _f64p), ("infectivity", _f64p),
+        ("nbeta_row", C.c_int32), ("beta_rows", _f64p), ("beta_row_of", _i32p),
+        ("areafactor", _f64p), ("Ntime", _f64p), ("geo_spline", _f64p),
+        ("nefoi", C.c_int32), ("efoi_spline", _f64p), ("efoi_agedist", _f64p), ("efoi_ref", _i32p),
+        ("nobs_spline", C.c_int32), ("obs_spline", _f64p),
+    ]
+
+
+class SimBatch(C.Structure):
+    _fields_ = [
+        ("nparticle", C.c_int32), ("ngroup", C.c_int32), ("groups", C.POINTER(ParamTables)),
+        ("group_of", _i32p), ("seed", C.c_uint64), ("stream_of", _u32p),
+        ("ti", C.c_int32), ("tf", C.c_int32), ("pop_in", _i32p),
+        ("L_out", _f64p), ("pop_out", _i32p), ("transnum_out", _i32p), ("pop_traj_out", _i32p),
+        ("form", C.c_int32),
+    ]
+
+
+def _ptr(a: Optional[np.ndarray], ctype):
+    if a is None:
+        return C.cast(None, C.POINTER(ctype))
+    assert a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+
+
+def _i32(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.int32))
+
+
+MODEL_INT_ARRAYS = ("trans_from", "trans_to", "democatpos_age", "M_rowptr", "M_to", "obs_sett_i", "obs_sett_f",
+                    "obs_value_kind", "obs_model", "obs_factor_spline", "obs_cell_ptr", "obs_cells")
+MODEL_F64_ARRAYS = ("M_diag", "M_val", "M_factor", "pop_init", "obs_value", "obs_sd", "obs_shape", "obs_threshold",
+                    "obs_factor")
+TABLE_INT_ARRAYS = ("beta_row_of", "efoi_ref")
+TABLE_F64_ARRAYS = ("transrate", "susceptibility", "infectivity", "beta_rows", "areafactor", "Ntime", "geo_spline",
+                    "efoi_spline", "efoi_agedist", "obs_spline")
+
+
+class Model:
+    """Parameter-independent model arrays + the ``beep_model_desc`` over them."""
+
+    def __init__(self, arrays: Dict[str, np.ndarray]):
+        d = arrays
+        dims = [int(x) for x in d["dims"]]
+        (self.narea, self.nage, self.ndemocatpos, self.nstrain, self.ncomp, self.ntrans,
+         self.ndivision, self.period, self.division_per_time) = dims
+        self.dt = float(np.asarray(d["dt"]).reshape(-1)[0])
+        self.popsize = float(np.asarray(d["popsize"]).reshape(-1)[0])
+        self.infection_trans = int(np.asarray(d["infection_trans"]).reshape(-1)[0])
+        self.arr: Dict[str, np.ndarray] = {}
+        for k in MODEL_INT_ARRAYS:
+            self.arr[k] = _i32(d[k]).reshape(-1)
+        for k in MODEL_F64_ARRAYS:
+            self.arr[k] = _f64(d[k]).reshape(-1)
+        self.nobs = int(self.arr["obs_sett_i"].size)
+        self.desc = ModelDesc()
+        for k in ("narea", "nage", "ndemocatpos", "nstrain", "ncomp", "ntrans", "ndivision", "period",
+                  "division_per_time", "infection_trans", "nobs"):
+            setattr(self.desc, k, getattr(self, k))
+        self.desc.dt = self.dt
+        self.desc.popsize = self.popsize
+        for k in MODEL_INT_ARRAYS:
+            setattr(self.desc, k, _ptr(self.arr[k], C.c_int32))
+        for k in MODEL_F64_ARRAYS:
+            setattr(self.desc, k, _ptr(self.arr[k], C.c_double))
+        self.sections = None
+        if "section_ti" in d:
+            self.sections = list(zip(_i32(d["section_ti"]).tolist(), _i32(d["section_tf"]).tolist()))
+
+    @property
+    def pop_size(self) -> int:
+        return self.narea * self.ncomp * self.ndemocatpos
+
+    @property
+    def trans_size(self) -> int:
+        return self.narea * self.ntrans * self.ndemocatpos
+
+
+class Tables:
+    """One parameter set's tables (``beep_param_tables``)."""
+
+    def __init__(self, arrays: Dict[str, np.ndarray], prefix: str = ""):
+        self.arr: Dict[str, np.ndarray] = {}
+        for k in TABLE_INT_ARRAYS:
+            self.arr[k] = _i32(arrays[prefix + k]).reshape(-1)
+        for k in TABLE_F64_ARRAYS:
+            self.arr[k] = _f64(arrays[prefix + k]).reshape(-1)
+        self.shapes = {k: np.asarray(arrays[prefix + k]).shape for k in TABLE_INT_ARRAYS + TABLE_F64_ARRAYS}
+        self.st = ParamTables()
+        for k in TABLE_INT_ARRAYS:
+            setattr(self.st, k, _ptr(self.arr[k], C.c_int32))
+        for k in TABLE_F64_ARRAYS:
+            setattr(self.st, k, _ptr(self.arr[k], C.c_double))
+        self.st.nbeta_row = int(self.shapes["beta_rows"][0])
+        self.st.nefoi = int(self.shapes["efoi_spline"][0])
+        self.st.nobs_spline = int(self.shapes["obs_spline"][0]) if len(self.shapes["obs_spline"]) == 2 else 0
+
+
+class Batch:
+    """A ``beep_sim_batch`` plus the output arrays it writes into."""
+
+    def __init__(self, model: Model, tables: Sequence[Tables], nparticle: int, seed: int, ti: int = 0,
+                 tf: Optional[int] = None, group_of=None, stream_of=None, pop_in=None,
+                 want_L: bool = True, want_pop: bool = False, want_transnum: bool = False,
+                 want_pop_traj: bool = False, form: int = FORM_PLAIN_FP64):
+        tf = model.ndivision if tf is None else tf
+        self.tables = list(tables)
+        self.groups = (ParamTables * max(1, len(self.tables)))(*[t.st for t in self.tables])
+        self.group_of = None if group_of is None else _i32(group_of)
+        self.stream_of = None if stream_of is None else np.ascontiguousarray(np.asarray(stream_of, np.uint32))
+        self.pop_in = None if pop_in is None else _i32(pop_in)
+        ns = tf - ti
+        self.L = np.zeros(nparticle, np.float64) if want_L else None
+        self.pop = np.zeros((nparticle, model.narea, model.ncomp, model.ndemocatpos), np.int32) if want_pop else None
+        self.transnum = (np.zeros((nparticle, ns, model.narea, model.ntrans, model.ndemocatpos), np.int32)
+                         if want_transnum else None)
+        self.pop_traj = (np.zeros((nparticle, ns, model.narea, model.ncomp, model.ndemocatpos), np.int32)
+                         if want_pop_traj else None)
+        b = SimBatch()
+        b.nparticle = nparticle
+        b.ngroup = len(self.tables)
+        b.groups = self.groups
+        b.group_of = _ptr(self.group_of, C.c_int32)
+        b.seed = seed
+        b.stream_of = _ptr(self.stream_of, C.c_uint32)
+        b.ti, b.tf = ti, tf
+        b.pop_in = _ptr(self.pop_in, C.c_int32)
+        b.L_out = _ptr(self.L, C.c_double)
+        b.pop_out = _ptr(self.pop, C.c_int32)
+        b.transnum_out = _ptr(self.transnum, C.c_int32)
+        b.pop_traj_out = _ptr(self.pop_traj, C.c_int32)
+        b.form = form
+        self.st = b
+
+
+def load_model_bundle(arrays: Dict[str, np.ndarray]):
+    """(Model, [Tables per parameter set]) from a bundle's arrays."""
+    m = Model(arrays)
+    ng = int(np.asarray(arrays.get("ngroup", [1])).reshape(-1)[0])
+    return m, [Tables(arrays, f"g{k}.") for k in range(ng)]
+
+
+# ---------------------------------------------------------------------------
+# the CUDA library
+
+_LIB = None
+
+
+def library_path() -> str:
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "libbeep_gpu.so")
+
+
+def lib():
+    """Loads libbeep_gpu.so (built by ``beep_gb300.build``); raises if it is missing."""
+    global _LIB
+    if _LIB is None:
+        path = library_path()
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is missing: build the CUDA library first (beep_gb300.build.build())")
+        L = C.CDLL(path)
+        L.beep_abi_version.restype = C.c_int32
+        L.beep_last_error.restype = C.c_char_p
+        L.beep_device_init.argtypes = [C.c_int32]
+        L.beep_model_create.argtypes = [C.POINTER(ModelDesc), C.POINTER(C.c_void_p)]
+        L.beep_model_destroy.argtypes = [C.c_void_p]
+        L.beep_simulate.argtypes = [C.c_void_p, C.POINTER(SimBatch)]
+        for f in ("beep_device_init", "beep_model_create", "beep_model_destroy", "beep_simulate"):
+            getattr(L, f).restype = C.c_int32
+        _LIB = L
+    return _LIB
+
+
+class BeepError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+def check(status: int) -> None:
+    if status != 0:
+        raise BeepError(status, (lib().beep_last_error() or b"").decode())
+
+
+class DeviceModel:
+    """A ``beep_model`` handle on the GPU."""
+
+    def __init__(self, model: Model, device: int = 0):
+        L = lib()
+        check(L.beep_device_init(device))
+        self.model = model
+        h = C.c_void_p()
+        check(L.beep_model_create(C.byref(model.desc), C.byref(h)))
+        self.h = h
+
+    def simulate(self, batch: Batch) -> Batch:
+        check(lib().beep_simulate(self.h, C.byref(batch.st)))
+        return batch
+
+    def close(self):
+        if self.h:
+            lib().beep_model_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

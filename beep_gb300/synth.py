@@ -1,0 +1,248 @@
+"""Seeded synthetic workloads for the SEIR-H-D model family.
+
+Every workload is generated from a seed by one recipe:
+
+* compartments S, E, I, H, R, D with exponential residence times
+  (E mean 1/sigma, I mean 1/gamma, H mean ``h_mean``) and transitions
+  S->E (infection), E->I, I->H (p_H), I->R (1-p_H), H->D (p_D), H->R (1-p_D);
+* ``narea`` areas with integer populations split over ``nage`` age groups by
+  a Dirichlet(2,...,2) draw;
+* an age-mixing matrix, symmetric, entries U(lo, hi), diagonal multiplied;
+* a gravity area-mixing kernel exp(-d/scale) on U(0,1)^2 coordinates with
+  rows normalised (optionally with random long-range entries);
+* R(t) as a piecewise-linear spline, optional area covariates and stepped
+  age-mixing factors;
+* E individuals seeded in area 0 (Poisson(10));
+* observations: daily E->I counts and weekly H->D counts per area (or per
+  area and age, or weekly H populations), the observed values coming from one
+  simulation at the true parameters plus normal noise of variance
+  max(count, 5), with the standard deviation column loaded from the file
+  ("normal load").
+
+``write_beep_inputs`` writes the workload in the reference's own input format
+(TOML + CSV, the format documented for examples/*.toml of the reference) so
+that the reference itself can run it; ``beep_gb300.model_builder`` builds the
+device tables from the same spec without the reference.
+"""
+from __future__ import annotations
+
+import dataclasses
+import os
+from typing import List, Optional
+
+import numpy as np
+
+
+@dataclasses.dataclass
+class Workload:
+    name: str
+    seed: int
+    narea: int
+    nage: int
+    days: int
+    steps_per_day: int
+    pop: np.ndarray                 # [A][G] int64
+    age_mix: np.ndarray             # [G][G] raw matrix as written to CSV
+    geo: np.ndarray                 # [A][A] raw matrix as written to CSV
+    seed_E: np.ndarray              # [A][G] initial exposed
+    sigma_inv: float = 4.0
+    gamma_inv: float = 5.0
+    h_mean: float = 8.0
+    p_H: float = 0.05
+    p_D: float = 0.2
+    R_bp: List[int] = dataclasses.field(default_factory=list)   # knot days, first 0 last days
+    R_val: List[float] = dataclasses.field(default_factory=list)
+    efoi: float = 0.0
+    covar: Optional[np.ndarray] = None        # [ncovar][A]
+    covar_effect: List[float] = dataclasses.field(default_factory=list)
+    matmod: List[dict] = dataclasses.field(default_factory=list)  # {"ages": [..], "bp": [...], "val": [...]}
+    obs_kind: str = "cases_deaths"            # cases_deaths | cases_age | hosp_pop
+    # prior ranges (inference modes)
+    R_prior: tuple = (0.5, 4.0)
+    sigma_inv_prior: tuple = (2.0, 6.0)
+    gamma_inv_prior: tuple = (3.0, 8.0)
+    h_mean_prior: tuple = (4.0, 12.0)
+
+    @property
+    def ndivision(self) -> int:
+        return self.days * self.steps_per_day
+
+    def age_names(self) -> List[str]:
+        return [f"age{a}" for a in range(self.nage)]
+
+    def area_names(self) -> List[str]:
+        return [f"A{c}" for c in range(self.narea)]
+
+
+def _gravity(rng, n, scale, long_range_frac=0.0, long_range_max=0.01):
+    xy = rng.random((n, 2))
+    d = np.sqrt(((xy[:, None, :] - xy[None, :, :]) ** 2).sum(-1))
+    k = np.exp(-d / scale)
+    if long_range_frac > 0:
+        mask = rng.random((n, n)) < long_range_frac
+        k = k + mask * rng.uniform(0.0, long_range_max, (n, n))
+    k = k / k.sum(1, keepdims=True)
+    return k
+
+
+def _split_pop(rng, total, nage):
+    w = rng.dirichlet([2.0] * nage)
+    parts = np.floor(w * total).astype(np.int64)
+    parts[0] += total - parts.sum()
+    return parts
+
+
+def seir_hd_small(seed: int = 20260000, narea: int = 10, nage: int = 3, days: int = 100,
+                  steps_per_day: int = 4, nknot: int = 5, name: str = "c0") -> Workload:
+    """Plain PMCMC likelihood workload (10 areas x 3 ages, dt 0.25, 100 days)."""
+    rng = np.random.default_rng(seed)
+    totals = rng.integers(50000, 500001, narea)
+    pop = np.stack([_split_pop(rng, int(t), nage) for t in totals])
+    am = rng.uniform(0.5, 2.0, (nage, nage))
+    am = np.triu(am) + np.triu(am, 1).T
+    am[np.diag_indices(nage)] *= 3.0
+    geo = _gravity(rng, narea, 0.2)
+    seedE = np.zeros((narea, nage), np.int64)
+    seedE[0, nage // 2] = max(1, rng.poisson(10))
+    bp = [int(round(k * days / (nknot - 1))) for k in range(nknot)]
+    val = [2.5] + list(rng.uniform(0.6, 2.5, nknot - 1))
+    return Workload(name=name, seed=seed, narea=narea, nage=nage, days=days, steps_per_day=steps_per_day,
+                    pop=pop, age_mix=am, geo=geo, seed_E=seedE, R_bp=bp, R_val=[float(v) for v in val])
+
+
+def _fmt(x) -> str:
+    return repr(float(x))
+
+
+def write_beep_inputs(w: Workload, outdir: str, obs_values: Optional[dict] = None) -> str:
+    """Writes the workload as a reference TOML + CSV directory; returns the TOML path.
+
+    ``obs_values`` maps data-file name -> {column -> (values, sds)}; without it
+    placeholder observations (0, sd 1) of the right shape are written."""
+    os.makedirs(outdir, exist_ok=True)
+    data = os.path.join(outdir, "data")
+    os.makedirs(data, exist_ok=True)
+    A, G = w.narea, w.nage
+    ages, areas = w.age_names(), w.area_names()
+
+    with open(os.path.join(data, "population.csv"), "w") as f:
+        cols = ["area"] + (ages if G > 1 else ["population"])
+        if w.covar is not None:
+            cols += [f"cov{j}" for j in range(w.covar.shape[0])]
+        f.write(",".join(cols) + "\n")
+        for c in range(A):
+            row = [areas[c]] + [str(int(v)) for v in w.pop[c]]
+            if w.covar is not None:
+                row += [_fmt(w.covar[j, c]) for j in range(w.covar.shape[0])]
+            f.write(",".join(row) + "\n")
+    if G > 1:
+        with open(os.path.join(data, "age_mixing_matrix.csv"), "w") as f:
+            for a in range(G):
+                f.write(",".join(_fmt(v) for v in w.age_mix[a]) + "\n")
+    if A > 1:
+        with open(os.path.join(data, "geo_mixing_matrix.csv"), "w") as f:
+            for c in range(A):
+                f.write(",".join(_fmt(v) for v in w.geo[c]) + "\n")
+    comps = ["S", "E", "I", "H", "R", "D"]
+    with open(os.path.join(data, "init_pop.csv"), "w") as f:
+        f.write("area," + ("age," if G > 1 else "") + "compartment,population\n")
+        for c in range(A):
+            for a in range(G):
+                for co in comps:
+                    if co == "S":
+                        v = int(w.pop[c, a] - w.seed_E[c, a])
+                    elif co == "E":
+                        v = int(w.seed_E[c, a])
+                    else:
+                        v = 0
+                    f.write(f"{areas[c]}," + (f"{ages[a]}," if G > 1 else "") + f"{co},{v}\n")
+
+    tables = data_tables(w)
+    for tab in tables:
+        rows = tab["times"]
+        cols = tab["columns"]
+        vals = (obs_values or {}).get(tab["file"])
+        with open(os.path.join(data, tab["file"]), "w") as f:
+            f.write("time," + ",".join(f"{c},{c} SD" for c in cols) + "\n")
+            for r, t in enumerate(rows):
+                cells = []
+                for c in cols:
+                    if vals is None:
+                        cells += ["0", "1"]
+                    else:
+                        v, sd = vals[c]
+                        cells += [str(int(v[r])), _fmt(sd[r])]
+                f.write(f"{t}," + ",".join(cells) + "\n")
+
+    nk = len(w.R_bp)
+    bp = "|".join(["start"] + [str(b) for b in w.R_bp[1:-1]] + ["end"])
+    rval = "|".join(_fmt(v) for v in w.R_val)
+    rprior = "|".join([f"Uniform({w.R_prior[0]},{w.R_prior[1]})"] * nk)
+    lines = [
+        'time_format = "number"',
+        'start = "0"',
+        f'end = "{w.days}"',
+        f'steps_per_unit_time = {w.steps_per_day}',
+        'datadir = "data"',
+        'outputdir = "output"',
+        'areas = "population.csv"',
+        'init_pop = "init_pop.csv"',
+    ]
+    if G > 1:
+        lines.append('ages = {cats="' + " | ".join(ages) + '"}')
+        lines.append('age_mixing_matrix = "age_mixing_matrix.csv"')
+    if A > 1:
+        lines.append('geo_mixing_matrix = "geo_mixing_matrix.csv"')
+    lines += [
+        "comps = [",
+        '{name="S"},',
+        f'{{name="E", dist="Exp", mean_value="{_fmt(w.sigma_inv)}", mean_prior="Uniform({w.sigma_inv_prior[0]},{w.sigma_inv_prior[1]})"}},',
+        f'{{name="I", dist="Exp", mean_value="{_fmt(w.gamma_inv)}", inf_value="1", mean_prior="Uniform({w.gamma_inv_prior[0]},{w.gamma_inv_prior[1]})"}},',
+        f'{{name="H", dist="Exp", mean_value="{_fmt(w.h_mean)}", mean_prior="Uniform({w.h_mean_prior[0]},{w.h_mean_prior[1]})"}},',
+        '{name="R"},',
+        '{name="D"}',
+        "]",
+        "trans = [",
+        '{from="S", to="E", infection="yes"},',
+        '{from="E", to="I"},',
+        f'{{from="I", to="H", prob_value="{_fmt(w.p_H)}", prob_prior="Dir(1)"}},',
+        '{from="I", to="R", prob_value="*", prob_prior="Dir(1)"},',
+        f'{{from="H", to="D", prob_value="{_fmt(w.p_D)}", prob_prior="Dir(1)"}},',
+        '{from="H", to="R", prob_value="*", prob_prior="Dir(1)"}',
+        "]",
+        f'R_spline = [{{ value="{rval}", prior="{rprior}", bp="{bp}"}}]',
+        f'efoi_spline = [{{ value="{_fmt(w.efoi)}"}}]',
+        "data_tables = [",
+    ]
+    for tab in tables:
+        lines.append("{" + ", ".join(f'{k}="{v}"' for k, v in tab["toml"].items()) + "},")
+    lines += ["]"]
+    toml = os.path.join(outdir, f"{w.name}.toml")
+    with open(toml, "w") as f:
+        f.write("\n".join(lines) + "\n")
+    return toml
+
+
+def data_tables(w: Workload) -> List[dict]:
+    """The observation tables of the workload, in the order they are declared."""
+    areas = w.area_names()
+    tabs = []
+    if w.obs_kind == "cases_deaths":
+        tabs.append(dict(file="cases.csv", times=list(range(0, w.days)), columns=areas,
+                         toml=dict(type="transition", observation="E->I", timestep="1", obsmodel="normal load",
+                                   geo_dep="area", file="cases.csv")))
+        tabs.append(dict(file="deaths.csv", times=list(range(0, w.days - 6, 7)), columns=areas,
+                         toml=dict(type="transition", observation="H->D", timestep="7", obsmodel="normal load",
+                                   geo_dep="area", file="deaths.csv")))
+    elif w.obs_kind == "cases_age":
+        for a, an in enumerate(w.age_names()):
+            tabs.append(dict(file=f"cases_{an}.csv", times=list(range(0, w.days)), columns=areas,
+                             toml=dict(type="transition", observation="E->I", timestep="1", obsmodel="normal load",
+                                       geo_dep="area", democats_filt=f"age:{an}", file=f"cases_{an}.csv")))
+    elif w.obs_kind == "hosp_pop":
+        tabs.append(dict(file="hosp.csv", times=list(range(0, w.days, 7)), columns=areas,
+                         toml=dict(type="population", observation="H", obsmodel="normal load",
+                                   geo_dep="area", file="hosp.csv")))
+    else:
+        raise ValueError(w.obs_kind)
+    return tabs

@@ -1,0 +1,176 @@
+/* beep_gpu.h -- C ABI of the GB300 implementation of BEEP's tau-leap
+ * simulation and observation log-likelihood.
+ *
+ * The reference has no plugin interface: the hot path is the in-process C++
+ * class State (src/state.hh:14-134) with ObservationModel
+ * (src/obsmodel.hh:10-41).  A caller that already ran State::set_param for a
+ * parameter set (src/state.cc:66-91) holds every table the path reads; this
+ * ABI takes those tables as plain arrays and returns what the reference would
+ * have stored in State (transnum, pop) and what ObservationModel::calculate /
+ * calculate_section would have returned (the log-likelihood L, EF = -2 L).
+ *
+ * Conventions
+ *  - All sizes are int32_t, all real tables are IEEE double, counts int32_t.
+ *  - Arrays are row-major in the index order of the reference's nested
+ *    vectors, e.g. transnum[sett][c][tr][dp] (src/state.hh:25).
+ *  - Every entry point returns beep_status; beep_last_error() gives the text
+ *    of the last failure on the calling thread.  The library never exits the
+ *    process (the reference calls exit() through emsg, src/utils.cc:296-316).
+ *  - Random variates come from a keyed counter-based stream (Philox4x32-10),
+ *    key = seed, counter = (cell, step, stream, purpose|iteration), so any
+ *    particle's trajectory is reproducible from (seed, stream) alone.
+ */
+#ifndef BEEP_GPU_H
+#define BEEP_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BEEP_GPU_ABI_VERSION 1
+
+typedef enum beep_status {
+	BEEP_OK = 0,
+	BEEP_BAD_INPUT = 1,      /* inconsistent sizes, indices out of range, NULL where required */
+	BEEP_NAN_RATE = 2,       /* a transition mean was NaN (reference: emsgEC("State",4)) */
+	BEEP_OOM = 3,            /* device or host allocation failed */
+	BEEP_TIMEOUT = 4,        /* a bounded device wait gave up */
+	BEEP_DEVICE_ERROR = 5,   /* CUDA runtime error */
+	BEEP_NO_DEVICE = 6,      /* no CUDA device, or the kernels were not built for it */
+	BEEP_COUNT_OVERFLOW = 7  /* a draw or a population left the int32 range */
+} beep_status;
+
+/* Observation model of one observation (src/consts.hh:42, ObsModelFunc). */
+enum beep_obs_model {
+	BEEP_OBS_NORMAL = 0,
+	BEEP_OBS_NORMAL_PERCENT = 1,
+	BEEP_OBS_POISSON = 2,
+	BEEP_OBS_NEGBIN = 3
+};
+
+/* Kind of observed value (src/consts.hh:160-161: THRESH, UNKNOWN sentinels). */
+enum beep_obs_value_kind {
+	BEEP_OBSVAL_VALUE = 0,
+	BEEP_OBSVAL_UNKNOWN = 1,
+	BEEP_OBSVAL_THRESH = 2
+};
+
+/* Encoding of an observation's contributing cells (the reference's
+ * obs_trans / obs_pop index, src/obsmodel.cc:174-217):
+ *   cell >= 0 : transition cell, cell = (c*ntrans + tr)*ndemocatpos + dp
+ *   cell <  0 : population cell, -1-cell = (c*ncomp + co)*ndemocatpos + dp
+ * The cells of one observation are listed in the order the reference visits
+ * them (c, then transitions before populations, then tr or co, then dp). */
+#define BEEP_POP_CELL(c, co, dp, ncomp, ndp) (-1 - (((c) * (ncomp) + (co)) * (ndp) + (dp)))
+
+/* Parameter-independent model: what State::simulate and ObservationModel read
+ * from Details, Data and Model.  Host pointers; copied at beep_model_create. */
+typedef struct beep_model_desc {
+	int32_t narea, nage, ndemocatpos, nstrain, ncomp, ntrans;
+	int32_t ndivision;          /* steps, Details::ndivision */
+	int32_t period;             /* Details::period (areafactor rows) */
+	int32_t division_per_time;  /* Details::division_per_time */
+	double dt;                  /* double(period)/ndivision (src/state.cc:384) */
+	double popsize;             /* Data::popsize */
+
+	const int32_t *trans_from;      /* [ntrans] */
+	const int32_t *trans_to;        /* [ntrans] */
+	int32_t infection_trans;        /* Model::infection_trans */
+	const int32_t *democatpos_age;  /* [ndemocatpos/nstrain] Data::democatpos[dp][0] */
+
+	/* geographic mixing Data::genQ.M (src/struct.hh:232-237) and genQ.factor */
+	const double *M_diag;       /* [narea] */
+	const int32_t *M_rowptr;    /* [narea+1] row c lists genQ.M.to[c] / val[c] */
+	const int32_t *M_to;        /* [nnz] */
+	const double *M_val;        /* [nnz] */
+	const double *M_factor;     /* [narea] */
+
+	const double *pop_init;     /* [narea][ncomp][ndemocatpos] Area::pop_init, integer-valued */
+
+	/* observations Data::obs (src/struct.hh:340-354) */
+	int32_t nobs;
+	const int32_t *obs_sett_i;      /* [nobs] */
+	const int32_t *obs_sett_f;      /* [nobs] */
+	const int32_t *obs_value_kind;  /* [nobs] beep_obs_value_kind */
+	const double *obs_value;        /* [nobs] */
+	const int32_t *obs_model;       /* [nobs] beep_obs_model */
+	const double *obs_sd;           /* [nobs] (normal models) */
+	const double *obs_shape;        /* [nobs] (negative binomial) */
+	const double *obs_threshold;    /* [nobs] datatable threshold (THRESH values) */
+	const double *obs_factor;       /* [nobs] */
+	const int32_t *obs_factor_spline; /* [nobs] row of beep_param_tables.obs_spline, or -1 */
+	const int32_t *obs_cell_ptr;    /* [nobs+1] */
+	const int32_t *obs_cells;       /* [obs_cell_ptr[nobs]] encoded cells */
+} beep_model_desc;
+
+/* Tables that State::set_param derives from one parameter set θ
+ * (src/state.cc:66-91; src/model.cc:1010-1362).  Host pointers. */
+typedef struct beep_param_tables {
+	const double *transrate;      /* [ntrans][ndemocatpos] */
+	const double *susceptibility; /* [ndemocatpos] */
+	const double *infectivity;    /* [ncomp] paramval[comp[co].infectivity_param] */
+	int32_t nbeta_row;
+	const double *beta_rows;      /* [nbeta_row][ndivision] beta[st][c][.] rows */
+	const int32_t *beta_row_of;   /* [nstrain][narea] row of beta_rows */
+	const double *areafactor;     /* [period][narea] */
+	const double *Ntime;          /* [ndivision][nage][nage] */
+	const double *geo_spline;     /* [ndivision] disc_spline[geo_spline_ref] */
+	int32_t nefoi;
+	const double *efoi_spline;    /* [nefoi][ndivision] disc_spline of each efoi spline */
+	const double *efoi_agedist;   /* [nefoi][nage] */
+	const int32_t *efoi_ref;      /* [nstrain][narea] Model::efoi_spl_ref */
+	int32_t nobs_spline;
+	const double *obs_spline;     /* [nobs_spline][ndivision] factor splines of observations */
+} beep_param_tables;
+
+/* Arithmetic form of the kernels. */
+enum beep_form {
+	BEEP_FORM_PLAIN_FP64 = 0  /* FP64 in the reference's summation order: bit-exact transnum/pop */
+};
+
+/* One batch of particles advanced over steps [ti, tf): State::simulate(ti,tf)
+ * (src/state.cc:596-638) followed by the observation log-likelihood over the
+ * observations whose window lies inside [ti, tf) -- all observations for
+ * (0, ndivision) as in ObservationModel::calculate (src/obsmodel.cc:22-35),
+ * a filter section's observations as in calculate_section (:39-58).
+ * Host pointers unless the entry point says otherwise. */
+typedef struct beep_sim_batch {
+	int32_t nparticle;
+	int32_t ngroup;                      /* parameter sets */
+	const beep_param_tables *groups;     /* [ngroup] */
+	const int32_t *group_of;             /* [nparticle] or NULL (all particles use group 0) */
+	uint64_t seed;                       /* Philox key */
+	const uint32_t *stream_of;           /* [nparticle] or NULL (stream = particle index) */
+	int32_t ti, tf;                      /* 0 <= ti < tf <= ndivision */
+	const int32_t *pop_in;               /* [nparticle][narea][ncomp][ndemocatpos] pop[ti]; NULL when ti == 0 (Area::pop_init) */
+	double *L_out;                       /* [nparticle] log-likelihood, or NULL */
+	int32_t *pop_out;                    /* [nparticle][narea][ncomp][ndemocatpos] pop[tf] (pop[tf-1] updated by step tf-1), or NULL */
+	int32_t *transnum_out;               /* [nparticle][tf-ti][narea][ntrans][ndemocatpos], or NULL */
+	int32_t *pop_traj_out;               /* [nparticle][tf-ti][narea][ncomp][ndemocatpos] pop[ti..tf-1], or NULL */
+	int32_t form;                        /* beep_form */
+} beep_sim_batch;
+
+typedef struct beep_model beep_model;    /* device-resident model + work buffers */
+
+/* Library and device. */
+int32_t beep_abi_version(void);
+const char *beep_last_error(void);
+beep_status beep_device_init(int32_t device);
+
+/* Model lifetime (replaces constructing Data/Model/ObservationModel for the
+ * hot path: src/main.cc:148-160). */
+beep_status beep_model_create(const beep_model_desc *desc, beep_model **out);
+beep_status beep_model_destroy(beep_model *model);
+
+/* State::simulate for a batch (src/state.cc:582-638 + src/obsmodel.cc:22-58).
+ * Host buffers; host<->device copies happen inside the call. */
+beep_status beep_simulate(beep_model *model, const beep_sim_batch *batch);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

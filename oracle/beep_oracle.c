@@ -1,0 +1,466 @@
+/* beep_oracle.c -- CPU restatement of the reference's tau-leap + observation
+ * log-likelihood.  TEST INFRASTRUCTURE ONLY (parity checker and the timed CPU
+ * baseline); see beep_oracle.h for the reference functions it follows.
+ * Build with -ffp-contract=off so every FP64 operation is rounded as written. */
+#include "beep_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "beep_rng_ref.h"
+
+double beep_oracle_exp(double x) { return beep_exp(x); }
+double beep_oracle_log(double x) { return beep_log(x); }
+double beep_oracle_log_factorial(double k) { return beep_log_factorial(k); }
+
+int32_t beep_oracle_poisson(double mean, uint64_t seed, uint32_t cell, uint32_t step,
+                            uint32_t stream, uint32_t purpose)
+{
+	return beep_poisson_ref(mean, (uint32_t)seed, (uint32_t)(seed >> 32), cell, step, stream, purpose);
+}
+
+/* ---- log-densities: src/utils.cc:107-170 ------------------------------- */
+
+static double normal_probability(double x, double mean, double var)
+{
+	return -0.5 * log(2 * M_PI * var) - (x - mean) * (x - mean) / (2 * var);
+}
+
+static double poisson_probability(int i, double lam)
+{
+	if (lam == 0) return i == 0 ? 0 : -1000000000.0;
+	if (i < 0) return -1000000000.0;
+	return i * log(lam) - lam - lgamma(i + 1);
+}
+
+static double negative_binomial_probability(unsigned int val, double m, double shape)
+{
+	return lgamma(shape + val) - lgamma(val + 1) - lgamma(shape) + shape * log(shape / (shape + m))
+	       + val * log(m / (shape + m));
+}
+
+/* ObservationModel::obs_prob, src/obsmodel.cc:245-305 */
+double beep_oracle_obs_prob(double value, int32_t value_kind, double val, int32_t model,
+                            double sd, double shape, double thresh)
+{
+	if (value < 0) value = 0;
+	if (value_kind == BEEP_OBSVAL_UNKNOWN) return 0;
+	if (value_kind == BEEP_OBSVAL_THRESH) {
+		switch (model) {
+		case BEEP_OBS_NORMAL:
+		case BEEP_OBS_NORMAL_PERCENT:
+			if (value < thresh) return normal_probability(thresh, thresh, sd * sd);
+			return normal_probability(thresh, value, sd * sd);
+		case BEEP_OBS_POISSON: {
+			double lam = value; if (lam < 1) lam = 1;
+			double sum = 0.0;
+			for (double v = 0; v <= thresh; v++) sum += exp(poisson_probability((int)v, lam));
+			return log(sum);
+		}
+		case BEEP_OBS_NEGBIN: {
+			double mm = value; if (mm < 1) mm = 1;
+			double sum = 0.0;
+			for (double v = 0; v <= thresh; v++) sum += exp(negative_binomial_probability((unsigned)v, mm, shape));
+			return log(sum);
+		}
+		}
+		return NAN;
+	}
+	switch (model) {
+	case BEEP_OBS_NORMAL:
+	case BEEP_OBS_NORMAL_PERCENT:
+		return normal_probability(val, value, sd * sd);
+	case BEEP_OBS_POISSON: {
+		double lam = value; if (lam < 1) lam = 1;
+		return poisson_probability((int)(val + 0.5), lam);
+	}
+	case BEEP_OBS_NEGBIN: {
+		double mm = value; if (mm < 1) mm = 1;
+		return negative_binomial_probability((unsigned)(int)(val + 0.5), mm, shape);
+	}
+	}
+	return NAN;
+}
+
+/* ---- per-batch observation index (src/obsmodel.cc:174-217) -------------- */
+
+typedef struct {
+	int32_t ti, tf;
+	int32_t ncell_t, ncell_p;
+	int32_t *t_ptr, *t_obs;   /* [(tf-ti)*ncell_t + 1], obs lists of transition cells */
+	int32_t *p_ptr, *p_obs;   /* same for population cells */
+	int32_t *scored;          /* observation indices scored, ascending */
+	int32_t nscored;
+} obs_index;
+
+static void obs_index_free(obs_index *ix)
+{
+	free(ix->t_ptr); free(ix->t_obs); free(ix->p_ptr); free(ix->p_obs); free(ix->scored);
+}
+
+static int obs_index_build(const beep_model_desc *m, int32_t ti, int32_t tf, obs_index *ix)
+{
+	memset(ix, 0, sizeof *ix);
+	ix->ti = ti; ix->tf = tf;
+	int32_t ns = tf - ti;
+	ix->ncell_t = m->narea * m->ntrans * m->ndemocatpos;
+	ix->ncell_p = m->narea * m->ncomp * m->ndemocatpos;
+	size_t nt = (size_t)ns * ix->ncell_t, np = (size_t)ns * ix->ncell_p;
+	ix->t_ptr = calloc(nt + 1, sizeof(int32_t));
+	ix->p_ptr = calloc(np + 1, sizeof(int32_t));
+	ix->scored = malloc(sizeof(int32_t) * (size_t)(m->nobs > 0 ? m->nobs : 1));
+	if (!ix->t_ptr || !ix->p_ptr || !ix->scored) return BEEP_OOM;
+	for (int32_t i = 0; i < m->nobs; i++) {
+		if (m->obs_sett_i[i] >= ti && m->obs_sett_f[i] <= tf) ix->scored[ix->nscored++] = i;
+	}
+	for (int pass = 0; pass < 2; pass++) {
+		for (int32_t k = 0; k < ix->nscored; k++) {
+			int32_t i = ix->scored[k];
+			for (int32_t s = m->obs_sett_i[i]; s < m->obs_sett_f[i]; s++) {
+				for (int32_t q = m->obs_cell_ptr[i]; q < m->obs_cell_ptr[i + 1]; q++) {
+					int32_t cell = m->obs_cells[q];
+					if (cell >= 0) {
+						size_t slot = (size_t)(s - ti) * ix->ncell_t + cell;
+						if (pass == 0) ix->t_ptr[slot + 1]++;
+						else ix->t_obs[ix->t_ptr[slot]++] = i;
+					} else {
+						size_t slot = (size_t)(s - ti) * ix->ncell_p + (size_t)(-1 - cell);
+						if (pass == 0) ix->p_ptr[slot + 1]++;
+						else ix->p_obs[ix->p_ptr[slot]++] = i;
+					}
+				}
+			}
+		}
+		if (pass == 0) {
+			for (size_t k = 0; k < nt; k++) ix->t_ptr[k + 1] += ix->t_ptr[k];
+			for (size_t k = 0; k < np; k++) ix->p_ptr[k + 1] += ix->p_ptr[k];
+			ix->t_obs = malloc(sizeof(int32_t) * (size_t)(ix->t_ptr[nt] + 1));
+			ix->p_obs = malloc(sizeof(int32_t) * (size_t)(ix->p_ptr[np] + 1));
+			if (!ix->t_obs || !ix->p_obs) return BEEP_OOM;
+		} else {
+			/* the fill pass advanced each start to the next start: shift back */
+			for (size_t k = nt; k > 0; k--) ix->t_ptr[k] = ix->t_ptr[k - 1];
+			ix->t_ptr[0] = 0;
+			for (size_t k = np; k > 0; k--) ix->p_ptr[k] = ix->p_ptr[k - 1];
+			ix->p_ptr[0] = 0;
+		}
+	}
+	return BEEP_OK;
+}
+
+/* ---- one particle ------------------------------------------------------- */
+
+typedef struct {
+	double *pop, *popnext;      /* [A][C][DP] */
+	double *Imap, *Idiag;       /* [nstrain][A*G] */
+	double *dinf, *NMI, *I, *eta; /* [G] */
+	double *tmean;              /* [T][DP] */
+	int32_t *tn_traj;           /* [(tf-ti)][A][T][DP] */
+	double *pop_traj;           /* [(tf-ti)][A][C][DP] */
+	double *obs_value;          /* [nobs] */
+	double *infdif;             /* [T] */
+} work;
+
+static void scatter_inf(const beep_model_desc *m, const double *dinf, int32_t c,
+                        double *Ima, double *Idia)
+{
+	int32_t G = m->nage;
+	double diag = m->M_diag[c];
+	int32_t j0 = m->M_rowptr[c], j1 = m->M_rowptr[c + 1];
+	int32_t v = c * G;
+	for (int32_t a = 0; a < G; a++) {
+		double di = dinf[a];
+		if (di != 0) {
+			Idia[v + a] += di * diag;
+			for (int32_t j = j0; j < j1; j++) Ima[m->M_to[j] * G + a] += di * m->M_val[j];
+		}
+	}
+}
+
+static int simulate_particle(const beep_model_desc *m, const beep_sim_batch *b, const obs_index *ix,
+                             int32_t p, work *w)
+{
+	const int32_t A = m->narea, G = m->nage, C = m->ncomp, T = m->ntrans, DP = m->ndemocatpos;
+	const int32_t NS = m->nstrain, DPS = DP / NS;
+	const size_t popsz = (size_t)A * C * DP, tnsz = (size_t)A * T * DP, AG = (size_t)A * G;
+	const int32_t grp = b->group_of ? b->group_of[p] : 0;
+	const beep_param_tables *tb = &b->groups[grp];
+	const uint32_t stream = b->stream_of ? b->stream_of[p] : (uint32_t)p;
+	const uint32_t k0 = (uint32_t)b->seed, k1 = (uint32_t)(b->seed >> 32);
+
+	for (int32_t tr = 0; tr < T; tr++)
+		w->infdif[tr] = tb->infectivity[m->trans_to[tr]] - tb->infectivity[m->trans_from[tr]];
+
+	if (b->ti == 0) memcpy(w->pop, m->pop_init, sizeof(double) * popsz);
+	else for (size_t k = 0; k < popsz; k++) w->pop[k] = (double)b->pop_in[(size_t)p * popsz + k];
+
+	for (int32_t sett = b->ti; sett < b->tf; sett++) {
+		int32_t *tn = w->tn_traj + (size_t)(sett - b->ti) * tnsz;
+		if (sett == b->ti) {                               /* set_I_from_pop, src/state.cc:223-290 */
+			memset(w->Imap, 0, sizeof(double) * AG * NS);
+			memset(w->Idiag, 0, sizeof(double) * AG * NS);
+			for (int32_t st = 0; st < NS; st++) {
+				for (int32_t c = 0; c < A; c++) {
+					for (int32_t a = 0; a < G; a++) w->dinf[a] = 0;
+					for (int32_t co = 0; co < C; co++) {
+						double inf = tb->infectivity[co];
+						if (inf != 0) {
+							int32_t dpp = st * DPS;
+							for (int32_t dp = 0; dp < DPS; dp++) {
+								double pv = w->pop[((size_t)c * C + co) * DP + dpp];
+								if (pv != 0) w->dinf[m->democatpos_age[dp]] += inf * pv;
+								dpp++;
+							}
+						}
+					}
+					scatter_inf(m, w->dinf, c, w->Imap + st * AG, w->Idiag + st * AG);
+				}
+			}
+		} else {                                           /* update_I_from_transnum, src/state.cc:178-219 */
+			const int32_t *tprev = tn - tnsz;
+			for (int32_t st = 0; st < NS; st++) {
+				for (int32_t c = 0; c < A; c++) {
+					for (int32_t a = 0; a < G; a++) w->dinf[a] = 0;
+					for (int32_t tr = 0; tr < T; tr++) {
+						double di = w->infdif[tr];
+						if (di != 0) {
+							int32_t dpp = st * DPS;
+							for (int32_t dp = 0; dp < DPS; dp++) {
+								double num = (double)tprev[((size_t)c * T + tr) * DP + dpp];
+								if (num != 0) w->dinf[m->democatpos_age[dp]] += di * num;
+								dpp++;
+							}
+						}
+					}
+					scatter_inf(m, w->dinf, c, w->Imap + st * AG, w->Idiag + st * AG);
+				}
+			}
+		}
+
+		for (int32_t c = 0; c < A; c++) {                 /* set_transmean, src/state.cc:380-456 */
+			double *pc = w->pop + (size_t)c * C * DP;
+			int32_t itr = m->infection_trans;
+			double *sus_pop = pc + (size_t)m->trans_from[itr] * DP;
+			if (NS > 1) {
+				for (int32_t dp = 0; dp < DPS; dp++) {
+					double sum = 0.0;
+					for (int32_t st = 1; st < NS; st++) {
+						int32_t dpp = DPS * st + dp;
+						sum += sus_pop[dpp]; sus_pop[dpp] = 0;
+					}
+					sus_pop[dp] += sum;
+				}
+			}
+			for (int32_t st = 0; st < NS; st++) {
+				/* get_NMI, src/state.cc:547-578 */
+				const double *Id = w->Idiag + st * AG, *Im = w->Imap + st * AG;
+				double d = tb->geo_spline[sett];
+				double omd = 1 - d;
+				double fac = m->M_factor[c];
+				if (G == 1) {
+					double val = Id[c] * (d + fac * omd) + Im[c] * d;
+					if (val < 0) val = 0;
+					w->NMI[0] = val;
+				} else {
+					int32_t v = c * G;
+					for (int32_t a = 0; a < G; a++) w->I[a] = (Id[v + a] + Im[v + a]) * d + fac * Id[v + a] * omd;
+					const double *N = tb->Ntime + (size_t)sett * G * G;
+					for (int32_t a = 0; a < G; a++) {
+						double sum = 0.0;
+						for (int32_t aa = 0; aa < G; aa++) sum += N[a * G + aa] * w->I[aa];
+						if (sum < 0) sum = 0;
+						w->NMI[a] = sum;
+					}
+				}
+				double be = tb->beta_rows[(size_t)tb->beta_row_of[st * A + c] * m->ndivision + sett];
+				be *= tb->areafactor[(size_t)(sett / m->division_per_time) * A + c];
+				int32_t ei = tb->efoi_ref[st * A + c];
+				double et = tb->efoi_spline[(size_t)ei * m->ndivision + sett] / m->popsize;
+				for (int32_t a = 0; a < G; a++) w->eta[a] = et * tb->efoi_agedist[(size_t)ei * G + a];
+				int32_t dpp = st * DPS;
+				for (int32_t dp = 0; dp < DPS; dp++) {
+					double popu = sus_pop[dp];
+					if (popu <= 0) w->tmean[itr * DP + dpp] = 0;
+					else {
+						int32_t a = m->democatpos_age[dp];
+						double v = m->dt * popu * tb->susceptibility[dpp] * (be * w->NMI[a] + w->eta[a]);
+						if (v != v) return BEEP_NAN_RATE;
+						w->tmean[itr * DP + dpp] = v;
+					}
+					dpp++;
+				}
+			}
+			for (int32_t tr = 0; tr < T; tr++) {
+				if (tr == itr) continue;
+				int32_t from = m->trans_from[tr];
+				for (int32_t dp = 0; dp < DP; dp++) {
+					double popu = pc[(size_t)from * DP + dp];
+					if (popu <= 0) w->tmean[tr * DP + dp] = 0;
+					else w->tmean[tr * DP + dp] = m->dt * popu * tb->transrate[(size_t)tr * DP + dp];
+				}
+			}
+			for (int32_t tr = 0; tr < T; tr++) {           /* draws, src/state.cc:614-631 */
+				for (int32_t dp = 0; dp < DP; dp++) {
+					double mean = w->tmean[tr * DP + dp];
+					int32_t cell = (c * T + tr) * DP + dp;
+					if (mean == 0) tn[cell] = 0;
+					else {
+						if (mean > 1000000000.0) return BEEP_COUNT_OVERFLOW;
+						tn[cell] = beep_poisson_ref(mean, k0, k1, (uint32_t)cell, (uint32_t)sett, stream,
+						                            BEEP_PURPOSE_TRANS);
+					}
+				}
+			}
+		}
+		memcpy(w->pop_traj + (size_t)(sett - b->ti) * popsz, w->pop, sizeof(double) * popsz);
+
+		/* update_pop, src/state.cc:460-485 (pop[sett+1]; also formed after the last step) */
+		memcpy(w->popnext, w->pop, sizeof(double) * popsz);
+		for (int32_t c = 0; c < A; c++) {
+			double *pn = w->popnext + (size_t)c * C * DP;
+			for (int32_t tr = 0; tr < T; tr++) {
+				int32_t from = m->trans_from[tr], to = m->trans_to[tr];
+				for (int32_t dp = 0; dp < DP; dp++) {
+					double num = (double)tn[((size_t)c * T + tr) * DP + dp];
+					if (num != 0) { pn[(size_t)from * DP + dp] -= num; pn[(size_t)to * DP + dp] += num; }
+				}
+			}
+		}
+		double *sw = w->pop; w->pop = w->popnext; w->popnext = sw;
+	}
+
+	/* outputs */
+	if (b->pop_out) {
+		int32_t *po = b->pop_out + (size_t)p * popsz;
+		for (size_t k = 0; k < popsz; k++) {
+			double v = w->pop[k];
+			if (v > 2147483647.0 || v < -2147483648.0) return BEEP_COUNT_OVERFLOW;
+			po[k] = (int32_t)v;
+		}
+	}
+	size_t nsteps = (size_t)(b->tf - b->ti);
+	if (b->transnum_out) memcpy(b->transnum_out + (size_t)p * nsteps * tnsz, w->tn_traj, sizeof(int32_t) * nsteps * tnsz);
+	if (b->pop_traj_out) {
+		int32_t *po = b->pop_traj_out + (size_t)p * nsteps * popsz;
+		for (size_t k = 0; k < nsteps * popsz; k++) po[k] = (int32_t)w->pop_traj[k];
+	}
+
+	if (b->L_out) {                                       /* get_obs_value_section + calculate */
+		for (int32_t k = 0; k < ix->nscored; k++) w->obs_value[ix->scored[k]] = 0;
+		for (int32_t sett = b->ti; sett < b->tf; sett++) {
+			const int32_t *tn = w->tn_traj + (size_t)(sett - b->ti) * tnsz;
+			const double *pp = w->pop_traj + (size_t)(sett - b->ti) * popsz;
+			for (int32_t c = 0; c < A; c++) {
+				for (int32_t tr = 0; tr < T; tr++) {
+					for (int32_t dp = 0; dp < DP; dp++) {
+						int32_t cell = (c * T + tr) * DP + dp;
+						double num = (double)tn[cell];
+						if (num != 0) {
+							size_t slot = (size_t)(sett - b->ti) * ix->ncell_t + cell;
+							for (int32_t q = ix->t_ptr[slot]; q < ix->t_ptr[slot + 1]; q++) {
+								int32_t ob = ix->t_obs[q];
+								int32_t spl = m->obs_factor_spline[ob];
+								if (spl < 0) w->obs_value[ob] += m->obs_factor[ob] * num;
+								else w->obs_value[ob] += m->obs_factor[ob] * num * tb->obs_spline[(size_t)spl * m->ndivision + sett];
+							}
+						}
+					}
+				}
+				for (int32_t co = 0; co < C; co++) {
+					for (int32_t dp = 0; dp < DP; dp++) {
+						int32_t cell = (c * C + co) * DP + dp;
+						size_t slot = (size_t)(sett - b->ti) * ix->ncell_p + cell;
+						if (ix->p_ptr[slot + 1] > ix->p_ptr[slot]) {
+							double num = pp[cell];
+							for (int32_t q = ix->p_ptr[slot]; q < ix->p_ptr[slot + 1]; q++) {
+								int32_t ob = ix->p_obs[q];
+								w->obs_value[ob] += m->obs_factor[ob] * num;
+							}
+						}
+					}
+				}
+			}
+		}
+		double L = 0.0;
+		for (int32_t k = 0; k < ix->nscored; k++) {
+			int32_t i = ix->scored[k];
+			L += beep_oracle_obs_prob(w->obs_value[i], m->obs_value_kind[i], m->obs_value[i], m->obs_model[i],
+			                          m->obs_sd[i], m->obs_shape[i], m->obs_threshold[i]);
+		}
+		if (L != L) return BEEP_NAN_RATE;
+		b->L_out[p] = L;
+	}
+	return BEEP_OK;
+}
+
+static int work_alloc(const beep_model_desc *m, int32_t nsteps, work *w)
+{
+	const size_t A = m->narea, G = m->nage, C = m->ncomp, T = m->ntrans, DP = m->ndemocatpos, NS = m->nstrain;
+	memset(w, 0, sizeof *w);
+	w->pop = malloc(sizeof(double) * A * C * DP);
+	w->popnext = malloc(sizeof(double) * A * C * DP);
+	w->Imap = malloc(sizeof(double) * A * G * NS);
+	w->Idiag = malloc(sizeof(double) * A * G * NS);
+	w->dinf = malloc(sizeof(double) * G);
+	w->NMI = malloc(sizeof(double) * G);
+	w->I = malloc(sizeof(double) * G);
+	w->eta = malloc(sizeof(double) * G);
+	w->tmean = malloc(sizeof(double) * T * DP);
+	w->tn_traj = malloc(sizeof(int32_t) * (size_t)nsteps * A * T * DP);
+	w->pop_traj = malloc(sizeof(double) * (size_t)nsteps * A * C * DP);
+	w->obs_value = malloc(sizeof(double) * (size_t)(m->nobs > 0 ? m->nobs : 1));
+	w->infdif = malloc(sizeof(double) * T);
+	if (!w->pop || !w->popnext || !w->Imap || !w->Idiag || !w->dinf || !w->NMI || !w->I || !w->eta ||
+	    !w->tmean || !w->tn_traj || !w->pop_traj || !w->obs_value || !w->infdif) return BEEP_OOM;
+	return BEEP_OK;
+}
+
+static void work_free(work *w)
+{
+	free(w->pop); free(w->popnext); free(w->Imap); free(w->Idiag); free(w->dinf); free(w->NMI);
+	free(w->I); free(w->eta); free(w->tmean); free(w->tn_traj); free(w->pop_traj); free(w->obs_value);
+	free(w->infdif);
+}
+
+int beep_oracle_simulate(const beep_model_desc *m, const beep_sim_batch *b, int nthreads)
+{
+	if (!m || !b || b->ti < 0 || b->tf <= b->ti || b->tf > m->ndivision || m->nstrain < 1 ||
+	    m->ndemocatpos % m->nstrain != 0 || b->nparticle < 0 || !b->groups)
+		return BEEP_BAD_INPUT;
+	if (b->ti > 0 && !b->pop_in) return BEEP_BAD_INPUT;
+	obs_index ix;
+	int st = obs_index_build(m, b->ti, b->tf, &ix);
+	if (st != BEEP_OK) { obs_index_free(&ix); return st; }
+	int status = BEEP_OK;
+#ifdef _OPENMP
+	if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+	(void)nthreads;
+#endif
+#pragma omp parallel
+	{
+		work w;
+		int ws = work_alloc(m, b->tf - b->ti, &w);
+		if (ws != BEEP_OK) {
+#pragma omp critical
+			status = ws;
+		}
+#pragma omp for schedule(dynamic, 1)
+		for (int32_t p = 0; p < b->nparticle; p++) {
+			if (ws != BEEP_OK || status != BEEP_OK) continue;
+			int s = simulate_particle(m, b, &ix, p, &w);
+			if (s != BEEP_OK) {
+#pragma omp critical
+				status = s;
+			}
+		}
+		work_free(&w);
+	}
+	obs_index_free(&ix);
+	return status;
+}

@@ -1,0 +1,49 @@
+/* beep_oracle.h -- CPU restatement of BEEP's tau-leap simulation and
+ * observation log-likelihood.  TEST INFRASTRUCTURE ONLY: the parity checker
+ * and the timed CPU baseline.  The product never links it.
+ *
+ * It consumes the same plain tables as the C ABI in include/beep_gpu.h and
+ * follows the reference loop by loop:
+ *   State::simulate(ti,tf)            src/state.cc:596-638
+ *   State::set_I_from_pop             src/state.cc:223-290
+ *   State::set_Imap_sett / update_I_from_transnum  src/state.cc:164-219
+ *   State::get_NMI                    src/state.cc:547-578
+ *   State::set_transmean              src/state.cc:380-456
+ *   State::update_pop                 src/state.cc:460-485
+ *   ObservationModel::calculate(_section), get_obs_value_section, obs_prob
+ *                                     src/obsmodel.cc:22-109,245-305
+ *   normal/poisson/negative_binomial_probability  src/utils.cc:107-170
+ * Transition counts are drawn from the keyed stream of beep_rng_ref.h (the
+ * same stream the replay hook feeds to the compiled reference).
+ */
+#ifndef BEEP_ORACLE_H
+#define BEEP_ORACLE_H
+
+#include "../include/beep_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Runs a batch exactly as beep_simulate specifies, on nthreads host threads
+ * (0 = all).  Returns 0 on success, else a beep_status code. */
+int beep_oracle_simulate(const beep_model_desc *m, const beep_sim_batch *b, int nthreads);
+
+/* One Poisson draw from the keyed stream (exposed for sampler tests). */
+int32_t beep_oracle_poisson(double mean, uint64_t seed, uint32_t cell, uint32_t step,
+                            uint32_t stream, uint32_t purpose);
+
+/* Project exp / log / log-factorial used inside the sampler (for tests). */
+double beep_oracle_exp(double x);
+double beep_oracle_log(double x);
+double beep_oracle_log_factorial(double k);
+
+/* obs_prob of one observation value (src/obsmodel.cc:245-305). */
+double beep_oracle_obs_prob(double value, int32_t value_kind, double obs_value, int32_t model,
+                            double sd, double shape, double threshold);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

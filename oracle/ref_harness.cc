@@ -1,0 +1,394 @@
+// ref_harness.cc -- drives the compiled reference (BEEP's own C++ sources,
+// built in place from the reference tree by oracle/Makefile.ref) to produce
+// golden vectors.  TEST INFRASTRUCTURE ONLY.
+//
+// It builds Inputs -> Details -> Mpi -> Data -> Model -> ObservationModel as
+// src/main.cc:125-160 does, then for each particle calls State::simulate(θ)
+// (src/state.cc:582-592), and, for particle-filter sections, the sectioned
+// State::simulate(ti,tf) + ObservationModel::calculate_section
+// (src/state.cc:596-638, src/obsmodel.cc:39-58).  Every poisson_sample call
+// (src/utils.cc:148-153) is interposed at link time (-Wl,--wrap) and answered
+// from the project's keyed Philox stream, so the reference consumes exactly
+// the variates the oracle restatement and the CUDA kernels consume.
+//
+// It writes one bundle file: the parameter-independent model, the tables
+// set_param produced, and the reference's outputs (log-likelihoods,
+// transition counts and populations).
+//
+// usage: ref_harness out=FILE [npart=N] [ntraj=N] [seed=S] [pf=0|1] [theta=FILE] -- <BEEP key=value...>
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+#include "inputs.hh"
+#include "details.hh"
+#include "mpi.hh"
+#include "data.hh"
+#include "model.hh"
+#include "obsmodel.hh"
+#include "state.hh"
+#include "utils.hh"
+#include "timers.hh"
+
+extern "C" {
+#include "beep_rng_ref.h"
+}
+
+// ---- replay hook ---------------------------------------------------------
+
+namespace {
+struct Replay {
+	bool active = false;
+	const State *st = nullptr;
+	uint32_t k0 = 0, k1 = 0, stream = 0;
+	unsigned sett = 0, c = 0, tr = 0, dp = 0;
+	unsigned narea = 0, ntrans = 0, ndp = 0, ndiv = 0;
+	unsigned long long ncalls = 0;
+	void advance() {
+		if (++dp < ndp) return;
+		dp = 0;
+		if (++tr < ntrans) return;
+		tr = 0;
+		if (++c < narea) return;
+		c = 0; sett++;
+	}
+};
+Replay g_replay;
+}  // namespace
+
+extern "C" int __real__Z14poisson_sampled(double lam);
+
+// Answers the reference's k-th poisson_sample(mean) call of a simulate(ti,tf)
+// with the keyed draw of the (sett, c, tr, dp) cell that call belongs to.  The
+// cell is found by walking transmean[sett][c][tr][dp] in the reference's loop
+// order (src/state.cc:608-631), skipping cells whose mean is 0 (no call).
+extern "C" int __wrap__Z14poisson_sampled(double lam)
+{
+	Replay &r = g_replay;
+	if (!r.active) return __real__Z14poisson_sampled(lam);
+	while (true) {
+		if (r.sett >= r.ndiv) { fprintf(stderr, "replay: cursor ran past the last step\n"); abort(); }
+		double m = r.st->transmean[r.sett][r.c][r.tr][r.dp];
+		if (m != 0) break;
+		r.advance();
+	}
+	double m = r.st->transmean[r.sett][r.c][r.tr][r.dp];
+	if (memcmp(&m, &lam, sizeof m) != 0) {
+		fprintf(stderr, "replay: mean mismatch at sett=%u c=%u tr=%u dp=%u: %.17g vs %.17g\n",
+		        r.sett, r.c, r.tr, r.dp, m, lam);
+		abort();
+	}
+	uint32_t cell = (r.c * r.ntrans + r.tr) * r.ndp + r.dp;
+	int v = beep_poisson_ref(lam, r.k0, r.k1, cell, r.sett, r.stream, BEEP_PURPOSE_TRANS);
+	r.ncalls++;
+	r.advance();
+	return v;
+}
+
+// ---- bundle writer -------------------------------------------------------
+
+namespace {
+struct Bundle {
+	FILE *f = nullptr;
+	void open(const std::string &fn) {
+		f = fopen(fn.c_str(), "wb");
+		if (!f) { fprintf(stderr, "cannot open %s\n", fn.c_str()); exit(1); }
+		fwrite("BEEPBND1", 1, 8, f);
+	}
+	void rec(const std::string &name, char type, const std::vector<uint64_t> &dims, const void *data, size_t esz) {
+		uint32_t nl = (uint32_t)name.size();
+		fwrite(&nl, 4, 1, f); fwrite(name.data(), 1, nl, f);
+		fwrite(&type, 1, 1, f);
+		uint32_t nd = (uint32_t)dims.size(); fwrite(&nd, 4, 1, f);
+		size_t n = 1;
+		for (auto d : dims) { fwrite(&d, 8, 1, f); n *= d; }
+		if (n) fwrite(data, esz, n, f);
+	}
+	void d(const std::string &n, const std::vector<double> &v, std::vector<uint64_t> dims = {}) {
+		if (dims.empty()) dims = {v.size()};
+		rec(n, 'd', dims, v.data(), 8);
+	}
+	void i(const std::string &n, const std::vector<int32_t> &v, std::vector<uint64_t> dims = {}) {
+		if (dims.empty()) dims = {v.size()};
+		rec(n, 'i', dims, v.data(), 4);
+	}
+	void scalar_d(const std::string &n, double v) { d(n, std::vector<double>{v}); }
+	void scalar_i(const std::string &n, int32_t v) { i(n, std::vector<int32_t>{v}); }
+	void close() { if (f) fclose(f); f = nullptr; }
+};
+
+std::vector<std::vector<double>> read_theta(const std::string &fn)
+{
+	std::vector<std::vector<double>> out;
+	std::ifstream in(fn);
+	std::string line;
+	while (std::getline(in, line)) {
+		if (line.empty()) continue;
+		std::vector<double> row;
+		std::stringstream ss(line);
+		std::string tok;
+		while (std::getline(ss, tok, ',')) row.push_back(strtod(tok.c_str(), nullptr));
+		out.push_back(row);
+	}
+	return out;
+}
+}  // namespace
+
+int main(int argc, char **argv)
+{
+	std::map<std::string, std::string> opt;
+	int split = argc;
+	for (int k = 1; k < argc; k++) {
+		if (std::string(argv[k]) == "--") { split = k; break; }
+		std::string s = argv[k];
+		auto e = s.find('=');
+		if (e == std::string::npos) { fprintf(stderr, "bad option %s\n", argv[k]); return 2; }
+		opt[s.substr(0, e)] = s.substr(e + 1);
+	}
+	if (!opt.count("out")) { fprintf(stderr, "out= is required\n"); return 2; }
+	int npart = opt.count("npart") ? atoi(opt["npart"].c_str()) : 4;
+	int ntraj = opt.count("ntraj") ? atoi(opt["ntraj"].c_str()) : 1;
+	uint64_t seed = opt.count("seed") ? strtoull(opt["seed"].c_str(), nullptr, 0) : 12345;
+	bool pf = opt.count("pf") && opt["pf"] == "1";
+
+	std::vector<char *> bargv;
+	bargv.push_back(argv[0]);
+	for (int k = split + 1; k < argc; k++) bargv.push_back(argv[k]);
+	int bargc = (int)bargv.size();
+
+	timersinit();
+	MPI_Init(&bargc, nullptr);
+	Inputs inputs(bargc, bargv.data());
+	Details details(inputs);
+	Mpi mpi(details);
+	Data data(inputs, details, mpi);
+	Model model(inputs, details, data, mpi);
+	sran(mpi.core * 10000 + inputs.find_integer("seed", 0) + 100);
+	ObservationModel obsmodel(details, data, model);
+
+	const unsigned A = data.narea, G = data.nage, DP = data.ndemocatpos, NS = data.nstrain;
+	const unsigned C = model.comp.size(), T = model.trans.size(), S = details.ndivision;
+	const unsigned DPS = data.ndemocatpos_per_strain;
+
+	std::vector<std::vector<double>> thetas;
+	if (opt.count("theta")) thetas = read_theta(opt["theta"]);
+	else thetas.push_back(model.simulated_values());
+	for (auto &th : thetas) {
+		if (th.size() != model.param.size()) { fprintf(stderr, "theta has %zu values, model has %zu parameters\n", th.size(), model.param.size()); return 2; }
+	}
+	int ngroup = (int)thetas.size();
+
+	Bundle B;
+	B.open(opt["out"]);
+
+	// ---- parameter-independent model (beep_model_desc) ----
+	B.i("dims", {(int32_t)A, (int32_t)G, (int32_t)DP, (int32_t)NS, (int32_t)C, (int32_t)T, (int32_t)S,
+	             (int32_t)details.period, (int32_t)details.division_per_time});
+	B.scalar_d("dt", double(details.period) / details.ndivision);
+	B.scalar_d("popsize", (double)data.popsize);
+	std::vector<int32_t> tf(T), tt(T);
+	for (unsigned tr = 0; tr < T; tr++) { tf[tr] = model.trans[tr].from; tt[tr] = model.trans[tr].to; }
+	B.i("trans_from", tf); B.i("trans_to", tt);
+	B.scalar_i("infection_trans", (int32_t)model.infection_trans);
+	std::vector<int32_t> dpage(DPS);
+	for (unsigned dp = 0; dp < DPS; dp++) dpage[dp] = data.democatpos[dp][0];
+	B.i("democatpos_age", dpage);
+	{
+		std::vector<double> diag(A), val, fac(A);
+		std::vector<int32_t> rowptr(A + 1, 0), to;
+		for (unsigned c = 0; c < A; c++) {
+			diag[c] = data.genQ.M.diag[c];
+			fac[c] = data.genQ.factor[c];
+			for (unsigned j = 0; j < data.genQ.M.to[c].size(); j++) {
+				to.push_back(data.genQ.M.to[c][j]);
+				val.push_back(data.genQ.M.val[c][j]);
+			}
+			rowptr[c + 1] = (int32_t)to.size();
+		}
+		B.d("M_diag", diag); B.i("M_rowptr", rowptr); B.i("M_to", to); B.d("M_val", val); B.d("M_factor", fac);
+	}
+	{
+		std::vector<double> pi((size_t)A * C * DP);
+		for (unsigned c = 0; c < A; c++)
+			for (unsigned co = 0; co < C; co++)
+				for (unsigned dp = 0; dp < DP; dp++) pi[((size_t)c * C + co) * DP + dp] = data.area[c].pop_init[co][dp];
+		B.d("pop_init", pi, {A, C, DP});
+	}
+	// observations; cells in the order the reference visits them (src/obsmodel.cc:74-109)
+	std::map<unsigned, int32_t> spline_row;
+	std::vector<unsigned> spline_rows;
+	{
+		unsigned nobs = data.nobs;
+		std::vector<int32_t> si(nobs), sf(nobs), kind(nobs), mdl(nobs), fspl(nobs), cptr(nobs + 1, 0), cells;
+		std::vector<double> val(nobs), sd(nobs), shape(nobs), thr(nobs), fac(nobs);
+		for (unsigned i = 0; i < nobs; i++) {
+			const auto &ob = data.obs[i];
+			si[i] = ob.sett_i; sf[i] = ob.sett_f;
+			kind[i] = ob.value == UNKNOWN ? 1 : (ob.value == THRESH ? 2 : 0);
+			val[i] = ob.value; sd[i] = ob.sd; shape[i] = ob.shape;
+			thr[i] = data.datatable[ob.datatable].threshold;
+			fac[i] = ob.factor; mdl[i] = (int32_t)ob.obsmodel;
+			if (ob.factor_spline == UNSET) fspl[i] = -1;
+			else {
+				if (!spline_row.count(ob.factor_spline)) {
+					spline_row[ob.factor_spline] = (int32_t)spline_rows.size();
+					spline_rows.push_back(ob.factor_spline);
+				}
+				fspl[i] = spline_row[ob.factor_spline];
+			}
+			struct K { unsigned c, kind, x, dp; int32_t cell; };
+			std::vector<K> ks;
+			const auto &dtab = data.datatable[ob.datatable];
+			for (auto c : ob.area)
+				for (auto dp : ob.dp_sel) {
+					for (auto tr : dtab.translist) ks.push_back({c, 0, tr, dp, (int32_t)((c * T + tr) * DP + dp)});
+					for (auto co : dtab.complist) ks.push_back({c, 1, co, dp, (int32_t)(-1 - (int32_t)((c * C + co) * DP + dp))});
+				}
+			std::stable_sort(ks.begin(), ks.end(), [](const K &a, const K &b) {
+				if (a.c != b.c) return a.c < b.c;
+				if (a.kind != b.kind) return a.kind < b.kind;
+				if (a.x != b.x) return a.x < b.x;
+				return a.dp < b.dp;
+			});
+			for (auto &k : ks) cells.push_back(k.cell);
+			cptr[i + 1] = (int32_t)cells.size();
+		}
+		B.i("obs_sett_i", si); B.i("obs_sett_f", sf); B.i("obs_value_kind", kind); B.d("obs_value", val);
+		B.i("obs_model", mdl); B.d("obs_sd", sd); B.d("obs_shape", shape); B.d("obs_threshold", thr);
+		B.d("obs_factor", fac); B.i("obs_factor_spline", fspl); B.i("obs_cell_ptr", cptr); B.i("obs_cells", cells);
+	}
+	if (pf) {
+		std::vector<int32_t> sti, stf;
+		for (unsigned s = 0; s < obsmodel.nsection; s++) { sti.push_back(obsmodel.section_ti[s]); stf.push_back(obsmodel.section_tf[s]); }
+		B.i("section_ti", sti); B.i("section_tf", stf);
+	}
+
+	// ---- per parameter set: tables from set_param, then the particles ----
+	g_replay.k0 = (uint32_t)seed; g_replay.k1 = (uint32_t)(seed >> 32);
+	g_replay.narea = A; g_replay.ntrans = T; g_replay.ndp = DP; g_replay.ndiv = S;
+	B.i("seed_words", {(int32_t)g_replay.k0, (int32_t)g_replay.k1});
+	B.scalar_i("ngroup", ngroup);
+	B.scalar_i("npart", npart);
+	B.scalar_i("ntraj", ntraj);
+
+	for (int gidx = 0; gidx < ngroup; gidx++) {
+		std::string gp = "g" + std::to_string(gidx) + ".";
+		B.d(gp + "theta", thetas[gidx]);
+		State state(details, data, model, obsmodel);
+		state.set_param(thetas[gidx]);
+		{
+			std::vector<double> v;
+			for (unsigned tr = 0; tr < T; tr++) {
+				if (state.transrate[tr].size() == DP) for (unsigned dp = 0; dp < DP; dp++) v.push_back(state.transrate[tr][dp]);
+				else for (unsigned dp = 0; dp < DP; dp++) v.push_back(0.0);   // infection transition: no rate
+			}
+			B.d(gp + "transrate", v, {T, DP});
+			B.d(gp + "susceptibility", state.susceptibility);
+			std::vector<double> inf(C);
+			for (unsigned co = 0; co < C; co++) inf[co] = thetas[gidx][model.comp[co].infectivity_param];
+			B.d(gp + "infectivity", inf);
+			// beta rows, deduplicated by content (the reference copies one row per R-spline to its areas, src/model.cc:1339-1345)
+			std::vector<std::vector<double>> rows;
+			std::vector<int32_t> rowof(NS * A);
+			for (unsigned st = 0; st < NS; st++)
+				for (unsigned c = 0; c < A; c++) {
+					const auto &r = state.beta[st][c];
+					unsigned k = 0;
+					while (k < rows.size() && rows[k] != r) k++;
+					if (k == rows.size()) rows.push_back(r);
+					rowof[st * A + c] = (int32_t)k;
+				}
+			std::vector<double> br;
+			for (auto &r : rows) br.insert(br.end(), r.begin(), r.end());
+			B.d(gp + "beta_rows", br, {rows.size(), S});
+			B.i(gp + "beta_row_of", rowof, {NS, A});
+			std::vector<double> af;
+			for (unsigned t = 0; t < details.period; t++) af.insert(af.end(), state.areafactor[t].begin(), state.areafactor[t].end());
+			B.d(gp + "areafactor", af, {details.period, A});
+			std::vector<double> nt;
+			for (unsigned s = 0; s < S; s++) for (unsigned a = 0; a < G; a++) nt.insert(nt.end(), state.Ntime[s][a].begin(), state.Ntime[s][a].end());
+			B.d(gp + "Ntime", nt, {S, G, G});
+			B.d(gp + "geo_spline", state.disc_spline[model.geo_spline_ref]);
+			std::vector<double> es, ea;
+			for (auto &info : model.efoispline_info) {
+				es.insert(es.end(), state.disc_spline[info.spline_ref].begin(), state.disc_spline[info.spline_ref].end());
+				ea.insert(ea.end(), info.efoi_agedist.begin(), info.efoi_agedist.end());
+			}
+			B.d(gp + "efoi_spline", es, {model.efoispline_info.size(), S});
+			B.d(gp + "efoi_agedist", ea, {model.efoispline_info.size(), G});
+			std::vector<int32_t> er;
+			for (unsigned st = 0; st < NS; st++) for (unsigned c = 0; c < A; c++) er.push_back(model.efoi_spl_ref[st][c]);
+			B.i(gp + "efoi_ref", er, {NS, A});
+			std::vector<double> os;
+			for (auto spl : spline_rows) os.insert(os.end(), state.disc_spline[spl].begin(), state.disc_spline[spl].end());
+			B.d(gp + "obs_spline", os, {spline_rows.size(), S});
+		}
+
+		std::vector<double> Lfull(npart), Lsec;
+		std::vector<int32_t> tnum, popt;
+		std::vector<double> chk;
+		for (int p = 0; p < npart; p++) {
+			uint32_t stream = (uint32_t)(gidx * npart + p);
+			g_replay.st = &state; g_replay.stream = stream;
+			g_replay.sett = 0; g_replay.c = 0; g_replay.tr = 0; g_replay.dp = 0;
+			g_replay.active = true;
+			if (!pf) {
+				state.simulate(thetas[gidx]);
+				Lfull[p] = obsmodel.calculate(&state);
+			} else {
+				state.set_param(thetas[gidx]);
+				for (unsigned sec = 0; sec < obsmodel.nsection; sec++) {
+					unsigned ti = obsmodel.section_ti[sec], tf2 = obsmodel.section_tf[sec];
+					g_replay.sett = ti; g_replay.c = 0; g_replay.tr = 0; g_replay.dp = 0;
+					state.simulate(ti, tf2);
+					Lsec.push_back(obsmodel.calculate_section(&state, sec));
+				}
+				Lfull[p] = obsmodel.calculate(&state);
+			}
+			g_replay.active = false;
+			// checksums over the whole trajectory (exact integer sums, weighted)
+			double s1 = 0, s2 = 0, s3 = 0, s4 = 0;
+			for (unsigned s = 0; s < S; s++)
+				for (unsigned c = 0; c < A; c++) {
+					for (unsigned tr = 0; tr < T; tr++)
+						for (unsigned dp = 0; dp < DP; dp++) {
+							double v = state.transnum[s][c][tr][dp];
+							s1 += v; s2 += v * (double)(1 + ((s * 131 + c * 31 + tr * 7 + dp) % 1009));
+						}
+					for (unsigned co = 0; co < C; co++)
+						for (unsigned dp = 0; dp < DP; dp++) {
+							double v = state.pop[s][c][co][dp];
+							s3 += v; s4 += v * (double)(1 + ((s * 131 + c * 31 + co * 7 + dp) % 1009));
+						}
+				}
+			chk.insert(chk.end(), {s1, s2, s3, s4});
+			if (p < ntraj) {
+				for (unsigned s = 0; s < S; s++)
+					for (unsigned c = 0; c < A; c++) {
+						for (unsigned tr = 0; tr < T; tr++)
+							for (unsigned dp = 0; dp < DP; dp++) tnum.push_back((int32_t)state.transnum[s][c][tr][dp]);
+						for (unsigned co = 0; co < C; co++)
+							for (unsigned dp = 0; dp < DP; dp++) popt.push_back((int32_t)state.pop[s][c][co][dp]);
+					}
+			}
+		}
+		B.d(gp + "L", Lfull);
+		if (pf) B.d(gp + "L_section", Lsec, {(uint64_t)npart, obsmodel.nsection});
+		B.d(gp + "checksum", chk, {(uint64_t)npart, 4});
+		int nt = std::min(ntraj, npart);
+		B.i(gp + "transnum", tnum, {(uint64_t)nt, S, A, T, DP});
+		B.i(gp + "pop", popt, {(uint64_t)nt, S, A, C, DP});
+	}
+	B.close();
+	fprintf(stderr, "ref_harness: %d groups x %d particles, %llu keyed draws\n", ngroup, npart, g_replay.ncalls);
+	return 0;
+}

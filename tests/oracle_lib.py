@@ -1,0 +1,40 @@
+"""Loads the oracle restatement (oracle/_build/libbeep_oracle.so) for tests and
+the CPU baseline.  The oracle is the parity checker, never the product."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+from beep_gb300 import capi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+_LIB = None
+
+
+def oracle_lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(ORACLE_DIR, "_build", "libbeep_oracle.so")
+        subprocess.run(["make", "-s", "-C", ORACLE_DIR], check=True)
+        L = C.CDLL(path)
+        L.beep_oracle_simulate.argtypes = [C.POINTER(capi.ModelDesc), C.POINTER(capi.SimBatch), C.c_int]
+        L.beep_oracle_simulate.restype = C.c_int
+        L.beep_oracle_poisson.argtypes = [C.c_double, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]
+        L.beep_oracle_poisson.restype = C.c_int32
+        for f in ("beep_oracle_exp", "beep_oracle_log", "beep_oracle_log_factorial"):
+            getattr(L, f).argtypes = [C.c_double]
+            getattr(L, f).restype = C.c_double
+        L.beep_oracle_obs_prob.argtypes = [C.c_double, C.c_int32, C.c_double, C.c_int32, C.c_double, C.c_double,
+                                           C.c_double]
+        L.beep_oracle_obs_prob.restype = C.c_double
+        _LIB = L
+    return _LIB
+
+
+def oracle_simulate(model: capi.Model, batch: capi.Batch, nthreads: int = 0) -> capi.Batch:
+    st = oracle_lib().beep_oracle_simulate(C.byref(model.desc), C.byref(batch.st), nthreads)
+    if st != 0:
+        raise RuntimeError(f"oracle failed: {capi.STATUS.get(st, st)}")
+    return batch
