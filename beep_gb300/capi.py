@@ -210,7 +210,18 @@ def lib():
         L.beep_model_create.argtypes = [C.POINTER(ModelDesc), C.POINTER(C.c_void_p)]
         L.beep_model_destroy.argtypes = [C.c_void_p]
         L.beep_simulate.argtypes = [C.c_void_p, C.POINTER(SimBatch)]
-        for f in ("beep_device_init", "beep_model_create", "beep_model_destroy", "beep_simulate"):
+        L.beep_batch_create.argtypes = [C.c_void_p, C.POINTER(SimBatch), C.POINTER(C.c_void_p)]
+        for f in ("beep_batch_stage", "beep_batch_upload", "beep_batch_launch", "beep_batch_download",
+                  "beep_batch_destroy"):
+            getattr(L, f).argtypes = [C.c_void_p]
+        L.beep_batch_time.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]
+        L.beep_batch_launches.argtypes = [C.c_void_p]
+        L.beep_batch_launches.restype = C.c_int32
+        L.beep_batch_bytes.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        L.beep_batch_bytes.restype = C.c_int32
+        for f in ("beep_device_init", "beep_model_create", "beep_model_destroy", "beep_simulate", "beep_batch_create",
+                  "beep_batch_stage", "beep_batch_upload", "beep_batch_launch", "beep_batch_download",
+                  "beep_batch_time", "beep_batch_destroy"):
             getattr(L, f).restype = C.c_int32
         _LIB = L
     return _LIB
@@ -245,6 +256,59 @@ class DeviceModel:
     def close(self):
         if self.h:
             lib().beep_model_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DeviceBatch:
+    """A ``beep_batch``: a batch kept on the device and run repeatedly."""
+
+    def __init__(self, dm: DeviceModel, batch: Batch):
+        self.batch = batch
+        self.dm = dm
+        h = C.c_void_p()
+        check(lib().beep_batch_create(dm.h, C.byref(batch.st), C.byref(h)))
+        self.h = h
+
+    def stage(self):
+        check(lib().beep_batch_stage(self.h))
+
+    def upload(self):
+        check(lib().beep_batch_upload(self.h))
+
+    def launch(self):
+        check(lib().beep_batch_launch(self.h))
+
+    def download(self) -> Batch:
+        check(lib().beep_batch_download(self.h))
+        return self.batch
+
+    def run(self) -> Batch:
+        self.upload()
+        self.launch()
+        return self.download()
+
+    def time(self, iters: int) -> float:
+        ms = C.c_double()
+        check(lib().beep_batch_time(self.h, iters, C.byref(ms)))
+        return ms.value
+
+    def bytes(self):
+        a, b = C.c_int64(), C.c_int64()
+        check(lib().beep_batch_bytes(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def launches(self) -> int:
+        return lib().beep_batch_launches(self.h)
+
+    def close(self):
+        if self.h:
+            lib().beep_batch_destroy(self.h)
             self.h = None
 
     def __del__(self):

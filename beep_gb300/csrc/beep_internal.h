@@ -1,0 +1,67 @@
+// Internal device-side layout of the model, the parameter-set tables and a
+// batch.  Shared by the host C++ (capi.cu) and the kernels.
+#pragma once
+
+#include <cstdint>
+
+#include "../../include/beep_gpu.h"
+
+namespace beep {
+
+// Parameter-independent model in HBM.  Area mixing is stored twice: by source
+// (the reference's genQ.M rows) and transposed by target, each target's
+// sources in ascending source order, so that a target's incremental sum can
+// be formed by one thread in the reference's order (src/state.cc:209-216).
+struct ModelDev {
+	int32_t A, G, DP, NS, DPS, C, T, S, period, div_per_time, nobs;
+	int32_t infection_trans;
+	double dt, popsize;
+	const int32_t *trans_from, *trans_to, *dp_age;
+	const double *M_diag, *M_factor;
+	const int32_t *csc_ptr, *csc_src;    // [A+1], [nnz]
+	const double *csc_val;               // [nnz]
+	const int32_t *pop_init;             // [A][C][DP]
+	// observations
+	const int32_t *obs_model, *obs_kind, *obs_spline, *obs_cell_ptr, *obs_cells, *obs_sett_i, *obs_sett_f;
+	const double *obs_value, *obs_sd, *obs_shape, *obs_thresh, *obs_factor;
+};
+
+// One parameter set's tables: offsets into the batch's table pool (doubles /
+// int32).  Tables shared between parameter sets share offsets.
+struct GroupDir {
+	int64_t transrate, susceptibility, infectivity, infdif, beta_rows, areafactor, Ntime, geo_spline,
+	    efoi_spline, efoi_agedist, obs_spline;          // double pool offsets
+	int64_t beta_row_of, efoi_ref;                      // int pool offsets
+};
+
+struct BatchDev {
+	int32_t P, ti, tf, ngroup;
+	uint32_t k0, k1;
+	const GroupDir *dirs;               // [ngroup]
+	const double *fpool;
+	const int32_t *ipool;
+	const int32_t *group_of;            // [P] or null
+	const uint32_t *stream_of;          // [P] or null
+	const int32_t *pop_in;              // [P][A][C][DP] or null (ti == 0)
+	// scored observations and their per-step activity
+	int32_t nscored;
+	const int32_t *scored;              // [nscored] ascending obs index
+	const int32_t *step_ptr;            // [tf-ti+1]
+	const int32_t *step_obs;            // scored-position of obs active at each step
+	// per-particle work (device)
+	int32_t *pop_a, *pop_b;             // [P][A][C][DP]
+	int32_t *tn;                        // [P][A][T][DP] current step's counts (when not writing a trajectory)
+	double *Imap, *Idiag, *dinf, *NMI;  // [P][NS][A][G]
+	double *obs_acc;                    // [P][nscored]
+	// outputs (device)
+	double *L;                          // [P] or null
+	int32_t *pop_out;                   // [P][A][C][DP] or null
+	int32_t *tn_traj;                   // [P][tf-ti][A][T][DP] or null
+	int32_t *pop_traj;                  // [P][tf-ti][A][C][DP] or null
+	int32_t *status;                    // [P] beep_status per particle
+};
+
+// launchers (sim_plain.cu)
+int launch_sim_plain(const ModelDev &m, const BatchDev &b, void *stream);
+
+}  // namespace beep

@@ -1,0 +1,615 @@
+// C ABI (include/beep_gpu.h): model creation, batch packing, launches.
+//
+// Host-side work per beep_simulate call:
+//   1. validate the batch and pack every input into one pinned staging
+//      buffer: the parameter-set tables (deduplicated by host pointer), the
+//      per-particle group/stream indices and start populations, and the
+//      per-step lists of active observations;
+//   2. one host->device copy, the kernel, one device->host copy of the
+//      outputs, all on the model's stream;
+//   3. per-particle status words are reduced to the returned beep_status.
+// Device memory is a per-model arena that only grows, so steady-state calls
+// allocate nothing.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "beep_internal.h"
+
+using namespace beep;
+
+namespace {
+
+thread_local std::string g_err;
+
+beep_status fail(beep_status s, const std::string &msg)
+{
+	g_err = msg;
+	return s;
+}
+
+#define CUDA_TRY(expr)                                                                         \
+	do {                                                                                       \
+		cudaError_t e_ = (expr);                                                               \
+		if (e_ != cudaSuccess)                                                                 \
+			return fail(e_ == cudaErrorMemoryAllocation ? BEEP_OOM : BEEP_DEVICE_ERROR,        \
+			            std::string(#expr) + ": " + cudaGetErrorString(e_));                   \
+	} while (0)
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// A device buffer that only grows.
+struct DevBuf {
+	void *ptr = nullptr;
+	size_t cap = 0;
+	cudaError_t reserve(size_t n)
+	{
+		if (n <= cap) return cudaSuccess;
+		if (ptr) cudaFree(ptr);
+		ptr = nullptr;
+		cap = 0;
+		cudaError_t e = cudaMalloc(&ptr, n);
+		if (e == cudaSuccess) cap = n;
+		return e;
+	}
+	void release()
+	{
+		if (ptr) cudaFree(ptr);
+		ptr = nullptr;
+		cap = 0;
+	}
+};
+
+struct HostBuf {
+	void *ptr = nullptr;
+	size_t cap = 0;
+	cudaError_t reserve(size_t n)
+	{
+		if (n <= cap) return cudaSuccess;
+		if (ptr) cudaFreeHost(ptr);
+		ptr = nullptr;
+		cap = 0;
+		cudaError_t e = cudaMallocHost(&ptr, n);
+		if (e == cudaSuccess) cap = n;
+		return e;
+	}
+	void release()
+	{
+		if (ptr) cudaFreeHost(ptr);
+		ptr = nullptr;
+		cap = 0;
+	}
+};
+
+// Sequential layout of named regions inside one buffer.
+struct Layout {
+	size_t size = 0;
+	size_t add(size_t bytes)
+	{
+		size_t off = align_up(size, 256);
+		size = off + bytes;
+		return off;
+	}
+};
+
+}  // namespace
+
+struct beep_model {
+	int device = 0;
+	cudaStream_t stream = nullptr;
+	ModelDev dev{};
+	DevBuf model_mem;
+	// host copies used to prepare batches
+	int32_t A, G, DP, NS, C, T, S, period, dpt, nobs;
+	std::vector<int32_t> obs_sett_i, obs_sett_f, obs_spline, trans_from_h, trans_to_h;
+	std::mutex mu;
+};
+
+extern "C" {
+
+int32_t beep_abi_version(void) { return BEEP_GPU_ABI_VERSION; }
+
+const char *beep_last_error(void) { return g_err.c_str(); }
+
+beep_status beep_device_init(int32_t device)
+{
+	int n = 0;
+	cudaError_t e = cudaGetDeviceCount(&n);
+	if (e != cudaSuccess || n == 0) return fail(BEEP_NO_DEVICE, "no CUDA device available");
+	if (device < 0 || device >= n) return fail(BEEP_BAD_INPUT, "device index out of range");
+	CUDA_TRY(cudaSetDevice(device));
+	cudaDeviceProp prop;
+	CUDA_TRY(cudaGetDeviceProperties(&prop, device));
+	if (prop.major * 10 + prop.minor != 103)
+		return fail(BEEP_NO_DEVICE, "the kernels are built for sm_103a; device is sm_" +
+		                                std::to_string(prop.major) + std::to_string(prop.minor));
+	return BEEP_OK;
+}
+
+beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
+{
+	if (!d || !out) return fail(BEEP_BAD_INPUT, "null argument");
+	*out = nullptr;
+	const int32_t A = d->narea, G = d->nage, DP = d->ndemocatpos, NS = d->nstrain, C = d->ncomp, T = d->ntrans;
+	const int32_t S = d->ndivision;
+	if (A <= 0 || G <= 0 || DP <= 0 || NS <= 0 || C <= 0 || T <= 0 || S <= 0 || d->period <= 0 ||
+	    d->division_per_time <= 0 || DP % NS != 0 || d->nobs < 0)
+		return fail(BEEP_BAD_INPUT, "model sizes must be positive and ndemocatpos a multiple of nstrain");
+	if ((S - 1) / d->division_per_time >= d->period) return fail(BEEP_BAD_INPUT, "ndivision exceeds period*division_per_time");
+	if (!d->trans_from || !d->trans_to || !d->democatpos_age || !d->M_diag || !d->M_rowptr || !d->M_factor ||
+	    !d->pop_init)
+		return fail(BEEP_BAD_INPUT, "missing model array");
+	if (d->infection_trans < 0 || d->infection_trans >= T) return fail(BEEP_BAD_INPUT, "infection_trans out of range");
+	for (int tr = 0; tr < T; tr++)
+		if (d->trans_from[tr] < 0 || d->trans_from[tr] >= C || d->trans_to[tr] < 0 || d->trans_to[tr] >= C)
+			return fail(BEEP_BAD_INPUT, "transition compartment out of range");
+	const int32_t DPS = DP / NS;
+	for (int dp = 0; dp < DPS; dp++)
+		if (d->democatpos_age[dp] < 0 || d->democatpos_age[dp] >= G) return fail(BEEP_BAD_INPUT, "democatpos_age out of range");
+	if (d->M_rowptr[0] != 0) return fail(BEEP_BAD_INPUT, "M_rowptr[0] must be 0");
+	for (int c = 0; c < A; c++)
+		if (d->M_rowptr[c + 1] < d->M_rowptr[c]) return fail(BEEP_BAD_INPUT, "M_rowptr not monotone");
+	const int32_t nnz = d->M_rowptr[A];
+	for (int j = 0; j < nnz; j++)
+		if (d->M_to[j] < 0 || d->M_to[j] >= A) return fail(BEEP_BAD_INPUT, "M_to out of range");
+	const size_t popsz = (size_t)A * C * DP;
+	std::vector<int32_t> pop_init(popsz);
+	for (size_t k = 0; k < popsz; k++) {
+		double v = d->pop_init[k];
+		if (v != std::floor(v) || v < -2147483648.0 || v > 2147483647.0)
+			return fail(BEEP_BAD_INPUT, "pop_init must be integer-valued within int32");
+		pop_init[k] = (int32_t)v;
+	}
+	const int32_t nobs = d->nobs;
+	int32_t ncells = 0;
+	if (nobs > 0) {
+		if (!d->obs_sett_i || !d->obs_sett_f || !d->obs_value_kind || !d->obs_value || !d->obs_model || !d->obs_sd ||
+		    !d->obs_shape || !d->obs_threshold || !d->obs_factor || !d->obs_factor_spline || !d->obs_cell_ptr ||
+		    !d->obs_cells)
+			return fail(BEEP_BAD_INPUT, "missing observation array");
+		if (d->obs_cell_ptr[0] != 0) return fail(BEEP_BAD_INPUT, "obs_cell_ptr[0] must be 0");
+		ncells = d->obs_cell_ptr[nobs];
+		for (int o = 0; o < nobs; o++) {
+			if (d->obs_sett_i[o] < 0 || d->obs_sett_f[o] <= d->obs_sett_i[o] || d->obs_sett_f[o] > S)
+				return fail(BEEP_BAD_INPUT, "observation time window out of range");
+			if (d->obs_cell_ptr[o + 1] < d->obs_cell_ptr[o]) return fail(BEEP_BAD_INPUT, "obs_cell_ptr not monotone");
+			if (d->obs_model[o] < 0 || d->obs_model[o] > 3 || d->obs_value_kind[o] < 0 || d->obs_value_kind[o] > 2)
+				return fail(BEEP_BAD_INPUT, "bad observation model or value kind");
+			bool has_pop = false;
+			for (int q = d->obs_cell_ptr[o]; q < d->obs_cell_ptr[o + 1]; q++) {
+				int32_t cell = d->obs_cells[q];
+				if (cell >= 0 ? cell >= A * T * DP : (-1 - cell) >= (int64_t)popsz)
+					return fail(BEEP_BAD_INPUT, "observation cell out of range");
+				has_pop |= cell < 0;
+			}
+			if (has_pop && d->obs_factor_spline[o] >= 0)
+				return fail(BEEP_BAD_INPUT, "population observations cannot carry a factor spline (src/obsmodel.cc:98)");
+		}
+	}
+	// transpose of the area mixing matrix, each target's sources ascending
+	std::vector<int32_t> csc_ptr(A + 1, 0), csc_src(nnz);
+	std::vector<double> csc_val(nnz);
+	for (int j = 0; j < nnz; j++) csc_ptr[d->M_to[j] + 1]++;
+	for (int t = 0; t < A; t++) csc_ptr[t + 1] += csc_ptr[t];
+	{
+		std::vector<int32_t> fill(csc_ptr.begin(), csc_ptr.end() - 1);
+		for (int c = 0; c < A; c++)
+			for (int j = d->M_rowptr[c]; j < d->M_rowptr[c + 1]; j++) {
+				int t = d->M_to[j];
+				csc_src[fill[t]] = c;
+				csc_val[fill[t]] = d->M_val[j];
+				fill[t]++;
+			}
+	}
+
+	beep_model *m = new beep_model();
+	m->A = A; m->G = G; m->DP = DP; m->NS = NS; m->C = C; m->T = T; m->S = S;
+	m->period = d->period; m->dpt = d->division_per_time; m->nobs = nobs;
+	m->obs_sett_i.assign(d->obs_sett_i, d->obs_sett_i + nobs);
+	m->obs_sett_f.assign(d->obs_sett_f, d->obs_sett_f + nobs);
+	m->obs_spline.assign(d->obs_factor_spline, d->obs_factor_spline + nobs);
+	m->trans_from_h.assign(d->trans_from, d->trans_from + T);
+	m->trans_to_h.assign(d->trans_to, d->trans_to + T);
+	cudaGetDevice(&m->device);
+
+	Layout L;
+	size_t o_tf = L.add(4 * T), o_tt = L.add(4 * T), o_age = L.add(4 * DPS), o_diag = L.add(8 * A),
+	       o_fac = L.add(8 * A), o_cp = L.add(4 * (A + 1)), o_cs = L.add(4 * (size_t)nnz), o_cv = L.add(8 * (size_t)nnz),
+	       o_pi = L.add(4 * popsz), o_om = L.add(4 * (size_t)nobs), o_ok = L.add(4 * (size_t)nobs),
+	       o_os = L.add(4 * (size_t)nobs), o_ocp = L.add(4 * (size_t)(nobs + 1)), o_oc = L.add(4 * (size_t)ncells),
+	       o_osi = L.add(4 * (size_t)nobs), o_osf = L.add(4 * (size_t)nobs), o_ov = L.add(8 * (size_t)nobs),
+	       o_osd = L.add(8 * (size_t)nobs), o_osh = L.add(8 * (size_t)nobs), o_oth = L.add(8 * (size_t)nobs),
+	       o_ofa = L.add(8 * (size_t)nobs);
+	std::vector<char> host(L.size);
+	auto put = [&](size_t off, const void *src, size_t n) { if (n) memcpy(host.data() + off, src, n); };
+	put(o_tf, d->trans_from, 4 * T); put(o_tt, d->trans_to, 4 * T); put(o_age, d->democatpos_age, 4 * DPS);
+	put(o_diag, d->M_diag, 8 * A); put(o_fac, d->M_factor, 8 * A); put(o_cp, csc_ptr.data(), 4 * (A + 1));
+	put(o_cs, csc_src.data(), 4 * (size_t)nnz); put(o_cv, csc_val.data(), 8 * (size_t)nnz);
+	put(o_pi, pop_init.data(), 4 * popsz);
+	if (nobs > 0) {
+		put(o_om, d->obs_model, 4 * (size_t)nobs); put(o_ok, d->obs_value_kind, 4 * (size_t)nobs);
+		put(o_os, d->obs_factor_spline, 4 * (size_t)nobs); put(o_ocp, d->obs_cell_ptr, 4 * (size_t)(nobs + 1));
+		put(o_oc, d->obs_cells, 4 * (size_t)ncells); put(o_osi, d->obs_sett_i, 4 * (size_t)nobs);
+		put(o_osf, d->obs_sett_f, 4 * (size_t)nobs); put(o_ov, d->obs_value, 8 * (size_t)nobs);
+		put(o_osd, d->obs_sd, 8 * (size_t)nobs); put(o_osh, d->obs_shape, 8 * (size_t)nobs);
+		put(o_oth, d->obs_threshold, 8 * (size_t)nobs); put(o_ofa, d->obs_factor, 8 * (size_t)nobs);
+	}
+	cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
+	if (e == cudaSuccess) e = m->model_mem.reserve(L.size);
+	if (e == cudaSuccess) e = cudaMemcpy(m->model_mem.ptr, host.data(), L.size, cudaMemcpyHostToDevice);
+	if (e != cudaSuccess) {
+		beep_model_destroy(m);
+		return fail(e == cudaErrorMemoryAllocation ? BEEP_OOM : BEEP_DEVICE_ERROR, std::string("model upload: ") + cudaGetErrorString(e));
+	}
+	char *base = (char *)m->model_mem.ptr;
+	ModelDev &md = m->dev;
+	md.A = A; md.G = G; md.DP = DP; md.NS = NS; md.DPS = DPS; md.C = C; md.T = T; md.S = S;
+	md.period = d->period; md.div_per_time = d->division_per_time; md.nobs = nobs;
+	md.infection_trans = d->infection_trans; md.dt = d->dt; md.popsize = d->popsize;
+	md.trans_from = (const int32_t *)(base + o_tf); md.trans_to = (const int32_t *)(base + o_tt);
+	md.dp_age = (const int32_t *)(base + o_age); md.M_diag = (const double *)(base + o_diag);
+	md.M_factor = (const double *)(base + o_fac); md.csc_ptr = (const int32_t *)(base + o_cp);
+	md.csc_src = (const int32_t *)(base + o_cs); md.csc_val = (const double *)(base + o_cv);
+	md.pop_init = (const int32_t *)(base + o_pi);
+	md.obs_model = (const int32_t *)(base + o_om); md.obs_kind = (const int32_t *)(base + o_ok);
+	md.obs_spline = (const int32_t *)(base + o_os); md.obs_cell_ptr = (const int32_t *)(base + o_ocp);
+	md.obs_cells = (const int32_t *)(base + o_oc); md.obs_sett_i = (const int32_t *)(base + o_osi);
+	md.obs_sett_f = (const int32_t *)(base + o_osf); md.obs_value = (const double *)(base + o_ov);
+	md.obs_sd = (const double *)(base + o_osd); md.obs_shape = (const double *)(base + o_osh);
+	md.obs_thresh = (const double *)(base + o_oth); md.obs_factor = (const double *)(base + o_ofa);
+	*out = m;
+	return BEEP_OK;
+}
+
+beep_status beep_model_destroy(beep_model *m)
+{
+	if (!m) return BEEP_OK;
+	if (m->stream) cudaStreamSynchronize(m->stream);
+	m->model_mem.release();
+	if (m->stream) cudaStreamDestroy(m->stream);
+	delete m;
+	return BEEP_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+struct TablePacker {
+	std::vector<double> f;
+	std::vector<int32_t> i;
+	std::map<std::pair<const void *, size_t>, int64_t> seen;
+	int64_t addf(const double *p, size_t n)
+	{
+		auto key = std::make_pair((const void *)p, n);
+		auto it = seen.find(key);
+		if (it != seen.end()) return it->second;
+		int64_t off = (int64_t)f.size();
+		f.insert(f.end(), p, p + n);
+		f.resize(align_up(f.size(), 4));
+		seen[key] = off;
+		return off;
+	}
+	int64_t addi(const int32_t *p, size_t n)
+	{
+		auto key = std::make_pair((const void *)p, n + ((size_t)1 << 62));
+		auto it = seen.find(key);
+		if (it != seen.end()) return it->second;
+		int64_t off = (int64_t)i.size();
+		i.insert(i.end(), p, p + n);
+		i.resize(align_up(i.size(), 8));
+		seen[key] = off;
+		return off;
+	}
+};
+
+beep_status pack_tables(const beep_model *m, const beep_sim_batch *b, TablePacker &pk, std::vector<GroupDir> &dirs)
+{
+	const size_t A = m->A, G = m->G, DP = m->DP, NS = m->NS, C = m->C, T = m->T, S = m->S;
+	dirs.resize(b->ngroup);
+	for (int g = 0; g < b->ngroup; g++) {
+		const beep_param_tables &t = b->groups[g];
+		if (!t.transrate || !t.susceptibility || !t.infectivity || !t.beta_rows || !t.beta_row_of || !t.areafactor ||
+		    !t.Ntime || !t.geo_spline || !t.efoi_spline || !t.efoi_agedist || !t.efoi_ref)
+			return fail(BEEP_BAD_INPUT, "parameter set " + std::to_string(g) + ": missing table");
+		if (t.nbeta_row <= 0 || t.nefoi <= 0 || t.nobs_spline < 0)
+			return fail(BEEP_BAD_INPUT, "parameter set " + std::to_string(g) + ": bad table counts");
+		for (size_t k = 0; k < NS * A; k++) {
+			if (t.beta_row_of[k] < 0 || t.beta_row_of[k] >= t.nbeta_row) return fail(BEEP_BAD_INPUT, "beta_row_of out of range");
+			if (t.efoi_ref[k] < 0 || t.efoi_ref[k] >= t.nefoi) return fail(BEEP_BAD_INPUT, "efoi_ref out of range");
+		}
+		for (int o = 0; o < m->nobs; o++)
+			if (m->obs_spline[o] >= t.nobs_spline) return fail(BEEP_BAD_INPUT, "obs_factor_spline beyond nobs_spline");
+		GroupDir &dd = dirs[g];
+		dd.transrate = pk.addf(t.transrate, T * DP);
+		dd.susceptibility = pk.addf(t.susceptibility, DP);
+		dd.infectivity = pk.addf(t.infectivity, C);
+		dd.infdif = (int64_t)pk.f.size();    // filled when the pool is staged
+		pk.f.resize(pk.f.size() + align_up(T, 4));
+		dd.beta_rows = pk.addf(t.beta_rows, (size_t)t.nbeta_row * S);
+		dd.areafactor = pk.addf(t.areafactor, (size_t)m->period * A);
+		dd.Ntime = pk.addf(t.Ntime, S * G * G);
+		dd.geo_spline = pk.addf(t.geo_spline, S);
+		dd.efoi_spline = pk.addf(t.efoi_spline, (size_t)t.nefoi * S);
+		dd.efoi_agedist = pk.addf(t.efoi_agedist, (size_t)t.nefoi * G);
+		dd.obs_spline = t.nobs_spline > 0 && t.obs_spline ? pk.addf(t.obs_spline, (size_t)t.nobs_spline * S) : 0;
+		dd.beta_row_of = pk.addi(t.beta_row_of, NS * A);
+		dd.efoi_ref = pk.addi(t.efoi_ref, NS * A);
+	}
+	return BEEP_OK;
+}
+
+}  // namespace
+
+
+// A prepared batch: the caller's host arrays (kept by pointer), pinned staging,
+// device inputs, work and outputs, and the kernel's view of them.
+struct beep_batch {
+	beep_model *m = nullptr;
+	beep_sim_batch b{};
+	HostBuf in_host, out_host;
+	DevBuf in_dev, work_dev, out_dev;
+	size_t in_size = 0, out_size = 0;
+	size_t o_f = 0, u_st = 0, u_L = 0, u_po = 0, u_tn = 0, u_pt = 0;
+	std::vector<GroupDir> dirs;
+	std::vector<int32_t> scored, step_ptr, step_obs;
+	BatchDev bd{};
+	cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+	bool pending = false;
+};
+
+namespace {
+
+beep_status check_batch(const beep_model *m, const beep_sim_batch *b)
+{
+	const int P = b->nparticle;
+	if (P <= 0 || b->ngroup <= 0 || !b->groups) return fail(BEEP_BAD_INPUT, "nparticle/ngroup/groups");
+	if (b->ti < 0 || b->tf <= b->ti || b->tf > m->S) return fail(BEEP_BAD_INPUT, "step range must satisfy 0 <= ti < tf <= ndivision");
+	if (b->ti > 0 && !b->pop_in) return fail(BEEP_BAD_INPUT, "pop_in is required when ti > 0");
+	if (b->form != BEEP_FORM_PLAIN_FP64) return fail(BEEP_BAD_INPUT, "unknown form");
+	if (b->group_of)
+		for (int p = 0; p < P; p++)
+			if (b->group_of[p] < 0 || b->group_of[p] >= b->ngroup) return fail(BEEP_BAD_INPUT, "group_of out of range");
+	return BEEP_OK;
+}
+
+// Packs the caller's current host arrays into the pinned staging buffer.
+beep_status stage_inputs(beep_batch *q)
+{
+	beep_model *m = q->m;
+	const beep_sim_batch *b = &q->b;
+	const int P = b->nparticle;
+	const size_t popsz = (size_t)m->A * m->C * m->DP;
+	TablePacker pk;
+	beep_status st = pack_tables(m, b, pk, q->dirs);
+	if (st != BEEP_OK) return st;
+	Layout in;
+	size_t o_dirs = in.add(sizeof(GroupDir) * q->dirs.size()), o_f = in.add(8 * pk.f.size()),
+	       o_i = in.add(4 * pk.i.size()), o_go = in.add(b->group_of ? 4 * (size_t)P : 0),
+	       o_so = in.add(b->stream_of ? 4 * (size_t)P : 0), o_pin = in.add(b->ti > 0 ? 4 * popsz * P : 0),
+	       o_sc = in.add(4 * q->scored.size()), o_sp = in.add(4 * q->step_ptr.size()),
+	       o_sobs = in.add(4 * q->step_obs.size());
+	CUDA_TRY(q->in_host.reserve(in.size));
+	CUDA_TRY(q->in_dev.reserve(in.size));
+	q->in_size = in.size;
+	char *h = (char *)q->in_host.ptr;
+	memcpy(h + o_dirs, q->dirs.data(), sizeof(GroupDir) * q->dirs.size());
+	memcpy(h + o_f, pk.f.data(), 8 * pk.f.size());
+	if (!pk.i.empty()) memcpy(h + o_i, pk.i.data(), 4 * pk.i.size());
+	if (b->group_of) memcpy(h + o_go, b->group_of, 4 * (size_t)P);
+	if (b->stream_of) memcpy(h + o_so, b->stream_of, 4 * (size_t)P);
+	if (b->ti > 0) memcpy(h + o_pin, b->pop_in, 4 * popsz * P);
+	if (!q->scored.empty()) memcpy(h + o_sc, q->scored.data(), 4 * q->scored.size());
+	memcpy(h + o_sp, q->step_ptr.data(), 4 * q->step_ptr.size());
+	if (!q->step_obs.empty()) memcpy(h + o_sobs, q->step_obs.data(), 4 * q->step_obs.size());
+	// infectivity difference of each transition, Model::get_infectivity_dif (src/model.cc:820-823)
+	double *fpool = (double *)(h + o_f);
+	for (int g = 0; g < b->ngroup; g++) {
+		const double *inf = b->groups[g].infectivity;
+		for (int tr = 0; tr < m->T; tr++)
+			fpool[q->dirs[g].infdif + tr] = inf[m->trans_to_h[tr]] - inf[m->trans_from_h[tr]];
+	}
+	char *di = (char *)q->in_dev.ptr;
+	BatchDev &bd = q->bd;
+	bd.dirs = (const GroupDir *)(di + o_dirs);
+	bd.fpool = (const double *)(di + o_f);
+	bd.ipool = (const int32_t *)(di + o_i);
+	bd.group_of = b->group_of ? (const int32_t *)(di + o_go) : nullptr;
+	bd.stream_of = b->stream_of ? (const uint32_t *)(di + o_so) : nullptr;
+	bd.pop_in = b->ti > 0 ? (const int32_t *)(di + o_pin) : nullptr;
+	bd.scored = (const int32_t *)(di + o_sc);
+	bd.step_ptr = (const int32_t *)(di + o_sp);
+	bd.step_obs = (const int32_t *)(di + o_sobs);
+	return BEEP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+beep_status beep_batch_create(beep_model *m, const beep_sim_batch *b, beep_batch **out)
+{
+	if (!m || !b || !out) return fail(BEEP_BAD_INPUT, "null argument");
+	*out = nullptr;
+	beep_status st = check_batch(m, b);
+	if (st != BEEP_OK) return st;
+	CUDA_TRY(cudaSetDevice(m->device));
+	beep_batch *q = new beep_batch();
+	q->m = m;
+	q->b = *b;
+	const int P = b->nparticle;
+	const size_t popsz = (size_t)m->A * m->C * m->DP, tnsz = (size_t)m->A * m->T * m->DP;
+	const size_t agsz = (size_t)m->NS * m->A * m->G;
+	const int nsteps = b->tf - b->ti;
+	// scored observations and the steps each is active in
+	q->step_ptr.assign(nsteps + 1, 0);
+	for (int o = 0; o < m->nobs; o++)
+		if (m->obs_sett_i[o] >= b->ti && m->obs_sett_f[o] <= b->tf) q->scored.push_back(o);
+	for (size_t k = 0; k < q->scored.size(); k++) {
+		int o = q->scored[k];
+		for (int s = m->obs_sett_i[o]; s < m->obs_sett_f[o]; s++) q->step_ptr[s - b->ti + 1]++;
+	}
+	for (int s = 0; s < nsteps; s++) q->step_ptr[s + 1] += q->step_ptr[s];
+	q->step_obs.resize(q->step_ptr[nsteps]);
+	{
+		std::vector<int32_t> fill(q->step_ptr.begin(), q->step_ptr.end() - 1);
+		for (size_t k = 0; k < q->scored.size(); k++) {
+			int o = q->scored[k];
+			for (int s = m->obs_sett_i[o]; s < m->obs_sett_f[o]; s++) q->step_obs[fill[s - b->ti]++] = (int32_t)k;
+		}
+	}
+	const int nscored = (int)q->scored.size();
+	auto bail = [&](beep_status s) { beep_batch_destroy(q); return s; };
+	st = stage_inputs(q);
+	if (st != BEEP_OK) return bail(st);
+
+	Layout wk;
+	size_t w_pa = wk.add(4 * popsz * P), w_pb = wk.add(4 * popsz * P), w_tn = wk.add(b->transnum_out ? 0 : 4 * tnsz * P),
+	       w_im = wk.add(8 * agsz * P), w_id = wk.add(8 * agsz * P), w_di = wk.add(8 * agsz * P),
+	       w_nmi = wk.add(8 * agsz * P), w_acc = wk.add(8 * (size_t)nscored * P);
+	Layout ou;
+	q->u_st = ou.add(4 * (size_t)P);
+	q->u_L = ou.add(b->L_out ? 8 * (size_t)P : 0);
+	q->u_po = ou.add(b->pop_out ? 4 * popsz * P : 0);
+	q->u_tn = ou.add(b->transnum_out ? 4 * tnsz * (size_t)nsteps * P : 0);
+	q->u_pt = ou.add(b->pop_traj_out ? 4 * popsz * (size_t)nsteps * P : 0);
+	q->out_size = ou.size;
+	cudaError_t e = q->work_dev.reserve(wk.size);
+	if (e == cudaSuccess) e = q->out_dev.reserve(ou.size);
+	if (e == cudaSuccess) e = q->out_host.reserve(ou.size);
+	if (e == cudaSuccess) e = cudaEventCreate(&q->ev0);
+	if (e == cudaSuccess) e = cudaEventCreate(&q->ev1);
+	if (e != cudaSuccess)
+		return bail(fail(e == cudaErrorMemoryAllocation ? BEEP_OOM : BEEP_DEVICE_ERROR, cudaGetErrorString(e)));
+	char *dw = (char *)q->work_dev.ptr, *dout = (char *)q->out_dev.ptr;
+	BatchDev &bd = q->bd;
+	bd.P = P; bd.ti = b->ti; bd.tf = b->tf; bd.ngroup = b->ngroup;
+	bd.k0 = (uint32_t)b->seed; bd.k1 = (uint32_t)(b->seed >> 32);
+	bd.nscored = nscored;
+	bd.pop_a = (int32_t *)(dw + w_pa); bd.pop_b = (int32_t *)(dw + w_pb);
+	bd.tn = b->transnum_out ? nullptr : (int32_t *)(dw + w_tn);
+	bd.Imap = (double *)(dw + w_im); bd.Idiag = (double *)(dw + w_id); bd.dinf = (double *)(dw + w_di);
+	bd.NMI = (double *)(dw + w_nmi); bd.obs_acc = (double *)(dw + w_acc);
+	bd.status = (int32_t *)(dout + q->u_st);
+	bd.L = b->L_out ? (double *)(dout + q->u_L) : nullptr;
+	bd.pop_out = b->pop_out ? (int32_t *)(dout + q->u_po) : nullptr;
+	bd.tn_traj = b->transnum_out ? (int32_t *)(dout + q->u_tn) : nullptr;
+	bd.pop_traj = b->pop_traj_out ? (int32_t *)(dout + q->u_pt) : nullptr;
+	*out = q;
+	return BEEP_OK;
+}
+
+beep_status beep_batch_stage(beep_batch *q)
+{
+	if (!q) return fail(BEEP_BAD_INPUT, "null batch");
+	beep_status st = check_batch(q->m, &q->b);
+	if (st != BEEP_OK) return st;
+	CUDA_TRY(cudaStreamSynchronize(q->m->stream));   // the staging buffer may still feed a copy
+	return stage_inputs(q);
+}
+
+beep_status beep_batch_upload(beep_batch *q)
+{
+	if (!q) return fail(BEEP_BAD_INPUT, "null batch");
+	CUDA_TRY(cudaMemcpyAsync(q->in_dev.ptr, q->in_host.ptr, q->in_size, cudaMemcpyHostToDevice, q->m->stream));
+	return BEEP_OK;
+}
+
+beep_status beep_batch_launch(beep_batch *q)
+{
+	if (!q) return fail(BEEP_BAD_INPUT, "null batch");
+	CUDA_TRY(cudaMemsetAsync(q->bd.status, 0, 4 * (size_t)q->bd.P, q->m->stream));
+	int le = launch_sim_plain(q->m->dev, q->bd, q->m->stream);
+	if (le != 0) return fail(BEEP_DEVICE_ERROR, std::string("kernel launch: ") + cudaGetErrorString((cudaError_t)le));
+	q->pending = true;
+	return BEEP_OK;
+}
+
+beep_status beep_batch_download(beep_batch *q)
+{
+	if (!q) return fail(BEEP_BAD_INPUT, "null batch");
+	const beep_sim_batch *b = &q->b;
+	CUDA_TRY(cudaMemcpyAsync(q->out_host.ptr, q->out_dev.ptr, q->out_size, cudaMemcpyDeviceToHost, q->m->stream));
+	CUDA_TRY(cudaStreamSynchronize(q->m->stream));
+	q->pending = false;
+	const beep_model *m = q->m;
+	const int P = b->nparticle, nsteps = b->tf - b->ti;
+	const size_t popsz = (size_t)m->A * m->C * m->DP, tnsz = (size_t)m->A * m->T * m->DP;
+	const char *ho = (const char *)q->out_host.ptr;
+	const int32_t *pst = (const int32_t *)(ho + q->u_st);
+	for (int p = 0; p < P; p++)
+		if (pst[p] != 0) return fail((beep_status)pst[p], "particle " + std::to_string(p) + " failed on the device");
+	if (b->L_out) memcpy(b->L_out, ho + q->u_L, 8 * (size_t)P);
+	if (b->pop_out) memcpy(b->pop_out, ho + q->u_po, 4 * popsz * P);
+	if (b->transnum_out) memcpy(b->transnum_out, ho + q->u_tn, 4 * tnsz * (size_t)nsteps * P);
+	if (b->pop_traj_out) memcpy(b->pop_traj_out, ho + q->u_pt, 4 * popsz * (size_t)nsteps * P);
+	return BEEP_OK;
+}
+
+beep_status beep_batch_time(beep_batch *q, int32_t iters, double *ms_per_launch)
+{
+	if (!q || iters <= 0 || !ms_per_launch) return fail(BEEP_BAD_INPUT, "bad argument");
+	cudaStream_t s = q->m->stream;
+	CUDA_TRY(cudaStreamSynchronize(s));
+	CUDA_TRY(cudaEventRecord(q->ev0, s));
+	for (int k = 0; k < iters; k++) {
+		beep_status st = beep_batch_launch(q);
+		if (st != BEEP_OK) return st;
+	}
+	CUDA_TRY(cudaEventRecord(q->ev1, s));
+	CUDA_TRY(cudaEventSynchronize(q->ev1));
+	float ms = 0;
+	CUDA_TRY(cudaEventElapsedTime(&ms, q->ev0, q->ev1));
+	*ms_per_launch = (double)ms / iters;
+	return BEEP_OK;
+}
+
+int32_t beep_batch_launches(const beep_batch *q) { return q ? 1 : 0; }
+
+beep_status beep_batch_bytes(const beep_batch *q, int64_t *h2d, int64_t *d2h)
+{
+	if (!q || !h2d || !d2h) return fail(BEEP_BAD_INPUT, "null argument");
+	*h2d = (int64_t)q->in_size;
+	*d2h = (int64_t)q->out_size;
+	return BEEP_OK;
+}
+
+beep_status beep_batch_destroy(beep_batch *q)
+{
+	if (!q) return BEEP_OK;
+	if (q->m && q->m->stream) cudaStreamSynchronize(q->m->stream);
+	q->in_host.release();
+	q->out_host.release();
+	q->in_dev.release();
+	q->work_dev.release();
+	q->out_dev.release();
+	if (q->ev0) cudaEventDestroy(q->ev0);
+	if (q->ev1) cudaEventDestroy(q->ev1);
+	delete q;
+	return BEEP_OK;
+}
+
+beep_status beep_simulate(beep_model *m, const beep_sim_batch *b)
+{
+	if (!m || !b) return fail(BEEP_BAD_INPUT, "null argument");
+	std::lock_guard<std::mutex> lock(m->mu);
+	beep_batch *q = nullptr;
+	beep_status st = beep_batch_create(m, b, &q);
+	if (st != BEEP_OK) return st;
+	st = beep_batch_upload(q);
+	if (st == BEEP_OK) st = beep_batch_launch(q);
+	if (st == BEEP_OK) st = beep_batch_download(q);
+	std::string err = g_err;
+	beep_batch_destroy(q);
+	g_err = err;
+	return st;
+}
+
+}  // extern "C"

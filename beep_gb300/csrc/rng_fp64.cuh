@@ -1,0 +1,159 @@
+// Keyed variate streams for the FP64 plain form.
+//
+// uniforms: Philox4x32-10 (Salmon et al., SC'11); key = 64-bit seed,
+//           counter = {cell, step, stream, (purpose << 24) | iteration};
+//           u = (2k+1) 2^-53 from 52 bits of two words, strictly inside (0,1).
+// Poisson:  mean < 10 sequential inversion; mean >= 10 PTRS (Hoermann 1993).
+// exp/log:  Cody-Waite reduction by ln 2 with a degree-14 Taylor series for
+//           e^r; log(m) = 2 atanh((m-1)/(m+1)) series; log k! exact below 23,
+//           Stirling series above.  Only IEEE +,-,*,/,sqrt are used, and this
+//           header is compiled without FMA contraction (--fmad=false), so the
+//           draws are a pure function of (seed, counter, mean) -- identical to
+//           any other IEEE-754 implementation of the same recipe.
+#pragma once
+
+#include <cstdint>
+
+namespace beep {
+
+constexpr uint32_t PURPOSE_TRANS = 0u;
+constexpr uint32_t PURPOSE_THIN = 1u;
+constexpr uint32_t PURPOSE_RESAMPLE = 2u;
+
+struct U4 { uint32_t x, y, z, w; };
+
+__device__ __forceinline__ U4 philox10(U4 c, uint32_t k0, uint32_t k1)
+{
+#pragma unroll
+	for (int r = 0; r < 10; r++) {
+		const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+		const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+		c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+		k0 += 0x9E3779B9u;
+		k1 += 0xBB67AE85u;
+	}
+	return c;
+}
+
+__device__ __forceinline__ double u01_pair(uint32_t a, uint32_t b)
+{
+	const uint64_t k = ((uint64_t)(a >> 6) << 26) | (uint64_t)(b >> 6);
+	return (double)(2ull * k + 1ull) * 1.1102230246251565e-16;
+}
+
+__device__ __forceinline__ double scale2(double x, int k)
+{
+	while (k > 1000) { x *= 1.0715086071862673e+301; k -= 1000; }
+	while (k < -1000) { x *= 9.332636185032189e-302; k += 1000; }
+	return x * __longlong_as_double((long long)((uint64_t)(k + 1023) << 52));
+}
+
+__device__ __forceinline__ double exp_p(double x)
+{
+	if (x != x) return x;
+	if (x > 709.0) return __longlong_as_double(0x7ff0000000000000ll);
+	if (x < -745.0) return 0.0;
+	const double kd = floor(x * 1.4426950408889634 + 0.5);
+	const int k = (int)kd;
+	const double r = (x - kd * 0.6931471803691238) - kd * 1.9082149292705877e-10;
+	double p = 1.1470745597729725e-11;
+	p = p * r + 1.6059043836821613e-10;
+	p = p * r + 2.08767569878681e-09;
+	p = p * r + 2.505210838544172e-08;
+	p = p * r + 2.755731922398589e-07;
+	p = p * r + 2.7557319223985893e-06;
+	p = p * r + 2.48015873015873e-05;
+	p = p * r + 0.0001984126984126984;
+	p = p * r + 0.001388888888888889;
+	p = p * r + 0.008333333333333333;
+	p = p * r + 0.041666666666666664;
+	p = p * r + 0.16666666666666666;
+	p = p * r + 0.5;
+	p = p * r + 1.0;
+	p = p * r + 1.0;
+	return scale2(p, k);
+}
+
+__device__ __forceinline__ double log_p(double x)
+{
+	if (!(x > 0.0)) return x == 0.0 ? -__longlong_as_double(0x7ff0000000000000ll) : __longlong_as_double(0x7ff8000000000000ll);
+	if (x == __longlong_as_double(0x7ff0000000000000ll)) return x;
+	int e = 0;
+	if (x < 9.332636185032189e-302) { x *= 1.2676506002282294e+30; e = -100; }
+	uint64_t b = (uint64_t)__double_as_longlong(x);
+	e += (int)((b >> 52) & 0x7ff) - 1023;
+	b = (b & 0x000fffffffffffffull) | 0x3ff0000000000000ull;
+	double m = __longlong_as_double((long long)b);
+	if (m > 1.4142135623730951) { m *= 0.5; e += 1; }
+	const double s = (m - 1.0) / (m + 1.0);
+	const double z = s * s;
+	double q = 1.0 / 21.0;
+	q = q * z + 1.0 / 19.0;
+	q = q * z + 1.0 / 17.0;
+	q = q * z + 1.0 / 15.0;
+	q = q * z + 1.0 / 13.0;
+	q = q * z + 1.0 / 11.0;
+	q = q * z + 1.0 / 9.0;
+	q = q * z + 1.0 / 7.0;
+	q = q * z + 1.0 / 5.0;
+	q = q * z + 1.0 / 3.0;
+	q = q * z + 1.0;
+	const double lm = 2.0 * s * q;
+	const double ed = (double)e;
+	return ed * 0.6931471803691238 + (ed * 1.9082149292705877e-10 + lm);
+}
+
+__device__ __forceinline__ double log_factorial_p(double k)
+{
+	if (k <= 22.0) {
+		double f = 1.0;
+		for (double j = 2.0; j <= k; j += 1.0) f *= j;
+		return log_p(f);
+	}
+	const double n = k + 1.0;
+	const double in = 1.0 / n, in2 = in * in;
+	const double corr = in * (1.0 / 12.0 - in2 * (1.0 / 360.0 - in2 * (1.0 / 1260.0 - in2 * (1.0 / 1680.0))));
+	return (n - 0.5) * log_p(n) - n + 0.9189385332046728 + corr;
+}
+
+// Poisson(mean) for cell/step/stream; -1 only after 2^24 rejections.
+__device__ __noinline__ int32_t poisson_fp64(double mean, uint32_t k0, uint32_t k1, uint32_t cell,
+                                              uint32_t step, uint32_t stream, uint32_t purpose)
+{
+	if (!(mean > 0.0)) return 0;
+	if (mean < 10.0) {
+		const U4 r = philox10(U4{cell, step, stream, purpose << 24}, k0, k1);
+		const double u = u01_pair(r.x, r.y);
+		double p = exp_p(-mean);
+		double F = p;
+		int32_t k = 0;
+		while (u > F && k < 1000) {
+			k++;
+			p = p * mean / (double)k;
+			F = F + p;
+		}
+		return k;
+	}
+	const double slam = sqrt(mean);
+	const double loglam = log_p(mean);
+	const double b = 0.931 + 2.53 * slam;
+	const double a = -0.059 + 0.02483 * b;
+	const double invalpha = 1.1239 + 1.1328 / (b - 3.4);
+	const double vr = 0.9277 - 3.6224 / (b - 2.0);
+	const double log_invalpha = log_p(invalpha);
+	for (uint32_t it = 0; it < (1u << 24); it++) {
+		const U4 r = philox10(U4{cell, step, stream, (purpose << 24) | it}, k0, k1);
+		const double U = u01_pair(r.x, r.y) - 0.5;
+		const double V = u01_pair(r.z, r.w);
+		const double us = 0.5 - fabs(U);
+		const double k = floor((2.0 * a / us + b) * U + mean + 0.43);
+		if (us >= 0.07 && V <= vr) return (int32_t)k;
+		if (k < 0.0 || (us < 0.013 && V > us)) continue;
+		const double lhs = log_p(V) + log_invalpha - log_p(a / (us * us) + b);
+		const double rhs = -mean + k * loglam - log_factorial_p(k);
+		if (lhs <= rhs) return (int32_t)k;
+	}
+	return -1;
+}
+
+}  // namespace beep

@@ -1,0 +1,311 @@
+"""Builds the hot path's tables for a synthetic SEIR-H-D workload without the
+reference: the parameter-independent model (Data / Model members) and, per
+parameter set, what ``State::set_param`` derives (src/state.cc:66-91).
+
+Each step restates the reference's arithmetic:
+  * area mixing: dense matrix rows -> diagonal + off-diagonal lists, then the
+    per-capita normalisation and genQ.factor of Data::geo_normalise
+    (src/data_matrix.cc:55-80, 205-223);
+  * age mixing: Data::age_mixing_matrix (scaling by age shares, symmetrising)
+    and Data::agematrix_normalise (src/data_matrix.cc:100-189);
+  * transition rates: Model::create_transrate (src/model.cc:1116-1140);
+  * splines: Model::create_disc_spline, piecewise linear at step midpoints
+    (src/model.cc:1018-1041);
+  * area factors from linear covariates, normalised by the population-weighted
+    mean: Model::create_areafactor / calculate_area_av (src/model.cc:1182-1250);
+  * age-mixing modifications: Model::create_Ntime (src/model.cc:1254-1301);
+  * beta = R(t) / lambda_max(NGM) with NGM = F V^-1 over the infectious states
+    (src/model.cc:1318-1362, 2485-2621).  The reference finds lambda_max by a
+    warm-started power iteration converged to ~1e-13; here it is taken from a
+    dense eigen-solve, so beta agrees with the reference to ~1e-13 relative.
+Everything else is bit-identical to the reference's tables (tested against
+the golden bundles made by the reference itself).
+"""
+from __future__ import annotations
+
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import synth
+
+COMPS = ["S", "E", "I", "H", "R", "D"]
+# (from, to) in declaration order; S->E is the infection transition
+TRANS = [(0, 1), (1, 2), (2, 3), (2, 4), (3, 5), (3, 4)]
+OBS_NORMAL = 0
+UNSET = 999999999.0
+
+
+def _seq_sum(vals) -> float:
+    s = 0.0
+    for v in vals:
+        s += float(v)
+    return s
+
+
+def model_arrays(w: synth.Workload, obs_values: Optional[dict] = None) -> Dict[str, np.ndarray]:
+    """The parameter-independent model (beep_model_desc fields) of a workload.
+
+    ``obs_values``: data file -> column -> (values, sds) as written to the
+    workload's data tables; placeholders (0, sd 1) when None."""
+    A, G = w.narea, w.nage
+    DP, C, T = G, len(COMPS), len(TRANS)
+    S = w.ndivision
+    pop = np.asarray(w.pop, np.int64)
+    total_pop = pop.sum(1)                       # Area::total_pop (unsigned)
+    popsize = float(total_pop.sum())
+
+    # area mixing (dense load, then per-capita normalisation)
+    diag = np.zeros(A)
+    rowptr = [0]
+    to: List[int] = []
+    val: List[float] = []
+    geo = np.asarray(w.geo, np.float64) if A > 1 else np.ones((1, 1))
+    for c in range(A):
+        d = float(geo[c, c])
+        tos = [i for i in range(A) if i != c and geo[c, i] != 0]
+        vs = [float(geo[c, i]) for i in tos]
+        s = d * float(total_pop[c])
+        for i, v in zip(tos, vs):
+            s += v * float(total_pop[i])
+        diag[c] = d / s
+        to += tos
+        val += [v / s for v in vs]
+        rowptr.append(len(to))
+    factor = np.array([(1.0 / float(total_pop[c])) / diag[c] for c in range(A)])
+
+    pop_init = np.zeros((A, C, DP))
+    pop_init[:, 0, :] = pop - w.seed_E
+    pop_init[:, 1, :] = w.seed_E
+
+    arr: Dict[str, np.ndarray] = {
+        "dims": np.array([A, G, DP, 1, C, T, S, w.days, w.steps_per_day], np.int32),
+        "dt": np.array([float(w.days) / S]),
+        "popsize": np.array([popsize]),
+        "trans_from": np.array([f for f, _ in TRANS], np.int32),
+        "trans_to": np.array([t for _, t in TRANS], np.int32),
+        "infection_trans": np.array([0], np.int32),
+        "democatpos_age": np.arange(G, dtype=np.int32),
+        "M_diag": diag, "M_rowptr": np.array(rowptr, np.int32), "M_to": np.array(to, np.int32),
+        "M_val": np.array(val, np.float64), "M_factor": factor, "pop_init": pop_init,
+    }
+    arr.update(_observations(w, obs_values))
+    return arr
+
+
+def _observations(w: synth.Workload, obs_values: Optional[dict]) -> Dict[str, np.ndarray]:
+    """Observation list in the reference's order: data table -> column -> row
+    (Data::load_timeseries_datatable, src/data.cc:1119-1320)."""
+    G, T, C = w.nage, len(TRANS), len(COMPS)
+    DP = G
+    spd = w.steps_per_day
+    si, sf, vals, sds, cptr, cells = [], [], [], [], [0], []
+    tr_of = {"E->I": 1, "H->D": 4}
+    for tab in synth.data_tables(w):
+        tt = tab["toml"]
+        nrow = len(tab["times"])
+        for ci, col in enumerate(tab["columns"]):
+            c = ci
+            if "democats_filt" in tt:
+                dps = [int(tt["democats_filt"].split("age")[-1])]
+            else:
+                dps = list(range(DP))
+            ov = obs_values.get(tab["file"], {}).get(col) if obs_values else None
+            for r, t in enumerate(tab["times"]):
+                if tt["type"] == "transition":
+                    step = int(tt["timestep"])
+                    si.append(t * spd)
+                    sf.append((t + step) * spd)
+                    tr = tr_of[tt["observation"]]
+                    cells += [(c * T + tr) * DP + dp for dp in dps]
+                else:
+                    si.append(t * spd)
+                    sf.append(t * spd + 1)
+                    co = COMPS.index(tt["observation"])
+                    cells += [-1 - ((c * C + co) * DP + dp) for dp in dps]
+                cptr.append(len(cells))
+                if ov is None:
+                    vals.append(0.0)
+                    sds.append(1.0)
+                else:
+                    vals.append(float(ov[0][r]))
+                    sds.append(float(ov[1][r]))
+    n = len(si)
+    return {
+        "obs_sett_i": np.array(si, np.int32), "obs_sett_f": np.array(sf, np.int32),
+        "obs_value_kind": np.zeros(n, np.int32), "obs_value": np.array(vals, np.float64),
+        "obs_model": np.full(n, OBS_NORMAL, np.int32), "obs_sd": np.array(sds, np.float64),
+        "obs_shape": np.zeros(n), "obs_threshold": np.full(n, UNSET), "obs_factor": np.ones(n),
+        "obs_factor_spline": np.full(n, -1, np.int32), "obs_cell_ptr": np.array(cptr, np.int32),
+        "obs_cells": np.array(cells, np.int32),
+    }
+
+
+def _disc_spline(days: int, S: int, bp: Sequence[float], vals: Sequence[float]) -> np.ndarray:
+    """Model::create_disc_spline (src/model.cc:1018-1041), factor 1, multfac 1."""
+    out = np.zeros(S)
+    p = 0
+    for s in range(S):
+        t = float((s + 0.5) * days) / S
+        while p + 1 < len(bp) and t > bp[p + 1]:
+            p += 1
+        if p + 1 == len(bp):
+            out[s] = out[s - 1]
+        else:
+            fac = (t - bp[p]) / (bp[p + 1] - bp[p])
+            out[s] = 1.0 * (vals[p] * 1.0 * (1 - fac) + vals[p + 1] * 1.0 * fac)
+    return out
+
+
+def age_matrix(w: synth.Workload) -> np.ndarray:
+    """genQ.N[0] after Data::age_mixing_matrix + agematrix_normalise."""
+    G = w.nage
+    if G == 1:
+        return np.ones((1, 1))
+    pop = np.asarray(w.pop, np.int64)
+    popa = pop.sum(0)                     # unsigned accumulation per age
+    poptot = float(pop.sum())
+    m = np.array(w.age_mix, np.float64)
+    for j in range(G):
+        for i in range(G):
+            m[j, i] = m[j, i] / (float(popa[j]) / poptot)
+    sym = np.empty_like(m)
+    for j in range(G):
+        for i in range(G):
+            sym[j, i] = 0.5 * (m[j, i] + m[i, j])
+    s = 0.0
+    s2 = 0.0
+    for a in range(G):
+        for aa in range(G):
+            s += float(popa[aa]) * sym[aa, a]
+            s2 += float(popa[aa])
+    s /= s2
+    return sym / s
+
+
+def param_tables(w: synth.Workload, sigma_inv: Optional[float] = None, gamma_inv: Optional[float] = None,
+                 R_scale: float = 1.0, h_mean: Optional[float] = None) -> Dict[str, np.ndarray]:
+    """set_param tables for one parameter set (defaults: the workload's true values).
+
+    ``R_scale`` multiplies every knot of R(t) (an R0 proposal)."""
+    A, G = w.narea, w.nage
+    DP, C, T, S = G, len(COMPS), len(TRANS), w.ndivision
+    si = w.sigma_inv if sigma_inv is None else sigma_inv
+    gi = w.gamma_inv if gamma_inv is None else gamma_inv
+    hm = w.h_mean if h_mean is None else h_mean
+    transrate = np.zeros((T, DP))
+    transrate[1, :] = 1.0 / si
+    transrate[2, :] = (1.0 / gi) * w.p_H
+    transrate[3, :] = (1.0 / gi) * (1 - w.p_H)
+    transrate[4, :] = (1.0 / hm) * w.p_D
+    transrate[5, :] = (1.0 / hm) * (1 - w.p_D)
+    sus = np.ones(DP)
+    inf = np.zeros(C)
+    inf[2] = 1.0
+    N0 = age_matrix(w)
+    Ntime = np.repeat(N0[None], S, axis=0)
+    for mm in w.matmod:
+        f = _disc_spline(w.days, S, mm["bp"], mm["val"])
+        for s in range(S):
+            for a in mm["ages"]:
+                Ntime[s, a, :] *= f[s]
+                Ntime[s, :, a] *= f[s]
+    Rv = [v * R_scale for v in w.R_val]
+    Rspl = _disc_spline(w.days, S, w.R_bp, Rv)
+    # NGM over infectious states E, I (Model::calculate_Vinv / calculate_F / calculate_NGM)
+    Q = DP
+    V = np.zeros((2 * Q, 2 * Q))
+    for dp in range(Q):
+        V[dp, dp] += transrate[1, dp]
+        V[Q + dp, dp] -= transrate[1, dp]
+        V[Q + dp, Q + dp] += transrate[2, dp]
+        V[Q + dp, Q + dp] += transrate[3, dp]
+    Vinv = np.linalg.inv(V)
+    pop = np.asarray(w.pop, np.float64)
+    dist = pop.sum(0) / pop.sum()
+    beta = np.zeros(S)
+    ratio = None
+    for s in range(S):
+        if s == 0 or not np.array_equal(Ntime[s - 1], Ntime[s]):
+            F = np.zeros((Q, 2 * Q))
+            for dp in range(Q):
+                for q in range(Q):
+                    F[q, Q + dp] += dist[q] * sus[q] * 1.0 * Ntime[s][q, dp]
+            NGM = F @ Vinv[:, :Q]
+            ratio = float(np.max(np.linalg.eigvals(NGM).real))
+        beta[s] = 1.0 * Rspl[s] / ratio
+    # area factors: covariates (linear) normalised by the population-weighted mean
+    af = np.ones((w.days, A))
+    if w.covar is not None:
+        for j in range(w.covar.shape[0]):
+            for c in range(A):
+                af[:, c] *= np.exp(w.covar_effect[j] * w.covar[j, c])
+        tp = np.asarray(w.pop, np.int64).sum(1)
+        area_av = 0.0
+        for c in range(A):
+            av = _seq_sum(af[:, c]) / w.days
+            area_av += av * float(tp[c])
+        area_av /= float(tp.sum())
+        af = af / area_av
+    return {
+        "transrate": transrate, "susceptibility": sus, "infectivity": inf,
+        "beta_rows": beta[None, :], "beta_row_of": np.zeros((1, A), np.int32),
+        "areafactor": af, "Ntime": Ntime, "geo_spline": np.ones(S),
+        "efoi_spline": np.full((1, S), float(w.efoi)), "efoi_agedist": np.ones((1, G)),
+        "efoi_ref": np.zeros((1, A), np.int32), "obs_spline": np.zeros((0, S)),
+    }
+
+
+def param_tables_batch(w: synth.Workload, R0, sigma_inv, gamma_inv) -> List[Dict[str, np.ndarray]]:
+    """set_param tables for many parameter sets that differ only in R0 (a
+    constant R(t)), 1/sigma and 1/gamma.  Tables that do not depend on these
+    are the same numpy arrays in every set (so the C ABI shares them)."""
+    base = param_tables(w)
+    n = len(R0)
+    S, DP = w.ndivision, w.nage
+    out = []
+    N0 = base["Ntime"][0]
+    pop = np.asarray(w.pop, np.float64)
+    dist = pop.sum(0) / pop.sum()
+    # NGM = diag(dist) N0 * v with v = Vinv[I,E] = 1/(gamma p_H + gamma (1-p_H)) for every age
+    lam0 = float(np.max(np.linalg.eigvals(dist[:, None] * N0).real))
+    for k in range(n):
+        g = 1.0 / gamma_inv[k]
+        tr = base["transrate"].copy()
+        tr[1, :] = 1.0 / sigma_inv[k]
+        tr[2, :] = g * w.p_H
+        tr[3, :] = g * (1 - w.p_H)
+        v = 1.0 / (tr[2, 0] + tr[3, 0])
+        beta = np.full((1, S), float(R0[k]) / (v * lam0))
+        t = dict(base)
+        t["transrate"] = tr
+        t["beta_rows"] = beta
+        out.append(t)
+    return out
+
+
+def observed_from_trajectory(arr: Dict[str, np.ndarray], transnum: np.ndarray, pop_traj: np.ndarray,
+                             rng) -> Tuple[np.ndarray, np.ndarray]:
+    """Observed values = the trajectory's sums over each observation's cells and
+    steps plus normal noise of variance max(count, 5); SD column sqrt(max(y, 5))."""
+    S = transnum.shape[0]
+    tn = transnum.reshape(S, -1).astype(np.int64)
+    pp = pop_traj.reshape(S, -1).astype(np.int64)
+    ctn = np.vstack([np.zeros((1, tn.shape[1]), np.int64), np.cumsum(tn, 0)])
+    cpp = np.vstack([np.zeros((1, pp.shape[1]), np.int64), np.cumsum(pp, 0)])
+    ptr = arr["obs_cell_ptr"]
+    cells = arr["obs_cells"]
+    si, sf = arr["obs_sett_i"], arr["obs_sett_f"]
+    nobs = len(si)
+    oid = np.repeat(np.arange(nobs), np.diff(ptr))
+    vals = np.zeros(nobs, np.int64)
+    tmask = cells >= 0
+    tc = cells[tmask]
+    to = oid[tmask]
+    np.add.at(vals, to, ctn[sf[to], tc] - ctn[si[to], tc])
+    pc = -1 - cells[~tmask]
+    po = oid[~tmask]
+    np.add.at(vals, po, cpp[sf[po], pc] - cpp[si[po], pc])
+    v = vals.astype(np.float64)
+    noisy = np.maximum(0, np.round(v + rng.normal(0.0, 1.0, nobs) * np.sqrt(np.maximum(v, 5.0))))
+    return noisy, np.sqrt(np.maximum(noisy, 5.0))

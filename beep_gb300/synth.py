@@ -246,3 +246,27 @@ def data_tables(w: Workload) -> List[dict]:
     else:
         raise ValueError(w.obs_kind)
     return tabs
+
+
+def abc_smc_large(seed: int = 20260001, narea: int = 150, nage: int = 4, days: int = 180,
+                  steps_per_day: int = 2, name: str = "c1") -> Workload:
+    """Batched ABC-SMC workload: 150 areas x 4 ages, dt 0.5, 180 days; area
+    populations log-normal(12, 0.8) rounded; constant R0 (a per-particle
+    parameter); daily E->I observations per area and age."""
+    rng = np.random.default_rng(seed)
+    totals = np.maximum(np.rint(rng.lognormal(12.0, 0.8, narea)).astype(np.int64), 100)
+    pop = np.stack([_split_pop(rng, int(t), nage) for t in totals])
+    am = rng.uniform(0.5, 2.0, (nage, nage))
+    am = np.triu(am) + np.triu(am, 1).T
+    am[np.diag_indices(nage)] *= 3.0
+    geo = _gravity(rng, narea, 0.2)
+    seedE = np.zeros((narea, nage), np.int64)
+    seedE[0, nage // 2] = max(1, rng.poisson(10))
+    return Workload(name=name, seed=seed, narea=narea, nage=nage, days=days, steps_per_day=steps_per_day,
+                    pop=pop, age_mix=am, geo=geo, seed_E=seedE, R_bp=[0, days], R_val=[2.5, 2.5],
+                    obs_kind="cases_age", R_prior=(1.5, 4.0))
+
+
+def abc_smc_priors(rng, n: int):
+    """Per-particle parameters from the ABC-SMC priors: R0 U(1.5,4), 1/sigma U(2,6), 1/gamma U(3,8)."""
+    return rng.uniform(1.5, 4.0, n), rng.uniform(2.0, 6.0, n), rng.uniform(3.0, 8.0, n)

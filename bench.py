@@ -1,0 +1,317 @@
+"""Benchmark of the tau-leap simulation + observation log-likelihood.
+
+Workload (default ``abc_smc``): one ABC-SMC generation -- 16384 particles, each
+with its own parameters drawn from the priors (R0 U(1.5,4), 1/sigma U(2,6),
+1/gamma U(3,8)), over 150 areas x 4 age groups, dt 0.5 day, 180 days (360
+steps), SEIR-H-D, daily cases per area and age (108,000 observations).  A
+step is one full simulation + log-likelihood of every particle.
+
+  value : particle.area.group.steps/s with the inputs already on the device
+          (CUDA events on the model's stream around the kernel launches);
+  e2e   : the same through the C ABI from host buffers: re-staging the
+          parameter tables into pinned memory, host->device copy, kernels,
+          device->host copy of the log-likelihoods, every step.
+
+``--impl reference`` times the reference's CPU algorithm for the same
+workload on this host's cores (the oracle restatement, all threads, a bounded
+sample of particles per step).
+
+usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_UNIT = 72          # int32 state in (6x4 B) + out (6x4 B) + transition counts out (6x4 B)
+METRIC = "particle.area.group.steps/s"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during a timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int = 0):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_workload(P: int, seed: int):
+    """Model + per-particle parameter tables of the ABC-SMC workload.  The
+    observed data are one simulation at the true parameters (made with the
+    library itself) plus noise."""
+    from beep_gb300 import capi, model_builder as mb, synth
+    w = synth.abc_smc_large()
+    arr0 = mb.model_arrays(w)
+    m0 = capi.Model(arr0)
+    t_true = capi.Tables(mb.param_tables(w))
+    dm0 = capi.DeviceModel(m0)
+    truth = dm0.simulate(capi.Batch(m0, [t_true], 1, seed ^ 0x5EED, want_transnum=True, want_pop_traj=True,
+                                    want_L=False))
+    dm0.close()
+    rng = np.random.default_rng(seed)
+    y, sd = mb.observed_from_trajectory(arr0, truth.transnum[0], truth.pop_traj[0], rng)
+    arr = dict(arr0)
+    arr["obs_value"], arr["obs_sd"] = y, sd
+    m = capi.Model(arr)
+    R0, si, gi = synth.abc_smc_priors(rng, P)
+    tabs = [capi.Tables(t) for t in mb.param_tables_batch(w, R0, si, gi)]
+    return w, m, tabs
+
+
+def cpu_throughput(m, tabs, seed, target_s: float, nthreads: int, max_particles: int):
+    """Oracle restatement on this host: units/s over a bounded particle sample."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from beep_gb300 import capi
+    from oracle_lib import oracle_simulate
+    units_per_particle = m.narea * m.nage * m.ndivision
+    n = max(1, nthreads)
+    t0 = time.perf_counter()
+    oracle_simulate(m, capi.Batch(m, tabs[:n], n, seed, group_of=np.arange(n)), nthreads)
+    dt = time.perf_counter() - t0
+    n2 = int(min(max_particles, max(n, n * target_s / max(dt, 1e-3))))
+    n2 = max(n, (n2 // n) * n)
+    t0 = time.perf_counter()
+    oracle_simulate(m, capi.Batch(m, tabs[:n2], n2, seed, group_of=np.arange(n2)), nthreads)
+    dt = time.perf_counter() - t0
+    return units_per_particle * n2 / dt, n2, dt
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return rank, ws, dist
+    return 0, 1, None
+
+
+def run_reference(args, rank, ws, dist):
+    if rank != 0:
+        return
+    from beep_gb300 import capi  # noqa: F401
+    nthreads = os.cpu_count() or 1
+    P = 16384
+    w, m, tabs = build_workload_cpu(P, args.seed)
+    upp = m.narea * m.nage * m.ndivision
+    # per step a bounded sample sized for a few seconds of work
+    _, n2, dt = cpu_throughput(m, tabs, args.seed, 3.0, nthreads, P)
+    times = []
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_lib import oracle_simulate
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        oracle_simulate(m, capi.Batch(m, tabs[:n2], n2, args.seed + k, group_of=np.arange(n2)), nthreads)
+        if k >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    t = statistics.mean(times)
+    value = upp * n2 / t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "particle.area.group.steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(m, P, note=f"sample of {n2} particles per step"),
+        "loglik_evals_per_s": n2 / t,
+        "cpu_baseline": {"value": value, "unit": "particle.area.group.steps/s", "cores": nthreads, "kind": "port",
+                         "sample": f"{n2} of {P} particles per step, full 360-step horizon + log-likelihood"},
+        "e2e": {"value": value, "unit": "particle.area.group.steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def build_workload_cpu(P, seed):
+    """The same workload without a GPU: the observed data come from the oracle
+    (only used by the reference arm, which runs the oracle anyway)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from beep_gb300 import capi, model_builder as mb, synth
+    from oracle_lib import oracle_simulate
+    w = synth.abc_smc_large()
+    arr0 = mb.model_arrays(w)
+    m0 = capi.Model(arr0)
+    t_true = capi.Tables(mb.param_tables(w))
+    truth = oracle_simulate(m0, capi.Batch(m0, [t_true], 1, seed ^ 0x5EED, want_transnum=True, want_pop_traj=True,
+                                           want_L=False))
+    rng = np.random.default_rng(seed)
+    y, sd = mb.observed_from_trajectory(arr0, truth.transnum[0], truth.pop_traj[0], rng)
+    arr = dict(arr0)
+    arr["obs_value"], arr["obs_sd"] = y, sd
+    m = capi.Model(arr)
+    R0, si, gi = synth.abc_smc_priors(rng, P)
+    tabs = [capi.Tables(t) for t in mb.param_tables_batch(w, R0, si, gi)]
+    return w, m, tabs
+
+
+def workload_config(m, P, note=None):
+    c = {"workload": "abc_smc_generation_150x4", "particles": P, "areas": m.narea, "ages": m.nage,
+         "steps": m.ndivision, "dt_days": m.dt, "observations": m.nobs, "model": "SEIR-H-D",
+         "l2": "working set larger than L2 (per-particle state and observation sums, GB scale)"}
+    if note:
+        c["note"] = note
+    return c
+
+
+def run_ours(args, rank, ws, dist):
+    from beep_gb300 import build as bbuild, capi
+    bbuild.build()
+    P = args.particles
+    seed = args.seed + 7919 * rank
+    w, m, tabs = build_workload(P, seed)
+    dm = capi.DeviceModel(m, device=int(os.environ.get("LOCAL_RANK", "0")) if ws > 1 else 0)
+    batch = capi.Batch(m, tabs, P, seed, group_of=np.arange(P), stream_of=np.arange(P) + rank * P)
+    db = capi.DeviceBatch(dm, batch)
+    h2d, d2h = db.bytes()
+    db.upload()
+    units = P * m.narea * m.nage * m.ndivision
+    # warm-up
+    db.time(args.warmup)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    # device-resident timing
+    barrier()
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as cs:
+        ms = db.time(args.steps)
+    clocks = cs.summary()
+    t_dev = ms / 1e3
+    # end-to-end timing through host buffers
+    barrier()
+    e2e_times = []
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        db.stage()
+        db.upload()
+        db.launch()
+        db.download()
+        e2e_times.append(time.perf_counter() - t0)
+    t_e2e = statistics.mean(e2e_times)
+    if dist is not None:
+        import torch
+        tt = torch.tensor([t_dev, t_e2e], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_dev, t_e2e = float(tt[0]), float(tt[1])
+    assert np.all(np.isfinite(batch.L))
+    if rank != 0:
+        return
+    hbm, hbm_kind = peaks()
+    achieved = BYTES_PER_UNIT * units / t_dev / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        traffic = json.load(open(tp)).get("sim_plain_kernel")
+    cpu = None
+    if not args.no_cpu:
+        nthreads = os.cpu_count() or 1
+        v, n2, dt = cpu_throughput(m, tabs, seed, args.cpu_seconds, nthreads, P)
+        cpu = {"value": v, "unit": "particle.area.group.steps/s", "cores": nthreads, "kind": "port",
+               "sample": f"{n2} of {P} particles (full 360-step horizon + log-likelihood), {dt:.1f} s"}
+    line = {
+        "metric": METRIC, "value": units * ws / t_dev, "unit": "particle.area.group.steps/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_dev * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(m, P),
+        "form": "plain_fp64",
+        "loglik_evals_per_s": P * ws / t_dev,
+        "clocks": clocks,
+        "e2e": {"value": units * ws / t_e2e, "unit": "particle.area.group.steps/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e * 1e3},
+        "gpu_launches": args.steps * db.launches(),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_kind": hbm_kind, "traffic": traffic,
+                     "algorithmic_bytes": f"{BYTES_PER_UNIT} B x {units} units per launch"},
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+    db.close()
+    dm.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--particles", type=int, default=16384)
+    ap.add_argument("--seed", type=int, default=20260001)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank, ws, dist = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, rank, ws, dist)
+    else:
+        run_ours(args, rank, ws, dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -32,6 +32,12 @@ extern "C" {
 
 #define BEEP_GPU_ABI_VERSION 1
 
+#if defined(__GNUC__)
+#define BEEP_API __attribute__((visibility("default")))
+#else
+#define BEEP_API
+#endif
+
 typedef enum beep_status {
 	BEEP_OK = 0,
 	BEEP_BAD_INPUT = 1,      /* inconsistent sizes, indices out of range, NULL where required */
@@ -156,18 +162,40 @@ typedef struct beep_sim_batch {
 typedef struct beep_model beep_model;    /* device-resident model + work buffers */
 
 /* Library and device. */
-int32_t beep_abi_version(void);
-const char *beep_last_error(void);
-beep_status beep_device_init(int32_t device);
+BEEP_API int32_t beep_abi_version(void);
+BEEP_API const char *beep_last_error(void);
+BEEP_API beep_status beep_device_init(int32_t device);
 
 /* Model lifetime (replaces constructing Data/Model/ObservationModel for the
  * hot path: src/main.cc:148-160). */
-beep_status beep_model_create(const beep_model_desc *desc, beep_model **out);
-beep_status beep_model_destroy(beep_model *model);
+BEEP_API beep_status beep_model_create(const beep_model_desc *desc, beep_model **out);
+BEEP_API beep_status beep_model_destroy(beep_model *model);
 
 /* State::simulate for a batch (src/state.cc:582-638 + src/obsmodel.cc:22-58).
- * Host buffers; host<->device copies happen inside the call. */
-beep_status beep_simulate(beep_model *model, const beep_sim_batch *batch);
+ * Host buffers; host<->device copies happen inside the call.  Equivalent to
+ * beep_batch_create + upload + launch + download + destroy. */
+BEEP_API beep_status beep_simulate(beep_model *model, const beep_sim_batch *batch);
+
+/* The same call in stages, for callers that keep a batch resident and repeat
+ * it (PMCMC proposals, ABC-SMC generations, serving).  The batch keeps the
+ * caller's beep_sim_batch host pointers: beep_batch_stage re-reads them into
+ * pinned staging memory, beep_batch_upload copies the staging to the device,
+ * beep_batch_launch enqueues the kernels on the model's stream (inputs and
+ * outputs stay on the device), beep_batch_download copies the outputs into
+ * the caller's host arrays and waits.  beep_batch_time runs `iters` launches
+ * between two CUDA events on the model's stream and reports the mean device
+ * time per launch.  Same reference functions as beep_simulate. */
+typedef struct beep_batch beep_batch;
+BEEP_API beep_status beep_batch_create(beep_model *model, const beep_sim_batch *batch, beep_batch **out);
+BEEP_API beep_status beep_batch_stage(beep_batch *batch);
+BEEP_API beep_status beep_batch_upload(beep_batch *batch);
+BEEP_API beep_status beep_batch_launch(beep_batch *batch);
+BEEP_API beep_status beep_batch_download(beep_batch *batch);
+BEEP_API beep_status beep_batch_time(beep_batch *batch, int32_t iters, double *ms_per_launch);
+BEEP_API int32_t beep_batch_launches(const beep_batch *batch);   /* kernels per launch */
+/* bytes moved host->device by beep_batch_upload and device->host by beep_batch_download */
+BEEP_API beep_status beep_batch_bytes(const beep_batch *batch, int64_t *h2d, int64_t *d2h);
+BEEP_API beep_status beep_batch_destroy(beep_batch *batch);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,136 @@
+"""Generates the golden fixtures in this folder from the reference itself.
+
+Needs the reference source tree (default /root/reference) and builds the
+reference oracle with oracle/Makefile.ref.  For each fixture:
+  1. a seeded synthetic workload is written in the reference's TOML/CSV format
+     with placeholder observations;
+  2. the reference (driven by the keyed variate stream) simulates once at the
+     true parameters; the observed values are that trajectory's sums plus
+     normal noise of variance max(count, 5), written back with an SD column;
+  3. the reference runs again and its model, set_param tables, per-particle
+     log-likelihoods, checksums and (for a few particles) full transition and
+     population trajectories are saved as a bundle ``<name>.bnd``.
+
+usage: python tests/golden/make_golden.py [--ref /root/reference]
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from beep_gb300 import bundle, synth  # noqa: E402
+
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+
+
+def run_harness(workdir, toml, out, npart, ntraj, seed, mode, pf=False, theta=None):
+    cmd = [HARNESS, f"out={out}", f"npart={npart}", f"ntraj={ntraj}", f"seed={seed}", f"pf={1 if pf else 0}"]
+    if theta is not None:
+        cmd.append(f"theta={theta}")
+    cmd += ["--", f"inputfile={os.path.basename(toml)}", f"mode={mode}"]
+    r = subprocess.run(cmd, cwd=workdir, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"harness failed:\n{r.stdout}\n{r.stderr}")
+    return bundle.read_bundle(out)
+
+
+def obs_values_from(b, w: synth.Workload):
+    """Per data file and column: (values, sd) from trajectory 0 of bundle b plus noise."""
+    tn = b["g0.transnum"][0].astype(np.int64)     # [S][A][T][DP]
+    pop = b["g0.pop"][0].astype(np.int64)         # [S][A][C][DP]
+    T = tn.shape[2]
+    C = pop.shape[2]
+    DP = tn.shape[3]
+    cells = b["obs_cells"]
+    ptr = b["obs_cell_ptr"]
+    si, sf = b["obs_sett_i"], b["obs_sett_f"]
+    rng = np.random.default_rng(w.seed + 7)
+    vals = []
+    for o in range(len(si)):
+        v = 0
+        for s in range(si[o], sf[o]):
+            for q in range(ptr[o], ptr[o + 1]):
+                cell = int(cells[q])
+                if cell >= 0:
+                    c, rem = divmod(cell, T * DP)
+                    tr, dp = divmod(rem, DP)
+                    v += tn[s, c, tr, dp]
+                else:
+                    k = -1 - cell
+                    c, rem = divmod(k, C * DP)
+                    co, dp = divmod(rem, DP)
+                    v += pop[s, c, co, dp]
+        vals.append(v)
+    vals = np.array(vals, np.float64)
+    sd = np.sqrt(np.maximum(vals, 5.0))
+    noisy = np.maximum(0, np.round(vals + rng.normal(0.0, 1.0, len(vals)) * sd))
+    # observation order = data table -> column -> row (src/data.cc:1119-1320)
+    out = {}
+    k = 0
+    for tab in synth.data_tables(w):
+        out[tab["file"]] = {}
+        nrow = len(tab["times"])
+        for col in tab["columns"]:
+            out[tab["file"]][col] = (noisy[k:k + nrow], np.sqrt(np.maximum(noisy[k:k + nrow], 5.0)))
+            k += nrow
+    assert k == len(vals), (k, len(vals))
+    return out
+
+
+def make_fixture(name, w: synth.Workload, npart, ntraj, seed, pf=False, theta_rows=None, keep_dir=None):
+    work = tempfile.mkdtemp(prefix=f"golden_{name}_")
+    try:
+        toml = synth.write_beep_inputs(w, work)
+        mode = "pmcmc" if pf else "abcsmc"
+        b0 = run_harness(work, toml, os.path.join(work, "b0.bnd"), 1, 1, seed + 1, mode, pf=False)
+        vals = obs_values_from(b0, w)
+        synth.write_beep_inputs(w, work, obs_values=vals)
+        theta = None
+        if theta_rows is not None:
+            theta = os.path.join(work, "theta.csv")
+            with open(theta, "w") as f:
+                for row in theta_rows:
+                    f.write(",".join(repr(float(x)) for x in row) + "\n")
+        out = os.path.join(HERE, f"{name}.bnd")
+        run_harness(work, toml, out, npart, ntraj, seed, mode, pf=pf, theta=theta)
+        if keep_dir:
+            shutil.copytree(work, os.path.join(keep_dir, name), dirs_exist_ok=True)
+        print(f"{name}: {os.path.getsize(out) / 1e3:.0f} kB")
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--keep", default=None, help="keep the generated TOML/CSV inputs here")
+    a = ap.parse_args()
+    subprocess.run(["make", "-s", "-f", "oracle/Makefile.ref", f"REF={a.ref}", "-j8"], cwd=ROOT, check=True)
+
+    # tiny: 4 areas x 3 ages, 40 days at dt 0.25
+    tiny = synth.seir_hd_small(seed=20260100, narea=4, nage=3, days=40, name="tiny")
+    make_fixture("tiny_sim", tiny, npart=8, ntraj=3, seed=0x1234567890ABCDEF)
+    # particle-filter sections need period >= 10 x the largest observation step (src/details.cc:115)
+    tiny70 = synth.seir_hd_small(seed=20260102, narea=3, nage=2, days=70, name="tiny70")
+    make_fixture("tiny_pf", tiny70, npart=6, ntraj=2, seed=0x0F1E2D3C4B5A6978, pf=True)
+    # one age group (the reference's nage == 1 branch of get_NMI, src/state.cc:555-560)
+    one = synth.seir_hd_small(seed=20260101, narea=5, nage=1, days=30, name="oneage")
+    make_fixture("oneage_sim", one, npart=6, ntraj=2, seed=77)
+    # the 10-area x 3-age plain PMCMC workload at full horizon
+    c0 = synth.seir_hd_small(seed=20260000, narea=10, nage=3, days=100, name="c0")
+    make_fixture("c0_sim", c0, npart=16, ntraj=1, seed=20260000)
+    make_fixture("c0_pf", c0, npart=8, ntraj=1, seed=20260001, pf=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,87 @@
+"""CUDA plain FP64 form vs the reference (golden fixtures) and the oracle,
+called through the C ABI (libbeep_gpu.so).  Bar: transition counts and
+populations bit-exact; log-likelihood within 1e-12 relative."""
+import numpy as np
+import pytest
+
+from beep_gb300 import capi
+from golden_util import FIXTURES, PF_FIXTURES, checksums, load
+from oracle_lib import oracle_simulate
+
+pytestmark = pytest.mark.gpu
+L_RTOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def built():
+    from beep_gb300 import build
+    build.build()
+    return capi.lib()
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_full_simulation_matches_reference(built, name):
+    b, m, tabs, seed = load(name)
+    P = int(b["npart"][0])
+    nt = b["g0.transnum"].shape[0]
+    dm = capi.DeviceModel(m)
+    bt = dm.simulate(capi.Batch(m, tabs, P, seed, want_transnum=True, want_pop_traj=True, want_pop=True))
+    assert np.array_equal(bt.transnum[:nt], b["g0.transnum"])
+    assert np.array_equal(bt.pop_traj[:nt], b["g0.pop"])
+    for p in range(P):
+        assert np.array_equal(checksums(bt.transnum[p], bt.pop_traj[p]), b["g0.checksum"][p])
+    np.testing.assert_allclose(bt.L, b["g0.L"], rtol=L_RTOL, atol=0)
+    dm.close()
+
+
+@pytest.mark.parametrize("name", PF_FIXTURES)
+def test_sections_match_reference(built, name):
+    b, m, tabs, seed = load(name)
+    P = int(b["npart"][0])
+    dm = capi.DeviceModel(m)
+    pop = None
+    tns = []
+    for k, (ti, tf) in enumerate(m.sections):
+        bt = dm.simulate(capi.Batch(m, tabs, P, seed, ti=ti, tf=tf, pop_in=pop, want_pop=True, want_transnum=True))
+        np.testing.assert_allclose(bt.L, b["g0.L_section"][:, k], rtol=L_RTOL, atol=1e-12)
+        pop = bt.pop
+        tns.append(bt.transnum)
+    tn = np.concatenate(tns, axis=1)
+    assert np.array_equal(tn[:b["g0.transnum"].shape[0]], b["g0.transnum"])
+    dm.close()
+
+
+def test_many_particles_and_groups_match_oracle(built):
+    """Mixed parameter sets (group_of) and caller-chosen streams over 200
+    particles: identical counts and populations to the oracle."""
+    b, m, tabs, seed = load("c0_sim")
+    t2 = capi.Tables({k: (v * 1.3 if k == "g0.beta_rows" else v) for k, v in b.items()}, "g0.")
+    P = 200
+    rng = np.random.default_rng(5)
+    group_of = rng.integers(0, 2, P)
+    stream_of = rng.permutation(100000)[:P].astype(np.uint32)
+    dm = capi.DeviceModel(m)
+    g = dm.simulate(capi.Batch(m, [tabs[0], t2], P, seed, group_of=group_of, stream_of=stream_of,
+                               want_pop=True, want_transnum=True))
+    o = oracle_simulate(m, capi.Batch(m, [tabs[0], t2], P, seed, group_of=group_of, stream_of=stream_of,
+                                      want_pop=True, want_transnum=True))
+    assert np.array_equal(g.transnum, o.transnum)
+    assert np.array_equal(g.pop, o.pop)
+    np.testing.assert_allclose(g.L, o.L, rtol=L_RTOL, atol=0)
+    dm.close()
+
+
+def test_device_errors_are_statuses(built):
+    b, m, tabs, seed = load("tiny_sim")
+    dm = capi.DeviceModel(m)
+    with pytest.raises(capi.BeepError) as e:
+        dm.simulate(capi.Batch(m, tabs, 4, seed, ti=5, tf=3))
+    assert e.value.status == 1
+    bad = capi.Tables({k: (v * np.nan if k == "g0.beta_rows" else v) for k, v in b.items()}, "g0.")
+    with pytest.raises(capi.BeepError) as e:
+        dm.simulate(capi.Batch(m, [bad], 2, seed))
+    assert e.value.status == 2
+    # the model stays usable after an error
+    ok = dm.simulate(capi.Batch(m, tabs, 2, seed))
+    np.testing.assert_allclose(ok.L, b["g0.L"][:2], rtol=L_RTOL)
+    dm.close()
