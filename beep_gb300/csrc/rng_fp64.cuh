@@ -1,9 +1,13 @@
 // Keyed variate streams for the FP64 plain form.
 //
-// uniforms: Philox4x32-10 (Salmon et al., SC'11); key = 64-bit seed,
-//           counter = {cell, step, stream, (purpose << 24) | iteration};
-//           u = (2k+1) 2^-53 from 52 bits of two words, strictly inside (0,1).
-// Poisson:  mean < 10 sequential inversion; mean >= 10 PTRS (Hoermann 1993).
+// uniforms: Philox4x32-10 (Salmon et al., SC'11); key = 64-bit seed; a word
+//           w gives u = (w + 1/2) 2^-32, strictly inside (0,1).
+// Poisson:  draw of transition tr in column col = c*ndemocatpos + dp at step
+//           sett of stream s:
+//           mean < 10  sequential inversion, u from word tr%4 of
+//                      Philox({col, sett, s, (0<<24) | tr/4});
+//           mean >= 10 PTRS (Hoermann 1993), iteration it takes (U, V) from
+//                      words 0,1 of Philox({col, sett, s, (1<<24)|(tr<<16)|it}).
 // exp/log:  Cody-Waite reduction by ln 2 with a degree-14 Taylor series for
 //           e^r; log(m) = 2 atanh((m-1)/(m+1)) series; log k! exact below 23,
 //           Stirling series above.  Only IEEE +,-,*,/,sqrt are used, and this
@@ -16,9 +20,10 @@
 
 namespace beep {
 
-constexpr uint32_t PURPOSE_TRANS = 0u;
-constexpr uint32_t PURPOSE_THIN = 1u;
-constexpr uint32_t PURPOSE_RESAMPLE = 2u;
+constexpr uint32_t PURPOSE_INV = 0u;
+constexpr uint32_t PURPOSE_PTRS = 1u;
+constexpr uint32_t PURPOSE_THIN = 2u;
+constexpr uint32_t PURPOSE_RESAMPLE = 3u;
 
 struct U4 { uint32_t x, y, z, w; };
 
@@ -35,10 +40,14 @@ __device__ __forceinline__ U4 philox10(U4 c, uint32_t k0, uint32_t k1)
 	return c;
 }
 
-__device__ __forceinline__ double u01_pair(uint32_t a, uint32_t b)
+__device__ __forceinline__ double u01_d(uint32_t w)
 {
-	const uint64_t k = ((uint64_t)(a >> 6) << 26) | (uint64_t)(b >> 6);
-	return (double)(2ull * k + 1ull) * 1.1102230246251565e-16;
+	return (double)w * 2.3283064365386963e-10 + 1.1641532182693481e-10;
+}
+
+__device__ __forceinline__ uint32_t word_of(const U4 &r, uint32_t i)
+{
+	return i == 0 ? r.x : i == 1 ? r.y : i == 2 ? r.z : r.w;
 }
 
 __device__ __forceinline__ double scale2(double x, int k)
@@ -116,14 +125,15 @@ __device__ __forceinline__ double log_factorial_p(double k)
 	return (n - 0.5) * log_p(n) - n + 0.9189385332046728 + corr;
 }
 
-// Poisson(mean) for cell/step/stream; -1 only after 2^24 rejections.
-__device__ __noinline__ int32_t poisson_fp64(double mean, uint32_t k0, uint32_t k1, uint32_t cell,
-                                              uint32_t step, uint32_t stream, uint32_t purpose)
+// Poisson(mean) of transition tr in column col at step sett; -1 after 65536
+// rejections (reported as an error by the caller).
+__device__ __noinline__ int32_t poisson_fp64(double mean, uint32_t k0, uint32_t k1, uint32_t col, uint32_t tr,
+                                              uint32_t sett, uint32_t stream)
 {
 	if (!(mean > 0.0)) return 0;
 	if (mean < 10.0) {
-		const U4 r = philox10(U4{cell, step, stream, purpose << 24}, k0, k1);
-		const double u = u01_pair(r.x, r.y);
+		const U4 r = philox10(U4{col, sett, stream, (PURPOSE_INV << 24) | (tr >> 2)}, k0, k1);
+		const double u = u01_d(word_of(r, tr & 3u));
 		double p = exp_p(-mean);
 		double F = p;
 		int32_t k = 0;
@@ -141,10 +151,10 @@ __device__ __noinline__ int32_t poisson_fp64(double mean, uint32_t k0, uint32_t 
 	const double invalpha = 1.1239 + 1.1328 / (b - 3.4);
 	const double vr = 0.9277 - 3.6224 / (b - 2.0);
 	const double log_invalpha = log_p(invalpha);
-	for (uint32_t it = 0; it < (1u << 24); it++) {
-		const U4 r = philox10(U4{cell, step, stream, (purpose << 24) | it}, k0, k1);
-		const double U = u01_pair(r.x, r.y) - 0.5;
-		const double V = u01_pair(r.z, r.w);
+	for (uint32_t it = 0; it < 65536u; it++) {
+		const U4 r = philox10(U4{col, sett, stream, (PURPOSE_PTRS << 24) | (tr << 16) | it}, k0, k1);
+		const double U = u01_d(r.x) - 0.5;
+		const double V = u01_d(r.y);
 		const double us = 0.5 - fabs(U);
 		const double k = floor((2.0 * a / us + b) * U + mean + 0.43);
 		if (us >= 0.07 && V <= vr) return (int32_t)k;

@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 			else if (mean != 0) {
 				if (mean > 1000000000.0) set_status(status, BEEP_COUNT_OVERFLOW);
 				else {
-					n = poisson_fp64(mean, b.k0, b.k1, (uint32_t)cell, (uint32_t)sett, stream, PURPOSE_TRANS);
+					n = poisson_fp64(mean, b.k0, b.k1, (uint32_t)(c * DP + dp), (uint32_t)tr, (uint32_t)sett, stream);
 					if (n < 0) { set_status(status, BEEP_TIMEOUT); n = 0; }
 				}
 			}

@@ -18,10 +18,10 @@ double beep_oracle_exp(double x) { return beep_exp(x); }
 double beep_oracle_log(double x) { return beep_log(x); }
 double beep_oracle_log_factorial(double k) { return beep_log_factorial(k); }
 
-int32_t beep_oracle_poisson(double mean, uint64_t seed, uint32_t cell, uint32_t step,
-                            uint32_t stream, uint32_t purpose)
+int32_t beep_oracle_poisson(double mean, uint64_t seed, uint32_t col, uint32_t tr, uint32_t step,
+                            uint32_t stream)
 {
-	return beep_poisson_ref(mean, (uint32_t)seed, (uint32_t)(seed >> 32), cell, step, stream, purpose);
+	return beep_poisson_ref(mean, (uint32_t)seed, (uint32_t)(seed >> 32), col, tr, step, stream);
 }
 
 /* ---- log-densities: src/utils.cc:107-170 ------------------------------- */
@@ -311,8 +311,9 @@ static int simulate_particle(const beep_model_desc *m, const beep_sim_batch *b, 
 					if (mean == 0) tn[cell] = 0;
 					else {
 						if (mean > 1000000000.0) return BEEP_COUNT_OVERFLOW;
-						tn[cell] = beep_poisson_ref(mean, k0, k1, (uint32_t)cell, (uint32_t)sett, stream,
-						                            BEEP_PURPOSE_TRANS);
+						tn[cell] = beep_poisson_ref(mean, k0, k1, (uint32_t)(c * DP + dp), (uint32_t)tr,
+						                            (uint32_t)sett, stream);
+						if (tn[cell] < 0) return BEEP_TIMEOUT;
 					}
 				}
 			}

@@ -30,8 +30,8 @@ extern "C" {
 int beep_oracle_simulate(const beep_model_desc *m, const beep_sim_batch *b, int nthreads);
 
 /* One Poisson draw from the keyed stream (exposed for sampler tests). */
-int32_t beep_oracle_poisson(double mean, uint64_t seed, uint32_t cell, uint32_t step,
-                            uint32_t stream, uint32_t purpose);
+int32_t beep_oracle_poisson(double mean, uint64_t seed, uint32_t col, uint32_t tr, uint32_t step,
+                            uint32_t stream);
 
 /* Project exp / log / log-factorial used inside the sampler (for tests). */
 double beep_oracle_exp(double x);

@@ -9,14 +9,19 @@
  * keyed stream instead:
  *
  *   uniforms : Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random
- *              numbers: as easy as 1, 2, 3", SC'11).  key = 64-bit seed,
- *              counter = {cell, step, stream, (purpose << 24) | iteration}.
- *              A pair of 32-bit words gives u = (2k+1) * 2^-53, k a 52-bit
- *              integer, so u lies strictly inside (0, 1).
- *   Poisson  : mean < 10  -> sequential inversion (one uniform);
+ *              numbers: as easy as 1, 2, 3", SC'11).  key = 64-bit seed.
+ *              A 32-bit word w gives u = (w + 1/2) 2^-32, strictly in (0, 1).
+ *   Poisson  : the draw of transition tr in column (area c, dp) at step sett
+ *              of stream s, column index col = c*ndemocatpos + dp:
+ *              mean < 10  -> sequential inversion with the word tr%4 of
+ *                            Philox({col, sett, s, (0<<24) | tr/4}), so one
+ *                            Philox call serves four transitions;
  *              mean >= 10 -> PTRS, transformed rejection with squeeze
- *              (W. Hoermann, "The transformed rejection method for generating
- *              Poisson random variables", Insurance: Math. & Econ. 12, 1993).
+ *                            (W. Hoermann, "The transformed rejection method
+ *                            for generating Poisson random variables",
+ *                            Insurance: Math. & Econ. 12, 1993); iteration it
+ *                            takes (U, V) from words 0, 1 of
+ *                            Philox({col, sett, s, (1<<24) | (tr<<16) | it}).
  *   exp/log  : written here from the mathematics (Cody-Waite reduction by
  *              ln 2 + Taylor series of e^r; log by the atanh series), using
  *              only IEEE-754 +,-,*,/ and sqrt so that the host and the GPU
@@ -29,9 +34,10 @@
 #include <stdint.h>
 #include <string.h>
 
-#define BEEP_PURPOSE_TRANS 0u   /* transition counts of the tau-leap       */
-#define BEEP_PURPOSE_THIN 1u    /* binomial thinning of coupled proposals  */
-#define BEEP_PURPOSE_RESAMPLE 2u/* particle-filter resampling uniforms     */
+#define BEEP_PURPOSE_INV 0u      /* inversion words of transition draws       */
+#define BEEP_PURPOSE_PTRS 1u     /* rejection pairs of transition draws       */
+#define BEEP_PURPOSE_THIN 2u     /* binomial thinning of coupled proposals    */
+#define BEEP_PURPOSE_RESAMPLE 3u /* particle-filter resampling uniforms       */
 
 typedef struct { uint32_t v[4]; } beep_u32x4;
 
@@ -61,10 +67,9 @@ static inline beep_u32x4 beep_philox4x32_10(beep_u32x4 ctr, uint32_t k0, uint32_
 	return ctr;
 }
 
-static inline double beep_u01_from_pair(uint32_t a, uint32_t b)
+static inline double beep_u01(uint32_t w)
 {
-	uint64_t k = ((uint64_t)(a >> 6) << 26) | (uint64_t)(b >> 6);   /* 52 bits */
-	return (double)(2u * k + 1u) * 1.1102230246251565e-16;            /* 2^-53 */
+	return (double)w * 2.3283064365386963e-10 + 1.1641532182693481e-10;   /* (w + 1/2) 2^-32, exact */
 }
 
 /* ---- exp / log / log-factorial written from the mathematics ------------- */
@@ -159,14 +164,15 @@ static inline double beep_log_factorial(double k)
 
 #define BEEP_INV_KMAX 1000
 
-static inline int32_t beep_poisson_ref(double mean, uint32_t k0, uint32_t k1, uint32_t cell,
-                                       uint32_t step, uint32_t stream, uint32_t purpose)
+/* Draw of transition tr of column col (= c*ndemocatpos + dp) at step sett. */
+static inline int32_t beep_poisson_ref(double mean, uint32_t k0, uint32_t k1, uint32_t col,
+                                       uint32_t tr, uint32_t sett, uint32_t stream)
 {
 	if (!(mean > 0.0)) return 0;
 	if (mean < 10.0) {
-		beep_u32x4 c = {{cell, step, stream, purpose << 24}};
+		beep_u32x4 c = {{col, sett, stream, (BEEP_PURPOSE_INV << 24) | (tr >> 2)}};
 		beep_u32x4 r = beep_philox4x32_10(c, k0, k1);
-		double u = beep_u01_from_pair(r.v[0], r.v[1]);
+		double u = beep_u01(r.v[tr & 3u]);
 		double p = beep_exp(-mean);
 		double F = p;
 		int32_t k = 0;
@@ -184,11 +190,11 @@ static inline int32_t beep_poisson_ref(double mean, uint32_t k0, uint32_t k1, ui
 	double invalpha = 1.1239 + 1.1328 / (b - 3.4);
 	double vr = 0.9277 - 3.6224 / (b - 2.0);
 	double log_invalpha = beep_log(invalpha);
-	for (uint32_t it = 0; it < (1u << 24); it++) {
-		beep_u32x4 c = {{cell, step, stream, (purpose << 24) | it}};
+	for (uint32_t it = 0; it < 65536u; it++) {
+		beep_u32x4 c = {{col, sett, stream, (BEEP_PURPOSE_PTRS << 24) | (tr << 16) | it}};
 		beep_u32x4 r = beep_philox4x32_10(c, k0, k1);
-		double U = beep_u01_from_pair(r.v[0], r.v[1]) - 0.5;
-		double V = beep_u01_from_pair(r.v[2], r.v[3]);
+		double U = beep_u01(r.v[0]) - 0.5;
+		double V = beep_u01(r.v[1]);
 		double us = 0.5 - fabs(U);
 		double k = floor((2.0 * a / us + b) * U + mean + 0.43);
 		if (us >= 0.07 && V <= vr) return (int32_t)k;
@@ -197,7 +203,7 @@ static inline int32_t beep_poisson_ref(double mean, uint32_t k0, uint32_t k1, ui
 		double rhs = -mean + k * loglam - beep_log_factorial(k);
 		if (lhs <= rhs) return (int32_t)k;
 	}
-	return -1;   /* unreachable in practice: 2^24 rejections */
+	return -1;   /* 65536 rejections: reported as an error by the callers */
 }
 
 #endif

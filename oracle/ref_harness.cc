@@ -87,8 +87,8 @@ extern "C" int __wrap__Z14poisson_sampled(double lam)
 		        r.sett, r.c, r.tr, r.dp, m, lam);
 		abort();
 	}
-	uint32_t cell = (r.c * r.ntrans + r.tr) * r.ndp + r.dp;
-	int v = beep_poisson_ref(lam, r.k0, r.k1, cell, r.sett, r.stream, BEEP_PURPOSE_TRANS);
+	int v = beep_poisson_ref(lam, r.k0, r.k1, r.c * r.ndp + r.dp, r.tr, r.sett, r.stream);
+	if (v < 0) { fprintf(stderr, "replay: rejection sampler gave up\n"); abort(); }
 	r.ncalls++;
 	r.advance();
 	return v;
