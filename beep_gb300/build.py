@@ -26,6 +26,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = {
     "capi.cu": [],
     "sim_plain.cu": ["--fmad=false"],
+    "sim_fast.cu": [],
 }
 
 

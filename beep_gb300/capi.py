@@ -20,6 +20,7 @@ STATUS = {0: "OK", 1: "BAD_INPUT", 2: "NAN_RATE", 3: "OOM", 4: "TIMEOUT", 5: "DE
           6: "NO_DEVICE", 7: "COUNT_OVERFLOW"}
 
 FORM_PLAIN_FP64 = 0
+FORM_FAST = 1
 
 
 class ModelDesc(C.Structure):

@@ -4,6 +4,8 @@
 
 #include <cstdint>
 
+#include <vector_types.h>
+
 #include "../../include/beep_gpu.h"
 
 namespace beep {
@@ -24,6 +26,11 @@ struct ModelDev {
 	// observations
 	const int32_t *obs_model, *obs_kind, *obs_spline, *obs_cell_ptr, *obs_cells, *obs_sett_i, *obs_sett_f;
 	const double *obs_value, *obs_sd, *obs_shape, *obs_thresh, *obs_factor;
+	// FP32 copies for the fast form
+	const float *Mdense;                 // [A][A] source-major, diagonal zero
+	const float *M_diag_f, *M_factor_f;  // [A]
+	const float *csc_val_f;              // [nnz]
+	const float2 *obs_np;                // [nobs] normal models: (-0.5 log(2 pi sd^2), 1/(2 sd^2))
 };
 
 // One parameter set's tables: offsets into the batch's table pool (doubles /
@@ -39,6 +46,7 @@ struct BatchDev {
 	uint32_t k0, k1;
 	const GroupDir *dirs;               // [ngroup]
 	const double *fpool;
+	const float *fpool32;               // FP32 copy of fpool (fast form)
 	const int32_t *ipool;
 	const int32_t *group_of;            // [P] or null
 	const uint32_t *stream_of;          // [P] or null
@@ -48,6 +56,11 @@ struct BatchDev {
 	const int32_t *scored;              // [nscored] ascending obs index
 	const int32_t *step_ptr;            // [tf-ti+1]
 	const int32_t *step_obs;            // scored-position of obs active at each step
+	// fast form: observation accumulator slots and completion lists
+	int32_t nslots, m_in_smem;
+	const int32_t *slot_of;             // [nscored] slot of each scored observation
+	const int32_t *end_ptr;             // [tf-ti+1]
+	const int32_t *end_pos;             // scored-positions completing at each step
 	// per-particle work (device)
 	int32_t *pop_a, *pop_b;             // [P][A][C][DP]
 	int32_t *tn;                        // [P][A][T][DP] current step's counts (when not writing a trajectory)
@@ -61,7 +74,10 @@ struct BatchDev {
 	int32_t *status;                    // [P] beep_status per particle
 };
 
-// launchers (sim_plain.cu)
-int launch_sim_plain(const ModelDev &m, const BatchDev &b, void *stream);
+// launchers
+int launch_sim_plain(const ModelDev &m, const BatchDev &b, void *stream);   // sim_plain.cu
+int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream);    // sim_fast.cu
+size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem);
+int fast_threads();
 
 }  // namespace beep

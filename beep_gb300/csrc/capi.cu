@@ -209,6 +209,22 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 			}
 	}
 
+	// FP32 copies for the fast form: dense source-major mixing matrix (diagonal
+	// kept separately), the transpose's values, and per-observation constants
+	// of the normal log-density
+	std::vector<float> Mdense((size_t)A * A, 0.f), Mdiag_f(A), Mfac_f(A), csc_val_f(nnz);
+	for (int c = 0; c < A; c++) {
+		Mdiag_f[c] = (float)d->M_diag[c];
+		Mfac_f[c] = (float)d->M_factor[c];
+		for (int j = d->M_rowptr[c]; j < d->M_rowptr[c + 1]; j++) Mdense[(size_t)c * A + d->M_to[j]] += (float)d->M_val[j];
+	}
+	for (int j = 0; j < nnz; j++) csc_val_f[j] = (float)csc_val[j];
+	std::vector<float2> obs_np(nobs > 0 ? nobs : 1);
+	for (int o = 0; o < nobs; o++) {
+		const double var = d->obs_sd[o] * d->obs_sd[o];
+		obs_np[o] = make_float2((float)(-0.5 * std::log(2 * 3.14159265358979323846 * var)), (float)(1.0 / (2 * var)));
+	}
+
 	beep_model *m = new beep_model();
 	m->A = A; m->G = G; m->DP = DP; m->NS = NS; m->C = C; m->T = T; m->S = S;
 	m->period = d->period; m->dpt = d->division_per_time; m->nobs = nobs;
@@ -226,7 +242,8 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	       o_os = L.add(4 * (size_t)nobs), o_ocp = L.add(4 * (size_t)(nobs + 1)), o_oc = L.add(4 * (size_t)ncells),
 	       o_osi = L.add(4 * (size_t)nobs), o_osf = L.add(4 * (size_t)nobs), o_ov = L.add(8 * (size_t)nobs),
 	       o_osd = L.add(8 * (size_t)nobs), o_osh = L.add(8 * (size_t)nobs), o_oth = L.add(8 * (size_t)nobs),
-	       o_ofa = L.add(8 * (size_t)nobs);
+	       o_ofa = L.add(8 * (size_t)nobs), o_md = L.add(4 * (size_t)A * A), o_mdg = L.add(4 * (size_t)A),
+	       o_mfc = L.add(4 * (size_t)A), o_cvf = L.add(4 * (size_t)nnz), o_onp = L.add(8 * (size_t)nobs);
 	std::vector<char> host(L.size);
 	auto put = [&](size_t off, const void *src, size_t n) { if (n) memcpy(host.data() + off, src, n); };
 	put(o_tf, d->trans_from, 4 * T); put(o_tt, d->trans_to, 4 * T); put(o_age, d->democatpos_age, 4 * DPS);
@@ -241,6 +258,9 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 		put(o_osd, d->obs_sd, 8 * (size_t)nobs); put(o_osh, d->obs_shape, 8 * (size_t)nobs);
 		put(o_oth, d->obs_threshold, 8 * (size_t)nobs); put(o_ofa, d->obs_factor, 8 * (size_t)nobs);
 	}
+	put(o_md, Mdense.data(), 4 * (size_t)A * A); put(o_mdg, Mdiag_f.data(), 4 * (size_t)A);
+	put(o_mfc, Mfac_f.data(), 4 * (size_t)A); put(o_cvf, csc_val_f.data(), 4 * (size_t)nnz);
+	if (nobs > 0) put(o_onp, obs_np.data(), 8 * (size_t)nobs);
 	cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
 	if (e == cudaSuccess) e = m->model_mem.reserve(L.size);
 	if (e == cudaSuccess) e = cudaMemcpy(m->model_mem.ptr, host.data(), L.size, cudaMemcpyHostToDevice);
@@ -264,6 +284,9 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	md.obs_sett_f = (const int32_t *)(base + o_osf); md.obs_value = (const double *)(base + o_ov);
 	md.obs_sd = (const double *)(base + o_osd); md.obs_shape = (const double *)(base + o_osh);
 	md.obs_thresh = (const double *)(base + o_oth); md.obs_factor = (const double *)(base + o_ofa);
+	md.Mdense = (const float *)(base + o_md); md.M_diag_f = (const float *)(base + o_mdg);
+	md.M_factor_f = (const float *)(base + o_mfc); md.csc_val_f = (const float *)(base + o_cvf);
+	md.obs_np = (const float2 *)(base + o_onp);
 	*out = m;
 	return BEEP_OK;
 }
@@ -359,7 +382,7 @@ struct beep_batch {
 	size_t in_size = 0, out_size = 0;
 	size_t o_f = 0, u_st = 0, u_L = 0, u_po = 0, u_tn = 0, u_pt = 0;
 	std::vector<GroupDir> dirs;
-	std::vector<int32_t> scored, step_ptr, step_obs;
+	std::vector<int32_t> scored, step_ptr, step_obs, slot_of, end_ptr, end_pos;
 	BatchDev bd{};
 	cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 	bool pending = false;
@@ -373,7 +396,7 @@ beep_status check_batch(const beep_model *m, const beep_sim_batch *b)
 	if (P <= 0 || b->ngroup <= 0 || !b->groups) return fail(BEEP_BAD_INPUT, "nparticle/ngroup/groups");
 	if (b->ti < 0 || b->tf <= b->ti || b->tf > m->S) return fail(BEEP_BAD_INPUT, "step range must satisfy 0 <= ti < tf <= ndivision");
 	if (b->ti > 0 && !b->pop_in) return fail(BEEP_BAD_INPUT, "pop_in is required when ti > 0");
-	if (b->form != BEEP_FORM_PLAIN_FP64) return fail(BEEP_BAD_INPUT, "unknown form");
+	if (b->form != BEEP_FORM_PLAIN_FP64 && b->form != BEEP_FORM_FAST) return fail(BEEP_BAD_INPUT, "unknown form");
 	if (b->group_of)
 		for (int p = 0; p < P; p++)
 			if (b->group_of[p] < 0 || b->group_of[p] >= b->ngroup) return fail(BEEP_BAD_INPUT, "group_of out of range");
@@ -390,12 +413,15 @@ beep_status stage_inputs(beep_batch *q)
 	TablePacker pk;
 	beep_status st = pack_tables(m, b, pk, q->dirs);
 	if (st != BEEP_OK) return st;
+	const bool fast = b->form == BEEP_FORM_FAST;
 	Layout in;
 	size_t o_dirs = in.add(sizeof(GroupDir) * q->dirs.size()), o_f = in.add(8 * pk.f.size()),
+	       o_f32 = in.add(fast ? 4 * pk.f.size() : 0),
 	       o_i = in.add(4 * pk.i.size()), o_go = in.add(b->group_of ? 4 * (size_t)P : 0),
 	       o_so = in.add(b->stream_of ? 4 * (size_t)P : 0), o_pin = in.add(b->ti > 0 ? 4 * popsz * P : 0),
 	       o_sc = in.add(4 * q->scored.size()), o_sp = in.add(4 * q->step_ptr.size()),
-	       o_sobs = in.add(4 * q->step_obs.size());
+	       o_sobs = in.add(4 * q->step_obs.size()), o_slot = in.add(4 * q->slot_of.size()),
+	       o_ep = in.add(4 * q->end_ptr.size()), o_epos = in.add(4 * q->end_pos.size());
 	CUDA_TRY(q->in_host.reserve(in.size));
 	CUDA_TRY(q->in_dev.reserve(in.size));
 	q->in_size = in.size;
@@ -409,12 +435,19 @@ beep_status stage_inputs(beep_batch *q)
 	if (!q->scored.empty()) memcpy(h + o_sc, q->scored.data(), 4 * q->scored.size());
 	memcpy(h + o_sp, q->step_ptr.data(), 4 * q->step_ptr.size());
 	if (!q->step_obs.empty()) memcpy(h + o_sobs, q->step_obs.data(), 4 * q->step_obs.size());
+	if (!q->slot_of.empty()) memcpy(h + o_slot, q->slot_of.data(), 4 * q->slot_of.size());
+	if (!q->end_ptr.empty()) memcpy(h + o_ep, q->end_ptr.data(), 4 * q->end_ptr.size());
+	if (!q->end_pos.empty()) memcpy(h + o_epos, q->end_pos.data(), 4 * q->end_pos.size());
 	// infectivity difference of each transition, Model::get_infectivity_dif (src/model.cc:820-823)
 	double *fpool = (double *)(h + o_f);
 	for (int g = 0; g < b->ngroup; g++) {
 		const double *inf = b->groups[g].infectivity;
 		for (int tr = 0; tr < m->T; tr++)
 			fpool[q->dirs[g].infdif + tr] = inf[m->trans_to_h[tr]] - inf[m->trans_from_h[tr]];
+	}
+	if (fast) {
+		float *f32 = (float *)(h + o_f32);
+		for (size_t k = 0; k < pk.f.size(); k++) f32[k] = (float)fpool[k];
 	}
 	char *di = (char *)q->in_dev.ptr;
 	BatchDev &bd = q->bd;
@@ -427,6 +460,10 @@ beep_status stage_inputs(beep_batch *q)
 	bd.scored = (const int32_t *)(di + o_sc);
 	bd.step_ptr = (const int32_t *)(di + o_sp);
 	bd.step_obs = (const int32_t *)(di + o_sobs);
+	bd.fpool32 = fast ? (const float *)(di + o_f32) : nullptr;
+	bd.slot_of = (const int32_t *)(di + o_slot);
+	bd.end_ptr = (const int32_t *)(di + o_ep);
+	bd.end_pos = (const int32_t *)(di + o_epos);
 	return BEEP_OK;
 }
 
@@ -466,14 +503,56 @@ beep_status beep_batch_create(beep_model *m, const beep_sim_batch *b, beep_batch
 		}
 	}
 	const int nscored = (int)q->scored.size();
+	if (b->form == BEEP_FORM_FAST) {
+		// accumulator slots: observations whose windows do not overlap share a
+		// slot (greedy interval colouring in window-start order)
+		q->slot_of.assign(nscored, -1);
+		std::vector<int32_t> order(nscored);
+		for (int k = 0; k < nscored; k++) order[k] = k;
+		std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+			return m->obs_sett_i[q->scored[x]] < m->obs_sett_i[q->scored[y]];
+		});
+		std::vector<std::pair<int32_t, int32_t>> busy;   // (sett_f, slot) min-heap
+		std::vector<int32_t> freeslots;
+		int32_t nslots = 0;
+		auto cmp = [](const std::pair<int32_t, int32_t> &x, const std::pair<int32_t, int32_t> &y) { return x.first > y.first; };
+		for (int k : order) {
+			const int o = q->scored[k];
+			while (!busy.empty() && busy.front().first <= m->obs_sett_i[o]) {
+				freeslots.push_back(busy.front().second);
+				std::pop_heap(busy.begin(), busy.end(), cmp);
+				busy.pop_back();
+			}
+			int32_t sl;
+			if (!freeslots.empty()) { sl = freeslots.back(); freeslots.pop_back(); }
+			else sl = nslots++;
+			q->slot_of[k] = sl;
+			busy.push_back({m->obs_sett_f[o], sl});
+			std::push_heap(busy.begin(), busy.end(), cmp);
+		}
+		q->bd.nslots = nslots;
+		q->end_ptr.assign(nsteps + 1, 0);
+		for (int k = 0; k < nscored; k++) q->end_ptr[m->obs_sett_f[q->scored[k]] - 1 - b->ti + 1]++;
+		for (int s2 = 0; s2 < nsteps; s2++) q->end_ptr[s2 + 1] += q->end_ptr[s2];
+		q->end_pos.resize(nscored);
+		std::vector<int32_t> fill(q->end_ptr.begin(), q->end_ptr.end() - 1);
+		for (int k = 0; k < nscored; k++) q->end_pos[fill[m->obs_sett_f[q->scored[k]] - 1 - b->ti]++] = k;
+		const size_t limit = 227 * 1024;
+		if (fast_smem_bytes(m->dev, nslots, false) > limit) {
+			delete q;
+			return fail(BEEP_BAD_INPUT, "model too large for the particle-resident fast form (shared memory)");
+		}
+		q->bd.m_in_smem = fast_smem_bytes(m->dev, nslots, true) <= limit ? 1 : 0;
+	}
 	auto bail = [&](beep_status s) { beep_batch_destroy(q); return s; };
 	st = stage_inputs(q);
 	if (st != BEEP_OK) return bail(st);
 
 	Layout wk;
-	size_t w_pa = wk.add(4 * popsz * P), w_pb = wk.add(4 * popsz * P), w_tn = wk.add(b->transnum_out ? 0 : 4 * tnsz * P),
-	       w_im = wk.add(8 * agsz * P), w_id = wk.add(8 * agsz * P), w_di = wk.add(8 * agsz * P),
-	       w_nmi = wk.add(8 * agsz * P), w_acc = wk.add(8 * (size_t)nscored * P);
+	const size_t PW = b->form == BEEP_FORM_FAST ? 0 : (size_t)P;   // the fast form keeps its state on chip
+	size_t w_pa = wk.add(4 * popsz * PW), w_pb = wk.add(4 * popsz * PW), w_tn = wk.add(b->transnum_out ? 0 : 4 * tnsz * PW),
+	       w_im = wk.add(8 * agsz * PW), w_id = wk.add(8 * agsz * PW), w_di = wk.add(8 * agsz * PW),
+	       w_nmi = wk.add(8 * agsz * PW), w_acc = wk.add(8 * (size_t)nscored * PW);
 	Layout ou;
 	q->u_st = ou.add(4 * (size_t)P);
 	q->u_L = ou.add(b->L_out ? 8 * (size_t)P : 0);
@@ -526,7 +605,8 @@ beep_status beep_batch_launch(beep_batch *q)
 {
 	if (!q) return fail(BEEP_BAD_INPUT, "null batch");
 	CUDA_TRY(cudaMemsetAsync(q->bd.status, 0, 4 * (size_t)q->bd.P, q->m->stream));
-	int le = launch_sim_plain(q->m->dev, q->bd, q->m->stream);
+	int le = q->b.form == BEEP_FORM_FAST ? launch_sim_fast(q->m->dev, q->bd, q->m->stream)
+	                                     : launch_sim_plain(q->m->dev, q->bd, q->m->stream);
 	if (le != 0) return fail(BEEP_DEVICE_ERROR, std::string("kernel launch: ") + cudaGetErrorString((cudaError_t)le));
 	q->pending = true;
 	return BEEP_OK;

@@ -127,7 +127,7 @@ __device__ __forceinline__ double log_factorial_p(double k)
 
 // Poisson(mean) of transition tr in column col at step sett; -1 after 65536
 // rejections (reported as an error by the caller).
-__device__ __noinline__ int32_t poisson_fp64(double mean, uint32_t k0, uint32_t k1, uint32_t col, uint32_t tr,
+static __device__ __noinline__ int32_t poisson_fp64(double mean, uint32_t k0, uint32_t k1, uint32_t col, uint32_t tr,
                                               uint32_t sett, uint32_t stream)
 {
 	if (!(mean > 0.0)) return 0;

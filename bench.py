@@ -223,7 +223,8 @@ def run_ours(args, rank, ws, dist):
     seed = args.seed + 7919 * rank
     w, m, tabs = build_workload(P, seed)
     dm = capi.DeviceModel(m, device=int(os.environ.get("LOCAL_RANK", "0")) if ws > 1 else 0)
-    batch = capi.Batch(m, tabs, P, seed, group_of=np.arange(P), stream_of=np.arange(P) + rank * P)
+    form = capi.FORM_FAST if args.form == "fast" else capi.FORM_PLAIN_FP64
+    batch = capi.Batch(m, tabs, P, seed, group_of=np.arange(P), stream_of=np.arange(P) + rank * P, form=form)
     db = capi.DeviceBatch(dm, batch)
     h2d, d2h = db.bytes()
     db.upload()
@@ -258,6 +259,17 @@ def run_ours(args, rank, ws, dist):
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_dev, t_e2e = float(tt[0]), float(tt[1])
     assert np.all(np.isfinite(batch.L))
+    # the plain FP64 form on a subset of the particles (same workload, units/s)
+    plain = None
+    if form == capi.FORM_FAST and args.plain_particles > 0:
+        Pp = min(P, args.plain_particles)
+        pb = capi.DeviceBatch(dm, capi.Batch(m, tabs[:Pp], Pp, seed, group_of=np.arange(Pp), form=capi.FORM_PLAIN_FP64))
+        pb.upload()
+        pb.time(1)
+        pms = pb.time(1)
+        plain = {"value": Pp * m.narea * m.nage * m.ndivision / (pms / 1e3), "unit": "particle.area.group.steps/s",
+                 "ms_per_step": pms, "particles": Pp, "loglik_evals_per_s": Pp / (pms / 1e3)}
+        pb.close()
     if rank != 0:
         return
     hbm, hbm_kind = peaks()
@@ -265,7 +277,7 @@ def run_ours(args, rank, ws, dist):
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
-        traffic = json.load(open(tp)).get("sim_plain_kernel")
+        traffic = json.load(open(tp)).get("sim_fast_kernel" if args.form == "fast" else "sim_plain_kernel")
     cpu = None
     if not args.no_cpu:
         nthreads = os.cpu_count() or 1
@@ -275,9 +287,10 @@ def run_ours(args, rank, ws, dist):
     line = {
         "metric": METRIC, "value": units * ws / t_dev, "unit": "particle.area.group.steps/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_dev * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": workload_config(m, P),
-        "form": "plain_fp64",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.form == "fast" else "f64",
+        "data": "synthetic", "config": workload_config(m, P),
+        "form": args.form,
+        "plain_fp64": plain,
         "loglik_evals_per_s": P * ws / t_dev,
         "clocks": clocks,
         "e2e": {"value": units * ws / t_e2e, "unit": "particle.area.group.steps/s", "h2d_bytes_per_step": h2d,
@@ -303,6 +316,8 @@ def main():
     ap.add_argument("--seed", type=int, default=20260001)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--form", default="fast", choices=["fast", "plain"])
+    ap.add_argument("--plain-particles", type=int, default=1024)
     args = ap.parse_args()
     rank, ws, dist = dist_setup(args)
     if args.impl == "reference":

@@ -134,7 +134,10 @@ typedef struct beep_param_tables {
 
 /* Arithmetic form of the kernels. */
 enum beep_form {
-	BEEP_FORM_PLAIN_FP64 = 0  /* FP64 in the reference's summation order: bit-exact transnum/pop */
+	BEEP_FORM_PLAIN_FP64 = 0, /* FP64 in the reference's summation order: bit-exact transnum/pop */
+	BEEP_FORM_FAST = 1        /* particle-resident, FP32 rates and draws on the same keyed streams,
+	                             exact integer observation sums, compensated FP32 log-densities
+	                             reduced in FP64 */
 };
 
 /* One batch of particles advanced over steps [ti, tf): State::simulate(ti,tf)
