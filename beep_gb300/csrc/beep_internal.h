@@ -31,6 +31,8 @@ struct ModelDev {
 	const float *M_diag_f, *M_factor_f;  // [A]
 	const float *csc_val_f;              // [nnz]
 	const float2 *obs_np;                // [nobs] normal models: (-0.5 log(2 pi sd^2), 1/(2 sd^2))
+	const float *obs_value_f;            // [nobs]
+	int32_t dp_age_unique;               // each age has exactly one dp per strain
 };
 
 // One parameter set's tables: offsets into the batch's table pool (doubles /

@@ -13,9 +13,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <unordered_map>
 #include <mutex>
 #include <string>
 #include <utility>
@@ -109,6 +111,7 @@ struct beep_model {
 	// host copies used to prepare batches
 	int32_t A, G, DP, NS, C, T, S, period, dpt, nobs;
 	std::vector<int32_t> obs_sett_i, obs_sett_f, obs_spline, trans_from_h, trans_to_h;
+	int32_t max_obs_spline = -1;
 	std::mutex mu;
 };
 
@@ -220,7 +223,9 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	}
 	for (int j = 0; j < nnz; j++) csc_val_f[j] = (float)csc_val[j];
 	std::vector<float2> obs_np(nobs > 0 ? nobs : 1);
+	std::vector<float> obs_value_f(nobs > 0 ? nobs : 1);
 	for (int o = 0; o < nobs; o++) {
+		obs_value_f[o] = (float)d->obs_value[o];
 		const double var = d->obs_sd[o] * d->obs_sd[o];
 		obs_np[o] = make_float2((float)(-0.5 * std::log(2 * 3.14159265358979323846 * var)), (float)(1.0 / (2 * var)));
 	}
@@ -231,6 +236,7 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	m->obs_sett_i.assign(d->obs_sett_i, d->obs_sett_i + nobs);
 	m->obs_sett_f.assign(d->obs_sett_f, d->obs_sett_f + nobs);
 	m->obs_spline.assign(d->obs_factor_spline, d->obs_factor_spline + nobs);
+	for (int o = 0; o < nobs; o++) m->max_obs_spline = std::max(m->max_obs_spline, d->obs_factor_spline[o]);
 	m->trans_from_h.assign(d->trans_from, d->trans_from + T);
 	m->trans_to_h.assign(d->trans_to, d->trans_to + T);
 	cudaGetDevice(&m->device);
@@ -243,7 +249,8 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	       o_osi = L.add(4 * (size_t)nobs), o_osf = L.add(4 * (size_t)nobs), o_ov = L.add(8 * (size_t)nobs),
 	       o_osd = L.add(8 * (size_t)nobs), o_osh = L.add(8 * (size_t)nobs), o_oth = L.add(8 * (size_t)nobs),
 	       o_ofa = L.add(8 * (size_t)nobs), o_md = L.add(4 * (size_t)A * A), o_mdg = L.add(4 * (size_t)A),
-	       o_mfc = L.add(4 * (size_t)A), o_cvf = L.add(4 * (size_t)nnz), o_onp = L.add(8 * (size_t)nobs);
+	       o_mfc = L.add(4 * (size_t)A), o_cvf = L.add(4 * (size_t)nnz), o_onp = L.add(8 * (size_t)nobs),
+	       o_ovf = L.add(4 * (size_t)nobs);
 	std::vector<char> host(L.size);
 	auto put = [&](size_t off, const void *src, size_t n) { if (n) memcpy(host.data() + off, src, n); };
 	put(o_tf, d->trans_from, 4 * T); put(o_tt, d->trans_to, 4 * T); put(o_age, d->democatpos_age, 4 * DPS);
@@ -261,6 +268,7 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	put(o_md, Mdense.data(), 4 * (size_t)A * A); put(o_mdg, Mdiag_f.data(), 4 * (size_t)A);
 	put(o_mfc, Mfac_f.data(), 4 * (size_t)A); put(o_cvf, csc_val_f.data(), 4 * (size_t)nnz);
 	if (nobs > 0) put(o_onp, obs_np.data(), 8 * (size_t)nobs);
+	if (nobs > 0) put(o_ovf, obs_value_f.data(), 4 * (size_t)nobs);
 	cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
 	if (e == cudaSuccess) e = m->model_mem.reserve(L.size);
 	if (e == cudaSuccess) e = cudaMemcpy(m->model_mem.ptr, host.data(), L.size, cudaMemcpyHostToDevice);
@@ -287,6 +295,13 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	md.Mdense = (const float *)(base + o_md); md.M_diag_f = (const float *)(base + o_mdg);
 	md.M_factor_f = (const float *)(base + o_mfc); md.csc_val_f = (const float *)(base + o_cvf);
 	md.obs_np = (const float2 *)(base + o_onp);
+	md.obs_value_f = (const float *)(base + o_ovf);
+	{
+		std::vector<int> cnt(G, 0);
+		for (int dp = 0; dp < DPS; dp++) cnt[d->democatpos_age[dp]]++;
+		md.dp_age_unique = 1;
+		for (int a = 0; a < G; a++) if (cnt[a] != 1) md.dp_age_unique = 0;
+	}
 	*out = m;
 	return BEEP_OK;
 }
@@ -308,7 +323,14 @@ namespace {
 struct TablePacker {
 	std::vector<double> f;
 	std::vector<int32_t> i;
-	std::map<std::pair<const void *, size_t>, int64_t> seen;
+	struct KeyHash {
+		size_t operator()(const std::pair<const void *, size_t> &k) const
+		{
+			return std::hash<const void *>()(k.first) * 31u + std::hash<size_t>()(k.second);
+		}
+	};
+	std::unordered_map<std::pair<const void *, size_t>, int64_t, KeyHash> seen;
+	std::unordered_map<const int32_t *, std::pair<int32_t, int32_t>> ranges;
 	int64_t addf(const double *p, size_t n)
 	{
 		auto key = std::make_pair((const void *)p, n);
@@ -344,12 +366,19 @@ beep_status pack_tables(const beep_model *m, const beep_sim_batch *b, TablePacke
 			return fail(BEEP_BAD_INPUT, "parameter set " + std::to_string(g) + ": missing table");
 		if (t.nbeta_row <= 0 || t.nefoi <= 0 || t.nobs_spline < 0)
 			return fail(BEEP_BAD_INPUT, "parameter set " + std::to_string(g) + ": bad table counts");
-		for (size_t k = 0; k < NS * A; k++) {
-			if (t.beta_row_of[k] < 0 || t.beta_row_of[k] >= t.nbeta_row) return fail(BEEP_BAD_INPUT, "beta_row_of out of range");
-			if (t.efoi_ref[k] < 0 || t.efoi_ref[k] >= t.nefoi) return fail(BEEP_BAD_INPUT, "efoi_ref out of range");
-		}
-		for (int o = 0; o < m->nobs; o++)
-			if (m->obs_spline[o] >= t.nobs_spline) return fail(BEEP_BAD_INPUT, "obs_factor_spline beyond nobs_spline");
+		// index tables shared between parameter sets are scanned once (range of values cached)
+		auto range_of = [&](const int32_t *p) {
+			auto it = pk.ranges.find(p);
+			if (it != pk.ranges.end()) return it->second;
+			std::pair<int32_t, int32_t> r{INT32_MAX, INT32_MIN};
+			for (size_t k = 0; k < NS * A; k++) { r.first = std::min(r.first, p[k]); r.second = std::max(r.second, p[k]); }
+			pk.ranges[p] = r;
+			return r;
+		};
+		const auto rb = range_of(t.beta_row_of), re = range_of(t.efoi_ref);
+		if (rb.first < 0 || rb.second >= t.nbeta_row) return fail(BEEP_BAD_INPUT, "beta_row_of out of range");
+		if (re.first < 0 || re.second >= t.nefoi) return fail(BEEP_BAD_INPUT, "efoi_ref out of range");
+		if (m->max_obs_spline >= t.nobs_spline) return fail(BEEP_BAD_INPUT, "obs_factor_spline beyond nobs_spline");
 		GroupDir &dd = dirs[g];
 		dd.transrate = pk.addf(t.transrate, T * DP);
 		dd.susceptibility = pk.addf(t.susceptibility, DP);

@@ -89,14 +89,14 @@ __device__ __forceinline__ int32_t poisson_fp32(float mean, uint32_t k0, uint32_
 	return -1;
 }
 
-__device__ float obs_lp_fast(double value, int o, const ModelDev &m)
+__device__ float obs_lp_fast(float vf, int o, const ModelDev &m)
 {
 	const int kind = m.obs_kind[o], model = m.obs_model[o];
-	if (value < 0) value = 0;
+	double value = vf < 0.f ? 0.0 : (double)vf;
 	if (kind == BEEP_OBSVAL_UNKNOWN) return 0.f;
 	if (kind == BEEP_OBSVAL_VALUE && (model == BEEP_OBS_NORMAL || model == BEEP_OBS_NORMAL_PERCENT)) {
 		const float2 np = m.obs_np[o];                       // (-0.5 log(2 pi var), 1/(2 var))
-		const float d = (float)(m.obs_value[o] - value);
+		const float d = m.obs_value_f[o] - (vf < 0.f ? 0.f : vf);
 		return np.x - d * d * np.y;
 	}
 	if (kind == BEEP_OBSVAL_VALUE && model == BEEP_OBS_POISSON) {
@@ -125,17 +125,71 @@ __device__ float obs_lp_fast(double value, int o, const ModelDev &m)
 	return (float)log(sum);
 }
 
+// Row stride of the area-mixing matrix in shared memory: congruent to 8 mod 32
+// so that the FOI loop's 4 source rows x 8 targets per warp hit 32 banks.
+__host__ __device__ inline int ms_lda(int A) { return A + ((40 - A % 32) % 32); }
+
 struct FastSmem {
-	float *Ms;       // [A][A] source-major, diagonal zero (or null: read M from global)
-	int32_t *pop;    // [A][C][DP]
-	int32_t *tn;     // [A][T][DP]
-	float *Icnt;     // [NS][A][G]
-	float *Imap;     // [NS][A][G]
-	double *slot;    // [nslots]
-	float *red;      // [2*NT] reductions
+	float *Ms;         // [A][lda] source-major, diagonal zero (or null: M read from global)
+	int32_t *pop[2];   // [A][C][DP] current / next
+	int32_t *tn;       // [A][T][DP]
+	float *Icnt[2];    // [NS][A][G] current / next
+	float *Imap;       // [NS][A][G]
+	float *slot;       // [nslots]
+	float *red;        // [2*NT]
 };
 
-template <int NT>
+// Imap[st][t][a] = sum_c M[c][t] Icnt[st][c][a] (off-diagonal M).  Lane layout:
+// 4 consecutive lanes share a target t and split the sources c = cg (mod 4);
+// the quad's partial sums are combined with two butterfly shuffles.
+template <int NT, int kMaxG>
+__device__ __forceinline__ void foi(const ModelDev &m, const float *Ms, int lda, const float *Icnt, float *Imap, int tid)
+{
+	const int A = m.A, G = m.G;
+	const int cg = tid & 3;
+	for (int st = 0; st < m.NS; st++) {
+		const float *I = Icnt + st * A * G;
+		for (int t0 = 0; t0 < A; t0 += NT / 4) {
+			const int t = t0 + (tid >> 2);
+			float acc[kMaxG];
+#pragma unroll
+			for (int a = 0; a < kMaxG; a++) acc[a] = 0.f;
+			if (t < A) {
+				if (Ms) {
+#pragma unroll 2
+					for (int c = cg; c < A; c += 4) {
+						const float mv = Ms[c * lda + t];
+						const float *Ic = I + c * G;
+#pragma unroll
+						for (int a = 0; a < kMaxG; a++)
+							if (a < G) acc[a] = fmaf(mv, Ic[a], acc[a]);
+					}
+				} else {
+					for (int c = cg; c < A; c += 4) {
+						const float mv = __ldg(m.Mdense + (size_t)c * A + t);
+						const float *Ic = I + c * G;
+#pragma unroll
+						for (int a = 0; a < kMaxG; a++)
+							if (a < G) acc[a] = fmaf(mv, Ic[a], acc[a]);
+					}
+				}
+			}
+#pragma unroll
+			for (int a = 0; a < kMaxG; a++) {
+				if (a < G) {
+					acc[a] += __shfl_xor_sync(0xffffffffu, acc[a], 1);
+					acc[a] += __shfl_xor_sync(0xffffffffu, acc[a], 2);
+				}
+			}
+			if (t < A && cg == 0)
+#pragma unroll
+				for (int a = 0; a < kMaxG; a++)
+					if (a < G) Imap[(st * A + t) * G + a] = acc[a];
+		}
+	}
+}
+
+template <int NT, int kMaxG>
 __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const BatchDev b)
 {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -145,6 +199,7 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 	const int A = m.A, G = m.G, DP = m.DP, NS = m.NS, DPS = m.DPS, C = m.C, T = m.T;
 	const int popsz = A * C * DP, tnsz = A * T * DP, agsz = NS * A * G, ncol = A * DP;
 	const int nsteps = b.tf - b.ti;
+	const int lda = ms_lda(A);
 	const GroupDir dir = b.dirs[b.group_of ? b.group_of[p] : 0];
 	const uint32_t stream = b.stream_of ? b.stream_of[p] : (uint32_t)p;
 	const float *fp = b.fpool32;
@@ -156,23 +211,40 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 	const int32_t *beta_row_of = ip + dir.beta_row_of, *efoi_ref = ip + dir.efoi_ref;
 	int32_t *status = b.status + p;
 
-	// shared-memory carve-up
 	FastSmem s;
 	{
 		size_t off = 0;
 		auto take = [&](size_t bytes) { unsigned char *q = smem_raw + off; off += (bytes + 15) & ~(size_t)15; return q; };
-		s.slot = (double *)take(sizeof(double) * b.nslots);
-		s.Ms = b.m_in_smem ? (float *)take(sizeof(float) * A * A) : nullptr;
-		s.pop = (int32_t *)take(sizeof(int32_t) * popsz);
+		s.Ms = b.m_in_smem ? (float *)take(sizeof(float) * A * lda) : nullptr;
+		s.pop[0] = (int32_t *)take(sizeof(int32_t) * popsz);
+		s.pop[1] = (int32_t *)take(sizeof(int32_t) * popsz);
 		s.tn = (int32_t *)take(sizeof(int32_t) * tnsz);
-		s.Icnt = (float *)take(sizeof(float) * agsz);
+		s.Icnt[0] = (float *)take(sizeof(float) * agsz);
+		s.Icnt[1] = (float *)take(sizeof(float) * agsz);
 		s.Imap = (float *)take(sizeof(float) * agsz);
+		s.slot = (float *)take(sizeof(float) * b.nslots);
 		s.red = (float *)take(sizeof(float) * 2 * NT);
 	}
 	if (s.Ms)
-		for (int k = tid; k < A * A; k += NT) s.Ms[k] = m.Mdense[k];
-	for (int k = tid; k < popsz; k += NT) s.pop[k] = b.ti == 0 ? m.pop_init[k] : b.pop_in[(size_t)p * popsz + k];
-	for (int k = tid; k < b.nslots; k += NT) s.slot[k] = 0.0;
+		for (int k = tid; k < A * A; k += NT) s.Ms[(k / A) * lda + k % A] = m.Mdense[k];
+	for (int k = tid; k < popsz; k += NT) s.pop[0][k] = b.ti == 0 ? m.pop_init[k] : b.pop_in[(size_t)p * popsz + k];
+	for (int k = tid; k < b.nslots; k += NT) s.slot[k] = 0.f;
+	for (int k = tid; k < agsz; k += NT) s.Icnt[1][k] = 0.f;
+	__syncthreads();
+	// infectious counts of the start populations (set_I_from_pop, src/state.cc:223-290)
+	for (int idx = tid; idx < agsz; idx += NT) {
+		const int a = idx % G, c = (idx / G) % A, st = idx / (G * A);
+		float v = 0.f;
+		for (int co = 0; co < C; co++) {
+			const float inf = infectivity[co];
+			if (inf != 0.f)
+				for (int dp = 0; dp < DPS; dp++)
+					if (m.dp_age[dp] == a) v += inf * (float)s.pop[0][(c * C + co) * DP + st * DPS + dp];
+		}
+		s.Icnt[0][idx] = v;
+	}
+	__syncthreads();
+	foi<NT, kMaxG>(m, s.Ms, lda, s.Icnt[0], s.Imap, tid);
 	float Lsum = 0.f, Lcmp = 0.f;           // compensated per-thread log-likelihood
 	__syncthreads();
 
@@ -180,61 +252,40 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 	const int inf_from = m.trans_from[itr];
 	const float dt = (float)m.dt;
 	const float inv_popsize = (float)(1.0 / m.popsize);
+	int cur = 0;
 	for (int sett = b.ti; sett < b.tf; sett++) {
-		// ---- 1: infectious counts per (strain, area, age)
-		for (int idx = tid; idx < agsz; idx += NT) {
-			const int a = idx % G, c = (idx / G) % A, st = idx / (G * A);
-			float v = 0.f;
-			for (int co = 0; co < C; co++) {
-				const float inf = infectivity[co];
-				if (inf != 0.f)
-					for (int dp = 0; dp < DPS; dp++)
-						if (m.dp_age[dp] == a) v += inf * (float)s.pop[(c * C + co) * DP + st * DPS + dp];
-			}
-			s.Icnt[idx] = v;
-		}
-		__syncthreads();
-
-		// ---- 2: Imap = M^T Icnt (off-diagonal part; the diagonal is applied in 3)
-		for (int idx = tid; idx < agsz; idx += NT) {
-			const int a = idx % G, t = (idx / G) % A, st = idx / (G * A);
-			const float *I = s.Icnt + st * A * G + a;
-			float acc = 0.f;
-			if (s.Ms) {
-				for (int c = 0; c < A; c++) acc = fmaf(s.Ms[c * A + t], I[c * G], acc);
-			} else {
-				for (int j = m.csc_ptr[t]; j < m.csc_ptr[t + 1]; j++) acc = fmaf(m.csc_val_f[j], I[m.csc_src[j] * G], acc);
-			}
-			s.Imap[idx] = acc;
-		}
+		int32_t *pc = cur ? s.pop[1] : s.pop[0], *pn = cur ? s.pop[0] : s.pop[1];
+		const float *Ic_cur = cur ? s.Icnt[1] : s.Icnt[0];
+		float *Ic_nxt = cur ? s.Icnt[0] : s.Icnt[1];
 		if (NS > 1) {
-			__syncthreads();
 			// strain shift of the susceptible population (src/state.cc:392-401)
 			for (int idx = tid; idx < A * DPS; idx += NT) {
 				const int dp = idx % DPS, c = idx / DPS;
-				int32_t *sp = s.pop + (c * C + inf_from) * DP;
+				int32_t *sp = pc + (c * C + inf_from) * DP;
 				int32_t sum = 0;
 				for (int st = 1; st < NS; st++) { sum += sp[DPS * st + dp]; sp[DPS * st + dp] = 0; }
 				sp[dp] += sum;
 			}
+			__syncthreads();
 		}
-		__syncthreads();
 
-		// ---- 3: per column: NMI, means, draws
+		// ---- A: per column (c, dp): NMI, means, draws, next population, next infectious count
 		const float d = geo[sett], omd = 1.f - d;
 		for (int col = tid; col < ncol; col += NT) {
 			const int c = col / DP, dp = col % DP;
 			const int st = dp / DPS, dpl = dp % DPS, a = m.dp_age[dpl];
 			U4 inv{0, 0, 0, 0};
 			uint32_t inv_call = 0xffffffffu;
+			int32_t *pcol = pc + c * C * DP + dp, *ncol_p = pn + c * C * DP + dp;
+			for (int co = 0; co < C; co++) ncol_p[co * DP] = pcol[co * DP];
 			for (int tr = 0; tr < T; tr++) {
 				float mean;
 				if (tr == itr) {
-					const float popu = (float)s.pop[(c * C + inf_from) * DP + dpl];
+					const float popu = (float)pc[(c * C + inf_from) * DP + dpl];
 					if (popu <= 0.f) mean = 0.f;
 					else {
 						const float fac = m.M_factor_f[c], dg = m.M_diag_f[c];
-						const float *Ic = s.Icnt + (st * A + c) * G, *Im = s.Imap + (st * A + c) * G;
+						const float *Ic = Ic_cur + (st * A + c) * G, *Im = s.Imap + (st * A + c) * G;
 						const float *N = Ntime + ((size_t)sett * G + a) * G;
 						float nmi = 0.f;
 						for (int aa = 0; aa < G; aa++) {
@@ -249,7 +300,7 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 						mean = dt * popu * sus[dp] * (be * nmi + eta);
 					}
 				} else {
-					const float popu = (float)s.pop[(c * C + m.trans_from[tr]) * DP + dp];
+					const float popu = (float)pcol[m.trans_from[tr] * DP];
 					mean = popu <= 0.f ? 0.f : dt * popu * transrate[tr * DP + dp];
 				}
 				int32_t n = 0;
@@ -262,69 +313,70 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 					}
 				}
 				s.tn[(c * T + tr) * DP + dp] = n;
+				if (n != 0) {
+					ncol_p[m.trans_from[tr] * DP] -= n;
+					ncol_p[m.trans_to[tr] * DP] += n;
+				}
 			}
+			float iv = 0.f;
+			for (int co = 0; co < C; co++) {
+				const float inf = infectivity[co];
+				if (inf != 0.f) iv = fmaf(inf, (float)ncol_p[co * DP], iv);
+			}
+			if (m.dp_age_unique) Ic_nxt[(st * A + c) * G + a] = iv;
+			else atomicAdd(Ic_nxt + (st * A + c) * G + a, iv);
 		}
 		__syncthreads();
 
+		// ---- B: observation sums of the step (completed ones -> log-density); FOI for the next step
 		if (b.pop_traj)
-			for (int k = tid; k < popsz; k += NT) b.pop_traj[((size_t)p * nsteps + (sett - b.ti)) * popsz + k] = s.pop[k];
-		// ---- 4: observation gathers (integer counts, exact in FP64)
+			for (int k = tid; k < popsz; k += NT) b.pop_traj[((size_t)p * nsteps + (sett - b.ti)) * popsz + k] = pc[k];
+		if (b.tn_traj)
+			for (int k = tid; k < tnsz; k += NT) b.tn_traj[((size_t)p * nsteps + (sett - b.ti)) * tnsz + k] = s.tn[k];
 		const int a0 = b.step_ptr[sett - b.ti], a1 = b.step_ptr[sett - b.ti + 1];
 		for (int k = a0 + tid; k < a1; k += NT) {
 			const int pos = b.step_obs[k];
 			const int o = b.scored[pos];
-			const double fac = m.obs_factor[o];
+			const float fac = (float)m.obs_factor[o];
 			const int spl = m.obs_spline[o];
-			double v = 0.0;
+			const int sl = b.slot_of[pos];
+			float v = s.slot[sl];
 			for (int q = m.obs_cell_ptr[o]; q < m.obs_cell_ptr[o + 1]; q++) {
 				const int cell = m.obs_cells[q];
-				const double num = cell >= 0 ? (double)s.tn[cell] : (double)s.pop[-1 - cell];
-				v += spl < 0 ? fac * num : fac * num * obs_spline[(size_t)spl * m.S + sett];
+				const float num = cell >= 0 ? (float)s.tn[cell] : (float)pc[-1 - cell];
+				v += spl < 0 ? fac * num : fac * num * (float)obs_spline[(size_t)spl * m.S + sett];
 			}
-			s.slot[b.slot_of[pos]] += v;
-		}
-		__syncthreads();
-
-		// ---- 5: population update per column; completed observations
-		for (int col = tid; col < ncol; col += NT) {
-			const int c = col / DP, dp = col % DP;
-			for (int co = 0; co < C; co++) {
-				int32_t v = s.pop[(c * C + co) * DP + dp];
-				for (int tr = 0; tr < T; tr++) {
-					const int32_t n = s.tn[(c * T + tr) * DP + dp];
-					if (m.trans_from[tr] == co) v -= n;
-					if (m.trans_to[tr] == co) v += n;
-				}
-				s.pop[(c * C + co) * DP + dp] = v;
+			if (sett == m.obs_sett_f[o] - 1) {
+				const float lp = obs_lp_fast(v, o, m);
+				v = 0.f;
+				const float y = lp - Lcmp;      // Kahan
+				const float tt = Lsum + y;
+				Lcmp = (tt - Lsum) - y;
+				Lsum = tt;
 			}
+			s.slot[sl] = v;
 		}
-		if (b.tn_traj)
-			for (int k = tid; k < tnsz; k += NT) b.tn_traj[((size_t)p * nsteps + (sett - b.ti)) * tnsz + k] = s.tn[k];
-		const int e0 = b.end_ptr[sett - b.ti], e1 = b.end_ptr[sett - b.ti + 1];
-		for (int k = e0 + tid; k < e1; k += NT) {
-			const int pos = b.end_pos[k];
-			const int sl = b.slot_of[pos];
-			const float lp = obs_lp_fast(s.slot[sl], b.scored[pos], m);
-			s.slot[sl] = 0.0;
-			const float y = lp - Lcmp;      // Kahan
-			const float t = Lsum + y;
-			Lcmp = (t - Lsum) - y;
-			Lsum = t;
-		}
+		if (!m.dp_age_unique)
+			for (int k = tid; k < agsz; k += NT) (cur ? s.Icnt[1] : s.Icnt[0])[k] = 0.f;   // next step's accumulation target
+		foi<NT, kMaxG>(m, s.Ms, lda, Ic_nxt, s.Imap, tid);
 		__syncthreads();
+		cur ^= 1;
 	}
 
 	if (b.pop_out)
-		for (int k = tid; k < popsz; k += NT) b.pop_out[(size_t)p * popsz + k] = s.pop[k];
+		for (int k = tid; k < popsz; k += NT) b.pop_out[(size_t)p * popsz + k] = (cur ? s.pop[1] : s.pop[0])[k];
 	if (b.L) {
 		s.red[tid] = Lsum;
 		s.red[NT + tid] = Lcmp;
 		__syncthreads();
-		if (tid == 0) {
+		if (tid < 32) {
 			double S = 0.0;
-			for (int k = 0; k < NT; k++) S += (double)s.red[k] - (double)s.red[NT + k];
-			if (S != S) atomicCAS(status, 0, BEEP_NAN_RATE);
-			b.L[p] = S;
+			for (int k = tid; k < NT; k += 32) S += (double)s.red[k] - (double)s.red[NT + k];
+			for (int o = 16; o > 0; o >>= 1) S += __shfl_xor_sync(0xffffffffu, S, o);
+			if (tid == 0) {
+				if (S != S) atomicCAS(status, 0, BEEP_NAN_RATE);
+				b.L[p] = S;
+			}
 		}
 	}
 }
@@ -335,8 +387,8 @@ size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem)
 {
 	auto r = [](size_t x) { return (x + 15) & ~(size_t)15; };
 	const size_t agsz = (size_t)m.NS * m.A * m.G;
-	return r(8 * (size_t)nslots) + (m_in_smem ? r(4 * (size_t)m.A * m.A) : 0) + r(4 * (size_t)m.A * m.C * m.DP) +
-	       r(4 * (size_t)m.A * m.T * m.DP) + 2 * r(4 * agsz) + r(4 * 2 * (size_t)kFastThreads);
+	return (m_in_smem ? r(4 * (size_t)m.A * ms_lda(m.A)) : 0) + 2 * r(4 * (size_t)m.A * m.C * m.DP) +
+	       r(4 * (size_t)m.A * m.T * m.DP) + 3 * r(4 * agsz) + r(4 * (size_t)nslots) + r(4 * 2 * (size_t)kFastThreads);
 }
 
 int fast_threads() { return kFastThreads; }
@@ -352,11 +404,12 @@ int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream)
 		init = true;
 	}
 	if (b.P == 0) return 0;
+	if (m.G > 16) return (int)cudaErrorInvalidValue;
 	const size_t smem = fast_smem_bytes(m, b.nslots, b.m_in_smem != 0);
-	cudaError_t e = cudaFuncSetAttribute(sim_fast_kernel<kFastThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-	                                     (int)smem);
+	auto kern = m.G <= 4 ? sim_fast_kernel<kFastThreads, 4> : sim_fast_kernel<kFastThreads, 16>;
+	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	if (e != cudaSuccess) return (int)e;
-	sim_fast_kernel<kFastThreads><<<b.P, kFastThreads, smem, (cudaStream_t)stream>>>(m, b);
+	kern<<<b.P, kFastThreads, smem, (cudaStream_t)stream>>>(m, b);
 	return (int)cudaGetLastError();
 }
 
