@@ -32,6 +32,9 @@ struct ModelDev {
 	const float *csc_val_f;              // [nnz]
 	const float2 *obs_np;                // [nobs] normal models: (-0.5 log(2 pi sd^2), 1/(2 sd^2))
 	const float *obs_value_f;            // [nobs]
+	const float *obs_factor_f, *obs_shape_f;  // [nobs]
+	const int32_t *obs_cells_f;          // cells in the fast form's column-major shared layout:
+	                                     // tr*ncol + col (transition) or -1-(co*ncol + col) (population)
 	int32_t dp_age_unique;               // each age has exactly one dp per strain
 };
 

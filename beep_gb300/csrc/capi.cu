@@ -223,9 +223,25 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	}
 	for (int j = 0; j < nnz; j++) csc_val_f[j] = (float)csc_val[j];
 	std::vector<float2> obs_np(nobs > 0 ? nobs : 1);
-	std::vector<float> obs_value_f(nobs > 0 ? nobs : 1);
+	std::vector<float> obs_value_f(nobs > 0 ? nobs : 1), obs_factor_f(nobs > 0 ? nobs : 1), obs_shape_f(nobs > 0 ? nobs : 1);
+	std::vector<int32_t> obs_cells_f(ncells > 0 ? ncells : 1);
+	{
+		const int ncol = A * DP;
+		for (int q = 0; q < ncells; q++) {
+			const int32_t cell = d->obs_cells[q];
+			if (cell >= 0) {
+				const int c = cell / (T * DP), tr = (cell / DP) % T, dp = cell % DP;
+				obs_cells_f[q] = tr * ncol + c * DP + dp;
+			} else {
+				const int k = -1 - cell, c = k / (C * DP), co = (k / DP) % C, dp = k % DP;
+				obs_cells_f[q] = -1 - (co * ncol + c * DP + dp);
+			}
+		}
+	}
 	for (int o = 0; o < nobs; o++) {
 		obs_value_f[o] = (float)d->obs_value[o];
+		obs_factor_f[o] = (float)d->obs_factor[o];
+		obs_shape_f[o] = (float)d->obs_shape[o];
 		const double var = d->obs_sd[o] * d->obs_sd[o];
 		obs_np[o] = make_float2((float)(-0.5 * std::log(2 * 3.14159265358979323846 * var)), (float)(1.0 / (2 * var)));
 	}
@@ -250,7 +266,8 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	       o_osd = L.add(8 * (size_t)nobs), o_osh = L.add(8 * (size_t)nobs), o_oth = L.add(8 * (size_t)nobs),
 	       o_ofa = L.add(8 * (size_t)nobs), o_md = L.add(4 * (size_t)A * A), o_mdg = L.add(4 * (size_t)A),
 	       o_mfc = L.add(4 * (size_t)A), o_cvf = L.add(4 * (size_t)nnz), o_onp = L.add(8 * (size_t)nobs),
-	       o_ovf = L.add(4 * (size_t)nobs);
+	       o_ovf = L.add(4 * (size_t)nobs), o_off = L.add(4 * (size_t)nobs), o_oshf = L.add(4 * (size_t)nobs),
+	       o_ocf = L.add(4 * (size_t)ncells);
 	std::vector<char> host(L.size);
 	auto put = [&](size_t off, const void *src, size_t n) { if (n) memcpy(host.data() + off, src, n); };
 	put(o_tf, d->trans_from, 4 * T); put(o_tt, d->trans_to, 4 * T); put(o_age, d->democatpos_age, 4 * DPS);
@@ -269,6 +286,9 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	put(o_mfc, Mfac_f.data(), 4 * (size_t)A); put(o_cvf, csc_val_f.data(), 4 * (size_t)nnz);
 	if (nobs > 0) put(o_onp, obs_np.data(), 8 * (size_t)nobs);
 	if (nobs > 0) put(o_ovf, obs_value_f.data(), 4 * (size_t)nobs);
+	if (nobs > 0) put(o_off, obs_factor_f.data(), 4 * (size_t)nobs);
+	if (nobs > 0) put(o_oshf, obs_shape_f.data(), 4 * (size_t)nobs);
+	if (ncells > 0) put(o_ocf, obs_cells_f.data(), 4 * (size_t)ncells);
 	cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
 	if (e == cudaSuccess) e = m->model_mem.reserve(L.size);
 	if (e == cudaSuccess) e = cudaMemcpy(m->model_mem.ptr, host.data(), L.size, cudaMemcpyHostToDevice);
@@ -296,6 +316,9 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	md.M_factor_f = (const float *)(base + o_mfc); md.csc_val_f = (const float *)(base + o_cvf);
 	md.obs_np = (const float2 *)(base + o_onp);
 	md.obs_value_f = (const float *)(base + o_ovf);
+	md.obs_factor_f = (const float *)(base + o_off);
+	md.obs_shape_f = (const float *)(base + o_oshf);
+	md.obs_cells_f = (const int32_t *)(base + o_ocf);
 	{
 		std::vector<int> cnt(G, 0);
 		for (int dp = 0; dp < DPS; dp++) cnt[d->democatpos_age[dp]]++;

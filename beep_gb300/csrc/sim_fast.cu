@@ -34,20 +34,58 @@
 namespace beep {
 namespace {
 
-constexpr int kFastThreads = 640;
-
-__constant__ float c_rcp[256];   // 1/k for the inversion recurrence
+constexpr int kFastThreads = 640;   // largest CTA; smaller models use 128 or 256 threads
 
 __device__ __forceinline__ float u01_f(uint32_t w)
 {
 	return __uint2float_rn(w) * 2.3283064365386963e-10f + 1.1641532182693481e-10f;
 }
 
-// FP32 Poisson draw on the keyed stream of poisson_fp64 (same counters/words).
-__device__ __forceinline__ int32_t poisson_fp32(float mean, uint32_t k0, uint32_t k1, uint32_t col, uint32_t tr,
-                                                uint32_t sett, uint32_t stream, U4 &inv, uint32_t &inv_call)
+// Shared-memory image of one particle and of the tables it reads.  State is
+// stored column-major (index [comp or trans][col], col = c*DP + dp) so that the
+// 32 columns of a warp touch 32 consecutive words.
+struct FastSmem {
+	float *Ms;            // [A][lda] source-major area mixing, diagonal zero (or null)
+	int32_t *pop0, *pop1; // [C][ncol] current / next (swapped every step)
+	int32_t *tn;          // [T][ncol]
+	float *Ic0, *Ic1;     // [NS][A][G] infectious counts, current / next
+	float *Imap;          // [NS][A][G]
+	float *slot;          // [nslots]
+	// per-particle constants
+	int32_t *from, *to;   // [T]
+	int32_t *age;         // [DPS]
+	float *inf;           // [C]
+	float *rate;          // [T][DP]
+	float *sus;           // [DP]
+	float *rcp;           // [64] 1/k
+	float *lnfact;        // [32] log k!
+	// per-step slices (step being simulated)
+	float *be;            // [NS][A] beta * areafactor
+	float *eta;           // [NS][A][G] external force of infection per capita
+	float *N;             // [G][G] age mixing
+	float *red;           // [2*NT]; red[0] also carries the geo spline value d
+};
+
+__host__ __device__ inline int ms_lda(int A) { return A + ((40 - A % 32) % 32); }
+
+// log k! - (-mean + k log mean), written without cancellation: for k >= 32
+// Stirling's series of log Gamma(k+1) with x = (mean - n)/n, n = k+1, gives
+// rhs = k (log1p(x) - x) - x - log(n)/2 - log(2 pi)/2 - 1/(12n) + 1/(360n^3).
+__device__ __forceinline__ float ptrs_rhs(float k, float mean, float loglam, const float *lnfact)
 {
-	if (!(mean > 0.f)) return 0;
+	if (k < 32.f) return fmaf(k, loglam, -mean) - lnfact[(int)k];
+	const float n = k + 1.f;
+	const float x = (mean - n) / n;
+	const float in = 1.f / n;
+	const float corr = in * (0.083333333f - in * in * 0.0027777778f);
+	return k * (log1pf(x) - x) - x - 0.5f * logf(n) - 0.91893853f - corr;
+}
+
+// FP32 Poisson draw on the keyed stream of the FP64 form (same counters/words).
+__device__ __forceinline__ int32_t poisson_fp32(float mean, uint32_t k0, uint32_t k1, uint32_t col, uint32_t tr,
+                                                uint32_t sett, uint32_t stream, U4 &inv, uint32_t &inv_call,
+                                                const float *rcp, const float *lnfact)
+{
 	if (mean < 10.f) {
 		const uint32_t call = tr >> 2;
 		if (inv_call != call) {
@@ -58,9 +96,9 @@ __device__ __forceinline__ int32_t poisson_fp32(float mean, uint32_t k0, uint32_
 		float p = expf(-mean);
 		float F = p;
 		int32_t k = 0;
-		while (u > F && k < 255) {
+		while (u > F && k < 63) {
 			k++;
-			p = p * mean * c_rcp[k];
+			p = p * mean * rcp[k];
 			const float Fn = F + p;
 			if (Fn == F) break;          // FP32 tail exhausted
 			F = Fn;
@@ -83,34 +121,31 @@ __device__ __forceinline__ int32_t poisson_fp32(float mean, uint32_t k0, uint32_
 		if (us >= 0.07f && V <= vr) return (int32_t)k;
 		if (k < 0.0f || (us < 0.013f && V > us)) continue;
 		const float lhs = logf(V) + log_invalpha - logf(a / (us * us) + b);
-		const float rhs = -mean + k * loglam - lgammaf(k + 1.0f);
-		if (lhs <= rhs) return (int32_t)k;
+		if (lhs <= ptrs_rhs(k, mean, loglam, lnfact)) return (int32_t)k;
 	}
 	return -1;
 }
 
+// log-density of one completed observation (src/obsmodel.cc:245-305) in FP32;
+// thresholded values (rare) in FP64 as the reference evaluates them.
 __device__ float obs_lp_fast(float vf, int o, const ModelDev &m)
 {
 	const int kind = m.obs_kind[o], model = m.obs_model[o];
-	double value = vf < 0.f ? 0.0 : (double)vf;
+	const float v = vf < 0.f ? 0.f : vf;
 	if (kind == BEEP_OBSVAL_UNKNOWN) return 0.f;
-	if (kind == BEEP_OBSVAL_VALUE && (model == BEEP_OBS_NORMAL || model == BEEP_OBS_NORMAL_PERCENT)) {
-		const float2 np = m.obs_np[o];                       // (-0.5 log(2 pi var), 1/(2 var))
-		const float d = m.obs_value_f[o] - (vf < 0.f ? 0.f : vf);
-		return np.x - d * d * np.y;
+	if (kind == BEEP_OBSVAL_VALUE) {
+		if (model == BEEP_OBS_NORMAL || model == BEEP_OBS_NORMAL_PERCENT) {
+			const float2 np = m.obs_np[o];                     // (-0.5 log(2 pi var), 1/(2 var))
+			const float d = m.obs_value_f[o] - v;
+			return np.x - d * d * np.y;
+		}
+		const float lam = v < 1.f ? 1.f : v;
+		const float y = floorf(m.obs_value_f[o] + 0.5f);
+		if (model == BEEP_OBS_POISSON) return y * logf(lam) - lam - lgammaf(y + 1.f);
+		const float sh = m.obs_shape_f[o];
+		return lgammaf(sh + y) - lgammaf(y + 1.f) - lgammaf(sh) + sh * logf(sh / (sh + lam)) + y * logf(lam / (sh + lam));
 	}
-	if (kind == BEEP_OBSVAL_VALUE && model == BEEP_OBS_POISSON) {
-		const float lam = value < 1 ? 1.f : (float)value;
-		const int i = (int)(m.obs_value[o] + 0.5);
-		return (float)i * logf(lam) - lam - lgammaf((float)i + 1.f);
-	}
-	if (kind == BEEP_OBSVAL_VALUE && model == BEEP_OBS_NEGBIN) {
-		const float mm = value < 1 ? 1.f : (float)value, sh = (float)m.obs_shape[o];
-		const float v = (float)(int)(m.obs_value[o] + 0.5);
-		return lgammaf(sh + v) - lgammaf(v + 1.f) - lgammaf(sh) + sh * logf(sh / (sh + mm)) + v * logf(mm / (sh + mm));
-	}
-	// thresholded values: rare; evaluated in FP64 as the reference does (src/obsmodel.cc:251-280)
-	const double thresh = m.obs_thresh[o], sd = m.obs_sd[o];
+	const double value = v, thresh = m.obs_thresh[o], sd = m.obs_sd[o];
 	if (model == BEEP_OBS_NORMAL || model == BEEP_OBS_NORMAL_PERCENT) {
 		const double var = sd * sd;
 		const double x = value < thresh ? thresh : value;
@@ -118,31 +153,18 @@ __device__ float obs_lp_fast(float vf, int o, const ModelDev &m)
 	}
 	const double lam = value < 1 ? 1 : value, sh = m.obs_shape[o];
 	double sum = 0.0;
-	for (double v = 0; v <= thresh; v++) {
-		if (model == BEEP_OBS_POISSON) sum += exp(v * log(lam) - lam - lgamma(v + 1));
-		else sum += exp(lgamma(sh + v) - lgamma(v + 1) - lgamma(sh) + sh * log(sh / (sh + lam)) + v * log(lam / (sh + lam)));
+	for (double k = 0; k <= thresh; k++) {
+		if (model == BEEP_OBS_POISSON) sum += exp(k * log(lam) - lam - lgamma(k + 1));
+		else sum += exp(lgamma(sh + k) - lgamma(k + 1) - lgamma(sh) + sh * log(sh / (sh + lam)) + k * log(lam / (sh + lam)));
 	}
 	return (float)log(sum);
 }
 
-// Row stride of the area-mixing matrix in shared memory: congruent to 8 mod 32
-// so that the FOI loop's 4 source rows x 8 targets per warp hit 32 banks.
-__host__ __device__ inline int ms_lda(int A) { return A + ((40 - A % 32) % 32); }
-
-struct FastSmem {
-	float *Ms;         // [A][lda] source-major, diagonal zero (or null: M read from global)
-	int32_t *pop[2];   // [A][C][DP] current / next
-	int32_t *tn;       // [A][T][DP]
-	float *Icnt[2];    // [NS][A][G] current / next
-	float *Imap;       // [NS][A][G]
-	float *slot;       // [nslots]
-	float *red;        // [2*NT]
-};
-
-// Imap[st][t][a] = sum_c M[c][t] Icnt[st][c][a] (off-diagonal M).  Lane layout:
-// 4 consecutive lanes share a target t and split the sources c = cg (mod 4);
-// the quad's partial sums are combined with two butterfly shuffles.
-template <int NT, int kMaxG>
+// Imap[st][t][a] = sum_c M[c][t] Icnt[st][c][a] (off-diagonal M).  Four
+// consecutive lanes share a target t and split the sources c = cg (mod 4); the
+// quad's partials are combined with two butterfly shuffles.  With the row
+// stride congruent to 8 mod 32 a warp's 4 rows x 8 targets hit 32 banks.
+template <int NT, int MG>
 __device__ __forceinline__ void foi(const ModelDev &m, const float *Ms, int lda, const float *Icnt, float *Imap, int tid)
 {
 	const int A = m.A, G = m.G;
@@ -151,9 +173,9 @@ __device__ __forceinline__ void foi(const ModelDev &m, const float *Ms, int lda,
 		const float *I = Icnt + st * A * G;
 		for (int t0 = 0; t0 < A; t0 += NT / 4) {
 			const int t = t0 + (tid >> 2);
-			float acc[kMaxG];
+			float acc[MG];
 #pragma unroll
-			for (int a = 0; a < kMaxG; a++) acc[a] = 0.f;
+			for (int a = 0; a < MG; a++) acc[a] = 0.f;
 			if (t < A) {
 				if (Ms) {
 #pragma unroll 2
@@ -161,7 +183,7 @@ __device__ __forceinline__ void foi(const ModelDev &m, const float *Ms, int lda,
 						const float mv = Ms[c * lda + t];
 						const float *Ic = I + c * G;
 #pragma unroll
-						for (int a = 0; a < kMaxG; a++)
+						for (int a = 0; a < MG; a++)
 							if (a < G) acc[a] = fmaf(mv, Ic[a], acc[a]);
 					}
 				} else {
@@ -169,13 +191,13 @@ __device__ __forceinline__ void foi(const ModelDev &m, const float *Ms, int lda,
 						const float mv = __ldg(m.Mdense + (size_t)c * A + t);
 						const float *Ic = I + c * G;
 #pragma unroll
-						for (int a = 0; a < kMaxG; a++)
+						for (int a = 0; a < MG; a++)
 							if (a < G) acc[a] = fmaf(mv, Ic[a], acc[a]);
 					}
 				}
 			}
 #pragma unroll
-			for (int a = 0; a < kMaxG; a++) {
+			for (int a = 0; a < MG; a++) {
 				if (a < G) {
 					acc[a] += __shfl_xor_sync(0xffffffffu, acc[a], 1);
 					acc[a] += __shfl_xor_sync(0xffffffffu, acc[a], 2);
@@ -183,13 +205,37 @@ __device__ __forceinline__ void foi(const ModelDev &m, const float *Ms, int lda,
 			}
 			if (t < A && cg == 0)
 #pragma unroll
-				for (int a = 0; a < kMaxG; a++)
+				for (int a = 0; a < MG; a++)
 					if (a < G) Imap[(st * A + t) * G + a] = acc[a];
 		}
 	}
 }
 
-template <int NT, int kMaxG>
+struct Tabs {
+	const float *rate, *sus, *inf, *beta_rows, *areafactor, *Ntime, *geo, *efoi_spline, *efoi_age, *obs_spline;
+	const int32_t *beta_row_of, *efoi_ref;
+};
+
+// Per-step table slices for step sett: beta*areafactor per (strain, area), the
+// external force of infection per (strain, area, age), the age-mixing matrix
+// and the geographic spline (src/state.cc:403-423, 547-553).
+template <int NT>
+__device__ __forceinline__ void stage_step(const ModelDev &m, const Tabs &tb, FastSmem &s, int sett, int tid)
+{
+	const int A = m.A, G = m.G, NSA = m.NS * m.A;
+	const float inv_popsize = (float)(1.0 / m.popsize);
+	for (int k = tid; k < NSA; k += NT) {
+		const int c = k % A;
+		s.be[k] = tb.beta_rows[(size_t)tb.beta_row_of[k] * m.S + sett] * tb.areafactor[(size_t)(sett / m.div_per_time) * A + c];
+		const int ei = tb.efoi_ref[k];
+		const float et = tb.efoi_spline[(size_t)ei * m.S + sett] * inv_popsize;
+		for (int a = 0; a < G; a++) s.eta[k * G + a] = et * tb.efoi_age[(size_t)ei * G + a];
+	}
+	for (int k = tid; k < G * G; k += NT) s.N[k] = tb.Ntime[(size_t)sett * G * G + k];
+	if (tid == 0) s.red[0] = tb.geo[sett];
+}
+
+template <int NT, int MG>
 __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const BatchDev b)
 {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -197,18 +243,20 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 	if (p >= b.P) return;
 	const int tid = threadIdx.x;
 	const int A = m.A, G = m.G, DP = m.DP, NS = m.NS, DPS = m.DPS, C = m.C, T = m.T;
-	const int popsz = A * C * DP, tnsz = A * T * DP, agsz = NS * A * G, ncol = A * DP;
+	const int ncol = A * DP, popsz = C * ncol, tnsz = T * ncol, agsz = NS * A * G;
 	const int nsteps = b.tf - b.ti;
 	const int lda = ms_lda(A);
 	const GroupDir dir = b.dirs[b.group_of ? b.group_of[p] : 0];
 	const uint32_t stream = b.stream_of ? b.stream_of[p] : (uint32_t)p;
-	const float *fp = b.fpool32;
-	const int32_t *ip = b.ipool;
-	const float *transrate = fp + dir.transrate, *sus = fp + dir.susceptibility, *infectivity = fp + dir.infectivity;
-	const float *beta_rows = fp + dir.beta_rows, *areafactor = fp + dir.areafactor, *Ntime = fp + dir.Ntime;
-	const float *geo = fp + dir.geo_spline, *efoi_spline = fp + dir.efoi_spline, *efoi_age = fp + dir.efoi_agedist;
-	const double *obs_spline = b.fpool + dir.obs_spline;
-	const int32_t *beta_row_of = ip + dir.beta_row_of, *efoi_ref = ip + dir.efoi_ref;
+	Tabs tb;
+	{
+		const float *fp = b.fpool32;
+		tb.rate = fp + dir.transrate; tb.sus = fp + dir.susceptibility; tb.inf = fp + dir.infectivity;
+		tb.beta_rows = fp + dir.beta_rows; tb.areafactor = fp + dir.areafactor; tb.Ntime = fp + dir.Ntime;
+		tb.geo = fp + dir.geo_spline; tb.efoi_spline = fp + dir.efoi_spline; tb.efoi_age = fp + dir.efoi_agedist;
+		tb.obs_spline = fp + dir.obs_spline;
+		tb.beta_row_of = b.ipool + dir.beta_row_of; tb.efoi_ref = b.ipool + dir.efoi_ref;
+	}
 	int32_t *status = b.status + p;
 
 	FastSmem s;
@@ -216,52 +264,74 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 		size_t off = 0;
 		auto take = [&](size_t bytes) { unsigned char *q = smem_raw + off; off += (bytes + 15) & ~(size_t)15; return q; };
 		s.Ms = b.m_in_smem ? (float *)take(sizeof(float) * A * lda) : nullptr;
-		s.pop[0] = (int32_t *)take(sizeof(int32_t) * popsz);
-		s.pop[1] = (int32_t *)take(sizeof(int32_t) * popsz);
-		s.tn = (int32_t *)take(sizeof(int32_t) * tnsz);
-		s.Icnt[0] = (float *)take(sizeof(float) * agsz);
-		s.Icnt[1] = (float *)take(sizeof(float) * agsz);
-		s.Imap = (float *)take(sizeof(float) * agsz);
-		s.slot = (float *)take(sizeof(float) * b.nslots);
-		s.red = (float *)take(sizeof(float) * 2 * NT);
+		s.pop0 = (int32_t *)take(4 * (size_t)popsz);
+		s.pop1 = (int32_t *)take(4 * (size_t)popsz);
+		s.tn = (int32_t *)take(4 * (size_t)tnsz);
+		s.Ic0 = (float *)take(4 * (size_t)agsz);
+		s.Ic1 = (float *)take(4 * (size_t)agsz);
+		s.Imap = (float *)take(4 * (size_t)agsz);
+		s.slot = (float *)take(4 * (size_t)b.nslots);
+		s.from = (int32_t *)take(4 * (size_t)T);
+		s.to = (int32_t *)take(4 * (size_t)T);
+		s.age = (int32_t *)take(4 * (size_t)DPS);
+		s.inf = (float *)take(4 * (size_t)C);
+		s.rate = (float *)take(4 * (size_t)T * DP);
+		s.sus = (float *)take(4 * (size_t)DP);
+		s.rcp = (float *)take(4 * 64);
+		s.lnfact = (float *)take(4 * 32);
+		s.be = (float *)take(4 * (size_t)NS * A);
+		s.eta = (float *)take(4 * (size_t)agsz);
+		s.N = (float *)take(4 * (size_t)G * G);
+		s.red = (float *)take(4 * 2 * (size_t)NT);
 	}
 	if (s.Ms)
 		for (int k = tid; k < A * A; k += NT) s.Ms[(k / A) * lda + k % A] = m.Mdense[k];
-	for (int k = tid; k < popsz; k += NT) s.pop[0][k] = b.ti == 0 ? m.pop_init[k] : b.pop_in[(size_t)p * popsz + k];
+	for (int k = tid; k < popsz; k += NT) {
+		// global layout [c][co][dp] -> shared [co][c*DP+dp]
+		const int dp = k % DP, co = (k / DP) % C, c = k / (DP * C);
+		s.pop0[co * ncol + c * DP + dp] = b.ti == 0 ? m.pop_init[k] : b.pop_in[(size_t)p * popsz + k];
+	}
 	for (int k = tid; k < b.nslots; k += NT) s.slot[k] = 0.f;
-	for (int k = tid; k < agsz; k += NT) s.Icnt[1][k] = 0.f;
+	for (int k = tid; k < agsz; k += NT) s.Ic1[k] = 0.f;
+	for (int k = tid; k < T; k += NT) { s.from[k] = m.trans_from[k]; s.to[k] = m.trans_to[k]; }
+	for (int k = tid; k < DPS; k += NT) s.age[k] = m.dp_age[k];
+	for (int k = tid; k < C; k += NT) s.inf[k] = tb.inf[k];
+	for (int k = tid; k < T * DP; k += NT) s.rate[k] = tb.rate[k];
+	for (int k = tid; k < DP; k += NT) s.sus[k] = tb.sus[k];
+	for (int k = tid; k < 64; k += NT) s.rcp[k] = k == 0 ? 0.f : 1.f / (float)k;
+	for (int k = tid; k < 32; k += NT) s.lnfact[k] = (float)lgamma((double)k + 1.0);
 	__syncthreads();
 	// infectious counts of the start populations (set_I_from_pop, src/state.cc:223-290)
 	for (int idx = tid; idx < agsz; idx += NT) {
 		const int a = idx % G, c = (idx / G) % A, st = idx / (G * A);
 		float v = 0.f;
 		for (int co = 0; co < C; co++) {
-			const float inf = infectivity[co];
+			const float inf = s.inf[co];
 			if (inf != 0.f)
 				for (int dp = 0; dp < DPS; dp++)
-					if (m.dp_age[dp] == a) v += inf * (float)s.pop[0][(c * C + co) * DP + st * DPS + dp];
+					if (s.age[dp] == a) v += inf * (float)s.pop0[co * ncol + c * DP + st * DPS + dp];
 		}
-		s.Icnt[0][idx] = v;
+		s.Ic0[idx] = v;
 	}
+	stage_step<NT>(m, tb, s, b.ti, tid);
 	__syncthreads();
-	foi<NT, kMaxG>(m, s.Ms, lda, s.Icnt[0], s.Imap, tid);
+	foi<NT, MG>(m, s.Ms, lda, s.Ic0, s.Imap, tid);
 	float Lsum = 0.f, Lcmp = 0.f;           // compensated per-thread log-likelihood
 	__syncthreads();
 
 	const int itr = m.infection_trans;
 	const int inf_from = m.trans_from[itr];
 	const float dt = (float)m.dt;
-	const float inv_popsize = (float)(1.0 / m.popsize);
-	int cur = 0;
+	bool cur = false;
 	for (int sett = b.ti; sett < b.tf; sett++) {
-		int32_t *pc = cur ? s.pop[1] : s.pop[0], *pn = cur ? s.pop[0] : s.pop[1];
-		const float *Ic_cur = cur ? s.Icnt[1] : s.Icnt[0];
-		float *Ic_nxt = cur ? s.Icnt[0] : s.Icnt[1];
+		int32_t *pc = cur ? s.pop1 : s.pop0, *pn = cur ? s.pop0 : s.pop1;
+		const float *Ic_cur = cur ? s.Ic1 : s.Ic0;
+		float *Ic_nxt = cur ? s.Ic0 : s.Ic1;
 		if (NS > 1) {
 			// strain shift of the susceptible population (src/state.cc:392-401)
 			for (int idx = tid; idx < A * DPS; idx += NT) {
 				const int dp = idx % DPS, c = idx / DPS;
-				int32_t *sp = pc + (c * C + inf_from) * DP;
+				int32_t *sp = pc + inf_from * ncol + c * DP;
 				int32_t sum = 0;
 				for (int st = 1; st < NS; st++) { sum += sp[DPS * st + dp]; sp[DPS * st + dp] = 0; }
 				sp[dp] += sum;
@@ -269,82 +339,87 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 			__syncthreads();
 		}
 
-		// ---- A: per column (c, dp): NMI, means, draws, next population, next infectious count
-		const float d = geo[sett], omd = 1.f - d;
+		// ---- A: per column (c, dp): NMI, means, draws, next population and infectious count
+		const float d = s.red[0], omd = 1.f - d;
 		for (int col = tid; col < ncol; col += NT) {
-			const int c = col / DP, dp = col % DP;
-			const int st = dp / DPS, dpl = dp % DPS, a = m.dp_age[dpl];
+			const int c = col / DP, dp = col - c * DP;
+			const int st = dp / DPS, dpl = dp - st * DPS, a = s.age[dpl];
 			U4 inv{0, 0, 0, 0};
 			uint32_t inv_call = 0xffffffffu;
-			int32_t *pcol = pc + c * C * DP + dp, *ncol_p = pn + c * C * DP + dp;
-			for (int co = 0; co < C; co++) ncol_p[co * DP] = pcol[co * DP];
+			for (int co = 0; co < C; co++) pn[co * ncol + col] = pc[co * ncol + col];
 			for (int tr = 0; tr < T; tr++) {
 				float mean;
 				if (tr == itr) {
-					const float popu = (float)pc[(c * C + inf_from) * DP + dpl];
+					const float popu = (float)pc[inf_from * ncol + c * DP + dpl];
 					if (popu <= 0.f) mean = 0.f;
 					else {
 						const float fac = m.M_factor_f[c], dg = m.M_diag_f[c];
 						const float *Ic = Ic_cur + (st * A + c) * G, *Im = s.Imap + (st * A + c) * G;
-						const float *N = Ntime + ((size_t)sett * G + a) * G;
+						const float *N = s.N + a * G;
 						float nmi = 0.f;
-						for (int aa = 0; aa < G; aa++) {
-							const float id = Ic[aa] * dg;
-							nmi = fmaf(N[aa], (id + Im[aa]) * d + fac * id * omd, nmi);
+#pragma unroll
+						for (int aa = 0; aa < MG; aa++) {
+							if (aa < G) {
+								const float id = Ic[aa] * dg;
+								nmi = fmaf(N[aa], (id + Im[aa]) * d + fac * id * omd, nmi);
+							}
 						}
 						nmi = fmaxf(nmi, 0.f);
-						const float be = beta_rows[(size_t)beta_row_of[st * A + c] * m.S + sett] *
-						                 areafactor[(size_t)(sett / m.div_per_time) * A + c];
-						const int ei = efoi_ref[st * A + c];
-						const float eta = efoi_spline[(size_t)ei * m.S + sett] * inv_popsize * efoi_age[(size_t)ei * G + a];
-						mean = dt * popu * sus[dp] * (be * nmi + eta);
+						mean = dt * popu * s.sus[dp] * (s.be[st * A + c] * nmi + s.eta[(st * A + c) * G + a]);
 					}
 				} else {
-					const float popu = (float)pcol[m.trans_from[tr] * DP];
-					mean = popu <= 0.f ? 0.f : dt * popu * transrate[tr * DP + dp];
+					const float popu = (float)pc[s.from[tr] * ncol + col];
+					mean = popu <= 0.f ? 0.f : dt * popu * s.rate[tr * DP + dp];
 				}
 				int32_t n = 0;
-				if (mean != mean) atomicCAS(status, 0, BEEP_NAN_RATE);
-				else if (mean > 0.f) {
+				if (mean > 0.f) {
 					if (mean > 1.0e9f) atomicCAS(status, 0, BEEP_COUNT_OVERFLOW);
 					else {
-						n = poisson_fp32(mean, b.k0, b.k1, (uint32_t)col, (uint32_t)tr, (uint32_t)sett, stream, inv, inv_call);
+						n = poisson_fp32(mean, b.k0, b.k1, (uint32_t)col, (uint32_t)tr, (uint32_t)sett, stream, inv, inv_call,
+						                 s.rcp, s.lnfact);
 						if (n < 0) { atomicCAS(status, 0, BEEP_TIMEOUT); n = 0; }
 					}
-				}
-				s.tn[(c * T + tr) * DP + dp] = n;
+				} else if (mean != mean) atomicCAS(status, 0, BEEP_NAN_RATE);
+				s.tn[tr * ncol + col] = n;
 				if (n != 0) {
-					ncol_p[m.trans_from[tr] * DP] -= n;
-					ncol_p[m.trans_to[tr] * DP] += n;
+					pn[s.from[tr] * ncol + col] -= n;
+					pn[s.to[tr] * ncol + col] += n;
 				}
 			}
 			float iv = 0.f;
 			for (int co = 0; co < C; co++) {
-				const float inf = infectivity[co];
-				if (inf != 0.f) iv = fmaf(inf, (float)ncol_p[co * DP], iv);
+				const float inf = s.inf[co];
+				if (inf != 0.f) iv = fmaf(inf, (float)pn[co * ncol + col], iv);
 			}
 			if (m.dp_age_unique) Ic_nxt[(st * A + c) * G + a] = iv;
 			else atomicAdd(Ic_nxt + (st * A + c) * G + a, iv);
 		}
 		__syncthreads();
 
-		// ---- B: observation sums of the step (completed ones -> log-density); FOI for the next step
+		// ---- B: observation sums of the step (completed ones -> log-density),
+		//         next step's table slices and force of infection
 		if (b.pop_traj)
-			for (int k = tid; k < popsz; k += NT) b.pop_traj[((size_t)p * nsteps + (sett - b.ti)) * popsz + k] = pc[k];
+			for (int k = tid; k < popsz; k += NT) {
+				const int dp = k % DP, co = (k / DP) % C, c = k / (DP * C);
+				b.pop_traj[((size_t)p * nsteps + (sett - b.ti)) * popsz + k] = pc[co * ncol + c * DP + dp];
+			}
 		if (b.tn_traj)
-			for (int k = tid; k < tnsz; k += NT) b.tn_traj[((size_t)p * nsteps + (sett - b.ti)) * tnsz + k] = s.tn[k];
+			for (int k = tid; k < tnsz; k += NT) {
+				const int dp = k % DP, tr = (k / DP) % T, c = k / (DP * T);
+				b.tn_traj[((size_t)p * nsteps + (sett - b.ti)) * tnsz + k] = s.tn[tr * ncol + c * DP + dp];
+			}
 		const int a0 = b.step_ptr[sett - b.ti], a1 = b.step_ptr[sett - b.ti + 1];
 		for (int k = a0 + tid; k < a1; k += NT) {
 			const int pos = b.step_obs[k];
 			const int o = b.scored[pos];
-			const float fac = (float)m.obs_factor[o];
+			const float fac = m.obs_factor_f[o];
 			const int spl = m.obs_spline[o];
 			const int sl = b.slot_of[pos];
 			float v = s.slot[sl];
 			for (int q = m.obs_cell_ptr[o]; q < m.obs_cell_ptr[o + 1]; q++) {
-				const int cell = m.obs_cells[q];
+				const int cell = m.obs_cells_f[q];
 				const float num = cell >= 0 ? (float)s.tn[cell] : (float)pc[-1 - cell];
-				v += spl < 0 ? fac * num : fac * num * (float)obs_spline[(size_t)spl * m.S + sett];
+				v += spl < 0 ? fac * num : fac * num * tb.obs_spline[(size_t)spl * m.S + sett];
 			}
 			if (sett == m.obs_sett_f[o] - 1) {
 				const float lp = obs_lp_fast(v, o, m);
@@ -357,15 +432,22 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 			s.slot[sl] = v;
 		}
 		if (!m.dp_age_unique)
-			for (int k = tid; k < agsz; k += NT) (cur ? s.Icnt[1] : s.Icnt[0])[k] = 0.f;   // next step's accumulation target
-		foi<NT, kMaxG>(m, s.Ms, lda, Ic_nxt, s.Imap, tid);
+			for (int k = tid; k < agsz; k += NT) (cur ? s.Ic1 : s.Ic0)[k] = 0.f;   // next step's accumulation target
+		if (sett + 1 < b.tf) stage_step<NT>(m, tb, s, sett + 1, tid);
+		foi<NT, MG>(m, s.Ms, lda, Ic_nxt, s.Imap, tid);
 		__syncthreads();
-		cur ^= 1;
+		cur = !cur;
 	}
 
-	if (b.pop_out)
-		for (int k = tid; k < popsz; k += NT) b.pop_out[(size_t)p * popsz + k] = (cur ? s.pop[1] : s.pop[0])[k];
+	if (b.pop_out) {
+		const int32_t *pf = cur ? s.pop1 : s.pop0;
+		for (int k = tid; k < popsz; k += NT) {
+			const int dp = k % DP, co = (k / DP) % C, c = k / (DP * C);
+			b.pop_out[(size_t)p * popsz + k] = pf[co * ncol + c * DP + dp];
+		}
+	}
 	if (b.L) {
+		__syncthreads();
 		s.red[tid] = Lsum;
 		s.red[NT + tid] = Lcmp;
 		__syncthreads();
@@ -383,34 +465,43 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 
 }  // namespace
 
+static int pick_threads(const ModelDev &m)
+{
+	const int ncol = m.A * m.DP;
+	return ncol <= 128 ? 128 : ncol <= 256 ? 256 : 640;
+}
+
 size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem)
 {
 	auto r = [](size_t x) { return (x + 15) & ~(size_t)15; };
-	const size_t agsz = (size_t)m.NS * m.A * m.G;
-	return (m_in_smem ? r(4 * (size_t)m.A * ms_lda(m.A)) : 0) + 2 * r(4 * (size_t)m.A * m.C * m.DP) +
-	       r(4 * (size_t)m.A * m.T * m.DP) + 3 * r(4 * agsz) + r(4 * (size_t)nslots) + r(4 * 2 * (size_t)kFastThreads);
+	const size_t A = m.A, G = m.G, DP = m.DP, NS = m.NS, C = m.C, T = m.T, DPS = m.DPS;
+	const size_t agsz = NS * A * G, ncol = A * DP;
+	return (m_in_smem ? r(4 * A * ms_lda(m.A)) : 0) + 2 * r(4 * C * ncol) + r(4 * T * ncol) + 4 * r(4 * agsz) +
+	       r(4 * (size_t)nslots) + 2 * r(4 * T) + r(4 * DPS) + r(4 * C) + r(4 * T * DP) + r(4 * DP) + r(4 * 64) +
+	       r(4 * 32) + r(4 * NS * A) + r(4 * G * G) + r(4 * 2 * (size_t)pick_threads(m));
 }
 
 int fast_threads() { return kFastThreads; }
 
+template <int NT>
+static int launch_nt(const ModelDev &m, const BatchDev &b, size_t smem, cudaStream_t st)
+{
+	auto kern = m.G <= 4 ? sim_fast_kernel<NT, 4> : sim_fast_kernel<NT, 16>;
+	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	if (e != cudaSuccess) return (int)e;
+	kern<<<b.P, NT, smem, st>>>(m, b);
+	return (int)cudaGetLastError();
+}
+
 int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream)
 {
-	static bool init = false;
-	if (!init) {
-		float rcp[256];
-		rcp[0] = 0.f;
-		for (int k = 1; k < 256; k++) rcp[k] = 1.0f / (float)k;
-		cudaMemcpyToSymbol(c_rcp, rcp, sizeof rcp);
-		init = true;
-	}
 	if (b.P == 0) return 0;
 	if (m.G > 16) return (int)cudaErrorInvalidValue;
 	const size_t smem = fast_smem_bytes(m, b.nslots, b.m_in_smem != 0);
-	auto kern = m.G <= 4 ? sim_fast_kernel<kFastThreads, 4> : sim_fast_kernel<kFastThreads, 16>;
-	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-	if (e != cudaSuccess) return (int)e;
-	kern<<<b.P, kFastThreads, smem, (cudaStream_t)stream>>>(m, b);
-	return (int)cudaGetLastError();
+	const int nt = pick_threads(m);
+	cudaStream_t st = (cudaStream_t)stream;
+	return nt == 128 ? launch_nt<128>(m, b, smem, st) : nt == 256 ? launch_nt<256>(m, b, smem, st)
+	                                                               : launch_nt<640>(m, b, smem, st);
 }
 
 }  // namespace beep
