@@ -194,7 +194,8 @@ _LIB = None
 
 
 def library_path() -> str:
-    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "libbeep_gpu.so")
+    """In-tree libbeep_gpu.so; BEEP_GPU_LIB overrides the path (for instrumented builds)."""
+    return os.environ.get("BEEP_GPU_LIB") or os.path.join(os.path.dirname(os.path.abspath(__file__)), "libbeep_gpu.so")
 
 
 def lib():

@@ -36,6 +36,7 @@ struct ModelDev {
 	const int32_t *obs_cells_f;          // cells in the fast form's column-major shared layout:
 	                                     // tr*ncol + col (transition) or -1-(co*ncol + col) (population)
 	int32_t dp_age_unique;               // each age has exactly one dp per strain
+	float inv_popsize_f;                 // 1 / Data::popsize
 };
 
 // One parameter set's tables: offsets into the batch's table pool (doubles /
@@ -62,10 +63,9 @@ struct BatchDev {
 	const int32_t *step_ptr;            // [tf-ti+1]
 	const int32_t *step_obs;            // scored-position of obs active at each step
 	// fast form: observation accumulator slots and completion lists
-	int32_t nslots, m_in_smem;
-	const int32_t *slot_of;             // [nscored] slot of each scored observation
-	const int32_t *end_ptr;             // [tf-ti+1]
-	const int32_t *end_pos;             // scored-positions completing at each step
+	int32_t nslots, m_in_smem, nefoi_stage;   // nefoi_stage: efoi age tables staged in shared memory (0 = read from L2)
+	const int4 *tasks;                  // [2 * step_ptr[tf-ti]] per (step, active observation):
+	                                    // {slot, obs, first cell, ncell | last<<31}, {factor bits, spline, cell offset, 0}
 	// per-particle work (device)
 	int32_t *pop_a, *pop_b;             // [P][A][C][DP]
 	int32_t *tn;                        // [P][A][T][DP] current step's counts (when not writing a trajectory)
@@ -82,7 +82,7 @@ struct BatchDev {
 // launchers
 int launch_sim_plain(const ModelDev &m, const BatchDev &b, void *stream);   // sim_plain.cu
 int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream);    // sim_fast.cu
-size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem);
+size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_stage);
 int fast_threads();
 
 }  // namespace beep

@@ -110,7 +110,8 @@ struct beep_model {
 	DevBuf model_mem;
 	// host copies used to prepare batches
 	int32_t A, G, DP, NS, C, T, S, period, dpt, nobs;
-	std::vector<int32_t> obs_sett_i, obs_sett_f, obs_spline, trans_from_h, trans_to_h;
+	std::vector<int32_t> obs_sett_i, obs_sett_f, obs_spline, trans_from_h, trans_to_h, obs_cell_ptr_h, obs_cells_f_h;
+	std::vector<float> obs_factor_f_h;
 	int32_t max_obs_spline = -1;
 	std::mutex mu;
 };
@@ -253,6 +254,9 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	m->obs_sett_f.assign(d->obs_sett_f, d->obs_sett_f + nobs);
 	m->obs_spline.assign(d->obs_factor_spline, d->obs_factor_spline + nobs);
 	for (int o = 0; o < nobs; o++) m->max_obs_spline = std::max(m->max_obs_spline, d->obs_factor_spline[o]);
+	m->obs_cell_ptr_h.assign(d->obs_cell_ptr, d->obs_cell_ptr + (nobs > 0 ? nobs + 1 : 0));
+	m->obs_cells_f_h.assign(obs_cells_f.begin(), obs_cells_f.begin() + ncells);
+	m->obs_factor_f_h.assign(obs_factor_f.begin(), obs_factor_f.begin() + nobs);
 	m->trans_from_h.assign(d->trans_from, d->trans_from + T);
 	m->trans_to_h.assign(d->trans_to, d->trans_to + T);
 	cudaGetDevice(&m->device);
@@ -316,6 +320,7 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	md.M_factor_f = (const float *)(base + o_mfc); md.csc_val_f = (const float *)(base + o_cvf);
 	md.obs_np = (const float2 *)(base + o_onp);
 	md.obs_value_f = (const float *)(base + o_ovf);
+	md.inv_popsize_f = (float)(1.0 / d->popsize);
 	md.obs_factor_f = (const float *)(base + o_off);
 	md.obs_shape_f = (const float *)(base + o_oshf);
 	md.obs_cells_f = (const int32_t *)(base + o_ocf);
@@ -434,7 +439,7 @@ struct beep_batch {
 	size_t in_size = 0, out_size = 0;
 	size_t o_f = 0, u_st = 0, u_L = 0, u_po = 0, u_tn = 0, u_pt = 0;
 	std::vector<GroupDir> dirs;
-	std::vector<int32_t> scored, step_ptr, step_obs, slot_of, end_ptr, end_pos;
+	std::vector<int32_t> scored, step_ptr, step_obs, slot_of, tasks;
 	BatchDev bd{};
 	cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 	bool pending = false;
@@ -472,8 +477,7 @@ beep_status stage_inputs(beep_batch *q)
 	       o_i = in.add(4 * pk.i.size()), o_go = in.add(b->group_of ? 4 * (size_t)P : 0),
 	       o_so = in.add(b->stream_of ? 4 * (size_t)P : 0), o_pin = in.add(b->ti > 0 ? 4 * popsz * P : 0),
 	       o_sc = in.add(4 * q->scored.size()), o_sp = in.add(4 * q->step_ptr.size()),
-	       o_sobs = in.add(4 * q->step_obs.size()), o_slot = in.add(4 * q->slot_of.size()),
-	       o_ep = in.add(4 * q->end_ptr.size()), o_epos = in.add(4 * q->end_pos.size());
+	       o_sobs = in.add(4 * q->step_obs.size()), o_tasks = in.add(4 * q->tasks.size());
 	CUDA_TRY(q->in_host.reserve(in.size));
 	CUDA_TRY(q->in_dev.reserve(in.size));
 	q->in_size = in.size;
@@ -487,9 +491,7 @@ beep_status stage_inputs(beep_batch *q)
 	if (!q->scored.empty()) memcpy(h + o_sc, q->scored.data(), 4 * q->scored.size());
 	memcpy(h + o_sp, q->step_ptr.data(), 4 * q->step_ptr.size());
 	if (!q->step_obs.empty()) memcpy(h + o_sobs, q->step_obs.data(), 4 * q->step_obs.size());
-	if (!q->slot_of.empty()) memcpy(h + o_slot, q->slot_of.data(), 4 * q->slot_of.size());
-	if (!q->end_ptr.empty()) memcpy(h + o_ep, q->end_ptr.data(), 4 * q->end_ptr.size());
-	if (!q->end_pos.empty()) memcpy(h + o_epos, q->end_pos.data(), 4 * q->end_pos.size());
+	if (!q->tasks.empty()) memcpy(h + o_tasks, q->tasks.data(), 4 * q->tasks.size());
 	// infectivity difference of each transition, Model::get_infectivity_dif (src/model.cc:820-823)
 	double *fpool = (double *)(h + o_f);
 	for (int g = 0; g < b->ngroup; g++) {
@@ -513,9 +515,7 @@ beep_status stage_inputs(beep_batch *q)
 	bd.step_ptr = (const int32_t *)(di + o_sp);
 	bd.step_obs = (const int32_t *)(di + o_sobs);
 	bd.fpool32 = fast ? (const float *)(di + o_f32) : nullptr;
-	bd.slot_of = (const int32_t *)(di + o_slot);
-	bd.end_ptr = (const int32_t *)(di + o_ep);
-	bd.end_pos = (const int32_t *)(di + o_epos);
+	bd.tasks = (const int4 *)(di + o_tasks);
 	return BEEP_OK;
 }
 
@@ -583,18 +583,34 @@ beep_status beep_batch_create(beep_model *m, const beep_sim_batch *b, beep_batch
 			std::push_heap(busy.begin(), busy.end(), cmp);
 		}
 		q->bd.nslots = nslots;
-		q->end_ptr.assign(nsteps + 1, 0);
-		for (int k = 0; k < nscored; k++) q->end_ptr[m->obs_sett_f[q->scored[k]] - 1 - b->ti + 1]++;
-		for (int s2 = 0; s2 < nsteps; s2++) q->end_ptr[s2 + 1] += q->end_ptr[s2];
-		q->end_pos.resize(nscored);
-		std::vector<int32_t> fill(q->end_ptr.begin(), q->end_ptr.end() - 1);
-		for (int k = 0; k < nscored; k++) q->end_pos[fill[m->obs_sett_f[q->scored[k]] - 1 - b->ti]++] = k;
+		// one 32-byte task per (step, active observation), in step_obs order:
+		// {slot, obs, first cell, ncell | last<<31}, {factor bits, spline, cell offset, 0}
+		q->tasks.resize((size_t)8 * q->step_obs.size());
+		for (int s2 = 0; s2 < nsteps; s2++)
+			for (int k = q->step_ptr[s2]; k < q->step_ptr[s2 + 1]; k++) {
+				const int pos = q->step_obs[k], o = q->scored[pos];
+				const int c0 = m->obs_cell_ptr_h[o], nc = m->obs_cell_ptr_h[o + 1] - c0;
+				const bool last = b->ti + s2 == m->obs_sett_f[o] - 1;
+				int32_t *t = &q->tasks[(size_t)8 * k];
+				float fac = m->obs_factor_f_h[o];
+				int32_t fbits;
+				memcpy(&fbits, &fac, 4);
+				t[0] = q->slot_of[pos]; t[1] = o; t[2] = nc > 0 ? m->obs_cells_f_h[c0] : 0;
+				t[3] = (int32_t)((uint32_t)nc | (last ? 0x80000000u : 0u));
+				t[4] = fbits; t[5] = m->obs_spline[o]; t[6] = c0; t[7] = 0;
+			}
 		const size_t limit = 227 * 1024;
-		if (fast_smem_bytes(m->dev, nslots, false) > limit) {
+		int nefoi = 1 << 30;
+		for (int g = 0; g < b->ngroup; g++) nefoi = std::min(nefoi, (int)b->groups[g].nefoi);
+		if (b->ngroup > 1)
+			for (int g = 1; g < b->ngroup; g++)
+				if (b->groups[g].nefoi != b->groups[0].nefoi) nefoi = 0;
+		q->bd.nefoi_stage = nefoi * m->G <= 1024 ? nefoi : 0;
+		if (fast_smem_bytes(m->dev, nslots, false, q->bd.nefoi_stage) > limit || m->NS * m->A > 640 || m->G * m->G > 640) {
 			delete q;
 			return fail(BEEP_BAD_INPUT, "model too large for the particle-resident fast form (shared memory)");
 		}
-		q->bd.m_in_smem = fast_smem_bytes(m->dev, nslots, true) <= limit ? 1 : 0;
+		q->bd.m_in_smem = fast_smem_bytes(m->dev, nslots, true, q->bd.nefoi_stage) <= limit ? 1 : 0;
 	}
 	auto bail = [&](beep_status s) { beep_batch_destroy(q); return s; };
 	st = stage_inputs(q);

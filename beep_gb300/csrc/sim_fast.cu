@@ -36,6 +36,8 @@ namespace {
 
 constexpr int kFastThreads = 640;   // largest CTA; smaller models use 128 or 256 threads
 
+__constant__ float c_lnfact[32];   // log k!, k < 32
+
 __device__ __forceinline__ float u01_f(uint32_t w)
 {
 	return __uint2float_rn(w) * 2.3283064365386963e-10f + 1.1641532182693481e-10f;
@@ -59,11 +61,14 @@ struct FastSmem {
 	float *sus;           // [DP]
 	float *rcp;           // [64] 1/k
 	float *lnfact;        // [32] log k!
-	// per-step slices (step being simulated)
-	float *be;            // [NS][A] beta * areafactor
-	float *eta;           // [NS][A][G] external force of infection per capita
-	float *N;             // [G][G] age mixing
-	float *red;           // [2*NT]; red[0] also carries the geo spline value d
+	int32_t *brow, *eref; // [NS][A] beta row and efoi spline of each (strain, area)
+	float *eage;          // [nefoi][G] efoi age distributions (when they fit)
+	// per-step slices, double-buffered: [0] the step simulated, [1] the next one
+	float *be0, *be1;     // [NS][A] beta * areafactor
+	float *et0, *et1;     // [NS][A] external force of infection per capita (before the age factor)
+	float *N0, *N1;       // [G][G] age mixing
+	float *dgeo;          // [2] geographic spline value
+	float *red;           // [2*NT]
 };
 
 __host__ __device__ inline int ms_lda(int A) { return A + ((40 - A % 32) % 32); }
@@ -216,23 +221,37 @@ struct Tabs {
 	const int32_t *beta_row_of, *efoi_ref;
 };
 
-// Per-step table slices for step sett: beta*areafactor per (strain, area), the
-// external force of infection per (strain, area, age), the age-mixing matrix
-// and the geographic spline (src/state.cc:403-423, 547-553).
+// Per-step table slices: beta*areafactor and the external force of infection
+// per (strain, area), the age-mixing matrix and the geographic spline
+// (src/state.cc:403-423, 547-553).  The loads for step sett are issued by
+// slice_load early in the previous step's draw phase (their latency hides
+// behind the draws) and stored by slice_store after it.
+struct SliceRegs {
+	float be, et, N, d;
+};
+
 template <int NT>
-__device__ __forceinline__ void stage_step(const ModelDev &m, const Tabs &tb, FastSmem &s, int sett, int tid)
+__device__ __forceinline__ SliceRegs slice_load(const ModelDev &m, const Tabs &tb, const FastSmem &s, int sett, int tid)
 {
-	const int A = m.A, G = m.G, NSA = m.NS * m.A;
-	const float inv_popsize = (float)(1.0 / m.popsize);
-	for (int k = tid; k < NSA; k += NT) {
-		const int c = k % A;
-		s.be[k] = tb.beta_rows[(size_t)tb.beta_row_of[k] * m.S + sett] * tb.areafactor[(size_t)(sett / m.div_per_time) * A + c];
-		const int ei = tb.efoi_ref[k];
-		const float et = tb.efoi_spline[(size_t)ei * m.S + sett] * inv_popsize;
-		for (int a = 0; a < G; a++) s.eta[k * G + a] = et * tb.efoi_age[(size_t)ei * G + a];
+	SliceRegs r{0.f, 0.f, 0.f, 0.f};
+	const int A = m.A, NSA = m.NS * m.A, G = m.G;
+	if (tid < NSA) {
+		const int c = tid % A;
+		r.be = __ldg(tb.beta_rows + (size_t)s.brow[tid] * m.S + sett) *
+		       __ldg(tb.areafactor + (size_t)(sett / m.div_per_time) * A + c);
+		r.et = __ldg(tb.efoi_spline + (size_t)s.eref[tid] * m.S + sett) * m.inv_popsize_f;
 	}
-	for (int k = tid; k < G * G; k += NT) s.N[k] = tb.Ntime[(size_t)sett * G * G + k];
-	if (tid == 0) s.red[0] = tb.geo[sett];
+	if (tid < G * G) r.N = __ldg(tb.Ntime + (size_t)sett * G * G + tid);
+	if (tid == 0) r.d = __ldg(tb.geo + sett);
+	return r;
+}
+
+template <int NT>
+__device__ __forceinline__ void slice_store(const ModelDev &m, FastSmem &s, const SliceRegs &r, int buf, int tid)
+{
+	if (tid < m.NS * m.A) { (buf ? s.be1 : s.be0)[tid] = r.be; (buf ? s.et1 : s.et0)[tid] = r.et; }
+	if (tid < m.G * m.G) (buf ? s.N1 : s.N0)[tid] = r.N;
+	if (tid == 0) s.dgeo[buf] = r.d;
 }
 
 template <int NT, int MG>
@@ -279,9 +298,16 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 		s.sus = (float *)take(4 * (size_t)DP);
 		s.rcp = (float *)take(4 * 64);
 		s.lnfact = (float *)take(4 * 32);
-		s.be = (float *)take(4 * (size_t)NS * A);
-		s.eta = (float *)take(4 * (size_t)agsz);
-		s.N = (float *)take(4 * (size_t)G * G);
+		s.brow = (int32_t *)take(4 * (size_t)NS * A);
+		s.eref = (int32_t *)take(4 * (size_t)NS * A);
+		s.eage = (float *)take(4 * (size_t)b.nefoi_stage * G);
+		s.be0 = (float *)take(4 * (size_t)NS * A);
+		s.et0 = (float *)take(4 * (size_t)NS * A);
+		s.N0 = (float *)take(4 * (size_t)G * G);
+		s.be1 = (float *)take(4 * (size_t)NS * A);
+		s.et1 = (float *)take(4 * (size_t)NS * A);
+		s.N1 = (float *)take(4 * (size_t)G * G);
+		s.dgeo = (float *)take(4 * 2);
 		s.red = (float *)take(4 * 2 * (size_t)NT);
 	}
 	if (s.Ms)
@@ -299,7 +325,9 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 	for (int k = tid; k < T * DP; k += NT) s.rate[k] = tb.rate[k];
 	for (int k = tid; k < DP; k += NT) s.sus[k] = tb.sus[k];
 	for (int k = tid; k < 64; k += NT) s.rcp[k] = k == 0 ? 0.f : 1.f / (float)k;
-	for (int k = tid; k < 32; k += NT) s.lnfact[k] = (float)lgamma((double)k + 1.0);
+	for (int k = tid; k < 32; k += NT) s.lnfact[k] = c_lnfact[k];
+	for (int k = tid; k < NS * A; k += NT) { s.brow[k] = tb.beta_row_of[k]; s.eref[k] = tb.efoi_ref[k]; }
+	for (int k = tid; k < b.nefoi_stage * G; k += NT) s.eage[k] = tb.efoi_age[k];
 	__syncthreads();
 	// infectious counts of the start populations (set_I_from_pop, src/state.cc:223-290)
 	for (int idx = tid; idx < agsz; idx += NT) {
@@ -313,7 +341,7 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 		}
 		s.Ic0[idx] = v;
 	}
-	stage_step<NT>(m, tb, s, b.ti, tid);
+	slice_store<NT>(m, s, slice_load<NT>(m, tb, s, b.ti, tid), 0, tid);
 	__syncthreads();
 	foi<NT, MG>(m, s.Ms, lda, s.Ic0, s.Imap, tid);
 	float Lsum = 0.f, Lcmp = 0.f;           // compensated per-thread log-likelihood
@@ -323,8 +351,11 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 	const int inf_from = m.trans_from[itr];
 	const float dt = (float)m.dt;
 	bool cur = false;
+	int sb = 0;                                          // slice buffer of the step simulated
 	for (int sett = b.ti; sett < b.tf; sett++) {
 		int32_t *pc = cur ? s.pop1 : s.pop0, *pn = cur ? s.pop0 : s.pop1;
+		const SliceRegs nxt = sett + 1 < b.tf ? slice_load<NT>(m, tb, s, sett + 1, tid) : SliceRegs{0.f, 0.f, 0.f, 0.f};
+		const float *be = sb ? s.be1 : s.be0, *et = sb ? s.et1 : s.et0, *Nm = sb ? s.N1 : s.N0;
 		const float *Ic_cur = cur ? s.Ic1 : s.Ic0;
 		float *Ic_nxt = cur ? s.Ic0 : s.Ic1;
 		if (NS > 1) {
@@ -340,7 +371,7 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 		}
 
 		// ---- A: per column (c, dp): NMI, means, draws, next population and infectious count
-		const float d = s.red[0], omd = 1.f - d;
+		const float d = s.dgeo[sb], omd = 1.f - d;
 		for (int col = tid; col < ncol; col += NT) {
 			const int c = col / DP, dp = col - c * DP;
 			const int st = dp / DPS, dpl = dp - st * DPS, a = s.age[dpl];
@@ -355,7 +386,7 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 					else {
 						const float fac = m.M_factor_f[c], dg = m.M_diag_f[c];
 						const float *Ic = Ic_cur + (st * A + c) * G, *Im = s.Imap + (st * A + c) * G;
-						const float *N = s.N + a * G;
+						const float *N = Nm + a * G;
 						float nmi = 0.f;
 #pragma unroll
 						for (int aa = 0; aa < MG; aa++) {
@@ -365,7 +396,9 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 							}
 						}
 						nmi = fmaxf(nmi, 0.f);
-						mean = dt * popu * s.sus[dp] * (s.be[st * A + c] * nmi + s.eta[(st * A + c) * G + a]);
+						const int sc = st * A + c;
+						const float eage = b.nefoi_stage ? s.eage[s.eref[sc] * G + a] : __ldg(tb.efoi_age + (size_t)s.eref[sc] * G + a);
+						mean = dt * popu * s.sus[dp] * (be[sc] * nmi + et[sc] * eage);
 					}
 				} else {
 					const float popu = (float)pc[s.from[tr] * ncol + col];
@@ -394,6 +427,7 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 			if (m.dp_age_unique) Ic_nxt[(st * A + c) * G + a] = iv;
 			else atomicAdd(Ic_nxt + (st * A + c) * G + a, iv);
 		}
+		if (sett + 1 < b.tf) slice_store<NT>(m, s, nxt, sb ^ 1, tid);
 		__syncthreads();
 
 		// ---- B: observation sums of the step (completed ones -> log-density),
@@ -410,33 +444,36 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 			}
 		const int a0 = b.step_ptr[sett - b.ti], a1 = b.step_ptr[sett - b.ti + 1];
 		for (int k = a0 + tid; k < a1; k += NT) {
-			const int pos = b.step_obs[k];
-			const int o = b.scored[pos];
-			const float fac = m.obs_factor_f[o];
-			const int spl = m.obs_spline[o];
-			const int sl = b.slot_of[pos];
-			float v = s.slot[sl];
-			for (int q = m.obs_cell_ptr[o]; q < m.obs_cell_ptr[o + 1]; q++) {
-				const int cell = m.obs_cells_f[q];
-				const float num = cell >= 0 ? (float)s.tn[cell] : (float)pc[-1 - cell];
-				v += spl < 0 ? fac * num : fac * num * tb.obs_spline[(size_t)spl * m.S + sett];
+			const int4 t0 = __ldg(b.tasks + 2 * k), t1 = __ldg(b.tasks + 2 * k + 1);
+			const float fac = __int_as_float(t1.x);
+			const int spl = t1.y;
+			const float w = spl < 0 ? fac : fac * tb.obs_spline[(size_t)spl * m.S + sett];
+			const int nc = t0.w & 0x7fffffff;
+			float v = s.slot[t0.x];
+			if (nc > 0) {
+				const int cell = t0.z;
+				v = fmaf(w, cell >= 0 ? (float)s.tn[cell] : (float)pc[-1 - cell], v);
 			}
-			if (sett == m.obs_sett_f[o] - 1) {
-				const float lp = obs_lp_fast(v, o, m);
+			for (int i = 1; i < nc; i++) {
+				const int cell = __ldg(m.obs_cells_f + t1.z + i);
+				v = fmaf(w, cell >= 0 ? (float)s.tn[cell] : (float)pc[-1 - cell], v);
+			}
+			if (t0.w < 0) {                  // the observation's last step: log-density
+				const float lp = obs_lp_fast(v, t0.y, m);
 				v = 0.f;
 				const float y = lp - Lcmp;      // Kahan
 				const float tt = Lsum + y;
 				Lcmp = (tt - Lsum) - y;
 				Lsum = tt;
 			}
-			s.slot[sl] = v;
+			s.slot[t0.x] = v;
 		}
 		if (!m.dp_age_unique)
 			for (int k = tid; k < agsz; k += NT) (cur ? s.Ic1 : s.Ic0)[k] = 0.f;   // next step's accumulation target
-		if (sett + 1 < b.tf) stage_step<NT>(m, tb, s, sett + 1, tid);
 		foi<NT, MG>(m, s.Ms, lda, Ic_nxt, s.Imap, tid);
 		__syncthreads();
 		cur = !cur;
+		sb ^= 1;
 	}
 
 	if (b.pop_out) {
@@ -471,14 +508,15 @@ static int pick_threads(const ModelDev &m)
 	return ncol <= 128 ? 128 : ncol <= 256 ? 256 : 640;
 }
 
-size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem)
+size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_stage)
 {
 	auto r = [](size_t x) { return (x + 15) & ~(size_t)15; };
 	const size_t A = m.A, G = m.G, DP = m.DP, NS = m.NS, C = m.C, T = m.T, DPS = m.DPS;
 	const size_t agsz = NS * A * G, ncol = A * DP;
-	return (m_in_smem ? r(4 * A * ms_lda(m.A)) : 0) + 2 * r(4 * C * ncol) + r(4 * T * ncol) + 4 * r(4 * agsz) +
+	return (m_in_smem ? r(4 * A * ms_lda(m.A)) : 0) + 2 * r(4 * C * ncol) + r(4 * T * ncol) + 3 * r(4 * agsz) +
 	       r(4 * (size_t)nslots) + 2 * r(4 * T) + r(4 * DPS) + r(4 * C) + r(4 * T * DP) + r(4 * DP) + r(4 * 64) +
-	       r(4 * 32) + r(4 * NS * A) + r(4 * G * G) + r(4 * 2 * (size_t)pick_threads(m));
+	       r(4 * 32) + 2 * r(4 * NS * A) + r(4 * (size_t)nefoi_stage * G) + 2 * (2 * r(4 * NS * A) + r(4 * G * G)) +
+	       r(8) + r(4 * 2 * (size_t)pick_threads(m));
 }
 
 int fast_threads() { return kFastThreads; }
@@ -497,8 +535,18 @@ int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream)
 {
 	if (b.P == 0) return 0;
 	if (m.G > 16) return (int)cudaErrorInvalidValue;
-	const size_t smem = fast_smem_bytes(m, b.nslots, b.m_in_smem != 0);
+	const size_t smem = fast_smem_bytes(m, b.nslots, b.m_in_smem != 0, b.nefoi_stage);
 	const int nt = pick_threads(m);
+	const int NSA = m.NS * m.A;
+	if (NSA > nt || m.G * m.G > nt) return (int)cudaErrorInvalidValue;   // slices: one item per thread
+	static bool init = false;
+	if (!init) {
+		float lf[32];
+		for (int k = 0; k < 32; k++) lf[k] = (float)std::lgamma((double)k + 1.0);
+		cudaError_t e = cudaMemcpyToSymbol(c_lnfact, lf, sizeof lf);
+		if (e != cudaSuccess) return (int)e;
+		init = true;
+	}
 	cudaStream_t st = (cudaStream_t)stream;
 	return nt == 128 ? launch_nt<128>(m, b, smem, st) : nt == 256 ? launch_nt<256>(m, b, smem, st)
 	                                                               : launch_nt<640>(m, b, smem, st);
