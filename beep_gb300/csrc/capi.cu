@@ -23,11 +23,11 @@
 #include <utility>
 #include <vector>
 
-#include "beep_internal.h"
+#include "capi_internal.h"
 
 using namespace beep;
 
-namespace {
+namespace beep {
 
 thread_local std::string g_err;
 
@@ -37,84 +37,25 @@ beep_status fail(beep_status s, const std::string &msg)
 	return s;
 }
 
-#define CUDA_TRY(expr)                                                                         \
-	do {                                                                                       \
-		cudaError_t e_ = (expr);                                                               \
-		if (e_ != cudaSuccess)                                                                 \
-			return fail(e_ == cudaErrorMemoryAllocation ? BEEP_OOM : BEEP_DEVICE_ERROR,        \
-			            std::string(#expr) + ": " + cudaGetErrorString(e_));                   \
-	} while (0)
-
-size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
-
-// A device buffer that only grows.
-struct DevBuf {
-	void *ptr = nullptr;
-	size_t cap = 0;
-	cudaError_t reserve(size_t n)
-	{
-		if (n <= cap) return cudaSuccess;
-		if (ptr) cudaFree(ptr);
-		ptr = nullptr;
-		cap = 0;
-		cudaError_t e = cudaMalloc(&ptr, n);
-		if (e == cudaSuccess) cap = n;
-		return e;
+void build_obs_lists(const int32_t *sett_i, const int32_t *sett_f, int nobs, int ti, int tf, ObsLists &out)
+{
+	const int nsteps = tf - ti;
+	out.scored.clear();
+	out.step_ptr.assign(nsteps + 1, 0);
+	for (int o = 0; o < nobs; o++)
+		if (sett_i[o] >= ti && sett_f[o] <= tf) out.scored.push_back(o);
+	for (int o : out.scored)
+		for (int s = sett_i[o]; s < sett_f[o]; s++) out.step_ptr[s - ti + 1]++;
+	for (int s = 0; s < nsteps; s++) out.step_ptr[s + 1] += out.step_ptr[s];
+	out.step_obs.resize(out.step_ptr[nsteps]);
+	std::vector<int32_t> fill(out.step_ptr.begin(), out.step_ptr.end() - 1);
+	for (size_t k = 0; k < out.scored.size(); k++) {
+		const int o = out.scored[k];
+		for (int s = sett_i[o]; s < sett_f[o]; s++) out.step_obs[fill[s - ti]++] = (int32_t)k;
 	}
-	void release()
-	{
-		if (ptr) cudaFree(ptr);
-		ptr = nullptr;
-		cap = 0;
-	}
-};
+}
 
-struct HostBuf {
-	void *ptr = nullptr;
-	size_t cap = 0;
-	cudaError_t reserve(size_t n)
-	{
-		if (n <= cap) return cudaSuccess;
-		if (ptr) cudaFreeHost(ptr);
-		ptr = nullptr;
-		cap = 0;
-		cudaError_t e = cudaMallocHost(&ptr, n);
-		if (e == cudaSuccess) cap = n;
-		return e;
-	}
-	void release()
-	{
-		if (ptr) cudaFreeHost(ptr);
-		ptr = nullptr;
-		cap = 0;
-	}
-};
-
-// Sequential layout of named regions inside one buffer.
-struct Layout {
-	size_t size = 0;
-	size_t add(size_t bytes)
-	{
-		size_t off = align_up(size, 256);
-		size = off + bytes;
-		return off;
-	}
-};
-
-}  // namespace
-
-struct beep_model {
-	int device = 0;
-	cudaStream_t stream = nullptr;
-	ModelDev dev{};
-	DevBuf model_mem;
-	// host copies used to prepare batches
-	int32_t A, G, DP, NS, C, T, S, period, dpt, nobs;
-	std::vector<int32_t> obs_sett_i, obs_sett_f, obs_spline, trans_from_h, trans_to_h, obs_cell_ptr_h, obs_cells_f_h;
-	std::vector<float> obs_factor_f_h;
-	int32_t max_obs_spline = -1;
-	std::mutex mu;
-};
+}  // namespace beep
 
 extern "C" {
 
@@ -538,21 +479,12 @@ beep_status beep_batch_create(beep_model *m, const beep_sim_batch *b, beep_batch
 	const size_t agsz = (size_t)m->NS * m->A * m->G;
 	const int nsteps = b->tf - b->ti;
 	// scored observations and the steps each is active in
-	q->step_ptr.assign(nsteps + 1, 0);
-	for (int o = 0; o < m->nobs; o++)
-		if (m->obs_sett_i[o] >= b->ti && m->obs_sett_f[o] <= b->tf) q->scored.push_back(o);
-	for (size_t k = 0; k < q->scored.size(); k++) {
-		int o = q->scored[k];
-		for (int s = m->obs_sett_i[o]; s < m->obs_sett_f[o]; s++) q->step_ptr[s - b->ti + 1]++;
-	}
-	for (int s = 0; s < nsteps; s++) q->step_ptr[s + 1] += q->step_ptr[s];
-	q->step_obs.resize(q->step_ptr[nsteps]);
 	{
-		std::vector<int32_t> fill(q->step_ptr.begin(), q->step_ptr.end() - 1);
-		for (size_t k = 0; k < q->scored.size(); k++) {
-			int o = q->scored[k];
-			for (int s = m->obs_sett_i[o]; s < m->obs_sett_f[o]; s++) q->step_obs[fill[s - b->ti]++] = (int32_t)k;
-		}
+		ObsLists ol;
+		build_obs_lists(m->obs_sett_i.data(), m->obs_sett_f.data(), m->nobs, b->ti, b->tf, ol);
+		q->scored.swap(ol.scored);
+		q->step_ptr.swap(ol.step_ptr);
+		q->step_obs.swap(ol.step_obs);
 	}
 	const int nscored = (int)q->scored.size();
 	if (b->form == BEEP_FORM_FAST) {

@@ -1,0 +1,105 @@
+// Host-side definitions shared by the C-ABI translation units: error text,
+// growable device/host buffers, buffer layouts and the model handle.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "beep_internal.h"
+
+namespace beep {
+
+// Records the message returned by beep_last_error() on this thread.
+beep_status fail(beep_status s, const std::string &msg);
+
+#define CUDA_TRY(expr)                                                                         \
+	do {                                                                                       \
+		cudaError_t e_ = (expr);                                                               \
+		if (e_ != cudaSuccess)                                                                 \
+			return ::beep::fail(e_ == cudaErrorMemoryAllocation ? BEEP_OOM : BEEP_DEVICE_ERROR, \
+			                    std::string(#expr) + ": " + cudaGetErrorString(e_));           \
+	} while (0)
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// A device buffer that only grows.
+struct DevBuf {
+	void *ptr = nullptr;
+	size_t cap = 0;
+	cudaError_t reserve(size_t n)
+	{
+		if (n <= cap) return cudaSuccess;
+		if (ptr) cudaFree(ptr);
+		ptr = nullptr;
+		cap = 0;
+		cudaError_t e = cudaMalloc(&ptr, n);
+		if (e == cudaSuccess) cap = n;
+		return e;
+	}
+	void release()
+	{
+		if (ptr) cudaFree(ptr);
+		ptr = nullptr;
+		cap = 0;
+	}
+};
+
+// A pinned host buffer that only grows.
+struct HostBuf {
+	void *ptr = nullptr;
+	size_t cap = 0;
+	cudaError_t reserve(size_t n)
+	{
+		if (n <= cap) return cudaSuccess;
+		if (ptr) cudaFreeHost(ptr);
+		ptr = nullptr;
+		cap = 0;
+		cudaError_t e = cudaMallocHost(&ptr, n);
+		if (e == cudaSuccess) cap = n;
+		return e;
+	}
+	void release()
+	{
+		if (ptr) cudaFreeHost(ptr);
+		ptr = nullptr;
+		cap = 0;
+	}
+};
+
+// Sequential layout of named regions inside one buffer (256-byte aligned).
+struct Layout {
+	size_t size = 0;
+	size_t add(size_t bytes)
+	{
+		size_t off = align_up(size, 256);
+		size = off + bytes;
+		return off;
+	}
+};
+
+// Scored observations of a step range and the steps each is active in
+// (positions into `scored`), as the kernels consume them.
+struct ObsLists {
+	std::vector<int32_t> scored, step_ptr, step_obs;
+};
+void build_obs_lists(const int32_t *sett_i, const int32_t *sett_f, int nobs, int ti, int tf, ObsLists &out);
+
+}  // namespace beep
+
+struct beep_model {
+	int device = 0;
+	cudaStream_t stream = nullptr;
+	beep::ModelDev dev{};
+	beep::DevBuf model_mem;
+	// host copies used to prepare batches
+	int32_t A, G, DP, NS, C, T, S, period, dpt, nobs;
+	std::vector<int32_t> obs_sett_i, obs_sett_f, obs_spline, trans_from_h, trans_to_h, obs_cell_ptr_h, obs_cells_f_h;
+	std::vector<float> obs_factor_f_h;
+	int32_t max_obs_spline = -1;
+	std::mutex mu;
+};
