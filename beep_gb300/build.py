@@ -27,6 +27,7 @@ UNITS = {
     "capi.cu": [],
     "sim_plain.cu": ["--fmad=false"],
     "sim_fast.cu": [],
+    "noalloc.cu": [],
 }
 
 

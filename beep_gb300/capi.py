@@ -221,6 +221,10 @@ def lib():
         L.beep_batch_launches.restype = C.c_int32
         L.beep_batch_bytes.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         L.beep_batch_bytes.restype = C.c_int32
+        L.beep_simulate_plain_noalloc.argtypes = [C.c_void_p, C.POINTER(ParamTables), C.c_int32, C.c_uint64,
+                                                  C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                  C.c_void_p]
+        L.beep_simulate_plain_noalloc.restype = C.c_int32
         for f in ("beep_device_init", "beep_model_create", "beep_model_destroy", "beep_simulate", "beep_batch_create",
                   "beep_batch_stage", "beep_batch_upload", "beep_batch_launch", "beep_batch_download",
                   "beep_batch_time", "beep_batch_destroy"):

@@ -200,6 +200,28 @@ BEEP_API int32_t beep_batch_launches(const beep_batch *batch);   /* kernels per 
 BEEP_API beep_status beep_batch_bytes(const beep_batch *batch, int64_t *h2d, int64_t *d2h);
 BEEP_API beep_status beep_batch_destroy(beep_batch *batch);
 
+/* Plain FP64 simulation that allocates no memory on the GPU.  No counterpart
+ * in the reference: it serves callers that cannot call cudaMalloc -- an
+ * application whose allocator or fixed memory budget owns all device memory,
+ * or code that must not trigger an allocation while it enqueues work.  The
+ * caller allocates and passes device pointers: the tables of one parameter
+ * set (every pointer in `tables` is a device pointer; the struct itself is in
+ * host memory), pop_in (when ti > 0), L_out [nparticle] and pop_out
+ * [nparticle][narea][ncomp][ndemocatpos] (either may be NULL).  Particle p
+ * uses variate stream p.  Working memory comes from one 64 MiB file-scope
+ * device array held by every GPU that loads the library; batches that need
+ * more are rejected with BEEP_BAD_INPUT (use fewer particles per call).  The
+ * first call on a device looks up the array's device address (make that call
+ * before any stream capture).  Calls share the array: the call clears what
+ * must start at zero, and calls that overlap on the GPU race.  The call
+ * enqueues on `stream` (a cudaStream_t, NULL = legacy default stream) and
+ * returns after the kernel finished, with its status.  Same results as
+ * beep_simulate with BEEP_FORM_PLAIN_FP64 on the same inputs. */
+BEEP_API beep_status beep_simulate_plain_noalloc(beep_model *model, const beep_param_tables *tables,
+                                                 int32_t nparticle, uint64_t seed, int32_t ti, int32_t tf,
+                                                 const int32_t *pop_in, double *L_out, int32_t *pop_out,
+                                                 void *stream);
+
 #ifdef __cplusplus
 }
 #endif
