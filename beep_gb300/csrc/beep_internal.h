@@ -63,7 +63,9 @@ struct BatchDev {
 	const int32_t *step_ptr;            // [tf-ti+1]
 	const int32_t *step_obs;            // scored-position of obs active at each step
 	// fast form: observation accumulator slots and completion lists
-	int32_t nslots, m_in_smem, nefoi_stage;   // nefoi_stage: efoi age tables staged in shared memory (0 = read from L2)
+	int32_t nslots, m_in_smem, nefoi_stage;
+	void *gstate;                       // fast form, large models: per-particle state in global memory (or null)
+	size_t gstate_stride;               // bytes per particle   // nefoi_stage: efoi age tables staged in shared memory (0 = read from L2)
 	const int4 *tasks;                  // [2 * step_ptr[tf-ti]] per (step, active observation):
 	                                    // {slot, obs, first cell, ncell | last<<31}, {factor bits, spline, cell offset, 0}
 	// per-particle work (device)
@@ -82,7 +84,8 @@ struct BatchDev {
 // launchers
 int launch_sim_plain(const ModelDev &m, const BatchDev &b, void *stream);   // sim_plain.cu
 int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream);    // sim_fast.cu
-size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_stage);
+size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_stage, bool state_global);
+size_t fast_gstate_stride(const ModelDev &m);
 int fast_threads();
 
 }  // namespace beep

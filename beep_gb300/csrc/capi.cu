@@ -384,6 +384,7 @@ struct beep_batch {
 	BatchDev bd{};
 	cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 	bool pending = false;
+	bool state_global = false;   // fast form keeps particle state in global memory
 };
 
 namespace {
@@ -538,11 +539,12 @@ beep_status beep_batch_create(beep_model *m, const beep_sim_batch *b, beep_batch
 			for (int g = 1; g < b->ngroup; g++)
 				if (b->groups[g].nefoi != b->groups[0].nefoi) nefoi = 0;
 		q->bd.nefoi_stage = nefoi * m->G <= 1024 ? nefoi : 0;
-		if (fast_smem_bytes(m->dev, nslots, false, q->bd.nefoi_stage) > limit || m->NS * m->A > 640 || m->G * m->G > 640) {
+		q->state_global = fast_smem_bytes(m->dev, nslots, false, q->bd.nefoi_stage, false) > limit;
+		if (fast_smem_bytes(m->dev, nslots, false, q->bd.nefoi_stage, true) > limit || m->NS * m->A > 640 || m->G * m->G > 640) {
 			delete q;
-			return fail(BEEP_BAD_INPUT, "model too large for the particle-resident fast form (shared memory)");
+			return fail(BEEP_BAD_INPUT, "model too large for the fast form (observation slots or tables exceed shared memory)");
 		}
-		q->bd.m_in_smem = fast_smem_bytes(m->dev, nslots, true, q->bd.nefoi_stage) <= limit ? 1 : 0;
+		q->bd.m_in_smem = fast_smem_bytes(m->dev, nslots, true, q->bd.nefoi_stage, q->state_global) <= limit ? 1 : 0;
 	}
 	auto bail = [&](beep_status s) { beep_batch_destroy(q); return s; };
 	st = stage_inputs(q);
@@ -550,6 +552,7 @@ beep_status beep_batch_create(beep_model *m, const beep_sim_batch *b, beep_batch
 
 	Layout wk;
 	const size_t PW = b->form == BEEP_FORM_FAST ? 0 : (size_t)P;   // the fast form keeps its state on chip
+	const size_t w_gs = wk.add(q->state_global ? fast_gstate_stride(m->dev) * (size_t)P : 0);
 	size_t w_pa = wk.add(4 * popsz * PW), w_pb = wk.add(4 * popsz * PW), w_tn = wk.add(b->transnum_out ? 0 : 4 * tnsz * PW),
 	       w_im = wk.add(8 * agsz * PW), w_id = wk.add(8 * agsz * PW), w_di = wk.add(8 * agsz * PW),
 	       w_nmi = wk.add(8 * agsz * PW), w_acc = wk.add(8 * (size_t)nscored * PW);
@@ -576,6 +579,8 @@ beep_status beep_batch_create(beep_model *m, const beep_sim_batch *b, beep_batch
 	bd.tn = b->transnum_out ? nullptr : (int32_t *)(dw + w_tn);
 	bd.Imap = (double *)(dw + w_im); bd.Idiag = (double *)(dw + w_id); bd.dinf = (double *)(dw + w_di);
 	bd.NMI = (double *)(dw + w_nmi); bd.obs_acc = (double *)(dw + w_acc);
+	bd.gstate = q->state_global ? (void *)(dw + w_gs) : nullptr;
+	bd.gstate_stride = q->state_global ? fast_gstate_stride(m->dev) : 0;
 	bd.status = (int32_t *)(dout + q->u_st);
 	bd.L = b->L_out ? (double *)(dout + q->u_L) : nullptr;
 	bd.pop_out = b->pop_out ? (int32_t *)(dout + q->u_po) : nullptr;

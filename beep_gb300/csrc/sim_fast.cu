@@ -80,10 +80,10 @@ __device__ __forceinline__ float ptrs_rhs(float k, float mean, float loglam, con
 {
 	if (k < 32.f) return fmaf(k, loglam, -mean) - lnfact[(int)k];
 	const float n = k + 1.f;
-	const float x = (mean - n) / n;
-	const float in = 1.f / n;
+	const float in = __fdividef(1.f, n);
+	const float x = (mean - n) * in;
 	const float corr = in * (0.083333333f - in * in * 0.0027777778f);
-	return k * (log1pf(x) - x) - x - 0.5f * logf(n) - 0.91893853f - corr;
+	return k * (log1pf(x) - x) - x - 0.5f * __logf(n) - 0.91893853f - corr;
 }
 
 // FP32 Poisson draw on the keyed stream of the FP64 form (same counters/words).
@@ -111,21 +111,22 @@ __device__ __forceinline__ int32_t poisson_fp32(float mean, uint32_t k0, uint32_
 		return k;
 	}
 	const float slam = sqrtf(mean);
-	const float loglam = logf(mean);
+	const float loglam = __logf(mean);
 	const float b = 0.931f + 2.53f * slam;
 	const float a = -0.059f + 0.02483f * b;
-	const float invalpha = 1.1239f + 1.1328f / (b - 3.4f);
-	const float vr = 0.9277f - 3.6224f / (b - 2.0f);
-	const float log_invalpha = logf(invalpha);
+	const float invalpha = 1.1239f + __fdividef(1.1328f, b - 3.4f);
+	const float vr = 0.9277f - __fdividef(3.6224f, b - 2.0f);
+	const float log_invalpha = __logf(invalpha);
+	const float two_a = 2.0f * a;
 	for (uint32_t it = 0; it < 65536u; it++) {
 		const U4 r = philox10(U4{col, sett, stream, (PURPOSE_PTRS << 24) | (tr << 16) | it}, k0, k1);
 		const float U = u01_f(r.x) - 0.5f;
 		const float V = u01_f(r.y);
 		const float us = 0.5f - fabsf(U);
-		const float k = floorf((2.0f * a / us + b) * U + mean + 0.43f);
+		const float k = floorf((__fdividef(two_a, us) + b) * U + mean + 0.43f);
 		if (us >= 0.07f && V <= vr) return (int32_t)k;
 		if (k < 0.0f || (us < 0.013f && V > us)) continue;
-		const float lhs = logf(V) + log_invalpha - logf(a / (us * us) + b);
+		const float lhs = __logf(V) + log_invalpha - __logf(__fdividef(a, us * us) + b);
 		if (lhs <= ptrs_rhs(k, mean, loglam, lnfact)) return (int32_t)k;
 	}
 	return -1;
@@ -283,12 +284,26 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 		size_t off = 0;
 		auto take = [&](size_t bytes) { unsigned char *q = smem_raw + off; off += (bytes + 15) & ~(size_t)15; return q; };
 		s.Ms = b.m_in_smem ? (float *)take(sizeof(float) * A * lda) : nullptr;
-		s.pop0 = (int32_t *)take(4 * (size_t)popsz);
-		s.pop1 = (int32_t *)take(4 * (size_t)popsz);
-		s.tn = (int32_t *)take(4 * (size_t)tnsz);
-		s.Ic0 = (float *)take(4 * (size_t)agsz);
-		s.Ic1 = (float *)take(4 * (size_t)agsz);
-		s.Imap = (float *)take(4 * (size_t)agsz);
+		if (b.gstate) {
+			// models too large for shared memory keep the particle's state in a global
+			// (L2-resident) region of the same layout
+			unsigned char *g = (unsigned char *)b.gstate + (size_t)p * b.gstate_stride;
+			size_t go = 0;
+			auto gtake = [&](size_t bytes) { unsigned char *q = g + go; go += (bytes + 255) & ~(size_t)255; return q; };
+			s.pop0 = (int32_t *)gtake(4 * (size_t)popsz);
+			s.pop1 = (int32_t *)gtake(4 * (size_t)popsz);
+			s.tn = (int32_t *)gtake(4 * (size_t)tnsz);
+			s.Ic0 = (float *)gtake(4 * (size_t)agsz);
+			s.Ic1 = (float *)gtake(4 * (size_t)agsz);
+			s.Imap = (float *)gtake(4 * (size_t)agsz);
+		} else {
+			s.pop0 = (int32_t *)take(4 * (size_t)popsz);
+			s.pop1 = (int32_t *)take(4 * (size_t)popsz);
+			s.tn = (int32_t *)take(4 * (size_t)tnsz);
+			s.Ic0 = (float *)take(4 * (size_t)agsz);
+			s.Ic1 = (float *)take(4 * (size_t)agsz);
+			s.Imap = (float *)take(4 * (size_t)agsz);
+		}
 		s.slot = (float *)take(4 * (size_t)b.nslots);
 		s.from = (int32_t *)take(4 * (size_t)T);
 		s.to = (int32_t *)take(4 * (size_t)T);
@@ -508,18 +523,25 @@ static int pick_threads(const ModelDev &m)
 	return ncol <= 128 ? 128 : ncol <= 256 ? 256 : 640;
 }
 
-size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_stage)
+size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_stage, bool state_global)
 {
 	auto r = [](size_t x) { return (x + 15) & ~(size_t)15; };
 	const size_t A = m.A, G = m.G, DP = m.DP, NS = m.NS, C = m.C, T = m.T, DPS = m.DPS;
 	const size_t agsz = NS * A * G, ncol = A * DP;
-	return (m_in_smem ? r(4 * A * ms_lda(m.A)) : 0) + 2 * r(4 * C * ncol) + r(4 * T * ncol) + 3 * r(4 * agsz) +
+	return (m_in_smem ? r(4 * A * ms_lda(m.A)) : 0) + (state_global ? 0 : 2 * r(4 * C * ncol) + r(4 * T * ncol) + 3 * r(4 * agsz)) +
 	       r(4 * (size_t)nslots) + 2 * r(4 * T) + r(4 * DPS) + r(4 * C) + r(4 * T * DP) + r(4 * DP) + r(4 * 64) +
 	       r(4 * 32) + 2 * r(4 * NS * A) + r(4 * (size_t)nefoi_stage * G) + 2 * (2 * r(4 * NS * A) + r(4 * G * G)) +
 	       r(8) + r(4 * 2 * (size_t)pick_threads(m));
 }
 
 int fast_threads() { return kFastThreads; }
+
+size_t fast_gstate_stride(const ModelDev &m)
+{
+	auto r = [](size_t x) { return (x + 255) & ~(size_t)255; };
+	const size_t agsz = (size_t)m.NS * m.A * m.G, ncol = (size_t)m.A * m.DP;
+	return 2 * r(4 * m.C * ncol) + r(4 * m.T * ncol) + 3 * r(4 * agsz);
+}
 
 template <int NT>
 static int launch_nt(const ModelDev &m, const BatchDev &b, size_t smem, cudaStream_t st)
@@ -535,7 +557,7 @@ int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream)
 {
 	if (b.P == 0) return 0;
 	if (m.G > 16) return (int)cudaErrorInvalidValue;
-	const size_t smem = fast_smem_bytes(m, b.nslots, b.m_in_smem != 0, b.nefoi_stage);
+	const size_t smem = fast_smem_bytes(m, b.nslots, b.m_in_smem != 0, b.nefoi_stage, b.gstate != nullptr);
 	const int nt = pick_threads(m);
 	const int NSA = m.NS * m.A;
 	if (NSA > nt || m.G * m.G > nt) return (int)cudaErrorInvalidValue;   // slices: one item per thread

@@ -270,3 +270,34 @@ def abc_smc_large(seed: int = 20260001, narea: int = 150, nage: int = 4, days: i
 def abc_smc_priors(rng, n: int):
     """Per-particle parameters from the ABC-SMC priors: R0 U(1.5,4), 1/sigma U(2,6), 1/gamma U(3,8)."""
     return rng.uniform(1.5, 4.0, n), rng.uniform(2.0, 6.0, n), rng.uniform(3.0, 8.0, n)
+
+
+def precision_large(seed: int = 20260002, narea: int = 350, nage: int = 10, days: int = 365,
+                    steps_per_day: int = 4, name: str = "c2") -> Workload:
+    """Precision workload: 350 areas x 10 ages, dt 0.25, 365 days.  Gravity
+    mixing exp(-d/0.1) plus 5% long-range entries U(0, 0.01); age mixing
+    U(0.2, 3) symmetric with 3 stepped modification factors; R(t) with 20
+    knots U(0.5, 2); two area covariates N(0,1) with effects 0.1 and 0.05;
+    daily cases and weekly deaths per area."""
+    rng = np.random.default_rng(seed)
+    totals = rng.integers(50000, 500001, narea)
+    pop = np.stack([_split_pop(rng, int(t), nage) for t in totals])
+    am = rng.uniform(0.2, 3.0, (nage, nage))
+    am = np.triu(am) + np.triu(am, 1).T
+    geo = _gravity(rng, narea, 0.1, long_range_frac=0.05, long_range_max=0.01)
+    seedE = np.zeros((narea, nage), np.int64)
+    seedE[0, nage // 2] = max(1, rng.poisson(10))
+    nknot = 20
+    bp = [int(round(k * days / (nknot - 1))) for k in range(nknot)]
+    val = [float(v) for v in rng.uniform(0.5, 2.0, nknot)]
+    val[0] = 2.5
+    matmod = []
+    groups = np.array_split(rng.permutation(nage), 3)
+    for g in groups:
+        t = int(rng.integers(30, days - 30))
+        f = float(rng.uniform(0.4, 1.0))
+        matmod.append({"ages": sorted(int(a) for a in g), "bp": [0, t, t, days], "val": [1.0, 1.0, f, f]})
+    covar = rng.normal(0.0, 1.0, (2, narea))
+    return Workload(name=name, seed=seed, narea=narea, nage=nage, days=days, steps_per_day=steps_per_day,
+                    pop=pop, age_mix=am, geo=geo, seed_E=seedE, R_bp=bp, R_val=val, covar=covar,
+                    covar_effect=[0.1, 0.05], matmod=matmod)

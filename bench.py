@@ -100,43 +100,59 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def build_workload(P: int, seed: int):
-    """Model + per-particle parameter tables of the ABC-SMC workload.  The
-    observed data are one simulation at the true parameters (made with the
-    library itself) plus noise."""
+WORKLOADS = {
+    # one ABC-SMC generation: every particle has its own parameters
+    "abc_smc": dict(name="abc_smc_generation_150x4", particles=16384),
+    # PMCMC likelihood batch on the 350-area x 10-age precision model: one parameter set
+    "precision": dict(name="pmcmc_precision_350x10", particles=1024),
+}
+
+
+def build_workload(kind: str, P: int, seed: int):
+    """Model + parameter tables of a workload.  The observed data are one
+    simulation at the true parameters (made with the library itself, fast
+    form) plus noise."""
     from beep_gb300 import capi, model_builder as mb, synth
-    w = synth.abc_smc_large()
+    w = synth.abc_smc_large() if kind == "abc_smc" else synth.precision_large()
     arr0 = mb.model_arrays(w)
     m0 = capi.Model(arr0)
     t_true = capi.Tables(mb.param_tables(w))
     dm0 = capi.DeviceModel(m0)
     truth = dm0.simulate(capi.Batch(m0, [t_true], 1, seed ^ 0x5EED, want_transnum=True, want_pop_traj=True,
-                                    want_L=False))
+                                    want_L=False, form=capi.FORM_FAST))
     dm0.close()
     rng = np.random.default_rng(seed)
     y, sd = mb.observed_from_trajectory(arr0, truth.transnum[0], truth.pop_traj[0], rng)
     arr = dict(arr0)
     arr["obs_value"], arr["obs_sd"] = y, sd
     m = capi.Model(arr)
-    R0, si, gi = synth.abc_smc_priors(rng, P)
-    tabs = [capi.Tables(t) for t in mb.param_tables_batch(w, R0, si, gi)]
-    return w, m, tabs
+    if kind == "abc_smc":
+        R0, si, gi = synth.abc_smc_priors(rng, P)
+        tabs = [capi.Tables(t) for t in mb.param_tables_batch(w, R0, si, gi)]
+        group_of = np.arange(P)
+    else:
+        tabs = [t_true]
+        group_of = np.zeros(P, np.int32)
+    return w, m, tabs, group_of
 
 
-def cpu_throughput(m, tabs, seed, target_s: float, nthreads: int, max_particles: int):
+def cpu_throughput(m, tabs, group_of, seed, target_s: float, nthreads: int, max_particles: int):
     """Oracle restatement on this host: units/s over a bounded particle sample."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from beep_gb300 import capi
     from oracle_lib import oracle_simulate
     units_per_particle = m.narea * m.nage * m.ndivision
     n = max(1, nthreads)
+    sub = lambda k: (tabs[:k] if len(tabs) > 1 else tabs), group_of[:k]
     t0 = time.perf_counter()
-    oracle_simulate(m, capi.Batch(m, tabs[:n], n, seed, group_of=np.arange(n)), nthreads)
+    tb, go = sub(n)
+    oracle_simulate(m, capi.Batch(m, tb, n, seed, group_of=go), nthreads)
     dt = time.perf_counter() - t0
     n2 = int(min(max_particles, max(n, n * target_s / max(dt, 1e-3))))
     n2 = max(n, (n2 // n) * n)
+    tb, go = sub(n2)
     t0 = time.perf_counter()
-    oracle_simulate(m, capi.Batch(m, tabs[:n2], n2, seed, group_of=np.arange(n2)), nthreads)
+    oracle_simulate(m, capi.Batch(m, tb, n2, seed, group_of=go), nthreads)
     dt = time.perf_counter() - t0
     return units_per_particle * n2 / dt, n2, dt
 
@@ -156,17 +172,18 @@ def run_reference(args, rank, ws, dist):
         return
     from beep_gb300 import capi  # noqa: F401
     nthreads = os.cpu_count() or 1
-    P = 16384
-    w, m, tabs = build_workload_cpu(P, args.seed)
+    P = args.particles or WORKLOADS[args.workload]["particles"]
+    w, m, tabs, group_of = build_workload_cpu(args.workload, P, args.seed)
     upp = m.narea * m.nage * m.ndivision
     # per step a bounded sample sized for a few seconds of work
-    _, n2, dt = cpu_throughput(m, tabs, args.seed, 3.0, nthreads, P)
+    _, n2, dt = cpu_throughput(m, tabs, group_of, args.seed, 3.0, nthreads, P)
     times = []
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_lib import oracle_simulate
     for k in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        oracle_simulate(m, capi.Batch(m, tabs[:n2], n2, args.seed + k, group_of=np.arange(n2)), nthreads)
+        oracle_simulate(m, capi.Batch(m, tabs[:n2] if len(tabs) > 1 else tabs, n2, args.seed + k,
+                                      group_of=group_of[:n2]), nthreads)
         if k >= args.warmup:
             times.append(time.perf_counter() - t0)
     t = statistics.mean(times)
@@ -175,7 +192,7 @@ def run_reference(args, rank, ws, dist):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "particle.area.group.steps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": workload_config(m, P, note=f"sample of {n2} particles per step"),
+        "config": workload_config(args.workload, m, P, note=f"sample of {n2} particles per step"),
         "loglik_evals_per_s": n2 / t,
         "cpu_baseline": {"value": value, "unit": "particle.area.group.steps/s", "cores": nthreads, "kind": "port",
                          "sample": f"{n2} of {P} particles per step, full 360-step horizon + log-likelihood"},
@@ -185,13 +202,13 @@ def run_reference(args, rank, ws, dist):
     print(json.dumps(line))
 
 
-def build_workload_cpu(P, seed):
+def build_workload_cpu(kind, P, seed):
     """The same workload without a GPU: the observed data come from the oracle
     (only used by the reference arm, which runs the oracle anyway)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from beep_gb300 import capi, model_builder as mb, synth
     from oracle_lib import oracle_simulate
-    w = synth.abc_smc_large()
+    w = synth.abc_smc_large() if kind == "abc_smc" else synth.precision_large()
     arr0 = mb.model_arrays(w)
     m0 = capi.Model(arr0)
     t_true = capi.Tables(mb.param_tables(w))
@@ -202,13 +219,15 @@ def build_workload_cpu(P, seed):
     arr = dict(arr0)
     arr["obs_value"], arr["obs_sd"] = y, sd
     m = capi.Model(arr)
-    R0, si, gi = synth.abc_smc_priors(rng, P)
-    tabs = [capi.Tables(t) for t in mb.param_tables_batch(w, R0, si, gi)]
-    return w, m, tabs
+    if kind == "abc_smc":
+        R0, si, gi = synth.abc_smc_priors(rng, P)
+        tabs = [capi.Tables(t) for t in mb.param_tables_batch(w, R0, si, gi)]
+        return w, m, tabs, np.arange(P)
+    return w, m, [t_true], np.zeros(P, np.int32)
 
 
-def workload_config(m, P, note=None):
-    c = {"workload": "abc_smc_generation_150x4", "particles": P, "areas": m.narea, "ages": m.nage,
+def workload_config(kind, m, P, note=None):
+    c = {"workload": WORKLOADS[kind]["name"], "particles": P, "areas": m.narea, "ages": m.nage,
          "steps": m.ndivision, "dt_days": m.dt, "observations": m.nobs, "model": "SEIR-H-D",
          "l2": "working set larger than L2 (per-particle state and observation sums, GB scale)"}
     if note:
@@ -219,12 +238,12 @@ def workload_config(m, P, note=None):
 def run_ours(args, rank, ws, dist):
     from beep_gb300 import build as bbuild, capi
     bbuild.build()
-    P = args.particles
+    P = args.particles or WORKLOADS[args.workload]["particles"]
     seed = args.seed + 7919 * rank
-    w, m, tabs = build_workload(P, seed)
+    w, m, tabs, group_of = build_workload(args.workload, P, seed)
     dm = capi.DeviceModel(m, device=int(os.environ.get("LOCAL_RANK", "0")) if ws > 1 else 0)
     form = capi.FORM_FAST if args.form == "fast" else capi.FORM_PLAIN_FP64
-    batch = capi.Batch(m, tabs, P, seed, group_of=np.arange(P), stream_of=np.arange(P) + rank * P, form=form)
+    batch = capi.Batch(m, tabs, P, seed, group_of=group_of, stream_of=np.arange(P) + rank * P, form=form)
     db = capi.DeviceBatch(dm, batch)
     h2d, d2h = db.bytes()
     db.upload()
@@ -263,12 +282,15 @@ def run_ours(args, rank, ws, dist):
     plain = None
     if form == capi.FORM_FAST and args.plain_particles > 0:
         Pp = min(P, args.plain_particles)
-        pb = capi.DeviceBatch(dm, capi.Batch(m, tabs[:Pp], Pp, seed, group_of=np.arange(Pp), form=capi.FORM_PLAIN_FP64))
+        tfp = args.plain_steps or m.ndivision
+        pb = capi.DeviceBatch(dm, capi.Batch(m, tabs[:Pp] if len(tabs) > 1 else tabs, Pp, seed, group_of=group_of[:Pp],
+                                             tf=tfp, form=capi.FORM_PLAIN_FP64))
         pb.upload()
         pb.time(1)
         pms = pb.time(1)
-        plain = {"value": Pp * m.narea * m.nage * m.ndivision / (pms / 1e3), "unit": "particle.area.group.steps/s",
-                 "ms_per_step": pms, "particles": Pp, "loglik_evals_per_s": Pp / (pms / 1e3)}
+        plain = {"value": Pp * m.narea * m.nage * tfp / (pms / 1e3), "unit": "particle.area.group.steps/s",
+                 "ms_per_step": pms, "particles": Pp, "steps": tfp,
+                 "loglik_evals_per_s": Pp / (pms / 1e3) * tfp / m.ndivision}
         pb.close()
     if rank != 0:
         return
@@ -281,14 +303,14 @@ def run_ours(args, rank, ws, dist):
     cpu = None
     if not args.no_cpu:
         nthreads = os.cpu_count() or 1
-        v, n2, dt = cpu_throughput(m, tabs, seed, args.cpu_seconds, nthreads, P)
+        v, n2, dt = cpu_throughput(m, tabs, group_of, seed, args.cpu_seconds, nthreads, P)
         cpu = {"value": v, "unit": "particle.area.group.steps/s", "cores": nthreads, "kind": "port",
                "sample": f"{n2} of {P} particles (full 360-step horizon + log-likelihood), {dt:.1f} s"}
     line = {
         "metric": METRIC, "value": units * ws / t_dev, "unit": "particle.area.group.steps/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_dev * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.form == "fast" else "f64",
-        "data": "synthetic", "config": workload_config(m, P),
+        "data": "synthetic", "config": workload_config(args.workload, m, P),
         "form": args.form,
         "plain_fp64": plain,
         "loglik_evals_per_s": P * ws / t_dev,
@@ -312,12 +334,14 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--particles", type=int, default=16384)
+    ap.add_argument("--workload", default="abc_smc", choices=sorted(WORKLOADS))
+    ap.add_argument("--particles", type=int, default=0, help="default: the workload's particle count")
     ap.add_argument("--seed", type=int, default=20260001)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--form", default="fast", choices=["fast", "plain"])
     ap.add_argument("--plain-particles", type=int, default=1024)
+    ap.add_argument("--plain-steps", type=int, default=0, help="time the plain form over this many steps (0: all)")
     args = ap.parse_args()
     rank, ws, dist = dist_setup(args)
     if args.impl == "reference":

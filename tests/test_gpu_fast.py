@@ -83,3 +83,21 @@ def test_fast_distribution_matches_oracle(built):
     assert stats.ks_2samp(fs_f, fs_o).pvalue > 1e-3
     assert stats.ks_2samp(f.L, o.L).pvalue > 1e-3
     dm.close()
+
+
+def test_fast_large_model_keeps_state_in_global_memory(built):
+    """A model whose per-particle state exceeds shared memory (200 areas x 8
+    ages) runs the fast form with its state in global memory: same streams,
+    trajectories follow the FP64 form."""
+    from beep_gb300 import model_builder as mb, synth
+    w = synth.seir_hd_small(seed=20260200, narea=200, nage=8, days=30, name="big")
+    m = capi.Model(mb.model_arrays(w))
+    t = capi.Tables(mb.param_tables(w))
+    dm = capi.DeviceModel(m)
+    P = 24
+    f = dm.simulate(capi.Batch(m, [t], P, 5, want_transnum=True, want_pop=True, form=capi.FORM_FAST))
+    g = dm.simulate(capi.Batch(m, [t], P, 5, want_transnum=True, want_pop=True))
+    same = np.array([np.array_equal(f.transnum[p], g.transnum[p]) for p in range(P)])
+    assert same.mean() >= 0.5, same.mean()
+    np.testing.assert_allclose(f.L[same], g.L[same], rtol=L_RTOL_FAST)
+    dm.close()
