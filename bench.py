@@ -143,7 +143,8 @@ def cpu_throughput(m, tabs, group_of, seed, target_s: float, nthreads: int, max_
     from oracle_lib import oracle_simulate
     units_per_particle = m.narea * m.nage * m.ndivision
     n = max(1, nthreads)
-    sub = lambda k: (tabs[:k] if len(tabs) > 1 else tabs), group_of[:k]
+    def sub(k):
+        return (tabs[:k] if len(tabs) > 1 else tabs), group_of[:k]
     t0 = time.perf_counter()
     tb, go = sub(n)
     oracle_simulate(m, capi.Batch(m, tb, n, seed, group_of=go), nthreads)
