@@ -28,6 +28,7 @@ UNITS = {
     "sim_plain.cu": ["--fmad=false"],
     "sim_fast.cu": [],
     "noalloc.cu": [],
+    "pf.cu": [],
 }
 
 

@@ -59,6 +59,15 @@ class SimBatch(C.Structure):
     ]
 
 
+class PFRequest(C.Structure):
+    _fields_ = [
+        ("nparticle", C.c_int32), ("tables", C.POINTER(ParamTables)), ("seed", C.c_uint64),
+        ("resample_stream", C.c_uint32), ("invT", C.c_double), ("nsection", C.c_int32),
+        ("section_ti", _i32p), ("section_tf", _i32p), ("form", C.c_int32),
+        ("loglik_out", _f64p), ("loglik_section_out", _f64p), ("L_out", _f64p), ("ancestors_out", _i32p),
+    ]
+
+
 def _ptr(a: Optional[np.ndarray], ctype):
     if a is None:
         return C.cast(None, C.POINTER(ctype))
@@ -225,6 +234,8 @@ def lib():
                                                   C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
                                                   C.c_void_p]
         L.beep_simulate_plain_noalloc.restype = C.c_int32
+        L.beep_pf_loglik.argtypes = [C.c_void_p, C.POINTER(PFRequest)]
+        L.beep_pf_loglik.restype = C.c_int32
         for f in ("beep_device_init", "beep_model_create", "beep_model_destroy", "beep_simulate", "beep_batch_create",
                   "beep_batch_stage", "beep_batch_upload", "beep_batch_launch", "beep_batch_download",
                   "beep_batch_time", "beep_batch_destroy"):
@@ -258,6 +269,24 @@ class DeviceModel:
     def simulate(self, batch: Batch) -> Batch:
         check(lib().beep_simulate(self.h, C.byref(batch.st)))
         return batch
+
+    def pf_loglik(self, tables: "Tables", N: int, seed: int, resample_stream: int, invT: float, sections,
+                  form: int = FORM_PLAIN_FP64):
+        """Bootstrap particle filter on the device: (estimate, per-section terms, L, ancestors)."""
+        ti = np.array([a for a, _ in sections], np.int32)
+        tf = np.array([b for _, b in sections], np.int32)
+        ns = len(sections)
+        ll = np.zeros(1)
+        lls = np.zeros(ns)
+        Lo = np.zeros((ns, N))
+        anc = np.zeros((ns, N), np.int32)
+        r = PFRequest()
+        r.nparticle, r.tables, r.seed, r.resample_stream, r.invT = N, C.pointer(tables.st), seed, resample_stream, invT
+        r.nsection, r.section_ti, r.section_tf, r.form = ns, _ptr(ti, C.c_int32), _ptr(tf, C.c_int32), form
+        r.loglik_out, r.loglik_section_out = _ptr(ll, C.c_double), _ptr(lls, C.c_double)
+        r.L_out, r.ancestors_out = _ptr(Lo, C.c_double), _ptr(anc, C.c_int32)
+        check(lib().beep_pf_loglik(self.h, C.byref(r)))
+        return float(ll[0]), lls, Lo, anc
 
     def close(self):
         if self.h:

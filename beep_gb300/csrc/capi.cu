@@ -370,31 +370,14 @@ beep_status pack_tables(const beep_model *m, const beep_sim_batch *b, TablePacke
 }  // namespace
 
 
-// A prepared batch: the caller's host arrays (kept by pointer), pinned staging,
-// device inputs, work and outputs, and the kernel's view of them.
-struct beep_batch {
-	beep_model *m = nullptr;
-	beep_sim_batch b{};
-	HostBuf in_host, out_host;
-	DevBuf in_dev, work_dev, out_dev;
-	size_t in_size = 0, out_size = 0;
-	size_t o_f = 0, u_st = 0, u_L = 0, u_po = 0, u_tn = 0, u_pt = 0;
-	std::vector<GroupDir> dirs;
-	std::vector<int32_t> scored, step_ptr, step_obs, slot_of, tasks;
-	BatchDev bd{};
-	cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-	bool pending = false;
-	bool state_global = false;   // fast form keeps particle state in global memory
-};
-
 namespace {
 
-beep_status check_batch(const beep_model *m, const beep_sim_batch *b)
+beep_status check_batch(const beep_model *m, const beep_sim_batch *b, bool device_io = false)
 {
 	const int P = b->nparticle;
 	if (P <= 0 || b->ngroup <= 0 || !b->groups) return fail(BEEP_BAD_INPUT, "nparticle/ngroup/groups");
 	if (b->ti < 0 || b->tf <= b->ti || b->tf > m->S) return fail(BEEP_BAD_INPUT, "step range must satisfy 0 <= ti < tf <= ndivision");
-	if (b->ti > 0 && !b->pop_in) return fail(BEEP_BAD_INPUT, "pop_in is required when ti > 0");
+	if (b->ti > 0 && !b->pop_in && !device_io) return fail(BEEP_BAD_INPUT, "pop_in is required when ti > 0");
 	if (b->form != BEEP_FORM_PLAIN_FP64 && b->form != BEEP_FORM_FAST) return fail(BEEP_BAD_INPUT, "unknown form");
 	if (b->group_of)
 		for (int p = 0; p < P; p++)
@@ -417,7 +400,7 @@ beep_status stage_inputs(beep_batch *q)
 	size_t o_dirs = in.add(sizeof(GroupDir) * q->dirs.size()), o_f = in.add(8 * pk.f.size()),
 	       o_f32 = in.add(fast ? 4 * pk.f.size() : 0),
 	       o_i = in.add(4 * pk.i.size()), o_go = in.add(b->group_of ? 4 * (size_t)P : 0),
-	       o_so = in.add(b->stream_of ? 4 * (size_t)P : 0), o_pin = in.add(b->ti > 0 ? 4 * popsz * P : 0),
+	       o_so = in.add(b->stream_of ? 4 * (size_t)P : 0), o_pin = in.add(b->ti > 0 && !q->device_io ? 4 * popsz * P : 0),
 	       o_sc = in.add(4 * q->scored.size()), o_sp = in.add(4 * q->step_ptr.size()),
 	       o_sobs = in.add(4 * q->step_obs.size()), o_tasks = in.add(4 * q->tasks.size());
 	CUDA_TRY(q->in_host.reserve(in.size));
@@ -429,7 +412,7 @@ beep_status stage_inputs(beep_batch *q)
 	if (!pk.i.empty()) memcpy(h + o_i, pk.i.data(), 4 * pk.i.size());
 	if (b->group_of) memcpy(h + o_go, b->group_of, 4 * (size_t)P);
 	if (b->stream_of) memcpy(h + o_so, b->stream_of, 4 * (size_t)P);
-	if (b->ti > 0) memcpy(h + o_pin, b->pop_in, 4 * popsz * P);
+	if (b->ti > 0 && !q->device_io) memcpy(h + o_pin, b->pop_in, 4 * popsz * P);
 	if (!q->scored.empty()) memcpy(h + o_sc, q->scored.data(), 4 * q->scored.size());
 	memcpy(h + o_sp, q->step_ptr.data(), 4 * q->step_ptr.size());
 	if (!q->step_obs.empty()) memcpy(h + o_sobs, q->step_obs.data(), 4 * q->step_obs.size());
@@ -452,7 +435,7 @@ beep_status stage_inputs(beep_batch *q)
 	bd.ipool = (const int32_t *)(di + o_i);
 	bd.group_of = b->group_of ? (const int32_t *)(di + o_go) : nullptr;
 	bd.stream_of = b->stream_of ? (const uint32_t *)(di + o_so) : nullptr;
-	bd.pop_in = b->ti > 0 ? (const int32_t *)(di + o_pin) : nullptr;
+	bd.pop_in = b->ti > 0 && !q->device_io ? (const int32_t *)(di + o_pin) : nullptr;
 	bd.scored = (const int32_t *)(di + o_sc);
 	bd.step_ptr = (const int32_t *)(di + o_sp);
 	bd.step_obs = (const int32_t *)(di + o_sobs);
@@ -469,12 +452,22 @@ beep_status beep_batch_create(beep_model *m, const beep_sim_batch *b, beep_batch
 {
 	if (!m || !b || !out) return fail(BEEP_BAD_INPUT, "null argument");
 	*out = nullptr;
-	beep_status st = check_batch(m, b);
+	return batch_create_internal(m, b, false, out);
+}
+
+}  // extern "C"
+
+beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, bool device_io, beep_batch **out)
+{
+	if (!m || !b || !out) return fail(BEEP_BAD_INPUT, "null argument");
+	*out = nullptr;
+	beep_status st = check_batch(m, b, device_io);
 	if (st != BEEP_OK) return st;
 	CUDA_TRY(cudaSetDevice(m->device));
 	beep_batch *q = new beep_batch();
 	q->m = m;
 	q->b = *b;
+	q->device_io = device_io;
 	const int P = b->nparticle;
 	const size_t popsz = (size_t)m->A * m->C * m->DP, tnsz = (size_t)m->A * m->T * m->DP;
 	const size_t agsz = (size_t)m->NS * m->A * m->G;
@@ -590,10 +583,12 @@ beep_status beep_batch_create(beep_model *m, const beep_sim_batch *b, beep_batch
 	return BEEP_OK;
 }
 
+extern "C" {
+
 beep_status beep_batch_stage(beep_batch *q)
 {
 	if (!q) return fail(BEEP_BAD_INPUT, "null batch");
-	beep_status st = check_batch(q->m, &q->b);
+	beep_status st = check_batch(q->m, &q->b, q->device_io);
 	if (st != BEEP_OK) return st;
 	CUDA_TRY(cudaStreamSynchronize(q->m->stream));   // the staging buffer may still feed a copy
 	return stage_inputs(q);

@@ -103,3 +103,29 @@ struct beep_model {
 	int32_t max_obs_spline = -1;
 	std::mutex mu;
 };
+
+// A prepared batch: the caller's host arrays (kept by pointer), pinned staging,
+// device inputs, work and outputs, and the kernel's view of them.
+struct beep_batch {
+	bool device_io = false;   // pop_in / L / pop_out are device buffers set by an internal caller
+	beep_model *m = nullptr;
+	beep_sim_batch b{};
+	beep::HostBuf in_host, out_host;
+	beep::DevBuf in_dev, work_dev, out_dev;
+	size_t in_size = 0, out_size = 0;
+	size_t o_f = 0, u_st = 0, u_L = 0, u_po = 0, u_tn = 0, u_pt = 0;
+	std::vector<beep::GroupDir> dirs;
+	std::vector<int32_t> scored, step_ptr, step_obs, slot_of, tasks;
+	beep::BatchDev bd{};
+	cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+	bool pending = false;
+	bool state_global = false;   // fast form keeps particle state in global memory
+};
+
+
+namespace beep {
+// beep_batch_create for internal callers whose start populations and outputs
+// live on the device (device_io: pop_in is not read from the host and the
+// caller sets bd.pop_in / bd.L / bd.pop_out before each launch).
+beep_status batch_create_internal(beep_model *m, const beep_sim_batch *b, bool device_io, beep_batch **out);
+}  // namespace beep

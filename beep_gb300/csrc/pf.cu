@@ -1,0 +1,199 @@
+// beep_pf_loglik: the bootstrap particle filter of PMCMC on the device
+// (PMCMC::obs_prob + bootstrap, src/pmcmc.cc:180-268; Mpi::end_sec_swap,
+// src/mpi.cc:215-327).
+//
+// Per filter section, on the model's stream with no host round trip:
+//   1. the simulation kernel (plain or fast form) advances every particle slot
+//      from its carried population and writes the section log-likelihood L;
+//   2. pf_bootstrap (one CTA) forms w = exp(invT (L - Lmax)), the cumulative
+//      sums in slot order, the section's term invT Lmax + log(sum w / N), and the
+//      ancestors: N uniforms (word 0 of Philox({j, section, stream, RESAMPLE})),
+//      each located in the cumulative sums, then the reference's placement
+//      (a selected particle keeps its own slot, the other slots take the
+//      surplus selections last-in first-out);
+//   3. pf_gather copies each slot's population from its ancestor's.
+// The cumulative sums and the placement are sequential in slot order, as in
+// the reference, so the ancestors match it exactly (the FP64 weights of the
+// plain form agree with the reference's to the last bits).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "capi_internal.h"
+#include "rng_fp64.cuh"
+
+namespace beep {
+namespace {
+
+constexpr int kBootThreads = 1024;
+
+__global__ void __launch_bounds__(kBootThreads) pf_bootstrap(const double *L, int N, double invT, uint32_t k0,
+                                                            uint32_t k1, uint32_t rstream, int sec, double *w,
+                                                            double *wsum, int32_t *sel, int32_t *bp, int32_t *extra,
+                                                            double *ob_sec, int32_t *anc, int32_t *status)
+{
+	__shared__ double red[kBootThreads];
+	__shared__ double s_sum;
+	const int tid = threadIdx.x;
+	double mx = -1000000000.0;                       // -LARGE, src/pmcmc.cc:223
+	for (int p = tid; p < N; p += kBootThreads) mx = fmax(mx, L[p]);
+	red[tid] = mx;
+	__syncthreads();
+	for (int o = kBootThreads / 2; o > 0; o >>= 1) {
+		if (tid < o) red[tid] = fmax(red[tid], red[tid + o]);
+		__syncthreads();
+	}
+	const double Lmax = red[0];
+	for (int p = tid; p < N; p += kBootThreads) w[p] = exp(invT * (L[p] - Lmax));
+	__syncthreads();
+	if (tid == 0) {
+		double sum = 0.0;
+		for (int p = 0; p < N; p++) {
+			sum += w[p];
+			wsum[p] = sum;
+		}
+		s_sum = sum;
+		ob_sec[sec] = invT * Lmax + log(sum / N);
+	}
+	__syncthreads();
+	const double sum = s_sum;
+	for (int j = tid; j < N; j += kBootThreads) {
+		const U4 r = philox10(U4{(uint32_t)j, (uint32_t)sec, rstream, PURPOSE_RESAMPLE << 24}, k0, k1);
+		const double z = u01_d(r.x) * sum;
+		int lo = 0, hi = N;                          // first slot with wsum >= z
+		while (lo < hi) {
+			const int mid = (lo + hi) >> 1;
+			if (z > wsum[mid]) lo = mid + 1;
+			else hi = mid;
+		}
+		if (lo == N) { atomicCAS(status, 0, BEEP_NAN_RATE); lo = N - 1; }
+		sel[j] = lo;
+	}
+	__syncthreads();
+	if (tid == 0) {
+		for (int p = 0; p < N; p++) bp[p] = -1;
+		int ne = 0;
+		for (int j = 0; j < N; j++) {
+			const int pp = sel[j];
+			if (bp[pp] == -1) bp[pp] = pp;
+			else extra[ne++] = pp;
+		}
+		for (int p = 0; p < N; p++)
+			if (bp[p] == -1) bp[p] = extra[--ne];
+	}
+	__syncthreads();
+	if (anc)
+		for (int p = tid; p < N; p += kBootThreads) anc[p] = bp[p];
+}
+
+__global__ void pf_gather(int32_t *dst, const int32_t *src, const int32_t *bp, int N, int popsz)
+{
+	const size_t n = (size_t)N * popsz;
+	for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+		const size_t p = k / popsz, i = k % popsz;
+		dst[k] = src[(size_t)bp[p] * popsz + i];
+	}
+}
+
+}  // namespace
+}  // namespace beep
+
+using namespace beep;
+
+extern "C" BEEP_API beep_status beep_pf_loglik(beep_model *m, const beep_pf_request *r)
+{
+	if (!m || !r || !r->tables) return fail(BEEP_BAD_INPUT, "null argument");
+	const int N = r->nparticle, ns = r->nsection;
+	if (N <= 0 || ns <= 0 || !r->section_ti || !r->section_tf || !r->loglik_out)
+		return fail(BEEP_BAD_INPUT, "nparticle, sections and loglik_out are required");
+	if (r->section_ti[0] != 0 || r->section_tf[ns - 1] != m->S)
+		return fail(BEEP_BAD_INPUT, "sections must cover [0, ndivision)");
+	for (int k = 0; k < ns; k++) {
+		if (r->section_tf[k] <= r->section_ti[k]) return fail(BEEP_BAD_INPUT, "empty section");
+		if (k > 0 && r->section_ti[k] != r->section_tf[k - 1]) return fail(BEEP_BAD_INPUT, "sections must be contiguous");
+	}
+	std::lock_guard<std::mutex> lock(m->mu);
+	CUDA_TRY(cudaSetDevice(m->device));
+	const size_t popsz = (size_t)m->A * m->C * m->DP;
+	cudaStream_t st = m->stream;
+
+	// one prepared batch per section (tables staged and uploaded once per call)
+	std::vector<beep_batch *> q(ns, nullptr);
+	auto cleanup = [&]() {
+		for (auto *x : q) beep_batch_destroy(x);
+	};
+	std::vector<double> Lhost_dummy(1);
+	for (int k = 0; k < ns; k++) {
+		beep_sim_batch b{};
+		b.nparticle = N; b.ngroup = 1; b.groups = r->tables; b.seed = r->seed;
+		b.ti = r->section_ti[k]; b.tf = r->section_tf[k];
+		b.form = r->form;
+		beep_status s = batch_create_internal(m, &b, true, &q[k]);
+		if (s != BEEP_OK) { std::string e = beep_last_error(); cleanup(); return fail(s, e); }
+	}
+	Layout L;
+	const size_t o_pa = L.add(4 * popsz * N), o_pb = L.add(4 * popsz * N), o_L = L.add(8 * (size_t)ns * N),
+	             o_w = L.add(8 * (size_t)N), o_ws = L.add(8 * (size_t)N), o_sel = L.add(4 * (size_t)N),
+	             o_bp = L.add(4 * (size_t)N), o_ex = L.add(4 * (size_t)N), o_ob = L.add(8 * (size_t)ns),
+	             o_anc = L.add(4 * (size_t)ns * N), o_st = L.add(4);
+	DevBuf work;
+	cudaError_t e = work.reserve(L.size);
+	if (e != cudaSuccess) { cleanup(); return fail(BEEP_OOM, std::string("particle filter buffers: ") + cudaGetErrorString(e)); }
+	char *d = (char *)work.ptr;
+	int32_t *popA = (int32_t *)(d + o_pa), *popB = (int32_t *)(d + o_pb);
+	double *Lall = (double *)(d + o_L), *obsec = (double *)(d + o_ob);
+	int32_t *anc = (int32_t *)(d + o_anc), *pst = (int32_t *)(d + o_st);
+	beep_status status = BEEP_OK;
+	std::string err;
+	auto bail = [&](beep_status s, const std::string &msg) { status = s; err = msg; };
+	if (cudaMemsetAsync(pst, 0, 4, st) != cudaSuccess) bail(BEEP_DEVICE_ERROR, "memset");
+	for (int k = 0; k < ns && status == BEEP_OK; k++) {
+		beep_batch *b = q[k];
+		if (beep_batch_upload(b) != BEEP_OK) { bail(BEEP_DEVICE_ERROR, beep_last_error()); break; }
+		b->bd.pop_in = k > 0 ? popA : nullptr;
+		b->bd.pop_out = popB;
+		b->bd.L = Lall + (size_t)k * N;
+		if (beep_batch_launch(b) != BEEP_OK) { bail(BEEP_DEVICE_ERROR, beep_last_error()); break; }
+		pf_bootstrap<<<1, kBootThreads, 0, st>>>(Lall + (size_t)k * N, N, r->invT, (uint32_t)r->seed,
+		                                         (uint32_t)(r->seed >> 32), r->resample_stream, k,
+		                                         (double *)(d + o_w), (double *)(d + o_ws), (int32_t *)(d + o_sel),
+		                                         (int32_t *)(d + o_bp), (int32_t *)(d + o_ex), obsec,
+		                                         anc + (size_t)k * N, pst);
+		if (k + 1 < ns) pf_gather<<<152 * 4, 256, 0, st>>>(popA, popB, (const int32_t *)(d + o_bp), N, (int)popsz);
+		if (cudaGetLastError() != cudaSuccess) bail(BEEP_DEVICE_ERROR, "bootstrap launch");
+	}
+	std::vector<double> ob(ns);
+	int32_t bst = 0;
+	if (status == BEEP_OK) {
+		e = cudaMemcpyAsync(ob.data(), obsec, 8 * (size_t)ns, cudaMemcpyDeviceToHost, st);
+		if (e == cudaSuccess) e = cudaMemcpyAsync(&bst, pst, 4, cudaMemcpyDeviceToHost, st);
+		if (e == cudaSuccess && r->L_out) e = cudaMemcpyAsync(r->L_out, Lall, 8 * (size_t)ns * N, cudaMemcpyDeviceToHost, st);
+		if (e == cudaSuccess && r->ancestors_out)
+			e = cudaMemcpyAsync(r->ancestors_out, anc, 4 * (size_t)ns * N, cudaMemcpyDeviceToHost, st);
+		if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+		if (e != cudaSuccess) bail(BEEP_DEVICE_ERROR, cudaGetErrorString(e));
+	}
+	// per-particle statuses of the simulation launches
+	for (int k = 0; k < ns && status == BEEP_OK; k++) {
+		std::vector<int32_t> ps(N);
+		if (cudaMemcpy(ps.data(), q[k]->bd.status, 4 * (size_t)N, cudaMemcpyDeviceToHost) != cudaSuccess) {
+			bail(BEEP_DEVICE_ERROR, "status copy");
+			break;
+		}
+		for (int p = 0; p < N; p++)
+			if (ps[p] != 0) { bail((beep_status)ps[p], "section " + std::to_string(k) + " particle " + std::to_string(p)); break; }
+	}
+	if (status == BEEP_OK && bst != 0) bail((beep_status)bst, "resampling found no particle (non-finite weights)");
+	cudaStreamSynchronize(st);
+	work.release();
+	cleanup();
+	if (status != BEEP_OK) return fail(status, err);
+	double total = 0.0;
+	for (int k = 0; k < ns; k++) total += ob[k];
+	*r->loglik_out = total;
+	if (r->loglik_section_out) memcpy(r->loglik_section_out, ob.data(), 8 * (size_t)ns);
+	return BEEP_OK;
+}

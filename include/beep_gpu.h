@@ -200,6 +200,33 @@ BEEP_API int32_t beep_batch_launches(const beep_batch *batch);   /* kernels per 
 BEEP_API beep_status beep_batch_bytes(const beep_batch *batch, int64_t *h2d, int64_t *d2h);
 BEEP_API beep_status beep_batch_destroy(beep_batch *batch);
 
+/* Bootstrap particle filter of PMCMC (PMCMC::obs_prob + bootstrap,
+ * src/pmcmc.cc:180-268; ancestor swap Mpi::end_sec_swap, src/mpi.cc:215-327)
+ * for one parameter set, run entirely on the device.  Particle slot p draws its
+ * transitions from stream p; the j-th resampling uniform of section s is word
+ * 0 of Philox({j, s, resample_stream, 3<<24}).  Sections are contiguous and
+ * cover [0, ndivision) (ObservationModel::split_observations,
+ * src/obsmodel.cc:326-348).  Outputs: the log-likelihood estimate
+ * sum_s (invT Lmax_s + log(sum_p w_p / N)), and optionally the per-section
+ * terms, per-section L [nsection][nparticle] and ancestors
+ * [nsection][nparticle] (backpart[s+1] of the reference).  Host buffers. */
+typedef struct beep_pf_request {
+	int32_t nparticle;
+	const beep_param_tables *tables;
+	uint64_t seed;
+	uint32_t resample_stream;
+	double invT;
+	int32_t nsection;
+	const int32_t *section_ti, *section_tf;   /* [nsection] */
+	int32_t form;                             /* beep_form of the simulation */
+	double *loglik_out;                       /* [1] */
+	double *loglik_section_out;               /* [nsection] or NULL */
+	double *L_out;                            /* [nsection][nparticle] or NULL */
+	int32_t *ancestors_out;                   /* [nsection][nparticle] or NULL */
+} beep_pf_request;
+
+BEEP_API beep_status beep_pf_loglik(beep_model *model, const beep_pf_request *request);
+
 /* Plain FP64 simulation that allocates no memory on the GPU.  No counterpart
  * in the reference: it serves callers that cannot call cudaMalloc -- an
  * application whose allocator or fixed memory budget owns all device memory,

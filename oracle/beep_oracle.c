@@ -465,3 +465,66 @@ int beep_oracle_simulate(const beep_model_desc *m, const beep_sim_batch *b, int 
 	obs_index_free(&ix);
 	return status;
 }
+
+
+/* ---- particle filter: src/pmcmc.cc:180-268, src/mpi.cc:215-327 ----------- */
+
+int beep_oracle_pf(const beep_model_desc *m, const beep_param_tables *tab, int32_t N, uint64_t seed,
+                   uint32_t resample_stream, double invT, int32_t form, int32_t nsec, const int32_t *sec_ti,
+                   const int32_t *sec_tf, double *loglik, double *loglik_sec, double *L_out, int32_t *anc_out,
+                   int nthreads)
+{
+	(void)form;
+	if (!m || !tab || N <= 0 || nsec <= 0) return BEEP_BAD_INPUT;
+	const size_t popsz = (size_t)m->narea * m->ncomp * m->ndemocatpos;
+	int32_t *pops = malloc(sizeof(int32_t) * popsz * N), *pout = malloc(sizeof(int32_t) * popsz * N);
+	double *L = malloc(sizeof(double) * N), *w = malloc(sizeof(double) * N), *wsum = malloc(sizeof(double) * N);
+	int32_t *bp = malloc(sizeof(int32_t) * N), *extra = malloc(sizeof(int32_t) * N);
+	if (!pops || !pout || !L || !w || !wsum || !bp || !extra) return BEEP_OOM;
+	const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+	double obprob = 0.0;
+	int st = BEEP_OK;
+	for (int32_t s = 0; s < nsec && st == BEEP_OK; s++) {
+		beep_sim_batch b;
+		memset(&b, 0, sizeof b);
+		b.nparticle = N; b.ngroup = 1; b.groups = tab; b.seed = seed;
+		b.ti = sec_ti[s]; b.tf = sec_tf[s];
+		b.pop_in = s > 0 ? pops : NULL;
+		b.L_out = L; b.pop_out = pout;
+		st = beep_oracle_simulate(m, &b, nthreads);
+		if (st != BEEP_OK) break;
+		if (L_out) memcpy(L_out + (size_t)s * N, L, sizeof(double) * N);
+		/* PMCMC::bootstrap */
+		double Lmax = -1000000000.0;
+		for (int32_t p = 0; p < N; p++) if (L[p] > Lmax) Lmax = L[p];
+		double sum = 0.0;
+		for (int32_t p = 0; p < N; p++) {
+			w[p] = exp(invT * (L[p] - Lmax));
+			sum += w[p];
+			wsum[p] = sum;
+		}
+		const double ob = invT * Lmax + log(sum / N);
+		if (loglik_sec) loglik_sec[s] = ob;
+		obprob += ob;
+		for (int32_t p = 0; p < N; p++) bp[p] = -1;
+		int32_t ne = 0;
+		for (int32_t j = 0; j < N; j++) {
+			beep_u32x4 c = {{(uint32_t)j, (uint32_t)s, resample_stream, BEEP_PURPOSE_RESAMPLE << 24}};
+			beep_u32x4 r = beep_philox4x32_10(c, k0, k1);
+			const double z = beep_u01(r.v[0]) * sum;
+			int32_t pp = 0;
+			while (pp < N && z > wsum[pp]) pp++;
+			if (pp == N) { st = BEEP_NAN_RATE; break; }
+			if (bp[pp] == -1) bp[pp] = pp;
+			else extra[ne++] = pp;
+		}
+		for (int32_t p = 0; p < N && st == BEEP_OK; p++)
+			if (bp[p] == -1) bp[p] = extra[--ne];
+		if (anc_out) memcpy(anc_out + (size_t)s * N, bp, sizeof(int32_t) * N);
+		/* Mpi::end_sec_swap: slot p continues from its ancestor's population */
+		for (int32_t p = 0; p < N; p++) memcpy(pops + (size_t)p * popsz, pout + (size_t)bp[p] * popsz, sizeof(int32_t) * popsz);
+	}
+	if (loglik) *loglik = obprob;
+	free(pops); free(pout); free(L); free(w); free(wsum); free(bp); free(extra);
+	return st;
+}

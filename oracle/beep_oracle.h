@@ -29,6 +29,20 @@ extern "C" {
  * (0 = all).  Returns 0 on success, else a beep_status code. */
 int beep_oracle_simulate(const beep_model_desc *m, const beep_sim_batch *b, int nthreads);
 
+/* Bootstrap particle filter (PMCMC::obs_prob + bootstrap + Mpi::end_sec_swap,
+ * src/pmcmc.cc:180-268, src/mpi.cc:215-327): per section, simulate every
+ * particle slot p from its carried population (stream p), weight
+ * w = exp(invT (L - Lmax)), add invT Lmax + log(sum w / N) to the estimate, and
+ * resample with the "selected particle keeps its own slot" placement; the j-th
+ * resampling uniform of section s is word 0 of
+ * Philox({j, s, resample_stream, RESAMPLE<<24}).  Outputs: the estimate, the
+ * per-section terms, per-section L [nsec][N] and ancestors [nsec][N] (each may
+ * be NULL). */
+int beep_oracle_pf(const beep_model_desc *m, const beep_param_tables *tab, int32_t N, uint64_t seed,
+                   uint32_t resample_stream, double invT, int32_t form, int32_t nsec, const int32_t *sec_ti,
+                   const int32_t *sec_tf, double *loglik, double *loglik_sec, double *L_out, int32_t *anc_out,
+                   int nthreads);
+
 /* One Poisson draw from the keyed stream (exposed for sampler tests). */
 int32_t beep_oracle_poisson(double mean, uint64_t seed, uint32_t col, uint32_t tr, uint32_t step,
                             uint32_t stream);

@@ -31,6 +31,12 @@
 
 #include "inputs.hh"
 #include "details.hh"
+#include "output.hh"
+// The particle-filter driver below calls the reference's own private
+// PMCMC::bootstrap; the access specifiers are lifted for this translation unit.
+#define private public
+#include "pmcmc.hh"
+#undef private
 #include "mpi.hh"
 #include "data.hh"
 #include "model.hh"
@@ -66,6 +72,28 @@ Replay g_replay;
 }  // namespace
 
 extern "C" int __real__Z14poisson_sampled(double lam);
+extern "C" double __real__Z3ranv();
+
+// ran() (src/utils.cc:50-69) answered from the keyed stream while a bootstrap
+// runs: the k-th call of section sec takes word 0 of
+// Philox({k, sec, stream, RESAMPLE<<24}) as u = (w + 1/2) 2^-32.
+namespace {
+struct RanReplay {
+	bool active = false;
+	uint32_t k0 = 0, k1 = 0, stream = 0, sec = 0, k = 0;
+};
+RanReplay g_ran;
+}  // namespace
+
+extern "C" double __wrap__Z3ranv()
+{
+	RanReplay &r = g_ran;
+	if (!r.active) return __real__Z3ranv();
+	beep_u32x4 c = {{r.k, r.sec, r.stream, BEEP_PURPOSE_RESAMPLE << 24}};
+	beep_u32x4 o = beep_philox4x32_10(c, r.k0, r.k1);
+	r.k++;
+	return beep_u01(o.v[0]);
+}
 
 // Answers the reference's k-th poisson_sample(mean) call of a simulate(ti,tf)
 // with the keyed draw of the (sett, c, tr, dp) cell that call belongs to.  The
@@ -380,6 +408,48 @@ int main(int argc, char **argv)
 							for (unsigned dp = 0; dp < DP; dp++) popt.push_back((int32_t)state.pop[s][c][co][dp]);
 					}
 			}
+		}
+		if (pf && opt.count("pfn")) {
+			// PMCMC::obs_prob (src/pmcmc.cc:180-207) driven section by section with
+			// the reference's own end_sec_swap and bootstrap; particle slot p draws
+			// from stream p, the resampling uniforms from stream `pfstream`.
+			const int NP = atoi(opt["pfn"].c_str());
+			const uint32_t pfstream = opt.count("pfstream") ? (uint32_t)strtoul(opt["pfstream"].c_str(), nullptr, 0) : 0xABCDu;
+			Output output(details, data, model, inputs, obsmodel, mpi);
+			PMCMC pm(details, data, model, inputs, output, obsmodel, mpi);
+			if ((int)pm.Ntot != NP) { fprintf(stderr, "nparticle must equal pfn\n"); return 2; }
+			pm.particle.clear();
+			for (int p2 = 0; p2 < NP; p2++) pm.particle.push_back(State(details, data, model, obsmodel));
+			for (int p2 = 0; p2 < NP; p2++) pm.particle[p2].set_param(thetas[gidx]);
+			std::vector<double> L(NP), Lsecs, obp;
+			std::vector<int32_t> anc;
+			double obprob = 0.0;
+			for (unsigned sec = 0; sec < obsmodel.nsection; sec++) {
+				const unsigned ti = obsmodel.section_ti[sec], tf2 = obsmodel.section_tf[sec];
+				if (sec > 0) mpi.end_sec_swap(pm.particle, ti, pm.backpart[sec], pm.buffersize);
+				for (int p2 = 0; p2 < NP; p2++) {
+					g_replay.st = &pm.particle[p2]; g_replay.stream = (uint32_t)p2;
+					g_replay.sett = ti; g_replay.c = 0; g_replay.tr = 0; g_replay.dp = 0;
+					g_replay.active = true;
+					pm.particle[p2].simulate(ti, tf2);
+					g_replay.active = false;
+					L[p2] = obsmodel.calculate_section(&pm.particle[p2], sec);
+				}
+				Lsecs.insert(Lsecs.end(), L.begin(), L.end());
+				g_ran.active = true; g_ran.k0 = g_replay.k0; g_ran.k1 = g_replay.k1;
+				g_ran.stream = pfstream; g_ran.sec = sec; g_ran.k = 0;
+				const double ob = pm.bootstrap(sec, L);
+				g_ran.active = false;
+				obprob += ob;
+				obp.push_back(ob);
+				for (int p2 = 0; p2 < NP; p2++) anc.push_back((int32_t)pm.backpart[sec + 1][p2]);
+			}
+			B.scalar_d(gp + "pf.obprob", obprob);
+			B.d(gp + "pf.obprob_section", obp);
+			B.d(gp + "pf.L_section", Lsecs, {obsmodel.nsection, (uint64_t)NP});
+			B.i(gp + "pf.ancestors", anc, {obsmodel.nsection, (uint64_t)NP});
+			B.scalar_d(gp + "pf.invT", pm.invT);
+			B.i(gp + "pf.stream", {(int32_t)pfstream});
 		}
 		B.d(gp + "L", Lfull);
 		if (pf) B.d(gp + "L_section", Lsec, {(uint64_t)npart, obsmodel.nsection});

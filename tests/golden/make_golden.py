@@ -33,11 +33,15 @@ from beep_gb300 import bundle, synth  # noqa: E402
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
 
 
-def run_harness(workdir, toml, out, npart, ntraj, seed, mode, pf=False, theta=None):
+def run_harness(workdir, toml, out, npart, ntraj, seed, mode, pf=False, theta=None, pfn=0):
     cmd = [HARNESS, f"out={out}", f"npart={npart}", f"ntraj={ntraj}", f"seed={seed}", f"pf={1 if pf else 0}"]
     if theta is not None:
         cmd.append(f"theta={theta}")
+    if pfn:
+        cmd.append(f"pfn={pfn}")
     cmd += ["--", f"inputfile={os.path.basename(toml)}", f"mode={mode}"]
+    if pfn:
+        cmd += [f"nparticle={pfn}", "nsample=400", "nburnin=200", "invT=1"]
     r = subprocess.run(cmd, cwd=workdir, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"harness failed:\n{r.stdout}\n{r.stderr}")
@@ -87,7 +91,7 @@ def obs_values_from(b, w: synth.Workload):
     return out
 
 
-def make_fixture(name, w: synth.Workload, npart, ntraj, seed, pf=False, theta_rows=None, keep_dir=None):
+def make_fixture(name, w: synth.Workload, npart, ntraj, seed, pf=False, theta_rows=None, keep_dir=None, pfn=0):
     work = tempfile.mkdtemp(prefix=f"golden_{name}_")
     try:
         toml = synth.write_beep_inputs(w, work)
@@ -102,7 +106,7 @@ def make_fixture(name, w: synth.Workload, npart, ntraj, seed, pf=False, theta_ro
                 for row in theta_rows:
                     f.write(",".join(repr(float(x)) for x in row) + "\n")
         out = os.path.join(HERE, f"{name}.bnd")
-        run_harness(work, toml, out, npart, ntraj, seed, mode, pf=pf, theta=theta)
+        run_harness(work, toml, out, npart, ntraj, seed, mode, pf=pf, theta=theta, pfn=pfn)
         if keep_dir:
             shutil.copytree(work, os.path.join(keep_dir, name), dirs_exist_ok=True)
         print(f"{name}: {os.path.getsize(out) / 1e3:.0f} kB")
@@ -122,14 +126,14 @@ def main():
     make_fixture("tiny_sim", tiny, npart=8, ntraj=3, seed=0x1234567890ABCDEF)
     # particle-filter sections need period >= 10 x the largest observation step (src/details.cc:115)
     tiny70 = synth.seir_hd_small(seed=20260102, narea=3, nage=2, days=70, name="tiny70")
-    make_fixture("tiny_pf", tiny70, npart=6, ntraj=2, seed=0x0F1E2D3C4B5A6978, pf=True)
+    make_fixture("tiny_pf", tiny70, npart=6, ntraj=2, seed=0x0F1E2D3C4B5A6978, pf=True, pfn=32)
     # one age group (the reference's nage == 1 branch of get_NMI, src/state.cc:555-560)
     one = synth.seir_hd_small(seed=20260101, narea=5, nage=1, days=30, name="oneage")
     make_fixture("oneage_sim", one, npart=6, ntraj=2, seed=77)
     # the 10-area x 3-age plain PMCMC workload at full horizon
     c0 = synth.seir_hd_small(seed=20260000, narea=10, nage=3, days=100, name="c0")
     make_fixture("c0_sim", c0, npart=16, ntraj=1, seed=20260000)
-    make_fixture("c0_pf", c0, npart=8, ntraj=1, seed=20260001, pf=True)
+    make_fixture("c0_pf", c0, npart=8, ntraj=1, seed=20260001, pf=True, pfn=64)
 
 
 if __name__ == "__main__":

@@ -85,3 +85,35 @@ def test_device_errors_are_statuses(built):
     ok = dm.simulate(capi.Batch(m, tabs, 2, seed))
     np.testing.assert_allclose(ok.L, b["g0.L"][:2], rtol=L_RTOL)
     dm.close()
+
+
+@pytest.mark.parametrize("name", PF_FIXTURES)
+def test_particle_filter_matches_reference(built, name):
+    """Device particle filter (plain form) vs the reference's own bootstrap and
+    ancestor swap: identical ancestors, estimate and section terms to 1e-12."""
+    b, m, tabs, seed = load(name)
+    N = b["g0.pf.ancestors"].shape[1]
+    dm = capi.DeviceModel(m)
+    ll, lls, L, anc = dm.pf_loglik(tabs[0], N, seed, int(b["g0.pf.stream"][0]), float(b["g0.pf.invT"][0]),
+                                   m.sections)
+    assert np.array_equal(anc, b["g0.pf.ancestors"])
+    np.testing.assert_allclose(L, b["g0.pf.L_section"], rtol=L_RTOL, atol=1e-12)
+    np.testing.assert_allclose(lls, b["g0.pf.obprob_section"], rtol=L_RTOL, atol=1e-12)
+    np.testing.assert_allclose(ll, b["g0.pf.obprob"][0], rtol=L_RTOL)
+    dm.close()
+
+
+def test_particle_filter_fast_form_and_oracle(built):
+    """The filter with the fast form runs to a finite estimate, and the plain
+    form agrees with the oracle's filter on a larger particle count."""
+    from oracle_lib import oracle_pf
+    b, m, tabs, seed = load("c0_pf")
+    dm = capi.DeviceModel(m)
+    N = 256
+    llg, _, _, ancg = dm.pf_loglik(tabs[0], N, seed + 3, 77, 1.0, m.sections)
+    llo, _, _, anco = oracle_pf(m, tabs[0], N, seed + 3, 77, 1.0, m.sections)
+    assert np.array_equal(ancg, anco)
+    np.testing.assert_allclose(llg, llo, rtol=L_RTOL)
+    llf, _, _, ancf = dm.pf_loglik(tabs[0], N, seed + 3, 77, 1.0, m.sections, form=capi.FORM_FAST)
+    assert np.isfinite(llf) and ancf.min() >= 0 and ancf.max() < N
+    dm.close()

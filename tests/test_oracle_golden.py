@@ -67,3 +67,17 @@ def test_section_split_equals_whole_run():
     # counts agree up to the first step where the rebuilt Imap differs from the
     # incremental one in the last bits; require the first half exactly
     assert np.array_equal(a.transnum, whole.transnum[:, :t1])
+
+
+@pytest.mark.parametrize("name", PF_FIXTURES)
+def test_oracle_particle_filter_matches_reference(name):
+    """Bootstrap particle filter: the reference's own end_sec_swap + bootstrap
+    (replayed uniforms) vs the oracle: same ancestors, estimate to 1e-12."""
+    from oracle_lib import oracle_pf
+    b, m, tabs, seed = load(name)
+    N = b["g0.pf.ancestors"].shape[1]
+    ll, lls, L, anc = oracle_pf(m, tabs[0], N, seed, int(b["g0.pf.stream"][0]), float(b["g0.pf.invT"][0]), m.sections)
+    assert np.array_equal(anc, b["g0.pf.ancestors"])
+    np.testing.assert_allclose(L, b["g0.pf.L_section"], rtol=L_RTOL, atol=1e-12)
+    np.testing.assert_allclose(lls, b["g0.pf.obprob_section"], rtol=L_RTOL, atol=1e-12)
+    np.testing.assert_allclose(ll, b["g0.pf.obprob"][0], rtol=L_RTOL)
