@@ -29,6 +29,7 @@ UNITS = {
     "sim_fast.cu": [],
     "noalloc.cu": [],
     "pf.cu": [],
+    "abc_weights.cu": [],
 }
 
 

@@ -234,6 +234,9 @@ def lib():
                                                   C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
                                                   C.c_void_p]
         L.beep_simulate_plain_noalloc.restype = C.c_int32
+        L.beep_abcsmc_weights.argtypes = [C.c_int32, C.c_int32, _f64p, _f64p, C.c_int32, _f64p, _f64p, _f64p,
+                                          C.c_double, C.c_int32, _f64p]
+        L.beep_abcsmc_weights.restype = C.c_int32
         L.beep_pf_loglik.argtypes = [C.c_void_p, C.POINTER(PFRequest)]
         L.beep_pf_loglik.restype = C.c_int32
         for f in ("beep_device_init", "beep_model_create", "beep_model_destroy", "beep_simulate", "beep_batch_create",
@@ -351,3 +354,17 @@ class DeviceBatch:
             self.close()
         except Exception:
             pass
+
+
+def abcsmc_weights(theta_new, logprior_new, theta_last, w_last, inv_cov, size: float, normalise: bool = True):
+    """ABC-SMC importance weights on the GPU (beep_abcsmc_weights)."""
+    tn = _f64(theta_new)
+    lp = _f64(logprior_new)
+    tl = _f64(theta_last)
+    wl = _f64(w_last)
+    ic = _f64(inv_cov)
+    out = np.zeros(tn.shape[0])
+    check(lib().beep_abcsmc_weights(tn.shape[1], tn.shape[0], _ptr(tn, C.c_double), _ptr(lp, C.c_double),
+                                    tl.shape[0], _ptr(tl, C.c_double), _ptr(wl, C.c_double), _ptr(ic, C.c_double),
+                                    size, 1 if normalise else 0, _ptr(out, C.c_double)))
+    return out

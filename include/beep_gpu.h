@@ -227,6 +227,20 @@ typedef struct beep_pf_request {
 
 BEEP_API beep_status beep_pf_loglik(beep_model *model, const beep_pf_request *request);
 
+/* ABC-SMC importance weights of a generation (ABCSMC::calculate_particle_weight
+ * + MVN::probability, src/abcsmc.cc:260-271, src/mvn.cc:185-196):
+ *   w_i = exp(logprior_i) / sum_j w_last_j exp(-0.5 (d/size)^T inv_cov (d/size)),
+ *   d = theta_new_i - theta_last_j over the nvar inferred parameters
+ * ([nnew][nvar], [nlast][nvar] row-major, inv_cov [nvar][nvar], nvar <= 16);
+ * with normalise != 0 the weights are divided by their mean
+ * (normalise_particle_weights, src/abcsmc.cc:275-283).  The pairwise kernel
+ * terms are computed in FP32 on the GPU and summed with compensation; the
+ * per-particle sums, the prior factor and the normalisation are FP64. */
+BEEP_API beep_status beep_abcsmc_weights(int32_t nvar, int32_t nnew, const double *theta_new,
+                                         const double *logprior_new, int32_t nlast, const double *theta_last,
+                                         const double *w_last, const double *inv_cov, double size,
+                                         int32_t normalise, double *w_out);
+
 /* Plain FP64 simulation that allocates no memory on the GPU.  No counterpart
  * in the reference: it serves callers that cannot call cudaMalloc -- an
  * application whose allocator or fixed memory budget owns all device memory,

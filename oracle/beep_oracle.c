@@ -528,3 +528,34 @@ int beep_oracle_pf(const beep_model_desc *m, const beep_param_tables *tab, int32
 	free(pops); free(pout); free(L); free(w); free(wsum); free(bp); free(extra);
 	return st;
 }
+
+
+/* ---- ABC-SMC importance weights: src/abcsmc.cc:260-283, src/mvn.cc:185-196 */
+
+void beep_oracle_abcsmc_weights(int32_t nvar, int32_t nnew, const double *theta_new, const double *logprior_new,
+                                int32_t nlast, const double *theta_last, const double *w_last,
+                                const double *inv_cov, double size, int32_t normalise, double *w_out)
+{
+	for (int32_t i = 0; i < nnew; i++) {
+		const double *pend = theta_new + (size_t)i * nvar;
+		double sum = 0.0;
+		for (int32_t j = 0; j < nlast; j++) {
+			const double *pstart = theta_last + (size_t)j * nvar;
+			double q = 0;                                   /* MVN::probability */
+			for (int32_t v1 = 0; v1 < nvar; v1++)
+				for (int32_t v2 = 0; v2 < nvar; v2++) {
+					double val1 = pend[v1] - pstart[v1];
+					double val2 = pend[v2] - pstart[v2];
+					q += (val1 / size) * inv_cov[v1 * nvar + v2] * (val2 / size);
+				}
+			sum += w_last[j] * exp(-0.5 * q);
+		}
+		w_out[i] = exp(logprior_new[i]) / sum;
+	}
+	if (normalise) {
+		double wsum = 0.0;
+		for (int32_t i = 0; i < nnew; i++) wsum += w_out[i];
+		wsum /= nnew;
+		for (int32_t i = 0; i < nnew; i++) w_out[i] /= wsum;
+	}
+}

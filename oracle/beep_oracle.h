@@ -43,6 +43,12 @@ int beep_oracle_pf(const beep_model_desc *m, const beep_param_tables *tab, int32
                    const int32_t *sec_tf, double *loglik, double *loglik_sec, double *L_out, int32_t *anc_out,
                    int nthreads);
 
+/* ABC-SMC weights (src/abcsmc.cc:260-283, src/mvn.cc:185-196), FP64 as the
+ * reference computes them. */
+void beep_oracle_abcsmc_weights(int32_t nvar, int32_t nnew, const double *theta_new, const double *logprior_new,
+                                int32_t nlast, const double *theta_last, const double *w_last,
+                                const double *inv_cov, double size, int32_t normalise, double *w_out);
+
 /* One Poisson draw from the keyed stream (exposed for sampler tests). */
 int32_t beep_oracle_poisson(double mean, uint64_t seed, uint32_t col, uint32_t tr, uint32_t step,
                             uint32_t stream);

@@ -33,6 +33,9 @@ def oracle_lib():
                                      C.c_uint32, C.c_double, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         L.beep_oracle_pf.restype = C.c_int
+        L.beep_oracle_abcsmc_weights.argtypes = [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
+                                                 C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]
+        L.beep_oracle_abcsmc_weights.restype = None
         _LIB = L
     return _LIB
 
@@ -61,3 +64,17 @@ def oracle_pf(model: capi.Model, tables: capi.Tables, N: int, seed: int, resampl
     if st != 0:
         raise RuntimeError(f"oracle particle filter failed: {capi.STATUS.get(st, st)}")
     return float(ll[0]), lls, L, anc
+
+
+def oracle_abcsmc_weights(theta_new, logprior_new, theta_last, w_last, inv_cov, size, normalise=True):
+    import numpy as np
+    tn = np.ascontiguousarray(theta_new, np.float64)
+    lp = np.ascontiguousarray(logprior_new, np.float64)
+    tl = np.ascontiguousarray(theta_last, np.float64)
+    wl = np.ascontiguousarray(w_last, np.float64)
+    ic = np.ascontiguousarray(inv_cov, np.float64)
+    out = np.zeros(tn.shape[0])
+    oracle_lib().beep_oracle_abcsmc_weights(tn.shape[1], tn.shape[0], tn.ctypes.data, lp.ctypes.data, tl.shape[0],
+                                            tl.ctypes.data, wl.ctypes.data, ic.ctypes.data, float(size),
+                                            1 if normalise else 0, out.ctypes.data)
+    return out
