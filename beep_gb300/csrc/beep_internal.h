@@ -34,7 +34,11 @@ struct ModelDev {
 	const float *obs_value_f;            // [nobs]
 	const float *obs_factor_f, *obs_shape_f;  // [nobs]
 	const int32_t *obs_cells_f;          // cells in the fast form's column-major shared layout:
-	                                     // tr*ncol + col (transition) or -1-(co*ncol + col) (population)
+	                                     // row*ncol + col (row = tn_row[tr]) or -1-(co*ncol + col) (population)
+	const int32_t *obs_cells_full;       // the same with row = tr (all transition rows stored)
+	int32_t tn_row[16];                  // row of each observed transition in the fast form's counts, or -1
+	int32_t tn_rows;                     // number of observed transitions
+	int32_t pop_obs;                     // some observation reads populations
 	int32_t dp_age_unique;               // each age has exactly one dp per strain
 	float inv_popsize_f;                 // 1 / Data::popsize
 };
@@ -64,6 +68,7 @@ struct BatchDev {
 	const int32_t *step_obs;            // scored-position of obs active at each step
 	// fast form: observation accumulator slots and completion lists
 	int32_t nslots, m_in_smem, nefoi_stage;
+	int32_t tn_full, pop_single;        // fast form: store every transition row / one population buffer
 	void *gstate;                       // fast form, large models: per-particle state in global memory (or null)
 	size_t gstate_stride;               // bytes per particle   // nefoi_stage: efoi age tables staged in shared memory (0 = read from L2)
 	const int4 *tasks;                  // [2 * step_ptr[tf-ti]] per (step, active observation):
@@ -84,7 +89,8 @@ struct BatchDev {
 // launchers
 int launch_sim_plain(const ModelDev &m, const BatchDev &b, void *stream);   // sim_plain.cu
 int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream);    // sim_fast.cu
-size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_stage, bool state_global);
+size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_stage, bool state_global, int tnrows,
+                       bool pop_single);
 size_t fast_gstate_stride(const ModelDev &m);
 int fast_threads();
 

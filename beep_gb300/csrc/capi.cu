@@ -166,17 +166,29 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	for (int j = 0; j < nnz; j++) csc_val_f[j] = (float)csc_val[j];
 	std::vector<float2> obs_np(nobs > 0 ? nobs : 1);
 	std::vector<float> obs_value_f(nobs > 0 ? nobs : 1), obs_factor_f(nobs > 0 ? nobs : 1), obs_shape_f(nobs > 0 ? nobs : 1);
-	std::vector<int32_t> obs_cells_f(ncells > 0 ? ncells : 1);
+	std::vector<int32_t> obs_cells_f(ncells > 0 ? ncells : 1), obs_cells_full(ncells > 0 ? ncells : 1);
+	int32_t tn_row[16];
+	int32_t tn_rows = 0, pop_obs = 0;
 	{
 		const int ncol = A * DP;
+		std::vector<int> seen(T, 0);
+		for (int q = 0; q < ncells; q++) {
+			const int32_t cell = d->obs_cells[q];
+			if (cell >= 0) seen[(cell / DP) % T] = 1;
+			else pop_obs = 1;
+		}
+		for (int tr = 0; tr < 16; tr++) tn_row[tr] = -1;
+		for (int tr = 0; tr < T && tr < 16; tr++)
+			if (seen[tr]) tn_row[tr] = tn_rows++;
 		for (int q = 0; q < ncells; q++) {
 			const int32_t cell = d->obs_cells[q];
 			if (cell >= 0) {
 				const int c = cell / (T * DP), tr = (cell / DP) % T, dp = cell % DP;
-				obs_cells_f[q] = tr * ncol + c * DP + dp;
+				obs_cells_f[q] = (tr < 16 ? tn_row[tr] : 0) * ncol + c * DP + dp;
+				obs_cells_full[q] = tr * ncol + c * DP + dp;
 			} else {
 				const int k = -1 - cell, c = k / (C * DP), co = (k / DP) % C, dp = k % DP;
-				obs_cells_f[q] = -1 - (co * ncol + c * DP + dp);
+				obs_cells_f[q] = obs_cells_full[q] = -1 - (co * ncol + c * DP + dp);
 			}
 		}
 	}
@@ -197,6 +209,7 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	for (int o = 0; o < nobs; o++) m->max_obs_spline = std::max(m->max_obs_spline, d->obs_factor_spline[o]);
 	m->obs_cell_ptr_h.assign(d->obs_cell_ptr, d->obs_cell_ptr + (nobs > 0 ? nobs + 1 : 0));
 	m->obs_cells_f_h.assign(obs_cells_f.begin(), obs_cells_f.begin() + ncells);
+	m->obs_cells_full_h.assign(obs_cells_full.begin(), obs_cells_full.begin() + ncells);
 	m->obs_factor_f_h.assign(obs_factor_f.begin(), obs_factor_f.begin() + nobs);
 	m->trans_from_h.assign(d->trans_from, d->trans_from + T);
 	m->trans_to_h.assign(d->trans_to, d->trans_to + T);
@@ -212,7 +225,7 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	       o_ofa = L.add(8 * (size_t)nobs), o_md = L.add(4 * (size_t)A * A), o_mdg = L.add(4 * (size_t)A),
 	       o_mfc = L.add(4 * (size_t)A), o_cvf = L.add(4 * (size_t)nnz), o_onp = L.add(8 * (size_t)nobs),
 	       o_ovf = L.add(4 * (size_t)nobs), o_off = L.add(4 * (size_t)nobs), o_oshf = L.add(4 * (size_t)nobs),
-	       o_ocf = L.add(4 * (size_t)ncells);
+	       o_ocf = L.add(4 * (size_t)ncells), o_ocfull = L.add(4 * (size_t)ncells);
 	std::vector<char> host(L.size);
 	auto put = [&](size_t off, const void *src, size_t n) { if (n) memcpy(host.data() + off, src, n); };
 	put(o_tf, d->trans_from, 4 * T); put(o_tt, d->trans_to, 4 * T); put(o_age, d->democatpos_age, 4 * DPS);
@@ -234,6 +247,7 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	if (nobs > 0) put(o_off, obs_factor_f.data(), 4 * (size_t)nobs);
 	if (nobs > 0) put(o_oshf, obs_shape_f.data(), 4 * (size_t)nobs);
 	if (ncells > 0) put(o_ocf, obs_cells_f.data(), 4 * (size_t)ncells);
+	if (ncells > 0) put(o_ocfull, obs_cells_full.data(), 4 * (size_t)ncells);
 	cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
 	if (e == cudaSuccess) e = m->model_mem.reserve(L.size);
 	if (e == cudaSuccess) e = cudaMemcpy(m->model_mem.ptr, host.data(), L.size, cudaMemcpyHostToDevice);
@@ -265,6 +279,10 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	md.obs_factor_f = (const float *)(base + o_off);
 	md.obs_shape_f = (const float *)(base + o_oshf);
 	md.obs_cells_f = (const int32_t *)(base + o_ocf);
+	md.obs_cells_full = (const int32_t *)(base + o_ocfull);
+	for (int tr = 0; tr < 16; tr++) md.tn_row[tr] = tn_row[tr];
+	md.tn_rows = tn_rows;
+	md.pop_obs = pop_obs;
 	{
 		std::vector<int> cnt(G, 0);
 		for (int dp = 0; dp < DPS; dp++) cnt[d->democatpos_age[dp]]++;
@@ -521,7 +539,8 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 				float fac = m->obs_factor_f_h[o];
 				int32_t fbits;
 				memcpy(&fbits, &fac, 4);
-				t[0] = q->slot_of[pos]; t[1] = o; t[2] = nc > 0 ? m->obs_cells_f_h[c0] : 0;
+				const std::vector<int32_t> &enc = b->transnum_out ? m->obs_cells_full_h : m->obs_cells_f_h;
+				t[0] = q->slot_of[pos]; t[1] = o; t[2] = nc > 0 ? enc[c0] : 0;
 				t[3] = (int32_t)((uint32_t)nc | (last ? 0x80000000u : 0u));
 				t[4] = fbits; t[5] = m->obs_spline[o]; t[6] = c0; t[7] = 0;
 			}
@@ -532,12 +551,19 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 			for (int g = 1; g < b->ngroup; g++)
 				if (b->groups[g].nefoi != b->groups[0].nefoi) nefoi = 0;
 		q->bd.nefoi_stage = nefoi * m->G <= 1024 ? nefoi : 0;
-		q->state_global = fast_smem_bytes(m->dev, nslots, false, q->bd.nefoi_stage, false) > limit;
-		if (fast_smem_bytes(m->dev, nslots, false, q->bd.nefoi_stage, true) > limit || m->NS * m->A > 640 || m->G * m->G > 640) {
+		// counts of unobserved transitions are not stored unless a trajectory is requested; one
+		// population buffer suffices when no observation reads populations and strains do not mix
+		q->bd.tn_full = b->transnum_out ? 1 : 0;
+		q->bd.pop_single = (!m->dev.pop_obs && m->NS == 1 && !b->pop_traj_out) ? 1 : 0;
+		const int tnrows = q->bd.tn_full ? m->T : m->dev.tn_rows;
+		const bool ps = q->bd.pop_single != 0;
+		q->state_global = fast_smem_bytes(m->dev, nslots, false, q->bd.nefoi_stage, false, tnrows, ps) > limit;
+		if (fast_smem_bytes(m->dev, nslots, false, q->bd.nefoi_stage, true, tnrows, ps) > limit || m->NS * m->A > 640 ||
+		    m->G * m->G > 640 || m->T > 8) {
 			delete q;
-			return fail(BEEP_BAD_INPUT, "model too large for the fast form (observation slots or tables exceed shared memory)");
+			return fail(BEEP_BAD_INPUT, "model too large for the fast form (observation slots or tables exceed shared memory, or more than 8 transitions)");
 		}
-		q->bd.m_in_smem = fast_smem_bytes(m->dev, nslots, true, q->bd.nefoi_stage, q->state_global) <= limit ? 1 : 0;
+		q->bd.m_in_smem = fast_smem_bytes(m->dev, nslots, true, q->bd.nefoi_stage, q->state_global, tnrows, ps) <= limit ? 1 : 0;
 	}
 	auto bail = [&](beep_status s) { beep_batch_destroy(q); return s; };
 	st = stage_inputs(q);

@@ -98,7 +98,8 @@ struct beep_model {
 	beep::DevBuf model_mem;
 	// host copies used to prepare batches
 	int32_t A, G, DP, NS, C, T, S, period, dpt, nobs;
-	std::vector<int32_t> obs_sett_i, obs_sett_f, obs_spline, trans_from_h, trans_to_h, obs_cell_ptr_h, obs_cells_f_h;
+	std::vector<int32_t> obs_sett_i, obs_sett_f, obs_spline, trans_from_h, trans_to_h, obs_cell_ptr_h, obs_cells_f_h,
+	    obs_cells_full_h;
 	std::vector<float> obs_factor_f_h;
 	int32_t max_obs_spline = -1;
 	std::mutex mu;

@@ -35,6 +35,7 @@ namespace beep {
 namespace {
 
 constexpr int kFastThreads = 640;   // largest CTA; smaller models use 128 or 256 threads
+constexpr int kMaxT = 8;            // transitions per model in the fast form
 
 __constant__ float c_lnfact[32];   // log k!, k < 32
 
@@ -55,6 +56,7 @@ struct FastSmem {
 	float *slot;          // [nslots]
 	// per-particle constants
 	int32_t *from, *to;   // [T]
+	int32_t *trow;        // [T] row of the transition in tn, or -1 (not observed)
 	int32_t *age;         // [DPS]
 	float *inf;           // [C]
 	float *rate;          // [T][DP]
@@ -264,6 +266,7 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 	const int tid = threadIdx.x;
 	const int A = m.A, G = m.G, DP = m.DP, NS = m.NS, DPS = m.DPS, C = m.C, T = m.T;
 	const int ncol = A * DP, popsz = C * ncol, tnsz = T * ncol, agsz = NS * A * G;
+	const int tnrows = b.tn_full ? T : m.tn_rows;        // stored transition rows
 	const int nsteps = b.tf - b.ti;
 	const int lda = ms_lda(A);
 	const GroupDir dir = b.dirs[b.group_of ? b.group_of[p] : 0];
@@ -291,21 +294,22 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 			size_t go = 0;
 			auto gtake = [&](size_t bytes) { unsigned char *q = g + go; go += (bytes + 255) & ~(size_t)255; return q; };
 			s.pop0 = (int32_t *)gtake(4 * (size_t)popsz);
-			s.pop1 = (int32_t *)gtake(4 * (size_t)popsz);
-			s.tn = (int32_t *)gtake(4 * (size_t)tnsz);
+			s.pop1 = b.pop_single ? s.pop0 : (int32_t *)gtake(4 * (size_t)popsz);
+			s.tn = (int32_t *)gtake(4 * (size_t)tnrows * ncol);
 			s.Ic0 = (float *)gtake(4 * (size_t)agsz);
 			s.Ic1 = (float *)gtake(4 * (size_t)agsz);
 			s.Imap = (float *)gtake(4 * (size_t)agsz);
 		} else {
 			s.pop0 = (int32_t *)take(4 * (size_t)popsz);
-			s.pop1 = (int32_t *)take(4 * (size_t)popsz);
-			s.tn = (int32_t *)take(4 * (size_t)tnsz);
+			s.pop1 = b.pop_single ? s.pop0 : (int32_t *)take(4 * (size_t)popsz);
+			s.tn = (int32_t *)take(4 * (size_t)tnrows * ncol);
 			s.Ic0 = (float *)take(4 * (size_t)agsz);
 			s.Ic1 = (float *)take(4 * (size_t)agsz);
 			s.Imap = (float *)take(4 * (size_t)agsz);
 		}
 		s.slot = (float *)take(4 * (size_t)b.nslots);
 		s.from = (int32_t *)take(4 * (size_t)T);
+		s.trow = (int32_t *)take(4 * (size_t)T);
 		s.to = (int32_t *)take(4 * (size_t)T);
 		s.age = (int32_t *)take(4 * (size_t)DPS);
 		s.inf = (float *)take(4 * (size_t)C);
@@ -334,7 +338,11 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 	}
 	for (int k = tid; k < b.nslots; k += NT) s.slot[k] = 0.f;
 	for (int k = tid; k < agsz; k += NT) s.Ic1[k] = 0.f;
-	for (int k = tid; k < T; k += NT) { s.from[k] = m.trans_from[k]; s.to[k] = m.trans_to[k]; }
+	for (int k = tid; k < T; k += NT) {
+		s.from[k] = m.trans_from[k];
+		s.to[k] = m.trans_to[k];
+		s.trow[k] = b.tn_full ? k : m.tn_row[k];
+	}
 	for (int k = tid; k < DPS; k += NT) s.age[k] = m.dp_age[k];
 	for (int k = tid; k < C; k += NT) s.inf[k] = tb.inf[k];
 	for (int k = tid; k < T * DP; k += NT) s.rate[k] = tb.rate[k];
@@ -392,33 +400,47 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 			const int st = dp / DPS, dpl = dp - st * DPS, a = s.age[dpl];
 			U4 inv{0, 0, 0, 0};
 			uint32_t inv_call = 0xffffffffu;
-			for (int co = 0; co < C; co++) pn[co * ncol + col] = pc[co * ncol + col];
-			for (int tr = 0; tr < T; tr++) {
-				float mean;
-				if (tr == itr) {
-					const float popu = (float)pc[inf_from * ncol + c * DP + dpl];
-					if (popu <= 0.f) mean = 0.f;
-					else {
-						const float fac = m.M_factor_f[c], dg = m.M_diag_f[c];
-						const float *Ic = Ic_cur + (st * A + c) * G, *Im = s.Imap + (st * A + c) * G;
-						const float *N = Nm + a * G;
-						float nmi = 0.f;
+			// means of all transitions from the step's populations (src/state.cc:380-456)
+			float minf = 0.f;
+			{
+				const float popu = (float)pc[inf_from * ncol + c * DP + dpl];
+				if (popu > 0.f) {
+					const float fac = m.M_factor_f[c], dg = m.M_diag_f[c];
+					const float *Ic = Ic_cur + (st * A + c) * G, *Im = s.Imap + (st * A + c) * G;
+					const float *N = Nm + a * G;
+					float nmi = 0.f;
 #pragma unroll
-						for (int aa = 0; aa < MG; aa++) {
-							if (aa < G) {
-								const float id = Ic[aa] * dg;
-								nmi = fmaf(N[aa], (id + Im[aa]) * d + fac * id * omd, nmi);
-							}
+					for (int aa = 0; aa < MG; aa++) {
+						if (aa < G) {
+							const float id = Ic[aa] * dg;
+							nmi = fmaf(N[aa], (id + Im[aa]) * d + fac * id * omd, nmi);
 						}
-						nmi = fmaxf(nmi, 0.f);
-						const int sc = st * A + c;
-						const float eage = b.nefoi_stage ? s.eage[s.eref[sc] * G + a] : __ldg(tb.efoi_age + (size_t)s.eref[sc] * G + a);
-						mean = dt * popu * s.sus[dp] * (be[sc] * nmi + et[sc] * eage);
 					}
-				} else {
-					const float popu = (float)pc[s.from[tr] * ncol + col];
-					mean = popu <= 0.f ? 0.f : dt * popu * s.rate[tr * DP + dp];
+					nmi = fmaxf(nmi, 0.f);
+					const int sc = st * A + c;
+					const float eage = b.nefoi_stage ? s.eage[s.eref[sc] * G + a] : __ldg(tb.efoi_age + (size_t)s.eref[sc] * G + a);
+					minf = dt * popu * s.sus[dp] * (be[sc] * nmi + et[sc] * eage);
 				}
+			}
+			float mv[kMaxT];
+#pragma unroll
+			for (int tr = 0; tr < kMaxT; tr++) {
+				mv[tr] = 0.f;
+				if (tr < T) {
+					if (tr == itr) mv[tr] = minf;
+					else {
+						const float popu = (float)pc[s.from[tr] * ncol + col];
+						mv[tr] = popu <= 0.f ? 0.f : dt * popu * s.rate[tr * DP + dp];
+					}
+				}
+			}
+			if (pn != pc)
+				for (int co = 0; co < C; co++) pn[co * ncol + col] = pc[co * ncol + col];
+			// draws; the populations are updated after every mean was formed
+			for (int tr = 0; tr < T; tr++) {
+				float mean = mv[0];
+#pragma unroll
+				for (int k = 1; k < kMaxT; k++) mean = tr == k ? mv[k] : mean;
 				int32_t n = 0;
 				if (mean > 0.f) {
 					if (mean > 1.0e9f) atomicCAS(status, 0, BEEP_COUNT_OVERFLOW);
@@ -428,7 +450,8 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 						if (n < 0) { atomicCAS(status, 0, BEEP_TIMEOUT); n = 0; }
 					}
 				} else if (mean != mean) atomicCAS(status, 0, BEEP_NAN_RATE);
-				s.tn[tr * ncol + col] = n;
+				const int row = s.trow[tr];
+				if (row >= 0) s.tn[row * ncol + col] = n;
 				if (n != 0) {
 					pn[s.from[tr] * ncol + col] -= n;
 					pn[s.to[tr] * ncol + col] += n;
@@ -470,7 +493,7 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 				v = fmaf(w, cell >= 0 ? (float)s.tn[cell] : (float)pc[-1 - cell], v);
 			}
 			for (int i = 1; i < nc; i++) {
-				const int cell = __ldg(m.obs_cells_f + t1.z + i);
+				const int cell = __ldg((b.tn_full ? m.obs_cells_full : m.obs_cells_f) + t1.z + i);
 				v = fmaf(w, cell >= 0 ? (float)s.tn[cell] : (float)pc[-1 - cell], v);
 			}
 			if (t0.w < 0) {                  // the observation's last step: log-density
@@ -523,13 +546,14 @@ static int pick_threads(const ModelDev &m)
 	return ncol <= 128 ? 128 : ncol <= 256 ? 256 : 640;
 }
 
-size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_stage, bool state_global)
+size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_stage, bool state_global,
+                       int tnrows, bool pop_single)
 {
 	auto r = [](size_t x) { return (x + 15) & ~(size_t)15; };
 	const size_t A = m.A, G = m.G, DP = m.DP, NS = m.NS, C = m.C, T = m.T, DPS = m.DPS;
 	const size_t agsz = NS * A * G, ncol = A * DP;
-	return (m_in_smem ? r(4 * A * ms_lda(m.A)) : 0) + (state_global ? 0 : 2 * r(4 * C * ncol) + r(4 * T * ncol) + 3 * r(4 * agsz)) +
-	       r(4 * (size_t)nslots) + 2 * r(4 * T) + r(4 * DPS) + r(4 * C) + r(4 * T * DP) + r(4 * DP) + r(4 * 64) +
+	return (m_in_smem ? r(4 * A * ms_lda(m.A)) : 0) + (state_global ? 0 : (pop_single ? 1 : 2) * r(4 * C * ncol) + r(4 * (size_t)tnrows * ncol) + 3 * r(4 * agsz)) +
+	       r(4 * (size_t)nslots) + 3 * r(4 * T) + r(4 * DPS) + r(4 * C) + r(4 * T * DP) + r(4 * DP) + r(4 * 64) +
 	       r(4 * 32) + 2 * r(4 * NS * A) + r(4 * (size_t)nefoi_stage * G) + 2 * (2 * r(4 * NS * A) + r(4 * G * G)) +
 	       r(8) + r(4 * 2 * (size_t)pick_threads(m));
 }
@@ -540,7 +564,7 @@ size_t fast_gstate_stride(const ModelDev &m)
 {
 	auto r = [](size_t x) { return (x + 255) & ~(size_t)255; };
 	const size_t agsz = (size_t)m.NS * m.A * m.G, ncol = (size_t)m.A * m.DP;
-	return 2 * r(4 * m.C * ncol) + r(4 * m.T * ncol) + 3 * r(4 * agsz);
+	return 2 * r(4 * m.C * ncol) + r(4 * m.T * ncol) + 3 * r(4 * agsz);   // upper bound for any row/buffer choice
 }
 
 template <int NT>
@@ -556,8 +580,9 @@ static int launch_nt(const ModelDev &m, const BatchDev &b, size_t smem, cudaStre
 int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream)
 {
 	if (b.P == 0) return 0;
-	if (m.G > 16) return (int)cudaErrorInvalidValue;
-	const size_t smem = fast_smem_bytes(m, b.nslots, b.m_in_smem != 0, b.nefoi_stage, b.gstate != nullptr);
+	if (m.G > 16 || m.T > kMaxT) return (int)cudaErrorInvalidValue;
+	const size_t smem = fast_smem_bytes(m, b.nslots, b.m_in_smem != 0, b.nefoi_stage, b.gstate != nullptr,
+	                                    b.tn_full ? m.T : m.tn_rows, b.pop_single != 0);
 	const int nt = pick_threads(m);
 	const int NSA = m.NS * m.A;
 	if (NSA > nt || m.G * m.G > nt) return (int)cudaErrorInvalidValue;   // slices: one item per thread
