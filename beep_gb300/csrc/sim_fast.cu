@@ -168,53 +168,117 @@ __device__ float obs_lp_fast(float vf, int o, const ModelDev &m)
 	return (float)log(sum);
 }
 
-// Imap[st][t][a] = sum_c M[c][t] Icnt[st][c][a] (off-diagonal M).  Four
-// consecutive lanes share a target t and split the sources c = cg (mod 4); the
-// quad's partials are combined with two butterfly shuffles.  With the row
-// stride congruent to 8 mod 32 a warp's 4 rows x 8 targets hit 32 banks.
+// Imap[st][t][a] = sum_c M[c][t] Icnt[st][c][a] (off-diagonal M).  The
+// infectious counts are stored with the age stride MG (the age count rounded
+// up to a multiple of 4) so that a source's ages load as float4.
+//  * M in shared memory: four consecutive lanes share a target t and split the
+//    sources c = cg (mod 4); the row stride is congruent to 8 mod 32 so that a
+//    warp's 4 rows x 8 targets hit 32 banks.
+//  * M in global memory (L2): four lanes share a target pair (t, t+1), each pair
+//    of matrix entries loads as one float2, eight sources in flight per lane.
+// The quad's partial sums are combined with two butterfly shuffles.
 template <int NT, int MG>
 __device__ __forceinline__ void foi(const ModelDev &m, const float *Ms, int lda, const float *Icnt, float *Imap, int tid)
 {
-	const int A = m.A, G = m.G;
+	const int A = m.A;
 	const int cg = tid & 3;
 	for (int st = 0; st < m.NS; st++) {
-		const float *I = Icnt + st * A * G;
-		for (int t0 = 0; t0 < A; t0 += NT / 4) {
-			const int t = t0 + (tid >> 2);
-			float acc[MG];
+		const float *I = Icnt + st * A * MG;
+		float *Y = Imap + st * A * MG;
+		if (Ms) {
+			for (int t0 = 0; t0 < A; t0 += NT / 4) {
+				const int t = t0 + (tid >> 2);
+				float acc[MG];
 #pragma unroll
-			for (int a = 0; a < MG; a++) acc[a] = 0.f;
-			if (t < A) {
-				if (Ms) {
+				for (int a = 0; a < MG; a++) acc[a] = 0.f;
+				if (t < A) {
 #pragma unroll 2
 					for (int c = cg; c < A; c += 4) {
 						const float mv = Ms[c * lda + t];
-						const float *Ic = I + c * G;
+						const float4 *Ic = reinterpret_cast<const float4 *>(I + c * MG);
 #pragma unroll
-						for (int a = 0; a < MG; a++)
-							if (a < G) acc[a] = fmaf(mv, Ic[a], acc[a]);
-					}
-				} else {
-					for (int c = cg; c < A; c += 4) {
-						const float mv = __ldg(m.Mdense + (size_t)c * A + t);
-						const float *Ic = I + c * G;
-#pragma unroll
-						for (int a = 0; a < MG; a++)
-							if (a < G) acc[a] = fmaf(mv, Ic[a], acc[a]);
+						for (int q = 0; q < MG / 4; q++) {
+							const float4 v = Ic[q];
+							acc[4 * q] = fmaf(mv, v.x, acc[4 * q]);
+							acc[4 * q + 1] = fmaf(mv, v.y, acc[4 * q + 1]);
+							acc[4 * q + 2] = fmaf(mv, v.z, acc[4 * q + 2]);
+							acc[4 * q + 3] = fmaf(mv, v.w, acc[4 * q + 3]);
+						}
 					}
 				}
-			}
 #pragma unroll
-			for (int a = 0; a < MG; a++) {
-				if (a < G) {
+				for (int a = 0; a < MG; a++) {
 					acc[a] += __shfl_xor_sync(0xffffffffu, acc[a], 1);
 					acc[a] += __shfl_xor_sync(0xffffffffu, acc[a], 2);
 				}
-			}
-			if (t < A && cg == 0)
+				if (t < A && cg == 0) {
+					float4 *Yt = reinterpret_cast<float4 *>(Y + t * MG);
 #pragma unroll
-				for (int a = 0; a < MG; a++)
-					if (a < G) Imap[(st * A + t) * G + a] = acc[a];
+					for (int q = 0; q < MG / 4; q++) Yt[q] = make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
+				}
+			}
+		} else {
+			const int npair = (A + 1) / 2;
+			const bool even = (A & 1) == 0;
+			for (int p0 = 0; p0 < npair; p0 += NT / 4) {
+				const int tp = p0 + (tid >> 2);
+				const int t = 2 * tp;
+				float a0[MG], a1[MG];
+#pragma unroll
+				for (int a = 0; a < MG; a++) { a0[a] = 0.f; a1[a] = 0.f; }
+				if (tp < npair) {
+					const bool has1 = t + 1 < A;
+					for (int cb = cg; cb < A; cb += 32) {
+						float2 mv[8];
+#pragma unroll
+						for (int u = 0; u < 8; u++) {
+							const int c = cb + 4 * u;
+							mv[u] = make_float2(0.f, 0.f);
+							if (c < A) {
+								const float *row = m.Mdense + (size_t)c * A + t;
+								if (even) mv[u] = __ldg(reinterpret_cast<const float2 *>(row));
+								else mv[u] = make_float2(__ldg(row), has1 ? __ldg(row + 1) : 0.f);
+							}
+						}
+#pragma unroll
+						for (int u = 0; u < 8; u++) {
+							const int c = cb + 4 * u;
+							if (c < A) {
+								const float4 *Ic = reinterpret_cast<const float4 *>(I + c * MG);
+#pragma unroll
+								for (int q = 0; q < MG / 4; q++) {
+									const float4 v = Ic[q];
+									a0[4 * q] = fmaf(mv[u].x, v.x, a0[4 * q]);
+									a0[4 * q + 1] = fmaf(mv[u].x, v.y, a0[4 * q + 1]);
+									a0[4 * q + 2] = fmaf(mv[u].x, v.z, a0[4 * q + 2]);
+									a0[4 * q + 3] = fmaf(mv[u].x, v.w, a0[4 * q + 3]);
+									a1[4 * q] = fmaf(mv[u].y, v.x, a1[4 * q]);
+									a1[4 * q + 1] = fmaf(mv[u].y, v.y, a1[4 * q + 1]);
+									a1[4 * q + 2] = fmaf(mv[u].y, v.z, a1[4 * q + 2]);
+									a1[4 * q + 3] = fmaf(mv[u].y, v.w, a1[4 * q + 3]);
+								}
+							}
+						}
+					}
+				}
+#pragma unroll
+				for (int a = 0; a < MG; a++) {
+					a0[a] += __shfl_xor_sync(0xffffffffu, a0[a], 1);
+					a0[a] += __shfl_xor_sync(0xffffffffu, a0[a], 2);
+					a1[a] += __shfl_xor_sync(0xffffffffu, a1[a], 1);
+					a1[a] += __shfl_xor_sync(0xffffffffu, a1[a], 2);
+				}
+				if (tp < npair && cg == 0) {
+					float4 *Y0 = reinterpret_cast<float4 *>(Y + t * MG);
+#pragma unroll
+					for (int q = 0; q < MG / 4; q++) Y0[q] = make_float4(a0[4 * q], a0[4 * q + 1], a0[4 * q + 2], a0[4 * q + 3]);
+					if (t + 1 < A) {
+						float4 *Y1 = reinterpret_cast<float4 *>(Y + (t + 1) * MG);
+#pragma unroll
+						for (int q = 0; q < MG / 4; q++) Y1[q] = make_float4(a1[4 * q], a1[4 * q + 1], a1[4 * q + 2], a1[4 * q + 3]);
+					}
+				}
+			}
 		}
 	}
 }
@@ -265,7 +329,7 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 	if (p >= b.P) return;
 	const int tid = threadIdx.x;
 	const int A = m.A, G = m.G, DP = m.DP, NS = m.NS, DPS = m.DPS, C = m.C, T = m.T;
-	const int ncol = A * DP, popsz = C * ncol, tnsz = T * ncol, agsz = NS * A * G;
+	const int ncol = A * DP, popsz = C * ncol, tnsz = T * ncol, agsz = NS * A * MG;   // ages padded to MG
 	const int tnrows = b.tn_full ? T : m.tn_rows;        // stored transition rows
 	const int nsteps = b.tf - b.ti;
 	const int lda = ms_lda(A);
@@ -296,17 +360,16 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 			s.pop0 = (int32_t *)gtake(4 * (size_t)popsz);
 			s.pop1 = b.pop_single ? s.pop0 : (int32_t *)gtake(4 * (size_t)popsz);
 			s.tn = (int32_t *)gtake(4 * (size_t)tnrows * ncol);
-			s.Ic0 = (float *)gtake(4 * (size_t)agsz);
-			s.Ic1 = (float *)gtake(4 * (size_t)agsz);
-			s.Imap = (float *)gtake(4 * (size_t)agsz);
 		} else {
 			s.pop0 = (int32_t *)take(4 * (size_t)popsz);
 			s.pop1 = b.pop_single ? s.pop0 : (int32_t *)take(4 * (size_t)popsz);
 			s.tn = (int32_t *)take(4 * (size_t)tnrows * ncol);
-			s.Ic0 = (float *)take(4 * (size_t)agsz);
-			s.Ic1 = (float *)take(4 * (size_t)agsz);
-			s.Imap = (float *)take(4 * (size_t)agsz);
 		}
+		// the infectious counts and the force of infection stay on chip in both cases
+		// (the FOI reads each of them A times per step)
+		s.Ic0 = (float *)take(4 * (size_t)agsz);
+		s.Ic1 = (float *)take(4 * (size_t)agsz);
+		s.Imap = (float *)take(4 * (size_t)agsz);
 		s.slot = (float *)take(4 * (size_t)b.nslots);
 		s.from = (int32_t *)take(4 * (size_t)T);
 		s.trow = (int32_t *)take(4 * (size_t)T);
@@ -354,9 +417,9 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 	__syncthreads();
 	// infectious counts of the start populations (set_I_from_pop, src/state.cc:223-290)
 	for (int idx = tid; idx < agsz; idx += NT) {
-		const int a = idx % G, c = (idx / G) % A, st = idx / (G * A);
+		const int a = idx % MG, c = (idx / MG) % A, st = idx / (MG * A);
 		float v = 0.f;
-		for (int co = 0; co < C; co++) {
+		for (int co = 0; co < C && a < G; co++) {
 			const float inf = s.inf[co];
 			if (inf != 0.f)
 				for (int dp = 0; dp < DPS; dp++)
@@ -406,7 +469,7 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 				const float popu = (float)pc[inf_from * ncol + c * DP + dpl];
 				if (popu > 0.f) {
 					const float fac = m.M_factor_f[c], dg = m.M_diag_f[c];
-					const float *Ic = Ic_cur + (st * A + c) * G, *Im = s.Imap + (st * A + c) * G;
+					const float *Ic = Ic_cur + (st * A + c) * MG, *Im = s.Imap + (st * A + c) * MG;
 					const float *N = Nm + a * G;
 					float nmi = 0.f;
 #pragma unroll
@@ -462,8 +525,8 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 				const float inf = s.inf[co];
 				if (inf != 0.f) iv = fmaf(inf, (float)pn[co * ncol + col], iv);
 			}
-			if (m.dp_age_unique) Ic_nxt[(st * A + c) * G + a] = iv;
-			else atomicAdd(Ic_nxt + (st * A + c) * G + a, iv);
+			if (m.dp_age_unique) Ic_nxt[(st * A + c) * MG + a] = iv;
+			else atomicAdd(Ic_nxt + (st * A + c) * MG + a, iv);
 		}
 		if (sett + 1 < b.tf) slice_store<NT>(m, s, nxt, sb ^ 1, tid);
 		__syncthreads();
@@ -551,8 +614,8 @@ size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_
 {
 	auto r = [](size_t x) { return (x + 15) & ~(size_t)15; };
 	const size_t A = m.A, G = m.G, DP = m.DP, NS = m.NS, C = m.C, T = m.T, DPS = m.DPS;
-	const size_t agsz = NS * A * G, ncol = A * DP;
-	return (m_in_smem ? r(4 * A * ms_lda(m.A)) : 0) + (state_global ? 0 : (pop_single ? 1 : 2) * r(4 * C * ncol) + r(4 * (size_t)tnrows * ncol) + 3 * r(4 * agsz)) +
+	const size_t agsz = NS * A * (size_t)((m.G + 3) & ~3), ncol = A * DP;
+	return (m_in_smem ? r(4 * A * ms_lda(m.A)) : 0) + (state_global ? 0 : (pop_single ? 1 : 2) * r(4 * C * ncol) + r(4 * (size_t)tnrows * ncol)) + 3 * r(4 * agsz) +
 	       r(4 * (size_t)nslots) + 3 * r(4 * T) + r(4 * DPS) + r(4 * C) + r(4 * T * DP) + r(4 * DP) + r(4 * 64) +
 	       r(4 * 32) + 2 * r(4 * NS * A) + r(4 * (size_t)nefoi_stage * G) + 2 * (2 * r(4 * NS * A) + r(4 * G * G)) +
 	       r(8) + r(4 * 2 * (size_t)pick_threads(m));
@@ -563,14 +626,16 @@ int fast_threads() { return kFastThreads; }
 size_t fast_gstate_stride(const ModelDev &m)
 {
 	auto r = [](size_t x) { return (x + 255) & ~(size_t)255; };
-	const size_t agsz = (size_t)m.NS * m.A * m.G, ncol = (size_t)m.A * m.DP;
-	return 2 * r(4 * m.C * ncol) + r(4 * m.T * ncol) + 3 * r(4 * agsz);   // upper bound for any row/buffer choice
+	const size_t ncol = (size_t)m.A * m.DP;
+	return 2 * r(4 * m.C * ncol) + r(4 * m.T * ncol);   // upper bound for any row/buffer choice
 }
 
 template <int NT>
 static int launch_nt(const ModelDev &m, const BatchDev &b, size_t smem, cudaStream_t st)
 {
-	auto kern = m.G <= 4 ? sim_fast_kernel<NT, 4> : sim_fast_kernel<NT, 16>;
+	// MG: the age count rounded up to a multiple of 4 (the stride of the infectious counts)
+	auto kern = m.G <= 4 ? sim_fast_kernel<NT, 4> : m.G <= 8 ? sim_fast_kernel<NT, 8>
+	          : m.G <= 12 ? sim_fast_kernel<NT, 12> : sim_fast_kernel<NT, 16>;
 	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	if (e != cudaSuccess) return (int)e;
 	kern<<<b.P, NT, smem, st>>>(m, b);
