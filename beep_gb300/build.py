@@ -30,6 +30,7 @@ UNITS = {
     "noalloc.cu": [],
     "pf.cu": [],
     "abc_weights.cu": [],
+    "mbp.cu": [],
 }
 
 

@@ -68,6 +68,17 @@ class PFRequest(C.Structure):
     ]
 
 
+class MbpRequest(C.Structure):
+    _fields_ = [
+        ("groups", C.POINTER(ParamTables)), ("ngroup", C.c_int32), ("group_of", _i32p), ("seed", C.c_uint64),
+        ("stream_of", _u32p), ("inf_update", C.c_int32), ("simu", C.POINTER(C.c_uint8)), ("L_out", _f64p),
+    ]
+
+
+INF_UPDATE = 0
+INF_DIF_UPDATE = 1
+
+
 def _ptr(a: Optional[np.ndarray], ctype):
     if a is None:
         return C.cast(None, C.POINTER(ctype))
@@ -239,6 +250,18 @@ def lib():
         L.beep_abcsmc_weights.restype = C.c_int32
         L.beep_pf_loglik.argtypes = [C.c_void_p, C.POINTER(PFRequest)]
         L.beep_pf_loglik.restype = C.c_int32
+        L.beep_mbp_create.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]
+        L.beep_mbp_destroy.argtypes = [C.c_void_p]
+        for f in ("beep_mbp_initialise", "beep_mbp_propose"):
+            getattr(L, f).argtypes = [C.c_void_p, C.POINTER(MbpRequest)]
+        L.beep_mbp_accept.argtypes = [C.c_void_p, C.POINTER(C.c_uint8)]
+        L.beep_mbp_state_likelihood.argtypes = [C.c_void_p, C.POINTER(MbpRequest), _f64p]
+        L.beep_mbp_acceptance.argtypes = [C.c_int32] + [C.c_double] * 6
+        L.beep_mbp_acceptance.restype = C.c_double
+        L.beep_mbp_read_state.argtypes = [C.c_void_p, C.c_int32, _i32p, _f64p]
+        for f in ("beep_mbp_create", "beep_mbp_destroy", "beep_mbp_initialise", "beep_mbp_propose", "beep_mbp_accept",
+                  "beep_mbp_state_likelihood", "beep_mbp_read_state"):
+            getattr(L, f).restype = C.c_int32
         for f in ("beep_device_init", "beep_model_create", "beep_model_destroy", "beep_simulate", "beep_batch_create",
                   "beep_batch_stage", "beep_batch_upload", "beep_batch_launch", "beep_batch_download",
                   "beep_batch_time", "beep_batch_destroy"):
@@ -368,3 +391,81 @@ def abcsmc_weights(theta_new, logprior_new, theta_last, w_last, inv_cov, size: f
                                     tl.shape[0], _ptr(tl, C.c_double), _ptr(wl, C.c_double), _ptr(ic, C.c_double),
                                     size, 1 if normalise else 0, _ptr(out, C.c_double)))
     return out
+
+
+class MbpChains:
+    """A ``beep_mbp_chains`` set: nchain MBP chains with two trajectory states each."""
+
+    def __init__(self, dm: DeviceModel, nchain: int, form: int = FORM_PLAIN_FP64):
+        self.dm = dm
+        self.model = dm.model
+        self.nchain = nchain
+        h = C.c_void_p()
+        check(lib().beep_mbp_create(dm.h, nchain, form, C.byref(h)))
+        self.h = h
+
+    def _request(self, tables: Sequence[Tables], seed: int, group_of=None, stream_of=None,
+                 inf_update: int = INF_DIF_UPDATE, simu=None, want_L: bool = True):
+        keep = {}
+        r = MbpRequest()
+        keep["groups"] = (ParamTables * len(tables))(*[t.st for t in tables])
+        r.groups, r.ngroup = keep["groups"], len(tables)
+        keep["go"] = None if group_of is None else _i32(group_of)
+        r.group_of = _ptr(keep["go"], C.c_int32)
+        r.seed = seed
+        keep["so"] = None if stream_of is None else np.ascontiguousarray(np.asarray(stream_of, np.uint32))
+        r.stream_of = _ptr(keep["so"], C.c_uint32)
+        r.inf_update = inf_update
+        keep["simu"] = None if simu is None else np.ascontiguousarray(np.asarray(simu, np.uint8))
+        r.simu = _ptr(keep["simu"], C.c_uint8)
+        keep["L"] = np.zeros(self.nchain) if want_L else None
+        r.L_out = _ptr(keep["L"], C.c_double)
+        return r, keep
+
+    def initialise(self, tables: Sequence[Tables], seed: int, group_of=None, stream_of=None) -> np.ndarray:
+        """State::simulate of every chain; returns the log-likelihoods."""
+        r, keep = self._request(tables, seed, group_of, stream_of)
+        check(lib().beep_mbp_initialise(self.h, C.byref(r)))
+        return keep["L"]
+
+    def propose(self, tables: Sequence[Tables], seed: int, group_of=None, stream_of=None,
+                inf_update: int = INF_DIF_UPDATE, simu=None) -> np.ndarray:
+        """Mbp::mbp of every chain; returns the proposals' log-likelihoods."""
+        r, keep = self._request(tables, seed, group_of, stream_of, inf_update, simu)
+        check(lib().beep_mbp_propose(self.h, C.byref(r)))
+        return keep["L"]
+
+    def accept(self, accept) -> None:
+        a = np.ascontiguousarray(np.asarray(accept, np.uint8))
+        check(lib().beep_mbp_accept(self.h, _ptr(a, C.c_uint8)))
+
+    def state_likelihood(self, tables: Sequence[Tables], group_of=None) -> np.ndarray:
+        """State::likelihood of every chain's current state under the given tables."""
+        r, keep = self._request(tables, 0, group_of, want_L=False)
+        out = np.zeros(self.nchain)
+        check(lib().beep_mbp_state_likelihood(self.h, C.byref(r), _ptr(out, C.c_double)))
+        return out
+
+    def read_state(self, chain: int):
+        m = self.model
+        tn = np.zeros((m.ndivision, m.narea, m.ntrans, m.ndemocatpos), np.int32)
+        mean = np.zeros(tn.shape, np.float64)
+        check(lib().beep_mbp_read_state(self.h, chain, _ptr(tn, C.c_int32), _ptr(mean, C.c_double)))
+        return tn, mean
+
+    def close(self):
+        if self.h:
+            lib().beep_mbp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def mbp_acceptance(cutoff: bool, invT: float, EFcut: float, EF_prop: float, EF_init: float, Pr_prop: float,
+                   Pr_init: float) -> float:
+    """Mbp::get_al (beep_mbp_acceptance)."""
+    return lib().beep_mbp_acceptance(1 if cutoff else 0, invT, EFcut, EF_prop, EF_init, Pr_prop, Pr_init)

@@ -84,6 +84,17 @@ struct BatchDev {
 	int32_t *tn_traj;                   // [P][tf-ti][A][T][DP] or null
 	int32_t *pop_traj;                  // [P][tf-ti][A][C][DP] or null
 	int32_t *status;                    // [P] beep_status per particle
+	// MBP chains (plain form; mode 0 = plain simulation of the fields above)
+	int32_t mode;                       // 1: new chain state (Mbp::mbp; initialisation = every cell SIMU)
+	                                    // 2: State::likelihood of the current state under this batch's tables
+	int32_t inf_dif;                    // mode 1: Imap' = Imap + dImap (INF_DIF_UPDATE)
+	int32_t simu_all;                   // mode 1: every cell drawn afresh (State::simulate)
+	const uint8_t *simu;                // [P][S][A] 1 = SIMU cell, or null
+	const uint8_t *cur;                 // [P] slot (0/1) holding each chain's current state
+	int32_t *ch_tn;                     // [2][P][S][A][T][DP]
+	double *ch_mean;                    // [2][P][S][A][T][DP]
+	double *ch_Imap, *ch_Idiag;         // [2][P][S][NS][A][G]
+	double *Li;                         // [P] mode 2 output
 };
 
 // launchers

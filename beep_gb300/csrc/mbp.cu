@@ -1,0 +1,201 @@
+// MBP chains on the device: the reference's Mbp pair of states
+// (src/mbp.hh:58-59) for many chains at once.
+//
+// Each chain owns two trajectory slots in one HBM allocation,
+//   transnum  int32 [2][nchain][S][A][T][DP]
+//   transmean FP64  [2][nchain][S][A][T][DP]
+//   Imap, Idiag FP64 [2][nchain][S][NS][A][G]
+// and a host-side record of which slot is its current state (the device
+// reads a copy uploaded with every launch).  A proposal is written to the
+// other slot; accepting it flips the record (swap_initial_propose_state), so
+// no state is ever copied.  The kernels are the plain FP64 form's
+// (sim_plain.cu, modes 1 and 2), which reproduce the reference's counts
+// bit for bit under the keyed variate stream.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "capi_internal.h"
+
+using namespace beep;
+
+struct beep_mbp_chains {
+	beep_model *m = nullptr;
+	int32_t nchain = 0, form = 0;
+	DevBuf traj, aux;
+	std::vector<uint8_t> cur;            // current slot of each chain
+	int32_t *tn = nullptr;
+	double *mean = nullptr, *Imap = nullptr, *Idiag = nullptr;
+	bool initialised = false;
+	size_t tnsz = 0, agsz = 0;
+};
+
+namespace {
+
+// One launch of the chain kernel over every chain: mode 1 writes the
+// non-current slot (simu_all: State::simulate), mode 2 scores the current one.
+beep_status run_chains(beep_mbp_chains *c, const beep_mbp_request *r, int mode, bool simu_all, double *Li_out)
+{
+	beep_model *m = c->m;
+	if (!r || !r->groups || r->ngroup <= 0) return fail(BEEP_BAD_INPUT, "the request needs parameter tables");
+	if (r->inf_update != BEEP_INF_UPDATE && r->inf_update != BEEP_INF_DIF_UPDATE)
+		return fail(BEEP_BAD_INPUT, "unknown inf_update");
+	if (mode != 1 || !simu_all)
+		if (!c->initialised) return fail(BEEP_BAD_INPUT, "chains are not initialised");
+	std::lock_guard<std::mutex> lock(m->mu);
+	CUDA_TRY(cudaSetDevice(m->device));
+	const int P = c->nchain;
+	beep_sim_batch b{};
+	b.nparticle = P; b.ngroup = r->ngroup; b.groups = r->groups; b.group_of = r->group_of;
+	b.seed = r->seed; b.stream_of = r->stream_of; b.ti = 0; b.tf = m->S;
+	b.L_out = mode == 1 ? r->L_out : nullptr;
+	b.form = BEEP_FORM_PLAIN_FP64;
+	beep_batch *q = nullptr;
+	beep_status st = batch_create_internal(m, &b, false, &q);
+	if (st != BEEP_OK) return st;
+	auto done = [&](beep_status s) {
+		std::string e = s == BEEP_OK ? std::string() : std::string(beep_last_error());
+		beep_batch_destroy(q);
+		return s == BEEP_OK ? s : fail(s, e);
+	};
+	const bool mask = mode == 1 && !simu_all && r->simu;
+	Layout L;
+	const size_t o_cur = L.add((size_t)P), o_simu = L.add(mask ? (size_t)P * m->S * m->A : 0),
+	             o_li = L.add(8 * (size_t)P);
+	cudaError_t e = c->aux.reserve(L.size);
+	if (e != cudaSuccess) return done(fail(BEEP_OOM, std::string("chain buffers: ") + cudaGetErrorString(e)));
+	char *d = (char *)c->aux.ptr;
+	e = cudaMemcpyAsync(d + o_cur, c->cur.data(), (size_t)P, cudaMemcpyHostToDevice, m->stream);
+	if (e == cudaSuccess && mask)
+		e = cudaMemcpyAsync(d + o_simu, r->simu, (size_t)P * m->S * m->A, cudaMemcpyHostToDevice, m->stream);
+	if (e != cudaSuccess) return done(fail(BEEP_DEVICE_ERROR, cudaGetErrorString(e)));
+	BatchDev &bd = q->bd;
+	bd.mode = mode;
+	bd.inf_dif = r->inf_update == BEEP_INF_DIF_UPDATE ? 1 : 0;
+	bd.simu_all = simu_all ? 1 : 0;
+	bd.simu = mask ? (const uint8_t *)(d + o_simu) : nullptr;
+	bd.cur = (const uint8_t *)(d + o_cur);
+	bd.ch_tn = c->tn; bd.ch_mean = c->mean; bd.ch_Imap = c->Imap; bd.ch_Idiag = c->Idiag;
+	bd.Li = (double *)(d + o_li);
+	st = beep_batch_upload(q);
+	if (st == BEEP_OK) st = beep_batch_launch(q);
+	if (st == BEEP_OK) st = beep_batch_download(q);   // waits; checks every chain's status
+	if (st == BEEP_OK && mode == 2) {
+		e = cudaMemcpy(Li_out, bd.Li, 8 * (size_t)P, cudaMemcpyDeviceToHost);
+		if (e != cudaSuccess) st = fail(BEEP_DEVICE_ERROR, cudaGetErrorString(e));
+	}
+	return done(st);
+}
+
+}  // namespace
+
+extern "C" {
+
+BEEP_API beep_status beep_mbp_create(beep_model *m, int32_t nchain, int32_t form, beep_mbp_chains **out)
+{
+	if (!m || !out || nchain <= 0) return fail(BEEP_BAD_INPUT, "model, nchain > 0 and out are required");
+	*out = nullptr;
+	if (form != BEEP_FORM_PLAIN_FP64) return fail(BEEP_BAD_INPUT, "MBP chains exist in the plain FP64 form only");
+	std::lock_guard<std::mutex> lock(m->mu);
+	CUDA_TRY(cudaSetDevice(m->device));
+	beep_mbp_chains *c = new beep_mbp_chains();
+	c->m = m;
+	c->nchain = nchain;
+	c->form = form;
+	c->tnsz = (size_t)m->A * m->T * m->DP;
+	c->agsz = (size_t)m->NS * m->A * m->G;
+	const size_t slots = 2 * (size_t)nchain * m->S;
+	Layout L;
+	const size_t o_tn = L.add(4 * slots * c->tnsz), o_mean = L.add(8 * slots * c->tnsz),
+	             o_im = L.add(8 * slots * c->agsz), o_id = L.add(8 * slots * c->agsz);
+	cudaError_t e = c->traj.reserve(L.size);
+	if (e != cudaSuccess) {
+		delete c;
+		return fail(BEEP_OOM, "chain states (" + std::to_string(L.size >> 20) + " MiB): " + cudaGetErrorString(e));
+	}
+	char *d = (char *)c->traj.ptr;
+	c->tn = (int32_t *)(d + o_tn);
+	c->mean = (double *)(d + o_mean);
+	c->Imap = (double *)(d + o_im);
+	c->Idiag = (double *)(d + o_id);
+	c->cur.assign(nchain, 0);
+	*out = c;
+	return BEEP_OK;
+}
+
+BEEP_API beep_status beep_mbp_destroy(beep_mbp_chains *c)
+{
+	if (!c) return BEEP_OK;
+	if (c->m) {
+		cudaSetDevice(c->m->device);
+		cudaStreamSynchronize(c->m->stream);
+	}
+	c->traj.release();
+	c->aux.release();
+	delete c;
+	return BEEP_OK;
+}
+
+BEEP_API beep_status beep_mbp_initialise(beep_mbp_chains *c, const beep_mbp_request *r)
+{
+	if (!c) return fail(BEEP_BAD_INPUT, "null chains");
+	beep_status st = run_chains(c, r, 1, true, nullptr);
+	if (st != BEEP_OK) return st;
+	for (auto &x : c->cur) x ^= 1;
+	c->initialised = true;
+	return BEEP_OK;
+}
+
+BEEP_API beep_status beep_mbp_propose(beep_mbp_chains *c, const beep_mbp_request *r)
+{
+	if (!c) return fail(BEEP_BAD_INPUT, "null chains");
+	return run_chains(c, r, 1, false, nullptr);
+}
+
+BEEP_API beep_status beep_mbp_accept(beep_mbp_chains *c, const uint8_t *accept)
+{
+	if (!c || !accept) return fail(BEEP_BAD_INPUT, "null argument");
+	if (!c->initialised) return fail(BEEP_BAD_INPUT, "chains are not initialised");
+	for (int k = 0; k < c->nchain; k++)
+		if (accept[k]) c->cur[k] ^= 1;
+	return BEEP_OK;
+}
+
+BEEP_API beep_status beep_mbp_state_likelihood(beep_mbp_chains *c, const beep_mbp_request *r, double *Li_out)
+{
+	if (!c || !Li_out) return fail(BEEP_BAD_INPUT, "null argument");
+	return run_chains(c, r, 2, false, Li_out);
+}
+
+BEEP_API double beep_mbp_acceptance(int32_t cutoff_mode, double invT, double EFcut, double EF_prop, double EF_init,
+                                    double Pr_prop, double Pr_init)
+{
+	double al = 0.0;
+	if (cutoff_mode) {
+		if (EF_prop < EFcut) al = exp(Pr_prop - Pr_init);
+	} else {
+		al = exp(-invT * 0.5 * (EF_prop - EF_init) + Pr_prop - Pr_init);
+	}
+	if (al > 1) al = 1;
+	return al;
+}
+
+BEEP_API beep_status beep_mbp_read_state(beep_mbp_chains *c, int32_t chain, int32_t *transnum_out,
+                                         double *transmean_out)
+{
+	if (!c || chain < 0 || chain >= c->nchain) return fail(BEEP_BAD_INPUT, "chain out of range");
+	if (!c->initialised) return fail(BEEP_BAD_INPUT, "chains are not initialised");
+	std::lock_guard<std::mutex> lock(c->m->mu);
+	CUDA_TRY(cudaSetDevice(c->m->device));
+	CUDA_TRY(cudaStreamSynchronize(c->m->stream));
+	const size_t S = c->m->S;
+	const size_t off = ((size_t)c->cur[chain] * c->nchain + chain) * S * c->tnsz;
+	if (transnum_out) CUDA_TRY(cudaMemcpy(transnum_out, c->tn + off, 4 * S * c->tnsz, cudaMemcpyDeviceToHost));
+	if (transmean_out) CUDA_TRY(cudaMemcpy(transmean_out, c->mean + off, 8 * S * c->tnsz, cudaMemcpyDeviceToHost));
+	return BEEP_OK;
+}
+
+}  // extern "C"

@@ -8,6 +8,12 @@
 //                      Philox({col, sett, s, (0<<24) | tr/4});
 //           mean >= 10 PTRS (Hoermann 1993), iteration it takes (U, V) from
 //                      words 0,1 of Philox({col, sett, s, (1<<24)|(tr<<16)|it}).
+// Binomial: thinning of a count n with probability p, q = min(p, 1-p):
+//           n q < 10   sequential inversion, u from word tr%4 of
+//                      Philox({col, sett, s, (2<<24) | tr/4});
+//           n q >= 10  BTRS (Hoermann 1993), iteration it takes (U, V) from
+//                      words 0,1 of Philox({col, sett, s, (4<<24)|(tr<<16)|it});
+//           for q = 1-p the draw is n minus the draw for q.
 // exp/log:  Cody-Waite reduction by ln 2 with a degree-14 Taylor series for
 //           e^r; log(m) = 2 atanh((m-1)/(m+1)) series; log k! exact below 23,
 //           Stirling series above.  Only IEEE +,-,*,/,sqrt are used, and this
@@ -24,6 +30,7 @@ constexpr uint32_t PURPOSE_INV = 0u;
 constexpr uint32_t PURPOSE_PTRS = 1u;
 constexpr uint32_t PURPOSE_THIN = 2u;
 constexpr uint32_t PURPOSE_RESAMPLE = 3u;
+constexpr uint32_t PURPOSE_BTRS = 4u;
 
 struct U4 { uint32_t x, y, z, w; };
 
@@ -164,6 +171,58 @@ static __device__ __noinline__ int32_t poisson_fp64(double mean, uint32_t k0, ui
 		if (lhs <= rhs) return (int32_t)k;
 	}
 	return -1;
+}
+
+// Binomial(n, p) thinning of transition tr in column col at step sett (the
+// coupled proposal's count when the proposed mean is below the current one);
+// -1 after 65536 rejections.
+static __device__ __noinline__ int32_t binomial_fp64(double p, int32_t n, uint32_t k0, uint32_t k1, uint32_t col,
+                                               uint32_t tr, uint32_t sett, uint32_t stream)
+{
+	if (n <= 0 || !(p > 0.0)) return 0;
+	if (p >= 1.0) return n;
+	const bool flip = p > 0.5;
+	const double q = flip ? 1.0 - p : p;
+	const double nd = (double)n;
+	int32_t k;
+	if (nd * q < 10.0) {
+		const U4 r = philox10(U4{col, sett, stream, (PURPOSE_THIN << 24) | (tr >> 2)}, k0, k1);
+		const double u = u01_d(word_of(r, tr & 3u));
+		const double ratio = q / (1.0 - q);
+		double f = exp_p(nd * log_p(1.0 - q));
+		double F = f;
+		k = 0;
+		while (u > F && k < n) {
+			f = f * ratio * (double)(n - k) / (double)(k + 1);
+			k++;
+			F = F + f;
+		}
+	} else {
+		const double spq = sqrt(nd * q * (1.0 - q));
+		const double b = 1.15 + 2.53 * spq;
+		const double a = -0.0873 + 0.0248 * b + 0.01 * q;
+		const double c = nd * q + 0.5;
+		const double alpha = (2.83 + 5.1 / b) * spq;
+		const double vr = 0.92 - 4.2 / b;
+		const double m = floor((nd + 1.0) * q);
+		const double lpq = log_p(q / (1.0 - q));
+		const double h = log_factorial_p(m) + log_factorial_p(nd - m);
+		k = -1;
+		for (uint32_t it = 0; it < 65536u; it++) {
+			const U4 r = philox10(U4{col, sett, stream, (PURPOSE_BTRS << 24) | (tr << 16) | it}, k0, k1);
+			const double U = u01_d(r.x) - 0.5;
+			const double V = u01_d(r.y);
+			const double us = 0.5 - fabs(U);
+			const double kd = floor((2.0 * a / us + b) * U + c);
+			if (kd < 0.0 || kd > nd) continue;
+			if (us >= 0.07 && V <= vr) { k = (int32_t)kd; break; }
+			const double lhs = log_p(V * alpha / (a / (us * us) + b));
+			const double rhs = h - log_factorial_p(kd) - log_factorial_p(nd - kd) + (kd - m) * lpq;
+			if (lhs <= rhs) { k = (int32_t)kd; break; }
+		}
+		if (k < 0) return -1;
+	}
+	return flip ? n - k : k;
 }
 
 }  // namespace beep

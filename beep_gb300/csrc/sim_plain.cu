@@ -14,6 +14,18 @@
 // The log-likelihood of the scored observations is reduced at the end with
 // compensated (Neumaier) sums; the reference sums naively in index order
 // (src/obsmodel.cc:28), so the two agree to rounding (1e-12 relative).
+//
+// The same kernel advances MBP chains (src/mbp.cc:252-330), whose two states
+// per chain (Mbp::initial, Mbp::propose) are full trajectories in HBM:
+//   mode 1  a new state in the slot that is not current: every cell coupled
+//           to the current state (n' = n + Poisson(m'-m), n, or
+//           Binomial(n, m'/m)) unless it is a SIMU cell; Imap' either
+//           recomputed (INF_UPDATE) or Imap + dImap with dImap built from
+//           the count differences (INF_DIF_UPDATE, src/state.cc:109-123).
+//           Initialisation (State::simulate) is this mode with every cell SIMU.
+//   mode 2  State::likelihood (src/state.cc:812-826) of the current state
+//           with the means recomputed under this batch's tables on the fixed
+//           state (Mbp::parameter_proposal, src/mbp.cc:460-478).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -90,6 +102,13 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 	const double *efoi_age = fp + dir.efoi_agedist, *obs_spline = fp + dir.obs_spline;
 	const int32_t *beta_row_of = ip + dir.beta_row_of, *efoi_ref = ip + dir.efoi_ref;
 
+	// MBP chains: slot of the current state and of the state being written
+	const int mode = b.mode;
+	const int cs_i = mode ? b.cur[p] : 0, cs_p = 1 - cs_i;
+	const bool dif = mode == 1 && b.inf_dif && !b.simu_all;
+	auto chs = [&](int slot, int s) { return ((size_t)slot * b.P + p) * m.S + s; };
+	double Lsum = 0.0, Lcmp = 0.0;   // mode 2: compensated partial sum of this thread
+
 	int32_t *pop_cur = b.pop_a + (size_t)p * popsz;
 	int32_t *pop_nxt = b.pop_b + (size_t)p * popsz;
 	double *Imap = b.Imap + (size_t)p * agsz, *Idiag = b.Idiag + (size_t)p * agsz;
@@ -105,11 +124,15 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 	const int itr = m.infection_trans;
 	const int inf_from = m.trans_from[itr];
 	for (int sett = b.ti; sett < b.tf; sett++) {
-		int32_t *tn = b.tn_traj ? b.tn_traj + ((size_t)p * nsteps + (sett - b.ti)) * tnsz : b.tn + (size_t)p * tnsz;
-		const int32_t *tn_prev = b.tn_traj ? tn - tnsz : tn;   // single buffer still holds the previous step
+		int32_t *tn = mode ? b.ch_tn + chs(mode == 1 ? cs_p : cs_i, sett) * tnsz
+		          : b.tn_traj ? b.tn_traj + ((size_t)p * nsteps + (sett - b.ti)) * tnsz : b.tn + (size_t)p * tnsz;
+		const int32_t *tn_prev = b.tn_traj || mode ? tn - tnsz : tn;   // single buffer still holds the previous step
+		const int32_t *tn_base = dif && sett > 0 ? b.ch_tn + chs(cs_i, sett - 1) * tnsz : nullptr;
+		double *Im_s = mode ? b.ch_Imap + chs(mode == 1 ? cs_p : cs_i, sett) * agsz : Imap;
+		double *Id_s = mode ? b.ch_Idiag + chs(mode == 1 ? cs_p : cs_i, sett) * agsz : Idiag;
 
 		// ---- A: dinf per (strain, source area, age)
-		for (int idx = tid; idx < (int)agsz; idx += nth) {
+		for (int idx = tid; idx < (int)agsz && mode != 2 && !(dif && sett == 0); idx += nth) {
 			const int a = idx % G, c = (idx / G) % A, st = idx / (G * A);
 			double s = 0.0;
 			if (sett == b.ti) {
@@ -129,7 +152,8 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 					if (di != 0) {
 						for (int dp = 0; dp < DPS; dp++) {
 							if (m.dp_age[dp] != a) continue;
-							const double num = (double)tn_prev[((size_t)c * T + tr) * DP + st * DPS + dp];
+							const size_t cl = ((size_t)c * T + tr) * DP + st * DPS + dp;
+							const double num = tn_base ? (double)(tn_prev[cl] - tn_base[cl]) : (double)tn_prev[cl];
 							if (num != 0) s += di * num;
 						}
 					}
@@ -140,26 +164,40 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 		__syncthreads();
 
 		// ---- B: Imap/Idiag per (strain, target area, age), sources in ascending order
-		for (int idx = tid; idx < (int)agsz; idx += nth) {
+		// (INF_DIF_UPDATE: the running sums are dImap/dIdiag and the state's maps
+		// are the current state's plus them)
+		for (int idx = tid; idx < (int)agsz && mode != 2; idx += nth) {
 			const int a = idx % G, t = (idx / G) % A, st = idx / (G * A);
 			const double *dst = dinf + (size_t)st * A * G;
 			double im = sett == b.ti ? 0.0 : Imap[idx];
 			double id = sett == b.ti ? 0.0 : Idiag[idx];
-			const double dself = dst[t * G + a];
-			if (dself != 0) id += dself * m.M_diag[t];
-			for (int j = m.csc_ptr[t]; j < m.csc_ptr[t + 1]; j++) {
-				const double d = dst[m.csc_src[j] * G + a];
-				if (d != 0) im += d * m.csc_val[j];
+			if (!(dif && sett == 0)) {
+				const double dself = dst[t * G + a];
+				if (dself != 0) id += dself * m.M_diag[t];
+				for (int j = m.csc_ptr[t]; j < m.csc_ptr[t + 1]; j++) {
+					const double d = dst[m.csc_src[j] * G + a];
+					if (d != 0) im += d * m.csc_val[j];
+				}
 			}
 			Imap[idx] = im;
 			Idiag[idx] = id;
+			if (mode == 1) {
+				if (dif) {
+					const size_t io = chs(cs_i, sett) * agsz + idx;
+					Im_s[idx] = b.ch_Imap[io] + im;
+					Id_s[idx] = b.ch_Idiag[io] + id;
+				} else {
+					Im_s[idx] = im;
+					Id_s[idx] = id;
+				}
+			}
 		}
 		__syncthreads();
 
 		// ---- C: NMI per (strain, area, age); strain shift of the susceptible population
 		for (int idx = tid; idx < (int)agsz; idx += nth) {
 			const int a = idx % G, c = (idx / G) % A, st = idx / (G * A);
-			const double *Id = Idiag + (size_t)st * A * G, *Im = Imap + (size_t)st * A * G;
+			const double *Id = Id_s + (size_t)st * A * G, *Im = Im_s + (size_t)st * A * G;
 			const double d = geo[sett];
 			const double omd = 1 - d;
 			const double fac = m.M_factor[c];
@@ -215,21 +253,42 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 				const double popu = (double)pop_cur[((size_t)c * C + m.trans_from[tr]) * DP + dp];
 				mean = popu <= 0 ? 0 : m.dt * popu * transrate[(size_t)tr * DP + dp];
 			}
+			if (mode == 2) {                    // State::likelihood term of the fixed count
+				if (mean != mean) set_status(status, BEEP_NAN_RATE);
+				const double lp = poisson_lp(tn[cell], mean);
+				const double t = Lsum + lp;
+				Lcmp += fabs(Lsum) >= fabs(lp) ? (Lsum - t) + lp : (lp - t) + Lsum;
+				Lsum = t;
+				continue;
+			}
 			int32_t n = 0;
 			if (mean != mean) set_status(status, BEEP_NAN_RATE);
 			else if (mean != 0) {
 				if (mean > 1000000000.0) set_status(status, BEEP_COUNT_OVERFLOW);
 				else {
-					n = poisson_fp64(mean, b.k0, b.k1, (uint32_t)(c * DP + dp), (uint32_t)tr, (uint32_t)sett, stream);
+					const uint32_t col = (uint32_t)(c * DP + dp);
+					if (mode == 0 || b.simu_all || (b.simu && b.simu[((size_t)p * m.S + sett) * A + c])) {
+						n = poisson_fp64(mean, b.k0, b.k1, col, (uint32_t)tr, (uint32_t)sett, stream);
+					} else {                        // coupled to the current state (src/mbp.cc:293-305)
+						const size_t ci = chs(cs_i, sett) * tnsz + cell;
+						const int32_t ni = b.ch_tn[ci];
+						const double ri = b.ch_mean[ci];
+						if (mean > ri) {
+							n = poisson_fp64(mean - ri, b.k0, b.k1, col, (uint32_t)tr, (uint32_t)sett, stream);
+							if (n >= 0) n += ni;
+						} else if (mean == ri) n = ni;
+						else n = binomial_fp64(mean / ri, ni, b.k0, b.k1, col, (uint32_t)tr, (uint32_t)sett, stream);
+					}
 					if (n < 0) { set_status(status, BEEP_TIMEOUT); n = 0; }
 				}
 			}
+			if (mode == 1) b.ch_mean[chs(cs_p, sett) * tnsz + cell] = mean;
 			tn[cell] = n;
 		}
 		__syncthreads();
 
 		// ---- E: observation sums (one thread per active observation, cells in reference order)
-		const int s0 = b.step_ptr[sett - b.ti], s1 = b.step_ptr[sett - b.ti + 1];
+		const int s0 = b.step_ptr[sett - b.ti], s1 = mode == 2 ? s0 : b.step_ptr[sett - b.ti + 1];
 		for (int k = s0 + tid; k < s1; k += nth) {
 			const int pos = b.step_obs[k];
 			const int o = b.scored[pos];
@@ -270,10 +329,26 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 	if (b.pop_out)
 		for (size_t k = tid; k < popsz; k += nth) b.pop_out[(size_t)p * popsz + k] = pop_cur[k];
 
-	if (b.L) {
+	__shared__ double part_s[kThreads], part_c[kThreads];
+	if (mode == 2) {
+		// the threads' compensated partial sums, combined in thread order
+		part_s[tid] = Lsum;
+		part_c[tid] = Lcmp;
+		__syncthreads();
+		if (tid == 0) {
+			double S = 0.0, Cc = 0.0;
+			for (int k = 0; k < nth; k++) {
+				const double x = part_s[k];
+				const double t = S + x;
+				Cc += fabs(S) >= fabs(x) ? (S - t) + x : (x - t) + S;
+				S = t;
+				Cc += part_c[k];
+			}
+			b.Li[p] = S + Cc;
+		}
+	} else if (b.L) {
 		// each thread sums a contiguous run of scored observations (Neumaier), then the
 		// partials are combined in thread order by thread 0
-		__shared__ double part_s[kThreads], part_c[kThreads];
 		const int per = (b.nscored + nth - 1) / nth;
 		const int k0 = tid * per, k1 = min(b.nscored, k0 + per);
 		double s = 0.0, cmp = 0.0;

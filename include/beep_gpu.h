@@ -241,6 +241,60 @@ BEEP_API beep_status beep_abcsmc_weights(int32_t nvar, int32_t nnew, const doubl
                                          const double *w_last, const double *inv_cov, double size,
                                          int32_t normalise, double *w_out);
 
+/* ---- MBP chains: model-based proposals (Mbp, src/mbp.cc) -----------------
+ * A chain set keeps, for each chain, two full trajectory states on the
+ * device -- the reference's Mbp::initial and Mbp::propose (transnum,
+ * transmean, Imap, Idiag over all ndivision steps, src/state.hh:21-28) -- and
+ * which of the two is the chain's current state.  Only BEEP_FORM_PLAIN_FP64
+ * chains exist so far (bit-exact with the reference's counts). */
+typedef struct beep_mbp_chains beep_mbp_chains;
+
+typedef enum beep_inf_update {
+	BEEP_INF_UPDATE = 0,       /* Imap recomputed from the new state's counts (State::set_Imap_sett) */
+	BEEP_INF_DIF_UPDATE = 1    /* Imap' = Imap + dImap from the count differences (set_Imap_using_dI) */
+} beep_inf_update;
+
+typedef struct beep_mbp_request {
+	const beep_param_tables *groups;   /* parameter sets (State::set_param tables) */
+	int32_t ngroup;
+	const int32_t *group_of;           /* [nchain] parameter set of each chain, or NULL (all set 0) */
+	uint64_t seed;
+	const uint32_t *stream_of;         /* [nchain] variate stream of each chain's draws, or NULL (chain index) */
+	int32_t inf_update;                /* beep_inf_update (beep_mbp_propose) */
+	const uint8_t *simu;               /* [nchain][ndivision][narea] 1 = simulate the cell afresh (SIMU,
+	                                      Mbp::mbp_slicetime / mbp_fixedtree), or NULL: all coupled */
+	double *L_out;                     /* [nchain] log-likelihood of the new state (EF = -2 L), or NULL */
+} beep_mbp_request;
+
+BEEP_API beep_status beep_mbp_create(beep_model *model, int32_t nchain, int32_t form, beep_mbp_chains **out);
+BEEP_API beep_status beep_mbp_destroy(beep_mbp_chains *chains);
+/* State::simulate(theta) (src/state.cc:582-592) of every chain over
+ * [0, ndivision); the result becomes the chain's current state. */
+BEEP_API beep_status beep_mbp_initialise(beep_mbp_chains *chains, const beep_mbp_request *request);
+/* Mbp::mbp (src/mbp.cc:252-330): every chain's proposed state from its
+ * current state, under the request's tables: a coupled cell draws
+ * n' = n + Poisson(m'-m) (m' > m), n (m' = m) or Binomial(n, m'/m) (m' < m)
+ * from the keyed stream of the chain; a SIMU cell draws Poisson(m'). */
+BEEP_API beep_status beep_mbp_propose(beep_mbp_chains *chains, const beep_mbp_request *request);
+/* Mbp::swap_initial_propose_state (src/mbp.cc:241-246) for every chain with
+ * accept[k] != 0: its last proposal becomes its current state. */
+BEEP_API beep_status beep_mbp_accept(beep_mbp_chains *chains, const uint8_t *accept);
+/* State::likelihood (src/state.cc:812-826) of every chain's current state,
+ * with the transition means recomputed under the request's tables on the
+ * fixed state (Mbp::parameter_proposal, src/mbp.cc:460-478); with the chain's
+ * own tables this is the likelihood of its stored means.  Li_out [nchain]. */
+BEEP_API beep_status beep_mbp_state_likelihood(beep_mbp_chains *chains, const beep_mbp_request *request,
+                                               double *Li_out);
+/* Mbp::get_al (src/mbp.cc:334-361): with cutoff_mode != 0 (CUTOFF)
+ * al = EF_prop < EFcut ? exp(Pr_prop - Pr_init) : 0, else (INVT)
+ * al = exp(-invT/2 (EF_prop - EF_init) + Pr_prop - Pr_init); capped at 1. */
+BEEP_API double beep_mbp_acceptance(int32_t cutoff_mode, double invT, double EFcut, double EF_prop,
+                                    double EF_init, double Pr_prop, double Pr_init);
+/* The current state of one chain: transnum [ndivision][narea][ntrans][ndemocatpos]
+ * and/or transmean of the same shape (either may be NULL). */
+BEEP_API beep_status beep_mbp_read_state(beep_mbp_chains *chains, int32_t chain, int32_t *transnum_out,
+                                         double *transmean_out);
+
 /* Plain FP64 simulation that allocates no memory on the GPU.  No counterpart
  * in the reference: it serves callers that cannot call cudaMalloc -- an
  * application whose allocator or fixed memory budget owns all device memory,

@@ -24,6 +24,12 @@ int32_t beep_oracle_poisson(double mean, uint64_t seed, uint32_t col, uint32_t t
 	return beep_poisson_ref(mean, (uint32_t)seed, (uint32_t)(seed >> 32), col, tr, step, stream);
 }
 
+int32_t beep_oracle_binomial(double p, int32_t n, uint64_t seed, uint32_t col, uint32_t tr, uint32_t step,
+                             uint32_t stream)
+{
+	return beep_binomial_ref(p, n, (uint32_t)seed, (uint32_t)(seed >> 32), col, tr, step, stream);
+}
+
 /* ---- log-densities: src/utils.cc:107-170 ------------------------------- */
 
 static double normal_probability(double x, double mean, double var)
@@ -182,128 +188,233 @@ static void scatter_inf(const beep_model_desc *m, const double *dinf, int32_t c,
 	}
 }
 
+/* set_I_from_pop, src/state.cc:223-290: Imap/Idiag [NS][A*G] from pop */
+static void inf_from_pop(const beep_model_desc *m, const beep_param_tables *tb, const double *pop, work *w,
+                         double *Imap, double *Idiag)
+{
+	const int32_t A = m->narea, G = m->nage, C = m->ncomp, DP = m->ndemocatpos, NS = m->nstrain, DPS = DP / NS;
+	const size_t AG = (size_t)A * G;
+	memset(Imap, 0, sizeof(double) * AG * NS);
+	memset(Idiag, 0, sizeof(double) * AG * NS);
+	for (int32_t st = 0; st < NS; st++) {
+		for (int32_t c = 0; c < A; c++) {
+			for (int32_t a = 0; a < G; a++) w->dinf[a] = 0;
+			for (int32_t co = 0; co < C; co++) {
+				double inf = tb->infectivity[co];
+				if (inf != 0) {
+					int32_t dpp = st * DPS;
+					for (int32_t dp = 0; dp < DPS; dp++) {
+						double pv = pop[((size_t)c * C + co) * DP + dpp];
+						if (pv != 0) w->dinf[m->democatpos_age[dp]] += inf * pv;
+						dpp++;
+					}
+				}
+			}
+			scatter_inf(m, w->dinf, c, Imap + st * AG, Idiag + st * AG);
+		}
+	}
+}
+
+/* update_I_from_transnum, src/state.cc:178-219: adds the infectivity change
+ * of the counts tn (minus base, when given: the coupled proposal's
+ * dtransnum, src/mbp.cc:308-309,320) to Imap/Idiag */
+static void inf_update(const beep_model_desc *m, const int32_t *tn, const int32_t *base, work *w, double *Imap,
+                       double *Idiag)
+{
+	const int32_t A = m->narea, G = m->nage, T = m->ntrans, DP = m->ndemocatpos, NS = m->nstrain, DPS = DP / NS;
+	const size_t AG = (size_t)A * G;
+	for (int32_t st = 0; st < NS; st++) {
+		for (int32_t c = 0; c < A; c++) {
+			for (int32_t a = 0; a < G; a++) w->dinf[a] = 0;
+			for (int32_t tr = 0; tr < T; tr++) {
+				double di = w->infdif[tr];
+				if (di != 0) {
+					int32_t dpp = st * DPS;
+					for (int32_t dp = 0; dp < DPS; dp++) {
+						const size_t cell = ((size_t)c * T + tr) * DP + dpp;
+						double num = base ? (double)(tn[cell] - base[cell]) : (double)tn[cell];
+						if (num != 0) w->dinf[m->democatpos_age[dp]] += di * num;
+						dpp++;
+					}
+				}
+			}
+			scatter_inf(m, w->dinf, c, Imap + st * AG, Idiag + st * AG);
+		}
+	}
+}
+
+/* set_transmean for area c, src/state.cc:380-456 (with get_NMI,
+ * src/state.cc:547-578): w->tmean[T][DP] from pop (the susceptible
+ * population of other strains is moved to strain 0 in place) */
+static int transmean_area(const beep_model_desc *m, const beep_param_tables *tb, double *pop, const double *Imap,
+                          const double *Idiag, int32_t sett, int32_t c, work *w)
+{
+	const int32_t A = m->narea, G = m->nage, C = m->ncomp, T = m->ntrans, DP = m->ndemocatpos;
+	const int32_t NS = m->nstrain, DPS = DP / NS;
+	const size_t AG = (size_t)A * G;
+	double *pc = pop + (size_t)c * C * DP;
+	int32_t itr = m->infection_trans;
+	double *sus_pop = pc + (size_t)m->trans_from[itr] * DP;
+	if (NS > 1) {
+		for (int32_t dp = 0; dp < DPS; dp++) {
+			double sum = 0.0;
+			for (int32_t st = 1; st < NS; st++) {
+				int32_t dpp = DPS * st + dp;
+				sum += sus_pop[dpp]; sus_pop[dpp] = 0;
+			}
+			sus_pop[dp] += sum;
+		}
+	}
+	for (int32_t st = 0; st < NS; st++) {
+		const double *Id = Idiag + st * AG, *Im = Imap + st * AG;
+		double d = tb->geo_spline[sett];
+		double omd = 1 - d;
+		double fac = m->M_factor[c];
+		if (G == 1) {
+			double val = Id[c] * (d + fac * omd) + Im[c] * d;
+			if (val < 0) val = 0;
+			w->NMI[0] = val;
+		} else {
+			int32_t v = c * G;
+			for (int32_t a = 0; a < G; a++) w->I[a] = (Id[v + a] + Im[v + a]) * d + fac * Id[v + a] * omd;
+			const double *N = tb->Ntime + (size_t)sett * G * G;
+			for (int32_t a = 0; a < G; a++) {
+				double sum = 0.0;
+				for (int32_t aa = 0; aa < G; aa++) sum += N[a * G + aa] * w->I[aa];
+				if (sum < 0) sum = 0;
+				w->NMI[a] = sum;
+			}
+		}
+		double be = tb->beta_rows[(size_t)tb->beta_row_of[st * A + c] * m->ndivision + sett];
+		be *= tb->areafactor[(size_t)(sett / m->division_per_time) * A + c];
+		int32_t ei = tb->efoi_ref[st * A + c];
+		double et = tb->efoi_spline[(size_t)ei * m->ndivision + sett] / m->popsize;
+		for (int32_t a = 0; a < G; a++) w->eta[a] = et * tb->efoi_agedist[(size_t)ei * G + a];
+		int32_t dpp = st * DPS;
+		for (int32_t dp = 0; dp < DPS; dp++) {
+			double popu = sus_pop[dp];
+			if (popu <= 0) w->tmean[itr * DP + dpp] = 0;
+			else {
+				int32_t a = m->democatpos_age[dp];
+				double v = m->dt * popu * tb->susceptibility[dpp] * (be * w->NMI[a] + w->eta[a]);
+				if (v != v) return BEEP_NAN_RATE;
+				w->tmean[itr * DP + dpp] = v;
+			}
+			dpp++;
+		}
+	}
+	for (int32_t tr = 0; tr < T; tr++) {
+		if (tr == itr) continue;
+		int32_t from = m->trans_from[tr];
+		for (int32_t dp = 0; dp < DP; dp++) {
+			double popu = pc[(size_t)from * DP + dp];
+			if (popu <= 0) w->tmean[tr * DP + dp] = 0;
+			else w->tmean[tr * DP + dp] = m->dt * popu * tb->transrate[(size_t)tr * DP + dp];
+		}
+	}
+	return BEEP_OK;
+}
+
+/* update_pop, src/state.cc:460-485: popnext = pop + the flows of tn */
+static void update_pop(const beep_model_desc *m, const double *pop, const int32_t *tn, double *popnext)
+{
+	const int32_t A = m->narea, C = m->ncomp, T = m->ntrans, DP = m->ndemocatpos;
+	memcpy(popnext, pop, sizeof(double) * (size_t)A * C * DP);
+	for (int32_t c = 0; c < A; c++) {
+		double *pn = popnext + (size_t)c * C * DP;
+		for (int32_t tr = 0; tr < T; tr++) {
+			int32_t from = m->trans_from[tr], to = m->trans_to[tr];
+			for (int32_t dp = 0; dp < DP; dp++) {
+				double num = (double)tn[((size_t)c * T + tr) * DP + dp];
+				if (num != 0) { pn[(size_t)from * DP + dp] -= num; pn[(size_t)to * DP + dp] += num; }
+			}
+		}
+	}
+}
+
+/* get_obs_value_section + calculate, src/obsmodel.cc:22-109, over the
+ * trajectory in w (steps ti..tf-1) */
+static int loglik_traj(const beep_model_desc *m, const beep_param_tables *tb, const obs_index *ix, int32_t ti,
+                       int32_t tf, const int32_t *tn_traj, const double *pop_traj, work *w, double *Lout)
+{
+	const int32_t A = m->narea, C = m->ncomp, T = m->ntrans, DP = m->ndemocatpos;
+	const size_t popsz = (size_t)A * C * DP, tnsz = (size_t)A * T * DP;
+	for (int32_t k = 0; k < ix->nscored; k++) w->obs_value[ix->scored[k]] = 0;
+	for (int32_t sett = ti; sett < tf; sett++) {
+		const int32_t *tn = tn_traj + (size_t)(sett - ti) * tnsz;
+		const double *pp = pop_traj + (size_t)(sett - ti) * popsz;
+		for (int32_t c = 0; c < A; c++) {
+			for (int32_t tr = 0; tr < T; tr++) {
+				for (int32_t dp = 0; dp < DP; dp++) {
+					int32_t cell = (c * T + tr) * DP + dp;
+					double num = (double)tn[cell];
+					if (num != 0) {
+						size_t slot = (size_t)(sett - ti) * ix->ncell_t + cell;
+						for (int32_t q = ix->t_ptr[slot]; q < ix->t_ptr[slot + 1]; q++) {
+							int32_t ob = ix->t_obs[q];
+							int32_t spl = m->obs_factor_spline[ob];
+							if (spl < 0) w->obs_value[ob] += m->obs_factor[ob] * num;
+							else w->obs_value[ob] += m->obs_factor[ob] * num * tb->obs_spline[(size_t)spl * m->ndivision + sett];
+						}
+					}
+				}
+			}
+			for (int32_t co = 0; co < C; co++) {
+				for (int32_t dp = 0; dp < DP; dp++) {
+					int32_t cell = (c * C + co) * DP + dp;
+					size_t slot = (size_t)(sett - ti) * ix->ncell_p + cell;
+					if (ix->p_ptr[slot + 1] > ix->p_ptr[slot]) {
+						double num = pp[cell];
+						for (int32_t q = ix->p_ptr[slot]; q < ix->p_ptr[slot + 1]; q++) {
+							int32_t ob = ix->p_obs[q];
+							w->obs_value[ob] += m->obs_factor[ob] * num;
+						}
+					}
+				}
+			}
+		}
+	}
+	double L = 0.0;
+	for (int32_t k = 0; k < ix->nscored; k++) {
+		int32_t i = ix->scored[k];
+		L += beep_oracle_obs_prob(w->obs_value[i], m->obs_value_kind[i], m->obs_value[i], m->obs_model[i],
+		                          m->obs_sd[i], m->obs_shape[i], m->obs_threshold[i]);
+	}
+	if (L != L) return BEEP_NAN_RATE;
+	*Lout = L;
+	return BEEP_OK;
+}
+
+static void set_infdif(const beep_model_desc *m, const beep_param_tables *tb, work *w)
+{
+	for (int32_t tr = 0; tr < m->ntrans; tr++)
+		w->infdif[tr] = tb->infectivity[m->trans_to[tr]] - tb->infectivity[m->trans_from[tr]];
+}
+
 static int simulate_particle(const beep_model_desc *m, const beep_sim_batch *b, const obs_index *ix,
                              int32_t p, work *w)
 {
 	const int32_t A = m->narea, G = m->nage, C = m->ncomp, T = m->ntrans, DP = m->ndemocatpos;
-	const int32_t NS = m->nstrain, DPS = DP / NS;
+	const int32_t NS = m->nstrain;
 	const size_t popsz = (size_t)A * C * DP, tnsz = (size_t)A * T * DP, AG = (size_t)A * G;
 	const int32_t grp = b->group_of ? b->group_of[p] : 0;
 	const beep_param_tables *tb = &b->groups[grp];
 	const uint32_t stream = b->stream_of ? b->stream_of[p] : (uint32_t)p;
 	const uint32_t k0 = (uint32_t)b->seed, k1 = (uint32_t)(b->seed >> 32);
+	(void)AG; (void)NS;
 
-	for (int32_t tr = 0; tr < T; tr++)
-		w->infdif[tr] = tb->infectivity[m->trans_to[tr]] - tb->infectivity[m->trans_from[tr]];
-
+	set_infdif(m, tb, w);
 	if (b->ti == 0) memcpy(w->pop, m->pop_init, sizeof(double) * popsz);
 	else for (size_t k = 0; k < popsz; k++) w->pop[k] = (double)b->pop_in[(size_t)p * popsz + k];
 
 	for (int32_t sett = b->ti; sett < b->tf; sett++) {
 		int32_t *tn = w->tn_traj + (size_t)(sett - b->ti) * tnsz;
-		if (sett == b->ti) {                               /* set_I_from_pop, src/state.cc:223-290 */
-			memset(w->Imap, 0, sizeof(double) * AG * NS);
-			memset(w->Idiag, 0, sizeof(double) * AG * NS);
-			for (int32_t st = 0; st < NS; st++) {
-				for (int32_t c = 0; c < A; c++) {
-					for (int32_t a = 0; a < G; a++) w->dinf[a] = 0;
-					for (int32_t co = 0; co < C; co++) {
-						double inf = tb->infectivity[co];
-						if (inf != 0) {
-							int32_t dpp = st * DPS;
-							for (int32_t dp = 0; dp < DPS; dp++) {
-								double pv = w->pop[((size_t)c * C + co) * DP + dpp];
-								if (pv != 0) w->dinf[m->democatpos_age[dp]] += inf * pv;
-								dpp++;
-							}
-						}
-					}
-					scatter_inf(m, w->dinf, c, w->Imap + st * AG, w->Idiag + st * AG);
-				}
-			}
-		} else {                                           /* update_I_from_transnum, src/state.cc:178-219 */
-			const int32_t *tprev = tn - tnsz;
-			for (int32_t st = 0; st < NS; st++) {
-				for (int32_t c = 0; c < A; c++) {
-					for (int32_t a = 0; a < G; a++) w->dinf[a] = 0;
-					for (int32_t tr = 0; tr < T; tr++) {
-						double di = w->infdif[tr];
-						if (di != 0) {
-							int32_t dpp = st * DPS;
-							for (int32_t dp = 0; dp < DPS; dp++) {
-								double num = (double)tprev[((size_t)c * T + tr) * DP + dpp];
-								if (num != 0) w->dinf[m->democatpos_age[dp]] += di * num;
-								dpp++;
-							}
-						}
-					}
-					scatter_inf(m, w->dinf, c, w->Imap + st * AG, w->Idiag + st * AG);
-				}
-			}
-		}
+		if (sett == b->ti) inf_from_pop(m, tb, w->pop, w, w->Imap, w->Idiag);
+		else inf_update(m, tn - tnsz, NULL, w, w->Imap, w->Idiag);
 
-		for (int32_t c = 0; c < A; c++) {                 /* set_transmean, src/state.cc:380-456 */
-			double *pc = w->pop + (size_t)c * C * DP;
-			int32_t itr = m->infection_trans;
-			double *sus_pop = pc + (size_t)m->trans_from[itr] * DP;
-			if (NS > 1) {
-				for (int32_t dp = 0; dp < DPS; dp++) {
-					double sum = 0.0;
-					for (int32_t st = 1; st < NS; st++) {
-						int32_t dpp = DPS * st + dp;
-						sum += sus_pop[dpp]; sus_pop[dpp] = 0;
-					}
-					sus_pop[dp] += sum;
-				}
-			}
-			for (int32_t st = 0; st < NS; st++) {
-				/* get_NMI, src/state.cc:547-578 */
-				const double *Id = w->Idiag + st * AG, *Im = w->Imap + st * AG;
-				double d = tb->geo_spline[sett];
-				double omd = 1 - d;
-				double fac = m->M_factor[c];
-				if (G == 1) {
-					double val = Id[c] * (d + fac * omd) + Im[c] * d;
-					if (val < 0) val = 0;
-					w->NMI[0] = val;
-				} else {
-					int32_t v = c * G;
-					for (int32_t a = 0; a < G; a++) w->I[a] = (Id[v + a] + Im[v + a]) * d + fac * Id[v + a] * omd;
-					const double *N = tb->Ntime + (size_t)sett * G * G;
-					for (int32_t a = 0; a < G; a++) {
-						double sum = 0.0;
-						for (int32_t aa = 0; aa < G; aa++) sum += N[a * G + aa] * w->I[aa];
-						if (sum < 0) sum = 0;
-						w->NMI[a] = sum;
-					}
-				}
-				double be = tb->beta_rows[(size_t)tb->beta_row_of[st * A + c] * m->ndivision + sett];
-				be *= tb->areafactor[(size_t)(sett / m->division_per_time) * A + c];
-				int32_t ei = tb->efoi_ref[st * A + c];
-				double et = tb->efoi_spline[(size_t)ei * m->ndivision + sett] / m->popsize;
-				for (int32_t a = 0; a < G; a++) w->eta[a] = et * tb->efoi_agedist[(size_t)ei * G + a];
-				int32_t dpp = st * DPS;
-				for (int32_t dp = 0; dp < DPS; dp++) {
-					double popu = sus_pop[dp];
-					if (popu <= 0) w->tmean[itr * DP + dpp] = 0;
-					else {
-						int32_t a = m->democatpos_age[dp];
-						double v = m->dt * popu * tb->susceptibility[dpp] * (be * w->NMI[a] + w->eta[a]);
-						if (v != v) return BEEP_NAN_RATE;
-						w->tmean[itr * DP + dpp] = v;
-					}
-					dpp++;
-				}
-			}
-			for (int32_t tr = 0; tr < T; tr++) {
-				if (tr == itr) continue;
-				int32_t from = m->trans_from[tr];
-				for (int32_t dp = 0; dp < DP; dp++) {
-					double popu = pc[(size_t)from * DP + dp];
-					if (popu <= 0) w->tmean[tr * DP + dp] = 0;
-					else w->tmean[tr * DP + dp] = m->dt * popu * tb->transrate[(size_t)tr * DP + dp];
-				}
-			}
+		for (int32_t c = 0; c < A; c++) {
+			int s = transmean_area(m, tb, w->pop, w->Imap, w->Idiag, sett, c, w);
+			if (s != BEEP_OK) return s;
 			for (int32_t tr = 0; tr < T; tr++) {           /* draws, src/state.cc:614-631 */
 				for (int32_t dp = 0; dp < DP; dp++) {
 					double mean = w->tmean[tr * DP + dp];
@@ -321,17 +432,7 @@ static int simulate_particle(const beep_model_desc *m, const beep_sim_batch *b, 
 		memcpy(w->pop_traj + (size_t)(sett - b->ti) * popsz, w->pop, sizeof(double) * popsz);
 
 		/* update_pop, src/state.cc:460-485 (pop[sett+1]; also formed after the last step) */
-		memcpy(w->popnext, w->pop, sizeof(double) * popsz);
-		for (int32_t c = 0; c < A; c++) {
-			double *pn = w->popnext + (size_t)c * C * DP;
-			for (int32_t tr = 0; tr < T; tr++) {
-				int32_t from = m->trans_from[tr], to = m->trans_to[tr];
-				for (int32_t dp = 0; dp < DP; dp++) {
-					double num = (double)tn[((size_t)c * T + tr) * DP + dp];
-					if (num != 0) { pn[(size_t)from * DP + dp] -= num; pn[(size_t)to * DP + dp] += num; }
-				}
-			}
-		}
+		update_pop(m, w->pop, tn, w->popnext);
 		double *sw = w->pop; w->pop = w->popnext; w->popnext = sw;
 	}
 
@@ -351,50 +452,9 @@ static int simulate_particle(const beep_model_desc *m, const beep_sim_batch *b, 
 		for (size_t k = 0; k < nsteps * popsz; k++) po[k] = (int32_t)w->pop_traj[k];
 	}
 
-	if (b->L_out) {                                       /* get_obs_value_section + calculate */
-		for (int32_t k = 0; k < ix->nscored; k++) w->obs_value[ix->scored[k]] = 0;
-		for (int32_t sett = b->ti; sett < b->tf; sett++) {
-			const int32_t *tn = w->tn_traj + (size_t)(sett - b->ti) * tnsz;
-			const double *pp = w->pop_traj + (size_t)(sett - b->ti) * popsz;
-			for (int32_t c = 0; c < A; c++) {
-				for (int32_t tr = 0; tr < T; tr++) {
-					for (int32_t dp = 0; dp < DP; dp++) {
-						int32_t cell = (c * T + tr) * DP + dp;
-						double num = (double)tn[cell];
-						if (num != 0) {
-							size_t slot = (size_t)(sett - b->ti) * ix->ncell_t + cell;
-							for (int32_t q = ix->t_ptr[slot]; q < ix->t_ptr[slot + 1]; q++) {
-								int32_t ob = ix->t_obs[q];
-								int32_t spl = m->obs_factor_spline[ob];
-								if (spl < 0) w->obs_value[ob] += m->obs_factor[ob] * num;
-								else w->obs_value[ob] += m->obs_factor[ob] * num * tb->obs_spline[(size_t)spl * m->ndivision + sett];
-							}
-						}
-					}
-				}
-				for (int32_t co = 0; co < C; co++) {
-					for (int32_t dp = 0; dp < DP; dp++) {
-						int32_t cell = (c * C + co) * DP + dp;
-						size_t slot = (size_t)(sett - b->ti) * ix->ncell_p + cell;
-						if (ix->p_ptr[slot + 1] > ix->p_ptr[slot]) {
-							double num = pp[cell];
-							for (int32_t q = ix->p_ptr[slot]; q < ix->p_ptr[slot + 1]; q++) {
-								int32_t ob = ix->p_obs[q];
-								w->obs_value[ob] += m->obs_factor[ob] * num;
-							}
-						}
-					}
-				}
-			}
-		}
-		double L = 0.0;
-		for (int32_t k = 0; k < ix->nscored; k++) {
-			int32_t i = ix->scored[k];
-			L += beep_oracle_obs_prob(w->obs_value[i], m->obs_value_kind[i], m->obs_value[i], m->obs_model[i],
-			                          m->obs_sd[i], m->obs_shape[i], m->obs_threshold[i]);
-		}
-		if (L != L) return BEEP_NAN_RATE;
-		b->L_out[p] = L;
+	if (b->L_out) {
+		int s2 = loglik_traj(m, tb, ix, b->ti, b->tf, w->tn_traj, w->pop_traj, w, &b->L_out[p]);
+		if (s2 != BEEP_OK) return s2;
 	}
 	return BEEP_OK;
 }
@@ -461,6 +521,195 @@ int beep_oracle_simulate(const beep_model_desc *m, const beep_sim_batch *b, int 
 			}
 		}
 		work_free(&w);
+	}
+	obs_index_free(&ix);
+	return status;
+}
+
+
+/* ---- model-based proposals: src/mbp.cc:252-330, src/state.cc:109-123,812-826 */
+
+typedef struct {
+	int32_t *tn;                /* [S][A][T][DP] */
+	double *mean;               /* [S][A][T][DP] transmean */
+	double *Imap, *Idiag;       /* [S][NS][A*G] */
+} chain_state;
+
+static int chain_alloc(const beep_model_desc *m, chain_state *cs)
+{
+	const size_t S = m->ndivision, tnsz = (size_t)m->narea * m->ntrans * m->ndemocatpos;
+	const size_t IG = (size_t)m->nstrain * m->narea * m->nage;
+	cs->tn = malloc(sizeof(int32_t) * S * tnsz);
+	cs->mean = malloc(sizeof(double) * S * tnsz);
+	cs->Imap = malloc(sizeof(double) * S * IG);
+	cs->Idiag = malloc(sizeof(double) * S * IG);
+	return cs->tn && cs->mean && cs->Imap && cs->Idiag ? BEEP_OK : BEEP_OOM;
+}
+
+static void chain_free(chain_state *cs)
+{
+	free(cs->tn); free(cs->mean); free(cs->Imap); free(cs->Idiag);
+}
+
+/* Mbp::mbp (src/mbp.cc:252-330) from the state ini to the state pro under the
+ * tables tb.  simu_all: every cell is drawn afresh and Imap follows
+ * set_Imap_sett (this is State::simulate(0, S), src/state.cc:596-638, with
+ * transmean and Imap kept); otherwise simu [S][A] (or NULL) marks the SIMU
+ * cells and the others are coupled to ini. */
+static int mbp_chain(const beep_model_desc *m, const beep_param_tables *tb, const obs_index *ix, uint32_t k0,
+                     uint32_t k1, uint32_t stream, int32_t infupd, int simu_all, const uint8_t *simu,
+                     const chain_state *ini, chain_state *pro, work *w, double *L)
+{
+	const int32_t A = m->narea, C = m->ncomp, T = m->ntrans, DP = m->ndemocatpos, S = m->ndivision;
+	const size_t popsz = (size_t)A * C * DP, tnsz = (size_t)A * T * DP;
+	const size_t IG = (size_t)m->nstrain * A * m->nage;
+	const int dif = !simu_all && infupd == BEEP_INF_DIF_UPDATE;
+	set_infdif(m, tb, w);
+	memcpy(w->pop, m->pop_init, sizeof(double) * popsz);   /* pop_init, src/state.cc:59-62 */
+	memset(w->Imap, 0, sizeof(double) * IG);               /* dImap, dIdiag (src/mbp.cc:405-414) */
+	memset(w->Idiag, 0, sizeof(double) * IG);
+	for (int32_t sett = 0; sett < S; sett++) {
+		double *Im = pro->Imap + sett * IG, *Id = pro->Idiag + sett * IG;
+		int32_t *tn = pro->tn + sett * tnsz;
+		double *mn = pro->mean + sett * tnsz;
+		if (!dif) {                                        /* set_Imap_sett, src/state.cc:164-174 */
+			if (sett == 0) inf_from_pop(m, tb, w->pop, w, Im, Id);
+			else {
+				memcpy(Im, Im - IG, sizeof(double) * IG);
+				memcpy(Id, Id - IG, sizeof(double) * IG);
+				inf_update(m, tn - tnsz, NULL, w, Im, Id);
+			}
+		} else {                                           /* set_Imap_using_dI, src/state.cc:109-123 */
+			const double *Ii = ini->Imap + sett * IG, *Idi = ini->Idiag + sett * IG;
+			for (size_t v = 0; v < IG; v++) {
+				Im[v] = Ii[v] + w->Imap[v];
+				Id[v] = Idi[v] + w->Idiag[v];
+			}
+		}
+		for (int32_t c = 0; c < A; c++) {
+			int s = transmean_area(m, tb, w->pop, Im, Id, sett, c, w);
+			if (s != BEEP_OK) return s;
+			const int sim = simu_all || (simu && simu[(size_t)sett * A + c]);
+			for (int32_t tr = 0; tr < T; tr++) {
+				for (int32_t dp = 0; dp < DP; dp++) {
+					const size_t cell = ((size_t)c * T + tr) * DP + dp;
+					const uint32_t col = (uint32_t)(c * DP + dp);
+					const double rate_p = w->tmean[tr * DP + dp];
+					mn[cell] = rate_p;
+					const int32_t num_i = sim ? 0 : ini->tn[sett * tnsz + cell];
+					int32_t num_p = 0;
+					if (rate_p != 0) {
+						if (rate_p > 1000000000.0) return BEEP_COUNT_OVERFLOW;
+						if (sim) num_p = beep_poisson_ref(rate_p, k0, k1, col, (uint32_t)tr, (uint32_t)sett, stream);
+						else {
+							const double rate_i = ini->mean[sett * tnsz + cell];
+							if (rate_p > rate_i) {
+								num_p = beep_poisson_ref(rate_p - rate_i, k0, k1, col, (uint32_t)tr, (uint32_t)sett, stream);
+								if (num_p >= 0) num_p += num_i;
+							} else if (rate_p == rate_i) num_p = num_i;
+							else num_p = beep_binomial_ref(rate_p / rate_i, num_i, k0, k1, col, (uint32_t)tr,
+							                               (uint32_t)sett, stream);
+						}
+						if (num_p < 0) return BEEP_TIMEOUT;
+					}
+					tn[cell] = num_p;
+				}
+			}
+		}
+		memcpy(w->pop_traj + (size_t)sett * popsz, w->pop, sizeof(double) * popsz);
+		if (sett < S - 1) {
+			update_pop(m, w->pop, tn, w->popnext);
+			double *sw = w->pop; w->pop = w->popnext; w->popnext = sw;
+			if (dif) inf_update(m, tn, ini->tn + sett * tnsz, w, w->Imap, w->Idiag);
+		}
+	}
+	return L ? loglik_traj(m, tb, ix, 0, S, pro->tn, w->pop_traj, w, L) : BEEP_OK;
+}
+
+/* State::likelihood (src/state.cc:812-826) of the state cs; with tb, the
+ * transition means are first recomputed under tb on the fixed state
+ * (Mbp::parameter_proposal, src/mbp.cc:460-478), else the stored ones are used */
+static int state_likelihood(const beep_model_desc *m, const beep_param_tables *tb, const chain_state *cs, work *w,
+                            double *Li)
+{
+	const int32_t A = m->narea, C = m->ncomp, T = m->ntrans, DP = m->ndemocatpos, S = m->ndivision;
+	const size_t popsz = (size_t)A * C * DP, tnsz = (size_t)A * T * DP;
+	const size_t IG = (size_t)m->nstrain * A * m->nage;
+	double L = 0.0;
+	memcpy(w->pop, m->pop_init, sizeof(double) * popsz);
+	for (int32_t sett = 0; sett < S; sett++) {
+		const int32_t *tn = cs->tn + sett * tnsz;
+		for (int32_t c = 0; c < A; c++) {
+			if (tb) {
+				int s = transmean_area(m, tb, w->pop, cs->Imap + sett * IG, cs->Idiag + sett * IG, sett, c, w);
+				if (s != BEEP_OK) return s;
+			}
+			for (int32_t tr = 0; tr < T; tr++)
+				for (int32_t dp = 0; dp < DP; dp++) {
+					const size_t cell = ((size_t)c * T + tr) * DP + dp;
+					const double mean = tb ? w->tmean[tr * DP + dp] : cs->mean[sett * tnsz + cell];
+					L += poisson_probability(tn[cell], mean);
+				}
+		}
+		if (tb) {
+			update_pop(m, w->pop, tn, w->popnext);
+			double *sw = w->pop; w->pop = w->popnext; w->popnext = sw;
+		}
+	}
+	*Li = L;
+	return BEEP_OK;
+}
+
+int beep_oracle_mbp(const beep_model_desc *m, int32_t nchain, const beep_param_tables *groups,
+                    const int32_t *ginit, const int32_t *gprop, uint64_t seed, const uint32_t *sinit,
+                    const uint32_t *sprop, int32_t inf_update, const uint8_t *simu, double *L_init, double *L_prop,
+                    double *Li_init, double *Li_fixed, int32_t *tn_init, int32_t *tn_prop, int nthreads)
+{
+	if (!m || !groups || nchain < 0 || !ginit || !gprop || !sinit || !sprop) return BEEP_BAD_INPUT;
+	const int32_t S = m->ndivision;
+	const size_t tnsz = (size_t)m->narea * m->ntrans * m->ndemocatpos;
+	const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+	obs_index ix;
+	int status = obs_index_build(m, 0, S, &ix);
+	if (status != BEEP_OK) { obs_index_free(&ix); return status; }
+#ifdef _OPENMP
+	if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+	(void)nthreads;
+#endif
+#pragma omp parallel
+	{
+		work w;
+		chain_state a, b;
+		int ws = work_alloc(m, S, &w);
+		if (ws == BEEP_OK) ws = chain_alloc(m, &a);
+		if (ws == BEEP_OK) ws = chain_alloc(m, &b);
+		if (ws != BEEP_OK) {
+#pragma omp critical
+			status = ws;
+		}
+#pragma omp for schedule(dynamic, 1)
+		for (int32_t k = 0; k < nchain; k++) {
+			if (ws != BEEP_OK || status != BEEP_OK) continue;
+			const beep_param_tables *ti = &groups[ginit[k]], *tp = &groups[gprop[k]];
+			double Lv;
+			int s = mbp_chain(m, ti, &ix, k0, k1, sinit[k], BEEP_INF_UPDATE, 1, NULL, NULL, &a, &w, &Lv);
+			if (s == BEEP_OK && L_init) L_init[k] = Lv;
+			if (s == BEEP_OK && Li_init) s = state_likelihood(m, NULL, &a, &w, &Li_init[k]);
+			if (s == BEEP_OK && Li_fixed) s = state_likelihood(m, tp, &a, &w, &Li_fixed[k]);
+			if (s == BEEP_OK)
+				s = mbp_chain(m, tp, &ix, k0, k1, sprop[k], inf_update, 0,
+				              simu ? simu + (size_t)k * S * m->narea : NULL, &a, &b, &w, &Lv);
+			if (s == BEEP_OK && L_prop) L_prop[k] = Lv;
+			if (s == BEEP_OK && tn_init) memcpy(tn_init + (size_t)k * S * tnsz, a.tn, sizeof(int32_t) * S * tnsz);
+			if (s == BEEP_OK && tn_prop) memcpy(tn_prop + (size_t)k * S * tnsz, b.tn, sizeof(int32_t) * S * tnsz);
+			if (s != BEEP_OK) {
+#pragma omp critical
+				status = s;
+			}
+		}
+		if (ws == BEEP_OK || 1) { work_free(&w); }
+		chain_free(&a); chain_free(&b);
 	}
 	obs_index_free(&ix);
 	return status;

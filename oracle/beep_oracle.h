@@ -43,6 +43,21 @@ int beep_oracle_pf(const beep_model_desc *m, const beep_param_tables *tab, int32
                    const int32_t *sec_tf, double *loglik, double *loglik_sec, double *L_out, int32_t *anc_out,
                    int nthreads);
 
+/* Model-based proposals (Mbp::mbp, src/mbp.cc:252-330) for nchain chains.
+ * Chain k: the initial state is State::simulate(theta_k) over [0, ndivision)
+ * with tables groups[ginit[k]] and variate stream sinit[k]; the proposal is
+ * Mbp::mbp(theta'_k, inf_update) with tables groups[gprop[k]] and stream
+ * sprop[k], simu [k][ndivision][narea] marking SIMU cells (NULL: none).
+ * Outputs (each may be NULL): L_init / L_prop [nchain] log-likelihoods of the
+ * two states (EF = -2 L); Li_init [nchain] State::likelihood() of the initial
+ * state (src/state.cc:812-826); Li_fixed [nchain] the same with the means
+ * recomputed under theta'_k on the fixed initial state (parameter_proposal,
+ * src/mbp.cc:460-478); tn_init / tn_prop [nchain][S][A][T][DP]. */
+int beep_oracle_mbp(const beep_model_desc *m, int32_t nchain, const beep_param_tables *groups,
+                    const int32_t *ginit, const int32_t *gprop, uint64_t seed, const uint32_t *sinit,
+                    const uint32_t *sprop, int32_t inf_update, const uint8_t *simu, double *L_init, double *L_prop,
+                    double *Li_init, double *Li_fixed, int32_t *tn_init, int32_t *tn_prop, int nthreads);
+
 /* ABC-SMC weights (src/abcsmc.cc:260-283, src/mvn.cc:185-196), FP64 as the
  * reference computes them. */
 void beep_oracle_abcsmc_weights(int32_t nvar, int32_t nnew, const double *theta_new, const double *logprior_new,
@@ -52,6 +67,10 @@ void beep_oracle_abcsmc_weights(int32_t nvar, int32_t nnew, const double *theta_
 /* One Poisson draw from the keyed stream (exposed for sampler tests). */
 int32_t beep_oracle_poisson(double mean, uint64_t seed, uint32_t col, uint32_t tr, uint32_t step,
                             uint32_t stream);
+
+/* One Binomial(n, p) thinning draw from the keyed stream (for sampler tests). */
+int32_t beep_oracle_binomial(double p, int32_t n, uint64_t seed, uint32_t col, uint32_t tr, uint32_t step,
+                             uint32_t stream);
 
 /* Project exp / log / log-factorial used inside the sampler (for tests). */
 double beep_oracle_exp(double x);

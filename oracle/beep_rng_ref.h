@@ -22,6 +22,16 @@
  *                            Insurance: Math. & Econ. 12, 1993); iteration it
  *                            takes (U, V) from words 0, 1 of
  *                            Philox({col, sett, s, (1<<24) | (tr<<16) | it}).
+ *   Binomial : thinning of a count n with probability p (coupled proposals,
+ *              src/mbp.cc:300-303); with q = min(p, 1-p):
+ *              n q < 10   -> sequential inversion with the word tr%4 of
+ *                            Philox({col, sett, s, (2<<24) | tr/4});
+ *              n q >= 10  -> BTRS, transformed rejection with squeeze
+ *                            (W. Hoermann, "The generation of binomial random
+ *                            variates", J. Statist. Comput. Simul. 46, 1993);
+ *                            iteration it takes (U, V) from words 0, 1 of
+ *                            Philox({col, sett, s, (4<<24) | (tr<<16) | it});
+ *              a draw for q = 1-p is n minus the draw for q.
  *   exp/log  : written here from the mathematics (Cody-Waite reduction by
  *              ln 2 + Taylor series of e^r; log by the atanh series), using
  *              only IEEE-754 +,-,*,/ and sqrt so that the host and the GPU
@@ -38,6 +48,7 @@
 #define BEEP_PURPOSE_PTRS 1u     /* rejection pairs of transition draws       */
 #define BEEP_PURPOSE_THIN 2u     /* binomial thinning of coupled proposals    */
 #define BEEP_PURPOSE_RESAMPLE 3u /* particle-filter resampling uniforms       */
+#define BEEP_PURPOSE_BTRS 4u     /* rejection pairs of binomial thinning      */
 
 typedef struct { uint32_t v[4]; } beep_u32x4;
 
@@ -204,6 +215,61 @@ static inline int32_t beep_poisson_ref(double mean, uint32_t k0, uint32_t k1, ui
 		if (lhs <= rhs) return (int32_t)k;
 	}
 	return -1;   /* 65536 rejections: reported as an error by the callers */
+}
+
+/* ---- Binomial(n, p) from the keyed stream -------------------------------- */
+
+/* Thinning of count n of transition tr of column col at step sett; -1 after
+ * 65536 rejections. */
+static inline int32_t beep_binomial_ref(double p, int32_t n, uint32_t k0, uint32_t k1, uint32_t col,
+                                        uint32_t tr, uint32_t sett, uint32_t stream)
+{
+	if (n <= 0 || !(p > 0.0)) return 0;
+	if (p >= 1.0) return n;
+	const int flip = p > 0.5;
+	const double q = flip ? 1.0 - p : p;
+	const double nd = (double)n;
+	int32_t k;
+	if (nd * q < 10.0) {
+		beep_u32x4 c = {{col, sett, stream, (BEEP_PURPOSE_THIN << 24) | (tr >> 2)}};
+		beep_u32x4 r = beep_philox4x32_10(c, k0, k1);
+		const double u = beep_u01(r.v[tr & 3u]);
+		const double ratio = q / (1.0 - q);
+		double f = beep_exp(nd * beep_log(1.0 - q));
+		double F = f;
+		k = 0;
+		while (u > F && k < n) {
+			f = f * ratio * (double)(n - k) / (double)(k + 1);
+			k++;
+			F = F + f;
+		}
+	} else {
+		const double spq = sqrt(nd * q * (1.0 - q));
+		const double b = 1.15 + 2.53 * spq;
+		const double a = -0.0873 + 0.0248 * b + 0.01 * q;
+		const double c = nd * q + 0.5;
+		const double alpha = (2.83 + 5.1 / b) * spq;
+		const double vr = 0.92 - 4.2 / b;
+		const double m = floor((nd + 1.0) * q);
+		const double lpq = beep_log(q / (1.0 - q));
+		const double h = beep_log_factorial(m) + beep_log_factorial(nd - m);
+		k = -1;
+		for (uint32_t it = 0; it < 65536u; it++) {
+			beep_u32x4 cc = {{col, sett, stream, (BEEP_PURPOSE_BTRS << 24) | (tr << 16) | it}};
+			beep_u32x4 r = beep_philox4x32_10(cc, k0, k1);
+			const double U = beep_u01(r.v[0]) - 0.5;
+			const double V = beep_u01(r.v[1]);
+			const double us = 0.5 - fabs(U);
+			const double kd = floor((2.0 * a / us + b) * U + c);
+			if (kd < 0.0 || kd > nd) continue;
+			if (us >= 0.07 && V <= vr) { k = (int32_t)kd; break; }
+			const double lhs = beep_log(V * alpha / (a / (us * us) + b));
+			const double rhs = h - beep_log_factorial(kd) - beep_log_factorial(nd - kd) + (kd - m) * lpq;
+			if (lhs <= rhs) { k = (int32_t)kd; break; }
+		}
+		if (k < 0) return -1;
+	}
+	return flip ? n - k : k;
 }
 
 #endif

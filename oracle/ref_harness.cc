@@ -15,7 +15,11 @@
 // set_param produced, and the reference's outputs (log-likelihoods,
 // transition counts and populations).
 //
-// usage: ref_harness out=FILE [npart=N] [ntraj=N] [seed=S] [pf=0|1] [theta=FILE] -- <BEEP key=value...>
+// With mbp=N it also drives the reference's Mbp (src/mbp.cc:252-361): N
+// chains, each simulated at one parameter row and proposed at the next, with
+// binomial_sample (src/utils.cc:174-180) interposed like poisson_sample.
+//
+// usage: ref_harness out=FILE [npart=N] [ntraj=N] [seed=S] [pf=0|1] [theta=FILE] [mbp=N] -- <BEEP key=value...>
 
 #include <cmath>
 #include <cstdint>
@@ -36,6 +40,7 @@
 // PMCMC::bootstrap; the access specifiers are lifted for this translation unit.
 #define private public
 #include "pmcmc.hh"
+#include "mbp.hh"
 #undef private
 #include "mpi.hh"
 #include "data.hh"
@@ -55,6 +60,10 @@ namespace {
 struct Replay {
 	bool active = false;
 	const State *st = nullptr;
+	// Mbp::mbp replay: st is the proposed state, ini the initial one
+	bool mbp = false;
+	const State *ini = nullptr;
+	const std::vector<std::vector<Simu_or_mbp>> *sorm = nullptr;
 	uint32_t k0 = 0, k1 = 0, stream = 0;
 	unsigned sett = 0, c = 0, tr = 0, dp = 0;
 	unsigned narea = 0, ntrans = 0, ndp = 0, ndiv = 0;
@@ -72,7 +81,34 @@ Replay g_replay;
 }  // namespace
 
 extern "C" int __real__Z14poisson_sampled(double lam);
+extern "C" unsigned int __real__Z15binomial_sampledj(double p, unsigned int n);
 extern "C" double __real__Z3ranv();
+
+namespace {
+// Kind of draw Mbp::mbp makes for the cell under the cursor (src/mbp.cc:284-305):
+// 0 none, 1 Poisson(m'), 2 Poisson(m' - m), 3 Binomial(n, m'/m).
+int mbp_kind(const Replay &r)
+{
+	const double mp = r.st->transmean[r.sett][r.c][r.tr][r.dp];
+	if (mp == 0) return 0;
+	if ((*r.sorm)[r.sett][r.c] == SIMU) return 1;
+	const double mi = r.ini->transmean[r.sett][r.c][r.tr][r.dp];
+	if (mp > mi) return 2;
+	if (mp == mi) return 0;
+	return 3;
+}
+
+// Moves the cursor to the next cell that draws; returns its kind.
+int mbp_seek(Replay &r)
+{
+	while (true) {
+		if (r.sett >= r.ndiv) { fprintf(stderr, "replay: cursor ran past the last step\n"); abort(); }
+		const int k = mbp_kind(r);
+		if (k) return k;
+		r.advance();
+	}
+}
+}  // namespace
 
 // ran() (src/utils.cc:50-69) answered from the keyed stream while a bootstrap
 // runs: the k-th call of section sec takes word 0 of
@@ -103,6 +139,21 @@ extern "C" int __wrap__Z14poisson_sampled(double lam)
 {
 	Replay &r = g_replay;
 	if (!r.active) return __real__Z14poisson_sampled(lam);
+	if (r.mbp) {
+		const int kind = mbp_seek(r);
+		const double mp = r.st->transmean[r.sett][r.c][r.tr][r.dp];
+		const double want = kind == 1 ? mp : mp - r.ini->transmean[r.sett][r.c][r.tr][r.dp];
+		if (kind == 3 || memcmp(&want, &lam, sizeof lam) != 0) {
+			fprintf(stderr, "replay: MBP Poisson mismatch at sett=%u c=%u tr=%u dp=%u (kind %d): %.17g vs %.17g\n",
+			        r.sett, r.c, r.tr, r.dp, kind, want, lam);
+			abort();
+		}
+		int v = beep_poisson_ref(lam, r.k0, r.k1, r.c * r.ndp + r.dp, r.tr, r.sett, r.stream);
+		if (v < 0) { fprintf(stderr, "replay: rejection sampler gave up\n"); abort(); }
+		r.ncalls++;
+		r.advance();
+		return v;
+	}
 	while (true) {
 		if (r.sett >= r.ndiv) { fprintf(stderr, "replay: cursor ran past the last step\n"); abort(); }
 		double m = r.st->transmean[r.sett][r.c][r.tr][r.dp];
@@ -120,6 +171,29 @@ extern "C" int __wrap__Z14poisson_sampled(double lam)
 	r.ncalls++;
 	r.advance();
 	return v;
+}
+
+// binomial_sample(p, n) (src/utils.cc:174-180), called by Mbp::mbp when the
+// proposed mean is below the initial one: answered with the keyed thinning
+// draw of the cell under the cursor.
+extern "C" unsigned int __wrap__Z15binomial_sampledj(double p, unsigned int n)
+{
+	Replay &r = g_replay;
+	if (!r.active || !r.mbp) return __real__Z15binomial_sampledj(p, n);
+	const int kind = mbp_seek(r);
+	const double mp = r.st->transmean[r.sett][r.c][r.tr][r.dp], mi = r.ini->transmean[r.sett][r.c][r.tr][r.dp];
+	const double want = mp / mi;
+	const int ni = (int)r.ini->transnum[r.sett][r.c][r.tr][r.dp];
+	if (kind != 3 || memcmp(&want, &p, sizeof p) != 0 || (unsigned int)ni != n) {
+		fprintf(stderr, "replay: MBP binomial mismatch at sett=%u c=%u tr=%u dp=%u (kind %d): p %.17g vs %.17g, n %d vs %u\n",
+		        r.sett, r.c, r.tr, r.dp, kind, want, p, ni, n);
+		abort();
+	}
+	int v = beep_binomial_ref(p, (int32_t)n, r.k0, r.k1, r.c * r.ndp + r.dp, r.tr, r.sett, r.stream);
+	if (v < 0) { fprintf(stderr, "replay: binomial rejection sampler gave up\n"); abort(); }
+	r.ncalls++;
+	r.advance();
+	return (unsigned int)v;
 }
 
 // ---- bundle writer -------------------------------------------------------
@@ -457,6 +531,84 @@ int main(int argc, char **argv)
 		int nt = std::min(ntraj, npart);
 		B.i(gp + "transnum", tnum, {(uint64_t)nt, S, A, T, DP});
 		B.i(gp + "pop", popt, {(uint64_t)nt, S, A, C, DP});
+	}
+	if (opt.count("mbp")) {
+		// MBP chains (src/mbp.cc:252-361,460-491, src/state.cc:812-826).  Chain k
+		// starts from State::simulate(theta[2k]) on stream 1000+k; its proposal is
+		// Mbp::mbp(theta[2k+1]) on stream 2000+100v+k in three variants v:
+		// 0 INF_DIF_UPDATE, 1 INF_UPDATE, 2 INF_DIF_UPDATE with SIMU cells
+		// (steps [S/4, S/2), areas with (c + sett + k) even).
+		const int NC = atoi(opt["mbp"].c_str());
+		if ((int)thetas.size() < 2 * NC) { fprintf(stderr, "mbp=%d needs %d parameter rows\n", NC, 2 * NC); return 2; }
+		Output output(details, data, model, inputs, obsmodel, mpi);
+		Mbp mb(INVT, details, data, model, obsmodel, output, mpi);
+		mb.invT = 1.0;
+		const InfUpdate iu[3] = {INF_DIF_UPDATE, INF_UPDATE, INF_DIF_UPDATE};
+		B.scalar_i("mbp.nchain", NC);
+		for (int v = 0; v < 3; v++) {
+			std::string vp = "mbp" + std::to_string(v) + ".";
+			std::vector<double> Li_, Lp_, Lii, Lif, EFi, EFp, Pri, Prp, al, chk;
+			std::vector<int32_t> simu((size_t)NC * S * A, 0), tni, tnp, si, sp;
+			for (int k = 0; k < NC; k++) {
+				State *ini = mb.initial;
+				g_replay.mbp = false; g_replay.st = ini; g_replay.stream = 1000u + k;
+				g_replay.sett = 0; g_replay.c = 0; g_replay.tr = 0; g_replay.dp = 0;
+				g_replay.active = true;
+				ini->simulate(thetas[2 * k]);
+				g_replay.active = false;
+				Li_.push_back(obsmodel.calculate(ini)); EFi.push_back(ini->EF); Pri.push_back(ini->Pr);
+				Lii.push_back(ini->likelihood());
+				mb.copy_initial_to_propse();                      // parameter_proposal on the fixed state
+				mb.propose->set_param(thetas[2 * k + 1]);
+				for (unsigned sett = 0; sett < S; sett++)
+					for (unsigned c = 0; c < A; c++) mb.propose->set_transmean(sett, c);
+				Lif.push_back(mb.propose->likelihood());
+				mb.simu_or_mbp_reset();
+				if (v == 2)
+					for (unsigned sett = S / 4; sett < S / 2; sett++)
+						for (unsigned c = 0; c < A; c++)
+							if ((c + sett + k) % 2 == 0) { mb.simu_or_mbp[sett][c] = SIMU; simu[((size_t)k * S + sett) * A + c] = 1; }
+				g_replay.mbp = true; g_replay.st = mb.propose; g_replay.ini = mb.initial; g_replay.sorm = &mb.simu_or_mbp;
+				g_replay.stream = 2000u + 100u * v + k;
+				g_replay.sett = 0; g_replay.c = 0; g_replay.tr = 0; g_replay.dp = 0;
+				g_replay.active = true;
+				Status ok = mb.mbp(thetas[2 * k + 1], iu[v]);
+				g_replay.active = false; g_replay.mbp = false;
+				if (ok != SUCCESS) { fprintf(stderr, "mbp: proposal %d outside the prior bounds\n", k); return 2; }
+				al.push_back(mb.get_al());                        // sets the proposal's EF and Pr
+				Lp_.push_back(obsmodel.calculate(mb.propose)); EFp.push_back(mb.propose->EF); Prp.push_back(mb.propose->Pr);
+				si.push_back((int32_t)(1000u + k)); sp.push_back((int32_t)(2000u + 100u * v + k));
+				for (const State *x : {(const State *)mb.initial, (const State *)mb.propose}) {
+					double s1 = 0, s2 = 0;
+					for (unsigned s = 0; s < S; s++)
+						for (unsigned c = 0; c < A; c++)
+							for (unsigned tr = 0; tr < T; tr++)
+								for (unsigned dp = 0; dp < DP; dp++) {
+									double val = x->transnum[s][c][tr][dp];
+									s1 += val; s2 += val * (double)(1 + ((s * 131 + c * 31 + tr * 7 + dp) % 1009));
+								}
+					chk.push_back(s1); chk.push_back(s2);
+				}
+				if (k < ntraj)
+					for (unsigned s = 0; s < S; s++)
+						for (unsigned c = 0; c < A; c++)
+							for (unsigned tr = 0; tr < T; tr++)
+								for (unsigned dp = 0; dp < DP; dp++) {
+									tni.push_back((int32_t)mb.initial->transnum[s][c][tr][dp]);
+									tnp.push_back((int32_t)mb.propose->transnum[s][c][tr][dp]);
+								}
+			}
+			B.scalar_i(vp + "inf_update", (int32_t)iu[v]);
+			B.i(vp + "simu", simu, {(uint64_t)NC, S, A});
+			B.i(vp + "stream_init", si); B.i(vp + "stream_prop", sp);
+			B.d(vp + "L_init", Li_); B.d(vp + "L_prop", Lp_); B.d(vp + "Li_init", Lii); B.d(vp + "Li_fixed", Lif);
+			B.d(vp + "EF_init", EFi); B.d(vp + "EF_prop", EFp); B.d(vp + "Pr_init", Pri); B.d(vp + "Pr_prop", Prp);
+			B.d(vp + "al", al);
+			B.d(vp + "checksum", chk, {(uint64_t)NC, 2, 2});
+			const int nt = std::min(ntraj, NC);
+			B.i(vp + "transnum_init", tni, {(uint64_t)nt, S, A, T, DP});
+			B.i(vp + "transnum_prop", tnp, {(uint64_t)nt, S, A, T, DP});
+		}
 	}
 	B.close();
 	fprintf(stderr, "ref_harness: %d groups x %d particles, %llu keyed draws\n", ngroup, npart, g_replay.ncalls);

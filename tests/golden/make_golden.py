@@ -33,12 +33,14 @@ from beep_gb300 import bundle, synth  # noqa: E402
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
 
 
-def run_harness(workdir, toml, out, npart, ntraj, seed, mode, pf=False, theta=None, pfn=0):
+def run_harness(workdir, toml, out, npart, ntraj, seed, mode, pf=False, theta=None, pfn=0, mbp=0):
     cmd = [HARNESS, f"out={out}", f"npart={npart}", f"ntraj={ntraj}", f"seed={seed}", f"pf={1 if pf else 0}"]
     if theta is not None:
         cmd.append(f"theta={theta}")
     if pfn:
         cmd.append(f"pfn={pfn}")
+    if mbp:
+        cmd.append(f"mbp={mbp}")
     cmd += ["--", f"inputfile={os.path.basename(toml)}", f"mode={mode}"]
     if pfn:
         cmd += [f"nparticle={pfn}", "nsample=400", "nburnin=200", "invT=1"]
@@ -91,7 +93,28 @@ def obs_values_from(b, w: synth.Workload):
     return out
 
 
-def make_fixture(name, w: synth.Workload, npart, ntraj, seed, pf=False, theta_rows=None, keep_dir=None, pfn=0):
+def mbp_theta_rows(base, nchain, seed):
+    """2*nchain parameter rows around the workload's own values: row 2k starts
+    chain k, row 2k+1 is its proposal.  Perturbed are the E, I and H mean
+    durations (positions 1, 2, 4), the I->H branch probability with its
+    complement (5, 6) and the R-spline knots (9..13) -- the reference's
+    parameter order for these workloads; the infectivity (3) is kept."""
+    rng = np.random.default_rng(seed + 11)
+    rows = []
+    for _ in range(2 * nchain):
+        t = np.array(base, np.float64)
+        for i, lo, hi in ((1, 2.0, 6.0), (2, 3.0, 8.0), (4, 4.0, 12.0)):
+            t[i] = min(hi - 1e-3, max(lo + 1e-3, t[i] * rng.uniform(0.85, 1.15)))
+        t[5] = t[5] * rng.uniform(0.7, 1.3)
+        t[6] = 1.0 - t[5]
+        for i in range(9, 14):
+            t[i] = min(3.99, max(0.51, t[i] * rng.uniform(0.85, 1.15)))
+        rows.append(t)
+    return rows
+
+
+def make_fixture(name, w: synth.Workload, npart, ntraj, seed, pf=False, theta_rows=None, keep_dir=None, pfn=0,
+                 mbp=0):
     work = tempfile.mkdtemp(prefix=f"golden_{name}_")
     try:
         toml = synth.write_beep_inputs(w, work)
@@ -105,8 +128,14 @@ def make_fixture(name, w: synth.Workload, npart, ntraj, seed, pf=False, theta_ro
             with open(theta, "w") as f:
                 for row in theta_rows:
                     f.write(",".join(repr(float(x)) for x in row) + "\n")
+        if mbp and theta_rows is None:
+            theta = os.path.join(work, "theta.csv")
+            base = b0["g0.theta"]
+            with open(theta, "w") as f:
+                for row in mbp_theta_rows(base, mbp, w.seed):
+                    f.write(",".join(repr(float(x)) for x in row) + "\n")
         out = os.path.join(HERE, f"{name}.bnd")
-        run_harness(work, toml, out, npart, ntraj, seed, mode, pf=pf, theta=theta, pfn=pfn)
+        run_harness(work, toml, out, npart, ntraj, seed, mode, pf=pf, theta=theta, pfn=pfn, mbp=mbp)
         if keep_dir:
             shutil.copytree(work, os.path.join(keep_dir, name), dirs_exist_ok=True)
         print(f"{name}: {os.path.getsize(out) / 1e3:.0f} kB")
@@ -134,6 +163,10 @@ def main():
     c0 = synth.seir_hd_small(seed=20260000, narea=10, nage=3, days=100, name="c0")
     make_fixture("c0_sim", c0, npart=16, ntraj=1, seed=20260000)
     make_fixture("c0_pf", c0, npart=8, ntraj=1, seed=20260001, pf=True, pfn=64)
+    # MBP chains: 4 chains, three proposal variants each (coupled draws, SIMU cells)
+    tmbp = synth.seir_hd_small(seed=20260103, narea=4, nage=2, days=40, name="tinymbp")
+    make_fixture("tiny_mbp", tmbp, npart=1, ntraj=1, seed=0x5EED0F00D, mbp=4)
+    make_fixture("c0_mbp", c0, npart=1, ntraj=0, seed=20260003, mbp=4)
 
 
 if __name__ == "__main__":

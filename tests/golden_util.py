@@ -10,6 +10,8 @@ from beep_gb300 import bundle, capi
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 FIXTURES = ["tiny_sim", "oneage_sim", "c0_sim"]
 PF_FIXTURES = ["tiny_pf", "c0_pf"]
+MBP_FIXTURES = ["tiny_mbp", "c0_mbp"]
+MBP_VARIANTS = 3   # 0 INF_DIF_UPDATE, 1 INF_UPDATE, 2 INF_DIF_UPDATE with SIMU cells
 
 
 def load(name):
@@ -30,3 +32,21 @@ def checksums(transnum, pop):
     tn = transnum.astype(np.float64)
     pp = pop.astype(np.float64)
     return np.array([tn.sum(), (tn * wt).sum(), pp.sum(), (pp * wp).sum()])
+
+
+def mbp_case(b, v):
+    """Inputs of MBP variant v of a fixture: (ginit, gprop, sinit, sprop, inf_update, simu)."""
+    nc = int(b["mbp.nchain"][0])
+    p = f"mbp{v}."
+    simu = b[p + "simu"].astype(np.uint8)
+    return (np.arange(nc) * 2, np.arange(nc) * 2 + 1, b[p + "stream_init"].astype(np.uint32),
+            b[p + "stream_prop"].astype(np.uint32), int(b[p + "inf_update"][0]), simu if simu.any() else None)
+
+
+def tn_checksums(transnum):
+    """The reference harness's two transition-count checksums of [S][A][T][DP]."""
+    S, A, T, DP = transnum.shape
+    s, c, t, d = np.meshgrid(np.arange(S), np.arange(A), np.arange(T), np.arange(DP), indexing="ij")
+    wt = 1 + ((s * 131 + c * 31 + t * 7 + d) % 1009)
+    tn = transnum.astype(np.float64)
+    return np.array([tn.sum(), (tn * wt).sum()])

@@ -23,6 +23,9 @@ def oracle_lib():
         L.beep_oracle_simulate.restype = C.c_int
         L.beep_oracle_poisson.argtypes = [C.c_double, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]
         L.beep_oracle_poisson.restype = C.c_int32
+        L.beep_oracle_binomial.argtypes = [C.c_double, C.c_int32, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
+                                           C.c_uint32]
+        L.beep_oracle_binomial.restype = C.c_int32
         for f in ("beep_oracle_exp", "beep_oracle_log", "beep_oracle_log_factorial"):
             getattr(L, f).argtypes = [C.c_double]
             getattr(L, f).restype = C.c_double
@@ -36,6 +39,10 @@ def oracle_lib():
         L.beep_oracle_abcsmc_weights.argtypes = [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
                                                  C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]
         L.beep_oracle_abcsmc_weights.restype = None
+        L.beep_oracle_mbp.argtypes = [C.POINTER(capi.ModelDesc), C.c_int32, C.POINTER(capi.ParamTables),
+                                      C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_int32,
+                                      C.c_void_p] + [C.c_void_p] * 6 + [C.c_int]
+        L.beep_oracle_mbp.restype = C.c_int
         _LIB = L
     return _LIB
 
@@ -77,4 +84,29 @@ def oracle_abcsmc_weights(theta_new, logprior_new, theta_last, w_last, inv_cov, 
     oracle_lib().beep_oracle_abcsmc_weights(tn.shape[1], tn.shape[0], tn.ctypes.data, lp.ctypes.data, tl.shape[0],
                                             tl.ctypes.data, wl.ctypes.data, ic.ctypes.data, float(size),
                                             1 if normalise else 0, out.ctypes.data)
+    return out
+
+
+def oracle_mbp(model: capi.Model, tables, ginit, gprop, seed: int, sinit, sprop, inf_update: int, simu=None,
+               want_tn: bool = False, nthreads: int = 0):
+    """MBP chains of the oracle: dict of L_init, L_prop, Li_init, Li_fixed (and tn_init / tn_prop)."""
+    import numpy as np
+    nc = len(ginit)
+    groups = (capi.ParamTables * len(tables))(*[t.st for t in tables])
+    gi = np.ascontiguousarray(ginit, np.int32)
+    gp = np.ascontiguousarray(gprop, np.int32)
+    si = np.ascontiguousarray(sinit, np.uint32)
+    sp = np.ascontiguousarray(sprop, np.uint32)
+    sm = None if simu is None else np.ascontiguousarray(simu, np.uint8)
+    out = {k: np.zeros(nc) for k in ("L_init", "L_prop", "Li_init", "Li_fixed")}
+    shape = (nc, model.ndivision, model.narea, model.ntrans, model.ndemocatpos)
+    if want_tn:
+        out["tn_init"] = np.zeros(shape, np.int32)
+        out["tn_prop"] = np.zeros(shape, np.int32)
+    p = lambda a: None if a is None else a.ctypes.data
+    st = oracle_lib().beep_oracle_mbp(C.byref(model.desc), nc, groups, p(gi), p(gp), seed, p(si), p(sp), inf_update,
+                                      p(sm), p(out["L_init"]), p(out["L_prop"]), p(out["Li_init"]),
+                                      p(out["Li_fixed"]), p(out.get("tn_init")), p(out.get("tn_prop")), nthreads)
+    if st != 0:
+        raise RuntimeError(f"oracle failed: {capi.STATUS.get(st, st)}")
     return out

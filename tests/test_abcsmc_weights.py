@@ -14,7 +14,8 @@ def generation(rng, nnew, nlast, nvar=3):
     tl = rng.uniform(lo, hi, (nlast, nvar))
     wl = rng.uniform(0.2, 2.0, nlast)
     tn = np.clip(tl[rng.integers(0, nlast, nnew)] + rng.normal(0, 0.2, (nnew, nvar)), lo, hi)
-    cov = np.cov(tl.T, aweights=wl)
+    # the weighted sample covariance needs more particles than parameters
+    cov = np.cov(tl.T, aweights=wl) if nlast > nvar else np.diag(((hi - lo) / 4) ** 2)
     ic = np.linalg.inv(cov)
     lp = np.full(nnew, -np.log(np.prod(hi - lo)))
     return tn, lp, tl, wl, ic
@@ -39,4 +40,5 @@ def test_gpu_weights_match_oracle(nnew, nlast):
     tn, lp, tl, wl, ic = generation(rng, nnew, nlast)
     g = capi.abcsmc_weights(tn, lp, tl, wl, ic, 1.3)
     o = oracle_abcsmc_weights(tn, lp, tl, wl, ic, 1.3)
+    assert np.all(np.isfinite(o)) and np.all(o > 0)
     np.testing.assert_allclose(g, o, rtol=1e-5)

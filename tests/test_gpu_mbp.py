@@ -1,0 +1,96 @@
+"""MBP chains on the GPU (beep_mbp_*, plain FP64 form) against the reference's
+own Mbp (golden fixtures) and the oracle restatement."""
+import numpy as np
+import pytest
+
+from beep_gb300 import capi
+from golden_util import MBP_FIXTURES, MBP_VARIANTS, load, mbp_case, tn_checksums
+from oracle_lib import oracle_mbp
+
+pytestmark = pytest.mark.gpu
+
+L_RTOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def device():
+    capi.check(capi.lib().beep_device_init(0))
+    return 0
+
+
+@pytest.mark.parametrize("name", MBP_FIXTURES)
+@pytest.mark.parametrize("v", range(MBP_VARIANTS))
+def test_mbp_matches_reference(device, name, v):
+    b, m, tabs, seed = load(name)
+    gi, gp, si, sp, iu, simu = mbp_case(b, v)
+    p = f"mbp{v}."
+    nc = len(gi)
+    dm = capi.DeviceModel(m)
+    ch = capi.MbpChains(dm, nc)
+    L0 = ch.initialise(tabs, seed, group_of=gi, stream_of=si)
+    np.testing.assert_allclose(L0, b[p + "L_init"], rtol=L_RTOL, atol=0)
+    np.testing.assert_allclose(ch.state_likelihood(tabs, group_of=gi), b[p + "Li_init"], rtol=L_RTOL, atol=0)
+    np.testing.assert_allclose(ch.state_likelihood(tabs, group_of=gp), b[p + "Li_fixed"], rtol=L_RTOL, atol=0)
+    L1 = ch.propose(tabs, seed, group_of=gp, stream_of=sp, inf_update=iu, simu=simu)
+    np.testing.assert_allclose(L1, b[p + "L_prop"], rtol=L_RTOL, atol=0)
+    nt = b[p + "transnum_init"].shape[0]
+    for k in range(nc):
+        tn, _ = ch.read_state(k)                 # still the initial state
+        assert np.array_equal(tn_checksums(tn), b[p + "checksum"][k, 0])
+        if k < nt:
+            assert np.array_equal(tn, b[p + "transnum_init"][k])
+    ch.accept(np.ones(nc, np.uint8))              # swap_initial_propose_state
+    for k in range(nc):
+        tn, _ = ch.read_state(k)
+        assert np.array_equal(tn_checksums(tn), b[p + "checksum"][k, 1])
+        if k < nt:
+            assert np.array_equal(tn, b[p + "transnum_prop"][k])
+    al = [capi.mbp_acceptance(False, 1.0, 0.0, -2 * L1[k], -2 * L0[k], b[p + "Pr_prop"][k], b[p + "Pr_init"][k])
+          for k in range(nc)]
+    np.testing.assert_allclose(al, b[p + "al"], rtol=1e-9, atol=1e-300)
+    ch.close()
+    dm.close()
+
+
+def test_mbp_many_chains_match_oracle(device):
+    """32 chains on the 10-area x 3-age workload, each kind of proposal, against
+    the oracle; a partial acceptance leaves rejected chains on their initial state."""
+    b, m, tabs, seed = load("c0_mbp")
+    nc = 32
+    ng = len(tabs)
+    rng = np.random.default_rng(5)
+    gi = rng.integers(0, ng, nc)
+    gp = rng.integers(0, ng, nc)
+    si = np.arange(nc, dtype=np.uint32) + 7000
+    sp = np.arange(nc, dtype=np.uint32) + 9000
+    simu = (rng.random((nc, m.ndivision, m.narea)) < 0.1).astype(np.uint8)
+    dm = capi.DeviceModel(m)
+    for iu, sm in ((capi.INF_DIF_UPDATE, None), (capi.INF_UPDATE, None), (capi.INF_DIF_UPDATE, simu)):
+        o = oracle_mbp(m, tabs, gi, gp, seed, si, sp, iu, sm, want_tn=True)
+        ch = capi.MbpChains(dm, nc)
+        np.testing.assert_allclose(ch.initialise(tabs, seed, group_of=gi, stream_of=si), o["L_init"], rtol=L_RTOL)
+        np.testing.assert_allclose(ch.state_likelihood(tabs, group_of=gp), o["Li_fixed"], rtol=L_RTOL)
+        Lp = ch.propose(tabs, seed, group_of=gp, stream_of=sp, inf_update=iu, simu=sm)
+        np.testing.assert_allclose(Lp, o["L_prop"], rtol=L_RTOL)
+        acc = (np.arange(nc) % 3 == 0).astype(np.uint8)
+        ch.accept(acc)
+        for k in range(0, nc, 5):
+            tn, _ = ch.read_state(k)
+            assert np.array_equal(tn, o["tn_prop"][k] if acc[k] else o["tn_init"][k])
+        ch.close()
+    dm.close()
+
+
+def test_mbp_errors(device):
+    b, m, tabs, seed = load("tiny_mbp")
+    dm = capi.DeviceModel(m)
+    ch = capi.MbpChains(dm, 2)
+    with pytest.raises(capi.BeepError) as e:
+        ch.propose(tabs, seed)
+    assert e.value.status == 1                    # BEEP_BAD_INPUT: not initialised
+    with pytest.raises(capi.BeepError):
+        capi.MbpChains(dm, 2, form=capi.FORM_FAST)
+    with pytest.raises(capi.BeepError):
+        ch.propose(tabs, seed, inf_update=7)
+    ch.close()
+    dm.close()
