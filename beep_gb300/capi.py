@@ -78,6 +78,18 @@ class MbpRequest(C.Structure):
 INF_UPDATE = 0
 INF_DIF_UPDATE = 1
 
+REQ_LIKELIHOOD, REQ_SCENARIO, REQ_PREDICTION = 0, 1, 2
+
+
+class Request(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("model", C.POINTER(ModelDesc)), ("batch", C.POINTER(SimBatch))]
+
+
+class RequestStats(C.Structure):
+    _fields_ = [("submit_s", C.c_double), ("admit_s", C.c_double), ("done_s", C.c_double),
+                ("gpu_start_s", C.c_double), ("gpu_end_s", C.c_double), ("device_bytes", C.c_int64),
+                ("state", C.c_int32), ("status", C.c_int32)]
+
 
 def _ptr(a: Optional[np.ndarray], ctype):
     if a is None:
@@ -261,6 +273,16 @@ def lib():
         L.beep_mbp_read_state.argtypes = [C.c_void_p, C.c_int32, _i32p, _f64p]
         for f in ("beep_mbp_create", "beep_mbp_destroy", "beep_mbp_initialise", "beep_mbp_propose", "beep_mbp_accept",
                   "beep_mbp_state_likelihood", "beep_mbp_read_state"):
+            getattr(L, f).restype = C.c_int32
+        L.beep_server_create.argtypes = [C.c_int32, C.c_int64, C.c_int32, C.POINTER(C.c_void_p)]
+        L.beep_server_destroy.argtypes = [C.c_void_p]
+        L.beep_serve_submit.argtypes = [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_uint64)]
+        L.beep_serve_poll.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(C.c_int32)]
+        L.beep_serve_wait.argtypes = [C.c_void_p, C.c_uint64, C.c_double]
+        L.beep_serve_stats.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(RequestStats)]
+        L.beep_serve_release.argtypes = [C.c_void_p, C.c_uint64]
+        for f in ("beep_server_create", "beep_server_destroy", "beep_serve_submit", "beep_serve_poll",
+                  "beep_serve_wait", "beep_serve_stats", "beep_serve_release"):
             getattr(L, f).restype = C.c_int32
         for f in ("beep_device_init", "beep_model_create", "beep_model_destroy", "beep_simulate", "beep_batch_create",
                   "beep_batch_stage", "beep_batch_upload", "beep_batch_launch", "beep_batch_download",
@@ -469,3 +491,54 @@ def mbp_acceptance(cutoff: bool, invT: float, EFcut: float, EF_prop: float, EF_i
                    Pr_init: float) -> float:
     """Mbp::get_al (beep_mbp_acceptance)."""
     return lib().beep_mbp_acceptance(1 if cutoff else 0, invT, EFcut, EF_prop, EF_init, Pr_prop, Pr_init)
+
+
+class Server:
+    """A ``beep_server``: continuous batching of requests on one GPU."""
+
+    def __init__(self, hbm_budget_bytes: int, max_inflight: int = 8, device: int = 0):
+        h = C.c_void_p()
+        check(lib().beep_server_create(device, int(hbm_budget_bytes), max_inflight, C.byref(h)))
+        self.h = h
+        self._live = {}
+
+    def submit(self, model: Model, batch: Batch, kind: int = REQ_LIKELIHOOD) -> int:
+        """Queues a request; the model and batch (and their arrays) are kept until it is released."""
+        r = Request()
+        r.kind = kind
+        r.model = C.pointer(model.desc)
+        r.batch = C.pointer(batch.st)
+        t = C.c_uint64()
+        check(lib().beep_serve_submit(self.h, C.byref(r), C.byref(t)))
+        self._live[t.value] = (model, batch, r)
+        return t.value
+
+    def poll(self, ticket: int) -> bool:
+        d = C.c_int32()
+        check(lib().beep_serve_poll(self.h, ticket, C.byref(d)))
+        return bool(d.value)
+
+    def wait(self, ticket: int, timeout_s: float = -1.0) -> Batch:
+        check(lib().beep_serve_wait(self.h, ticket, timeout_s))
+        return self._live[ticket][1]
+
+    def stats(self, ticket: int) -> dict:
+        st = RequestStats()
+        check(lib().beep_serve_stats(self.h, ticket, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in RequestStats._fields_}
+
+    def release(self, ticket: int) -> None:
+        check(lib().beep_serve_release(self.h, ticket))
+        self._live.pop(ticket, None)
+
+    def close(self):
+        if self.h:
+            lib().beep_server_destroy(self.h)
+            self.h = None
+            self._live.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

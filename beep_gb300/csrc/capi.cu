@@ -641,9 +641,23 @@ beep_status beep_batch_launch(beep_batch *q)
 beep_status beep_batch_download(beep_batch *q)
 {
 	if (!q) return fail(BEEP_BAD_INPUT, "null batch");
-	const beep_sim_batch *b = &q->b;
-	CUDA_TRY(cudaMemcpyAsync(q->out_host.ptr, q->out_dev.ptr, q->out_size, cudaMemcpyDeviceToHost, q->m->stream));
+	beep_status st = batch_download_enqueue(q);
+	if (st != BEEP_OK) return st;
 	CUDA_TRY(cudaStreamSynchronize(q->m->stream));
+	return batch_download_finish(q);
+}
+
+}  // extern "C"
+
+beep_status beep::batch_download_enqueue(beep_batch *q)
+{
+	CUDA_TRY(cudaMemcpyAsync(q->out_host.ptr, q->out_dev.ptr, q->out_size, cudaMemcpyDeviceToHost, q->m->stream));
+	return BEEP_OK;
+}
+
+beep_status beep::batch_download_finish(beep_batch *q)
+{
+	const beep_sim_batch *b = &q->b;
 	q->pending = false;
 	const beep_model *m = q->m;
 	const int P = b->nparticle, nsteps = b->tf - b->ti;
@@ -658,6 +672,8 @@ beep_status beep_batch_download(beep_batch *q)
 	if (b->pop_traj_out) memcpy(b->pop_traj_out, ho + q->u_pt, 4 * popsz * (size_t)nsteps * P);
 	return BEEP_OK;
 }
+
+extern "C" {
 
 beep_status beep_batch_time(beep_batch *q, int32_t iters, double *ms_per_launch)
 {
@@ -719,3 +735,10 @@ beep_status beep_simulate(beep_model *m, const beep_sim_batch *b)
 }
 
 }  // extern "C"
+
+size_t beep::model_device_bytes(const beep_model *m) { return m ? m->model_mem.cap : 0; }
+
+size_t beep::batch_device_bytes(const beep_batch *q)
+{
+	return q ? q->in_dev.cap + q->work_dev.cap + q->out_dev.cap : 0;
+}

@@ -129,4 +129,12 @@ namespace beep {
 // live on the device (device_io: pop_in is not read from the host and the
 // caller sets bd.pop_in / bd.L / bd.pop_out before each launch).
 beep_status batch_create_internal(beep_model *m, const beep_sim_batch *b, bool device_io, beep_batch **out);
+// beep_batch_download in two halves: the device->host copy enqueued on the
+// model's stream, and (once that copy completed) the status check and the
+// copy into the caller's arrays.
+beep_status batch_download_enqueue(beep_batch *q);
+beep_status batch_download_finish(beep_batch *q);
+// Device bytes held by a model / a batch.
+size_t model_device_bytes(const beep_model *m);
+size_t batch_device_bytes(const beep_batch *q);
 }  // namespace beep

@@ -267,6 +267,18 @@ def abc_smc_large(seed: int = 20260001, narea: int = 150, nage: int = 4, days: i
                     obs_kind="cases_age", R_prior=(1.5, 4.0))
 
 
+MBP_SIZES = ((20, 2), (80, 4), (200, 6), (350, 10))
+
+
+def mbp_chain_model(narea: int, nage: int, seed: int = 20260003) -> Workload:
+    """One model of the MBP-chain workload: the 10-area recipe at narea x nage,
+    dt 0.5 over 200 days, weekly hospital-population observations per area."""
+    w = seir_hd_small(seed=seed + 1000 * narea + nage, narea=narea, nage=nage, days=200, steps_per_day=2,
+                      name=f"mbp_{narea}x{nage}")
+    w.obs_kind = "hosp_pop"
+    return w
+
+
 def abc_smc_priors(rng, n: int):
     """Per-particle parameters from the ABC-SMC priors: R0 U(1.5,4), 1/sigma U(2,6), 1/gamma U(3,8)."""
     return rng.uniform(1.5, 4.0, n), rng.uniform(2.0, 6.0, n), rng.uniform(3.0, 8.0, n)

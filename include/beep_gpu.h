@@ -295,6 +295,53 @@ BEEP_API double beep_mbp_acceptance(int32_t cutoff_mode, double invT, double EFc
 BEEP_API beep_status beep_mbp_read_state(beep_mbp_chains *chains, int32_t chain, int32_t *transnum_out,
                                          double *transmean_out);
 
+/* ---- Serving: continuous batching of requests on one GPU -----------------
+ * A server runs simulation and likelihood requests of any model size
+ * concurrently.  A request is queued at submit; a worker thread admits
+ * queued requests in arrival order as running ones complete and free device
+ * memory -- first fit, holding back the room the oldest waiting request needs
+ * so that it is never overtaken forever -- up to max_inflight at once.  An
+ * admitted request gets its own device model and batch on its own stream, so
+ * its kernels overlap with the other running requests' on the device.  The
+ * results are those beep_simulate gives for the same model and batch.  The
+ * reference runs the same three kinds of work one after another in a
+ * single process (src/pmcmc.cc:180-207, src/simulate.cc:42-165). */
+typedef enum beep_request_kind {
+	BEEP_REQ_LIKELIHOOD = 0,   /* per-particle log-likelihood over [ti, tf) (PMCMC / ABC-SMC evaluations) */
+	BEEP_REQ_SCENARIO = 1,     /* trajectories from the initial state (mode=sim, src/simulate.cc:42-65) */
+	BEEP_REQ_PREDICTION = 2    /* continuation of given populations from ti (mode=prediction, src/simulate.cc:77-165) */
+} beep_request_kind;
+
+typedef struct beep_request {
+	int32_t kind;                    /* beep_request_kind */
+	const beep_model_desc *model;    /* copied at submit; its arrays must stay valid until the request is done */
+	const beep_sim_batch *batch;     /* copied at submit; its arrays must stay valid until the request is done */
+} beep_request;
+
+typedef struct beep_request_stats {
+	double submit_s, admit_s, done_s;   /* host clock, seconds since the server started */
+	double gpu_start_s, gpu_end_s;      /* device clock: first copy in, last copy out */
+	int64_t device_bytes;               /* device memory the request held */
+	int32_t state;                      /* 0 queued, 1 running, 2 done */
+	int32_t status;                     /* beep_status once done */
+} beep_request_stats;
+
+typedef struct beep_server beep_server;
+/* hbm_budget_bytes: device memory the server's requests may hold at once
+ * (a request larger than the budget runs alone). */
+BEEP_API beep_status beep_server_create(int32_t device, int64_t hbm_budget_bytes, int32_t max_inflight,
+                                        beep_server **out);
+/* Finishes every submitted request, then releases the server. */
+BEEP_API beep_status beep_server_destroy(beep_server *server);
+BEEP_API beep_status beep_serve_submit(beep_server *server, const beep_request *request, uint64_t *ticket);
+/* *done = 1 once the request finished; the return value is then its status. */
+BEEP_API beep_status beep_serve_poll(beep_server *server, uint64_t ticket, int32_t *done);
+/* Waits up to timeout_s (< 0: without limit); BEEP_TIMEOUT if still running. */
+BEEP_API beep_status beep_serve_wait(beep_server *server, uint64_t ticket, double timeout_s);
+BEEP_API beep_status beep_serve_stats(beep_server *server, uint64_t ticket, beep_request_stats *out);
+/* Forgets a finished request. */
+BEEP_API beep_status beep_serve_release(beep_server *server, uint64_t ticket);
+
 /* Plain FP64 simulation that allocates no memory on the GPU.  No counterpart
  * in the reference: it serves callers that cannot call cudaMalloc -- an
  * application whose allocator or fixed memory budget owns all device memory,
