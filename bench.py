@@ -158,6 +158,82 @@ def cpu_throughput(m, tabs, group_of, seed, target_s: float, nthreads: int, max_
     return units_per_particle * n2 / dt, n2, dt
 
 
+def serve_requests(n: int, seed: int):
+    """The serving workload's requests: areas U{10..400}, ages U{1..10},
+    horizon U(60, 365) days, dt 0.25 or 0.5, particles log-uniform in
+    [64, 8192], kinds likelihood / scenario / prediction in equal shares, the
+    10-area recipe's populations and mixing at each size, parameters from the
+    ABC-SMC priors (16 parameter sets per request)."""
+    from beep_gb300 import capi, model_builder as mb, synth
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for k in range(n):
+        A = int(rng.integers(10, 401))
+        G = int(rng.integers(1, 11))
+        days = int(rng.uniform(60, 365))
+        spd = int(rng.choice([4, 2]))
+        P = int(np.exp(rng.uniform(np.log(64), np.log(8192))))
+        kind = int(rng.integers(0, 3))
+        w = synth.seir_hd_small(seed=seed + 17 * k, narea=A, nage=G, days=days, steps_per_day=spd, name=f"req{k}")
+        m = capi.Model(mb.model_arrays(w))
+        ng = min(16, P)
+        R0, si, gi = synth.abc_smc_priors(rng, ng)
+        tabs = [capi.Tables(t) for t in mb.param_tables_batch(w, R0, si, gi)]
+        go = np.arange(P) % ng
+        ti = 0
+        if kind == capi.REQ_LIKELIHOOD:
+            b = capi.Batch(m, tabs, P, seed + k, group_of=go, form=capi.FORM_FAST)
+        elif kind == capi.REQ_SCENARIO:
+            b = capi.Batch(m, tabs, P, seed + k, group_of=go, want_pop=True, form=capi.FORM_FAST)
+        else:
+            ti = m.ndivision // 2
+            p0 = np.rint(m.arr["pop_init"]).astype(np.int32).reshape(1, -1)
+            b = capi.Batch(m, tabs, P, seed + k, group_of=go, ti=ti, pop_in=np.repeat(p0, P, 0), want_pop=True,
+                           form=capi.FORM_FAST)
+        reqs.append(dict(kind=kind, model=m, batch=b, particles=P, units=P * A * G * (m.ndivision - ti),
+                         size=f"{A}x{G}x{m.ndivision - ti}"))
+    return reqs
+
+
+def run_serving(nreq: int, rate: float, seed: int, budget_bytes: int, inflight: int):
+    """Submits the requests at Poisson arrival times and waits for all."""
+    from beep_gb300 import capi
+    reqs = serve_requests(nreq, seed)
+    rng = np.random.default_rng(seed + 1)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
+    srv = capi.Server(budget_bytes, inflight)
+    t0 = time.perf_counter()
+    tickets = []
+    for k, r in enumerate(reqs):
+        dt = arrivals[k] - (time.perf_counter() - t0)
+        if dt > 0:
+            time.sleep(dt)
+        tickets.append(srv.submit(r["model"], r["batch"], r["kind"]))
+    for t in tickets:
+        srv.wait(t)
+    st = [srv.stats(t) for t in tickets]
+    srv.close()
+    lat = np.array([s["done_s"] - s["submit_s"] for s in st])
+    wait = np.array([s["admit_s"] - s["submit_s"] for s in st])
+    span = max(s["done_s"] for s in st) - min(s["submit_s"] for s in st)
+    busy = sorted((s["gpu_start_s"], s["gpu_end_s"]) for s in st)
+    overlap = sum(1 for a, b in zip(busy, busy[1:]) if b[0] < a[1])
+    for r in reqs:
+        assert r["batch"].L is None or np.all(np.isfinite(r["batch"].L))
+    units = sum(r["units"] for r in reqs)
+    return {
+        "requests": nreq, "arrival_rate_per_s": rate, "max_inflight": inflight, "hbm_budget_gb": budget_bytes / 2**30,
+        "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+        "queue_wait_p50_ms": float(np.percentile(wait, 50) * 1e3),
+        "throughput": units / span, "unit": "particle.area.group.steps/s",
+        "loglik_evals_per_s": sum(r["particles"] for r in reqs) / span, "makespan_s": span,
+        "overlapping_request_pairs": overlap,
+        "kinds": {k: sum(1 for r in reqs if r["kind"] == i) for i, k in enumerate(("likelihood", "scenario",
+                                                                                   "prediction"))},
+        "form": "fast", "data": "synthetic, generated per request",
+    }
+
+
 def dist_setup(args):
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -301,6 +377,9 @@ def run_ours(args, rank, ws, dist):
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
         traffic = json.load(open(tp)).get("sim_fast_kernel" if args.form == "fast" else "sim_plain_kernel")
+    serving = None
+    if args.serve_requests > 0 and ws == 1:
+        serving = run_serving(args.serve_requests, 200.0, args.seed + 4242, 200 << 30, 8)
     cpu = None
     if not args.no_cpu:
         nthreads = os.cpu_count() or 1
@@ -323,6 +402,7 @@ def run_ours(args, rank, ws, dist):
                      "peak_kind": hbm_kind, "traffic": traffic,
                      "algorithmic_bytes": f"{BYTES_PER_UNIT} B x {units} units per launch"},
         "cpu_baseline": cpu,
+        "serving": serving,
     }
     print(json.dumps(line))
     db.close()
@@ -343,6 +423,8 @@ def main():
     ap.add_argument("--form", default="fast", choices=["fast", "plain"])
     ap.add_argument("--plain-particles", type=int, default=1024)
     ap.add_argument("--plain-steps", type=int, default=0, help="time the plain form over this many steps (0: all)")
+    ap.add_argument("--serve-requests", type=int, default=32,
+                    help="requests of the serving stream (Poisson arrivals at 200/s) after the main measurement")
     args = ap.parse_args()
     rank, ws, dist = dist_setup(args)
     if args.impl == "reference":
