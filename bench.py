@@ -234,6 +234,18 @@ def run_serving(nreq: int, rate: float, seed: int, budget_bytes: int, inflight: 
     }
 
 
+def profile_traffic(kind: str, P: int):
+    """DRAM bytes per launch of the fast kernel, from the committed ncu
+    summary of the workload (captured on a smaller particle count and scaled
+    by the particles, the part of the traffic that grows with them)."""
+    import re
+    f = os.path.join(ROOT, "profiles", "sim_fast_abc_smc.md" if kind == "abc_smc" else "sim_fast_precision.md")
+    if not os.path.exists(f):
+        return None
+    m = re.search(r"dram_bytes_per_particle:\s*([0-9.]+)", open(f).read())
+    return float(m.group(1)) * P if m else None
+
+
 def dist_setup(args):
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -373,10 +385,7 @@ def run_ours(args, rank, ws, dist):
         return
     hbm, hbm_kind = peaks()
     achieved = BYTES_PER_UNIT * units / t_dev / 1e9
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tp):
-        traffic = json.load(open(tp)).get("sim_fast_kernel" if args.form == "fast" else "sim_plain_kernel")
+    traffic = profile_traffic(args.workload, P) if args.form == "fast" else None
     serving = None
     if args.serve_requests > 0 and ws == 1:
         serving = run_serving(args.serve_requests, 200.0, args.seed + 4242, 200 << 30, 8)
