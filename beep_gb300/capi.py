@@ -249,6 +249,8 @@ def lib():
                   "beep_batch_destroy"):
             getattr(L, f).argtypes = [C.c_void_p]
         L.beep_batch_time.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]
+        L.beep_batch_foi_path.argtypes = [C.c_void_p]
+        L.beep_batch_foi_path.restype = C.c_int32
         L.beep_batch_launches.argtypes = [C.c_void_p]
         L.beep_batch_launches.restype = C.c_int32
         L.beep_batch_bytes.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
@@ -262,6 +264,8 @@ def lib():
         L.beep_abcsmc_weights.restype = C.c_int32
         L.beep_pf_loglik.argtypes = [C.c_void_p, C.POINTER(PFRequest)]
         L.beep_pf_loglik.restype = C.c_int32
+        L.beep_set_option.argtypes = [C.c_char_p, C.c_int64]
+        L.beep_set_option.restype = C.c_int32
         L.beep_mbp_create.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]
         L.beep_mbp_destroy.argtypes = [C.c_void_p]
         for f in ("beep_mbp_initialise", "beep_mbp_propose"):
@@ -290,6 +294,14 @@ def lib():
             getattr(L, f).restype = C.c_int32
         _LIB = L
     return _LIB
+
+
+FOI_AUTO, FOI_SIMT, FOI_TENSOR = 0, 1, 2
+
+
+def set_option(name: str, value: int) -> None:
+    """Process-wide library option (beep_set_option), e.g. ``set_option("fast_foi", FOI_TENSOR)``."""
+    check(lib().beep_set_option(name.encode(), int(value)))
 
 
 class BeepError(RuntimeError):
@@ -388,6 +400,10 @@ class DeviceBatch:
 
     def launches(self) -> int:
         return lib().beep_batch_launches(self.h)
+
+    def foi_path(self) -> int:
+        """1 = FP32 SIMT force of infection, 2 = tensor cores, 0 = plain form."""
+        return lib().beep_batch_foi_path(self.h)
 
     def close(self):
         if self.h:

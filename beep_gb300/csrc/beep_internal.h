@@ -41,6 +41,7 @@ struct ModelDev {
 	int32_t pop_obs;                     // some observation reads populations
 	int32_t dp_age_unique;               // each age has exactly one dp per strain
 	float inv_popsize_f;                 // 1 / Data::popsize
+	const unsigned char *tc_image;       // area mixing as BF16 pieces for the tensor-core FOI (foi_tc.cuh), or null
 };
 
 // One parameter set's tables: offsets into the batch's table pool (doubles /
@@ -95,6 +96,10 @@ struct BatchDev {
 	double *ch_mean;                    // [2][P][S][A][T][DP]
 	double *ch_Imap, *ch_Idiag;         // [2][P][S][NS][A][G]
 	double *Li;                         // [P] mode 2 output
+	// fast form: force of infection on the tensor cores (foi_tc.cuh); its shared
+	// memory starts at tc_smem_off bytes into the dynamic shared memory
+	int32_t foi_tc;
+	size_t tc_smem_off;
 };
 
 // launchers
@@ -103,6 +108,10 @@ int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream);    // s
 size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_stage, bool state_global, int tnrows,
                        bool pop_single);
 size_t fast_gstate_stride(const ModelDev &m);
+size_t fast_tc_smem_bytes(const ModelDev &m);   // shared memory of the tensor-core FOI
+int fast_pick_threads(const ModelDev &m);        // threads per CTA of the fast kernel for this model
+// library options (beep_set_option)
+int option_fast_foi();                           // 0 automatic, 1 FP32 SIMT, 2 tensor cores
 int fast_threads();
 
 }  // namespace beep

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <cmath>
 #include <cstring>
@@ -24,12 +25,14 @@
 #include <vector>
 
 #include "capi_internal.h"
+#include "foi_tc.cuh"
 
 using namespace beep;
 
 namespace beep {
 
 thread_local std::string g_err;
+std::atomic<int> g_fast_foi{0};
 
 beep_status fail(beep_status s, const std::string &msg)
 {
@@ -62,6 +65,17 @@ extern "C" {
 int32_t beep_abi_version(void) { return BEEP_GPU_ABI_VERSION; }
 
 const char *beep_last_error(void) { return g_err.c_str(); }
+
+beep_status beep_set_option(const char *name, int64_t value)
+{
+	if (!name) return fail(BEEP_BAD_INPUT, "null option name");
+	if (std::string(name) == "fast_foi") {
+		if (value < 0 || value > 2) return fail(BEEP_BAD_INPUT, "fast_foi must be 0, 1 or 2");
+		g_fast_foi.store((int)value);
+		return BEEP_OK;
+	}
+	return fail(BEEP_BAD_INPUT, std::string("unknown option ") + name);
+}
 
 beep_status beep_device_init(int32_t device)
 {
@@ -164,6 +178,41 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 		for (int j = d->M_rowptr[c]; j < d->M_rowptr[c + 1]; j++) Mdense[(size_t)c * A + d->M_to[j]] += (float)d->M_val[j];
 	}
 	for (int j = 0; j < nnz; j++) csc_val_f[j] = (float)csc_val[j];
+	// the tensor-core FOI's image of the off-diagonal matrix: per (target chunk,
+	// source chunk) three BF16 pieces hi + mid + lo of M[c][t], K-major (foi_tc.cuh)
+	std::vector<unsigned char> tc_img;
+	if (A >= 64 && tc::supported(A, NS)) {
+		const tc::Geom g = tc::geometry(A, NS);
+		tc_img.assign(g.image_bytes(), 0);
+		auto bf16 = [](float x) {   // round to nearest even; the inputs are finite
+			uint32_t u;
+			memcpy(&u, &x, 4);
+			return (uint16_t)((u + 0x7FFFu + ((u >> 16) & 1u)) >> 16);
+		};
+		auto f32 = [](uint16_t h) {
+			uint32_t u = (uint32_t)h << 16;
+			float x;
+			memcpy(&x, &u, 4);
+			return x;
+		};
+		for (int ct = 0; ct < g.nct; ct++)
+			for (int kc = 0; kc < g.nkc; kc++) {
+				unsigned char *ch = tc_img.data() + (size_t)(ct * g.nkc + kc) * g.chunk_bytes();
+				for (int n = 0; n < g.tw; n++)
+					for (int kl = 0; kl < tc::kChunkK; kl++) {
+						const int t = ct * g.tw + n, c = kc * tc::kChunkK + kl;
+						const float x = (t < A && c < A) ? Mdense[(size_t)c * A + t] : 0.f;
+						const uint16_t h = bf16(x);
+						const float r1 = x - f32(h);
+						const uint16_t mid = bf16(r1);
+						const uint16_t lo = bf16(r1 - f32(mid));
+						const uint32_t o = tc::kmajor_offset(n, kl, g.tw);
+						memcpy(ch + o, &h, 2);
+						memcpy(ch + g.piece_bytes() + o, &mid, 2);
+						memcpy(ch + 2 * g.piece_bytes() + o, &lo, 2);
+					}
+			}
+	}
 	std::vector<float2> obs_np(nobs > 0 ? nobs : 1);
 	std::vector<float> obs_value_f(nobs > 0 ? nobs : 1), obs_factor_f(nobs > 0 ? nobs : 1), obs_shape_f(nobs > 0 ? nobs : 1);
 	std::vector<int32_t> obs_cells_f(ncells > 0 ? ncells : 1), obs_cells_full(ncells > 0 ? ncells : 1);
@@ -225,7 +274,7 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	       o_ofa = L.add(8 * (size_t)nobs), o_md = L.add(4 * (size_t)A * A), o_mdg = L.add(4 * (size_t)A),
 	       o_mfc = L.add(4 * (size_t)A), o_cvf = L.add(4 * (size_t)nnz), o_onp = L.add(8 * (size_t)nobs),
 	       o_ovf = L.add(4 * (size_t)nobs), o_off = L.add(4 * (size_t)nobs), o_oshf = L.add(4 * (size_t)nobs),
-	       o_ocf = L.add(4 * (size_t)ncells), o_ocfull = L.add(4 * (size_t)ncells);
+	       o_ocf = L.add(4 * (size_t)ncells), o_ocfull = L.add(4 * (size_t)ncells), o_tc = L.add(tc_img.size());
 	std::vector<char> host(L.size);
 	auto put = [&](size_t off, const void *src, size_t n) { if (n) memcpy(host.data() + off, src, n); };
 	put(o_tf, d->trans_from, 4 * T); put(o_tt, d->trans_to, 4 * T); put(o_age, d->democatpos_age, 4 * DPS);
@@ -248,6 +297,7 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	if (nobs > 0) put(o_oshf, obs_shape_f.data(), 4 * (size_t)nobs);
 	if (ncells > 0) put(o_ocf, obs_cells_f.data(), 4 * (size_t)ncells);
 	if (ncells > 0) put(o_ocfull, obs_cells_full.data(), 4 * (size_t)ncells);
+	put(o_tc, tc_img.data(), tc_img.size());
 	cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
 	if (e == cudaSuccess) e = m->model_mem.reserve(L.size);
 	if (e == cudaSuccess) e = cudaMemcpy(m->model_mem.ptr, host.data(), L.size, cudaMemcpyHostToDevice);
@@ -280,6 +330,7 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	md.obs_shape_f = (const float *)(base + o_oshf);
 	md.obs_cells_f = (const int32_t *)(base + o_ocf);
 	md.obs_cells_full = (const int32_t *)(base + o_ocfull);
+	md.tc_image = tc_img.empty() ? nullptr : (const unsigned char *)(base + o_tc);
 	for (int tr = 0; tr < 16; tr++) md.tn_row[tr] = tn_row[tr];
 	md.tn_rows = tn_rows;
 	md.pop_obs = pop_obs;
@@ -564,6 +615,22 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 			return fail(BEEP_BAD_INPUT, "model too large for the fast form (observation slots or tables exceed shared memory, or more than 8 transitions)");
 		}
 		q->bd.m_in_smem = fast_smem_bytes(m->dev, nslots, true, q->bd.nefoi_stage, q->state_global, tnrows, ps) <= limit ? 1 : 0;
+		// force of infection on the tensor cores: large models (the matrix is streamed from
+		// L2 each step; the particle's populations and counts move to global memory to make
+		// room for the operand ring)
+		const int opt = option_fast_foi();
+		const bool can_tc = m->dev.tc_image != nullptr && fast_pick_threads(m->dev) == 640;
+		const bool want_tc = opt == 2 || (opt == 0 && m->A >= 300);
+		if (can_tc && want_tc) {
+			const size_t base = fast_smem_bytes(m->dev, nslots, false, q->bd.nefoi_stage, true, tnrows, ps);
+			const size_t off = (base + 127) & ~(size_t)127;
+			if (off + fast_tc_smem_bytes(m->dev) <= limit) {
+				q->bd.foi_tc = 1;
+				q->bd.tc_smem_off = off;
+				q->state_global = true;
+				q->bd.m_in_smem = 0;
+			}
+		}
 	}
 	auto bail = [&](beep_status s) { beep_batch_destroy(q); return s; };
 	st = stage_inputs(q);
@@ -695,6 +762,12 @@ beep_status beep_batch_time(beep_batch *q, int32_t iters, double *ms_per_launch)
 
 int32_t beep_batch_launches(const beep_batch *q) { return q ? 1 : 0; }
 
+int32_t beep_batch_foi_path(const beep_batch *q)
+{
+	if (!q || q->b.form != BEEP_FORM_FAST) return 0;
+	return q->bd.foi_tc ? 2 : 1;
+}
+
 beep_status beep_batch_bytes(const beep_batch *q, int64_t *h2d, int64_t *d2h)
 {
 	if (!q || !h2d || !d2h) return fail(BEEP_BAD_INPUT, "null argument");
@@ -742,3 +815,5 @@ size_t beep::batch_device_bytes(const beep_batch *q)
 {
 	return q ? q->in_dev.cap + q->work_dev.cap + q->out_dev.cap : 0;
 }
+
+int beep::option_fast_foi() { return g_fast_foi.load(); }

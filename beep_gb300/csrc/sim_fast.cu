@@ -23,6 +23,7 @@
 //   3 per column (c, dp): NMI, means, draws -> tn          (get_NMI, set_transmean, draws)
 //   4 observation gathers of the step                     (get_obs_value_section)
 //   5 population update; completed observations -> log-density
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -30,6 +31,7 @@
 
 #include "beep_internal.h"
 #include "rng_fp64.cuh"
+#include "foi_tc.cuh"
 
 namespace beep {
 namespace {
@@ -283,6 +285,73 @@ __device__ __forceinline__ void foi(const ModelDev &m, const float *Ms, int lda,
 	}
 }
 
+// Force of infection on the tensor cores (foi_tc.cuh) for one step, in two
+// halves so that the CTA's other warps work while the tensor cores run:
+//   foi_tensor_issue   every thread: counts Icnt [NS][A][MG] -> stacked BF16
+//                      pieces; then thread 0 streams the matrix chunks and
+//                      issues the MMAs (warp 0 is busy until it returns);
+//   foi_tensor_collect every thread: waits for the MMAs, thread 0 issues the
+//                      next step's first loads (with `more`), and the
+//                      accumulators are read back into Imap [NS][A][MG] (hi
+//                      rows written, a barrier, lo rows added).
+// Both return false (for every thread, after collect) if a wait gave up.
+template <int NT, int MG>
+__device__ void foi_tensor_issue(tc::Foi &f, uint32_t taddr, uint32_t step_no, const float *Icnt, int tid,
+                                 int *abort_flag)
+{
+	const tc::Geom &g = f.g;
+	const int A = g.A, NS = g.NS, kp = g.kpad(), R = g.arows();
+	for (int idx = tid; idx < NS * kp * 16; idx += NT) {
+		const int a = idx & 15, c = (idx >> 4) % kp, st = idx / (16 * kp);
+		const float v = (c < A && a < MG) ? Icnt[(st * A + c) * MG + a] : 0.f;
+		const __nv_bfloat16 h = __float2bfloat16_rn(v);
+		const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
+		*(__nv_bfloat16 *)(f.a + tc::kmajor_offset(st * 32 + a, c, R)) = h;
+		*(__nv_bfloat16 *)(f.a + tc::kmajor_offset(st * 32 + 16 + a, c, R)) = l;
+	}
+	tc::fence_async_smem();
+	__syncthreads();
+	if (tid == 0) {
+		if (!tc::issue_step(f, taddr, step_no)) {
+			atomicExch(abort_flag, 1);
+			tc::drain(f);
+		}
+	}
+}
+
+template <int NT, int MG>
+__device__ bool foi_tensor_collect(tc::Foi &f, uint32_t taddr, uint32_t step_no, bool more, float *Imap, int tid,
+                                   int *abort_flag)
+{
+	const tc::Geom &g = f.g;
+	const int A = g.A, NS = g.NS;
+	__syncwarp();
+	if (!tc::mbar_wait(f.done, step_no & 1u)) atomicExch(abort_flag, 1);
+	tc::tc_after_sync();
+	__syncwarp();
+	if (tid == 0 && more && !*(volatile int *)abort_flag) tc::prefetch(f, step_no + 1);
+	// rows of warp quarter qd: r = qd*16 + lane (lane < 16) = strain qd/2, piece qd%2, age lane
+	const int warp = tid >> 5, lane = tid & 31, qd = warp & 3, st = qd >> 1;
+	const int ngroups = (g.nct * g.tw + 15) >> 4;
+	for (int pass = 0; pass < 2; pass++) {
+		if ((qd & 1) == pass && st < NS) {
+			for (int gi = warp >> 2; gi < ngroups; gi += NT / 128) {
+				float v[16];
+				tc::tmem_ld16(taddr + ((uint32_t)(qd * 32) << 16) + (uint32_t)(gi * 16), v);
+				if (lane < MG) {
+					float *y = Imap + (st * A + gi * 16) * MG + lane;
+#pragma unroll
+					for (int i = 0; i < 16; i++)
+						if (gi * 16 + i < A) y[i * MG] = pass ? y[i * MG] + v[i] : v[i];
+				}
+			}
+		}
+		__syncthreads();
+	}
+	tc::tc_before_sync();
+	return !*(volatile int *)abort_flag;
+}
+
 struct Tabs {
 	const float *rate, *sus, *inf, *beta_rows, *areafactor, *Ntime, *geo, *efoi_spline, *efoi_age, *obs_spline;
 	const int32_t *beta_row_of, *efoi_ref;
@@ -321,7 +390,7 @@ __device__ __forceinline__ void slice_store(const ModelDev &m, FastSmem &s, cons
 	if (tid == 0) s.dgeo[buf] = r.d;
 }
 
-template <int NT, int MG>
+template <int NT, int MG, bool TC>
 __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const BatchDev b)
 {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -392,6 +461,38 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 		s.dgeo = (float *)take(4 * 2);
 		s.red = (float *)take(4 * 2 * (size_t)NT);
 	}
+	// tensor-core FOI (large models, 640 threads): chunk ring, stacked counts, barriers, tensor memory
+	__shared__ uint64_t tc_bars[2 * tc::kStages + 1];
+	__shared__ uint32_t tc_slot;
+	__shared__ int tc_abort;
+	tc::Foi tf;
+	constexpr bool use_tc = TC;   // tensor-core FOI (instantiated for 640 threads only)
+	uint32_t taddr = 0, tcols = 0;
+	if (use_tc) {
+		size_t off = b.tc_smem_off;
+		tf.g = tc::geometry(A, NS);
+		tf.stage0 = smem_raw + off;
+		tf.stage_stride = (tf.g.chunk_bytes() + 127) & ~(uint32_t)127;
+		tf.a = smem_raw + off + (size_t)tc::kStages * tf.stage_stride;
+		tf.full = tc_bars; tf.empty = tc_bars + tc::kStages; tf.done = tc_bars + 2 * tc::kStages;
+		tf.image = m.tc_image;
+		tf.pending = 0; tf.pend_par = 0;
+		tcols = tf.g.tmem_cols();
+		if ((tid >> 5) == 0) tc::tmem_alloc(&tc_slot, tcols);
+		if (tid == 0) {
+			tc_abort = 0;
+			for (int k = 0; k < tc::kStages; k++) { tc::mbar_init(&tf.full[k], 1); tc::mbar_init(&tf.empty[k], 1); }
+			tc::mbar_init(tf.done, 1);
+			tc::fence_mbar_init();
+		}
+		for (uint32_t k = tid; k < tf.g.a_bytes() / 4; k += NT) ((uint32_t *)tf.a)[k] = 0u;
+		tc::tc_before_sync();
+		__syncthreads();
+		tc::tc_after_sync();
+		taddr = tc_slot;
+		if (tid == 0) tc::prefetch(tf, 0);
+	}
+	uint32_t tc_step = 0;
 	if (s.Ms)
 		for (int k = tid; k < A * A; k += NT) s.Ms[(k / A) * lda + k % A] = m.Mdense[k];
 	for (int k = tid; k < popsz; k += NT) {
@@ -429,7 +530,14 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 	}
 	slice_store<NT>(m, s, slice_load<NT>(m, tb, s, b.ti, tid), 0, tid);
 	__syncthreads();
-	foi<NT, MG>(m, s.Ms, lda, s.Ic0, s.Imap, tid);
+	bool tc_ok = true;
+	if (use_tc) {
+		foi_tensor_issue<NT, MG>(tf, taddr, tc_step, s.Ic0, tid, &tc_abort);
+		tc_ok = foi_tensor_collect<NT, MG>(tf, taddr, tc_step, nsteps > 1, s.Imap, tid, &tc_abort);
+		tc_step++;
+	} else {
+		foi<NT, MG>(m, s.Ms, lda, s.Ic0, s.Imap, tid);
+	}
 	float Lsum = 0.f, Lcmp = 0.f;           // compensated per-thread log-likelihood
 	__syncthreads();
 
@@ -438,7 +546,7 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 	const float dt = (float)m.dt;
 	bool cur = false;
 	int sb = 0;                                          // slice buffer of the step simulated
-	for (int sett = b.ti; sett < b.tf; sett++) {
+	for (int sett = b.ti; sett < b.tf && tc_ok; sett++) {
 		int32_t *pc = cur ? s.pop1 : s.pop0, *pn = cur ? s.pop0 : s.pop1;
 		const SliceRegs nxt = sett + 1 < b.tf ? slice_load<NT>(m, tb, s, sett + 1, tid) : SliceRegs{0.f, 0.f, 0.f, 0.f};
 		const float *be = sb ? s.be1 : s.be0, *et = sb ? s.et1 : s.et0, *Nm = sb ? s.N1 : s.N0;
@@ -543,8 +651,12 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 				const int dp = k % DP, tr = (k / DP) % T, c = k / (DP * T);
 				b.tn_traj[((size_t)p * nsteps + (sett - b.ti)) * tnsz + k] = s.tn[tr * ncol + c * DP + dp];
 			}
+		const bool tc_now = use_tc && sett + 1 < b.tf;
+		if (tc_now) foi_tensor_issue<NT, MG>(tf, taddr, tc_step, Ic_nxt, tid, &tc_abort);
+		// with the tensor cores busy for warp 0, warps 1.. take the observations
+		const int ow = tc_now ? 32 : 0;
 		const int a0 = b.step_ptr[sett - b.ti], a1 = b.step_ptr[sett - b.ti + 1];
-		for (int k = a0 + tid; k < a1; k += NT) {
+		for (int k = a0 + tid - ow; tid >= ow && k < a1; k += NT - ow) {
 			const int4 t0 = __ldg(b.tasks + 2 * k), t1 = __ldg(b.tasks + 2 * k + 1);
 			const float fac = __int_as_float(t1.x);
 			const int spl = t1.y;
@@ -571,12 +683,31 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 		}
 		if (!m.dp_age_unique)
 			for (int k = tid; k < agsz; k += NT) (cur ? s.Ic1 : s.Ic0)[k] = 0.f;   // next step's accumulation target
-		foi<NT, MG>(m, s.Ms, lda, Ic_nxt, s.Imap, tid);
+		if (use_tc) {
+			if (tc_now) {
+				tc_ok = foi_tensor_collect<NT, MG>(tf, taddr, tc_step, sett + 2 < b.tf, s.Imap, tid, &tc_abort);
+				tc_step++;
+			}
+		} else {
+			foi<NT, MG>(m, s.Ms, lda, Ic_nxt, s.Imap, tid);
+		}
 		__syncthreads();
 		cur = !cur;
 		sb ^= 1;
 	}
 
+	if (use_tc) {
+		if (tid == 0) {
+			tc::drain(tf);                             // loads still in flight (only after a timeout)
+			if (!tc_ok) atomicCAS(status, 0, BEEP_TIMEOUT);
+		}
+		tc::tc_before_sync();
+		__syncthreads();
+		if ((tid >> 5) == 0) {
+			tc::tc_after_sync();
+			tc::tmem_dealloc(taddr, tcols);
+		}
+	}
 	if (b.pop_out) {
 		const int32_t *pf = cur ? s.pop1 : s.pop0;
 		for (int k = tid; k < popsz; k += NT) {
@@ -623,6 +754,14 @@ size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_
 
 int fast_threads() { return kFastThreads; }
 
+int fast_pick_threads(const ModelDev &m) { return pick_threads(m); }
+
+size_t fast_tc_smem_bytes(const ModelDev &m)
+{
+	const tc::Geom g = tc::geometry(m.A, m.NS);
+	return (size_t)tc::kStages * ((g.chunk_bytes() + 127) & ~(size_t)127) + g.a_bytes();
+}
+
 size_t fast_gstate_stride(const ModelDev &m)
 {
 	auto r = [](size_t x) { return (x + 255) & ~(size_t)255; };
@@ -630,12 +769,12 @@ size_t fast_gstate_stride(const ModelDev &m)
 	return 2 * r(4 * m.C * ncol) + r(4 * m.T * ncol);   // upper bound for any row/buffer choice
 }
 
-template <int NT>
+template <int NT, bool TC>
 static int launch_nt(const ModelDev &m, const BatchDev &b, size_t smem, cudaStream_t st)
 {
 	// MG: the age count rounded up to a multiple of 4 (the stride of the infectious counts)
-	auto kern = m.G <= 4 ? sim_fast_kernel<NT, 4> : m.G <= 8 ? sim_fast_kernel<NT, 8>
-	          : m.G <= 12 ? sim_fast_kernel<NT, 12> : sim_fast_kernel<NT, 16>;
+	auto kern = m.G <= 4 ? sim_fast_kernel<NT, 4, TC> : m.G <= 8 ? sim_fast_kernel<NT, 8, TC>
+	          : m.G <= 12 ? sim_fast_kernel<NT, 12, TC> : sim_fast_kernel<NT, 16, TC>;
 	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	if (e != cudaSuccess) return (int)e;
 	kern<<<b.P, NT, smem, st>>>(m, b);
@@ -646,8 +785,12 @@ int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream)
 {
 	if (b.P == 0) return 0;
 	if (m.G > 16 || m.T > kMaxT) return (int)cudaErrorInvalidValue;
-	const size_t smem = fast_smem_bytes(m, b.nslots, b.m_in_smem != 0, b.nefoi_stage, b.gstate != nullptr,
-	                                    b.tn_full ? m.T : m.tn_rows, b.pop_single != 0);
+	size_t smem = fast_smem_bytes(m, b.nslots, b.m_in_smem != 0, b.nefoi_stage, b.gstate != nullptr,
+	                              b.tn_full ? m.T : m.tn_rows, b.pop_single != 0);
+	if (b.foi_tc) {
+		if (!m.tc_image || pick_threads(m) != 640 || b.tc_smem_off < smem) return (int)cudaErrorInvalidValue;
+		smem = b.tc_smem_off + fast_tc_smem_bytes(m);
+	}
 	const int nt = pick_threads(m);
 	const int NSA = m.NS * m.A;
 	if (NSA > nt || m.G * m.G > nt) return (int)cudaErrorInvalidValue;   // slices: one item per thread
@@ -660,8 +803,9 @@ int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream)
 		init = true;
 	}
 	cudaStream_t st = (cudaStream_t)stream;
-	return nt == 128 ? launch_nt<128>(m, b, smem, st) : nt == 256 ? launch_nt<256>(m, b, smem, st)
-	                                                               : launch_nt<640>(m, b, smem, st);
+	if (b.foi_tc) return launch_nt<640, true>(m, b, smem, st);
+	return nt == 128 ? launch_nt<128, false>(m, b, smem, st) : nt == 256 ? launch_nt<256, false>(m, b, smem, st)
+	                                                                     : launch_nt<640, false>(m, b, smem, st);
 }
 
 }  // namespace beep

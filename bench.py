@@ -327,6 +327,7 @@ def workload_config(kind, m, P, note=None):
 def run_ours(args, rank, ws, dist):
     from beep_gb300 import build as bbuild, capi
     bbuild.build()
+    capi.set_option("fast_foi", {"auto": capi.FOI_AUTO, "simt": capi.FOI_SIMT, "tensor": capi.FOI_TENSOR}[args.foi])
     P = args.particles or WORKLOADS[args.workload]["particles"]
     seed = args.seed + 7919 * rank
     w, m, tabs, group_of = build_workload(args.workload, P, seed)
@@ -401,6 +402,7 @@ def run_ours(args, rank, ws, dist):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.form == "fast" else "f64",
         "data": "synthetic", "config": workload_config(args.workload, m, P),
         "form": args.form,
+        "foi": {0: None, 1: "fp32-simt", 2: "tensor-core split-bf16"}[db.foi_path()],
         "plain_fp64": plain,
         "loglik_evals_per_s": P * ws / t_dev,
         "clocks": clocks,
@@ -430,6 +432,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--form", default="fast", choices=["fast", "plain"])
+    ap.add_argument("--foi", default="auto", choices=["auto", "simt", "tensor"],
+                    help="force of infection of the fast form (library option fast_foi)")
     ap.add_argument("--plain-particles", type=int, default=1024)
     ap.add_argument("--plain-steps", type=int, default=0, help="time the plain form over this many steps (0: all)")
     ap.add_argument("--serve-requests", type=int, default=32,

@@ -199,6 +199,9 @@ BEEP_API int32_t beep_batch_launches(const beep_batch *batch);   /* kernels per 
 /* bytes moved host->device by beep_batch_upload and device->host by beep_batch_download */
 BEEP_API beep_status beep_batch_bytes(const beep_batch *batch, int64_t *h2d, int64_t *d2h);
 BEEP_API beep_status beep_batch_destroy(beep_batch *batch);
+/* Force-of-infection path the fast form of this batch runs: 1 = FP32 SIMT,
+ * 2 = tensor cores; 0 for the plain form. */
+BEEP_API int32_t beep_batch_foi_path(const beep_batch *batch);
 
 /* Bootstrap particle filter of PMCMC (PMCMC::obs_prob + bootstrap,
  * src/pmcmc.cc:180-268; ancestor swap Mpi::end_sec_swap, src/mpi.cc:215-327)
@@ -240,6 +243,15 @@ BEEP_API beep_status beep_abcsmc_weights(int32_t nvar, int32_t nnew, const doubl
                                          const double *logprior_new, int32_t nlast, const double *theta_last,
                                          const double *w_last, const double *inv_cov, double size,
                                          int32_t normalise, double *w_out);
+
+/* Library options (process-wide; no counterpart in the reference):
+ *   "fast_foi"  force of infection of the fast form: 0 = automatic (tensor
+ *               cores for models of 300 to 512 areas with one or two strains,
+ *               FP32 SIMT otherwise), 1 = FP32 SIMT, 2 = tensor cores wherever
+ *               supported (64 to 512 areas, one or two strains, more than 256
+ *               area x group columns).
+ * Unknown names or values give BEEP_BAD_INPUT. */
+BEEP_API beep_status beep_set_option(const char *name, int64_t value);
 
 /* ---- MBP chains: model-based proposals (Mbp, src/mbp.cc) -----------------
  * A chain set keeps, for each chain, two full trajectory states on the

@@ -5,6 +5,8 @@ import glob
 import os
 import re
 
+import pytest
+
 from beep_gb300 import build, capi
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -51,3 +53,13 @@ int main(void){printf("%zu %zu %zu %zu %zu\n", sizeof(beep_model_desc), sizeof(b
     got = [ctypes.sizeof(capi.ModelDesc), ctypes.sizeof(capi.ParamTables), ctypes.sizeof(capi.SimBatch),
            capi.ModelDesc.obs_cells.offset, capi.SimBatch.form.offset]
     assert [int(x) for x in out] == got
+
+
+def test_set_option_validates_names_and_values():
+    from beep_gb300 import capi
+    capi.set_option("fast_foi", capi.FOI_SIMT)
+    capi.set_option("fast_foi", capi.FOI_AUTO)
+    with pytest.raises(capi.BeepError):
+        capi.set_option("fast_foi", 7)
+    with pytest.raises(capi.BeepError):
+        capi.set_option("no_such_option", 1)

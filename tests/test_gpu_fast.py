@@ -101,3 +101,58 @@ def test_fast_large_model_keeps_state_in_global_memory(built):
     assert same.mean() >= 0.5, same.mean()
     np.testing.assert_allclose(f.L[same], g.L[same], rtol=L_RTOL_FAST)
     dm.close()
+
+
+@pytest.fixture
+def foi_option(built):
+    yield capi.set_option
+    capi.set_option("fast_foi", capi.FOI_AUTO)
+
+
+def test_tensor_core_foi_follows_fp64(foi_option):
+    """The force of infection on the tensor cores (split BF16, FP32 accumulation)
+    and the FP32 SIMT contraction both keep the fast form on the FP64
+    trajectories of a 100-area x 3-age model."""
+    from beep_gb300 import model_builder as mb, synth
+    w = synth.seir_hd_small(seed=20260201, narea=100, nage=3, days=60, name="mid")
+    m = capi.Model(mb.model_arrays(w))
+    t = capi.Tables(mb.param_tables(w))
+    dm = capi.DeviceModel(m)
+    P = 48
+    g = dm.simulate(capi.Batch(m, [t], P, 9, want_transnum=True, want_pop=True))
+    res = {}
+    for mode in (capi.FOI_SIMT, capi.FOI_TENSOR):
+        foi_option("fast_foi", mode)
+        db = capi.DeviceBatch(dm, capi.Batch(m, [t], P, 9, want_transnum=True, want_pop=True, form=capi.FORM_FAST))
+        assert db.foi_path() == mode
+        f = db.run()
+        db.close()
+        same = np.array([np.array_equal(f.transnum[p], g.transnum[p]) for p in range(P)])
+        assert same.mean() >= 0.6, (mode, same.mean())
+        np.testing.assert_allclose(f.L[same], g.L[same], rtol=L_RTOL_FAST)
+        res[mode] = f
+    both = np.array([np.array_equal(res[1].transnum[p], res[2].transnum[p]) for p in range(P)])
+    assert both.mean() >= 0.6, both.mean()
+    dm.close()
+
+
+def test_tensor_core_foi_distribution_matches_oracle(foi_option):
+    stats = pytest.importorskip("scipy.stats")
+    from beep_gb300 import model_builder as mb, synth
+    w = synth.seir_hd_small(seed=20260202, narea=90, nage=4, days=50, name="mid2")
+    m = capi.Model(mb.model_arrays(w))
+    t = capi.Tables(mb.param_tables(w))
+    foi_option("fast_foi", capi.FOI_TENSOR)
+    dm = capi.DeviceModel(m)
+    P = 300
+    db = capi.DeviceBatch(dm, capi.Batch(m, [t], P, 77, stream_of=np.arange(P) + 5 * 10 ** 5, want_pop=True,
+                                         form=capi.FORM_FAST))
+    assert db.foi_path() == capi.FOI_TENSOR
+    f = db.run()
+    db.close()
+    o = oracle_simulate(m, capi.Batch(m, [t], P, 78, want_pop=True))
+    fs_f = f.pop[:, :, 4:6, :].sum(axis=(1, 2, 3))
+    fs_o = o.pop[:, :, 4:6, :].sum(axis=(1, 2, 3))
+    assert stats.ks_2samp(fs_f, fs_o).pvalue > 1e-3
+    assert stats.ks_2samp(f.L, o.L).pvalue > 1e-3
+    dm.close()
