@@ -71,6 +71,7 @@ struct BatchDev {
 	int32_t nslots, m_in_smem, nefoi_stage;
 	int32_t tn_full, pop_single;        // fast form: store every transition row / one population buffer
 	void *gstate;                       // fast form, large models: per-particle state in global memory (or null)
+	int32_t tn_smem;                    // with gstate: the transition counts stay in shared memory
 	size_t gstate_stride;               // bytes per particle   // nefoi_stage: efoi age tables staged in shared memory (0 = read from L2)
 	const int4 *tasks;                  // [2 * step_ptr[tf-ti]] per (step, active observation):
 	                                    // {slot, obs, first cell, ncell | last<<31}, {factor bits, spline, cell offset, 0}
@@ -106,7 +107,7 @@ struct BatchDev {
 int launch_sim_plain(const ModelDev &m, const BatchDev &b, void *stream);   // sim_plain.cu
 int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream);    // sim_fast.cu
 size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_stage, bool state_global, int tnrows,
-                       bool pop_single);
+                       bool pop_single, bool tn_smem = false);
 size_t fast_gstate_stride(const ModelDev &m);
 size_t fast_tc_smem_bytes(const ModelDev &m);   // shared memory of the tensor-core FOI
 int fast_pick_threads(const ModelDev &m);        // threads per CTA of the fast kernel for this model

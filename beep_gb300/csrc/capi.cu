@@ -622,13 +622,17 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 		const bool can_tc = m->dev.tc_image != nullptr && fast_pick_threads(m->dev) == 640;
 		const bool want_tc = opt == 2 || (opt == 0 && m->A >= 300);
 		if (can_tc && want_tc) {
-			const size_t base = fast_smem_bytes(m->dev, nslots, false, q->bd.nefoi_stage, true, tnrows, ps);
-			const size_t off = (base + 127) & ~(size_t)127;
-			if (off + fast_tc_smem_bytes(m->dev) <= limit) {
-				q->bd.foi_tc = 1;
-				q->bd.tc_smem_off = off;
-				q->state_global = true;
-				q->bd.m_in_smem = 0;
+			// the transition counts stay on chip when they fit beside the operand ring
+			for (int tn_on_chip = 1; tn_on_chip >= 0 && !q->bd.foi_tc; tn_on_chip--) {
+				const size_t base = fast_smem_bytes(m->dev, nslots, false, q->bd.nefoi_stage, true, tnrows, ps, tn_on_chip != 0);
+				const size_t off = (base + 127) & ~(size_t)127;
+				if (off + fast_tc_smem_bytes(m->dev) <= limit) {
+					q->bd.foi_tc = 1;
+					q->bd.tc_smem_off = off;
+					q->bd.tn_smem = tn_on_chip;
+					q->state_global = true;
+					q->bd.m_in_smem = 0;
+				}
 			}
 		}
 	}

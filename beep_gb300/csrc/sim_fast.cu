@@ -428,7 +428,7 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 			auto gtake = [&](size_t bytes) { unsigned char *q = g + go; go += (bytes + 255) & ~(size_t)255; return q; };
 			s.pop0 = (int32_t *)gtake(4 * (size_t)popsz);
 			s.pop1 = b.pop_single ? s.pop0 : (int32_t *)gtake(4 * (size_t)popsz);
-			s.tn = (int32_t *)gtake(4 * (size_t)tnrows * ncol);
+			s.tn = b.tn_smem ? (int32_t *)take(4 * (size_t)tnrows * ncol) : (int32_t *)gtake(4 * (size_t)tnrows * ncol);
 		} else {
 			s.pop0 = (int32_t *)take(4 * (size_t)popsz);
 			s.pop1 = b.pop_single ? s.pop0 : (int32_t *)take(4 * (size_t)popsz);
@@ -741,12 +741,13 @@ static int pick_threads(const ModelDev &m)
 }
 
 size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_stage, bool state_global,
-                       int tnrows, bool pop_single)
+                       int tnrows, bool pop_single, bool tn_smem)
 {
 	auto r = [](size_t x) { return (x + 15) & ~(size_t)15; };
 	const size_t A = m.A, G = m.G, DP = m.DP, NS = m.NS, C = m.C, T = m.T, DPS = m.DPS;
 	const size_t agsz = NS * A * (size_t)((m.G + 3) & ~3), ncol = A * DP;
-	return (m_in_smem ? r(4 * A * ms_lda(m.A)) : 0) + (state_global ? 0 : (pop_single ? 1 : 2) * r(4 * C * ncol) + r(4 * (size_t)tnrows * ncol)) + 3 * r(4 * agsz) +
+	return (m_in_smem ? r(4 * A * ms_lda(m.A)) : 0) + (state_global ? 0 : (pop_single ? 1 : 2) * r(4 * C * ncol)) +
+	       (state_global && !tn_smem ? 0 : r(4 * (size_t)tnrows * ncol)) + 3 * r(4 * agsz) +
 	       r(4 * (size_t)nslots) + 3 * r(4 * T) + r(4 * DPS) + r(4 * C) + r(4 * T * DP) + r(4 * DP) + r(4 * 64) +
 	       r(4 * 32) + 2 * r(4 * NS * A) + r(4 * (size_t)nefoi_stage * G) + 2 * (2 * r(4 * NS * A) + r(4 * G * G)) +
 	       r(8) + r(4 * 2 * (size_t)pick_threads(m));
@@ -786,7 +787,7 @@ int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream)
 	if (b.P == 0) return 0;
 	if (m.G > 16 || m.T > kMaxT) return (int)cudaErrorInvalidValue;
 	size_t smem = fast_smem_bytes(m, b.nslots, b.m_in_smem != 0, b.nefoi_stage, b.gstate != nullptr,
-	                              b.tn_full ? m.T : m.tn_rows, b.pop_single != 0);
+	                              b.tn_full ? m.T : m.tn_rows, b.pop_single != 0, b.tn_smem != 0);
 	if (b.foi_tc) {
 		if (!m.tc_image || pick_threads(m) != 640 || b.tc_smem_off < smem) return (int)cudaErrorInvalidValue;
 		smem = b.tc_smem_off + fast_tc_smem_bytes(m);
