@@ -65,6 +65,7 @@ class PFRequest(C.Structure):
         ("resample_stream", C.c_uint32), ("invT", C.c_double), ("nsection", C.c_int32),
         ("section_ti", _i32p), ("section_tf", _i32p), ("form", C.c_int32),
         ("loglik_out", _f64p), ("loglik_section_out", _f64p), ("L_out", _f64p), ("ancestors_out", _i32p),
+        ("lineage_transnum_out", _i32p),
     ]
 
 
@@ -331,8 +332,9 @@ class DeviceModel:
         return batch
 
     def pf_loglik(self, tables: "Tables", N: int, seed: int, resample_stream: int, invT: float, sections,
-                  form: int = FORM_PLAIN_FP64):
-        """Bootstrap particle filter on the device: (estimate, per-section terms, L, ancestors)."""
+                  form: int = FORM_PLAIN_FP64, lineage: bool = False):
+        """Bootstrap particle filter on the device: (estimate, per-section terms, L, ancestors) and, with
+        lineage, the sampled particle's transition counts [S][A][T][DP] as a fifth element."""
         ti = np.array([a for a, _ in sections], np.int32)
         tf = np.array([b for _, b in sections], np.int32)
         ns = len(sections)
@@ -345,7 +347,12 @@ class DeviceModel:
         r.nsection, r.section_ti, r.section_tf, r.form = ns, _ptr(ti, C.c_int32), _ptr(tf, C.c_int32), form
         r.loglik_out, r.loglik_section_out = _ptr(ll, C.c_double), _ptr(lls, C.c_double)
         r.L_out, r.ancestors_out = _ptr(Lo, C.c_double), _ptr(anc, C.c_int32)
+        m = self.model
+        lin = np.zeros((m.ndivision, m.narea, m.ntrans, m.ndemocatpos), np.int32) if lineage else None
+        r.lineage_transnum_out = _ptr(lin, C.c_int32)
         check(lib().beep_pf_loglik(self.h, C.byref(r)))
+        if lineage:
+            return float(ll[0]), lls, Lo, anc, lin
         return float(ll[0]), lls, Lo, anc
 
     def close(self):

@@ -526,8 +526,12 @@ beep_status beep_batch_create(beep_model *m, const beep_sim_batch *b, beep_batch
 
 }  // extern "C"
 
-beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, bool device_io, beep_batch **out)
+beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, bool device_io, beep_batch **out,
+                                        bool device_traj)
 {
+	// a count trajectory is written: to the batch's output (transnum_out), or to a
+	// device buffer the caller sets in bd.tn_traj before each launch (device_traj)
+	const bool traj = b->transnum_out != nullptr || device_traj;
 	if (!m || !b || !out) return fail(BEEP_BAD_INPUT, "null argument");
 	*out = nullptr;
 	beep_status st = check_batch(m, b, device_io);
@@ -590,7 +594,7 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 				float fac = m->obs_factor_f_h[o];
 				int32_t fbits;
 				memcpy(&fbits, &fac, 4);
-				const std::vector<int32_t> &enc = b->transnum_out ? m->obs_cells_full_h : m->obs_cells_f_h;
+				const std::vector<int32_t> &enc = traj ? m->obs_cells_full_h : m->obs_cells_f_h;
 				t[0] = q->slot_of[pos]; t[1] = o; t[2] = nc > 0 ? enc[c0] : 0;
 				t[3] = (int32_t)((uint32_t)nc | (last ? 0x80000000u : 0u));
 				t[4] = fbits; t[5] = m->obs_spline[o]; t[6] = c0; t[7] = 0;
@@ -604,7 +608,7 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 		q->bd.nefoi_stage = nefoi * m->G <= 1024 ? nefoi : 0;
 		// counts of unobserved transitions are not stored unless a trajectory is requested; one
 		// population buffer suffices when no observation reads populations and strains do not mix
-		q->bd.tn_full = b->transnum_out ? 1 : 0;
+		q->bd.tn_full = traj ? 1 : 0;
 		q->bd.pop_single = (!m->dev.pop_obs && m->NS == 1 && !b->pop_traj_out) ? 1 : 0;
 		const int tnrows = q->bd.tn_full ? m->T : m->dev.tn_rows;
 		const bool ps = q->bd.pop_single != 0;
@@ -643,7 +647,7 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 	Layout wk;
 	const size_t PW = b->form == BEEP_FORM_FAST ? 0 : (size_t)P;   // the fast form keeps its state on chip
 	const size_t w_gs = wk.add(q->state_global ? fast_gstate_stride(m->dev) * (size_t)P : 0);
-	size_t w_pa = wk.add(4 * popsz * PW), w_pb = wk.add(4 * popsz * PW), w_tn = wk.add(b->transnum_out ? 0 : 4 * tnsz * PW),
+	size_t w_pa = wk.add(4 * popsz * PW), w_pb = wk.add(4 * popsz * PW), w_tn = wk.add(traj ? 0 : 4 * tnsz * PW),
 	       w_im = wk.add(8 * agsz * PW), w_id = wk.add(8 * agsz * PW), w_di = wk.add(8 * agsz * PW),
 	       w_nmi = wk.add(8 * agsz * PW), w_acc = wk.add(8 * (size_t)nscored * PW);
 	Layout ou;
@@ -666,7 +670,7 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 	bd.k0 = (uint32_t)b->seed; bd.k1 = (uint32_t)(b->seed >> 32);
 	bd.nscored = nscored;
 	bd.pop_a = (int32_t *)(dw + w_pa); bd.pop_b = (int32_t *)(dw + w_pb);
-	bd.tn = b->transnum_out ? nullptr : (int32_t *)(dw + w_tn);
+	bd.tn = traj ? nullptr : (int32_t *)(dw + w_tn);
 	bd.Imap = (double *)(dw + w_im); bd.Idiag = (double *)(dw + w_id); bd.dinf = (double *)(dw + w_di);
 	bd.NMI = (double *)(dw + w_nmi); bd.obs_acc = (double *)(dw + w_acc);
 	bd.gstate = q->state_global ? (void *)(dw + w_gs) : nullptr;

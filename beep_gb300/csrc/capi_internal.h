@@ -128,7 +128,11 @@ namespace beep {
 // beep_batch_create for internal callers whose start populations and outputs
 // live on the device (device_io: pop_in is not read from the host and the
 // caller sets bd.pop_in / bd.L / bd.pop_out before each launch).
-beep_status batch_create_internal(beep_model *m, const beep_sim_batch *b, bool device_io, beep_batch **out);
+// With device_traj the kernels write every step's transition counts to a
+// device buffer the caller sets in bd.tn_traj ([P][tf-ti][A][T][DP]) before
+// each launch.
+beep_status batch_create_internal(beep_model *m, const beep_sim_batch *b, bool device_io, beep_batch **out,
+                                  bool device_traj = false);
 // beep_batch_download in two halves: the device->host copy enqueued on the
 // model's stream, and (once that copy completed) the status check and the
 // copy into the caller's arrays.

@@ -12,6 +12,9 @@
 //      (a selected particle keeps its own slot, the other slots take the
 //      surplus selections last-in first-out);
 //   3. pf_gather copies each slot's population from its ancestor's.
+// With a lineage request every section also writes its slots' transition
+// counts, and the sampled particle's trajectory is assembled by walking the
+// ancestors back (Mpi::particle_sample, src/mpi.cc:331-389).
 // The cumulative sums and the placement are sequential in slot order, as in
 // the reference, so the ancestors match it exactly (the FP64 weights of the
 // plain form agree with the reference's to the last bits).
@@ -131,10 +134,13 @@ extern "C" BEEP_API beep_status beep_pf_loglik(beep_model *m, const beep_pf_requ
 		b.nparticle = N; b.ngroup = 1; b.groups = r->tables; b.seed = r->seed;
 		b.ti = r->section_ti[k]; b.tf = r->section_tf[k];
 		b.form = r->form;
-		beep_status s = batch_create_internal(m, &b, true, &q[k]);
+		beep_status s = batch_create_internal(m, &b, true, &q[k], r->lineage_transnum_out != nullptr);
 		if (s != BEEP_OK) { std::string e = beep_last_error(); cleanup(); return fail(s, e); }
 	}
+	const size_t tnsz = (size_t)m->A * m->T * m->DP;
+	const bool lineage = r->lineage_transnum_out != nullptr;
 	Layout L;
+	const size_t o_tn = L.add(lineage ? 4 * tnsz * (size_t)m->S * N : 0);
 	const size_t o_pa = L.add(4 * popsz * N), o_pb = L.add(4 * popsz * N), o_L = L.add(8 * (size_t)ns * N),
 	             o_w = L.add(8 * (size_t)N), o_ws = L.add(8 * (size_t)N), o_sel = L.add(4 * (size_t)N),
 	             o_bp = L.add(4 * (size_t)N), o_ex = L.add(4 * (size_t)N), o_ob = L.add(8 * (size_t)ns),
@@ -156,6 +162,8 @@ extern "C" BEEP_API beep_status beep_pf_loglik(beep_model *m, const beep_pf_requ
 		b->bd.pop_in = k > 0 ? popA : nullptr;
 		b->bd.pop_out = popB;
 		b->bd.L = Lall + (size_t)k * N;
+		// section k's counts of every slot: [slot][step - ti][cell] at N * ti cells in
+		if (lineage) b->bd.tn_traj = (int32_t *)(d + o_tn) + (size_t)N * r->section_ti[k] * tnsz;
 		if (beep_batch_launch(b) != BEEP_OK) { bail(BEEP_DEVICE_ERROR, beep_last_error()); break; }
 		pf_bootstrap<<<1, kBootThreads, 0, st>>>(Lall + (size_t)k * N, N, r->invT, (uint32_t)r->seed,
 		                                         (uint32_t)(r->seed >> 32), r->resample_stream, k,
@@ -187,6 +195,21 @@ extern "C" BEEP_API beep_status beep_pf_loglik(beep_model *m, const beep_pf_requ
 			if (ps[p] != 0) { bail((beep_status)ps[p], "section " + std::to_string(k) + " particle " + std::to_string(p)); break; }
 	}
 	if (status == BEEP_OK && bst != 0) bail((beep_status)bst, "resampling found no particle (non-finite weights)");
+	if (status == BEEP_OK && lineage) {
+		// Mpi::particle_sample: start from the particle the last resampling put in slot
+		// 0 and walk the ancestors back, copying each section from the slot its
+		// ancestor held then
+		std::vector<int32_t> a((size_t)ns * N);
+		e = cudaMemcpy(a.data(), anc, 4 * (size_t)ns * N, cudaMemcpyDeviceToHost);
+		int32_t pcur = a[(size_t)(ns - 1) * N + 0];
+		for (int k = ns - 1; k >= 0 && e == cudaSuccess; k--) {
+			const int ti = r->section_ti[k], nst = r->section_tf[k] - ti;
+			const int32_t *src = (int32_t *)(d + o_tn) + ((size_t)N * ti + (size_t)pcur * nst) * tnsz;
+			e = cudaMemcpy(r->lineage_transnum_out + (size_t)ti * tnsz, src, 4 * (size_t)nst * tnsz, cudaMemcpyDeviceToHost);
+			if (k > 0) pcur = a[(size_t)(k - 1) * N + pcur];
+		}
+		if (e != cudaSuccess) bail(BEEP_DEVICE_ERROR, std::string("lineage copy: ") + cudaGetErrorString(e));
+	}
 	cudaStreamSynchronize(st);
 	work.release();
 	cleanup();

@@ -226,6 +226,12 @@ typedef struct beep_pf_request {
 	double *loglik_section_out;               /* [nsection] or NULL */
 	double *L_out;                            /* [nsection][nparticle] or NULL */
 	int32_t *ancestors_out;                   /* [nsection][nparticle] or NULL */
+	/* the sampled lineage (Mpi::particle_sample, src/mpi.cc:331-389): the
+	 * transition counts [ndivision][narea][ntrans][ndemocatpos] of the particle
+	 * the last resampling put in slot 0, each section taken from the slot its
+	 * ancestor occupied then; NULL to skip (it keeps every slot's counts on the
+	 * device for the whole run) */
+	int32_t *lineage_transnum_out;
 } beep_pf_request;
 
 BEEP_API beep_status beep_pf_loglik(beep_model *model, const beep_pf_request *request);

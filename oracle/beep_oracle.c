@@ -721,11 +721,16 @@ int beep_oracle_mbp(const beep_model_desc *m, int32_t nchain, const beep_param_t
 int beep_oracle_pf(const beep_model_desc *m, const beep_param_tables *tab, int32_t N, uint64_t seed,
                    uint32_t resample_stream, double invT, int32_t form, int32_t nsec, const int32_t *sec_ti,
                    const int32_t *sec_tf, double *loglik, double *loglik_sec, double *L_out, int32_t *anc_out,
-                   int nthreads)
+                   int32_t *lineage_out, int nthreads)
 {
 	(void)form;
 	if (!m || !tab || N <= 0 || nsec <= 0) return BEEP_BAD_INPUT;
 	const size_t popsz = (size_t)m->narea * m->ncomp * m->ndemocatpos;
+	const size_t tnsz = (size_t)m->narea * m->ntrans * m->ndemocatpos;
+	/* every slot's counts of every section, [section start * N + slot * steps][cell] */
+	int32_t *tn_all = lineage_out ? malloc(sizeof(int32_t) * tnsz * (size_t)m->ndivision * N) : NULL;
+	int32_t *anc_all = lineage_out ? malloc(sizeof(int32_t) * (size_t)nsec * N) : NULL;
+	if (lineage_out && (!tn_all || !anc_all)) return BEEP_OOM;
 	int32_t *pops = malloc(sizeof(int32_t) * popsz * N), *pout = malloc(sizeof(int32_t) * popsz * N);
 	double *L = malloc(sizeof(double) * N), *w = malloc(sizeof(double) * N), *wsum = malloc(sizeof(double) * N);
 	int32_t *bp = malloc(sizeof(int32_t) * N), *extra = malloc(sizeof(int32_t) * N);
@@ -740,6 +745,7 @@ int beep_oracle_pf(const beep_model_desc *m, const beep_param_tables *tab, int32
 		b.ti = sec_ti[s]; b.tf = sec_tf[s];
 		b.pop_in = s > 0 ? pops : NULL;
 		b.L_out = L; b.pop_out = pout;
+		if (tn_all) b.transnum_out = tn_all + (size_t)N * sec_ti[s] * tnsz;
 		st = beep_oracle_simulate(m, &b, nthreads);
 		if (st != BEEP_OK) break;
 		if (L_out) memcpy(L_out + (size_t)s * N, L, sizeof(double) * N);
@@ -770,10 +776,22 @@ int beep_oracle_pf(const beep_model_desc *m, const beep_param_tables *tab, int32
 		for (int32_t p = 0; p < N && st == BEEP_OK; p++)
 			if (bp[p] == -1) bp[p] = extra[--ne];
 		if (anc_out) memcpy(anc_out + (size_t)s * N, bp, sizeof(int32_t) * N);
+		if (anc_all) memcpy(anc_all + (size_t)s * N, bp, sizeof(int32_t) * N);
 		/* Mpi::end_sec_swap: slot p continues from its ancestor's population */
 		for (int32_t p = 0; p < N; p++) memcpy(pops + (size_t)p * popsz, pout + (size_t)bp[p] * popsz, sizeof(int32_t) * popsz);
 	}
 	if (loglik) *loglik = obprob;
+	if (lineage_out && st == BEEP_OK) {
+		/* Mpi::particle_sample, src/mpi.cc:331-389 */
+		int32_t p = anc_all[(size_t)(nsec - 1) * N + 0];
+		for (int32_t k = nsec - 1; k >= 0; k--) {
+			const int32_t ti = sec_ti[k], nst = sec_tf[k] - ti;
+			memcpy(lineage_out + (size_t)ti * tnsz, tn_all + ((size_t)N * ti + (size_t)p * nst) * tnsz,
+			       sizeof(int32_t) * (size_t)nst * tnsz);
+			if (k > 0) p = anc_all[(size_t)(k - 1) * N + p];
+		}
+	}
+	free(tn_all); free(anc_all);
 	free(pops); free(pout); free(L); free(w); free(wsum); free(bp); free(extra);
 	return st;
 }

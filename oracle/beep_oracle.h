@@ -36,12 +36,13 @@ int beep_oracle_simulate(const beep_model_desc *m, const beep_sim_batch *b, int 
  * resample with the "selected particle keeps its own slot" placement; the j-th
  * resampling uniform of section s is word 0 of
  * Philox({j, s, resample_stream, RESAMPLE<<24}).  Outputs: the estimate, the
- * per-section terms, per-section L [nsec][N] and ancestors [nsec][N] (each may
- * be NULL). */
+ * per-section terms, per-section L [nsec][N], ancestors [nsec][N] and the
+ * sampled lineage's counts [S][A][T][DP] (Mpi::particle_sample, src/mpi.cc:331-389)
+ * (each may be NULL). */
 int beep_oracle_pf(const beep_model_desc *m, const beep_param_tables *tab, int32_t N, uint64_t seed,
                    uint32_t resample_stream, double invT, int32_t form, int32_t nsec, const int32_t *sec_ti,
                    const int32_t *sec_tf, double *loglik, double *loglik_sec, double *L_out, int32_t *anc_out,
-                   int nthreads);
+                   int32_t *lineage_out, int nthreads);
 
 /* Model-based proposals (Mbp::mbp, src/mbp.cc:252-330) for nchain chains.
  * Chain k: the initial state is State::simulate(theta_k) over [0, ndivision)

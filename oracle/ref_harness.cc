@@ -19,7 +19,8 @@
 // chains, each simulated at one parameter row and proposed at the next, with
 // binomial_sample (src/utils.cc:174-180) interposed like poisson_sample.
 //
-// usage: ref_harness out=FILE [npart=N] [ntraj=N] [seed=S] [pf=0|1] [theta=FILE] [mbp=N] -- <BEEP key=value...>
+// usage: ref_harness out=FILE [npart=N] [ntraj=N] [seed=S] [pf=0|1] [theta=FILE] [mbp=N] [sampledir=DIR]
+//                    -- <BEEP key=value...>
 
 #include <cmath>
 #include <cstdint>
@@ -517,6 +518,26 @@ int main(int argc, char **argv)
 				obprob += ob;
 				obp.push_back(ob);
 				for (int p2 = 0; p2 < NP; p2++) anc.push_back((int32_t)pm.backpart[sec + 1][p2]);
+			}
+			// the sampled lineage (Mpi::particle_sample, src/mpi.cc:331-389) and, when
+			// sampledir= is given, its sample files (Mpi::gather_samples -> State::save,
+			// src/mpi.cc:677-720, src/state.cc:709-739)
+			{
+				Particle part = mpi.particle_sample(0, pm.backpart, pm.particle, obsmodel);
+				std::vector<int32_t> lin;
+				for (unsigned s = 0; s < S; s++)
+					for (unsigned c = 0; c < A; c++)
+						for (unsigned tr = 0; tr < T; tr++)
+							for (unsigned dp = 0; dp < DP; dp++) lin.push_back((int32_t)part.transnum[s][c][tr][dp]);
+				B.i(gp + "pf.lineage_transnum", lin, {S, A, T, DP});
+				B.scalar_d(gp + "pf.lineage_EF", part.EF);
+				if (opt.count("sampledir")) {           // Mpi::gather_samples, src/mpi.cc:677-720
+					std::vector<ParamSample> psamp;
+					std::vector<Sample> opsamp;
+					std::vector<Particle> parts{part};
+					State st(details, data, model, obsmodel);
+					mpi.gather_samples(psamp, opsamp, parts, st, opt["sampledir"] + "/");
+				}
 			}
 			B.scalar_d(gp + "pf.obprob", obprob);
 			B.d(gp + "pf.obprob_section", obp);

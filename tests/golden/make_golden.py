@@ -33,8 +33,10 @@ from beep_gb300 import bundle, synth  # noqa: E402
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
 
 
-def run_harness(workdir, toml, out, npart, ntraj, seed, mode, pf=False, theta=None, pfn=0, mbp=0):
+def run_harness(workdir, toml, out, npart, ntraj, seed, mode, pf=False, theta=None, pfn=0, mbp=0, sampledir=None):
     cmd = [HARNESS, f"out={out}", f"npart={npart}", f"ntraj={ntraj}", f"seed={seed}", f"pf={1 if pf else 0}"]
+    if sampledir:
+        cmd.append(f"sampledir={sampledir}")
     if theta is not None:
         cmd.append(f"theta={theta}")
     if pfn:
@@ -114,7 +116,7 @@ def mbp_theta_rows(base, nchain, seed):
 
 
 def make_fixture(name, w: synth.Workload, npart, ntraj, seed, pf=False, theta_rows=None, keep_dir=None, pfn=0,
-                 mbp=0):
+                 mbp=0, samples=False):
     work = tempfile.mkdtemp(prefix=f"golden_{name}_")
     try:
         toml = synth.write_beep_inputs(w, work)
@@ -135,7 +137,14 @@ def make_fixture(name, w: synth.Workload, npart, ntraj, seed, pf=False, theta_ro
                 for row in mbp_theta_rows(base, mbp, w.seed):
                     f.write(",".join(repr(float(x)) for x in row) + "\n")
         out = os.path.join(HERE, f"{name}.bnd")
-        run_harness(work, toml, out, npart, ntraj, seed, mode, pf=pf, theta=theta, pfn=pfn, mbp=mbp)
+        sdir = os.path.join(work, "samples") if samples else None
+        if sdir:
+            os.makedirs(sdir)
+        run_harness(work, toml, out, npart, ntraj, seed, mode, pf=pf, theta=theta, pfn=pfn, mbp=mbp, sampledir=sdir)
+        if sdir:
+            # the reference's own sample files of the sampled lineage
+            for f in sorted(os.listdir(sdir)):
+                shutil.copy(os.path.join(sdir, f), os.path.join(HERE, f"{name}_{f}"))
         if keep_dir:
             shutil.copytree(work, os.path.join(keep_dir, name), dirs_exist_ok=True)
         print(f"{name}: {os.path.getsize(out) / 1e3:.0f} kB")
@@ -155,7 +164,7 @@ def main():
     make_fixture("tiny_sim", tiny, npart=8, ntraj=3, seed=0x1234567890ABCDEF)
     # particle-filter sections need period >= 10 x the largest observation step (src/details.cc:115)
     tiny70 = synth.seir_hd_small(seed=20260102, narea=3, nage=2, days=70, name="tiny70")
-    make_fixture("tiny_pf", tiny70, npart=6, ntraj=2, seed=0x0F1E2D3C4B5A6978, pf=True, pfn=32)
+    make_fixture("tiny_pf", tiny70, npart=6, ntraj=2, seed=0x0F1E2D3C4B5A6978, pf=True, pfn=32, samples=True)
     # one age group (the reference's nage == 1 branch of get_NMI, src/state.cc:555-560)
     one = synth.seir_hd_small(seed=20260101, narea=5, nage=1, days=30, name="oneage")
     make_fixture("oneage_sim", one, npart=6, ntraj=2, seed=77)

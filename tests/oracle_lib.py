@@ -34,7 +34,7 @@ def oracle_lib():
         L.beep_oracle_obs_prob.restype = C.c_double
         L.beep_oracle_pf.argtypes = [C.POINTER(capi.ModelDesc), C.POINTER(capi.ParamTables), C.c_int32, C.c_uint64,
                                      C.c_uint32, C.c_double, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
-                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         L.beep_oracle_pf.restype = C.c_int
         L.beep_oracle_abcsmc_weights.argtypes = [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
                                                  C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]
@@ -55,8 +55,9 @@ def oracle_simulate(model: capi.Model, batch: capi.Batch, nthreads: int = 0) -> 
 
 
 def oracle_pf(model: capi.Model, tables: capi.Tables, N: int, seed: int, resample_stream: int, invT: float,
-              sections, nthreads: int = 0):
-    """Bootstrap particle filter of the oracle: (estimate, per-section terms, L [nsec][N], ancestors [nsec][N])."""
+              sections, nthreads: int = 0, lineage: bool = False):
+    """Bootstrap particle filter of the oracle: (estimate, per-section terms, L [nsec][N], ancestors [nsec][N])
+    and, with lineage, the sampled lineage's counts [S][A][T][DP] as a fifth element."""
     import numpy as np
     ti = np.array([a for a, _ in sections], np.int32)
     tf = np.array([b for _, b in sections], np.int32)
@@ -65,11 +66,14 @@ def oracle_pf(model: capi.Model, tables: capi.Tables, N: int, seed: int, resampl
     lls = np.zeros(ns)
     L = np.zeros((ns, N))
     anc = np.zeros((ns, N), np.int32)
+    lin = np.zeros((model.ndivision, model.narea, model.ntrans, model.ndemocatpos), np.int32) if lineage else None
     st = oracle_lib().beep_oracle_pf(C.byref(model.desc), C.byref(tables.st), N, seed, resample_stream, invT, 0, ns,
                                      ti.ctypes.data, tf.ctypes.data, ll.ctypes.data, lls.ctypes.data, L.ctypes.data,
-                                     anc.ctypes.data, nthreads)
+                                     anc.ctypes.data, None if lin is None else lin.ctypes.data, nthreads)
     if st != 0:
         raise RuntimeError(f"oracle particle filter failed: {capi.STATUS.get(st, st)}")
+    if lineage:
+        return float(ll[0]), lls, L, anc, lin
     return float(ll[0]), lls, L, anc
 
 

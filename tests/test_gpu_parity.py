@@ -94,9 +94,10 @@ def test_particle_filter_matches_reference(built, name):
     b, m, tabs, seed = load(name)
     N = b["g0.pf.ancestors"].shape[1]
     dm = capi.DeviceModel(m)
-    ll, lls, L, anc = dm.pf_loglik(tabs[0], N, seed, int(b["g0.pf.stream"][0]), float(b["g0.pf.invT"][0]),
-                                   m.sections)
+    ll, lls, L, anc, lin = dm.pf_loglik(tabs[0], N, seed, int(b["g0.pf.stream"][0]), float(b["g0.pf.invT"][0]),
+                                        m.sections, lineage=True)
     assert np.array_equal(anc, b["g0.pf.ancestors"])
+    assert np.array_equal(lin, b["g0.pf.lineage_transnum"])     # Mpi::particle_sample
     np.testing.assert_allclose(L, b["g0.pf.L_section"], rtol=L_RTOL, atol=1e-12)
     np.testing.assert_allclose(lls, b["g0.pf.obprob_section"], rtol=L_RTOL, atol=1e-12)
     np.testing.assert_allclose(ll, b["g0.pf.obprob"][0], rtol=L_RTOL)
@@ -110,10 +111,15 @@ def test_particle_filter_fast_form_and_oracle(built):
     b, m, tabs, seed = load("c0_pf")
     dm = capi.DeviceModel(m)
     N = 256
-    llg, _, _, ancg = dm.pf_loglik(tabs[0], N, seed + 3, 77, 1.0, m.sections)
-    llo, _, _, anco = oracle_pf(m, tabs[0], N, seed + 3, 77, 1.0, m.sections)
+    llg, _, _, ancg, ling = dm.pf_loglik(tabs[0], N, seed + 3, 77, 1.0, m.sections, lineage=True)
+    llo, _, _, anco, lino = oracle_pf(m, tabs[0], N, seed + 3, 77, 1.0, m.sections, lineage=True)
     assert np.array_equal(ancg, anco)
+    assert np.array_equal(ling, lino)
     np.testing.assert_allclose(llg, llo, rtol=L_RTOL)
-    llf, _, _, ancf = dm.pf_loglik(tabs[0], N, seed + 3, 77, 1.0, m.sections, form=capi.FORM_FAST)
+    llf, _, _, ancf, linf = dm.pf_loglik(tabs[0], N, seed + 3, 77, 1.0, m.sections, form=capi.FORM_FAST, lineage=True)
     assert np.isfinite(llf) and ancf.min() >= 0 and ancf.max() < N
+    # the fast form's lineage is a full trajectory: counts in every section, infections included
+    assert linf.min() >= 0
+    for ti, tf in m.sections:
+        assert linf[ti:tf].sum() > 0
     dm.close()

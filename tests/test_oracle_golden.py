@@ -76,8 +76,11 @@ def test_oracle_particle_filter_matches_reference(name):
     from oracle_lib import oracle_pf
     b, m, tabs, seed = load(name)
     N = b["g0.pf.ancestors"].shape[1]
-    ll, lls, L, anc = oracle_pf(m, tabs[0], N, seed, int(b["g0.pf.stream"][0]), float(b["g0.pf.invT"][0]), m.sections)
+    ll, lls, L, anc, lin = oracle_pf(m, tabs[0], N, seed, int(b["g0.pf.stream"][0]), float(b["g0.pf.invT"][0]),
+                                     m.sections, lineage=True)
     assert np.array_equal(anc, b["g0.pf.ancestors"])
+    # the reference's Mpi::particle_sample of the same filter run
+    assert np.array_equal(lin, b["g0.pf.lineage_transnum"])
     np.testing.assert_allclose(L, b["g0.pf.L_section"], rtol=L_RTOL, atol=1e-12)
     np.testing.assert_allclose(lls, b["g0.pf.obprob_section"], rtol=L_RTOL, atol=1e-12)
     np.testing.assert_allclose(ll, b["g0.pf.obprob"][0], rtol=L_RTOL)
