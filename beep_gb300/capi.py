@@ -271,6 +271,8 @@ def lib():
         L.beep_mbp_destroy.argtypes = [C.c_void_p]
         for f in ("beep_mbp_initialise", "beep_mbp_propose"):
             getattr(L, f).argtypes = [C.c_void_p, C.POINTER(MbpRequest)]
+        L.beep_mbp_set_state.argtypes = [C.c_void_p, C.POINTER(MbpRequest), _i32p]
+        L.beep_mbp_set_state.restype = C.c_int32
         L.beep_mbp_accept.argtypes = [C.c_void_p, C.POINTER(C.c_uint8)]
         L.beep_mbp_state_likelihood.argtypes = [C.c_void_p, C.POINTER(MbpRequest), _f64p]
         L.beep_mbp_acceptance.argtypes = [C.c_int32] + [C.c_double] * 6
@@ -471,6 +473,13 @@ class MbpChains:
         """State::simulate of every chain; returns the log-likelihoods."""
         r, keep = self._request(tables, seed, group_of, stream_of)
         check(lib().beep_mbp_initialise(self.h, C.byref(r)))
+        return keep["L"]
+
+    def set_state(self, tables: Sequence[Tables], transnum, group_of=None) -> np.ndarray:
+        """State::initialise_from_particle of every chain from given counts; returns the log-likelihoods."""
+        tn = np.ascontiguousarray(transnum, np.int32)
+        r, keep = self._request(tables, 0, group_of)
+        check(lib().beep_mbp_set_state(self.h, C.byref(r), _ptr(tn, C.c_int32)))
         return keep["L"]
 
     def propose(self, tables: Sequence[Tables], seed: int, group_of=None, stream_of=None,

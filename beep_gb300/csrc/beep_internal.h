@@ -89,6 +89,8 @@ struct BatchDev {
 	// MBP chains (plain form; mode 0 = plain simulation of the fields above)
 	int32_t mode;                       // 1: new chain state (Mbp::mbp; initialisation = every cell SIMU)
 	                                    // 2: State::likelihood of the current state under this batch's tables
+	                                    // 3: state rebuilt from the counts in the non-current slot
+	                                    //    (State::initialise_from_particle)
 	int32_t inf_dif;                    // mode 1: Imap' = Imap + dImap (INF_DIF_UPDATE)
 	int32_t simu_all;                   // mode 1: every cell drawn afresh (State::simulate)
 	const uint8_t *simu;                // [P][S][A] 1 = SIMU cell, or null

@@ -9,8 +9,8 @@
 // reads a copy uploaded with every launch).  A proposal is written to the
 // other slot; accepting it flips the record (swap_initial_propose_state), so
 // no state is ever copied.  The kernels are the plain FP64 form's
-// (sim_plain.cu, modes 1 and 2), which reproduce the reference's counts
-// bit for bit under the keyed variate stream.
+// (sim_plain.cu, modes 1-3), which reproduce the reference's counts bit for
+// bit under the keyed variate stream.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -36,14 +36,15 @@ struct beep_mbp_chains {
 namespace {
 
 // One launch of the chain kernel over every chain: mode 1 writes the
-// non-current slot (simu_all: State::simulate), mode 2 scores the current one.
+// non-current slot (simu_all: State::simulate), mode 3 rebuilds the
+// non-current slot from its counts, mode 2 scores the current one.
 beep_status run_chains(beep_mbp_chains *c, const beep_mbp_request *r, int mode, bool simu_all, double *Li_out)
 {
 	beep_model *m = c->m;
 	if (!r || !r->groups || r->ngroup <= 0) return fail(BEEP_BAD_INPUT, "the request needs parameter tables");
 	if (r->inf_update != BEEP_INF_UPDATE && r->inf_update != BEEP_INF_DIF_UPDATE)
 		return fail(BEEP_BAD_INPUT, "unknown inf_update");
-	if (mode != 1 || !simu_all)
+	if (mode == 2 || (mode == 1 && !simu_all))
 		if (!c->initialised) return fail(BEEP_BAD_INPUT, "chains are not initialised");
 	std::lock_guard<std::mutex> lock(m->mu);
 	CUDA_TRY(cudaSetDevice(m->device));
@@ -51,7 +52,7 @@ beep_status run_chains(beep_mbp_chains *c, const beep_mbp_request *r, int mode, 
 	beep_sim_batch b{};
 	b.nparticle = P; b.ngroup = r->ngroup; b.groups = r->groups; b.group_of = r->group_of;
 	b.seed = r->seed; b.stream_of = r->stream_of; b.ti = 0; b.tf = m->S;
-	b.L_out = mode == 1 ? r->L_out : nullptr;
+	b.L_out = mode != 2 ? r->L_out : nullptr;
 	b.form = BEEP_FORM_PLAIN_FP64;
 	beep_batch *q = nullptr;
 	beep_status st = batch_create_internal(m, &b, false, &q);
@@ -143,6 +144,26 @@ BEEP_API beep_status beep_mbp_initialise(beep_mbp_chains *c, const beep_mbp_requ
 {
 	if (!c) return fail(BEEP_BAD_INPUT, "null chains");
 	beep_status st = run_chains(c, r, 1, true, nullptr);
+	if (st != BEEP_OK) return st;
+	for (auto &x : c->cur) x ^= 1;
+	c->initialised = true;
+	return BEEP_OK;
+}
+
+BEEP_API beep_status beep_mbp_set_state(beep_mbp_chains *c, const beep_mbp_request *r, const int32_t *transnum)
+{
+	if (!c || !transnum) return fail(BEEP_BAD_INPUT, "null argument");
+	{
+		std::lock_guard<std::mutex> lock(c->m->mu);
+		CUDA_TRY(cudaSetDevice(c->m->device));
+		CUDA_TRY(cudaStreamSynchronize(c->m->stream));
+		const size_t S = c->m->S, per = S * c->tnsz;
+		for (int k = 0; k < c->nchain; k++) {
+			const size_t off = ((size_t)(1 - c->cur[k]) * c->nchain + k) * per;
+			CUDA_TRY(cudaMemcpyAsync(c->tn + off, transnum + (size_t)k * per, 4 * per, cudaMemcpyHostToDevice, c->m->stream));
+		}
+	}
+	beep_status st = run_chains(c, r, 3, false, nullptr);
 	if (st != BEEP_OK) return st;
 	for (auto &x : c->cur) x ^= 1;
 	c->initialised = true;

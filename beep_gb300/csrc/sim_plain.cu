@@ -23,6 +23,9 @@
 //           recomputed (INF_UPDATE) or Imap + dImap with dImap built from
 //           the count differences (INF_DIF_UPDATE, src/state.cc:109-123).
 //           Initialisation (State::simulate) is this mode with every cell SIMU.
+//   mode 3  State::initialise_from_particle (src/state.cc:294-322): the counts
+//           already in the slot that is not current are kept; Imap
+//           (set_Imap), the means (set_transmean) and L are recomputed.
 //   mode 2  State::likelihood (src/state.cc:812-826) of the current state
 //           with the means recomputed under this batch's tables on the fixed
 //           state (Mbp::parameter_proposal, src/mbp.cc:460-478).
@@ -106,6 +109,7 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 	const int mode = b.mode;
 	const int cs_i = mode ? b.cur[p] : 0, cs_p = 1 - cs_i;
 	const bool dif = mode == 1 && b.inf_dif && !b.simu_all;
+	const bool writes = mode == 1 || mode == 3;          // the non-current slot receives a state
 	auto chs = [&](int slot, int s) { return ((size_t)slot * b.P + p) * m.S + s; };
 	double Lsum = 0.0, Lcmp = 0.0;   // mode 2: compensated partial sum of this thread
 
@@ -124,12 +128,12 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 	const int itr = m.infection_trans;
 	const int inf_from = m.trans_from[itr];
 	for (int sett = b.ti; sett < b.tf; sett++) {
-		int32_t *tn = mode ? b.ch_tn + chs(mode == 1 ? cs_p : cs_i, sett) * tnsz
+		int32_t *tn = mode ? b.ch_tn + chs(writes ? cs_p : cs_i, sett) * tnsz
 		          : b.tn_traj ? b.tn_traj + ((size_t)p * nsteps + (sett - b.ti)) * tnsz : b.tn + (size_t)p * tnsz;
 		const int32_t *tn_prev = b.tn_traj || mode ? tn - tnsz : tn;   // single buffer still holds the previous step
 		const int32_t *tn_base = dif && sett > 0 ? b.ch_tn + chs(cs_i, sett - 1) * tnsz : nullptr;
-		double *Im_s = mode ? b.ch_Imap + chs(mode == 1 ? cs_p : cs_i, sett) * agsz : Imap;
-		double *Id_s = mode ? b.ch_Idiag + chs(mode == 1 ? cs_p : cs_i, sett) * agsz : Idiag;
+		double *Im_s = mode ? b.ch_Imap + chs(writes ? cs_p : cs_i, sett) * agsz : Imap;
+		double *Id_s = mode ? b.ch_Idiag + chs(writes ? cs_p : cs_i, sett) * agsz : Idiag;
 
 		// ---- A: dinf per (strain, source area, age)
 		for (int idx = tid; idx < (int)agsz && mode != 2 && !(dif && sett == 0); idx += nth) {
@@ -181,7 +185,7 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 			}
 			Imap[idx] = im;
 			Idiag[idx] = id;
-			if (mode == 1) {
+			if (writes) {
 				if (dif) {
 					const size_t io = chs(cs_i, sett) * agsz + idx;
 					Im_s[idx] = b.ch_Imap[io] + im;
@@ -259,6 +263,11 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 				const double t = Lsum + lp;
 				Lcmp += fabs(Lsum) >= fabs(lp) ? (Lsum - t) + lp : (lp - t) + Lsum;
 				Lsum = t;
+				continue;
+			}
+			if (mode == 3) {                    // the given counts stay
+				if (mean != mean) set_status(status, BEEP_NAN_RATE);
+				b.ch_mean[chs(cs_p, sett) * tnsz + cell] = mean;
 				continue;
 			}
 			int32_t n = 0;

@@ -289,6 +289,15 @@ BEEP_API beep_status beep_mbp_destroy(beep_mbp_chains *chains);
 /* State::simulate(theta) (src/state.cc:582-592) of every chain over
  * [0, ndivision); the result becomes the chain's current state. */
 BEEP_API beep_status beep_mbp_initialise(beep_mbp_chains *chains, const beep_mbp_request *request);
+/* State::initialise_from_particle (src/state.cc:294-322) for every chain: the
+ * given transition counts [nchain][ndivision][narea][ntrans][ndemocatpos]
+ * become the chain's current state, with Imap, Idiag and the transition means
+ * recomputed under the request's tables and L_out (if set) from the
+ * observations.  (With several strains the reference applies update_pop
+ * before the strain shift of set_transmean here; this call follows
+ * State::simulate's order, which is the same for one strain.) */
+BEEP_API beep_status beep_mbp_set_state(beep_mbp_chains *chains, const beep_mbp_request *request,
+                                        const int32_t *transnum);
 /* Mbp::mbp (src/mbp.cc:252-330): every chain's proposed state from its
  * current state, under the request's tables: a coupled cell draws
  * n' = n + Poisson(m'-m) (m' > m), n (m' = m) or Binomial(n, m'/m) (m' < m)

@@ -94,3 +94,34 @@ def test_mbp_errors(device):
         ch.propose(tabs, seed, inf_update=7)
     ch.close()
     dm.close()
+
+
+def test_initialise_from_particle_restores_the_state(device):
+    """beep_mbp_set_state (State::initialise_from_particle) from the counts of
+    simulated chains rebuilds the same means bit for bit and the same
+    likelihoods, and the next proposal from the rebuilt state is identical."""
+    b, m, tabs, seed = load("c0_mbp")
+    nc = 6
+    gi = np.arange(nc) % len(tabs)
+    dm = capi.DeviceModel(m)
+    a = capi.MbpChains(dm, nc)
+    L0 = a.initialise(tabs, seed, group_of=gi, stream_of=np.arange(nc) + 300)
+    states = [a.read_state(k) for k in range(nc)]
+    tn = np.stack([s_[0] for s_ in states])
+    c = capi.MbpChains(dm, nc)
+    Lc = c.set_state(tabs, tn, group_of=gi)
+    np.testing.assert_allclose(Lc, L0, rtol=1e-12)
+    for k in range(nc):
+        tn2, mean2 = c.read_state(k)
+        assert np.array_equal(tn2, states[k][0])
+        assert np.array_equal(mean2, states[k][1])
+    np.testing.assert_array_equal(c.state_likelihood(tabs, group_of=gi), a.state_likelihood(tabs, group_of=gi))
+    gp = (gi + 1) % len(tabs)
+    for ch in (a, c):
+        ch.propose(tabs, seed, group_of=gp, stream_of=np.arange(nc) + 900, inf_update=capi.INF_DIF_UPDATE)
+        ch.accept(np.ones(nc, np.uint8))
+    for k in range(nc):
+        assert np.array_equal(a.read_state(k)[0], c.read_state(k)[0])
+    a.close()
+    c.close()
+    dm.close()
