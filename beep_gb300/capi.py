@@ -250,6 +250,10 @@ def lib():
                   "beep_batch_destroy"):
             getattr(L, f).argtypes = [C.c_void_p]
         L.beep_batch_time.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]
+        L.beep_batch_run_graph.argtypes = [C.c_void_p]
+        L.beep_batch_run_graph.restype = C.c_int32
+        L.beep_autotune.argtypes = [C.c_void_p, C.POINTER(SimBatch), C.POINTER(C.c_int32)]
+        L.beep_autotune.restype = C.c_int32
         L.beep_batch_foi_path.argtypes = [C.c_void_p]
         L.beep_batch_foi_path.restype = C.c_int32
         L.beep_batch_launches.argtypes = [C.c_void_p]
@@ -333,6 +337,12 @@ class DeviceModel:
         check(lib().beep_simulate(self.h, C.byref(batch.st)))
         return batch
 
+    def autotune(self, batch: Batch) -> int:
+        """Chooses the fast form's FOI path for this model by timing a sample of the batch."""
+        c = C.c_int32()
+        check(lib().beep_autotune(self.h, C.byref(batch.st), C.byref(c)))
+        return c.value
+
     def pf_loglik(self, tables: "Tables", N: int, seed: int, resample_stream: int, invT: float, sections,
                   form: int = FORM_PLAIN_FP64, lineage: bool = False):
         """Bootstrap particle filter on the device: (estimate, per-section terms, L, ancestors) and, with
@@ -396,6 +406,11 @@ class DeviceBatch:
         self.upload()
         self.launch()
         return self.download()
+
+    def run_graph(self) -> Batch:
+        """stage + upload + launch + download with the device work replayed as a CUDA graph."""
+        check(lib().beep_batch_run_graph(self.h))
+        return self.batch
 
     def time(self, iters: int) -> float:
         ms = C.c_double()

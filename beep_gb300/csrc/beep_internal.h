@@ -116,5 +116,6 @@ int fast_pick_threads(const ModelDev &m);        // threads per CTA of the fast 
 // library options (beep_set_option)
 int option_fast_foi();                           // 0 automatic, 1 FP32 SIMT, 2 tensor cores
 int fast_threads();
+int fast_prepare();                              // one-time constant tables of the fast kernel
 
 }  // namespace beep

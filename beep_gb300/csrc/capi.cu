@@ -622,7 +622,7 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 		// force of infection on the tensor cores: large models (the matrix is streamed from
 		// L2 each step; the particle's populations and counts move to global memory to make
 		// room for the operand ring)
-		const int opt = option_fast_foi();
+		const int opt = option_fast_foi() != 0 ? option_fast_foi() : m->tuned_foi;
 		const bool can_tc = m->dev.tc_image != nullptr && fast_pick_threads(m->dev) == 640;
 		const bool want_tc = opt == 2 || (opt == 0 && m->A >= 300);
 		if (can_tc && want_tc) {
@@ -641,6 +641,7 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 		}
 	}
 	auto bail = [&](beep_status s) { beep_batch_destroy(q); return s; };
+	if (b->form == BEEP_FORM_FAST && fast_prepare() != 0) return bail(fail(BEEP_DEVICE_ERROR, "constant tables"));
 	st = stage_inputs(q);
 	if (st != BEEP_OK) return bail(st);
 
@@ -770,6 +771,86 @@ beep_status beep_batch_time(beep_batch *q, int32_t iters, double *ms_per_launch)
 
 int32_t beep_batch_launches(const beep_batch *q) { return q ? 1 : 0; }
 
+beep_status beep_batch_run_graph(beep_batch *q)
+{
+	if (!q) return fail(BEEP_BAD_INPUT, "null batch");
+	if (q->device_io) return fail(BEEP_BAD_INPUT, "internal batches are not replayed as graphs");
+	beep_status st = beep_batch_stage(q);
+	if (st != BEEP_OK) return st;
+	cudaStream_t s = q->m->stream;
+	if (q->graph_exec && q->graph_in_size != q->in_size) {   // the staged inputs changed size: capture again
+		cudaGraphExecDestroy(q->graph_exec);
+		cudaGraphDestroy(q->graph);
+		q->graph_exec = nullptr;
+		q->graph = nullptr;
+	}
+	if (!q->graph_exec) {
+		CUDA_TRY(cudaStreamSynchronize(s));
+		CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+		beep_status cs = beep_batch_upload(q);
+		if (cs == BEEP_OK) cs = beep_batch_launch(q);
+		if (cs == BEEP_OK) cs = batch_download_enqueue(q);
+		cudaGraph_t g = nullptr;
+		cudaError_t e = cudaStreamEndCapture(s, &g);
+		if (cs != BEEP_OK) {
+			if (g) cudaGraphDestroy(g);
+			return cs;
+		}
+		if (e != cudaSuccess) return fail(BEEP_DEVICE_ERROR, std::string("graph capture: ") + cudaGetErrorString(e));
+		e = cudaGraphInstantiate(&q->graph_exec, g, 0);
+		if (e != cudaSuccess) {
+			cudaGraphDestroy(g);
+			return fail(BEEP_DEVICE_ERROR, std::string("graph instantiation: ") + cudaGetErrorString(e));
+		}
+		q->graph = g;
+		q->graph_in_size = q->in_size;
+	}
+	CUDA_TRY(cudaGraphLaunch(q->graph_exec, s));
+	CUDA_TRY(cudaStreamSynchronize(s));
+	return batch_download_finish(q);
+}
+
+beep_status beep_autotune(beep_model *m, const beep_sim_batch *b, int32_t *chosen)
+{
+	if (!m || !b) return fail(BEEP_BAD_INPUT, "null argument");
+	if (b->form != BEEP_FORM_FAST) return fail(BEEP_BAD_INPUT, "the autotuner chooses among fast-form kernels");
+	// a sample of the batch: two waves of particles over the first steps of its range
+	beep_sim_batch t = *b;
+	int dev_sms = 152;
+	cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, m->device);
+	t.nparticle = std::min(b->nparticle, 2 * dev_sms);
+	t.tf = std::min(b->tf, b->ti + 120);
+	t.L_out = nullptr;
+	t.pop_out = nullptr;
+	t.transnum_out = nullptr;
+	t.pop_traj_out = nullptr;
+	std::vector<double> L(t.nparticle);
+	t.L_out = L.data();
+	if (t.ti > 0 && !t.pop_in) return fail(BEEP_BAD_INPUT, "pop_in is required when ti > 0");
+	const int saved_opt = option_fast_foi();
+	const int saved_tuned = m->tuned_foi;
+	double best = 1e300;
+	int best_c = 1;
+	for (int cand = 1; cand <= 2; cand++) {
+		m->tuned_foi = cand;
+		beep_batch *q = nullptr;
+		beep_status st = beep_batch_create(m, &t, &q);
+		if (st != BEEP_OK) { m->tuned_foi = saved_tuned; return st; }
+		if (beep_batch_foi_path(q) != cand) { beep_batch_destroy(q); continue; }   // not available for this model
+		double ms = 0;
+		st = beep_batch_upload(q);
+		if (st == BEEP_OK) st = beep_batch_time(q, 1, &ms);      // warm-up
+		if (st == BEEP_OK) st = beep_batch_time(q, 2, &ms);
+		beep_batch_destroy(q);
+		if (st != BEEP_OK) { m->tuned_foi = saved_tuned; return st; }
+		if (ms < best) { best = ms; best_c = cand; }
+	}
+	(void)saved_opt;
+	m->tuned_foi = best_c;
+	if (chosen) *chosen = best_c;
+	return BEEP_OK;
+}
+
 int32_t beep_batch_foi_path(const beep_batch *q)
 {
 	if (!q || q->b.form != BEEP_FORM_FAST) return 0;
@@ -795,6 +876,8 @@ beep_status beep_batch_destroy(beep_batch *q)
 	q->out_dev.release();
 	if (q->ev0) cudaEventDestroy(q->ev0);
 	if (q->ev1) cudaEventDestroy(q->ev1);
+	if (q->graph_exec) cudaGraphExecDestroy(q->graph_exec);
+	if (q->graph) cudaGraphDestroy(q->graph);
 	delete q;
 	return BEEP_OK;
 }

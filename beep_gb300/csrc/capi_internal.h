@@ -102,6 +102,7 @@ struct beep_model {
 	    obs_cells_full_h;
 	std::vector<float> obs_factor_f_h;
 	int32_t max_obs_spline = -1;
+	int32_t tuned_foi = 0;        // fast-form FOI path chosen by beep_autotune (0: none)
 	std::mutex mu;
 };
 
@@ -121,6 +122,10 @@ struct beep_batch {
 	cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 	bool pending = false;
 	bool state_global = false;   // fast form keeps particle state in global memory
+	// CUDA graph of upload + status reset + kernel + download (beep_batch_run_graph)
+	cudaGraph_t graph = nullptr;
+	cudaGraphExec_t graph_exec = nullptr;
+	size_t graph_in_size = 0;
 };
 
 

@@ -28,6 +28,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <mutex>
 
 #include "beep_internal.h"
 #include "rng_fp64.cuh"
@@ -755,6 +756,21 @@ size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_
 
 int fast_threads() { return kFastThreads; }
 
+// log k! for k < 32 in constant memory, once per process (before any graph capture)
+int fast_prepare()
+{
+	static std::mutex mu;
+	static bool done = false;
+	std::lock_guard<std::mutex> lock(mu);
+	if (done) return 0;
+	float lf[32];
+	for (int k = 0; k < 32; k++) lf[k] = (float)std::lgamma((double)k + 1.0);
+	cudaError_t e = cudaMemcpyToSymbol(c_lnfact, lf, sizeof lf);
+	if (e != cudaSuccess) return (int)e;
+	done = true;
+	return 0;
+}
+
 int fast_pick_threads(const ModelDev &m) { return pick_threads(m); }
 
 size_t fast_tc_smem_bytes(const ModelDev &m)
@@ -795,13 +811,9 @@ int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream)
 	const int nt = pick_threads(m);
 	const int NSA = m.NS * m.A;
 	if (NSA > nt || m.G * m.G > nt) return (int)cudaErrorInvalidValue;   // slices: one item per thread
-	static bool init = false;
-	if (!init) {
-		float lf[32];
-		for (int k = 0; k < 32; k++) lf[k] = (float)std::lgamma((double)k + 1.0);
-		cudaError_t e = cudaMemcpyToSymbol(c_lnfact, lf, sizeof lf);
-		if (e != cudaSuccess) return (int)e;
-		init = true;
+	{
+		const int e = fast_prepare();
+		if (e != 0) return e;
 	}
 	cudaStream_t st = (cudaStream_t)stream;
 	if (b.foi_tc) return launch_nt<640, true>(m, b, smem, st);

@@ -199,6 +199,16 @@ BEEP_API int32_t beep_batch_launches(const beep_batch *batch);   /* kernels per 
 /* bytes moved host->device by beep_batch_upload and device->host by beep_batch_download */
 BEEP_API beep_status beep_batch_bytes(const beep_batch *batch, int64_t *h2d, int64_t *d2h);
 BEEP_API beep_status beep_batch_destroy(beep_batch *batch);
+/* stage + upload + launch + download, with the device work (input copy,
+ * status reset, kernel, output copy) captured once as a CUDA graph and
+ * replayed by later calls (captured again if the staged inputs change size). */
+BEEP_API beep_status beep_batch_run_graph(beep_batch *batch);
+/* Autotuner of the fast form for a model: times every force-of-infection path
+ * the model supports (1 = FP32 SIMT, 2 = tensor cores) on a sample of the
+ * given batch (two waves of particles, up to 120 steps) and records the
+ * fastest on the model; later batches of the model use it while the option
+ * fast_foi is automatic.  *chosen (may be NULL) receives the path. */
+BEEP_API beep_status beep_autotune(beep_model *model, const beep_sim_batch *batch, int32_t *chosen);
 /* Force-of-infection path the fast form of this batch runs: 1 = FP32 SIMT,
  * 2 = tensor cores; 0 for the plain form. */
 BEEP_API int32_t beep_batch_foi_path(const beep_batch *batch);
