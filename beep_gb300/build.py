@@ -31,6 +31,7 @@ UNITS = {
     "pf.cu": [],
     "abc_weights.cu": [],
     "mbp.cu": [],
+    "mbp_fast.cu": [],
     "serve.cu": [],
 }
 

@@ -99,6 +99,7 @@ struct BatchDev {
 	double *ch_mean;                    // [2][P][S][A][T][DP]
 	double *ch_Imap, *ch_Idiag;         // [2][P][S][NS][A][G]
 	double *Li;                         // [P] mode 2 output
+	float *ch_mean_f;                   // fast form chains: means [2][P][S][T][A*DP] (counts in ch_tn, same layout)
 	// fast form: force of infection on the tensor cores (foi_tc.cuh); its shared
 	// memory starts at tc_smem_off bytes into the dynamic shared memory
 	int32_t foi_tc;
@@ -117,5 +118,7 @@ int fast_pick_threads(const ModelDev &m);        // threads per CTA of the fast 
 int option_fast_foi();                           // 0 automatic, 1 FP32 SIMT, 2 tensor cores
 int fast_threads();
 int fast_prepare();                              // one-time constant tables of the fast kernel
+int fast_chain_prepare();                        // the same for the MBP-chain variants (mbp_fast.cu)
+int launch_sim_fast_chain(const ModelDev &m, const BatchDev &b, void *stream);   // mbp_fast.cu
 
 }  // namespace beep

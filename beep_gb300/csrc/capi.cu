@@ -527,7 +527,7 @@ beep_status beep_batch_create(beep_model *m, const beep_sim_batch *b, beep_batch
 }  // extern "C"
 
 beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, bool device_io, beep_batch **out,
-                                        bool device_traj)
+                                        bool device_traj, bool allow_tc)
 {
 	// a count trajectory is written: to the batch's output (transnum_out), or to a
 	// device buffer the caller sets in bd.tn_traj before each launch (device_traj)
@@ -623,7 +623,7 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 		// L2 each step; the particle's populations and counts move to global memory to make
 		// room for the operand ring)
 		const int opt = option_fast_foi() != 0 ? option_fast_foi() : m->tuned_foi;
-		const bool can_tc = m->dev.tc_image != nullptr && fast_pick_threads(m->dev) == 640;
+		const bool can_tc = allow_tc && m->dev.tc_image != nullptr && fast_pick_threads(m->dev) == 640;
 		const bool want_tc = opt == 2 || (opt == 0 && m->A >= 300);
 		if (can_tc && want_tc) {
 			// the transition counts stay on chip when they fit beside the operand ring

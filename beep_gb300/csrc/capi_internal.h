@@ -136,8 +136,9 @@ namespace beep {
 // With device_traj the kernels write every step's transition counts to a
 // device buffer the caller sets in bd.tn_traj ([P][tf-ti][A][T][DP]) before
 // each launch.
+// allow_tc = false keeps the fast form on the FP32 SIMT force of infection.
 beep_status batch_create_internal(beep_model *m, const beep_sim_batch *b, bool device_io, beep_batch **out,
-                                  bool device_traj = false);
+                                  bool device_traj = false, bool allow_tc = true);
 // beep_batch_download in two halves: the device->host copy enqueued on the
 // model's stream, and (once that copy completed) the status check and the
 // copy into the caller's arrays.

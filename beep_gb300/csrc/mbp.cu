@@ -1,10 +1,12 @@
 // MBP chains on the device: the reference's Mbp pair of states
 // (src/mbp.hh:58-59) for many chains at once.
 //
-// Each chain owns two trajectory slots in one HBM allocation,
+// Each chain owns two trajectory slots in one HBM allocation; plain FP64 form:
 //   transnum  int32 [2][nchain][S][A][T][DP]
 //   transmean FP64  [2][nchain][S][A][T][DP]
 //   Imap, Idiag FP64 [2][nchain][S][NS][A][G]
+// fast form (mbp_fast.cu): counts int32 and means FP32 [2][nchain][S][T][A*DP]
+// (column-major per step, the fast kernel's layout), no Imap;
 // and a host-side record of which slot is its current state (the device
 // reads a copy uploaded with every launch).  A proposal is written to the
 // other slot; accepting it flips the record (swap_initial_propose_state), so
@@ -29,11 +31,24 @@ struct beep_mbp_chains {
 	std::vector<uint8_t> cur;            // current slot of each chain
 	int32_t *tn = nullptr;
 	double *mean = nullptr, *Imap = nullptr, *Idiag = nullptr;
+	float *mean_f = nullptr;             // fast form
 	bool initialised = false;
 	size_t tnsz = 0, agsz = 0;
 };
 
 namespace {
+
+// [S][A][T][DP] (the reference's transnum) -> [S][T][A*DP] (the fast chains' layout)
+void to_fast_layout(const beep_mbp_chains *c, const int32_t *src, int32_t *dst)
+{
+	const int A = c->m->A, T = c->m->T, DP = c->m->DP, S = c->m->S;
+	const size_t ncol = (size_t)A * DP;
+	for (int s = 0; s < S; s++)
+		for (int a = 0; a < A; a++)
+			for (int t = 0; t < T; t++)
+				for (int dp = 0; dp < DP; dp++)
+					dst[((size_t)s * T + t) * ncol + (size_t)a * DP + dp] = src[(((size_t)s * A + a) * T + t) * DP + dp];
+}
 
 // One launch of the chain kernel over every chain: mode 1 writes the
 // non-current slot (simu_all: State::simulate), mode 3 rebuilds the
@@ -53,9 +68,9 @@ beep_status run_chains(beep_mbp_chains *c, const beep_mbp_request *r, int mode, 
 	b.nparticle = P; b.ngroup = r->ngroup; b.groups = r->groups; b.group_of = r->group_of;
 	b.seed = r->seed; b.stream_of = r->stream_of; b.ti = 0; b.tf = m->S;
 	b.L_out = mode != 2 ? r->L_out : nullptr;
-	b.form = BEEP_FORM_PLAIN_FP64;
+	b.form = c->form;
 	beep_batch *q = nullptr;
-	beep_status st = batch_create_internal(m, &b, false, &q);
+	beep_status st = batch_create_internal(m, &b, false, &q, false, false);
 	if (st != BEEP_OK) return st;
 	auto done = [&](beep_status s) {
 		std::string e = s == BEEP_OK ? std::string() : std::string(beep_last_error());
@@ -80,6 +95,7 @@ beep_status run_chains(beep_mbp_chains *c, const beep_mbp_request *r, int mode, 
 	bd.simu = mask ? (const uint8_t *)(d + o_simu) : nullptr;
 	bd.cur = (const uint8_t *)(d + o_cur);
 	bd.ch_tn = c->tn; bd.ch_mean = c->mean; bd.ch_Imap = c->Imap; bd.ch_Idiag = c->Idiag;
+	bd.ch_mean_f = c->mean_f;
 	bd.Li = (double *)(d + o_li);
 	st = beep_batch_upload(q);
 	if (st == BEEP_OK) st = beep_batch_launch(q);
@@ -99,7 +115,7 @@ BEEP_API beep_status beep_mbp_create(beep_model *m, int32_t nchain, int32_t form
 {
 	if (!m || !out || nchain <= 0) return fail(BEEP_BAD_INPUT, "model, nchain > 0 and out are required");
 	*out = nullptr;
-	if (form != BEEP_FORM_PLAIN_FP64) return fail(BEEP_BAD_INPUT, "MBP chains exist in the plain FP64 form only");
+	if (form != BEEP_FORM_PLAIN_FP64 && form != BEEP_FORM_FAST) return fail(BEEP_BAD_INPUT, "unknown form");
 	std::lock_guard<std::mutex> lock(m->mu);
 	CUDA_TRY(cudaSetDevice(m->device));
 	beep_mbp_chains *c = new beep_mbp_chains();
@@ -109,9 +125,10 @@ BEEP_API beep_status beep_mbp_create(beep_model *m, int32_t nchain, int32_t form
 	c->tnsz = (size_t)m->A * m->T * m->DP;
 	c->agsz = (size_t)m->NS * m->A * m->G;
 	const size_t slots = 2 * (size_t)nchain * m->S;
+	const bool fast = form == BEEP_FORM_FAST;
 	Layout L;
-	const size_t o_tn = L.add(4 * slots * c->tnsz), o_mean = L.add(8 * slots * c->tnsz),
-	             o_im = L.add(8 * slots * c->agsz), o_id = L.add(8 * slots * c->agsz);
+	const size_t o_tn = L.add(4 * slots * c->tnsz), o_mean = L.add((fast ? 4 : 8) * slots * c->tnsz),
+	             o_im = L.add(fast ? 0 : 8 * slots * c->agsz), o_id = L.add(fast ? 0 : 8 * slots * c->agsz);
 	cudaError_t e = c->traj.reserve(L.size);
 	if (e != cudaSuccess) {
 		delete c;
@@ -119,9 +136,12 @@ BEEP_API beep_status beep_mbp_create(beep_model *m, int32_t nchain, int32_t form
 	}
 	char *d = (char *)c->traj.ptr;
 	c->tn = (int32_t *)(d + o_tn);
-	c->mean = (double *)(d + o_mean);
-	c->Imap = (double *)(d + o_im);
-	c->Idiag = (double *)(d + o_id);
+	if (fast) c->mean_f = (float *)(d + o_mean);
+	else {
+		c->mean = (double *)(d + o_mean);
+		c->Imap = (double *)(d + o_im);
+		c->Idiag = (double *)(d + o_id);
+	}
 	c->cur.assign(nchain, 0);
 	*out = c;
 	return BEEP_OK;
@@ -158,9 +178,16 @@ BEEP_API beep_status beep_mbp_set_state(beep_mbp_chains *c, const beep_mbp_reque
 		CUDA_TRY(cudaSetDevice(c->m->device));
 		CUDA_TRY(cudaStreamSynchronize(c->m->stream));
 		const size_t S = c->m->S, per = S * c->tnsz;
+		std::vector<int32_t> tmp;
 		for (int k = 0; k < c->nchain; k++) {
 			const size_t off = ((size_t)(1 - c->cur[k]) * c->nchain + k) * per;
-			CUDA_TRY(cudaMemcpyAsync(c->tn + off, transnum + (size_t)k * per, 4 * per, cudaMemcpyHostToDevice, c->m->stream));
+			const int32_t *src = transnum + (size_t)k * per;
+			if (c->form == BEEP_FORM_FAST) {            // [S][A][T][DP] -> [S][T][A*DP]
+				tmp.resize(per);
+				to_fast_layout(c, src, tmp.data());
+				src = tmp.data();
+			}
+			CUDA_TRY(cudaMemcpy(c->tn + off, src, 4 * per, cudaMemcpyHostToDevice));
 		}
 	}
 	beep_status st = run_chains(c, r, 3, false, nullptr);
@@ -212,10 +239,27 @@ BEEP_API beep_status beep_mbp_read_state(beep_mbp_chains *c, int32_t chain, int3
 	std::lock_guard<std::mutex> lock(c->m->mu);
 	CUDA_TRY(cudaSetDevice(c->m->device));
 	CUDA_TRY(cudaStreamSynchronize(c->m->stream));
-	const size_t S = c->m->S;
-	const size_t off = ((size_t)c->cur[chain] * c->nchain + chain) * S * c->tnsz;
-	if (transnum_out) CUDA_TRY(cudaMemcpy(transnum_out, c->tn + off, 4 * S * c->tnsz, cudaMemcpyDeviceToHost));
-	if (transmean_out) CUDA_TRY(cudaMemcpy(transmean_out, c->mean + off, 8 * S * c->tnsz, cudaMemcpyDeviceToHost));
+	const size_t S = c->m->S, per = S * c->tnsz;
+	const size_t off = ((size_t)c->cur[chain] * c->nchain + chain) * per;
+	if (c->form != BEEP_FORM_FAST) {
+		if (transnum_out) CUDA_TRY(cudaMemcpy(transnum_out, c->tn + off, 4 * per, cudaMemcpyDeviceToHost));
+		if (transmean_out) CUDA_TRY(cudaMemcpy(transmean_out, c->mean + off, 8 * per, cudaMemcpyDeviceToHost));
+		return BEEP_OK;
+	}
+	std::vector<int32_t> tn(per), tr(per);
+	std::vector<float> mf(per);
+	CUDA_TRY(cudaMemcpy(tn.data(), c->tn + off, 4 * per, cudaMemcpyDeviceToHost));
+	CUDA_TRY(cudaMemcpy(mf.data(), c->mean_f + off, 4 * per, cudaMemcpyDeviceToHost));
+	const int A = c->m->A, T = c->m->T, DP = c->m->DP;
+	const size_t ncol = (size_t)A * DP;
+	for (size_t s = 0; s < S; s++)
+		for (int a = 0; a < A; a++)
+			for (int t = 0; t < T; t++)
+				for (int dp = 0; dp < DP; dp++) {
+					const size_t ref = ((s * A + a) * T + t) * DP + dp, fst = (s * T + t) * ncol + (size_t)a * DP + dp;
+					if (transnum_out) transnum_out[ref] = tn[fst];
+					if (transmean_out) transmean_out[ref] = (double)mf[fst];
+				}
 	return BEEP_OK;
 }
 

@@ -273,8 +273,11 @@ BEEP_API beep_status beep_set_option(const char *name, int64_t value);
  * A chain set keeps, for each chain, two full trajectory states on the
  * device -- the reference's Mbp::initial and Mbp::propose (transnum,
  * transmean, Imap, Idiag over all ndivision steps, src/state.hh:21-28) -- and
- * which of the two is the chain's current state.  Only BEEP_FORM_PLAIN_FP64
- * chains exist so far (bit-exact with the reference's counts). */
+ * which of the two is the chain's current state.  BEEP_FORM_PLAIN_FP64 chains
+ * reproduce the reference's counts bit for bit; BEEP_FORM_FAST chains draw
+ * from the same keyed streams with FP32 means (counts and means are kept as
+ * int32 and FP32; Imap is formed from the counts each step, so inf_update has
+ * no effect on them). */
 typedef struct beep_mbp_chains beep_mbp_chains;
 
 typedef enum beep_inf_update {

@@ -89,7 +89,7 @@ def test_mbp_errors(device):
         ch.propose(tabs, seed)
     assert e.value.status == 1                    # BEEP_BAD_INPUT: not initialised
     with pytest.raises(capi.BeepError):
-        capi.MbpChains(dm, 2, form=capi.FORM_FAST)
+        capi.MbpChains(dm, 2, form=9)
     with pytest.raises(capi.BeepError):
         ch.propose(tabs, seed, inf_update=7)
     ch.close()
@@ -122,6 +122,58 @@ def test_initialise_from_particle_restores_the_state(device):
         ch.accept(np.ones(nc, np.uint8))
     for k in range(nc):
         assert np.array_equal(a.read_state(k)[0], c.read_state(k)[0])
+    a.close()
+    c.close()
+    dm.close()
+
+
+def test_fast_chains_follow_plain_chains(device):
+    """Fast-form chains (FP32 means, same keyed streams, FP32 binomial
+    inversion) follow the plain FP64 chains: most initial states and coupled
+    proposals are identical, with log-likelihoods within 1e-6 and state
+    likelihoods within 1e-5 where they are."""
+    b, m, tabs, seed = load("c0_mbp")
+    nc = 32
+    gi = np.arange(nc) % len(tabs)
+    gp = (gi + 3) % len(tabs)
+    dm = capi.DeviceModel(m)
+    res = {}
+    for form in (capi.FORM_PLAIN_FP64, capi.FORM_FAST):
+        ch = capi.MbpChains(dm, nc, form=form)
+        L0 = ch.initialise(tabs, seed, group_of=gi, stream_of=np.arange(nc) + 100)
+        tn0 = np.stack([ch.read_state(k)[0] for k in range(nc)])
+        Li = ch.state_likelihood(tabs, group_of=gp)
+        L1 = ch.propose(tabs, seed, group_of=gp, stream_of=np.arange(nc) + 400, inf_update=capi.INF_DIF_UPDATE)
+        ch.accept(np.ones(nc, np.uint8))
+        tn1 = np.stack([ch.read_state(k)[0] for k in range(nc)])
+        res[form] = (L0, tn0, Li, L1, tn1)
+        ch.close()
+    (pL0, ptn0, pLi, pL1, ptn1), (fL0, ftn0, fLi, fL1, ftn1) = res[capi.FORM_PLAIN_FP64], res[capi.FORM_FAST]
+    same0 = np.array([np.array_equal(ptn0[k], ftn0[k]) for k in range(nc)])
+    assert same0.mean() >= 0.6, same0.mean()
+    np.testing.assert_allclose(fL0[same0], pL0[same0], rtol=1e-6)
+    np.testing.assert_allclose(fLi[same0], pLi[same0], rtol=1e-5)
+    same1 = same0 & np.array([np.array_equal(ptn1[k], ftn1[k]) for k in range(nc)])
+    assert same1.mean() >= 0.4, same1.mean()
+    np.testing.assert_allclose(fL1[same1], pL1[same1], rtol=1e-6)
+    dm.close()
+
+
+def test_fast_chains_state_round_trip(device):
+    b, m, tabs, seed = load("tiny_mbp")
+    nc = 4
+    gi = np.arange(nc) * 2
+    dm = capi.DeviceModel(m)
+    a = capi.MbpChains(dm, nc, form=capi.FORM_FAST)
+    L0 = a.initialise(tabs, seed, group_of=gi, stream_of=np.arange(nc) + 7)
+    st = [a.read_state(k) for k in range(nc)]
+    c = capi.MbpChains(dm, nc, form=capi.FORM_FAST)
+    Lc = c.set_state(tabs, np.stack([x[0] for x in st]), group_of=gi)
+    np.testing.assert_allclose(Lc, L0, rtol=1e-6)
+    for k in range(nc):
+        tn, mean = c.read_state(k)
+        assert np.array_equal(tn, st[k][0])
+        np.testing.assert_allclose(mean, st[k][1], rtol=1e-6)
     a.close()
     c.close()
     dm.close()
