@@ -34,6 +34,10 @@ struct beep_mbp_chains {
 	float *mean_f = nullptr;             // fast form
 	bool initialised = false;
 	size_t tnsz = 0, agsz = 0;
+	// prepared batches, reused while the request keeps its shape (with / without L)
+	beep_batch *q[2] = {nullptr, nullptr};
+	int32_t q_ngroup[2] = {0, 0};
+	bool q_go[2] = {false, false}, q_so[2] = {false, false};
 };
 
 namespace {
@@ -69,14 +73,32 @@ beep_status run_chains(beep_mbp_chains *c, const beep_mbp_request *r, int mode, 
 	b.seed = r->seed; b.stream_of = r->stream_of; b.ti = 0; b.tf = m->S;
 	b.L_out = mode != 2 ? r->L_out : nullptr;
 	b.form = c->form;
-	beep_batch *q = nullptr;
-	beep_status st = batch_create_internal(m, &b, false, &q, false, false);
-	if (st != BEEP_OK) return st;
-	auto done = [&](beep_status s) {
-		std::string e = s == BEEP_OK ? std::string() : std::string(beep_last_error());
-		beep_batch_destroy(q);
-		return s == BEEP_OK ? s : fail(s, e);
-	};
+	// reuse the prepared batch when the request has the same shape: re-stage its tables
+	const int slot = b.L_out ? 1 : 0;
+	beep_batch *q = c->q[slot];
+	beep_status st = BEEP_OK;
+	if (q && c->q_ngroup[slot] == b.ngroup && c->q_go[slot] == (b.group_of != nullptr) &&
+	    c->q_so[slot] == (b.stream_of != nullptr)) {
+		q->b = b;
+		q->bd.k0 = (uint32_t)b.seed;
+		q->bd.k1 = (uint32_t)(b.seed >> 32);
+		st = beep_batch_stage(q);
+		if (st != BEEP_OK) {
+			beep_batch_destroy(q);
+			c->q[slot] = nullptr;
+			return st;
+		}
+	} else {
+		if (q) beep_batch_destroy(q);
+		c->q[slot] = nullptr;
+		st = batch_create_internal(m, &b, false, &q, false, false);
+		if (st != BEEP_OK) return st;
+		c->q[slot] = q;
+		c->q_ngroup[slot] = b.ngroup;
+		c->q_go[slot] = b.group_of != nullptr;
+		c->q_so[slot] = b.stream_of != nullptr;
+	}
+	auto done = [&](beep_status s) { return s; };
 	const bool mask = mode == 1 && !simu_all && r->simu;
 	Layout L;
 	const size_t o_cur = L.add((size_t)P), o_simu = L.add(mask ? (size_t)P * m->S * m->A : 0),
@@ -154,6 +176,8 @@ BEEP_API beep_status beep_mbp_destroy(beep_mbp_chains *c)
 		cudaSetDevice(c->m->device);
 		cudaStreamSynchronize(c->m->stream);
 	}
+	for (auto *q : c->q)
+		if (q) beep_batch_destroy(q);
 	c->traj.release();
 	c->aux.release();
 	delete c;

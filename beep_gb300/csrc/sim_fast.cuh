@@ -397,30 +397,67 @@ __device__ __forceinline__ void slice_store(const ModelDev &m, FastSmem &s, cons
 	if (tid == 0) s.dgeo[buf] = r.d;
 }
 
-// Binomial(n, p) thinning on the keyed stream of the FP64 form: FP32
-// inversion below n q = 10 (the same word as the FP64 draw); above, the FP64
-// BTRS draw itself (rare: a large count thinned by a mean that fell).
+// Stirling remainder of log Gamma(z): log Gamma(z) - ((z - 1/2) log z - z + log(2 pi)/2)
+__device__ __forceinline__ float stirling_rem(float z)
+{
+	const float iz = __fdividef(1.f, z), iz2 = iz * iz;
+	return iz * (0.083333333f - iz2 * (0.0027777778f - iz2 * 0.00079365079f));
+}
+
+// Binomial(n, p) thinning in FP32 on the keyed stream of the FP64 form (same
+// counters and words): inversion below n q = 10, BTRS (Hoermann 1993) above.
+// The BTRS acceptance test log f(k)/f(m) is formed without cancellation as
+//   -(m+1/2) log1p(d/(m+1)) - (n-m+1/2) log1p(-d/(n-m+1))
+//   + d log((n-k+1) q / ((k+1) (1-q))) + Stirling remainders,  d = k - m,
+// instead of differences of large log-factorials.
 __device__ __forceinline__ int32_t binomial_fp32(float p, int32_t n, uint32_t k0, uint32_t k1, uint32_t col, uint32_t tr,
                                                  uint32_t sett, uint32_t stream)
 {
 	if (n <= 0 || !(p > 0.f)) return 0;
 	if (p >= 1.f) return n;
 	const bool flip = p > 0.5f;
-	const float q = flip ? 1.f - p : p;
+	const float q = flip ? 1.f - p : p, qc = 1.f - q;
 	const float nd = (float)n;
-	if (!(nd * q < 10.f)) return binomial_fp64((double)p, n, k0, k1, col, tr, sett, stream);
-	const U4 r = philox10(U4{col, sett, stream, (PURPOSE_THIN << 24) | (tr >> 2)}, k0, k1);
-	const float u = u01_f(word_of(r, tr & 3u));
-	const float ratio = q / (1.f - q);
-	float f = expf(nd * log1pf(-q));
-	float F = f;
 	int32_t k = 0;
-	while (u > F && k < n) {
-		f = f * ratio * (float)(n - k) / (float)(k + 1);
-		k++;
-		const float Fn = F + f;
-		if (Fn == F) break;                           // FP32 tail exhausted
-		F = Fn;
+	if (nd * q < 10.f) {
+		const U4 r = philox10(U4{col, sett, stream, (PURPOSE_THIN << 24) | (tr >> 2)}, k0, k1);
+		const float u = u01_f(word_of(r, tr & 3u));
+		const float ratio = q / qc;
+		float f = expf(nd * log1pf(-q));
+		float F = f;
+		while (u > F && k < n) {
+			f = f * ratio * (float)(n - k) / (float)(k + 1);
+			k++;
+			const float Fn = F + f;
+			if (Fn == F) break;                       // FP32 tail exhausted
+			F = Fn;
+		}
+	} else {
+		const float spq = sqrtf(nd * q * qc);
+		const float b = 1.15f + 2.53f * spq;
+		const float a = -0.0873f + 0.0248f * b + 0.01f * q;
+		const float c = nd * q + 0.5f;
+		const float alpha = (2.83f + __fdividef(5.1f, b)) * spq;
+		const float vr = 0.92f - __fdividef(4.2f, b);
+		const float m = floorf((nd + 1.f) * q);
+		const float em = stirling_rem(m + 1.f) + stirling_rem(nd - m + 1.f);
+		k = -1;
+		for (uint32_t it = 0; it < 65536u; it++) {
+			const U4 r = philox10(U4{col, sett, stream, (PURPOSE_BTRS << 24) | (tr << 16) | it}, k0, k1);
+			const float U = u01_f(r.x) - 0.5f;
+			const float V = u01_f(r.y);
+			const float us = 0.5f - fabsf(U);
+			const float kd = floorf((__fdividef(2.f * a, us) + b) * U + c);
+			if (kd < 0.f || kd > nd) continue;
+			if (us >= 0.07f && V <= vr) { k = (int32_t)kd; break; }
+			const float lhs = __logf(V * alpha / (__fdividef(a, us * us) + b));
+			const float d = kd - m;
+			const float rhs = -(m + 0.5f) * log1pf(d / (m + 1.f)) - (nd - m + 0.5f) * log1pf(-d / (nd - m + 1.f)) +
+			                  d * __logf((nd - kd + 1.f) * q / ((kd + 1.f) * qc)) + em - stirling_rem(kd + 1.f) -
+			                  stirling_rem(nd - kd + 1.f);
+			if (lhs <= rhs) { k = (int32_t)kd; break; }
+		}
+		if (k < 0) return -1;
 	}
 	return flip ? n - k : k;
 }

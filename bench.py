@@ -247,6 +247,82 @@ def profile_traffic(kind: str, P: int):
     return float(m.group(1)) * P if m else None
 
 
+def run_mbp_chains(sweeps: int, seed: int, nchain: int = 128, plain_sweeps: int = 1):
+    """MBP chains of uneven size: nchain chains on each of the models 20x2,
+    80x4, 200x6 and 350x10 (areas x ages, dt 0.5, 200 days, weekly hospital
+    populations).  A sweep is one coupled proposal per chain (parameters
+    perturbed by a factor exp(N(0, 0.05)) per parameter), the FP64 acceptance
+    ratio exp(L' - L) (uniform priors, invT = 1) and the accept step.  The four
+    models' proposals run concurrently (one host thread and stream each)."""
+    import threading
+    from beep_gb300 import capi, model_builder as mb, synth
+    rng = np.random.default_rng(seed)
+    models = []
+    for (A, G) in synth.MBP_SIZES:
+        w = synth.mbp_chain_model(A, G)
+        arr0 = mb.model_arrays(w)
+        m0 = capi.Model(arr0)
+        dm0 = capi.DeviceModel(m0)
+        truth = dm0.simulate(capi.Batch(m0, [capi.Tables(mb.param_tables(w))], 1, seed ^ A, want_transnum=True,
+                                        want_pop_traj=True, want_L=False, form=capi.FORM_FAST))
+        dm0.close()
+        y, sd = mb.observed_from_trajectory(arr0, truth.transnum[0], truth.pop_traj[0], rng)
+        arr = dict(arr0)
+        arr["obs_value"], arr["obs_sd"] = y, sd
+        m = capi.Model(arr)
+        th = np.stack([rng.uniform(2.2, 2.8, nchain), rng.uniform(3.6, 4.4, nchain), rng.uniform(4.5, 5.5, nchain)], 1)
+        props = []
+        for k in range(sweeps + plain_sweeps):
+            tp = th * np.exp(rng.normal(0, 0.05, th.shape))
+            props.append([capi.Tables(t) for t in mb.param_tables_batch(w, tp[:, 0], tp[:, 1], tp[:, 2])])
+        t0 = [capi.Tables(t) for t in mb.param_tables_batch(w, th[:, 0], th[:, 1], th[:, 2])]
+        models.append(dict(w=w, m=m, t0=t0, props=props, units=nchain * A * G * m.ndivision))
+    units = sum(x["units"] for x in models)
+    out = {}
+    for form, nsw in ((capi.FORM_FAST, sweeps), (capi.FORM_PLAIN_FP64, plain_sweeps)):
+        if nsw <= 0:
+            continue
+        for x in models:
+            x["dm"] = capi.DeviceModel(x["m"])
+            x["ch"] = capi.MbpChains(x["dm"], nchain, form=form)
+            x["L"] = x["ch"].initialise(x["t0"], seed, stream_of=np.arange(nchain), group_of=np.arange(nchain))
+        acc = []
+        times = []
+        base = 0 if form == capi.FORM_FAST else sweeps
+        for k in range(nsw):
+            res = {}
+
+            def work(i, x):
+                res[i] = x["ch"].propose(x["props"][base + k], seed, group_of=np.arange(nchain),
+                                         stream_of=np.arange(nchain) + (k + 1) * nchain,
+                                         inf_update=capi.INF_DIF_UPDATE)
+            t0 = time.perf_counter()
+            th_ = [threading.Thread(target=work, args=(i, x)) for i, x in enumerate(models)]
+            for t in th_:
+                t.start()
+            for t in th_:
+                t.join()
+            for i, x in enumerate(models):
+                al = np.minimum(1.0, np.exp(np.clip(res[i] - x["L"], -700, 0)))
+                ok = rng.random(nchain) < al
+                x["ch"].accept(ok.astype(np.uint8))
+                x["L"] = np.where(ok, res[i], x["L"])
+                acc.append(ok.mean())
+            times.append(time.perf_counter() - t0)
+        for x in models:
+            x["ch"].close()
+            x["dm"].close()
+        t = statistics.mean(times)
+        out["fast" if form == capi.FORM_FAST else "plain_fp64"] = {
+            "value": units / t, "unit": "chain.area.group.steps/s", "ms_per_sweep": t * 1e3, "sweeps": nsw,
+            "acceptance": float(np.mean(acc))}
+    out.update({"workload": "mbp_chains_uneven", "chains": 4 * nchain,
+                "models": [f"{A}x{G}" for (A, G) in synth.MBP_SIZES], "steps": models[0]["m"].ndivision,
+                "units_per_sweep": units, "data": "synthetic, weekly hospital populations",
+                "timing": "host wall clock per sweep (4 concurrent model streams, proposals + FP64 acceptance)"})
+    return out
+
+
 def dist_setup(args):
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -386,6 +462,9 @@ def run_ours(args, rank, ws, dist):
     hbm, hbm_kind = peaks()
     achieved = BYTES_PER_UNIT * units / t_dev / 1e9
     traffic = profile_traffic(args.workload, P) if args.form == "fast" else None
+    mbp = None
+    if args.mbp_sweeps > 0 and ws == 1:
+        mbp = run_mbp_chains(args.mbp_sweeps, args.seed + 99)
     serving = None
     if args.serve_requests > 0 and ws == 1:
         serving = run_serving(args.serve_requests, 200.0, args.seed + 4242, 200 << 30, 8)
@@ -413,6 +492,7 @@ def run_ours(args, rank, ws, dist):
                      "algorithmic_bytes": f"{BYTES_PER_UNIT} B x {units} units per launch"},
         "cpu_baseline": cpu,
         "serving": serving,
+        "mbp_chains": mbp,
     }
     print(json.dumps(line))
     db.close()
@@ -435,6 +515,8 @@ def main():
                     help="force of infection of the fast form (library option fast_foi)")
     ap.add_argument("--plain-particles", type=int, default=1024)
     ap.add_argument("--plain-steps", type=int, default=0, help="time the plain form over this many steps (0: all)")
+    ap.add_argument("--mbp-sweeps", type=int, default=3,
+                    help="sweeps of the MBP-chain workload (4 x 128 chains of uneven size) after the main measurement")
     ap.add_argument("--serve-requests", type=int, default=32,
                     help="requests of the serving stream (Poisson arrivals at 200/s) after the main measurement")
     args = ap.parse_args()
