@@ -46,6 +46,7 @@ class ParamTables(C.Structure):
         ("areafactor", _f64p), ("Ntime", _f64p), ("geo_spline", _f64p),
         ("nefoi", C.c_int32), ("efoi_spline", _f64p), ("efoi_agedist", _f64p), ("efoi_ref", _i32p),
         ("nobs_spline", C.c_int32), ("obs_spline", _f64p),
+        ("efoi_mult", _f64p), ("transmean_mult", _f64p),
     ]
 
 
@@ -78,6 +79,8 @@ class MbpRequest(C.Structure):
 
 INF_UPDATE = 0
 INF_DIF_UPDATE = 1
+
+ABI_VERSION = 2   # BEEP_GPU_ABI_VERSION of include/beep_gpu.h these structures mirror
 
 REQ_LIKELIHOOD, REQ_SCENARIO, REQ_PREDICTION = 0, 1, 2
 
@@ -171,6 +174,10 @@ class Tables:
             setattr(self.st, k, _ptr(self.arr[k], C.c_int32))
         for k in TABLE_F64_ARRAYS:
             setattr(self.st, k, _ptr(self.arr[k], C.c_double))
+        for k in ("efoi_mult", "transmean_mult"):        # prediction modifications (optional)
+            if arrays.get(prefix + k) is not None:
+                self.arr[k] = _f64(arrays[prefix + k]).reshape(-1)
+                setattr(self.st, k, _ptr(self.arr[k], C.c_double))
         self.st.nbeta_row = int(self.shapes["beta_rows"][0])
         self.st.nefoi = int(self.shapes["efoi_spline"][0])
         self.st.nobs_spline = int(self.shapes["obs_spline"][0]) if len(self.shapes["obs_spline"]) == 2 else 0

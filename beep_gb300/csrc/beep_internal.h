@@ -50,6 +50,7 @@ struct GroupDir {
 	int64_t transrate, susceptibility, infectivity, infdif, beta_rows, areafactor, Ntime, geo_spline,
 	    efoi_spline, efoi_agedist, obs_spline;          // double pool offsets
 	int64_t beta_row_of, efoi_ref;                      // int pool offsets
+	int64_t efoi_mult, tm_mult;                         // prediction multipliers (double pool), -1 if absent
 };
 
 struct BatchDev {

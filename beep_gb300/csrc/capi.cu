@@ -432,6 +432,8 @@ beep_status pack_tables(const beep_model *m, const beep_sim_batch *b, TablePacke
 		dd.obs_spline = t.nobs_spline > 0 && t.obs_spline ? pk.addf(t.obs_spline, (size_t)t.nobs_spline * S) : 0;
 		dd.beta_row_of = pk.addi(t.beta_row_of, NS * A);
 		dd.efoi_ref = pk.addi(t.efoi_ref, NS * A);
+		dd.efoi_mult = t.efoi_mult ? pk.addf(t.efoi_mult, S * A * NS) : -1;
+		dd.tm_mult = t.transmean_mult ? pk.addf(t.transmean_mult, S * A * T * DP) : -1;
 	}
 	return BEEP_OK;
 }

@@ -53,6 +53,8 @@ extern "C" BEEP_API beep_status beep_simulate_plain_noalloc(beep_model *m, const
 	if (nparticle <= 0) return fail(BEEP_BAD_INPUT, "nparticle must be positive");
 	if (ti < 0 || tf <= ti || tf > m->S) return fail(BEEP_BAD_INPUT, "step range must satisfy 0 <= ti < tf <= ndivision");
 	if (ti > 0 && !pop_in) return fail(BEEP_BAD_INPUT, "pop_in is required when ti > 0");
+	if (tab->efoi_mult || tab->transmean_mult)
+		return fail(BEEP_BAD_INPUT, "prediction multipliers are not taken by the allocation-free entry point");
 	if (!tab->transrate || !tab->susceptibility || !tab->infectivity || !tab->beta_rows || !tab->beta_row_of ||
 	    !tab->areafactor || !tab->Ntime || !tab->geo_spline || !tab->efoi_spline || !tab->efoi_agedist || !tab->efoi_ref)
 		return fail(BEEP_BAD_INPUT, "missing table");
@@ -103,6 +105,8 @@ extern "C" BEEP_API beep_status beep_simulate_plain_noalloc(beep_model *m, const
 	dir.efoi_spline = fslot((size_t)tab->nefoi * S);
 	dir.efoi_agedist = fslot((size_t)tab->nefoi * G);
 	dir.obs_spline = fslot((size_t)tab->nobs_spline * S);
+	dir.efoi_mult = -1;
+	dir.tm_mult = -1;
 	dir.beta_row_of = 0;
 	dir.efoi_ref = (int64_t)align_up(NS * A, 8);
 	const size_t ni = (size_t)dir.efoi_ref + NS * A;

@@ -362,6 +362,7 @@ __device__ bool foi_tensor_collect(tc::Foi &f, uint32_t taddr, uint32_t step_no,
 struct Tabs {
 	const float *rate, *sus, *inf, *beta_rows, *areafactor, *Ntime, *geo, *efoi_spline, *efoi_age, *obs_spline;
 	const int32_t *beta_row_of, *efoi_ref;
+	const float *efoi_mult, *tm_mult;       // prediction modifications, or null
 };
 
 // Per-step table slices: beta*areafactor and the external force of infection
@@ -383,6 +384,7 @@ __device__ __forceinline__ SliceRegs slice_load(const ModelDev &m, const Tabs &t
 		r.be = __ldg(tb.beta_rows + (size_t)s.brow[tid] * m.S + sett) *
 		       __ldg(tb.areafactor + (size_t)(sett / m.div_per_time) * A + c);
 		r.et = __ldg(tb.efoi_spline + (size_t)s.eref[tid] * m.S + sett) * m.inv_popsize_f;
+		if (tb.efoi_mult) r.et *= __ldg(tb.efoi_mult + ((size_t)sett * A + c) * m.NS + tid / A);
 	}
 	if (tid < G * G) r.N = __ldg(tb.Ntime + (size_t)sett * G * G + tid);
 	if (tid == 0) r.d = __ldg(tb.geo + sett);
@@ -484,6 +486,8 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 		tb.geo = fp + dir.geo_spline; tb.efoi_spline = fp + dir.efoi_spline; tb.efoi_age = fp + dir.efoi_agedist;
 		tb.obs_spline = fp + dir.obs_spline;
 		tb.beta_row_of = b.ipool + dir.beta_row_of; tb.efoi_ref = b.ipool + dir.efoi_ref;
+		tb.efoi_mult = dir.efoi_mult >= 0 ? fp + dir.efoi_mult : nullptr;
+		tb.tm_mult = dir.tm_mult >= 0 ? fp + dir.tm_mult : nullptr;
 	}
 	int32_t *status = b.status + p;
 	// MBP chains (CH): slot of the current state and of the state written; chain
@@ -681,6 +685,7 @@ __global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const
 						const float popu = (float)pc[s.from[tr] * ncol + col];
 						mv[tr] = popu <= 0.f ? 0.f : dt * popu * s.rate[tr * DP + dp];
 					}
+					if (tb.tm_mult) mv[tr] *= __ldg(tb.tm_mult + ((size_t)sett * A + c) * T * DP + tr * DP + dp);
 				}
 			}
 			if (pn != pc)

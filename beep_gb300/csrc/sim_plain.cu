@@ -104,6 +104,8 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 	const double *Ntime = fp + dir.Ntime, *geo = fp + dir.geo_spline, *efoi_spline = fp + dir.efoi_spline;
 	const double *efoi_age = fp + dir.efoi_agedist, *obs_spline = fp + dir.obs_spline;
 	const int32_t *beta_row_of = ip + dir.beta_row_of, *efoi_ref = ip + dir.efoi_ref;
+	const double *efoi_mult = dir.efoi_mult >= 0 ? fp + dir.efoi_mult : nullptr;
+	const double *tm_mult = dir.tm_mult >= 0 ? fp + dir.tm_mult : nullptr;
 
 	// MBP chains: slot of the current state and of the state being written
 	const int mode = b.mode;
@@ -249,7 +251,8 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 					double be = beta_rows[(size_t)beta_row_of[st * A + c] * m.S + sett];
 					be *= areafactor[(size_t)(sett / m.div_per_time) * A + c];
 					const int ei = efoi_ref[st * A + c];
-					const double et = efoi_spline[(size_t)ei * m.S + sett] / m.popsize;
+					double et = efoi_spline[(size_t)ei * m.S + sett] / m.popsize;
+					if (efoi_mult) et *= efoi_mult[((size_t)sett * A + c) * NS + st];
 					const double eta = et * efoi_age[(size_t)ei * G + a];
 					mean = m.dt * popu * sus[dp] * (be * NMI[((size_t)st * A + c) * G + a] + eta);
 				}
@@ -257,6 +260,7 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 				const double popu = (double)pop_cur[((size_t)c * C + m.trans_from[tr]) * DP + dp];
 				mean = popu <= 0 ? 0 : m.dt * popu * transrate[(size_t)tr * DP + dp];
 			}
+			if (tm_mult) mean *= tm_mult[(size_t)sett * tnsz + cell];   // prediction modifications
 			if (mode == 2) {                    // State::likelihood term of the fixed count
 				if (mean != mean) set_status(status, BEEP_NAN_RATE);
 				const double lp = poisson_lp(tn[cell], mean);

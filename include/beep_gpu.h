@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define BEEP_GPU_ABI_VERSION 1
+#define BEEP_GPU_ABI_VERSION 2
 
 #if defined(__GNUC__)
 #define BEEP_API __attribute__((visibility("default")))
@@ -130,6 +130,12 @@ typedef struct beep_param_tables {
 	const int32_t *efoi_ref;      /* [nstrain][narea] Model::efoi_spl_ref */
 	int32_t nobs_spline;
 	const double *obs_spline;     /* [nobs_spline][ndivision] factor splines of observations */
+	/* PREDICTION-mode model modifications (ModelMod, src/model.cc:1446-1585), NULL when
+	 * absent: the external force of infection of area c, strain st at step s is
+	 * multiplied by efoi_mult[s][c][st] and every transition mean by
+	 * transmean_mult[s][c][tr][dp] (State::set_transmean, src/state.cc:415,446-453) */
+	const double *efoi_mult;      /* [ndivision][narea][nstrain] or NULL */
+	const double *transmean_mult; /* [ndivision][narea][ntrans][ndemocatpos] or NULL */
 } beep_param_tables;
 
 /* Arithmetic form of the kernels. */

@@ -289,6 +289,7 @@ static int transmean_area(const beep_model_desc *m, const beep_param_tables *tb,
 		be *= tb->areafactor[(size_t)(sett / m->division_per_time) * A + c];
 		int32_t ei = tb->efoi_ref[st * A + c];
 		double et = tb->efoi_spline[(size_t)ei * m->ndivision + sett] / m->popsize;
+		if (tb->efoi_mult) et *= tb->efoi_mult[((size_t)sett * A + c) * NS + st];   /* src/state.cc:415 */
 		for (int32_t a = 0; a < G; a++) w->eta[a] = et * tb->efoi_agedist[(size_t)ei * G + a];
 		int32_t dpp = st * DPS;
 		for (int32_t dp = 0; dp < DPS; dp++) {
@@ -311,6 +312,10 @@ static int transmean_area(const beep_model_desc *m, const beep_param_tables *tb,
 			if (popu <= 0) w->tmean[tr * DP + dp] = 0;
 			else w->tmean[tr * DP + dp] = m->dt * popu * tb->transrate[(size_t)tr * DP + dp];
 		}
+	}
+	if (tb->transmean_mult) {                            /* src/state.cc:446-453 */
+		const double *mu = tb->transmean_mult + ((size_t)sett * A + c) * T * DP;
+		for (int32_t k = 0; k < T * DP; k++) w->tmean[k] *= mu[k];
 	}
 	return BEEP_OK;
 }

@@ -123,3 +123,37 @@ def test_particle_filter_fast_form_and_oracle(built):
     for ti, tf in m.sections:
         assert linf[ti:tf].sum() > 0
     dm.close()
+
+
+def test_prediction_multipliers_match_oracle(built):
+    """PREDICTION-mode modifications (efoi_mult, transmean_mult; src/state.cc:415,
+    446-453): the plain form equals the oracle restatement bit for bit, the fast
+    form follows it, and all-ones multipliers change nothing."""
+    from oracle_lib import oracle_simulate
+    b, m, tabs, seed = load("c0_sim")
+    rng = np.random.default_rng(11)
+    S, A, T, DP, NS = m.ndivision, m.narea, m.ntrans, m.ndemocatpos, m.nstrain
+    base = {k: v for k, v in b.items() if k.startswith("g0.")}
+    arr = {k[3:]: v for k, v in base.items()}
+    arr["efoi_mult"] = rng.uniform(0.5, 1.5, (S, A, NS))
+    tm = np.ones((S, A, T, DP))
+    tm[S // 3:] *= rng.uniform(0.6, 1.1, (S - S // 3, A, T, DP))   # an intervention from a third of the horizon
+    arr["transmean_mult"] = tm
+    tmod = capi.Tables(arr)
+    P = 24
+    dm = capi.DeviceModel(m)
+    g = dm.simulate(capi.Batch(m, [tmod], P, seed, want_transnum=True))
+    o = oracle_simulate(m, capi.Batch(m, [tmod], P, seed, want_transnum=True))
+    assert np.array_equal(g.transnum, o.transnum)
+    np.testing.assert_allclose(g.L, o.L, rtol=1e-12)
+    plain0 = dm.simulate(capi.Batch(m, tabs, P, seed, want_transnum=True))
+    assert not np.array_equal(g.transnum, plain0.transnum)          # the modification acts
+    ones = dict(arr)
+    ones["efoi_mult"] = np.ones((S, A, NS))
+    ones["transmean_mult"] = np.ones((S, A, T, DP))
+    u = dm.simulate(capi.Batch(m, [capi.Tables(ones)], P, seed, want_transnum=True))
+    assert np.array_equal(u.transnum, plain0.transnum)
+    f = dm.simulate(capi.Batch(m, [tmod], P, seed, want_transnum=True, form=capi.FORM_FAST))
+    same = np.array([np.array_equal(f.transnum[p], g.transnum[p]) for p in range(P)])
+    assert same.mean() >= 0.6, same.mean()
+    dm.close()
