@@ -323,6 +323,21 @@ def run_mbp_chains(sweeps: int, seed: int, nchain: int = 128, plain_sweeps: int 
     return out
 
 
+def max_over_ranks(dist, *times):
+    """The slowest rank's times (every rank gets them); identity on one rank."""
+    if dist is None:
+        return times
+    import torch
+    tt = torch.tensor(list(times), dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return tuple(float(x) for x in tt)
+
+
+def units_total(units_per_rank: int, ws: int) -> int:
+    """Whole-job units of a weak-scaling run: every rank processes its own batch."""
+    return units_per_rank * ws
+
+
 def dist_setup(args):
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -437,11 +452,7 @@ def run_ours(args, rank, ws, dist):
         db.run_graph()                               # re-stage tables, replay copies + kernel, unpack L
         e2e_times.append(time.perf_counter() - t0)
     t_e2e = statistics.mean(e2e_times)
-    if dist is not None:
-        import torch
-        tt = torch.tensor([t_dev, t_e2e], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_dev, t_e2e = float(tt[0]), float(tt[1])
+    t_dev, t_e2e = max_over_ranks(dist, t_dev, t_e2e)
     assert np.all(np.isfinite(batch.L))
     # the plain FP64 form on a subset of the particles (same workload, units/s)
     plain = None
@@ -475,7 +486,7 @@ def run_ours(args, rank, ws, dist):
         cpu = {"value": v, "unit": "particle.area.group.steps/s", "cores": nthreads, "kind": "port",
                "sample": f"{n2} of {P} particles (full 360-step horizon + log-likelihood), {dt:.1f} s"}
     line = {
-        "metric": METRIC, "value": units * ws / t_dev, "unit": "particle.area.group.steps/s", "n_gpus": ws,
+        "metric": METRIC, "value": units_total(units, ws) / t_dev, "unit": "particle.area.group.steps/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_dev * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.form == "fast" else "f64",
         "data": "synthetic", "config": workload_config(args.workload, m, P),
@@ -484,7 +495,7 @@ def run_ours(args, rank, ws, dist):
         "plain_fp64": plain,
         "loglik_evals_per_s": P * ws / t_dev,
         "clocks": clocks,
-        "e2e": {"value": units * ws / t_e2e, "unit": "particle.area.group.steps/s", "h2d_bytes_per_step": h2d,
+        "e2e": {"value": units_total(units, ws) / t_e2e, "unit": "particle.area.group.steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e * 1e3},
         "gpu_launches": args.steps * db.launches(),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
