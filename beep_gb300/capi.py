@@ -80,13 +80,14 @@ class MbpRequest(C.Structure):
 INF_UPDATE = 0
 INF_DIF_UPDATE = 1
 
-ABI_VERSION = 2   # BEEP_GPU_ABI_VERSION of include/beep_gpu.h these structures mirror
+ABI_VERSION = 3   # BEEP_GPU_ABI_VERSION of include/beep_gpu.h these structures mirror
 
-REQ_LIKELIHOOD, REQ_SCENARIO, REQ_PREDICTION = 0, 1, 2
+REQ_LIKELIHOOD, REQ_SCENARIO, REQ_PREDICTION, REQ_PF_LIKELIHOOD = 0, 1, 2, 3
 
 
 class Request(C.Structure):
-    _fields_ = [("kind", C.c_int32), ("model", C.POINTER(ModelDesc)), ("batch", C.POINTER(SimBatch))]
+    _fields_ = [("kind", C.c_int32), ("model", C.POINTER(ModelDesc)), ("batch", C.POINTER(SimBatch)),
+                ("pf", C.POINTER(PFRequest))]
 
 
 class RequestStats(C.Structure):
@@ -567,14 +568,42 @@ class Server:
         self._live[t.value] = (model, batch, r)
         return t.value
 
+    def submit_pf(self, model: Model, tables: Tables, N: int, seed: int, resample_stream: int, invT: float,
+                  sections, form: int = FORM_PLAIN_FP64, lineage: bool = False) -> int:
+        """Queues a particle-filter likelihood request; wait() returns a dict with loglik,
+        loglik_section, L [nsec][N], ancestors [nsec][N] (and lineage)."""
+        ti = np.array([a for a, _ in sections], np.int32)
+        tf = np.array([b for _, b in sections], np.int32)
+        ns = len(sections)
+        out = {"loglik": np.zeros(1), "loglik_section": np.zeros(ns), "L": np.zeros((ns, N)),
+               "ancestors": np.zeros((ns, N), np.int32)}
+        if lineage:
+            out["lineage"] = np.zeros((model.ndivision, model.narea, model.ntrans, model.ndemocatpos), np.int32)
+        r = PFRequest()
+        r.nparticle, r.tables, r.seed, r.resample_stream, r.invT = N, C.pointer(tables.st), seed, resample_stream, invT
+        r.nsection, r.section_ti, r.section_tf, r.form = ns, _ptr(ti, C.c_int32), _ptr(tf, C.c_int32), form
+        r.loglik_out, r.loglik_section_out = _ptr(out["loglik"], C.c_double), _ptr(out["loglik_section"], C.c_double)
+        r.L_out, r.ancestors_out = _ptr(out["L"], C.c_double), _ptr(out["ancestors"], C.c_int32)
+        r.lineage_transnum_out = _ptr(out.get("lineage"), C.c_int32)
+        rq = Request()
+        rq.kind = REQ_PF_LIKELIHOOD
+        rq.model = C.pointer(model.desc)
+        rq.pf = C.pointer(r)
+        t = C.c_uint64()
+        check(lib().beep_serve_submit(self.h, C.byref(rq), C.byref(t)))
+        self._live[t.value] = (model, tables, r, rq, ti, tf, out)
+        return t.value
+
     def poll(self, ticket: int) -> bool:
         d = C.c_int32()
         check(lib().beep_serve_poll(self.h, ticket, C.byref(d)))
         return bool(d.value)
 
-    def wait(self, ticket: int, timeout_s: float = -1.0) -> Batch:
+    def wait(self, ticket: int, timeout_s: float = -1.0):
+        """The request's Batch (simulation kinds) or output dict (particle filter) once done."""
         check(lib().beep_serve_wait(self.h, ticket, timeout_s))
-        return self._live[ticket][1]
+        live = self._live[ticket]
+        return live[-1] if isinstance(live[-1], dict) else live[1]
 
     def stats(self, ticket: int) -> dict:
         st = RequestStats()

@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -41,6 +42,9 @@ struct Req {
 	int32_t kind = 0;
 	beep_model_desc desc{};
 	beep_sim_batch batch{};
+	beep_pf_request pf{};               // BEEP_REQ_PF_LIKELIHOOD
+	std::thread pf_thread;              // runs the filter (sections with host steps between them)
+	std::atomic<bool> pf_finished{false};
 	size_t est = 0, bytes = 0;
 	beep_model *m = nullptr;
 	beep_batch *q = nullptr;
@@ -88,6 +92,25 @@ size_t estimate_bytes(const beep_model_desc &d, const beep_sim_batch &b)
 	return model + in + work + out + 5 * 256;
 }
 
+// Device bytes of a particle-filter request: the model, one prepared batch
+// per section, the carried populations and weights, and the lineage counts.
+size_t estimate_pf_bytes(const beep_model_desc &d, const beep_pf_request &r)
+{
+	beep_sim_batch b{};
+	b.nparticle = r.nparticle;
+	b.ngroup = 1;
+	b.groups = r.tables;
+	b.ti = 0;
+	b.tf = d.ndivision;
+	b.form = r.form;
+	double L = 0;
+	b.L_out = &L;
+	const size_t N = r.nparticle, popsz = (size_t)d.narea * d.ncomp * d.ndemocatpos;
+	const size_t tnsz = (size_t)d.narea * d.ntrans * d.ndemocatpos;
+	return 2 * estimate_bytes(d, b) + N * (8 * popsz + 64 + 12 * (size_t)r.nsection) +
+	       (r.lineage_transnum_out ? 4 * tnsz * (size_t)d.ndivision * N : 0);
+}
+
 }  // namespace
 
 struct beep_server {
@@ -113,6 +136,7 @@ namespace {
 
 void release_request_memory(Req *r)
 {
+	if (r->pf_thread.joinable()) r->pf_thread.join();
 	if (r->q) beep_batch_destroy(r->q);
 	if (r->m) beep_model_destroy(r->m);
 	if (r->ev_start) cudaEventDestroy(r->ev_start);
@@ -122,10 +146,45 @@ void release_request_memory(Req *r)
 	r->ev_start = r->ev_end = nullptr;
 }
 
+// A particle-filter request runs on its own host thread: the filter steps
+// section by section with host work in between (beep_pf_loglik), so it cannot
+// be one enqueue; its kernels still run on the request's own stream beside
+// the others'.
+void run_pf_request(beep_server *s, Req *r)
+{
+	cudaSetDevice(s->device);
+	beep_status st = beep_model_create(&r->desc, &r->m);
+	if (st == BEEP_OK) {
+		cudaEventCreate(&r->ev_start);
+		cudaEventCreate(&r->ev_end);
+		cudaEventRecord(r->ev_start, r->m->stream);
+		st = beep_pf_loglik(r->m, &r->pf);
+		cudaEventRecord(r->ev_end, r->m->stream);
+		cudaEventSynchronize(r->ev_end);
+		float a = 0, b = 0;
+		if (cudaEventElapsedTime(&a, s->ev0, r->ev_start) == cudaSuccess &&
+		    cudaEventElapsedTime(&b, s->ev0, r->ev_end) == cudaSuccess) {
+			r->g_start = a * 1e-3;
+			r->g_end = b * 1e-3;
+		}
+	}
+	if (st != BEEP_OK) {
+		r->status = st;
+		r->err = beep_last_error();
+	}
+	r->pf_finished.store(true);
+	s->cv_work.notify_all();
+}
+
 // Creates the request's model and batch and enqueues its work (worker thread,
 // server lock not held).
 void start_request(beep_server *s, Req *r)
 {
+	if (r->kind == BEEP_REQ_PF_LIKELIHOOD) {
+		r->bytes = r->est;
+		r->pf_thread = std::thread(run_pf_request, s, r);
+		return;
+	}
 	beep_status st = beep_model_create(&r->desc, &r->m);
 	if (st == BEEP_OK) st = beep_batch_create(r->m, &r->batch, &r->q);
 	if (st == BEEP_OK) {
@@ -178,11 +237,14 @@ void worker_main(beep_server *s)
 		// retire completed requests
 		for (size_t i = 0; i < s->running.size();) {
 			Req *r = s->running[i];
-			cudaError_t e = r->ev_end ? cudaEventQuery(r->ev_end) : cudaSuccess;
+			const bool pf = r->kind == BEEP_REQ_PF_LIKELIHOOD;
+			cudaError_t e = pf ? (r->pf_finished.load() ? cudaSuccess : cudaErrorNotReady)
+			                   : r->ev_end ? cudaEventQuery(r->ev_end) : cudaSuccess;
 			if (e == cudaErrorNotReady) { i++; continue; }
 			s->running.erase(s->running.begin() + i);
 			lk.unlock();
-			if (r->status == BEEP_OK) finish_request(s, r, e);
+			if (pf) r->pf_thread.join();
+			else if (r->status == BEEP_OK) finish_request(s, r, e);
 			lk.lock();
 			r->t_done = s->now();
 			r->state = 2;
@@ -291,16 +353,40 @@ BEEP_API beep_status beep_server_destroy(beep_server *s)
 
 BEEP_API beep_status beep_serve_submit(beep_server *s, const beep_request *rq, uint64_t *ticket)
 {
-	if (!s || !rq || !rq->model || !rq->batch || !ticket) return fail(BEEP_BAD_INPUT, "null argument");
-	if (rq->kind < BEEP_REQ_LIKELIHOOD || rq->kind > BEEP_REQ_PREDICTION) return fail(BEEP_BAD_INPUT, "unknown request kind");
+	if (!s || !rq || !rq->model || !ticket) return fail(BEEP_BAD_INPUT, "null argument");
+	if (rq->kind < BEEP_REQ_LIKELIHOOD || rq->kind > BEEP_REQ_PF_LIKELIHOOD) return fail(BEEP_BAD_INPUT, "unknown request kind");
+	if (rq->model->narea <= 0 || rq->model->ndivision <= 0 || !rq->model->M_rowptr)
+		return fail(BEEP_BAD_INPUT, "bad model description");
+	if (rq->kind == BEEP_REQ_PF_LIKELIHOOD) {
+		if (!rq->pf || !rq->pf->tables || rq->pf->nparticle <= 0 || rq->pf->nsection <= 0 || !rq->pf->loglik_out)
+			return fail(BEEP_BAD_INPUT, "a particle-filter request needs tables, particles, sections and loglik_out");
+		Req *r = new Req();
+		r->kind = rq->kind;
+		r->desc = *rq->model;
+		r->pf = *rq->pf;
+		r->est = estimate_pf_bytes(r->desc, r->pf);
+		{
+			std::lock_guard<std::mutex> lk(s->mu);
+			if (s->stop) {
+				delete r;
+				return fail(BEEP_BAD_INPUT, "the server is shutting down");
+			}
+			r->id = s->next_id++;
+			r->t_submit = s->now();
+			s->reqs[r->id] = r;
+			s->queue.push_back(r);
+			*ticket = r->id;
+		}
+		s->cv_work.notify_all();
+		return BEEP_OK;
+	}
+	if (!rq->batch) return fail(BEEP_BAD_INPUT, "the request needs a batch");
 	const beep_sim_batch &b = *rq->batch;
 	if (b.nparticle <= 0 || b.ngroup <= 0 || !b.groups || b.ti < 0 || b.tf <= b.ti)
 		return fail(BEEP_BAD_INPUT, "nparticle, groups and a step range are required");
 	if (rq->kind == BEEP_REQ_LIKELIHOOD && !b.L_out) return fail(BEEP_BAD_INPUT, "a likelihood request needs L_out");
 	if (rq->kind == BEEP_REQ_PREDICTION && (b.ti == 0 || !b.pop_in))
 		return fail(BEEP_BAD_INPUT, "a prediction request continues given populations from ti > 0");
-	if (rq->model->narea <= 0 || rq->model->ndivision <= 0 || !rq->model->M_rowptr)
-		return fail(BEEP_BAD_INPUT, "bad model description");
 	Req *r = new Req();
 	r->kind = rq->kind;
 	r->desc = *rq->model;

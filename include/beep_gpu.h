@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define BEEP_GPU_ABI_VERSION 2
+#define BEEP_GPU_ABI_VERSION 3
 
 #if defined(__GNUC__)
 #define BEEP_API __attribute__((visibility("default")))
@@ -355,13 +355,16 @@ BEEP_API beep_status beep_mbp_read_state(beep_mbp_chains *chains, int32_t chain,
 typedef enum beep_request_kind {
 	BEEP_REQ_LIKELIHOOD = 0,   /* per-particle log-likelihood over [ti, tf) (PMCMC / ABC-SMC evaluations) */
 	BEEP_REQ_SCENARIO = 1,     /* trajectories from the initial state (mode=sim, src/simulate.cc:42-65) */
-	BEEP_REQ_PREDICTION = 2    /* continuation of given populations from ti (mode=prediction, src/simulate.cc:77-165) */
+	BEEP_REQ_PREDICTION = 2,   /* continuation of given populations from ti (mode=prediction, src/simulate.cc:77-165) */
+	BEEP_REQ_PF_LIKELIHOOD = 3 /* particle-filter likelihood estimate (PMCMC::obs_prob): the particles'
+	                              states stay on the device from section to section */
 } beep_request_kind;
 
 typedef struct beep_request {
 	int32_t kind;                    /* beep_request_kind */
 	const beep_model_desc *model;    /* copied at submit; its arrays must stay valid until the request is done */
-	const beep_sim_batch *batch;     /* copied at submit; its arrays must stay valid until the request is done */
+	const beep_sim_batch *batch;     /* copied at submit (NULL for BEEP_REQ_PF_LIKELIHOOD); arrays as above */
+	const beep_pf_request *pf;       /* copied at submit (BEEP_REQ_PF_LIKELIHOOD only); arrays as above */
 } beep_request;
 
 typedef struct beep_request_stats {

@@ -134,3 +134,28 @@ def test_bad_requests():
     srv.wait(t2, 60.0)
     np.testing.assert_allclose(ok.L, b["g0.L"][:4], rtol=1e-12)
     srv.close()
+
+
+def test_particle_filter_requests_alone_and_in_the_mix():
+    """Particle-filter requests (states resident on the device between
+    sections) give the estimate, section terms, ancestors and lineage they give
+    through beep_pf_loglik alone, while simulation requests run beside them."""
+    b, m, tabs, seed = load("c0_pf")
+    dm = capi.DeviceModel(m)
+    cases = [(128, seed + 1, capi.FORM_PLAIN_FP64), (256, seed + 2, capi.FORM_FAST), (64, seed + 3, capi.FORM_PLAIN_FP64)]
+    alone = [dm.pf_loglik(tabs[0], N, sd, 5, 1.0, m.sections, form=f, lineage=True) for N, sd, f in cases]
+    dm.close()
+    srv = capi.Server(8 << 30, 4)
+    ts = [srv.submit_pf(m, tabs[0], N, sd, 5, 1.0, m.sections, form=f, lineage=True) for N, sd, f in cases]
+    mw, tw = synthetic(60, 4, 60, 4, 20260410)
+    sims = [capi.Batch(mw, tw, 500, 30 + k, group_of=np.arange(500) % 4, form=capi.FORM_FAST) for k in range(3)]
+    tsim = [srv.submit(mw, bt, capi.REQ_LIKELIHOOD) for bt in sims]
+    for t, ref in zip(ts, alone):
+        out = srv.wait(t, 120.0)
+        assert out["loglik"][0] == ref[0]
+        assert np.array_equal(out["loglik_section"], ref[1])
+        assert np.array_equal(out["ancestors"], ref[3])
+        assert np.array_equal(out["lineage"], ref[4])
+    for t in tsim:
+        srv.wait(t, 120.0)
+    srv.close()
