@@ -27,6 +27,7 @@ UNITS = {
     "capi.cu": [],
     "sim_plain.cu": ["--fmad=false"],
     "sim_fast.cu": [],
+    "sim_fast_ctas.cu": [],
     "noalloc.cu": [],
     "pf.cu": [],
     "abc_weights.cu": [],

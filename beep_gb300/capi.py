@@ -264,6 +264,8 @@ def lib():
         L.beep_autotune.restype = C.c_int32
         L.beep_batch_foi_path.argtypes = [C.c_void_p]
         L.beep_batch_foi_path.restype = C.c_int32
+        L.beep_batch_ctas_per_sm.argtypes = [C.c_void_p]
+        L.beep_batch_ctas_per_sm.restype = C.c_int32
         L.beep_batch_launches.argtypes = [C.c_void_p]
         L.beep_batch_launches.restype = C.c_int32
         L.beep_batch_bytes.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
@@ -436,6 +438,10 @@ class DeviceBatch:
     def foi_path(self) -> int:
         """1 = FP32 SIMT force of infection, 2 = tensor cores, 0 = plain form."""
         return lib().beep_batch_foi_path(self.h)
+
+    def ctas_per_sm(self) -> int:
+        """Particles (CTAs) per SM the fast-form kernel is laid out for; 0 = plain form."""
+        return lib().beep_batch_ctas_per_sm(self.h)
 
     def close(self):
         if self.h:

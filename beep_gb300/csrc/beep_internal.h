@@ -105,21 +105,29 @@ struct BatchDev {
 	// memory starts at tc_smem_off bytes into the dynamic shared memory
 	int32_t foi_tc;
 	size_t tc_smem_off;
+	int32_t nt;                         // fast form: threads per CTA (0: fast_pick_threads)
+	int32_t ctas;                       // fast form, nt == kDualThreads: CTAs resident per SM (2..4)
 };
 
 // launchers
 int launch_sim_plain(const ModelDev &m, const BatchDev &b, void *stream);   // sim_plain.cu
 int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream);    // sim_fast.cu
 size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_stage, bool state_global, int tnrows,
-                       bool pop_single, bool tn_smem = false);
+                       bool pop_single, bool tn_smem = false, int nt = 0);
 size_t fast_gstate_stride(const ModelDev &m);
 size_t fast_tc_smem_bytes(const ModelDev &m);   // shared memory of the tensor-core FOI
 int fast_pick_threads(const ModelDev &m);        // threads per CTA of the fast kernel for this model
 // library options (beep_set_option)
 int option_fast_foi();                           // 0 automatic, 1 FP32 SIMT, 2 tensor cores
+int option_fast_ctas();                          // 0 automatic, 1, or 2..4: particles (CTAs) per SM, at most
+constexpr int kDualThreads = 320;                // threads per CTA with several particles per SM
+constexpr size_t kSmemPerSM = 228 * 1024;        // shared memory per SM (each resident CTA reserves 1 KB)
 int fast_threads();
 int fast_prepare();                              // one-time constant tables of the fast kernel
 int fast_chain_prepare();                        // the same for the MBP-chain variants (mbp_fast.cu)
 int launch_sim_fast_chain(const ModelDev &m, const BatchDev &b, void *stream);   // mbp_fast.cu
+int fast_ctas_prepare();                         // constant tables of sim_fast_ctas.cu
+int fast_ctas_max(int G);                        // most 320-thread CTAs per SM for G ages
+int launch_sim_fast_ctas(const ModelDev &m, const BatchDev &b, size_t smem, void *stream);   // sim_fast_ctas.cu
 
 }  // namespace beep

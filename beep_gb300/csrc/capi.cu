@@ -33,6 +33,7 @@ namespace beep {
 
 thread_local std::string g_err;
 std::atomic<int> g_fast_foi{0};
+std::atomic<int> g_fast_ctas{0};
 
 beep_status fail(beep_status s, const std::string &msg)
 {
@@ -72,6 +73,11 @@ beep_status beep_set_option(const char *name, int64_t value)
 	if (std::string(name) == "fast_foi") {
 		if (value < 0 || value > 2) return fail(BEEP_BAD_INPUT, "fast_foi must be 0, 1 or 2");
 		g_fast_foi.store((int)value);
+		return BEEP_OK;
+	}
+	if (std::string(name) == "fast_ctas_per_sm") {
+		if (value < 0 || value > 4) return fail(BEEP_BAD_INPUT, "fast_ctas_per_sm must be 0 (automatic) or 1..4");
+		g_fast_ctas.store((int)value);
 		return BEEP_OK;
 	}
 	return fail(BEEP_BAD_INPUT, std::string("unknown option ") + name);
@@ -641,6 +647,24 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 				}
 			}
 		}
+		// several particles per SM (320-thread CTAs): as many as the SM's shared memory
+		// holds with each particle's state on chip, up to four; the matrix is read
+		// through L1 unless it fits beside every CTA's state.  Automatic: from three
+		// CTAs per SM (two run no faster than one CTA of 640 threads).
+		const int opt_ctas = option_fast_ctas() != 0 ? option_fast_ctas() : m->tuned_ctas;
+		if (allow_tc && !q->bd.foi_tc && opt_ctas != 1 && fast_pick_threads(m->dev) == 640 &&
+		    m->NS * m->A <= kDualThreads && m->G * m->G <= kDualThreads) {
+			const size_t s0 = fast_smem_bytes(m->dev, nslots, false, q->bd.nefoi_stage, false, tnrows, ps, false, kDualThreads);
+			const size_t s1 = fast_smem_bytes(m->dev, nslots, true, q->bd.nefoi_stage, false, tnrows, ps, false, kDualThreads);
+			const int kmax = std::min(opt_ctas >= 2 ? opt_ctas : 4, fast_ctas_max(m->G));
+			int k = (int)std::min<size_t>((size_t)kmax, kSmemPerSM / (s0 + 1024));
+			if (k >= (opt_ctas >= 2 ? 2 : 3)) {
+				q->bd.nt = kDualThreads;
+				q->bd.ctas = k;
+				q->state_global = false;
+				q->bd.m_in_smem = (size_t)k * (s1 + 1024) <= kSmemPerSM ? 1 : 0;
+			}
+		}
 	}
 	auto bail = [&](beep_status s) { beep_batch_destroy(q); return s; };
 	if (b->form == BEEP_FORM_FAST && fast_prepare() != 0) return bail(fail(BEEP_DEVICE_ERROR, "constant tables"));
@@ -829,27 +853,34 @@ beep_status beep_autotune(beep_model *m, const beep_sim_batch *b, int32_t *chose
 	std::vector<double> L(t.nparticle);
 	t.L_out = L.data();
 	if (t.ti > 0 && !t.pop_in) return fail(BEEP_BAD_INPUT, "pop_in is required when ti > 0");
-	const int saved_opt = option_fast_foi();
-	const int saved_tuned = m->tuned_foi;
+	const int saved_foi = m->tuned_foi, saved_ctas = m->tuned_ctas;
 	double best = 1e300;
-	int best_c = 1;
-	for (int cand = 1; cand <= 2; cand++) {
-		m->tuned_foi = cand;
+	int best_foi = 1, best_ctas = 1;
+	// candidates (force of infection path, particles per SM): SIMT with one, SIMT with
+	// as many as fit (up to four), tensor cores (one)
+	const int cands[3][2] = {{1, 1}, {1, 4}, {2, 1}};
+	for (const auto &c : cands) {
+		m->tuned_foi = c[0];
+		m->tuned_ctas = c[1];
 		beep_batch *q = nullptr;
 		beep_status st = beep_batch_create(m, &t, &q);
-		if (st != BEEP_OK) { m->tuned_foi = saved_tuned; return st; }
-		if (beep_batch_foi_path(q) != cand) { beep_batch_destroy(q); continue; }   // not available for this model
+		if (st != BEEP_OK) { m->tuned_foi = saved_foi; m->tuned_ctas = saved_ctas; return st; }
+		const int got = beep_batch_ctas_per_sm(q);
+		if (beep_batch_foi_path(q) != c[0] || (c[1] == 1) != (got == 1)) {   // not available for this model
+			beep_batch_destroy(q);
+			continue;
+		}
 		double ms = 0;
 		st = beep_batch_upload(q);
 		if (st == BEEP_OK) st = beep_batch_time(q, 1, &ms);      // warm-up
 		if (st == BEEP_OK) st = beep_batch_time(q, 2, &ms);
 		beep_batch_destroy(q);
-		if (st != BEEP_OK) { m->tuned_foi = saved_tuned; return st; }
-		if (ms < best) { best = ms; best_c = cand; }
+		if (st != BEEP_OK) { m->tuned_foi = saved_foi; m->tuned_ctas = saved_ctas; return st; }
+		if (ms < best) { best = ms; best_foi = c[0]; best_ctas = c[1]; }
 	}
-	(void)saved_opt;
-	m->tuned_foi = best_c;
-	if (chosen) *chosen = best_c;
+	m->tuned_foi = best_foi;
+	m->tuned_ctas = best_ctas;
+	if (chosen) *chosen = best_foi;
 	return BEEP_OK;
 }
 
@@ -857,6 +888,12 @@ int32_t beep_batch_foi_path(const beep_batch *q)
 {
 	if (!q || q->b.form != BEEP_FORM_FAST) return 0;
 	return q->bd.foi_tc ? 2 : 1;
+}
+
+int32_t beep_batch_ctas_per_sm(const beep_batch *q)
+{
+	if (!q || q->b.form != BEEP_FORM_FAST) return 0;
+	return q->bd.nt == kDualThreads ? q->bd.ctas : 1;
 }
 
 beep_status beep_batch_bytes(const beep_batch *q, int64_t *h2d, int64_t *d2h)
@@ -910,3 +947,5 @@ size_t beep::batch_device_bytes(const beep_batch *q)
 }
 
 int beep::option_fast_foi() { return g_fast_foi.load(); }
+
+int beep::option_fast_ctas() { return g_fast_ctas.load(); }

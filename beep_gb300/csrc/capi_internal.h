@@ -103,6 +103,7 @@ struct beep_model {
 	std::vector<float> obs_factor_f_h;
 	int32_t max_obs_spline = -1;
 	int32_t tuned_foi = 0;        // fast-form FOI path chosen by beep_autotune (0: none)
+	int32_t tuned_ctas = 0;       // fast-form particles per SM chosen by beep_autotune (0: none)
 	std::mutex mu;
 };
 
@@ -136,7 +137,8 @@ namespace beep {
 // With device_traj the kernels write every step's transition counts to a
 // device buffer the caller sets in bd.tn_traj ([P][tf-ti][A][T][DP]) before
 // each launch.
-// allow_tc = false keeps the fast form on the FP32 SIMT force of infection.
+// allow_tc = false keeps the fast form on its base kernel: FP32 SIMT force of
+// infection, one particle per SM.
 beep_status batch_create_internal(beep_model *m, const beep_sim_batch *b, bool device_io, beep_batch **out,
                                   bool device_traj = false, bool allow_tc = true);
 // beep_batch_download in two halves: the device->host copy enqueued on the

@@ -12,7 +12,7 @@ static int pick_threads(const ModelDev &m)
 }
 
 size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_stage, bool state_global,
-                       int tnrows, bool pop_single, bool tn_smem)
+                       int tnrows, bool pop_single, bool tn_smem, int nt)
 {
 	auto r = [](size_t x) { return (x + 15) & ~(size_t)15; };
 	const size_t A = m.A, G = m.G, DP = m.DP, NS = m.NS, C = m.C, T = m.T, DPS = m.DPS;
@@ -21,15 +21,16 @@ size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_
 	       (state_global && !tn_smem ? 0 : r(4 * (size_t)tnrows * ncol)) + 3 * r(4 * agsz) +
 	       r(4 * (size_t)nslots) + 3 * r(4 * T) + r(4 * DPS) + r(4 * C) + r(4 * T * DP) + r(4 * DP) + r(4 * 64) +
 	       r(4 * 32) + 2 * r(4 * NS * A) + r(4 * (size_t)nefoi_stage * G) + 2 * (2 * r(4 * NS * A) + r(4 * G * G)) +
-	       r(8) + r(4 * 2 * (size_t)pick_threads(m));
+	       r(8) + r(4 * 2 * (size_t)(nt > 0 ? nt : pick_threads(m)));
 }
 
 int fast_threads() { return kFastThreads; }
 
 int fast_prepare()
 {
-	const int e = prepare_constants();
-	return e != 0 ? e : fast_chain_prepare();
+	int e = prepare_constants();
+	if (e == 0) e = fast_chain_prepare();
+	return e != 0 ? e : fast_ctas_prepare();
 }
 
 int fast_pick_threads(const ModelDev &m) { return pick_threads(m); }
@@ -47,12 +48,12 @@ size_t fast_gstate_stride(const ModelDev &m)
 	return 2 * r(4 * m.C * ncol) + r(4 * m.T * ncol);   // upper bound for any row/buffer choice
 }
 
-template <int NT, bool TC>
+template <int NT, bool TC, int MB = min_ctas(NT)>
 static int launch_nt(const ModelDev &m, const BatchDev &b, size_t smem, cudaStream_t st)
 {
 	// MG: the age count rounded up to a multiple of 4 (the stride of the infectious counts)
-	auto kern = m.G <= 4 ? sim_fast_kernel<NT, 4, TC> : m.G <= 8 ? sim_fast_kernel<NT, 8, TC>
-	          : m.G <= 12 ? sim_fast_kernel<NT, 12, TC> : sim_fast_kernel<NT, 16, TC>;
+	auto kern = m.G <= 4 ? sim_fast_kernel<NT, 4, TC, false, MB> : m.G <= 8 ? sim_fast_kernel<NT, 8, TC, false, MB>
+	          : m.G <= 12 ? sim_fast_kernel<NT, 12, TC, false, MB> : sim_fast_kernel<NT, 16, TC, false, MB>;
 	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	if (e != cudaSuccess) return (int)e;
 	kern<<<b.P, NT, smem, st>>>(m, b);
@@ -64,13 +65,14 @@ int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream)
 	if (b.P == 0) return 0;
 	if (b.mode != 0) return launch_sim_fast_chain(m, b, stream);
 	if (m.G > 16 || m.T > kMaxT) return (int)cudaErrorInvalidValue;
+	const int nt = b.nt > 0 ? b.nt : pick_threads(m);
 	size_t smem = fast_smem_bytes(m, b.nslots, b.m_in_smem != 0, b.nefoi_stage, b.gstate != nullptr,
-	                              b.tn_full ? m.T : m.tn_rows, b.pop_single != 0, b.tn_smem != 0);
+	                              b.tn_full ? m.T : m.tn_rows, b.pop_single != 0, b.tn_smem != 0, nt);
 	if (b.foi_tc) {
 		if (!m.tc_image || pick_threads(m) != 640 || b.tc_smem_off < smem) return (int)cudaErrorInvalidValue;
 		smem = b.tc_smem_off + fast_tc_smem_bytes(m);
 	}
-	const int nt = pick_threads(m);
+	if (nt != pick_threads(m) && (nt != kDualThreads || b.foi_tc)) return (int)cudaErrorInvalidValue;
 	const int NSA = m.NS * m.A;
 	if (NSA > nt || m.G * m.G > nt) return (int)cudaErrorInvalidValue;   // slices: one item per thread
 	{
@@ -79,8 +81,12 @@ int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream)
 	}
 	cudaStream_t st = (cudaStream_t)stream;
 	if (b.foi_tc) return launch_nt<640, true>(m, b, smem, st);
-	return nt == 128 ? launch_nt<128, false>(m, b, smem, st) : nt == 256 ? launch_nt<256, false>(m, b, smem, st)
-	                                                                     : launch_nt<640, false>(m, b, smem, st);
+	switch (nt) {
+	case 128: return launch_nt<128, false>(m, b, smem, st);
+	case 256: return launch_nt<256, false>(m, b, smem, st);
+	case kDualThreads: return launch_sim_fast_ctas(m, b, smem, st);
+	default: return launch_nt<640, false>(m, b, smem, st);
+	}
 }
 
 }  // namespace beep

@@ -464,8 +464,15 @@ __device__ __forceinline__ int32_t binomial_fp32(float p, int32_t n, uint32_t k0
 	return flip ? n - k : k;
 }
 
-template <int NT, int MG, bool TC, bool CH = false>
-__global__ void __launch_bounds__(NT, 1) sim_fast_kernel(const ModelDev m, const BatchDev b)
+// CTAs resident per SM (MB): one of 640 threads; two to four of 320
+// (kDualThreads) when that many particles' state fits the SM's shared memory
+// -- the register budget per thread shrinks to 96 / 64 / 48 and the warps per
+// SM grow to 20 / 30 / 40, which hides the latency of the sampler and Philox
+// chains; two of 256 or four of 128 threads for small models.
+constexpr int min_ctas(int nt) { return nt >= 640 ? 1 : nt >= 256 ? 2 : 4; }
+
+template <int NT, int MG, bool TC, bool CH = false, int MB = min_ctas(NT)>
+__global__ void __launch_bounds__(NT, MB) sim_fast_kernel(const ModelDev m, const BatchDev b)
 {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	const int p = blockIdx.x;

@@ -420,6 +420,7 @@ def run_ours(args, rank, ws, dist):
     from beep_gb300 import build as bbuild, capi
     bbuild.build()
     capi.set_option("fast_foi", {"auto": capi.FOI_AUTO, "simt": capi.FOI_SIMT, "tensor": capi.FOI_TENSOR}[args.foi])
+    capi.set_option("fast_ctas_per_sm", args.ctas)
     P = args.particles or WORKLOADS[args.workload]["particles"]
     seed = args.seed + 7919 * rank
     w, m, tabs, group_of = build_workload(args.workload, P, seed)
@@ -522,6 +523,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--form", default="fast", choices=["fast", "plain"])
+    ap.add_argument("--ctas", type=int, default=0, choices=[0, 1, 2],
+                    help="particles (CTAs) per SM of the fast form, 0 = automatic (library option fast_ctas_per_sm)")
     ap.add_argument("--foi", default="auto", choices=["auto", "simt", "tensor"],
                     help="force of infection of the fast form (library option fast_foi)")
     ap.add_argument("--plain-particles", type=int, default=1024)

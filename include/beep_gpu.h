@@ -209,15 +209,20 @@ BEEP_API beep_status beep_batch_destroy(beep_batch *batch);
  * status reset, kernel, output copy) captured once as a CUDA graph and
  * replayed by later calls (captured again if the staged inputs change size). */
 BEEP_API beep_status beep_batch_run_graph(beep_batch *batch);
-/* Autotuner of the fast form for a model: times every force-of-infection path
- * the model supports (1 = FP32 SIMT, 2 = tensor cores) on a sample of the
- * given batch (two waves of particles, up to 120 steps) and records the
- * fastest on the model; later batches of the model use it while the option
- * fast_foi is automatic.  *chosen (may be NULL) receives the path. */
+/* Autotuner of the fast form for a model: times every kernel layout the
+ * model supports -- force of infection on FP32 SIMT (one or several particles
+ * per SM) or on the tensor cores -- on a sample of the given batch (two waves
+ * of particles, up to 120 steps) and records the fastest on the model; later
+ * batches of the model use it while the options fast_foi and
+ * fast_ctas_per_sm are automatic.  *chosen (may be NULL) receives the force
+ * of infection path (1 = FP32 SIMT, 2 = tensor cores). */
 BEEP_API beep_status beep_autotune(beep_model *model, const beep_sim_batch *batch, int32_t *chosen);
 /* Force-of-infection path the fast form of this batch runs: 1 = FP32 SIMT,
  * 2 = tensor cores; 0 for the plain form. */
 BEEP_API int32_t beep_batch_foi_path(const beep_batch *batch);
+/* Particles (CTAs) resident per SM that the fast form of this batch is laid
+ * out for: 1..4; 0 for the plain form. */
+BEEP_API int32_t beep_batch_ctas_per_sm(const beep_batch *batch);
 
 /* Bootstrap particle filter of PMCMC (PMCMC::obs_prob + bootstrap,
  * src/pmcmc.cc:180-268; ancestor swap Mpi::end_sec_swap, src/mpi.cc:215-327)
@@ -272,6 +277,12 @@ BEEP_API beep_status beep_abcsmc_weights(int32_t nvar, int32_t nnew, const doubl
  *               FP32 SIMT otherwise), 1 = FP32 SIMT, 2 = tensor cores wherever
  *               supported (64 to 512 areas, one or two strains, more than 256
  *               area x group columns).
+ *   "fast_ctas_per_sm"  particles resident per SM in the fast form, for models
+ *               of 257 to 640 area x group columns with at most 320 strain x
+ *               area pairs: 0 = automatic (several when at least three
+ *               particles' state fits the SM's shared memory, else one),
+ *               1 = one (640-thread CTAs), 2..4 = at most that many
+ *               (320-thread CTAs; at most 3 above 8 ages).
  * Unknown names or values give BEEP_BAD_INPUT. */
 BEEP_API beep_status beep_set_option(const char *name, int64_t value);
 

@@ -156,3 +156,56 @@ def test_tensor_core_foi_distribution_matches_oracle(foi_option):
     assert stats.ks_2samp(fs_f, fs_o).pvalue > 1e-3
     assert stats.ks_2samp(f.L, o.L).pvalue > 1e-3
     dm.close()
+
+
+@pytest.fixture
+def ctas_option(built):
+    yield capi.set_option
+    capi.set_option("fast_ctas_per_sm", 0)
+
+
+def test_several_particles_per_sm_follow_fp64(ctas_option):
+    """Two to four 320-thread CTAs per SM (smaller register budget, more warps)
+    run the same arithmetic per column as one 640-thread CTA: the particles
+    follow the FP64 trajectories and score them within the fast-form tolerance,
+    whichever layout runs; the automatic choice takes four for a model whose
+    state is small."""
+    from beep_gb300 import model_builder as mb, synth
+    w = synth.seir_hd_small(seed=20260203, narea=100, nage=4, days=60, name="mid3")
+    m = capi.Model(mb.model_arrays(w))
+    t = capi.Tables(mb.param_tables(w))
+    dm = capi.DeviceModel(m)
+    P = 96
+    g = dm.simulate(capi.Batch(m, [t], P, 11, want_transnum=True, want_pop=True))
+    res = {}
+    for k in (0, 1, 2, 3, 4):
+        ctas_option("fast_ctas_per_sm", k)
+        db = capi.DeviceBatch(dm, capi.Batch(m, [t], P, 11, want_transnum=True, want_pop=True, form=capi.FORM_FAST))
+        assert db.ctas_per_sm() == (4 if k == 0 else k), (k, db.ctas_per_sm())
+        assert db.foi_path() == capi.FOI_SIMT
+        f = db.run()
+        db.close()
+        same = np.array([np.array_equal(f.transnum[p], g.transnum[p]) for p in range(P)])
+        assert same.mean() >= 0.6, (k, same.mean())
+        np.testing.assert_allclose(f.L[same], g.L[same], rtol=L_RTOL_FAST)
+        res[k] = f
+    # the multi-CTA layouts read the area matrix the same way: identical results
+    for k in (3, 4):
+        assert np.array_equal(res[k].transnum, res[2].transnum)
+        assert np.array_equal(res[k].L, res[2].L)
+    dm.close()
+
+
+def test_several_particles_per_sm_not_taken_when_state_is_large(ctas_option):
+    """A model whose per-particle state exceeds half of the SM's shared memory
+    (300 areas x 10 ages) keeps one particle per SM."""
+    from beep_gb300 import model_builder as mb, synth
+    w = synth.seir_hd_small(seed=20260204, narea=300, nage=10, days=5, name="big2")
+    m = capi.Model(mb.model_arrays(w))
+    t = capi.Tables(mb.param_tables(w))
+    dm = capi.DeviceModel(m)
+    ctas_option("fast_ctas_per_sm", 4)
+    db = capi.DeviceBatch(dm, capi.Batch(m, [t], 4, 5, form=capi.FORM_FAST))
+    assert db.ctas_per_sm() == 1
+    db.close()
+    dm.close()
