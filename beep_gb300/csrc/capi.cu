@@ -648,20 +648,29 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 			}
 		}
 		// several particles per SM (320-thread CTAs): as many as the SM's shared memory
-		// holds with each particle's state on chip, up to four; the matrix is read
-		// through L1 unless it fits beside every CTA's state.  Automatic: from three
-		// CTAs per SM (two run no faster than one CTA of 640 threads).
+		// holds, up to four (three above 8 ages), each particle's state on chip -- or, for
+		// models whose state lives in global memory anyway, only the infectious counts,
+		// force of infection and observation slots (automatic: only if the one-CTA layout
+		// keeps the state in global memory too); the matrix is read through L1 unless it
+		// fits beside every CTA's share.  Automatic: from three CTAs per SM (two run no
+		// faster than one CTA of 640 threads).
 		const int opt_ctas = option_fast_ctas() != 0 ? option_fast_ctas() : m->tuned_ctas;
-		if (allow_tc && !q->bd.foi_tc && opt_ctas != 1 && fast_pick_threads(m->dev) == 640 &&
-		    m->NS * m->A <= kDualThreads && m->G * m->G <= kDualThreads) {
-			const size_t s0 = fast_smem_bytes(m->dev, nslots, false, q->bd.nefoi_stage, false, tnrows, ps, false, kDualThreads);
-			const size_t s1 = fast_smem_bytes(m->dev, nslots, true, q->bd.nefoi_stage, false, tnrows, ps, false, kDualThreads);
+		if (allow_tc && !q->bd.foi_tc && opt_ctas != 1 && fast_pick_threads(m->dev) == 640) {
 			const int kmax = std::min(opt_ctas >= 2 ? opt_ctas : 4, fast_ctas_max(m->G));
-			int k = (int)std::min<size_t>((size_t)kmax, kSmemPerSM / (s0 + 1024));
-			if (k >= (opt_ctas >= 2 ? 2 : 3)) {
+			const int kmin = opt_ctas >= 2 ? 2 : 3;
+			auto fit = [&](size_t bytes) { return (int)std::min<size_t>((size_t)kmax, kSmemPerSM / (bytes + 1024)); };
+			const int nefo = q->bd.nefoi_stage;
+			bool glob = false;
+			int k = fit(fast_smem_bytes(m->dev, nslots, false, nefo, false, tnrows, ps, false, kDualThreads));
+			if (k < kmin && (q->state_global || opt_ctas >= 2)) {
+				glob = true;
+				k = fit(fast_smem_bytes(m->dev, nslots, false, nefo, true, tnrows, ps, false, kDualThreads));
+			}
+			if (k >= kmin) {
 				q->bd.nt = kDualThreads;
 				q->bd.ctas = k;
-				q->state_global = false;
+				q->state_global = glob;
+				const size_t s1 = fast_smem_bytes(m->dev, nslots, true, nefo, glob, tnrows, ps, false, kDualThreads);
 				q->bd.m_in_smem = (size_t)k * (s1 + 1024) <= kSmemPerSM ? 1 : 0;
 			}
 		}

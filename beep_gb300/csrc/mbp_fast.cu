@@ -31,7 +31,6 @@ int launch_sim_fast_chain(const ModelDev &m, const BatchDev &b, void *stream)
 	const size_t smem = fast_smem_bytes(m, b.nslots, b.m_in_smem != 0, b.nefoi_stage, b.gstate != nullptr,
 	                                    b.tn_full ? m.T : m.tn_rows, b.pop_single != 0, b.tn_smem != 0);
 	const int nt = fast_pick_threads(m);
-	if (m.NS * m.A > nt || m.G * m.G > nt) return (int)cudaErrorInvalidValue;
 	const int e = prepare_constants();
 	if (e != 0) return e;
 	cudaStream_t st = (cudaStream_t)stream;

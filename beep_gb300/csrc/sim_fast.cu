@@ -74,7 +74,6 @@ int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream)
 	}
 	if (nt != pick_threads(m) && (nt != kDualThreads || b.foi_tc)) return (int)cudaErrorInvalidValue;
 	const int NSA = m.NS * m.A;
-	if (NSA > nt || m.G * m.G > nt) return (int)cudaErrorInvalidValue;   // slices: one item per thread
 	{
 		const int e = fast_prepare();
 		if (e != 0) return e;

@@ -374,29 +374,48 @@ struct SliceRegs {
 	float be, et, N, d;
 };
 
+// item i (strain, area) of a step's slices: beta * areafactor, external force of infection per capita
+__device__ __forceinline__ float2 slice_item(const ModelDev &m, const Tabs &tb, const FastSmem &s, int sett, int i)
+{
+	const int A = m.A, c = i % A;
+	const float be = __ldg(tb.beta_rows + (size_t)s.brow[i] * m.S + sett) *
+	                 __ldg(tb.areafactor + (size_t)(sett / m.div_per_time) * A + c);
+	float et = __ldg(tb.efoi_spline + (size_t)s.eref[i] * m.S + sett) * m.inv_popsize_f;
+	if (tb.efoi_mult) et *= __ldg(tb.efoi_mult + ((size_t)sett * A + c) * m.NS + i / A);
+	return make_float2(be, et);
+}
+
+// the first NT items of each kind go through registers; items beyond (models
+// with more (strain, area) pairs or age pairs than threads) are loaded when stored
 template <int NT>
 __device__ __forceinline__ SliceRegs slice_load(const ModelDev &m, const Tabs &tb, const FastSmem &s, int sett, int tid)
 {
 	SliceRegs r{0.f, 0.f, 0.f, 0.f};
-	const int A = m.A, NSA = m.NS * m.A, G = m.G;
-	if (tid < NSA) {
-		const int c = tid % A;
-		r.be = __ldg(tb.beta_rows + (size_t)s.brow[tid] * m.S + sett) *
-		       __ldg(tb.areafactor + (size_t)(sett / m.div_per_time) * A + c);
-		r.et = __ldg(tb.efoi_spline + (size_t)s.eref[tid] * m.S + sett) * m.inv_popsize_f;
-		if (tb.efoi_mult) r.et *= __ldg(tb.efoi_mult + ((size_t)sett * A + c) * m.NS + tid / A);
+	if (tid < m.NS * m.A) {
+		const float2 v = slice_item(m, tb, s, sett, tid);
+		r.be = v.x;
+		r.et = v.y;
 	}
-	if (tid < G * G) r.N = __ldg(tb.Ntime + (size_t)sett * G * G + tid);
+	if (tid < m.G * m.G) r.N = __ldg(tb.Ntime + (size_t)sett * m.G * m.G + tid);
 	if (tid == 0) r.d = __ldg(tb.geo + sett);
 	return r;
 }
 
 template <int NT>
-__device__ __forceinline__ void slice_store(const ModelDev &m, FastSmem &s, const SliceRegs &r, int buf, int tid)
+__device__ __forceinline__ void slice_store(const ModelDev &m, const Tabs &tb, FastSmem &s, const SliceRegs &r, int buf,
+                                            int sett, int tid)
 {
-	if (tid < m.NS * m.A) { (buf ? s.be1 : s.be0)[tid] = r.be; (buf ? s.et1 : s.et0)[tid] = r.et; }
-	if (tid < m.G * m.G) (buf ? s.N1 : s.N0)[tid] = r.N;
+	float *be = buf ? s.be1 : s.be0, *et = buf ? s.et1 : s.et0, *N = buf ? s.N1 : s.N0;
+	const int NSA = m.NS * m.A, GG = m.G * m.G;
+	if (tid < NSA) { be[tid] = r.be; et[tid] = r.et; }
+	if (tid < GG) N[tid] = r.N;
 	if (tid == 0) s.dgeo[buf] = r.d;
+	for (int i = tid + NT; i < NSA; i += NT) {
+		const float2 v = slice_item(m, tb, s, sett, i);
+		be[i] = v.x;
+		et[i] = v.y;
+	}
+	for (int i = tid + NT; i < GG; i += NT) N[i] = __ldg(tb.Ntime + (size_t)sett * GG + i);
 }
 
 // Stirling remainder of log Gamma(z): log Gamma(z) - ((z - 1/2) log z - z + log(2 pi)/2)
@@ -617,7 +636,7 @@ __global__ void __launch_bounds__(NT, MB) sim_fast_kernel(const ModelDev m, cons
 		}
 		s.Ic0[idx] = v;
 	}
-	slice_store<NT>(m, s, slice_load<NT>(m, tb, s, b.ti, tid), 0, tid);
+	slice_store<NT>(m, tb, s, slice_load<NT>(m, tb, s, b.ti, tid), 0, b.ti, tid);
 	__syncthreads();
 	bool tc_ok = true;
 	if (use_tc) {
@@ -767,7 +786,7 @@ __global__ void __launch_bounds__(NT, MB) sim_fast_kernel(const ModelDev m, cons
 			if (m.dp_age_unique) Ic_nxt[(st * A + c) * MG + a] = iv;
 			else atomicAdd(Ic_nxt + (st * A + c) * MG + a, iv);
 		}
-		if (sett + 1 < b.tf) slice_store<NT>(m, s, nxt, sb ^ 1, tid);
+		if (sett + 1 < b.tf) slice_store<NT>(m, tb, s, nxt, sb ^ 1, sett + 1, tid);
 		__syncthreads();
 
 		// ---- B: observation sums of the step (completed ones -> log-density),

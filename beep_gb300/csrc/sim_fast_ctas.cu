@@ -36,7 +36,6 @@ int launch_sim_fast_ctas(const ModelDev &m, const BatchDev &b, size_t smem, void
 {
 	if (b.nt != kDualThreads || b.ctas < 2 || b.ctas > fast_ctas_max(m.G) || b.foi_tc || b.mode != 0)
 		return (int)cudaErrorInvalidValue;
-	if (m.NS * m.A > kDualThreads || m.G * m.G > kDualThreads) return (int)cudaErrorInvalidValue;
 	const int e = prepare_constants();
 	if (e != 0) return e;
 	cudaStream_t st = (cudaStream_t)stream;

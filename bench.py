@@ -523,8 +523,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--form", default="fast", choices=["fast", "plain"])
-    ap.add_argument("--ctas", type=int, default=0, choices=[0, 1, 2],
-                    help="particles (CTAs) per SM of the fast form, 0 = automatic (library option fast_ctas_per_sm)")
+    ap.add_argument("--ctas", type=int, default=0, choices=[0, 1, 2, 3, 4],
+                    help="particles (CTAs) per SM of the fast form: 0 = automatic, 1 = one, 2..4 = at most that many "
+                         "(library option fast_ctas_per_sm)")
     ap.add_argument("--foi", default="auto", choices=["auto", "simt", "tensor"],
                     help="force of infection of the fast form (library option fast_foi)")
     ap.add_argument("--plain-particles", type=int, default=1024)

@@ -196,16 +196,28 @@ def test_several_particles_per_sm_follow_fp64(ctas_option):
     dm.close()
 
 
-def test_several_particles_per_sm_not_taken_when_state_is_large(ctas_option):
-    """A model whose per-particle state exceeds half of the SM's shared memory
-    (300 areas x 10 ages) keeps one particle per SM."""
+def test_several_particles_per_sm_with_state_in_global_memory(ctas_option):
+    """A model whose per-particle state lives in global memory (300 areas x 10
+    ages) runs three 320-thread particles per SM with only the infectious
+    counts, force of infection and slots on chip, and follows the FP64 form."""
     from beep_gb300 import model_builder as mb, synth
-    w = synth.seir_hd_small(seed=20260204, narea=300, nage=10, days=5, name="big2")
+    w = synth.seir_hd_small(seed=20260204, narea=300, nage=10, days=20, name="big2")
     m = capi.Model(mb.model_arrays(w))
     t = capi.Tables(mb.param_tables(w))
     dm = capi.DeviceModel(m)
-    ctas_option("fast_ctas_per_sm", 4)
-    db = capi.DeviceBatch(dm, capi.Batch(m, [t], 4, 5, form=capi.FORM_FAST))
-    assert db.ctas_per_sm() == 1
-    db.close()
+    P = 24
+    g = dm.simulate(capi.Batch(m, [t], P, 5, want_transnum=True, want_pop=True))
+    ctas_option("fast_foi", capi.FOI_SIMT)
+    try:
+        for k, want in ((1, 1), (4, 3)):
+            ctas_option("fast_ctas_per_sm", k)
+            db = capi.DeviceBatch(dm, capi.Batch(m, [t], P, 5, want_transnum=True, want_pop=True, form=capi.FORM_FAST))
+            assert db.ctas_per_sm() == want
+            f = db.run()
+            db.close()
+            same = np.array([np.array_equal(f.transnum[p], g.transnum[p]) for p in range(P)])
+            assert same.mean() >= 0.5, (k, same.mean())
+            np.testing.assert_allclose(f.L[same], g.L[same], rtol=L_RTOL_FAST)
+    finally:
+        ctas_option("fast_foi", capi.FOI_AUTO)
     dm.close()
