@@ -6,8 +6,10 @@ that back the structures alive for as long as the structures are in use.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
 import os
+import weakref
 from typing import Dict, List, Optional, Sequence
 
 import numpy as np
@@ -332,6 +334,27 @@ def check(status: int) -> None:
         raise BeepError(status, (lib().beep_last_error() or b"").decode())
 
 
+# Handles still open at interpreter exit are closed here, dependents first
+# (servers and MBP chain sets, then batches, then models), while the library
+# and the CUDA runtime are still loaded; finalisers at shutdown run in no
+# defined order.
+_OPEN: Dict[int, "weakref.WeakSet"] = {0: weakref.WeakSet(), 1: weakref.WeakSet(), 2: weakref.WeakSet()}
+
+
+def _track(obj, rank: int):
+    _OPEN[rank].add(obj)
+
+
+@atexit.register
+def _close_open_handles():
+    for rank in (0, 1, 2):
+        for obj in list(_OPEN[rank]):
+            try:
+                obj.close()
+            except Exception:
+                pass
+
+
 class DeviceModel:
     """A ``beep_model`` handle on the GPU."""
 
@@ -342,6 +365,7 @@ class DeviceModel:
         h = C.c_void_p()
         check(L.beep_model_create(C.byref(model.desc), C.byref(h)))
         self.h = h
+        _track(self, 2)
 
     def simulate(self, batch: Batch) -> Batch:
         check(lib().beep_simulate(self.h, C.byref(batch.st)))
@@ -398,6 +422,7 @@ class DeviceBatch:
         h = C.c_void_p()
         check(lib().beep_batch_create(dm.h, C.byref(batch.st), C.byref(h)))
         self.h = h
+        _track(self, 1)
 
     def stage(self):
         check(lib().beep_batch_stage(self.h))
@@ -479,6 +504,7 @@ class MbpChains:
         h = C.c_void_p()
         check(lib().beep_mbp_create(dm.h, nchain, form, C.byref(h)))
         self.h = h
+        _track(self, 0)
 
     def _request(self, tables: Sequence[Tables], seed: int, group_of=None, stream_of=None,
                  inf_update: int = INF_DIF_UPDATE, simu=None, want_L: bool = True):
@@ -562,6 +588,7 @@ class Server:
         check(lib().beep_server_create(device, int(hbm_budget_bytes), max_inflight, C.byref(h)))
         self.h = h
         self._live = {}
+        _track(self, 0)
 
     def submit(self, model: Model, batch: Batch, kind: int = REQ_LIKELIHOOD) -> int:
         """Queues a request; the model and batch (and their arrays) are kept until it is released."""
