@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <thread>
 #include <atomic>
 #include <climits>
 #include <cmath>
@@ -364,8 +365,21 @@ beep_status beep_model_destroy(beep_model *m)
 
 namespace {
 
+// The parameter tables of a batch in one pool, each distinct array once (by
+// address and length).  With copy, the pool is built in `f` (FP64, the plain
+// form); without, only the offsets are laid out and `pieces` lists what goes
+// where, for the caller to write straight into the staging buffer in FP32
+// (the fast form, which reads no FP64 table).
 struct TablePacker {
+	bool copy = true;
+	size_t fsize = 0;                     // pool length in values (a multiple of 4)
 	std::vector<double> f;
+	struct Piece {
+		const double *src;
+		size_t n;
+		int64_t off;
+	};
+	std::vector<Piece> pieces;
 	std::vector<int32_t> i;
 	struct KeyHash {
 		size_t operator()(const std::pair<const void *, size_t> &k) const
@@ -375,14 +389,26 @@ struct TablePacker {
 	};
 	std::unordered_map<std::pair<const void *, size_t>, int64_t, KeyHash> seen;
 	std::unordered_map<const int32_t *, std::pair<int32_t, int32_t>> ranges;
+	int64_t reserve(size_t n)             // n values, filled by the caller
+	{
+		const int64_t off = (int64_t)fsize;
+		fsize = align_up(fsize + n, 4);
+		if (copy) f.resize(fsize, 0.0);
+		return off;
+	}
 	int64_t addf(const double *p, size_t n)
 	{
 		auto key = std::make_pair((const void *)p, n);
 		auto it = seen.find(key);
 		if (it != seen.end()) return it->second;
-		int64_t off = (int64_t)f.size();
-		f.insert(f.end(), p, p + n);
-		f.resize(align_up(f.size(), 4));
+		const int64_t off = (int64_t)fsize;
+		if (copy) {
+			f.insert(f.end(), p, p + n);
+			f.resize(align_up(f.size(), 4), 0.0);
+		} else {
+			pieces.push_back(Piece{p, n, off});
+		}
+		fsize = align_up(fsize + n, 4);
 		seen[key] = off;
 		return off;
 	}
@@ -427,8 +453,7 @@ beep_status pack_tables(const beep_model *m, const beep_sim_batch *b, TablePacke
 		dd.transrate = pk.addf(t.transrate, T * DP);
 		dd.susceptibility = pk.addf(t.susceptibility, DP);
 		dd.infectivity = pk.addf(t.infectivity, C);
-		dd.infdif = (int64_t)pk.f.size();    // filled when the pool is staged
-		pk.f.resize(pk.f.size() + align_up(T, 4));
+		dd.infdif = pk.reserve(T);           // filled when the pool is staged
 		dd.beta_rows = pk.addf(t.beta_rows, (size_t)t.nbeta_row * S);
 		dd.areafactor = pk.addf(t.areafactor, (size_t)m->period * A);
 		dd.Ntime = pk.addf(t.Ntime, S * G * G);
@@ -469,13 +494,14 @@ beep_status stage_inputs(beep_batch *q)
 	const beep_sim_batch *b = &q->b;
 	const int P = b->nparticle;
 	const size_t popsz = (size_t)m->A * m->C * m->DP;
+	const bool fast = b->form == BEEP_FORM_FAST;
 	TablePacker pk;
+	pk.copy = !fast;
 	beep_status st = pack_tables(m, b, pk, q->dirs);
 	if (st != BEEP_OK) return st;
-	const bool fast = b->form == BEEP_FORM_FAST;
 	Layout in;
-	size_t o_dirs = in.add(sizeof(GroupDir) * q->dirs.size()), o_f = in.add(8 * pk.f.size()),
-	       o_f32 = in.add(fast ? 4 * pk.f.size() : 0),
+	size_t o_dirs = in.add(sizeof(GroupDir) * q->dirs.size()), o_f = in.add(fast ? 0 : 8 * pk.fsize),
+	       o_f32 = in.add(fast ? 4 * pk.fsize : 0),
 	       o_i = in.add(4 * pk.i.size()), o_go = in.add(b->group_of ? 4 * (size_t)P : 0),
 	       o_so = in.add(b->stream_of ? 4 * (size_t)P : 0), o_pin = in.add(b->ti > 0 && !q->device_io ? 4 * popsz * P : 0),
 	       o_sc = in.add(4 * q->scored.size()), o_sp = in.add(4 * q->step_ptr.size()),
@@ -485,7 +511,7 @@ beep_status stage_inputs(beep_batch *q)
 	q->in_size = in.size;
 	char *h = (char *)q->in_host.ptr;
 	memcpy(h + o_dirs, q->dirs.data(), sizeof(GroupDir) * q->dirs.size());
-	memcpy(h + o_f, pk.f.data(), 8 * pk.f.size());
+	if (!fast) memcpy(h + o_f, pk.f.data(), 8 * pk.fsize);
 	if (!pk.i.empty()) memcpy(h + o_i, pk.i.data(), 4 * pk.i.size());
 	if (b->group_of) memcpy(h + o_go, b->group_of, 4 * (size_t)P);
 	if (b->stream_of) memcpy(h + o_so, b->stream_of, 4 * (size_t)P);
@@ -495,20 +521,43 @@ beep_status stage_inputs(beep_batch *q)
 	if (!q->step_obs.empty()) memcpy(h + o_sobs, q->step_obs.data(), 4 * q->step_obs.size());
 	if (!q->tasks.empty()) memcpy(h + o_tasks, q->tasks.data(), 4 * q->tasks.size());
 	// infectivity difference of each transition, Model::get_infectivity_dif (src/model.cc:820-823)
-	double *fpool = (double *)(h + o_f);
-	for (int g = 0; g < b->ngroup; g++) {
-		const double *inf = b->groups[g].infectivity;
-		for (int tr = 0; tr < m->T; tr++)
-			fpool[q->dirs[g].infdif + tr] = inf[m->trans_to_h[tr]] - inf[m->trans_from_h[tr]];
-	}
-	if (fast) {
+	if (!fast) {
+		double *fpool = (double *)(h + o_f);
+		for (int g = 0; g < b->ngroup; g++) {
+			const double *inf = b->groups[g].infectivity;
+			for (int tr = 0; tr < m->T; tr++)
+				fpool[q->dirs[g].infdif + tr] = inf[m->trans_to_h[tr]] - inf[m->trans_from_h[tr]];
+		}
+	} else {
+		// the fast form's FP32 pool, converted from the caller's arrays by up to 8 threads
 		float *f32 = (float *)(h + o_f32);
-		for (size_t k = 0; k < pk.f.size(); k++) f32[k] = (float)fpool[k];
+		for (int g = 0; g < b->ngroup; g++) {
+			const double *inf = b->groups[g].infectivity;
+			for (int tr = 0; tr < m->T; tr++)
+				f32[q->dirs[g].infdif + tr] = (float)(inf[m->trans_to_h[tr]] - inf[m->trans_from_h[tr]]);
+		}
+		auto convert = [&](size_t k0, size_t k1) {
+			for (size_t k = k0; k < k1; k++) {
+				const TablePacker::Piece &pc = pk.pieces[k];
+				float *dst = f32 + pc.off;
+				for (size_t j = 0; j < pc.n; j++) dst[j] = (float)pc.src[j];
+			}
+		};
+		const size_t np = pk.pieces.size();
+		const unsigned hw = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+		const unsigned nth = pk.fsize > ((size_t)1 << 20) && np >= 2 * hw ? hw : 1;
+		if (nth == 1) {
+			convert(0, np);
+		} else {
+			std::vector<std::thread> th;
+			for (unsigned t = 0; t < nth; t++) th.emplace_back(convert, np * t / nth, np * (t + 1) / nth);
+			for (auto &x : th) x.join();
+		}
 	}
 	char *di = (char *)q->in_dev.ptr;
 	BatchDev &bd = q->bd;
 	bd.dirs = (const GroupDir *)(di + o_dirs);
-	bd.fpool = (const double *)(di + o_f);
+	bd.fpool = fast ? nullptr : (const double *)(di + o_f);
 	bd.ipool = (const int32_t *)(di + o_i);
 	bd.group_of = b->group_of ? (const int32_t *)(di + o_go) : nullptr;
 	bd.stream_of = b->stream_of ? (const uint32_t *)(di + o_so) : nullptr;
