@@ -33,6 +33,7 @@ UNITS = {
     "abc_weights.cu": [],
     "mbp.cu": [],
     "mbp_fast.cu": [],
+    "mbp_fast_ctas.cu": [],
     "serve.cu": [],
 }
 

@@ -294,6 +294,8 @@ def lib():
         L.beep_mbp_acceptance.argtypes = [C.c_int32] + [C.c_double] * 6
         L.beep_mbp_acceptance.restype = C.c_double
         L.beep_mbp_read_state.argtypes = [C.c_void_p, C.c_int32, _i32p, _f64p]
+        L.beep_mbp_ctas_per_sm.argtypes = [C.c_void_p]
+        L.beep_mbp_ctas_per_sm.restype = C.c_int32
         for f in ("beep_mbp_create", "beep_mbp_destroy", "beep_mbp_initialise", "beep_mbp_propose", "beep_mbp_accept",
                   "beep_mbp_state_likelihood", "beep_mbp_read_state"):
             getattr(L, f).restype = C.c_int32
@@ -561,6 +563,10 @@ class MbpChains:
         mean = np.zeros(tn.shape, np.float64)
         check(lib().beep_mbp_read_state(self.h, chain, _ptr(tn, C.c_int32), _ptr(mean, C.c_double)))
         return tn, mean
+
+    def ctas_per_sm(self) -> int:
+        """Chains per SM of the fast form's last prepared batch (0: plain form or none yet)."""
+        return lib().beep_mbp_ctas_per_sm(self.h)
 
     def close(self):
         if self.h:

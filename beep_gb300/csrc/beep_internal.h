@@ -129,5 +129,7 @@ int launch_sim_fast_chain(const ModelDev &m, const BatchDev &b, void *stream);  
 int fast_ctas_prepare();                         // constant tables of sim_fast_ctas.cu
 int fast_ctas_max(int G);                        // most 320-thread CTAs per SM for G ages
 int launch_sim_fast_ctas(const ModelDev &m, const BatchDev &b, size_t smem, void *stream);   // sim_fast_ctas.cu
+int fast_chain_ctas_prepare();                   // constant tables of mbp_fast_ctas.cu
+int launch_sim_fast_chain_ctas(const ModelDev &m, const BatchDev &b, size_t smem, void *stream);   // mbp_fast_ctas.cu
 
 }  // namespace beep

@@ -270,6 +270,7 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	m->trans_from_h.assign(d->trans_from, d->trans_from + T);
 	m->trans_to_h.assign(d->trans_to, d->trans_to + T);
 	cudaGetDevice(&m->device);
+	cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, m->device);
 
 	Layout L;
 	size_t o_tf = L.add(4 * T), o_tt = L.add(4 * T), o_age = L.add(4 * DPS), o_diag = L.add(8 * A),
@@ -584,7 +585,7 @@ beep_status beep_batch_create(beep_model *m, const beep_sim_batch *b, beep_batch
 }  // extern "C"
 
 beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, bool device_io, beep_batch **out,
-                                        bool device_traj, bool allow_tc)
+                                        bool device_traj, bool allow_tc, bool allow_ctas)
 {
 	// a count trajectory is written: to the batch's output (transnum_out), or to a
 	// device buffer the caller sets in bd.tn_traj before each launch (device_traj)
@@ -702,9 +703,10 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 		// force of infection and observation slots (automatic: only if the one-CTA layout
 		// keeps the state in global memory too); the matrix is read through L1 unless it
 		// fits beside every CTA's share.  Automatic: from three CTAs per SM (two run no
-		// faster than one CTA of 640 threads).
+		// faster than one CTA of 640 threads), and only for batches large enough to
+		// fill the SMs that way.
 		const int opt_ctas = option_fast_ctas() != 0 ? option_fast_ctas() : m->tuned_ctas;
-		if (allow_tc && !q->bd.foi_tc && opt_ctas != 1 && fast_pick_threads(m->dev) == 640) {
+		if (allow_ctas && !q->bd.foi_tc && opt_ctas != 1 && fast_pick_threads(m->dev) == 640) {
 			const int kmax = std::min(opt_ctas >= 2 ? opt_ctas : 4, fast_ctas_max(m->G));
 			const int kmin = opt_ctas >= 2 ? 2 : 3;
 			auto fit = [&](size_t bytes) { return (int)std::min<size_t>((size_t)kmax, kSmemPerSM / (bytes + 1024)); };
@@ -714,6 +716,21 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 			if (k < kmin && (q->state_global || opt_ctas >= 2)) {
 				glob = true;
 				k = fit(fast_smem_bytes(m->dev, nslots, false, nefo, true, tnrows, ps, false, kDualThreads));
+			}
+			if (opt_ctas == 0 && k >= kmin) {
+				// automatic: the layout with the shortest expected time, waves of k CTAs per SM
+				// each taking k / gain[k] of a one-CTA wave (gain measured on the ABC-SMC
+				// workload: 1, 1.0, 1.18, 1.26) -- small batches keep more SMs busy with one
+				const double gain[5] = {0.0, 1.0, 1.0, 1.18, 1.26};
+				auto cost = [&](int kk) {
+					const long long per_wave = (long long)kk * std::max(1, m->sms);
+					return (double)((P + per_wave - 1) / per_wave) * kk / gain[kk];
+				};
+				int best = 1;
+				for (int kk = 3; kk <= k; kk++)
+					if (cost(kk) < cost(best)) best = kk;
+				if (best == 1) k = 0;
+				else k = best;
 			}
 			if (k >= kmin) {
 				q->bd.nt = kDualThreads;

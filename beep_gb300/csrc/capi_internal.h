@@ -93,6 +93,7 @@ void build_obs_lists(const int32_t *sett_i, const int32_t *sett_f, int nobs, int
 
 struct beep_model {
 	int device = 0;
+	int sms = 152;                // SMs of the device
 	cudaStream_t stream = nullptr;
 	beep::ModelDev dev{};
 	beep::DevBuf model_mem;
@@ -137,10 +138,10 @@ namespace beep {
 // With device_traj the kernels write every step's transition counts to a
 // device buffer the caller sets in bd.tn_traj ([P][tf-ti][A][T][DP]) before
 // each launch.
-// allow_tc = false keeps the fast form on its base kernel: FP32 SIMT force of
-// infection, one particle per SM.
+// allow_tc = false keeps the fast form's force of infection on FP32 SIMT;
+// allow_ctas = false keeps it at one particle per SM.
 beep_status batch_create_internal(beep_model *m, const beep_sim_batch *b, bool device_io, beep_batch **out,
-                                  bool device_traj = false, bool allow_tc = true);
+                                  bool device_traj = false, bool allow_tc = true, bool allow_ctas = true);
 // beep_batch_download in two halves: the device->host copy enqueued on the
 // model's stream, and (once that copy completed) the status check and the
 // copy into the caller's arrays.

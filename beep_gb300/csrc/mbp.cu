@@ -13,6 +13,7 @@
 // no state is ever copied.  The kernels are the plain FP64 form's
 // (sim_plain.cu, modes 1-3), which reproduce the reference's counts bit for
 // bit under the keyed variate stream.
+#include <algorithm>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -91,7 +92,7 @@ beep_status run_chains(beep_mbp_chains *c, const beep_mbp_request *r, int mode, 
 	} else {
 		if (q) beep_batch_destroy(q);
 		c->q[slot] = nullptr;
-		st = batch_create_internal(m, &b, false, &q, false, false);
+		st = batch_create_internal(m, &b, false, &q, false, false, true);
 		if (st != BEEP_OK) return st;
 		c->q[slot] = q;
 		c->q_ngroup[slot] = b.ngroup;
@@ -253,6 +254,15 @@ BEEP_API double beep_mbp_acceptance(int32_t cutoff_mode, double invT, double EFc
 	}
 	if (al > 1) al = 1;
 	return al;
+}
+
+BEEP_API int32_t beep_mbp_ctas_per_sm(const beep_mbp_chains *c)
+{
+	if (!c) return 0;
+	int32_t k = 0;
+	for (beep_batch *q : c->q)
+		if (q) k = std::max(k, beep_batch_ctas_per_sm(q));
+	return k;
 }
 
 BEEP_API beep_status beep_mbp_read_state(beep_mbp_chains *c, int32_t chain, int32_t *transnum_out,

@@ -8,7 +8,11 @@
 
 namespace beep {
 
-int fast_chain_prepare() { return prepare_constants(); }
+int fast_chain_prepare()
+{
+	const int e = prepare_constants();
+	return e != 0 ? e : fast_chain_ctas_prepare();
+}
 
 namespace {
 
@@ -28,9 +32,11 @@ int launch_chain_nt(const ModelDev &m, const BatchDev &b, size_t smem, cudaStrea
 int launch_sim_fast_chain(const ModelDev &m, const BatchDev &b, void *stream)
 {
 	if (m.G > 16 || m.T > kMaxT || b.foi_tc || !b.ch_tn || !b.ch_mean_f) return (int)cudaErrorInvalidValue;
+	const int nt = b.nt > 0 ? b.nt : fast_pick_threads(m);
 	const size_t smem = fast_smem_bytes(m, b.nslots, b.m_in_smem != 0, b.nefoi_stage, b.gstate != nullptr,
-	                                    b.tn_full ? m.T : m.tn_rows, b.pop_single != 0, b.tn_smem != 0);
-	const int nt = fast_pick_threads(m);
+	                                    b.tn_full ? m.T : m.tn_rows, b.pop_single != 0, b.tn_smem != 0, nt);
+	if (nt == kDualThreads) return launch_sim_fast_chain_ctas(m, b, smem, stream);
+	if (nt != fast_pick_threads(m)) return (int)cudaErrorInvalidValue;
 	const int e = prepare_constants();
 	if (e != 0) return e;
 	cudaStream_t st = (cudaStream_t)stream;

@@ -351,6 +351,9 @@ BEEP_API double beep_mbp_acceptance(int32_t cutoff_mode, double invT, double EFc
  * and/or transmean of the same shape (either may be NULL). */
 BEEP_API beep_status beep_mbp_read_state(beep_mbp_chains *chains, int32_t chain, int32_t *transnum_out,
                                          double *transmean_out);
+/* Chains resident per SM in the fast form's last prepared batch (1..4; 0 for
+ * the plain form or before the first call). */
+BEEP_API int32_t beep_mbp_ctas_per_sm(const beep_mbp_chains *chains);
 
 /* ---- Serving: continuous batching of requests on one GPU -----------------
  * A server runs simulation and likelihood requests of any model size

@@ -168,8 +168,8 @@ def test_several_particles_per_sm_follow_fp64(ctas_option):
     """Two to four 320-thread CTAs per SM (smaller register budget, more warps)
     run the same arithmetic per column as one 640-thread CTA: the particles
     follow the FP64 trajectories and score them within the fast-form tolerance,
-    whichever layout runs; the automatic choice takes four for a model whose
-    state is small."""
+    whichever layout runs; the automatic choice takes four for a batch that
+    fills the SMs four deep and one for a small batch."""
     from beep_gb300 import model_builder as mb, synth
     w = synth.seir_hd_small(seed=20260203, narea=100, nage=4, days=60, name="mid3")
     m = capi.Model(mb.model_arrays(w))
@@ -181,7 +181,7 @@ def test_several_particles_per_sm_follow_fp64(ctas_option):
     for k in (0, 1, 2, 3, 4):
         ctas_option("fast_ctas_per_sm", k)
         db = capi.DeviceBatch(dm, capi.Batch(m, [t], P, 11, want_transnum=True, want_pop=True, form=capi.FORM_FAST))
-        assert db.ctas_per_sm() == (4 if k == 0 else k), (k, db.ctas_per_sm())
+        assert db.ctas_per_sm() == (1 if k == 0 else k), (k, db.ctas_per_sm())   # automatic: 96 particles fill no SM 4-deep
         assert db.foi_path() == capi.FOI_SIMT
         f = db.run()
         db.close()
@@ -193,6 +193,12 @@ def test_several_particles_per_sm_follow_fp64(ctas_option):
     for k in (3, 4):
         assert np.array_equal(res[k].transnum, res[2].transnum)
         assert np.array_equal(res[k].L, res[2].L)
+    # automatic choice by expected waves: four per SM once the batch fills them
+    ctas_option("fast_ctas_per_sm", 0)
+    for P2, want in ((152, 1), (4 * 152 * 2, 4)):
+        db = capi.DeviceBatch(dm, capi.Batch(m, [t], P2, 11, form=capi.FORM_FAST))
+        assert db.ctas_per_sm() == want, (P2, db.ctas_per_sm())
+        db.close()
     dm.close()
 
 

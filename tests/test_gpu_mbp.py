@@ -177,3 +177,51 @@ def test_fast_chains_state_round_trip(device):
     a.close()
     c.close()
     dm.close()
+
+
+@pytest.fixture
+def ctas_option(device):
+    yield capi.set_option
+    capi.set_option("fast_ctas_per_sm", 0)
+
+
+def test_fast_chains_several_per_sm_follow_plain_chains(ctas_option):
+    """Fast chains in 320-thread CTAs, four per SM, on a model of 70 areas x 4
+    ages (280 columns, 30 days): the same arithmetic per column as one
+    640-thread CTA per SM (identical states, log-likelihoods within 1e-6), and
+    the initial states and coupled proposals follow the plain FP64 chains."""
+    from beep_gb300 import model_builder as mb, synth
+    w = synth.seir_hd_small(seed=20260205, narea=70, nage=4, days=30, name="mbp70")
+    w.obs_kind = "hosp_pop"
+    m = capi.Model(mb.model_arrays(w))
+    t = capi.Tables(mb.param_tables(w))
+    nc = 24
+    go = np.zeros(nc, np.int32)
+    dm = capi.DeviceModel(m)
+    res = {}
+    for form, k in ((capi.FORM_PLAIN_FP64, 0), (capi.FORM_FAST, 1), (capi.FORM_FAST, 4)):
+        ctas_option("fast_ctas_per_sm", k)
+        ch = capi.MbpChains(dm, nc, form=form)
+        L0 = ch.initialise([t], 17, group_of=go, stream_of=np.arange(nc) + 100)
+        tn0 = np.stack([ch.read_state(i)[0] for i in range(nc)])
+        L1 = ch.propose([t], 18, group_of=go, stream_of=np.arange(nc) + 400, inf_update=capi.INF_DIF_UPDATE)
+        ch.accept(np.ones(nc, np.uint8))
+        tn1 = np.stack([ch.read_state(i)[0] for i in range(nc)])
+        if form == capi.FORM_FAST:
+            assert ch.ctas_per_sm() == k, (k, ch.ctas_per_sm())
+        res[(form, k)] = (L0, tn0, L1, tn1)
+        ch.close()
+    # same draws; the log-likelihood's per-thread partial sums group differently
+    r1, r4 = res[(capi.FORM_FAST, 1)], res[(capi.FORM_FAST, 4)]
+    assert np.array_equal(r1[1], r4[1]) and np.array_equal(r1[3], r4[3])
+    np.testing.assert_allclose(r4[0], r1[0], rtol=1e-6)
+    np.testing.assert_allclose(r4[2], r1[2], rtol=1e-6)
+    pL0, ptn0, pL1, ptn1 = res[(capi.FORM_PLAIN_FP64, 0)]
+    fL0, ftn0, fL1, ftn1 = res[(capi.FORM_FAST, 4)]
+    same0 = np.array([np.array_equal(ptn0[i], ftn0[i]) for i in range(nc)])
+    assert same0.mean() >= 0.5, same0.mean()
+    np.testing.assert_allclose(fL0[same0], pL0[same0], rtol=1e-6)
+    same1 = same0 & np.array([np.array_equal(ptn1[i], ftn1[i]) for i in range(nc)])
+    assert same1.mean() >= 0.3, same1.mean()
+    np.testing.assert_allclose(fL1[same1], pL1[same1], rtol=1e-6)
+    dm.close()
