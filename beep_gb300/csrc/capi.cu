@@ -356,6 +356,9 @@ beep_status beep_model_destroy(beep_model *m)
 {
 	if (!m) return BEEP_OK;
 	if (m->stream) cudaStreamSynchronize(m->stream);
+	for (beep_batch *q : m->pf.q) beep_batch_destroy(q);
+	m->pf.q.clear();
+	m->pf.work.release();
 	m->model_mem.release();
 	if (m->stream) cudaStreamDestroy(m->stream);
 	delete m;

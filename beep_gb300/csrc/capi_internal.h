@@ -105,6 +105,16 @@ struct beep_model {
 	int32_t max_obs_spline = -1;
 	int32_t tuned_foi = 0;        // fast-form FOI path chosen by beep_autotune (0: none)
 	int32_t tuned_ctas = 0;       // fast-form particles per SM chosen by beep_autotune (0: none)
+	// beep_pf_loglik's prepared section batches and buffers, kept while later calls
+	// have the same particles, sections, form and lineage request (PMCMC calls it
+	// once per proposal with new tables only)
+	struct PfCache {
+		int32_t N = 0, form = -1;
+		bool lineage = false;
+		std::vector<int32_t> ti, tf;
+		std::vector<beep_batch *> q;
+		beep::DevBuf work;
+	} pf;
 	std::mutex mu;
 };
 

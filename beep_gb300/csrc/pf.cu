@@ -20,6 +20,7 @@
 // plain form agree with the reference's to the last bits).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -123,35 +124,60 @@ extern "C" BEEP_API beep_status beep_pf_loglik(beep_model *m, const beep_pf_requ
 	const size_t popsz = (size_t)m->A * m->C * m->DP;
 	cudaStream_t st = m->stream;
 
-	// one prepared batch per section (tables staged and uploaded once per call)
-	std::vector<beep_batch *> q(ns, nullptr);
-	auto cleanup = [&]() {
-		for (auto *x : q) beep_batch_destroy(x);
-	};
-	std::vector<double> Lhost_dummy(1);
-	for (int k = 0; k < ns; k++) {
-		beep_sim_batch b{};
-		b.nparticle = N; b.ngroup = 1; b.groups = r->tables; b.seed = r->seed;
-		b.ti = r->section_ti[k]; b.tf = r->section_tf[k];
-		b.form = r->form;
-		beep_status s = batch_create_internal(m, &b, true, &q[k], r->lineage_transnum_out != nullptr);
-		if (s != BEEP_OK) { std::string e = beep_last_error(); cleanup(); return fail(s, e); }
-	}
-	const size_t tnsz = (size_t)m->A * m->T * m->DP;
+	// one prepared batch per section, kept on the model for later calls of the same
+	// shape (then only the tables are staged again and the keys changed)
 	const bool lineage = r->lineage_transnum_out != nullptr;
+	beep_model::PfCache &pc = m->pf;
+	auto drop_cache = [&]() {
+		for (auto *x : pc.q) beep_batch_destroy(x);
+		pc.q.clear();
+		pc.N = 0;
+		pc.form = -1;
+	};
+	const bool same = pc.N == N && pc.form == r->form && pc.lineage == lineage && (int)pc.q.size() == ns &&
+	                  std::equal(pc.ti.begin(), pc.ti.end(), r->section_ti) &&
+	                  std::equal(pc.tf.begin(), pc.tf.end(), r->section_tf);
+	if (!same) {
+		drop_cache();
+		pc.q.assign(ns, nullptr);
+		for (int k = 0; k < ns; k++) {
+			beep_sim_batch b{};
+			b.nparticle = N; b.ngroup = 1; b.groups = r->tables; b.seed = r->seed;
+			b.ti = r->section_ti[k]; b.tf = r->section_tf[k];
+			b.form = r->form;
+			beep_status s = batch_create_internal(m, &b, true, &pc.q[k], lineage);
+			if (s != BEEP_OK) { std::string e = beep_last_error(); drop_cache(); return fail(s, e); }
+		}
+		pc.N = N;
+		pc.form = r->form;
+		pc.lineage = lineage;
+		pc.ti.assign(r->section_ti, r->section_ti + ns);
+		pc.tf.assign(r->section_tf, r->section_tf + ns);
+	} else {
+		for (int k = 0; k < ns; k++) {
+			beep_batch *b = pc.q[k];
+			b->b.groups = r->tables;
+			b->b.seed = r->seed;
+			b->bd.k0 = (uint32_t)r->seed;
+			b->bd.k1 = (uint32_t)(r->seed >> 32);
+			beep_status s = beep_batch_stage(b);
+			if (s != BEEP_OK) { std::string e = beep_last_error(); drop_cache(); return fail(s, e); }
+		}
+	}
+	std::vector<beep_batch *> &q = pc.q;
+	const size_t tnsz = (size_t)m->A * m->T * m->DP;
 	Layout L;
 	const size_t o_tn = L.add(lineage ? 4 * tnsz * (size_t)m->S * N : 0);
 	const size_t o_pa = L.add(4 * popsz * N), o_pb = L.add(4 * popsz * N), o_L = L.add(8 * (size_t)ns * N),
 	             o_w = L.add(8 * (size_t)N), o_ws = L.add(8 * (size_t)N), o_sel = L.add(4 * (size_t)N),
 	             o_bp = L.add(4 * (size_t)N), o_ex = L.add(4 * (size_t)N), o_ob = L.add(8 * (size_t)ns),
-	             o_anc = L.add(4 * (size_t)ns * N), o_st = L.add(4);
-	DevBuf work;
-	cudaError_t e = work.reserve(L.size);
-	if (e != cudaSuccess) { cleanup(); return fail(BEEP_OOM, std::string("particle filter buffers: ") + cudaGetErrorString(e)); }
-	char *d = (char *)work.ptr;
+	             o_anc = L.add(4 * (size_t)ns * N), o_st = L.add(4), o_pst = L.add(4 * (size_t)ns * N);
+	cudaError_t e = pc.work.reserve(L.size);
+	if (e != cudaSuccess) { drop_cache(); return fail(BEEP_OOM, std::string("particle filter buffers: ") + cudaGetErrorString(e)); }
+	char *d = (char *)pc.work.ptr;
 	int32_t *popA = (int32_t *)(d + o_pa), *popB = (int32_t *)(d + o_pb);
 	double *Lall = (double *)(d + o_L), *obsec = (double *)(d + o_ob);
-	int32_t *anc = (int32_t *)(d + o_anc), *pst = (int32_t *)(d + o_st);
+	int32_t *anc = (int32_t *)(d + o_anc), *pst = (int32_t *)(d + o_st), *secst = (int32_t *)(d + o_pst);
 	beep_status status = BEEP_OK;
 	std::string err;
 	auto bail = [&](beep_status s, const std::string &msg) { status = s; err = msg; };
@@ -172,11 +198,16 @@ extern "C" BEEP_API beep_status beep_pf_loglik(beep_model *m, const beep_pf_requ
 		                                         anc + (size_t)k * N, pst);
 		if (k + 1 < ns) pf_gather<<<152 * 4, 256, 0, st>>>(popA, popB, (const int32_t *)(d + o_bp), N, (int)popsz);
 		if (cudaGetLastError() != cudaSuccess) bail(BEEP_DEVICE_ERROR, "bootstrap launch");
+		// the section's per-particle statuses, gathered for one copy at the end
+		if (cudaMemcpyAsync(secst + (size_t)k * N, b->bd.status, 4 * (size_t)N, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+			bail(BEEP_DEVICE_ERROR, "status gather");
 	}
 	std::vector<double> ob(ns);
+	std::vector<int32_t> ps((size_t)ns * N);
 	int32_t bst = 0;
 	if (status == BEEP_OK) {
 		e = cudaMemcpyAsync(ob.data(), obsec, 8 * (size_t)ns, cudaMemcpyDeviceToHost, st);
+		if (e == cudaSuccess) e = cudaMemcpyAsync(ps.data(), secst, 4 * (size_t)ns * N, cudaMemcpyDeviceToHost, st);
 		if (e == cudaSuccess) e = cudaMemcpyAsync(&bst, pst, 4, cudaMemcpyDeviceToHost, st);
 		if (e == cudaSuccess && r->L_out) e = cudaMemcpyAsync(r->L_out, Lall, 8 * (size_t)ns * N, cudaMemcpyDeviceToHost, st);
 		if (e == cudaSuccess && r->ancestors_out)
@@ -185,15 +216,12 @@ extern "C" BEEP_API beep_status beep_pf_loglik(beep_model *m, const beep_pf_requ
 		if (e != cudaSuccess) bail(BEEP_DEVICE_ERROR, cudaGetErrorString(e));
 	}
 	// per-particle statuses of the simulation launches
-	for (int k = 0; k < ns && status == BEEP_OK; k++) {
-		std::vector<int32_t> ps(N);
-		if (cudaMemcpy(ps.data(), q[k]->bd.status, 4 * (size_t)N, cudaMemcpyDeviceToHost) != cudaSuccess) {
-			bail(BEEP_DEVICE_ERROR, "status copy");
-			break;
-		}
+	for (int k = 0; k < ns && status == BEEP_OK; k++)
 		for (int p = 0; p < N; p++)
-			if (ps[p] != 0) { bail((beep_status)ps[p], "section " + std::to_string(k) + " particle " + std::to_string(p)); break; }
-	}
+			if (ps[(size_t)k * N + p] != 0) {
+				bail((beep_status)ps[(size_t)k * N + p], "section " + std::to_string(k) + " particle " + std::to_string(p));
+				break;
+			}
 	if (status == BEEP_OK && bst != 0) bail((beep_status)bst, "resampling found no particle (non-finite weights)");
 	if (status == BEEP_OK && lineage) {
 		// Mpi::particle_sample: start from the particle the last resampling put in slot
@@ -211,9 +239,10 @@ extern "C" BEEP_API beep_status beep_pf_loglik(beep_model *m, const beep_pf_requ
 		if (e != cudaSuccess) bail(BEEP_DEVICE_ERROR, std::string("lineage copy: ") + cudaGetErrorString(e));
 	}
 	cudaStreamSynchronize(st);
-	work.release();
-	cleanup();
-	if (status != BEEP_OK) return fail(status, err);
+	if (status != BEEP_OK) {
+		drop_cache();
+		return fail(status, err);
+	}
 	double total = 0.0;
 	for (int k = 0; k < ns; k++) total += ob[k];
 	*r->loglik_out = total;

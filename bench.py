@@ -247,6 +247,47 @@ def profile_traffic(kind: str, P: int):
     return float(m.group(1)) * P if m else None
 
 
+def run_particle_filter(reps: int, seed: int, N: int = 256, section_steps: int = 28):
+    """PMCMC likelihood estimates: the bootstrap particle filter of the
+    10-area x 3-age workload (dt 0.25, 100 days, 400 steps), N particles, one
+    parameter set, sections of 28 steps with multinomial resampling and the
+    ancestor-state gather on the device between sections.  Estimates per
+    second in both forms (each call is one full estimate: host in, estimate
+    out)."""
+    from beep_gb300 import capi, model_builder as mb, synth
+    w = synth.seir_hd_small()
+    arr0 = mb.model_arrays(w)
+    m0 = capi.Model(arr0)
+    t = capi.Tables(mb.param_tables(w))
+    dm = capi.DeviceModel(m0)
+    truth = dm.simulate(capi.Batch(m0, [t], 1, seed ^ 0x5EED, want_transnum=True, want_pop_traj=True, want_L=False,
+                                   form=capi.FORM_FAST))
+    dm.close()
+    rng = np.random.default_rng(seed)
+    y, sd = mb.observed_from_trajectory(arr0, truth.transnum[0], truth.pop_traj[0], rng)
+    arr = dict(arr0)
+    arr["obs_value"], arr["obs_sd"] = y, sd
+    m = capi.Model(arr)
+    S = m.ndivision
+    sections = [(a, min(a + section_steps, S)) for a in range(0, S, section_steps)]
+    dm = capi.DeviceModel(m)
+    out = {"workload": "pmcmc_pf_10x3", "particles": N, "steps": S, "sections": len(sections),
+           "timing": "host wall clock per estimate (beep_pf_loglik)"}
+    for form, name in ((capi.FORM_FAST, "fast"), (capi.FORM_PLAIN_FP64, "plain_fp64")):
+        for k in range(2):                                   # warm-up
+            dm.pf_loglik(t, N, seed + k, 5, 1.0, sections, form=form)
+        est = []
+        t0 = time.perf_counter()
+        for k in range(reps):
+            est.append(dm.pf_loglik(t, N, seed + 100 + k, 5, 1.0, sections, form=form)[0])
+        dt = (time.perf_counter() - t0) / reps
+        out[name] = {"estimates_per_s": 1.0 / dt, "ms_per_estimate": dt * 1e3,
+                     "value": N * m.narea * m.nage * S / dt, "unit": "particle.area.group.steps/s",
+                     "loglik_mean": float(np.mean(est)), "loglik_sd": float(np.std(est))}
+    dm.close()
+    return out
+
+
 def run_mbp_chains(sweeps: int, seed: int, nchain: int = 128, plain_sweeps: int = 1):
     """MBP chains of uneven size: nchain chains on each of the models 20x2,
     80x4, 200x6 and 350x10 (areas x ages, dt 0.5, 200 days, weekly hospital
@@ -477,6 +518,9 @@ def run_ours(args, rank, ws, dist):
     mbp = None
     if args.mbp_sweeps > 0 and ws == 1:
         mbp = run_mbp_chains(args.mbp_sweeps, args.seed + 99)
+    pf = None
+    if args.pf_estimates > 0 and ws == 1:
+        pf = run_particle_filter(args.pf_estimates, args.seed + 777)
     serving = None
     if args.serve_requests > 0 and ws == 1:
         serving = run_serving(args.serve_requests, 200.0, args.seed + 4242, 200 << 30, 8)
@@ -505,6 +549,7 @@ def run_ours(args, rank, ws, dist):
         "cpu_baseline": cpu,
         "serving": serving,
         "mbp_chains": mbp,
+        "particle_filter": pf,
     }
     print(json.dumps(line))
     db.close()
@@ -532,6 +577,8 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=0, help="time the plain form over this many steps (0: all)")
     ap.add_argument("--mbp-sweeps", type=int, default=3,
                     help="sweeps of the MBP-chain workload (4 x 128 chains of uneven size) after the main measurement")
+    ap.add_argument("--pf-estimates", type=int, default=10,
+                    help="particle-filter likelihood estimates (256 particles, 10 x 3 model) per form after the main measurement")
     ap.add_argument("--serve-requests", type=int, default=32,
                     help="requests of the serving stream (Poisson arrivals at 200/s) after the main measurement")
     args = ap.parse_args()

@@ -125,6 +125,33 @@ def test_particle_filter_fast_form_and_oracle(built):
     dm.close()
 
 
+def test_particle_filter_repeated_calls_reuse_prepared_sections(built):
+    """Calls of the same shape reuse the prepared section batches, with only the
+    tables and keys changed: each result equals that of a fresh model, in both
+    forms, with other parameter sets, seeds and shapes between the calls."""
+    b, m, tabs, seed = load("c0_pf")
+    N = 64
+    secs = m.sections
+    # a second parameter set: the transition rates and R(t) rows scaled
+    arr = dict(tabs[0].arr)
+    arr = {k: v.reshape(tabs[0].shapes[k]) for k, v in arr.items() if k in tabs[0].shapes}
+    arr["transrate"] = arr["transrate"] * 1.1
+    arr["beta_rows"] = arr["beta_rows"] * 0.9
+    t2 = capi.Tables(arr)
+    calls = [(tabs[0], seed + 1, capi.FORM_PLAIN_FP64, N), (t2, seed + 2, capi.FORM_PLAIN_FP64, N),
+             (tabs[0], seed + 3, capi.FORM_FAST, N), (t2, seed + 4, capi.FORM_FAST, N),
+             (tabs[0], seed + 5, capi.FORM_FAST, 32), (t2, seed + 6, capi.FORM_FAST, N)]
+    dm = capi.DeviceModel(m)
+    reused = [dm.pf_loglik(t, n, sd, 9, 1.0, secs, form=f) for t, sd, f, n in calls]
+    dm.close()
+    for (t, sd, f, n), got in zip(calls, reused):
+        fresh = capi.DeviceModel(m)
+        want = fresh.pf_loglik(t, n, sd, 9, 1.0, secs, form=f)
+        fresh.close()
+        assert got[0] == want[0]
+        assert np.array_equal(got[1], want[1]) and np.array_equal(got[2], want[2]) and np.array_equal(got[3], want[3])
+
+
 def test_prediction_multipliers_match_oracle(built):
     """PREDICTION-mode modifications (efoi_mult, transmean_mult; src/state.cc:415,
     446-453): the plain form equals the oracle restatement bit for bit, the fast
