@@ -57,6 +57,10 @@ class Workload:
     covar_effect: List[float] = dataclasses.field(default_factory=list)
     matmod: List[dict] = dataclasses.field(default_factory=list)  # {"ages": [..], "bp": [...], "val": [...]}
     obs_kind: str = "cases_deaths"            # cases_deaths | cases_age | hosp_pop
+    # discrete strains (the reference's `strains` command): names, susceptibility and
+    # R factor values/priors as TOML strings, and the exposed seeds of each strain
+    # [NS][A][G] (the susceptibles start in the first strain)
+    strains: Optional[dict] = None
     # prior ranges (inference modes)
     R_prior: tuple = (0.5, 4.0)
     sigma_inv_prior: tuple = (2.0, 6.0)
@@ -145,17 +149,32 @@ def write_beep_inputs(w: Workload, outdir: str, obs_values: Optional[dict] = Non
                 f.write(",".join(_fmt(v) for v in w.geo[c]) + "\n")
     comps = ["S", "E", "I", "H", "R", "D"]
     with open(os.path.join(data, "init_pop.csv"), "w") as f:
-        f.write("area," + ("age," if G > 1 else "") + "compartment,population\n")
-        for c in range(A):
-            for a in range(G):
-                for co in comps:
-                    if co == "S":
-                        v = int(w.pop[c, a] - w.seed_E[c, a])
-                    elif co == "E":
-                        v = int(w.seed_E[c, a])
-                    else:
-                        v = 0
-                    f.write(f"{areas[c]}," + (f"{ages[a]}," if G > 1 else "") + f"{co},{v}\n")
+        if w.strains is None:
+            f.write("area," + ("age," if G > 1 else "") + "compartment,population\n")
+            for c in range(A):
+                for a in range(G):
+                    for co in comps:
+                        if co == "S":
+                            v = int(w.pop[c, a] - w.seed_E[c, a])
+                        elif co == "E":
+                            v = int(w.seed_E[c, a])
+                        else:
+                            v = 0
+                        f.write(f"{areas[c]}," + (f"{ages[a]}," if G > 1 else "") + f"{co},{v}\n")
+        else:
+            seeds = np.asarray(w.strains["seed_E"])
+            f.write("area," + ("age," if G > 1 else "") + "strain,compartment,population\n")
+            for c in range(A):
+                for a in range(G):
+                    for st, sn in enumerate(w.strains["names"]):
+                        for co in comps:
+                            if co == "S":
+                                v = int(w.pop[c, a] - seeds[:, c, a].sum()) if st == 0 else 0
+                            elif co == "E":
+                                v = int(seeds[st, c, a])
+                            else:
+                                v = 0
+                            f.write(f"{areas[c]}," + (f"{ages[a]}," if G > 1 else "") + f"{sn},{co},{v}\n")
 
     tables = data_tables(w)
     for tab in tables:
@@ -188,6 +207,11 @@ def write_beep_inputs(w: Workload, outdir: str, obs_values: Optional[dict] = Non
         'areas = "population.csv"',
         'init_pop = "init_pop.csv"',
     ]
+    if w.strains is not None:
+        sd = w.strains
+        lines.append('strains = {cats="' + " | ".join(sd["names"]) + f'", sus_value="{sd["sus_value"]}", '
+                     f'sus_prior="{sd["sus_prior"]}", Rfactor_value="{sd["Rfactor_value"]}", '
+                     f'Rfactor_prior="{sd["Rfactor_prior"]}"' + "}")
     if G > 1:
         lines.append('ages = {cats="' + " | ".join(ages) + '"}')
         lines.append('age_mixing_matrix = "age_mixing_matrix.csv"')
@@ -246,6 +270,21 @@ def data_tables(w: Workload) -> List[dict]:
     else:
         raise ValueError(w.obs_kind)
     return tabs
+
+
+def seir_hd_strains(seed: int = 20260104, narea: int = 5, nage: int = 2, days: int = 60, name: str = "strains") -> Workload:
+    """The small SEIR-H-D workload with two strains (the reference's `strains`
+    command, as in its two-strain example): the second strain with
+    susceptibility factor 0.7 relative to the first and R factor 1.4; exposed
+    seeds of both strains in different areas; daily cases and weekly deaths per
+    area summed over ages and strains."""
+    w = seir_hd_small(seed=seed, narea=narea, nage=nage, days=days, name=name)
+    seeds = np.zeros((2, narea, nage), np.int64)
+    seeds[0] = w.seed_E
+    seeds[1, narea - 1, 0] = 8
+    w.strains = {"names": ["s1", "s2"], "sus_value": "0.7 | *", "sus_prior": "MDir(0.5)",
+                 "Rfactor_value": "1.0 | 1.4", "Rfactor_prior": "Fixed(1) | Uniform(0.5,2)", "seed_E": seeds}
+    return w
 
 
 def abc_smc_large(seed: int = 20260001, narea: int = 150, nage: int = 4, days: int = 180,

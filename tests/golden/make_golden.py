@@ -156,7 +156,15 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
     ap.add_argument("--keep", default=None, help="keep the generated TOML/CSV inputs here")
+    ap.add_argument("--only", default=None, help="comma-separated fixture names to (re)generate; default all")
     a = ap.parse_args()
+    only = set(a.only.split(",")) if a.only else None
+    global make_fixture
+    _make = make_fixture
+
+    def make_fixture(name, *args, **kw):          # noqa: F811 -- skips fixtures not asked for
+        if only is None or name in only:
+            _make(name, *args, **kw)
     subprocess.run(["make", "-s", "-f", "oracle/Makefile.ref", f"REF={a.ref}", "-j8"], cwd=ROOT, check=True)
 
     # tiny: 4 areas x 3 ages, 40 days at dt 0.25
@@ -168,6 +176,10 @@ def main():
     # one age group (the reference's nage == 1 branch of get_NMI, src/state.cc:555-560)
     one = synth.seir_hd_small(seed=20260101, narea=5, nage=1, days=30, name="oneage")
     make_fixture("oneage_sim", one, npart=6, ntraj=2, seed=77)
+    # two strains: the susceptible shift to the first strain, per-strain infectious maps and
+    # R factors (src/state.cc:392-401, 223-290; src/model.cc:1318-1362)
+    strains = synth.seir_hd_strains()
+    make_fixture("strain_sim", strains, npart=8, ntraj=2, seed=0x5712A1)
     # the 10-area x 3-age plain PMCMC workload at full horizon
     c0 = synth.seir_hd_small(seed=20260000, narea=10, nage=3, days=100, name="c0")
     make_fixture("c0_sim", c0, npart=16, ntraj=1, seed=20260000)
