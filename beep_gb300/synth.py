@@ -181,16 +181,24 @@ def write_beep_inputs(w: Workload, outdir: str, obs_values: Optional[dict] = Non
         rows = tab["times"]
         cols = tab["columns"]
         vals = (obs_values or {}).get(tab["file"])
+        sd_col = tab.get("sd_col", True)
         with open(os.path.join(data, tab["file"]), "w") as f:
-            f.write("time," + ",".join(f"{c},{c} SD" for c in cols) + "\n")
+            f.write("time," + ",".join(f"{c},{c} SD" if sd_col else c for c in cols) + "\n")
             for r, t in enumerate(rows):
                 cells = []
-                for c in cols:
+                for j, c in enumerate(cols):
                     if vals is None:
-                        cells += ["0", "1"]
+                        cells += ["0", "1"] if sd_col else ["1"]
+                        continue
+                    v, sd = vals[c]
+                    nd = tab.get("nodata_every")
+                    if nd and (r + j) % nd == 0:
+                        x = "."                                   # no data
+                    elif tab.get("censor_below") is not None and v[r] < tab["censor_below"]:
+                        x = "*"                                   # below the table's threshold
                     else:
-                        v, sd = vals[c]
-                        cells += [str(int(v[r])), _fmt(sd[r])]
+                        x = str(int(v[r]))
+                    cells += [x, _fmt(sd[r])] if sd_col else [x]
                 f.write(f"{t}," + ",".join(cells) + "\n")
 
     nk = len(w.R_bp)
@@ -267,6 +275,23 @@ def data_tables(w: Workload) -> List[dict]:
         tabs.append(dict(file="hosp.csv", times=list(range(0, w.days, 7)), columns=areas,
                          toml=dict(type="population", observation="H", obsmodel="normal load",
                                    geo_dep="area", file="hosp.csv")))
+    elif w.obs_kind == "obs_models":
+        # every observation model the reference parses (src/inputs.cc:413-473) with
+        # censored ('*' below the table's threshold) and missing ('.') entries
+        tabs.append(dict(file="cases.csv", times=list(range(0, w.days)), columns=areas, sd_col=False,
+                         toml=dict(type="transition", observation="E->I", timestep="1", obsmodel="normal 10%",
+                                   geo_dep="area", file="cases.csv")))
+        tabs.append(dict(file="deaths.csv", times=list(range(0, w.days - 6, 7)), columns=areas, sd_col=False,
+                         censor_below=5, nodata_every=5,
+                         toml=dict(type="transition", observation="H->D", timestep="7", obsmodel="poisson",
+                                   threshold="5", geo_dep="area", file="deaths.csv")))
+        tabs.append(dict(file="hosp.csv", times=list(range(0, w.days, 7)), columns=areas, sd_col=False,
+                         nodata_every=7,
+                         toml=dict(type="population", observation="H", obsmodel="normal 30",
+                                   geo_dep="area", file="hosp.csv")))
+        tabs.append(dict(file="cases_w.csv", times=list(range(0, w.days - 6, 7)), columns=areas, censor_below=20,
+                         toml=dict(type="transition", observation="E->I", timestep="7", obsmodel="normal load",
+                                   threshold="20", geo_dep="area", file="cases_w.csv")))
     else:
         raise ValueError(w.obs_kind)
     return tabs
@@ -284,6 +309,17 @@ def seir_hd_strains(seed: int = 20260104, narea: int = 5, nage: int = 2, days: i
     seeds[1, narea - 1, 0] = 8
     w.strains = {"names": ["s1", "s2"], "sus_value": "0.7 | *", "sus_prior": "MDir(0.5)",
                  "Rfactor_value": "1.0 | 1.4", "Rfactor_prior": "Fixed(1) | Uniform(0.5,2)", "seed_E": seeds}
+    return w
+
+
+def seir_hd_obs_models(seed: int = 20260105, narea: int = 4, nage: int = 2, days: int = 70,
+                       name: str = "obsmodels") -> Workload:
+    """The small SEIR-H-D workload observed through every observation model
+    the reference reads: normal with a percentage SD, Poisson with a threshold
+    (censored entries), normal with a fixed SD on populations, normal with
+    loaded SDs and a threshold; some entries missing."""
+    w = seir_hd_small(seed=seed, narea=narea, nage=nage, days=days, name=name)
+    w.obs_kind = "obs_models"
     return w
 
 

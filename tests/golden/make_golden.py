@@ -180,6 +180,9 @@ def main():
     # R factors (src/state.cc:392-401, 223-290; src/model.cc:1318-1362)
     strains = synth.seir_hd_strains()
     make_fixture("strain_sim", strains, npart=8, ntraj=2, seed=0x5712A1)
+    # every observation model: normal X%, Poisson with censoring, fixed-SD normal, loaded
+    # SDs with a threshold; missing entries (src/obsmodel.cc:245-305, src/data.cc:1589-1623)
+    make_fixture("obsmodel_sim", synth.seir_hd_obs_models(), npart=8, ntraj=2, seed=0x0B5E)
     # the 10-area x 3-age plain PMCMC workload at full horizon
     c0 = synth.seir_hd_small(seed=20260000, narea=10, nage=3, days=100, name="c0")
     make_fixture("c0_sim", c0, npart=16, ntraj=1, seed=20260000)
