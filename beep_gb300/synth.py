@@ -244,8 +244,23 @@ def write_beep_inputs(w: Workload, outdir: str, obs_values: Optional[dict] = Non
         "]",
         f'R_spline = [{{ value="{rval}", prior="{rprior}", bp="{bp}"}}]',
         f'efoi_spline = [{{ value="{_fmt(w.efoi)}"}}]',
-        "data_tables = [",
     ]
+    if w.covar is not None:
+        lines.append("area_covars = [")
+        for j, eff in enumerate(w.covar_effect):
+            lines.append(f'{{name="cov{j}", value="{_fmt(eff)}", prior="Uniform(-1,1)", func="linear"}},')
+        lines.append("]")
+    if w.matmod:
+        lines.append("age_mixing_modify = [")
+        for i, mm in enumerate(w.matmod):
+            mbp = "|".join(["start"] + [str(b) for b in mm["bp"][1:-1]] + ["end"])
+            names = "|".join(f"mm{i}_{k}" for k in range(len(mm["val"])))   # repeated break times need names
+            lines.append(f'{{type="row_column", agecat="{"|".join(ages[a] for a in mm["ages"])}", bp="{mbp}", '
+                         f'param="{names}", '
+                         f'value="{"|".join(_fmt(v) for v in mm["val"])}", '
+                         f'prior="{"|".join(f"Fixed({_fmt(v)})" for v in mm["val"])}"}},')
+        lines.append("]")
+    lines.append("data_tables = [")
     for tab in tables:
         lines.append("{" + ", ".join(f'{k}="{v}"' for k, v in tab["toml"].items()) + "},")
     lines += ["]"]
@@ -320,6 +335,21 @@ def seir_hd_obs_models(seed: int = 20260105, narea: int = 4, nage: int = 2, days
     loaded SDs and a threshold; some entries missing."""
     w = seir_hd_small(seed=seed, narea=narea, nage=nage, days=days, name=name)
     w.obs_kind = "obs_models"
+    return w
+
+
+def seir_hd_features(seed: int = 20260106, narea: int = 6, nage: int = 3, days: int = 60,
+                     name: str = "features") -> Workload:
+    """The small SEIR-H-D workload with the per-step tables that vary in time
+    and area: two area covariates (effects 0.3 and -0.2), stepped age-mixing
+    factors on two age groups from day 25, an external force of infection
+    (5 per day) and an R(t) spline of 7 knots."""
+    w = seir_hd_small(seed=seed, narea=narea, nage=nage, days=days, nknot=7, name=name)
+    rng = np.random.default_rng(seed + 1)
+    w.covar = rng.normal(0.0, 1.0, (2, narea))
+    w.covar_effect = [0.3, -0.2]
+    w.matmod = [{"ages": [0, 2], "bp": [0, 25, 25, days], "val": [1.0, 1.0, 0.6, 0.6]}]
+    w.efoi = 5.0
     return w
 
 

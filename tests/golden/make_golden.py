@@ -183,6 +183,9 @@ def main():
     # every observation model: normal X%, Poisson with censoring, fixed-SD normal, loaded
     # SDs with a threshold; missing entries (src/obsmodel.cc:245-305, src/data.cc:1589-1623)
     make_fixture("obsmodel_sim", synth.seir_hd_obs_models(), npart=8, ntraj=2, seed=0x0B5E)
+    # tables that vary with time and area: covariates (areafactor), stepped age-mixing
+    # factors (Ntime), external force of infection (src/model.cc:1144-1362, src/state.cc:403-423)
+    make_fixture("features_sim", synth.seir_hd_features(), npart=8, ntraj=2, seed=0xFEA7)
     # the 10-area x 3-age plain PMCMC workload at full horizon
     c0 = synth.seir_hd_small(seed=20260000, narea=10, nage=3, days=100, name="c0")
     make_fixture("c0_sim", c0, npart=16, ntraj=1, seed=20260000)
