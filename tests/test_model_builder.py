@@ -1,0 +1,41 @@
+"""The host restatement of State::set_param and the model set-up
+(beep_gb300/model_builder.py: Model::create_transrate, create_disc_spline,
+create_susceptibility, create_areafactor, create_Ntime, calculate_beta_from_R,
+src/model.cc:1010-1362; Data::geo_normalise and the age-matrix normalisation,
+src/data_matrix.cc:55-202) against the arrays the compiled reference itself
+produced for the golden fixtures' workloads."""
+import numpy as np
+import pytest
+
+from beep_gb300 import model_builder as mb, synth
+from golden_util import load
+
+WORKLOADS = {
+    "tiny_sim": lambda: synth.seir_hd_small(seed=20260100, narea=4, nage=3, days=40, name="tiny"),
+    "oneage_sim": lambda: synth.seir_hd_small(seed=20260101, narea=5, nage=1, days=30, name="oneage"),
+    "c0_sim": lambda: synth.seir_hd_small(seed=20260000, narea=10, nage=3, days=100, name="c0"),
+    # area covariates, stepped age-mixing factors, external force of infection, 7-knot R(t)
+    "features_sim": synth.seir_hd_features,
+}
+MODEL_KEYS = ("trans_from", "trans_to", "democatpos_age", "M_diag", "M_rowptr", "M_to", "M_val", "M_factor",
+              "pop_init", "obs_sett_i", "obs_sett_f", "obs_cell_ptr", "obs_cells", "obs_factor")
+TABLE_KEYS = ("transrate", "susceptibility", "infectivity", "beta_rows", "beta_row_of", "areafactor", "Ntime",
+              "geo_spline", "efoi_spline", "efoi_agedist", "efoi_ref")
+
+
+def _close(x, y):
+    x, y = np.asarray(x, np.float64).ravel(), np.asarray(y, np.float64).ravel()
+    assert x.shape == y.shape
+    np.testing.assert_allclose(x, y, rtol=1e-12, atol=1e-300)
+
+
+@pytest.mark.parametrize("name", sorted(WORKLOADS))
+def test_model_and_tables_match_reference(name):
+    b, _, _, _ = load(name)
+    w = WORKLOADS[name]()
+    arr = mb.model_arrays(w)
+    for k in MODEL_KEYS:
+        _close(arr[k], b[k])
+    t = mb.param_tables(w)
+    for k in TABLE_KEYS:
+        _close(t[k], b["g0." + k])
