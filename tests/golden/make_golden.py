@@ -186,6 +186,10 @@ def main():
     # tables that vary with time and area: covariates (areafactor), stepped age-mixing
     # factors (Ntime), external force of infection (src/model.cc:1144-1362, src/state.cc:403-423)
     make_fixture("features_sim", synth.seir_hd_features(), npart=8, ntraj=2, seed=0xFEA7)
+    # the particle filter on those tables (sections start part-way through the horizon;
+    # 84 days: the reference's sections need 10 times the weekly observation step)
+    make_fixture("features_pf", synth.seir_hd_features(days=84, name="features84"), npart=8, ntraj=1, seed=0xFEA8,
+                 pf=True, pfn=64)
     # the 10-area x 3-age plain PMCMC workload at full horizon
     c0 = synth.seir_hd_small(seed=20260000, narea=10, nage=3, days=100, name="c0")
     make_fixture("c0_sim", c0, npart=16, ntraj=1, seed=20260000)
