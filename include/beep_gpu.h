@@ -255,6 +255,10 @@ typedef struct beep_pf_request {
 	int32_t *lineage_transnum_out;
 } beep_pf_request;
 
+/* The section batches and device buffers a call prepares stay with the model
+ * and are reused by later calls with the same nparticle, sections, form and
+ * lineage request (only the tables and keys are staged again); they are freed
+ * by a call of another shape or by beep_model_destroy. */
 BEEP_API beep_status beep_pf_loglik(beep_model *model, const beep_pf_request *request);
 
 /* ABC-SMC importance weights of a generation (ABCSMC::calculate_particle_weight
