@@ -524,7 +524,6 @@ __global__ void __launch_bounds__(NT, MB) sim_fast_kernel(const ModelDev m, cons
 	// arrays [slot][chain][step][transition][column]
 	const int cmode = CH ? b.mode : 0;
 	const int cs_i = CH ? b.cur[p] : 0, cs_p = 1 - cs_i;
-	const bool cwrites = cmode == 1 || cmode == 3;
 	float Lst = 0.f, Lstc = 0.f;            // mode 2: compensated state log-likelihood of this thread
 
 	FastSmem s;
