@@ -73,7 +73,6 @@ int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream)
 		smem = b.tc_smem_off + fast_tc_smem_bytes(m);
 	}
 	if (nt != pick_threads(m) && (nt != kDualThreads || b.foi_tc)) return (int)cudaErrorInvalidValue;
-	const int NSA = m.NS * m.A;
 	{
 		const int e = fast_prepare();
 		if (e != 0) return e;
