@@ -918,12 +918,13 @@ beep_status beep_autotune(beep_model *m, const beep_sim_batch *b, int32_t *chose
 {
 	if (!m || !b) return fail(BEEP_BAD_INPUT, "null argument");
 	if (b->form != BEEP_FORM_FAST) return fail(BEEP_BAD_INPUT, "the autotuner chooses among fast-form kernels");
-	// a sample of the batch: two waves of particles over the first steps of its range
+	// a sample of the batch: its first particles over the first steps of its range
 	beep_sim_batch t = *b;
 	int dev_sms = 152;
 	cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, m->device);
-	t.nparticle = std::min(b->nparticle, 2 * dev_sms);
-	t.tf = std::min(b->tf, b->ti + 120);
+	// (two waves of the four-per-SM layout: every candidate fills the SMs alike)
+	t.nparticle = std::min(b->nparticle, 8 * dev_sms);
+	t.tf = std::min(b->tf, b->ti + 60);
 	t.L_out = nullptr;
 	t.pop_out = nullptr;
 	t.transnum_out = nullptr;
@@ -957,7 +958,9 @@ beep_status beep_autotune(beep_model *m, const beep_sim_batch *b, int32_t *chose
 		if (ms < best) { best = ms; best_foi = c[0]; best_ctas = c[1]; }
 	}
 	m->tuned_foi = best_foi;
-	m->tuned_ctas = best_ctas;
+	// several per SM won: later batches choose their count by the automatic rule
+	// (which keeps one per SM for batches too small to fill the SMs that way)
+	m->tuned_ctas = best_ctas == 1 ? 1 : 0;
 	if (chosen) *chosen = best_foi;
 	return BEEP_OK;
 }

@@ -211,11 +211,13 @@ BEEP_API beep_status beep_batch_destroy(beep_batch *batch);
 BEEP_API beep_status beep_batch_run_graph(beep_batch *batch);
 /* Autotuner of the fast form for a model: times every kernel layout the
  * model supports -- force of infection on FP32 SIMT (one or several particles
- * per SM) or on the tensor cores -- on a sample of the given batch (two waves
- * of particles, up to 120 steps) and records the fastest on the model; later
- * batches of the model use it while the options fast_foi and
- * fast_ctas_per_sm are automatic.  *chosen (may be NULL) receives the force
- * of infection path (1 = FP32 SIMT, 2 = tensor cores). */
+ * per SM) or on the tensor cores -- on a sample of the given batch (up to 8
+ * particles per SM, up to 60 steps) and records the fastest on the model;
+ * later batches of the model use it while the options fast_foi and
+ * fast_ctas_per_sm are automatic (when several particles per SM won, each
+ * batch still takes one per SM if it is too small to fill the SMs several
+ * deep).  *chosen (may be NULL) receives the force of infection path (1 =
+ * FP32 SIMT, 2 = tensor cores). */
 BEEP_API beep_status beep_autotune(beep_model *model, const beep_sim_batch *batch, int32_t *chosen);
 /* Force-of-infection path the fast form of this batch runs: 1 = FP32 SIMT,
  * 2 = tensor cores; 0 for the plain form. */

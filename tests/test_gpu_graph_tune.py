@@ -68,5 +68,8 @@ def test_autotuner_records_a_supported_path(built):
     assert chosen in (capi.FOI_SIMT, capi.FOI_TENSOR)
     db = capi.DeviceBatch(dm, bt)
     assert db.foi_path() == chosen            # later batches of the model use the choice
+    assert db.ctas_per_sm() >= 1 and (chosen == capi.FOI_SIMT or db.ctas_per_sm() == 1)
+    r = db.run()
+    assert np.isfinite(r.L).all()
     db.close()
     dm.close()
