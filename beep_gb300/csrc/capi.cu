@@ -701,39 +701,48 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 			}
 		}
 		// several particles per SM (320-thread CTAs): as many as the SM's shared memory
-		// holds, up to four (three above 8 ages), each particle's state on chip -- or, for
-		// models whose state lives in global memory anyway, only the infectious counts,
-		// force of infection and observation slots (automatic: only if the one-CTA layout
-		// keeps the state in global memory too); the matrix is read through L1 unless it
-		// fits beside every CTA's share.  Automatic: from three CTAs per SM (two run no
-		// faster than one CTA of 640 threads), and only for batches large enough to
-		// fill the SMs that way.
-		const int opt_ctas = option_fast_ctas() != 0 ? option_fast_ctas() : m->tuned_ctas;
-		if (allow_ctas && !q->bd.foi_tc && opt_ctas != 1 && fast_pick_threads(m->dev) == 640) {
-			const int kmax = std::min(opt_ctas >= 2 ? opt_ctas : 4, fast_ctas_max(m->G));
-			const int kmin = opt_ctas >= 2 ? 2 : 3;
+		// holds, up to four (three above 8 ages), each particle's state on chip -- or only
+		// the infectious counts, force of infection and observation slots, with the state
+		// in global memory, where the one-CTA layout keeps it there too or the layout is
+		// asked for (option) or preferred (autotuner); the matrix is read through L1 unless
+		// it fits beside every CTA's share.  Unless the option forces a count, the count
+		// comes from the expected time below, and one CTA of 640 threads per SM stays
+		// where that is faster.
+		const int forced = option_fast_ctas();
+		const int pref = forced != 0 ? 0 : m->tuned_ctas;
+		const bool asked = forced >= 2 || pref >= 2;
+		if (allow_ctas && !q->bd.foi_tc && forced != 1 && pref != 1 && fast_pick_threads(m->dev) == 640) {
+			const int kmax = std::min(forced >= 2 ? forced : 4, fast_ctas_max(m->G));
+			const int kmin = asked ? 2 : 3;
 			auto fit = [&](size_t bytes) { return (int)std::min<size_t>((size_t)kmax, kSmemPerSM / (bytes + 1024)); };
 			const int nefo = q->bd.nefoi_stage;
 			bool glob = false;
 			int k = fit(fast_smem_bytes(m->dev, nslots, false, nefo, false, tnrows, ps, false, kDualThreads));
-			if (k < kmin && (q->state_global || opt_ctas >= 2)) {
+			if (k < kmin && (q->state_global || asked)) {
 				glob = true;
 				k = fit(fast_smem_bytes(m->dev, nslots, false, nefo, true, tnrows, ps, false, kDualThreads));
 			}
-			if (opt_ctas == 0 && k >= kmin) {
-				// automatic: the layout with the shortest expected time, waves of k CTAs per SM
-				// each taking k / gain[k] of a one-CTA wave (gain measured on the ABC-SMC
-				// workload: 1, 1.0, 1.18, 1.26) -- small batches keep more SMs busy with one
-				const double gain[5] = {0.0, 1.0, 1.0, 1.18, 1.26};
-				auto cost = [&](int kk) {
-					const long long per_wave = (long long)kk * std::max(1, m->sms);
-					return (double)((P + per_wave - 1) / per_wave) * kk / gain[kk];
+			if (forced == 0 && k >= kmin) {
+				// expected time in units of one 640-thread wave: ceil(P / SMs) for one CTA per
+				// SM; (P / SMs) / gain(r) for 320-thread CTAs, r = min(k, P / SMs) of them
+				// resident per SM (the block scheduler spreads a small grid one per SM), gain =
+				// the SM throughput of r such CTAs against one 640-thread CTA, measured on the
+				// ABC-SMC workload: 0.5 (one alone has half the threads), 1.0, 1.18, 1.26
+				const double sms = (double)std::max(1, m->sms), per_sm = (double)P / sms;
+				auto gain = [](double r) {
+					static const double gt[5] = {0.0, 0.5, 1.0, 1.18, 1.26};
+					if (r >= 4.0) return gt[4];
+					const int i = (int)r;
+					return gt[i] + (r - i) * (gt[i + 1] - gt[i]);
 				};
-				int best = 1;
-				for (int kk = 3; kk <= k; kk++)
-					if (cost(kk) < cost(best)) best = kk;
-				if (best == 1) k = 0;
-				else k = best;
+				const double t_one = std::ceil(per_sm);
+				int best = 0;
+				double t_best = t_one;
+				for (int kk = kmin; kk <= k; kk++) {
+					const double t = per_sm / gain(std::min((double)kk, per_sm));
+					if (t < t_best * 0.999) { t_best = t; best = kk; }
+				}
+				k = best;
 			}
 			if (k >= kmin) {
 				q->bd.nt = kDualThreads;
@@ -958,9 +967,10 @@ beep_status beep_autotune(beep_model *m, const beep_sim_batch *b, int32_t *chose
 		if (ms < best) { best = ms; best_foi = c[0]; best_ctas = c[1]; }
 	}
 	m->tuned_foi = best_foi;
-	// several per SM won: later batches choose their count by the automatic rule
-	// (which keeps one per SM for batches too small to fill the SMs that way)
-	m->tuned_ctas = best_ctas == 1 ? 1 : 0;
+	// several per SM won: later batches take that layout where their size makes it
+	// faster by the expected-time rule (one per SM for batches too small to fill the
+	// SMs several deep)
+	m->tuned_ctas = best_ctas;
 	if (chosen) *chosen = best_foi;
 	return BEEP_OK;
 }
