@@ -180,6 +180,10 @@ def main():
     # R factors (src/state.cc:392-401, 223-290; src/model.cc:1318-1362)
     strains = synth.seir_hd_strains()
     make_fixture("strain_sim", strains, npart=8, ntraj=2, seed=0x5712A1)
+    # a two-strain model large enough for the several-particles-per-SM layout (280 columns;
+    # model and tables only)
+    make_fixture("strain70_model", synth.seir_hd_strains(narea=70, nage=2, days=20, name="strains70"), npart=2, ntraj=0,
+                 seed=0x5712A2)
     # every observation model: normal X%, Poisson with censoring, fixed-SD normal, loaded
     # SDs with a threshold; missing entries (src/obsmodel.cc:245-305, src/data.cc:1589-1623)
     make_fixture("obsmodel_sim", synth.seir_hd_obs_models(), npart=8, ntraj=2, seed=0x0B5E)

@@ -228,3 +228,27 @@ def test_several_particles_per_sm_with_state_in_global_memory(ctas_option):
     finally:
         ctas_option("fast_foi", capi.FOI_AUTO)
     dm.close()
+
+
+def test_several_particles_per_sm_with_two_strains(ctas_option):
+    """Two strains (70 areas x 2 ages x 2 strains, 280 columns; model and tables
+    from the reference) in the four-per-SM layout: the same draws as one
+    640-thread CTA per SM, and the particles follow the FP64 form."""
+    b, m, tabs, seed = load("strain70_model")
+    assert m.nstrain == 2 and m.narea * m.ndemocatpos > 256
+    dm = capi.DeviceModel(m)
+    P = 48
+    g = dm.simulate(capi.Batch(m, tabs, P, seed, want_transnum=True))
+    res = {}
+    for k in (1, 4):
+        ctas_option("fast_ctas_per_sm", k)
+        db = capi.DeviceBatch(dm, capi.Batch(m, tabs, P, seed, want_transnum=True, form=capi.FORM_FAST))
+        assert db.ctas_per_sm() == k
+        res[k] = db.run()
+        db.close()
+    assert np.array_equal(res[1].transnum, res[4].transnum)
+    np.testing.assert_allclose(res[4].L, res[1].L, rtol=1e-6)
+    same = np.array([np.array_equal(res[4].transnum[p], g.transnum[p]) for p in range(P)])
+    assert same.mean() >= 0.5, same.mean()
+    np.testing.assert_allclose(res[4].L[same], g.L[same], rtol=L_RTOL_FAST)
+    dm.close()
