@@ -252,3 +252,22 @@ def test_several_particles_per_sm_with_two_strains(ctas_option):
     assert same.mean() >= 0.5, same.mean()
     np.testing.assert_allclose(res[4].L[same], g.L[same], rtol=L_RTOL_FAST)
     dm.close()
+
+
+def test_tensor_core_foi_with_two_strains(foi_option):
+    """The tensor-core FOI with two strains (each strain's counts in its own
+    32 rows of the M = 64 operand) keeps the fast form on the FP64
+    trajectories of the 70-area two-strain reference model."""
+    b, m, tabs, seed = load("strain70_model")
+    dm = capi.DeviceModel(m)
+    P = 48
+    g = dm.simulate(capi.Batch(m, tabs, P, seed, want_transnum=True))
+    foi_option("fast_foi", capi.FOI_TENSOR)
+    db = capi.DeviceBatch(dm, capi.Batch(m, tabs, P, seed, want_transnum=True, form=capi.FORM_FAST))
+    assert db.foi_path() == capi.FOI_TENSOR
+    f = db.run()
+    db.close()
+    same = np.array([np.array_equal(f.transnum[p], g.transnum[p]) for p in range(P)])
+    assert same.mean() >= 0.5, same.mean()
+    np.testing.assert_allclose(f.L[same], g.L[same], rtol=L_RTOL_FAST)
+    dm.close()
