@@ -247,6 +247,28 @@ def profile_traffic(kind: str, P: int):
     return float(m.group(1)) * P if m else None
 
 
+def fp64_loglik_of_trajectory(m, transnum):
+    """The observation log-likelihood of one transition-count trajectory
+    [S][A][T][DP] in FP64 (ObservationModel::calculate with normal
+    observations, src/obsmodel.cc:22-58,245-305): every observation's count is an
+    exact integer sum over its steps and cells, then its normal log-density."""
+    a = m.arr
+    S = transnum.shape[0]
+    tn = transnum.reshape(S, -1).astype(np.int64)
+    cum = np.vstack([np.zeros((1, tn.shape[1]), np.int64), np.cumsum(tn, 0)])
+    ptr, cells = a["obs_cell_ptr"], a["obs_cells"]
+    si, sf = a["obs_sett_i"], a["obs_sett_f"]
+    if (cells < 0).any() or (a["obs_model"] != 0).any() or (a["obs_value_kind"] != 0).any():
+        return None                                   # population or non-normal observations: not handled here
+    obs_of_cell = np.repeat(np.arange(m.nobs), np.diff(ptr))
+    per_cell = cum[sf[obs_of_cell], cells] - cum[si[obs_of_cell], cells]
+    v = np.zeros(m.nobs)
+    np.add.at(v, obs_of_cell, per_cell.astype(np.float64))
+    v = np.maximum(v * a["obs_factor"], 0.0)
+    var = a["obs_sd"] ** 2
+    return float(np.sum(-0.5 * np.log(2 * np.pi * var) - (a["obs_value"] - v) ** 2 / (2 * var)))
+
+
 def run_particle_filter(reps: int, seed: int, N: int = 256, section_steps: int = 28):
     """PMCMC likelihood estimates: the bootstrap particle filter of the
     10-area x 3-age workload (dt 0.25, 100 days, 400 steps), N particles, one
@@ -510,6 +532,28 @@ def run_ours(args, rank, ws, dist):
                  "ms_per_step": pms, "particles": Pp, "steps": tfp,
                  "loglik_evals_per_s": Pp / (pms / 1e3) * tfp / m.ndivision}
         pb.close()
+    # the fast form's log-likelihood against the FP64 form on the same particles and streams:
+    # where the trajectories are identical, the error of the FP32 evaluation itself
+    acc = None
+    if form == capi.FORM_FAST and args.plain_particles > 0 and rank == 0:
+        traj_bytes = 4 * m.ndivision * m.narea * m.ntrans * m.ndemocatpos
+        na = int(max(8, min(32, 2e9 // traj_bytes, P)))
+        res = {}
+        for f in (capi.FORM_FAST, capi.FORM_PLAIN_FP64):
+            res[f] = dm.simulate(capi.Batch(m, tabs[:na] if len(tabs) > 1 else tabs, na, seed, group_of=group_of[:na],
+                                            want_transnum=True, form=f))
+        fa, pl = res[capi.FORM_FAST], res[capi.FORM_PLAIN_FP64]
+        same = np.array([np.array_equal(fa.transnum[k], pl.transnum[k]) for k in range(na)])
+        rel = np.abs(fa.L - pl.L) / np.abs(pl.L)
+        # every fast trajectory scored in FP64 on the host: the error of the FP32 evaluation
+        l64 = [fp64_loglik_of_trajectory(m, fa.transnum[k]) for k in range(na)]
+        own = [abs(fa.L[k] - l64[k]) / abs(l64[k]) for k in range(na) if l64[k] is not None]
+        acc = {"particles": na, "identical_trajectories": float(same.mean()),
+               "max_rel_err_identical": float(rel[same].max()) if same.any() else None,
+               "max_rel_err_vs_fp64_of_own_trajectory": float(max(own)) if own else None,
+               "tolerance": 1e-6,
+               "note": "particles whose FP32 draws crossed a near tie follow another trajectory; each fast "
+                       "trajectory is also scored in FP64 on the host"}
     if rank != 0:
         return
     hbm, hbm_kind = peaks()
@@ -538,6 +582,7 @@ def run_ours(args, rank, ws, dist):
         "form": args.form,
         "foi": {0: None, 1: "fp32-simt", 2: "tensor-core split-bf16"}[db.foi_path()],
         "plain_fp64": plain,
+        "loglik_vs_fp64": acc,
         "loglik_evals_per_s": P * ws / t_dev,
         "clocks": clocks,
         "e2e": {"value": units_total(units, ws) / t_e2e, "unit": "particle.area.group.steps/s", "h2d_bytes_per_step": h2d,
