@@ -49,7 +49,8 @@ def model_arrays(w: synth.Workload, obs_values: Optional[dict] = None) -> Dict[s
     ``obs_values``: data file -> column -> (values, sds) as written to the
     workload's data tables; placeholders (0, sd 1) when None."""
     A, G = w.narea, w.nage
-    DP, C, T = G, len(COMPS), len(TRANS)
+    NS = nstrain(w)
+    DP, C, T = G * NS, len(COMPS), len(TRANS)
     S = w.ndivision
     pop = np.asarray(w.pop, np.int64)
     total_pop = pop.sum(1)                       # Area::total_pop (unsigned)
@@ -74,12 +75,20 @@ def model_arrays(w: synth.Workload, obs_values: Optional[dict] = None) -> Dict[s
         rowptr.append(len(to))
     factor = np.array([(1.0 / float(total_pop[c])) / diag[c] for c in range(A)])
 
+    # dp = strain * G + age (the strain democat last, src/data.cc); susceptibles start
+    # in the first strain, the exposed seeds in their own strains
     pop_init = np.zeros((A, C, DP))
-    pop_init[:, 0, :] = pop - w.seed_E
-    pop_init[:, 1, :] = w.seed_E
+    if NS == 1:
+        pop_init[:, 0, :] = pop - w.seed_E
+        pop_init[:, 1, :] = w.seed_E
+    else:
+        seeds = np.asarray(w.strains["seed_E"])
+        pop_init[:, 0, :G] = pop - seeds.sum(0)
+        for st in range(NS):
+            pop_init[:, 1, st * G:(st + 1) * G] = seeds[st]
 
     arr: Dict[str, np.ndarray] = {
-        "dims": np.array([A, G, DP, 1, C, T, S, w.days, w.steps_per_day], np.int32),
+        "dims": np.array([A, G, DP, NS, C, T, S, w.days, w.steps_per_day], np.int32),
         "dt": np.array([float(w.days) / S]),
         "popsize": np.array([popsize]),
         "trans_from": np.array([f for f, _ in TRANS], np.int32),
@@ -93,11 +102,15 @@ def model_arrays(w: synth.Workload, obs_values: Optional[dict] = None) -> Dict[s
     return arr
 
 
+def nstrain(w: synth.Workload) -> int:
+    return 1 if w.strains is None else len(w.strains["names"])
+
+
 def _observations(w: synth.Workload, obs_values: Optional[dict]) -> Dict[str, np.ndarray]:
     """Observation list in the reference's order: data table -> column -> row
     (Data::load_timeseries_datatable, src/data.cc:1119-1320)."""
     G, T, C = w.nage, len(TRANS), len(COMPS)
-    DP = G
+    DP = G * nstrain(w)
     spd = w.steps_per_day
     si, sf, vals, sds, cptr, cells = [], [], [], [], [0], []
     tr_of = {"E->I": 1, "H->D": 4}
@@ -106,8 +119,9 @@ def _observations(w: synth.Workload, obs_values: Optional[dict]) -> Dict[str, np
         nrow = len(tab["times"])
         for ci, col in enumerate(tab["columns"]):
             c = ci
-            if "democats_filt" in tt:
-                dps = [int(tt["democats_filt"].split("age")[-1])]
+            if "democats_filt" in tt:                 # one age group, every strain
+                age = int(tt["democats_filt"].split("age")[-1])
+                dps = [dp for dp in range(DP) if dp % G == age]
             else:
                 dps = list(range(DP))
             ov = obs_values.get(tab["file"], {}).get(col) if obs_values else None
@@ -139,6 +153,13 @@ def _observations(w: synth.Workload, obs_values: Optional[dict]) -> Dict[str, np
         "obs_factor_spline": np.full(n, -1, np.int32), "obs_cell_ptr": np.array(cptr, np.int32),
         "obs_cells": np.array(cells, np.int32),
     }
+
+
+def _star_values(spec: str) -> np.ndarray:
+    """A '|'-separated value list where '*' stands for what completes the others to 1."""
+    parts = [p.strip() for p in spec.split("|")]
+    vals = [float(p) for p in parts if p != "*"]
+    return np.array([1.0 - sum(vals) if p == "*" else float(p) for p in parts])
 
 
 def _disc_spline(days: int, S: int, bp: Sequence[float], vals: Sequence[float]) -> np.ndarray:
@@ -189,7 +210,8 @@ def param_tables(w: synth.Workload, sigma_inv: Optional[float] = None, gamma_inv
 
     ``R_scale`` multiplies every knot of R(t) (an R0 proposal)."""
     A, G = w.narea, w.nage
-    DP, C, T, S = G, len(COMPS), len(TRANS), w.ndivision
+    NS = nstrain(w)
+    DP, C, T, S = G * NS, len(COMPS), len(TRANS), w.ndivision
     si = w.sigma_inv if sigma_inv is None else sigma_inv
     gi = w.gamma_inv if gamma_inv is None else gamma_inv
     hm = w.h_mean if h_mean is None else h_mean
@@ -199,7 +221,13 @@ def param_tables(w: synth.Workload, sigma_inv: Optional[float] = None, gamma_inv
     transrate[3, :] = (1.0 / gi) * (1 - w.p_H)
     transrate[4, :] = (1.0 / hm) * w.p_D
     transrate[5, :] = (1.0 / hm) * (1 - w.p_D)
-    sus = np.ones(DP)
+    # Model::create_susceptibility: the product over democats (ages have none, strains
+    # their values, '*' completing them to 1); R factors per strain
+    strain_sus, rfactor = np.ones(NS), np.ones(NS)
+    if NS > 1:
+        strain_sus = _star_values(w.strains["sus_value"])
+        rfactor = _star_values(w.strains["Rfactor_value"])
+    sus = np.repeat(strain_sus, G)
     inf = np.zeros(C)
     inf[2] = 1.0
     N0 = age_matrix(w)
@@ -212,28 +240,31 @@ def param_tables(w: synth.Workload, sigma_inv: Optional[float] = None, gamma_inv
                 Ntime[s, :, a] *= f[s]
     Rv = [v * R_scale for v in w.R_val]
     Rspl = _disc_spline(w.days, S, w.R_bp, Rv)
-    # NGM over infectious states E, I (Model::calculate_Vinv / calculate_F / calculate_NGM)
-    Q = DP
-    V = np.zeros((2 * Q, 2 * Q))
-    for dp in range(Q):
-        V[dp, dp] += transrate[1, dp]
-        V[Q + dp, dp] -= transrate[1, dp]
-        V[Q + dp, Q + dp] += transrate[2, dp]
-        V[Q + dp, Q + dp] += transrate[3, dp]
-    Vinv = np.linalg.inv(V)
     pop = np.asarray(w.pop, np.float64)
     dist = pop.sum(0) / pop.sum()
-    beta = np.zeros(S)
-    ratio = None
-    for s in range(S):
-        if s == 0 or not np.array_equal(Ntime[s - 1], Ntime[s]):
-            F = np.zeros((Q, 2 * Q))
-            for dp in range(Q):
-                for q in range(Q):
-                    F[q, Q + dp] += dist[q] * sus[q] * 1.0 * Ntime[s][q, dp]
-            NGM = F @ Vinv[:, :Q]
-            ratio = float(np.max(np.linalg.eigvals(NGM).real))
-        beta[s] = 1.0 * Rspl[s] / ratio
+    # per strain st: NGM over the infectious states E, I of that strain's age groups
+    # (Model::calculate_beta_from_R, calculate_Vinv, calculate_F, src/model.cc:1318-1362)
+    Q = G
+    beta = np.zeros((NS, S))
+    for st in range(NS):
+        V = np.zeros((2 * Q, 2 * Q))
+        for q in range(Q):
+            dp = st * Q + q
+            V[q, q] += transrate[1, dp]
+            V[Q + q, q] -= transrate[1, dp]
+            V[Q + q, Q + q] += transrate[2, dp]
+            V[Q + q, Q + q] += transrate[3, dp]
+        Vinv = np.linalg.inv(V)
+        ratio = None
+        for s in range(S):
+            if s == 0 or not np.array_equal(Ntime[s - 1], Ntime[s]):
+                F = np.zeros((Q, 2 * Q))
+                for a in range(Q):
+                    for q in range(Q):
+                        F[q, Q + a] += dist[q] * sus[st * Q + q] * 1.0 * Ntime[s][q, a]
+                NGM = F @ Vinv[:, :Q]
+                ratio = float(np.max(np.linalg.eigvals(NGM).real))
+            beta[st, s] = rfactor[st] * Rspl[s] / ratio
     # area factors: covariates (linear) normalised by the population-weighted mean
     af = np.ones((w.days, A))
     if w.covar is not None:
@@ -249,10 +280,10 @@ def param_tables(w: synth.Workload, sigma_inv: Optional[float] = None, gamma_inv
         af = af / area_av
     return {
         "transrate": transrate, "susceptibility": sus, "infectivity": inf,
-        "beta_rows": beta[None, :], "beta_row_of": np.zeros((1, A), np.int32),
+        "beta_rows": beta, "beta_row_of": np.repeat(np.arange(NS, dtype=np.int32)[:, None], A, 1),
         "areafactor": af, "Ntime": Ntime, "geo_spline": np.ones(S),
         "efoi_spline": np.full((1, S), float(w.efoi)), "efoi_agedist": np.ones((1, G)),
-        "efoi_ref": np.zeros((1, A), np.int32), "obs_spline": np.zeros((0, S)),
+        "efoi_ref": np.zeros((NS, A), np.int32), "obs_spline": np.zeros((0, S)),
     }
 
 

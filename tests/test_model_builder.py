@@ -16,8 +16,11 @@ WORKLOADS = {
     "c0_sim": lambda: synth.seir_hd_small(seed=20260000, narea=10, nage=3, days=100, name="c0"),
     # area covariates, stepped age-mixing factors, external force of infection, 7-knot R(t)
     "features_sim": synth.seir_hd_features,
+    # two strains: susceptibility and R factor per strain, one NGM per strain
+    "strain_sim": synth.seir_hd_strains,
+    "strain70_model": lambda: synth.seir_hd_strains(narea=70, nage=2, days=20, name="strains70"),
 }
-MODEL_KEYS = ("trans_from", "trans_to", "democatpos_age", "M_diag", "M_rowptr", "M_to", "M_val", "M_factor",
+MODEL_KEYS = ("dims", "trans_from", "trans_to", "democatpos_age", "M_diag", "M_rowptr", "M_to", "M_val", "M_factor",
               "pop_init", "obs_sett_i", "obs_sett_f", "obs_cell_ptr", "obs_cells", "obs_factor")
 TABLE_KEYS = ("transrate", "susceptibility", "infectivity", "beta_rows", "beta_row_of", "areafactor", "Ntime",
               "geo_spline", "efoi_spline", "efoi_agedist", "efoi_ref")
