@@ -581,6 +581,7 @@ def run_ours(args, rank, ws, dist):
         "data": "synthetic", "config": workload_config(args.workload, m, P),
         "form": args.form,
         "foi": {0: None, 1: "fp32-simt", 2: "tensor-core split-bf16"}[db.foi_path()],
+        "particles_per_sm": db.ctas_per_sm(),
         "plain_fp64": plain,
         "loglik_vs_fp64": acc,
         "loglik_evals_per_s": P * ws / t_dev,
