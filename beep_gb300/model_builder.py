@@ -32,7 +32,10 @@ from . import synth
 COMPS = ["S", "E", "I", "H", "R", "D"]
 # (from, to) in declaration order; S->E is the infection transition
 TRANS = [(0, 1), (1, 2), (2, 3), (2, 4), (3, 5), (3, 4)]
-OBS_NORMAL = 0
+OBS_NORMAL, OBS_NORMAL_PERCENT, OBS_POISSON = 0, 1, 2   # beep_obs_model
+OBSVAL_VALUE, OBSVAL_UNKNOWN, OBSVAL_THRESH = 0, 1, 2   # beep_obs_value_kind
+THRESH, UNKNOWN = 999999998.0, 999999997.0             # the reference's markers of censored / missing values
+EPSILON_FACTOR = 0.01                                   # the reference's default epsilon_factor
 UNSET = 999999999.0
 
 
@@ -106,17 +109,35 @@ def nstrain(w: synth.Workload) -> int:
     return 1 if w.strains is None else len(w.strains["names"])
 
 
+def _obsmodel(spec: str):
+    """(model, fixed sd, percent) of a data table's `obsmodel` string (src/inputs.cc:413-473)."""
+    parts = spec.split()
+    if parts[0].lower() == "poisson":
+        return OBS_POISSON, None, None
+    if len(parts) == 1 or parts[1].lower() == "load":
+        return OBS_NORMAL, None, None
+    if parts[1].endswith("%"):
+        return OBS_NORMAL_PERCENT, None, float(parts[1][:-1])
+    return OBS_NORMAL, float(parts[1]), None
+
+
 def _observations(w: synth.Workload, obs_values: Optional[dict]) -> Dict[str, np.ndarray]:
     """Observation list in the reference's order: data table -> column -> row
-    (Data::load_timeseries_datatable, src/data.cc:1119-1320)."""
+    (Data::load_timeseries_datatable, src/data.cc:1119-1320), with the values
+    the data files carry: missing ('.') and censored ('*', below the table's
+    threshold) entries as the reference marks them, and the standard deviation
+    of each observation model (Data::set_obs_sd, src/data.cc:1589-1623: a
+    percentage of the value blended with the column's largest value)."""
     G, T, C = w.nage, len(TRANS), len(COMPS)
     DP = G * nstrain(w)
     spd = w.steps_per_day
-    si, sf, vals, sds, cptr, cells = [], [], [], [], [0], []
+    si, sf, vals, sds, kinds, models, thr, cptr, cells = [], [], [], [], [], [], [], [0], []
     tr_of = {"E->I": 1, "H->D": 4}
     for tab in synth.data_tables(w):
         tt = tab["toml"]
         nrow = len(tab["times"])
+        model, fixed_sd, percent = _obsmodel(tt["obsmodel"])
+        threshold = float(tt["threshold"]) if "threshold" in tt else UNSET
         for ci, col in enumerate(tab["columns"]):
             c = ci
             if "democats_filt" in tt:                 # one age group, every strain
@@ -125,6 +146,7 @@ def _observations(w: synth.Workload, obs_values: Optional[dict]) -> Dict[str, np
             else:
                 dps = list(range(DP))
             ov = obs_values.get(tab["file"], {}).get(col) if obs_values else None
+            col_vals, col_kinds, col_sds = [], [], []
             for r, t in enumerate(tab["times"]):
                 if tt["type"] == "transition":
                     step = int(tt["timestep"])
@@ -138,18 +160,38 @@ def _observations(w: synth.Workload, obs_values: Optional[dict]) -> Dict[str, np
                     co = COMPS.index(tt["observation"])
                     cells += [-1 - ((c * C + co) * DP + dp) for dp in dps]
                 cptr.append(len(cells))
-                if ov is None:
-                    vals.append(0.0)
-                    sds.append(1.0)
-                else:
-                    vals.append(float(ov[0][r]))
-                    sds.append(float(ov[1][r]))
+                kind, v, sd = OBSVAL_VALUE, 1.0 if not tab.get("sd_col", True) else 0.0, 1.0
+                if ov is not None:
+                    nd = tab.get("nodata_every")
+                    v, sd = float(ov[0][r]), (float(ov[1][r]) if ov[1] is not None else 1.0)
+                    if nd and (r + ci) % nd == 0:
+                        kind, v = OBSVAL_UNKNOWN, UNKNOWN
+                    elif tab.get("censor_below") is not None and v < tab["censor_below"]:
+                        kind, v = OBSVAL_THRESH, THRESH
+                    v = v if kind != OBSVAL_VALUE else float(int(v))
+                col_vals.append(v)
+                col_kinds.append(kind)
+                col_sds.append(sd)
+            # standard deviations by observation model
+            vmax = max([v for v, k in zip(col_vals, col_kinds) if k == OBSVAL_VALUE], default=0.0)
+            for v, k, sd in zip(col_vals, col_kinds, col_sds):
+                if model == OBS_POISSON:
+                    sd = UNSET
+                elif percent is not None:
+                    sd = (v * (1 - EPSILON_FACTOR) + vmax * EPSILON_FACTOR) * 0.01 * percent
+                elif fixed_sd is not None:
+                    sd = fixed_sd
+                vals.append(v)
+                kinds.append(k)
+                sds.append(sd)
+                models.append(model)
+                thr.append(threshold)
     n = len(si)
     return {
         "obs_sett_i": np.array(si, np.int32), "obs_sett_f": np.array(sf, np.int32),
-        "obs_value_kind": np.zeros(n, np.int32), "obs_value": np.array(vals, np.float64),
-        "obs_model": np.full(n, OBS_NORMAL, np.int32), "obs_sd": np.array(sds, np.float64),
-        "obs_shape": np.zeros(n), "obs_threshold": np.full(n, UNSET), "obs_factor": np.ones(n),
+        "obs_value_kind": np.array(kinds, np.int32), "obs_value": np.array(vals, np.float64),
+        "obs_model": np.array(models, np.int32), "obs_sd": np.array(sds, np.float64),
+        "obs_shape": np.zeros(n), "obs_threshold": np.array(thr, np.float64), "obs_factor": np.ones(n),
         "obs_factor_spline": np.full(n, -1, np.int32), "obs_cell_ptr": np.array(cptr, np.int32),
         "obs_cells": np.array(cells, np.int32),
     }

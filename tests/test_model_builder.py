@@ -42,3 +42,27 @@ def test_model_and_tables_match_reference(name):
     t = mb.param_tables(w)
     for k in TABLE_KEYS:
         _close(t[k], b["g0." + k])
+
+
+def test_observations_match_reference_for_every_observation_model():
+    """The observation list of the workload observed through every model the
+    reference parses (normal X%, Poisson with censoring below a threshold,
+    fixed-SD normal, loaded SDs with a threshold, missing entries): values,
+    kinds, models, standard deviations (Data::set_obs_sd, src/data.cc:1589-1623)
+    and thresholds equal the reference's."""
+    b, _, _, _ = load("obsmodel_sim")
+    w = synth.seir_hd_obs_models()
+    # the observed values as the data files carried them: censored entries are below
+    # the threshold, missing ones any value
+    val, kind, sd = (np.asarray(b[k]) for k in ("obs_value", "obs_value_kind", "obs_sd"))
+    ov, k = {}, 0
+    for tab in synth.data_tables(w):
+        n = len(tab["times"])
+        ov[tab["file"]] = {}
+        for col in tab["columns"]:
+            ov[tab["file"]][col] = (np.where(kind[k:k + n] == 0, val[k:k + n], 0.0),
+                                    sd[k:k + n] if tab.get("sd_col", True) else None)
+            k += n
+    arr = mb.model_arrays(w, ov)
+    for key in MODEL_KEYS + ("obs_value_kind", "obs_value", "obs_model", "obs_sd", "obs_threshold"):
+        _close(arr[key], b[key])
