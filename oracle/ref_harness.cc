@@ -19,8 +19,14 @@
 // chains, each simulated at one parameter row and proposed at the next, with
 // binomial_sample (src/utils.cc:174-180) interposed like poisson_sample.
 //
+// With abcw=N abck=K it evaluates the reference's ABC-SMC importance weights
+// (ABCSMC::calculate_particle_weight, normalise_particle_weights and the
+// weighted MVN, src/abcsmc.cc:260-283, src/mvn.cc:39-196): parameter rows
+// 0..K-1 form the previous generation (weights 0.5 + 0.1 (j mod 7)), rows
+// K..K+N-1 are the new samples; BEEP's own inputs need nsample and ngeneration.
+//
 // usage: ref_harness out=FILE [npart=N] [ntraj=N] [seed=S] [pf=0|1] [theta=FILE] [mbp=N] [sampledir=DIR]
-//                    -- <BEEP key=value...>
+//                    [abcw=N abck=K] -- <BEEP key=value...>
 
 #include <cmath>
 #include <cstdint>
@@ -42,6 +48,7 @@
 #define private public
 #include "pmcmc.hh"
 #include "mbp.hh"
+#include "abcsmc.hh"
 #undef private
 #include "mpi.hh"
 #include "data.hh"
@@ -630,6 +637,47 @@ int main(int argc, char **argv)
 			B.i(vp + "transnum_init", tni, {(uint64_t)nt, S, A, T, DP});
 			B.i(vp + "transnum_prop", tnp, {(uint64_t)nt, S, A, T, DP});
 		}
+	}
+	if (opt.count("abcw")) {
+		const int NN = atoi(opt["abcw"].c_str()), K = atoi(opt["abck"].c_str());
+		if (K < 2 || NN < 1 || (int)thetas.size() < K + NN) {
+			fprintf(stderr, "abcw=%d abck=%d needs %d parameter rows\n", NN, K, K + NN);
+			return 2;
+		}
+		Output output(details, data, model, inputs, obsmodel, mpi);
+		ABCSMC abc(details, data, model, inputs, output, obsmodel, mpi);
+		Generation gl;
+		for (int j = 0; j < K; j++) {
+			ParamSample ps;
+			ps.run = 0; ps.EF = 0; ps.paramval = thetas[j];
+			gl.param_samp.push_back(ps);
+			gl.w.push_back(0.5 + 0.1 * (j % 7));
+		}
+		MVN mvn("ABCSMC", model.param_not_fixed, abc.propsize, ALL_PARAM, MULTIPLE);
+		mvn.setup(gl.param_samp, gl.w);
+		Generation gn;
+		std::vector<double> lp, tn, tl;
+		for (int i = 0; i < NN; i++) {
+			const auto &th = thetas[K + i];
+			gn.w.push_back(abc.calculate_particle_weight(th, gl, mvn));
+			ParamSample ps;
+			ps.run = 0; ps.EF = 0; ps.paramval = th;
+			gn.param_samp.push_back(ps);                     // normalise_particle_weights counts these
+			lp.push_back(model.prior(th));
+			for (auto v : mvn.var) tn.push_back(th[v]);
+		}
+		for (int j = 0; j < K; j++)
+			for (auto v : mvn.var) tl.push_back(thetas[j][v]);
+		const std::vector<double> w_raw = gn.w;
+		abc.normalise_particle_weights(gn);
+		std::vector<double> inv;
+		for (auto &row : mvn.inv_M) inv.insert(inv.end(), row.begin(), row.end());
+		const uint64_t nv = mvn.var.size();
+		B.scalar_d("abc.size", mvn.size);
+		B.d("abc.theta_new", tn, {(uint64_t)NN, nv}); B.d("abc.logprior_new", lp);
+		B.d("abc.theta_last", tl, {(uint64_t)K, nv}); B.d("abc.w_last", gl.w);
+		B.d("abc.inv_cov", inv, {nv, nv});
+		B.d("abc.w", w_raw); B.d("abc.w_norm", gn.w);
 	}
 	B.close();
 	fprintf(stderr, "ref_harness: %d groups x %d particles, %llu keyed draws\n", ngroup, npart, g_replay.ncalls);

@@ -33,8 +33,11 @@ from beep_gb300 import bundle, synth  # noqa: E402
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
 
 
-def run_harness(workdir, toml, out, npart, ntraj, seed, mode, pf=False, theta=None, pfn=0, mbp=0, sampledir=None):
+def run_harness(workdir, toml, out, npart, ntraj, seed, mode, pf=False, theta=None, pfn=0, mbp=0, sampledir=None,
+                abcw=None):
     cmd = [HARNESS, f"out={out}", f"npart={npart}", f"ntraj={ntraj}", f"seed={seed}", f"pf={1 if pf else 0}"]
+    if abcw:
+        cmd += [f"abcw={abcw[0]}", f"abck={abcw[1]}"]
     if sampledir:
         cmd.append(f"sampledir={sampledir}")
     if theta is not None:
@@ -46,6 +49,8 @@ def run_harness(workdir, toml, out, npart, ntraj, seed, mode, pf=False, theta=No
     cmd += ["--", f"inputfile={os.path.basename(toml)}", f"mode={mode}"]
     if pfn:
         cmd += [f"nparticle={pfn}", "nsample=400", "nburnin=200", "invT=1"]
+    if abcw:
+        cmd += ["nsample=100", "ngeneration=2"]
     r = subprocess.run(cmd, cwd=workdir, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"harness failed:\n{r.stdout}\n{r.stderr}")
@@ -116,7 +121,7 @@ def mbp_theta_rows(base, nchain, seed):
 
 
 def make_fixture(name, w: synth.Workload, npart, ntraj, seed, pf=False, theta_rows=None, keep_dir=None, pfn=0,
-                 mbp=0, samples=False):
+                 mbp=0, samples=False, abcw=None):
     work = tempfile.mkdtemp(prefix=f"golden_{name}_")
     try:
         toml = synth.write_beep_inputs(w, work)
@@ -130,17 +135,25 @@ def make_fixture(name, w: synth.Workload, npart, ntraj, seed, pf=False, theta_ro
             with open(theta, "w") as f:
                 for row in theta_rows:
                     f.write(",".join(repr(float(x)) for x in row) + "\n")
-        if mbp and theta_rows is None:
+        if (mbp or abcw) and theta_rows is None:
+            # MBP: a start and a proposal row per chain; ABC-SMC weights: the previous
+            # generation's rows, then the new samples' (all inside the prior bounds)
             theta = os.path.join(work, "theta.csv")
             base = b0["g0.theta"]
+            nrow_pairs = mbp if mbp else (abcw[0] + abcw[1] + 1) // 2
             with open(theta, "w") as f:
-                for row in mbp_theta_rows(base, mbp, w.seed):
+                for row in mbp_theta_rows(base, nrow_pairs, w.seed):
                     f.write(",".join(repr(float(x)) for x in row) + "\n")
         out = os.path.join(HERE, f"{name}.bnd")
         sdir = os.path.join(work, "samples") if samples else None
         if sdir:
             os.makedirs(sdir)
-        run_harness(work, toml, out, npart, ntraj, seed, mode, pf=pf, theta=theta, pfn=pfn, mbp=mbp, sampledir=sdir)
+        run_harness(work, toml, out, npart, ntraj, seed, mode, pf=pf, theta=theta, pfn=pfn, mbp=mbp, sampledir=sdir,
+                    abcw=abcw)
+        if abcw:
+            # only the weights' inputs and outputs are kept (the bundle holds every row's tables)
+            full = bundle.read_bundle(out)
+            bundle.write_bundle(out, {k: v for k, v in full.items() if k.startswith("abc.")})
         if sdir:
             # the reference's own sample files of the sampled lineage
             for f in sorted(os.listdir(sdir)):
@@ -202,6 +215,8 @@ def main():
     tmbp = synth.seir_hd_small(seed=20260103, narea=4, nage=2, days=40, name="tinymbp")
     make_fixture("tiny_mbp", tmbp, npart=1, ntraj=1, seed=0x5EED0F00D, mbp=4)
     make_fixture("c0_mbp", c0, npart=1, ntraj=0, seed=20260003, mbp=4)
+    # ABC-SMC importance weights: 40 previous-generation samples, 24 new ones
+    make_fixture("c0_abcw", c0, npart=1, ntraj=0, seed=20260004, abcw=(24, 40))
 
 
 if __name__ == "__main__":

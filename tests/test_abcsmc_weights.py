@@ -42,3 +42,29 @@ def test_gpu_weights_match_oracle(nnew, nlast):
     o = oracle_abcsmc_weights(tn, lp, tl, wl, ic, 1.3)
     assert np.all(np.isfinite(o)) and np.all(o > 0)
     np.testing.assert_allclose(g, o, rtol=1e-5)
+
+
+def _reference_case():
+    from beep_gb300 import bundle
+    import os
+    b = bundle.read_bundle(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "c0_abcw.bnd"))
+    return ([np.asarray(b["abc." + k]) for k in ("theta_new", "logprior_new", "theta_last", "w_last", "inv_cov")],
+            float(np.asarray(b["abc.size"]).ravel()[0]), np.asarray(b["abc.w"]), np.asarray(b["abc.w_norm"]))
+
+
+def test_oracle_weights_match_reference():
+    """The oracle against the reference's own ABCSMC::calculate_particle_weight
+    and normalise_particle_weights (weighted MVN of 40 samples of the 10-area
+    model's 12 free parameters, 24 new samples; tests/golden/c0_abcw.bnd)."""
+    args, size, w_ref, wn_ref = _reference_case()
+    np.testing.assert_allclose(oracle_abcsmc_weights(*args, size, normalise=False), w_ref, rtol=1e-12)
+    np.testing.assert_allclose(oracle_abcsmc_weights(*args, size, normalise=True), wn_ref, rtol=1e-12)
+
+
+@pytest.mark.gpu
+def test_gpu_weights_match_reference():
+    from beep_gb300 import build
+    build.build()
+    args, size, w_ref, wn_ref = _reference_case()
+    np.testing.assert_allclose(capi.abcsmc_weights(*args, size, normalise=False), w_ref, rtol=1e-5)
+    np.testing.assert_allclose(capi.abcsmc_weights(*args, size, normalise=True), wn_ref, rtol=1e-5)
