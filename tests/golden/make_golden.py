@@ -120,8 +120,13 @@ def mbp_theta_rows(base, nchain, seed):
     return rows
 
 
+ONLY = None   # fixture names to (re)generate (--only); None: all
+
+
 def make_fixture(name, w: synth.Workload, npart, ntraj, seed, pf=False, theta_rows=None, keep_dir=None, pfn=0,
                  mbp=0, samples=False, abcw=None):
+    if ONLY is not None and name not in ONLY:
+        return
     work = tempfile.mkdtemp(prefix=f"golden_{name}_")
     try:
         toml = synth.write_beep_inputs(w, work)
@@ -171,13 +176,8 @@ def main():
     ap.add_argument("--keep", default=None, help="keep the generated TOML/CSV inputs here")
     ap.add_argument("--only", default=None, help="comma-separated fixture names to (re)generate; default all")
     a = ap.parse_args()
-    only = set(a.only.split(",")) if a.only else None
-    global make_fixture
-    _make = make_fixture
-
-    def make_fixture(name, *args, **kw):          # noqa: F811 -- skips fixtures not asked for
-        if only is None or name in only:
-            _make(name, *args, **kw)
+    global ONLY
+    ONLY = set(a.only.split(",")) if a.only else None
     subprocess.run(["make", "-s", "-f", "oracle/Makefile.ref", f"REF={a.ref}", "-j8"], cwd=ROOT, check=True)
 
     # tiny: 4 areas x 3 ages, 40 days at dt 0.25
