@@ -284,11 +284,12 @@ BEEP_API beep_status beep_abcsmc_weights(int32_t nvar, int32_t nnew, const doubl
  *               supported (64 to 512 areas, one or two strains, more than 256
  *               area x group columns).
  *   "fast_ctas_per_sm"  particles resident per SM in the fast form, for models
- *               of 257 to 640 area x group columns with at most 320 strain x
- *               area pairs: 0 = automatic (several when at least three
- *               particles' state fits the SM's shared memory, else one),
- *               1 = one (640-thread CTAs), 2..4 = at most that many
- *               (320-thread CTAs; at most 3 above 8 ages).
+ *               of more than 256 area x group columns: 0 = automatic (several
+ *               when at least three particles' state fits the SM's shared
+ *               memory and the batch is large enough for several per SM to
+ *               finish sooner than one, else one), 1 = one (640-thread CTAs),
+ *               2..4 = at most that many (320-thread CTAs; at most 3 above 8
+ *               ages; the particles' state may then move to global memory).
  * Unknown names or values give BEEP_BAD_INPUT. */
 BEEP_API beep_status beep_set_option(const char *name, int64_t value);
 
