@@ -4,12 +4,18 @@
 // src/abcsmc.cc:275-283):
 //   w_i = exp(logprior_i) / sum_j w_j^last exp(-0.5 (d/size)^T M^-1 (d/size)),
 //   d = theta_i - theta_j over the inferred parameters; then w /= mean(w).
-// The N_new x N_last kernel terms are formed in FP32 (each is a quadratic form
-// of parameter differences of order one) and summed per particle with
-// compensation; the per-particle sums, the prior factor and the normalisation
-// are FP64.
+// The N_new x N_last kernel terms are formed in FP32 from parameters centred
+// on the last generation's FP64 mean (the differences are unchanged, and no
+// cancellation against a large common offset is left to FP32).  Each new
+// particle's sum  sum_j w_j exp(-q_j / 2)  is accumulated as a running
+// log-sum-exp -- the largest exponent so far, m, and the compensated sum of
+// exp(x_j - m) -- so that it cannot underflow even when every term would
+// (far-away particles); the per-particle log sums, the prior factor and the
+// normalisation are FP64.  Where the reference's FP64 sum underflows to zero
+// (its weight is then infinite) this one stays finite.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -22,24 +28,24 @@ constexpr int kAbcThreads = 256;
 constexpr int kAbcTile = 256;        // last-generation particles staged per pass
 constexpr int kMaxVar = 16;
 
-__global__ void __launch_bounds__(kAbcThreads) abc_kernel_sums(int nvar, int nnew, const float *th_new, int nlast,
-                                                               const float *th_last, const float *w_last,
-                                                               const float *A, double *sum_out)
+__global__ void __launch_bounds__(kAbcThreads) abc_kernel_logsums(int nvar, int nnew, const float *th_new, int nlast,
+                                                                  const float *th_last, const float *logw_last,
+                                                                  const float *A, double *logsum_out)
 {
 	__shared__ float s_th[kAbcTile * kMaxVar];
-	__shared__ float s_w[kAbcTile];
+	__shared__ float s_lw[kAbcTile];
 	__shared__ float s_A[kMaxVar * kMaxVar];
 	const int i = blockIdx.x * kAbcThreads + threadIdx.x;
 	for (int k = threadIdx.x; k < nvar * nvar; k += kAbcThreads) s_A[k] = A[k];
 	float x[kMaxVar];
 #pragma unroll
 	for (int v = 0; v < kMaxVar; v++) x[v] = (i < nnew && v < nvar) ? th_new[(size_t)i * nvar + v] : 0.f;
-	float s = 0.f, cmp = 0.f;
+	float mx = -INFINITY, s = 0.f, cmp = 0.f;      // running max exponent; compensated sum of exp(x_j - mx)
 	for (int j0 = 0; j0 < nlast; j0 += kAbcTile) {
 		const int nj = min(kAbcTile, nlast - j0);
 		__syncthreads();
 		for (int k = threadIdx.x; k < nj * nvar; k += kAbcThreads) s_th[k] = th_last[(size_t)j0 * nvar + k];
-		for (int k = threadIdx.x; k < nj; k += kAbcThreads) s_w[k] = w_last[j0 + k];
+		for (int k = threadIdx.x; k < nj; k += kAbcThreads) s_lw[k] = logw_last[j0 + k];
 		__syncthreads();
 		if (i < nnew) {
 			for (int j = 0; j < nj; j++) {
@@ -57,15 +63,22 @@ __global__ void __launch_bounds__(kAbcThreads) abc_kernel_sums(int nvar, int nne
 						q = fmaf(d[v1], r, q);
 					}
 				}
-				const float term = s_w[j] * expf(-0.5f * q);
-				const float y = term - cmp;          // Kahan
+				const float xe = s_lw[j] - 0.5f * q;
+				if (xe == -INFINITY) continue;       // a previous particle of weight zero
+				if (xe > mx) {                       // new largest exponent: rescale the sum
+					const float f = expf(mx - xe);
+					s *= f;
+					cmp *= f;
+					mx = xe;
+				}
+				const float y = expf(xe - mx) - cmp;   // Kahan
 				const float t = s + y;
 				cmp = (t - s) - y;
 				s = t;
 			}
 		}
 	}
-	if (i < nnew) sum_out[i] = (double)s - (double)cmp;
+	if (i < nnew) logsum_out[i] = (double)mx + log((double)s - (double)cmp);
 }
 
 }  // namespace
@@ -85,35 +98,62 @@ extern "C" BEEP_API beep_status beep_abcsmc_weights(int32_t nvar, int32_t nnew, 
 	int dev = 0;
 	CUDA_TRY(cudaGetDevice(&dev));
 	// (d/size)^T M^-1 (d/size) = d^T (M^-1 / size^2) d
-	std::vector<float> A((size_t)nvar * nvar), tn((size_t)nnew * nvar), tl((size_t)nlast * nvar), wl(nlast);
+	std::vector<float> A((size_t)nvar * nvar), tn((size_t)nnew * nvar), tl((size_t)nlast * nvar), lwl(nlast);
 	for (int k = 0; k < nvar * nvar; k++) A[k] = (float)(inv_cov[k] / (size * size));
-	for (size_t k = 0; k < tn.size(); k++) tn[k] = (float)theta_new[k];
-	for (size_t k = 0; k < tl.size(); k++) tl[k] = (float)theta_last[k];
-	for (int k = 0; k < nlast; k++) wl[k] = (float)w_last[k];
+	// both generations centred on the last one's mean (FP64) before rounding to FP32
+	std::vector<double> mean(nvar, 0.0);
+	for (int j = 0; j < nlast; j++)
+		for (int v = 0; v < nvar; v++) mean[v] += theta_last[(size_t)j * nvar + v];
+	for (int v = 0; v < nvar; v++) mean[v] /= nlast;
+	for (int i = 0; i < nnew; i++)
+		for (int v = 0; v < nvar; v++) tn[(size_t)i * nvar + v] = (float)(theta_new[(size_t)i * nvar + v] - mean[v]);
+	for (int j = 0; j < nlast; j++)
+		for (int v = 0; v < nvar; v++) tl[(size_t)j * nvar + v] = (float)(theta_last[(size_t)j * nvar + v] - mean[v]);
+	bool any_weight = false;
+	for (int k = 0; k < nlast; k++) {
+		if (!(w_last[k] >= 0.0)) return fail(BEEP_BAD_INPUT, "abcsmc weights: negative or NaN previous weight");
+		lwl[k] = w_last[k] > 0.0 ? (float)std::log(w_last[k]) : -INFINITY;
+		any_weight |= w_last[k] > 0.0;
+	}
+	if (!any_weight) return fail(BEEP_BAD_INPUT, "abcsmc weights: every previous weight is zero");
 	Layout L;
 	const size_t o_A = L.add(4 * A.size()), o_tn = L.add(4 * tn.size()), o_tl = L.add(4 * tl.size()),
-	             o_wl = L.add(4 * wl.size()), o_s = L.add(8 * (size_t)nnew);
+	             o_wl = L.add(4 * lwl.size()), o_s = L.add(8 * (size_t)nnew);
 	DevBuf buf;
 	CUDA_TRY(buf.reserve(L.size));
 	char *d = (char *)buf.ptr;
-	std::vector<double> sums(nnew);
+	std::vector<double> logsums(nnew);
 	cudaError_t e = cudaMemcpy(d + o_A, A.data(), 4 * A.size(), cudaMemcpyHostToDevice);
 	if (e == cudaSuccess) e = cudaMemcpy(d + o_tn, tn.data(), 4 * tn.size(), cudaMemcpyHostToDevice);
 	if (e == cudaSuccess) e = cudaMemcpy(d + o_tl, tl.data(), 4 * tl.size(), cudaMemcpyHostToDevice);
-	if (e == cudaSuccess) e = cudaMemcpy(d + o_wl, wl.data(), 4 * wl.size(), cudaMemcpyHostToDevice);
+	if (e == cudaSuccess) e = cudaMemcpy(d + o_wl, lwl.data(), 4 * lwl.size(), cudaMemcpyHostToDevice);
 	if (e == cudaSuccess) {
-		abc_kernel_sums<<<(nnew + kAbcThreads - 1) / kAbcThreads, kAbcThreads>>>(
+		abc_kernel_logsums<<<(nnew + kAbcThreads - 1) / kAbcThreads, kAbcThreads>>>(
 		    nvar, nnew, (const float *)(d + o_tn), nlast, (const float *)(d + o_tl), (const float *)(d + o_wl),
 		    (const float *)(d + o_A), (double *)(d + o_s));
 		e = cudaGetLastError();
 	}
-	if (e == cudaSuccess) e = cudaMemcpy(sums.data(), d + o_s, 8 * (size_t)nnew, cudaMemcpyDeviceToHost);
+	if (e == cudaSuccess) e = cudaMemcpy(logsums.data(), d + o_s, 8 * (size_t)nnew, cudaMemcpyDeviceToHost);
 	buf.release();
 	if (e != cudaSuccess) return fail(BEEP_DEVICE_ERROR, std::string("abcsmc weights: ") + cudaGetErrorString(e));
-	for (int i = 0; i < nnew; i++) w_out[i] = std::exp(logprior_new[i]) / sums[i];
-	if (normalise) {                                  // ABCSMC::normalise_particle_weights
+	std::vector<double> logw(nnew);
+	double lmax = -INFINITY;
+	for (int i = 0; i < nnew; i++) {
+		if (logsums[i] != logsums[i]) return fail(BEEP_NAN_RATE, "abcsmc weights: NaN kernel sum (non-finite parameters?)");
+		logw[i] = logprior_new[i] - logsums[i];
+		lmax = std::max(lmax, logw[i]);
+	}
+	if (!normalise) {
+		for (int i = 0; i < nnew; i++) w_out[i] = std::exp(logw[i]);
+	} else {
+		// ABCSMC::normalise_particle_weights, w /= mean(w), formed relative to the
+		// largest weight so that no weight overflows on the way
+		if (!(lmax > -INFINITY)) return fail(BEEP_BAD_INPUT, "abcsmc weights: every new particle has prior weight zero");
 		double wsum = 0.0;
-		for (int i = 0; i < nnew; i++) wsum += w_out[i];
+		for (int i = 0; i < nnew; i++) {
+			w_out[i] = std::exp(logw[i] - lmax);
+			wsum += w_out[i];
+		}
 		wsum /= nnew;
 		for (int i = 0; i < nnew; i++) w_out[i] /= wsum;
 	}

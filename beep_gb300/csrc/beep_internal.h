@@ -106,6 +106,7 @@ struct BatchDev {
 	int32_t foi_tc;
 	size_t tc_smem_off;
 	int32_t nt;                         // fast form: threads per CTA (0: fast_pick_threads)
+	uint32_t sampler_limit;             // rejection iterations before a draw reports BEEP_TIMEOUT (0: 65536)
 	int32_t ctas;                       // fast form, nt == kDualThreads: CTAs resident per SM (2..4)
 };
 
@@ -120,6 +121,7 @@ int fast_pick_threads(const ModelDev &m);        // threads per CTA of the fast 
 // library options (beep_set_option)
 int option_fast_foi();                           // 0 automatic, 1 FP32 SIMT, 2 tensor cores
 int option_fast_ctas();                          // 0 automatic, 1, or 2..4: particles (CTAs) per SM, at most
+uint32_t option_sampler_limit();                 // 0 (65536) or the rejection-iteration limit of the samplers
 constexpr int kDualThreads = 320;                // threads per CTA with several particles per SM
 constexpr size_t kSmemPerSM = 228 * 1024;        // shared memory per SM (each resident CTA reserves 1 KB)
 int fast_threads();

@@ -35,6 +35,7 @@ namespace beep {
 thread_local std::string g_err;
 std::atomic<int> g_fast_foi{0};
 std::atomic<int> g_fast_ctas{0};
+std::atomic<uint32_t> g_sampler_limit{0};
 
 beep_status fail(beep_status s, const std::string &msg)
 {
@@ -79,6 +80,11 @@ beep_status beep_set_option(const char *name, int64_t value)
 	if (std::string(name) == "fast_ctas_per_sm") {
 		if (value < 0 || value > 4) return fail(BEEP_BAD_INPUT, "fast_ctas_per_sm must be 0 (automatic) or 1..4");
 		g_fast_ctas.store((int)value);
+		return BEEP_OK;
+	}
+	if (std::string(name) == "sampler_iteration_limit") {
+		if (value < 0 || value > 65536) return fail(BEEP_BAD_INPUT, "sampler_iteration_limit must be 0 (default 65536) or 1..65536");
+		g_sampler_limit.store((uint32_t)value);
 		return BEEP_OK;
 	}
 	return fail(BEEP_BAD_INPUT, std::string("unknown option ") + name);
@@ -781,6 +787,7 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 	char *dw = (char *)q->work_dev.ptr, *dout = (char *)q->out_dev.ptr;
 	BatchDev &bd = q->bd;
 	bd.P = P; bd.ti = b->ti; bd.tf = b->tf; bd.ngroup = b->ngroup;
+	bd.sampler_limit = option_sampler_limit();
 	bd.k0 = (uint32_t)b->seed; bd.k1 = (uint32_t)(b->seed >> 32);
 	bd.nscored = nscored;
 	bd.pop_a = (int32_t *)(dw + w_pa); bd.pop_b = (int32_t *)(dw + w_pb);
@@ -1040,3 +1047,5 @@ size_t beep::batch_device_bytes(const beep_batch *q)
 int beep::option_fast_foi() { return g_fast_foi.load(); }
 
 int beep::option_fast_ctas() { return g_fast_ctas.load(); }
+
+uint32_t beep::option_sampler_limit() { return g_sampler_limit.load(); }

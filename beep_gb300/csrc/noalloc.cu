@@ -3,8 +3,8 @@
 //
 // Who needs it: a host application that owns every byte of device memory
 // through its own allocator or a fixed memory budget (an embedding framework
-// with a memory pool, a service that pre-reserves HBM at start-up), or code
-// that enqueues work where an allocation would stall or is forbidden.  Such a
+// with a memory pool, a service that pre-reserves HBM at start-up), where a
+// cudaMalloc by a library would fail or take memory the pool counts on.  Such a
 // caller allocates the inputs and outputs itself and passes device pointers;
 // the kernel's working memory (per-particle populations, counts, infectivity
 // maps, observation sums, the packed tables and observation lists) comes from
@@ -17,7 +17,9 @@
 // on each device should come before any stream capture).  Every call uses the
 // same array, which keeps the previous call's contents: the regions that must
 // start at zero are cleared by each call, and two calls whose work overlaps on
-// the GPU (for example on different streams) race on the array.
+// the GPU (for example on different streams) race on the array.  The call is
+// synchronous: it reads the caller's index tables on the host (in order on the
+// caller's stream) and returns once its kernel finished, on every path.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -72,15 +74,24 @@ extern "C" BEEP_API beep_status beep_simulate_plain_noalloc(beep_model *m, const
 	}
 	char *base = (char *)g_noalloc_addr[dev];
 	cudaStream_t st = (cudaStream_t)stream;
+	// Every return from here on waits for the work this call enqueued, so that no
+	// copy into the shared array is still in flight when the next call takes the lock.
+	struct StreamDrain {
+		cudaStream_t s;
+		~StreamDrain() { cudaStreamSynchronize(s); }
+	} drain{st};
 
 	const size_t A = m->A, G = m->G, DP = m->DP, NS = m->NS, C = m->C, T = m->T, S = m->S;
 	const size_t P = (size_t)nparticle, popsz = A * C * DP, tnsz = A * T * DP, agsz = NS * A * G;
-	// the index tables are read on the host to check their ranges (the kernel indexes with them)
+	// the index tables are read on the host to check their ranges (the kernel indexes
+	// with them); the reads are ordered on the caller's stream, behind whatever work
+	// of the caller's fills the tables there, and complete before the check
 	std::vector<int32_t> brow(NS * A), eref(NS * A);
 	std::vector<double> inf(C);
-	CUDA_TRY(cudaMemcpy(brow.data(), tab->beta_row_of, 4 * NS * A, cudaMemcpyDeviceToHost));
-	CUDA_TRY(cudaMemcpy(eref.data(), tab->efoi_ref, 4 * NS * A, cudaMemcpyDeviceToHost));
-	CUDA_TRY(cudaMemcpy(inf.data(), tab->infectivity, 8 * C, cudaMemcpyDeviceToHost));
+	CUDA_TRY(cudaMemcpyAsync(brow.data(), tab->beta_row_of, 4 * NS * A, cudaMemcpyDeviceToHost, st));
+	CUDA_TRY(cudaMemcpyAsync(eref.data(), tab->efoi_ref, 4 * NS * A, cudaMemcpyDeviceToHost, st));
+	CUDA_TRY(cudaMemcpyAsync(inf.data(), tab->infectivity, 8 * C, cudaMemcpyDeviceToHost, st));
+	CUDA_TRY(cudaStreamSynchronize(st));
 	for (size_t k = 0; k < NS * A; k++) {
 		if (brow[k] < 0 || brow[k] >= tab->nbeta_row) return fail(BEEP_BAD_INPUT, "beta_row_of out of range");
 		if (eref[k] < 0 || eref[k] >= tab->nefoi) return fail(BEEP_BAD_INPUT, "efoi_ref out of range");

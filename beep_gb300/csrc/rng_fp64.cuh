@@ -132,10 +132,10 @@ __device__ __forceinline__ double log_factorial_p(double k)
 	return (n - 0.5) * log_p(n) - n + 0.9189385332046728 + corr;
 }
 
-// Poisson(mean) of transition tr in column col at step sett; -1 after 65536
-// rejections (reported as an error by the caller).
+// Poisson(mean) of transition tr in column col at step sett; -1 after `limit`
+// rejections (65536 unless a test lowers it; reported as an error by the caller).
 static __device__ __noinline__ int32_t poisson_fp64(double mean, uint32_t k0, uint32_t k1, uint32_t col, uint32_t tr,
-                                              uint32_t sett, uint32_t stream)
+                                              uint32_t sett, uint32_t stream, uint32_t limit = 65536u)
 {
 	if (!(mean > 0.0)) return 0;
 	if (mean < 10.0) {
@@ -158,7 +158,7 @@ static __device__ __noinline__ int32_t poisson_fp64(double mean, uint32_t k0, ui
 	const double invalpha = 1.1239 + 1.1328 / (b - 3.4);
 	const double vr = 0.9277 - 3.6224 / (b - 2.0);
 	const double log_invalpha = log_p(invalpha);
-	for (uint32_t it = 0; it < 65536u; it++) {
+	for (uint32_t it = 0; it < limit; it++) {
 		const U4 r = philox10(U4{col, sett, stream, (PURPOSE_PTRS << 24) | (tr << 16) | it}, k0, k1);
 		const double U = u01_d(r.x) - 0.5;
 		const double V = u01_d(r.y);
@@ -175,9 +175,9 @@ static __device__ __noinline__ int32_t poisson_fp64(double mean, uint32_t k0, ui
 
 // Binomial(n, p) thinning of transition tr in column col at step sett (the
 // coupled proposal's count when the proposed mean is below the current one);
-// -1 after 65536 rejections.
+// -1 after `limit` rejections.
 static __device__ __noinline__ int32_t binomial_fp64(double p, int32_t n, uint32_t k0, uint32_t k1, uint32_t col,
-                                               uint32_t tr, uint32_t sett, uint32_t stream)
+                                               uint32_t tr, uint32_t sett, uint32_t stream, uint32_t limit = 65536u)
 {
 	if (n <= 0 || !(p > 0.0)) return 0;
 	if (p >= 1.0) return n;
@@ -208,7 +208,7 @@ static __device__ __noinline__ int32_t binomial_fp64(double p, int32_t n, uint32
 		const double lpq = log_p(q / (1.0 - q));
 		const double h = log_factorial_p(m) + log_factorial_p(nd - m);
 		k = -1;
-		for (uint32_t it = 0; it < 65536u; it++) {
+		for (uint32_t it = 0; it < limit; it++) {
 			const U4 r = philox10(U4{col, sett, stream, (PURPOSE_BTRS << 24) | (tr << 16) | it}, k0, k1);
 			const double U = u01_d(r.x) - 0.5;
 			const double V = u01_d(r.y);

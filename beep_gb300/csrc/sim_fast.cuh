@@ -100,7 +100,7 @@ __device__ __forceinline__ float ptrs_rhs(float k, float mean, float loglam, con
 // FP32 Poisson draw on the keyed stream of the FP64 form (same counters/words).
 __device__ __forceinline__ int32_t poisson_fp32(float mean, uint32_t k0, uint32_t k1, uint32_t col, uint32_t tr,
                                                 uint32_t sett, uint32_t stream, U4 &inv, uint32_t &inv_call,
-                                                const float *rcp, const float *lnfact)
+                                                const float *rcp, const float *lnfact, uint32_t limit)
 {
 	if (mean < 10.f) {
 		const uint32_t call = tr >> 2;
@@ -129,7 +129,7 @@ __device__ __forceinline__ int32_t poisson_fp32(float mean, uint32_t k0, uint32_
 	const float vr = 0.9277f - __fdividef(3.6224f, b - 2.0f);
 	const float log_invalpha = __logf(invalpha);
 	const float two_a = 2.0f * a;
-	for (uint32_t it = 0; it < 65536u; it++) {
+	for (uint32_t it = 0; it < limit; it++) {
 		const U4 r = philox10(U4{col, sett, stream, (PURPOSE_PTRS << 24) | (tr << 16) | it}, k0, k1);
 		const float U = u01_f(r.x) - 0.5f;
 		const float V = u01_f(r.y);
@@ -436,7 +436,7 @@ __device__ __forceinline__ float stirling_rem(float z)
 //   + d log((n-k+1) q / ((k+1) (1-q))) + Stirling remainders,  d = k - m,
 // instead of differences of large log-factorials.
 __device__ __forceinline__ int32_t binomial_fp32(float p, int32_t n, uint32_t k0, uint32_t k1, uint32_t col, uint32_t tr,
-                                                 uint32_t sett, uint32_t stream)
+                                                 uint32_t sett, uint32_t stream, uint32_t limit)
 {
 	if (n <= 0 || !(p > 0.f)) return 0;
 	if (p >= 1.f) return n;
@@ -467,7 +467,7 @@ __device__ __forceinline__ int32_t binomial_fp32(float p, int32_t n, uint32_t k0
 		const float m = floorf((nd + 1.f) * q);
 		const float em = stirling_rem(m + 1.f) + stirling_rem(nd - m + 1.f);
 		k = -1;
-		for (uint32_t it = 0; it < 65536u; it++) {
+		for (uint32_t it = 0; it < limit; it++) {
 			const U4 r = philox10(U4{col, sett, stream, (PURPOSE_BTRS << 24) | (tr << 16) | it}, k0, k1);
 			const float U = u01_f(r.x) - 0.5f;
 			const float V = u01_f(r.y);
@@ -654,6 +654,7 @@ __global__ void __launch_bounds__(NT, MB) sim_fast_kernel(const ModelDev m, cons
 
 	const int itr = m.infection_trans;
 	const int inf_from = m.trans_from[itr];
+	const uint32_t lim = b.sampler_limit ? b.sampler_limit : 65536u;
 	const float dt = (float)m.dt;
 	bool cur = false;
 	int sb = 0;                                          // slice buffer of the step simulated
@@ -747,17 +748,17 @@ __global__ void __launch_bounds__(NT, MB) sim_fast_kernel(const ModelDev m, cons
 							if (mean > 1.0e9f) atomicCAS(status, 0, BEEP_COUNT_OVERFLOW);
 							else if (b.simu_all || (b.simu && b.simu[((size_t)p * m.S + sett) * A + c])) {
 								n = poisson_fp32(mean, b.k0, b.k1, (uint32_t)col, (uint32_t)tr, (uint32_t)sett, stream, inv,
-								                 inv_call, s.rcp, s.lnfact);
+								                 inv_call, s.rcp, s.lnfact, lim);
 							} else {                       // coupled to the current state (src/mbp.cc:293-305)
 								const int32_t ni = b.ch_tn[ci];
 								const float ri = b.ch_mean_f[ci];
 								if (mean > ri) {
 									n = poisson_fp32(mean - ri, b.k0, b.k1, (uint32_t)col, (uint32_t)tr, (uint32_t)sett,
-									                 stream, inv, inv_call, s.rcp, s.lnfact);
+									                 stream, inv, inv_call, s.rcp, s.lnfact, lim);
 									if (n >= 0) n += ni;
 								} else if (mean == ri) n = ni;
 								else n = binomial_fp32(mean / ri, ni, b.k0, b.k1, (uint32_t)col, (uint32_t)tr, (uint32_t)sett,
-								                       stream);
+								                       stream, lim);
 							}
 							if (n < 0) { atomicCAS(status, 0, BEEP_TIMEOUT); n = 0; }
 						}
@@ -769,7 +770,7 @@ __global__ void __launch_bounds__(NT, MB) sim_fast_kernel(const ModelDev m, cons
 					if (mean > 1.0e9f) atomicCAS(status, 0, BEEP_COUNT_OVERFLOW);
 					else {
 						n = poisson_fp32(mean, b.k0, b.k1, (uint32_t)col, (uint32_t)tr, (uint32_t)sett, stream, inv, inv_call,
-						                 s.rcp, s.lnfact);
+						                 s.rcp, s.lnfact, lim);
 						if (n < 0) { atomicCAS(status, 0, BEEP_TIMEOUT); n = 0; }
 					}
 				} else if (mean != mean) atomicCAS(status, 0, BEEP_NAN_RATE);

@@ -89,6 +89,7 @@ __device__ __forceinline__ void set_status(int32_t *st, int v)
 
 __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, const BatchDev b)
 {
+	const uint32_t lim = b.sampler_limit ? b.sampler_limit : 65536u;   // sampler rejection iterations
 	const int p = blockIdx.x;
 	if (p >= b.P) return;
 	const int tid = threadIdx.x, nth = blockDim.x;
@@ -281,16 +282,16 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 				else {
 					const uint32_t col = (uint32_t)(c * DP + dp);
 					if (mode == 0 || b.simu_all || (b.simu && b.simu[((size_t)p * m.S + sett) * A + c])) {
-						n = poisson_fp64(mean, b.k0, b.k1, col, (uint32_t)tr, (uint32_t)sett, stream);
+						n = poisson_fp64(mean, b.k0, b.k1, col, (uint32_t)tr, (uint32_t)sett, stream, lim);
 					} else {                        // coupled to the current state (src/mbp.cc:293-305)
 						const size_t ci = chs(cs_i, sett) * tnsz + cell;
 						const int32_t ni = b.ch_tn[ci];
 						const double ri = b.ch_mean[ci];
 						if (mean > ri) {
-							n = poisson_fp64(mean - ri, b.k0, b.k1, col, (uint32_t)tr, (uint32_t)sett, stream);
+							n = poisson_fp64(mean - ri, b.k0, b.k1, col, (uint32_t)tr, (uint32_t)sett, stream, lim);
 							if (n >= 0) n += ni;
 						} else if (mean == ri) n = ni;
-						else n = binomial_fp64(mean / ri, ni, b.k0, b.k1, col, (uint32_t)tr, (uint32_t)sett, stream);
+						else n = binomial_fp64(mean / ri, ni, b.k0, b.k1, col, (uint32_t)tr, (uint32_t)sett, stream, lim);
 					}
 					if (n < 0) { set_status(status, BEEP_TIMEOUT); n = 0; }
 				}

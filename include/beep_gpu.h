@@ -415,7 +415,7 @@ BEEP_API beep_status beep_serve_release(beep_server *server, uint64_t ticket);
 /* Plain FP64 simulation that allocates no memory on the GPU.  No counterpart
  * in the reference: it serves callers that cannot call cudaMalloc -- an
  * application whose allocator or fixed memory budget owns all device memory,
- * or code that must not trigger an allocation while it enqueues work.  The
+ * where an allocation by a library fails or takes memory the pool counts on.  The
  * caller allocates and passes device pointers: the tables of one parameter
  * set (every pointer in `tables` is a device pointer; the struct itself is in
  * host memory), pop_in (when ti > 0), L_out [nparticle] and pop_out
@@ -426,8 +426,10 @@ BEEP_API beep_status beep_serve_release(beep_server *server, uint64_t ticket);
  * first call on a device looks up the array's device address (make that call
  * before any stream capture).  Calls share the array: the call clears what
  * must start at zero, and calls that overlap on the GPU race.  The call
- * enqueues on `stream` (a cudaStream_t, NULL = legacy default stream) and
- * returns after the kernel finished, with its status.  Same results as
+ * is synchronous: it enqueues on `stream` (a cudaStream_t, NULL = legacy
+ * default stream), first reading the index tables back to the host in stream
+ * order to check their ranges, and returns after the kernel finished, with
+ * its status (also when it fails part-way).  Same results as
  * beep_simulate with BEEP_FORM_PLAIN_FP64 on the same inputs. */
 BEEP_API beep_status beep_simulate_plain_noalloc(beep_model *model, const beep_param_tables *tables,
                                                  int32_t nparticle, uint64_t seed, int32_t ti, int32_t tf,

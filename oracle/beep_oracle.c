@@ -808,6 +808,8 @@ void beep_oracle_abcsmc_weights(int32_t nvar, int32_t nnew, const double *theta_
                                 int32_t nlast, const double *theta_last, const double *w_last,
                                 const double *inv_cov, double size, int32_t normalise, double *w_out)
 {
+	/* new particles are independent: spread over the host's threads (each sum in the reference's order) */
+#pragma omp parallel for schedule(static)
 	for (int32_t i = 0; i < nnew; i++) {
 		const double *pend = theta_new + (size_t)i * nvar;
 		double sum = 0.0;

@@ -1,6 +1,7 @@
 """Generates the golden fixtures in this folder from the reference itself.
 
-Needs the reference source tree (default /root/reference) and builds the
+Needs the reference source tree (--ref; default BEEP_REF_DIR, else a checkout
+named ``reference`` beside the repository) and builds the
 reference oracle with oracle/Makefile.ref.  For each fixture:
   1. a seeded synthetic workload is written in the reference's TOML/CSV format
      with placeholder observations;
@@ -11,7 +12,7 @@ reference oracle with oracle/Makefile.ref.  For each fixture:
      log-likelihoods, checksums and (for a few particles) full transition and
      population trajectories are saved as a bundle ``<name>.bnd``.
 
-usage: python tests/golden/make_golden.py [--ref /root/reference]
+usage: python tests/golden/make_golden.py [--ref REFERENCE_TREE]
 """
 from __future__ import annotations
 
@@ -172,7 +173,7 @@ def make_fixture(name, w: synth.Workload, npart, ntraj, seed, pf=False, theta_ro
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("BEEP_REF_DIR") or os.path.join(os.path.dirname(ROOT), "reference"))
     ap.add_argument("--keep", default=None, help="keep the generated TOML/CSV inputs here")
     ap.add_argument("--only", default=None, help="comma-separated fixture names to (re)generate; default all")
     a = ap.parse_args()

@@ -68,3 +68,90 @@ def test_gpu_weights_match_reference():
     args, size, w_ref, wn_ref = _reference_case()
     np.testing.assert_allclose(capi.abcsmc_weights(*args, size, normalise=False), w_ref, rtol=1e-5)
     np.testing.assert_allclose(capi.abcsmc_weights(*args, size, normalise=True), wn_ref, rtol=1e-5)
+
+
+def _logsumexp_weights(tn, lp, tl, wl, ic, size):
+    """FP64 weights through a log-sum-exp (no underflow), normalised to mean 1."""
+    out = np.zeros(len(tn))
+    for i in range(len(tn)):
+        d = (tn[i] - tl) / size
+        x = np.log(wl) - 0.5 * np.einsum("jv,vu,ju->j", d, ic, d)
+        m = x.max()
+        out[i] = lp[i] - (m + np.log(np.exp(x - m).sum()))
+    w = np.exp(out - out.max())
+    return w / w.mean()
+
+
+@pytest.mark.gpu
+def test_gpu_weights_large_offsets():
+    """Parameters of magnitude 1e3 with a spread of 1e-2: the differences are
+    formed from values centred on the last generation's mean, so FP32 keeps
+    the 1e-5 tolerance."""
+    from beep_gb300 import build
+    build.build()
+    rng = np.random.default_rng(11)
+    nvar, nnew, nlast = 3, 300, 400
+    tl = 1000.0 + rng.normal(0.0, 0.01, (nlast, nvar))
+    wl = rng.uniform(0.2, 2.0, nlast)
+    tn = tl[rng.integers(0, nlast, nnew)] + rng.normal(0, 0.003, (nnew, nvar))
+    ic = np.linalg.inv(np.cov(tl.T, aweights=wl))
+    lp = np.zeros(nnew)
+    g = capi.abcsmc_weights(tn, lp, tl, wl, ic, 1.0)
+    o = oracle_abcsmc_weights(tn, lp, tl, wl, ic, 1.0)
+    np.testing.assert_allclose(g, o, rtol=1e-5)
+
+
+@pytest.mark.gpu
+def test_gpu_weights_where_fp32_terms_underflow():
+    """New particles about 12 standard deviations from every previous one:
+    quadratic forms of a few hundred, whose exponentials underflow in FP32
+    (not in FP64).  The sums are kept as a running log-sum-exp, so the weights
+    still match the oracle's FP64 ones, unnormalised and normalised."""
+    from beep_gb300 import build
+    build.build()
+    rng = np.random.default_rng(12)
+    tn, lp, tl, wl, ic = generation(rng, 64, 200)
+    tn[:8] += 12.0 * np.sqrt(np.diag(np.linalg.inv(ic)))
+    for norm in (False, True):
+        g = capi.abcsmc_weights(tn, lp, tl, wl, ic, 1.0, normalise=norm)
+        o = oracle_abcsmc_weights(tn, lp, tl, wl, ic, 1.0, normalise=norm)
+        assert np.all(np.isfinite(o))
+        np.testing.assert_allclose(g, o, rtol=1e-5)
+
+
+@pytest.mark.gpu
+def test_gpu_weights_finite_where_every_term_underflows():
+    """A new particle 40 standard deviations from every previous one: its
+    kernel sum underflows even in FP64 (the reference's weight is then
+    infinite).  The normalised weights stay finite; checked against an FP64
+    log-sum-exp."""
+    from beep_gb300 import build
+    build.build()
+    rng = np.random.default_rng(12)
+    tn, lp, tl, wl, ic = generation(rng, 64, 200)
+    tn[:8] += 40.0 * np.sqrt(np.diag(np.linalg.inv(ic)))
+    g = capi.abcsmc_weights(tn, lp, tl, wl, ic, 1.0)
+    assert np.all(np.isfinite(g)) and np.all(g >= 0)
+    np.testing.assert_allclose(g, _logsumexp_weights(tn, lp, tl, wl, ic, 1.0), rtol=1e-5, atol=1e-300)
+
+
+@pytest.mark.gpu
+def test_gpu_weights_full_generation_size():
+    """16384 new against 16384 previous particles (the ABC-SMC generation of
+    150 areas x 4 ages), against the oracle's FP64 weights."""
+    from beep_gb300 import build
+    build.build()
+    rng = np.random.default_rng(13)
+    tn, lp, tl, wl, ic = generation(rng, 16384, 16384)
+    g = capi.abcsmc_weights(tn, lp, tl, wl, ic, 1.3)
+    o = oracle_abcsmc_weights(tn, lp, tl, wl, ic, 1.3)
+    np.testing.assert_allclose(g, o, rtol=1e-5)
+
+
+@pytest.mark.gpu
+def test_gpu_weights_reject_zero_previous_weights():
+    from beep_gb300 import build
+    build.build()
+    tn, lp, tl, wl, ic = generation(np.random.default_rng(14), 4, 8)
+    with pytest.raises(capi.BeepError):
+        capi.abcsmc_weights(tn, lp, tl, np.zeros_like(wl), ic, 1.3)

@@ -63,3 +63,8 @@ def test_set_option_validates_names_and_values():
         capi.set_option("fast_foi", 7)
     with pytest.raises(capi.BeepError):
         capi.set_option("no_such_option", 1)
+    capi.set_option("sampler_iteration_limit", 1)
+    capi.set_option("sampler_iteration_limit", 0)
+    for bad in (-1, 65537):
+        with pytest.raises(capi.BeepError):
+            capi.set_option("sampler_iteration_limit", bad)
