@@ -317,7 +317,7 @@ def lib():
     return _LIB
 
 
-FOI_AUTO, FOI_SIMT, FOI_TENSOR = 0, 1, 2
+FOI_AUTO, FOI_SIMT, FOI_TENSOR, FOI_BATCHED = 0, 1, 2, 3
 
 
 def set_option(name: str, value: int) -> None:
@@ -367,6 +367,11 @@ class DeviceModel:
         h = C.c_void_p()
         check(L.beep_model_create(C.byref(model.desc), C.byref(h)))
         self.h = h
+        # handles made on this model (batches, chain sets) that are still open: the
+        # model is destroyed only after the last of them, whatever order the garbage
+        # collector finalises them in
+        self._deps = 0
+        self._closing = False
         _track(self, 2)
 
     def simulate(self, batch: Batch) -> Batch:
@@ -405,8 +410,16 @@ class DeviceModel:
 
     def close(self):
         if self.h:
+            if self._deps > 0:
+                self._closing = True            # the last dependent handle destroys the model
+                return
             lib().beep_model_destroy(self.h)
             self.h = None
+
+    def _release_dep(self):
+        self._deps -= 1
+        if self._closing and self._deps == 0:
+            self.close()
 
     def __del__(self):
         try:
@@ -424,6 +437,7 @@ class DeviceBatch:
         h = C.c_void_p()
         check(lib().beep_batch_create(dm.h, C.byref(batch.st), C.byref(h)))
         self.h = h
+        dm._deps += 1
         _track(self, 1)
 
     def stage(self):
@@ -463,17 +477,20 @@ class DeviceBatch:
         return lib().beep_batch_launches(self.h)
 
     def foi_path(self) -> int:
-        """1 = FP32 SIMT force of infection, 2 = tensor cores, 0 = plain form."""
+        """1 = FP32 SIMT force of infection, 2 = tensor cores (one particle per CTA), 3 = tensor cores
+        batched over the particles (step-synchronous layout), 0 = plain form."""
         return lib().beep_batch_foi_path(self.h)
 
     def ctas_per_sm(self) -> int:
-        """Particles (CTAs) per SM the fast-form kernel is laid out for; 0 = plain form."""
+        """Particles (CTAs) per SM the fast-form kernel is laid out for; 0 = plain form or the
+        step-synchronous layout (particles not pinned to SMs)."""
         return lib().beep_batch_ctas_per_sm(self.h)
 
     def close(self):
         if self.h:
             lib().beep_batch_destroy(self.h)
             self.h = None
+            self.dm._release_dep()
 
     def __del__(self):
         try:
@@ -506,6 +523,7 @@ class MbpChains:
         h = C.c_void_p()
         check(lib().beep_mbp_create(dm.h, nchain, form, C.byref(h)))
         self.h = h
+        dm._deps += 1
         _track(self, 0)
 
     def _request(self, tables: Sequence[Tables], seed: int, group_of=None, stream_of=None,
@@ -572,6 +590,7 @@ class MbpChains:
         if self.h:
             lib().beep_mbp_destroy(self.h)
             self.h = None
+            self.dm._release_dep()
 
     def __del__(self):
         try:

@@ -107,6 +107,15 @@ struct BatchDev {
 	size_t tc_smem_off;
 	int32_t nt;                         // fast form: threads per CTA (0: fast_pick_threads)
 	uint32_t sampler_limit;             // rejection iterations before a draw reports BEEP_TIMEOUT (0: 65536)
+	// fast form, step-synchronous layout (sim_batched.cu): every particle advances one step
+	// at a time; the force of infection is one tensor-core product over the batch per step
+	int32_t batched;
+	int32_t *bx_pop;                    // [1 or 2][P][C][A*DP] populations (column-major per particle)
+	float *bx_ic;                       // [2][P][NS][A][G] infectious counts of the step / the next step
+	float *bx_y;                        // [P][NS][A][G] area-mixing contraction of the step's counts
+	float *bx_slot;                     // [P][nslots] observation accumulators
+	float2 *bx_kahan;                   // [P][step threads] compensated log-likelihood partial sums
+	int32_t *bx_work;                   // [tf-ti] particle counters of the step kernels
 	int32_t ctas;                       // fast form, nt == kDualThreads: CTAs resident per SM (2..4)
 };
 
@@ -119,7 +128,8 @@ size_t fast_gstate_stride(const ModelDev &m);
 size_t fast_tc_smem_bytes(const ModelDev &m);   // shared memory of the tensor-core FOI
 int fast_pick_threads(const ModelDev &m);        // threads per CTA of the fast kernel for this model
 // library options (beep_set_option)
-int option_fast_foi();                           // 0 automatic, 1 FP32 SIMT, 2 tensor cores
+int option_fast_foi();                           // 0 automatic, 1 FP32 SIMT, 2 tensor cores per particle,
+                                                 // 3 tensor cores batched over the particles (step-synchronous)
 int option_fast_ctas();                          // 0 automatic, 1, or 2..4: particles (CTAs) per SM, at most
 uint32_t option_sampler_limit();                 // 0 (65536) or the rejection-iteration limit of the samplers
 constexpr int kDualThreads = 320;                // threads per CTA with several particles per SM
@@ -133,5 +143,12 @@ int fast_ctas_max(int G);                        // most 320-thread CTAs per SM 
 int launch_sim_fast_ctas(const ModelDev &m, const BatchDev &b, size_t smem, void *stream);   // sim_fast_ctas.cu
 int fast_chain_ctas_prepare();                   // constant tables of mbp_fast_ctas.cu
 int launch_sim_fast_chain_ctas(const ModelDev &m, const BatchDev &b, size_t smem, void *stream);   // mbp_fast_ctas.cu
+// step-synchronous fast form (sim_batched.cu)
+bool batched_supported(const ModelDev &m);
+size_t batched_step_smem(const ModelDev &m, int tnrows);
+int batched_step_threads();
+int batched_prepare();                           // constant tables of sim_batched.cu
+int batched_launches(int nsteps);                // kernel launches of one batch run
+int launch_sim_batched(const ModelDev &m, const BatchDev &b, int sms, void *stream);
 
 }  // namespace beep

@@ -73,7 +73,7 @@ beep_status beep_set_option(const char *name, int64_t value)
 {
 	if (!name) return fail(BEEP_BAD_INPUT, "null option name");
 	if (std::string(name) == "fast_foi") {
-		if (value < 0 || value > 2) return fail(BEEP_BAD_INPUT, "fast_foi must be 0, 1 or 2");
+		if (value < 0 || value > 3) return fail(BEEP_BAD_INPUT, "fast_foi must be 0, 1, 2 or 3");
 		g_fast_foi.store((int)value);
 		return BEEP_OK;
 	}
@@ -686,13 +686,23 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 			return fail(BEEP_BAD_INPUT, "model too large for the fast form (observation slots or tables exceed shared memory, or more than 8 transitions)");
 		}
 		q->bd.m_in_smem = fast_smem_bytes(m->dev, nslots, true, q->bd.nefoi_stage, q->state_global, tnrows, ps) <= limit ? 1 : 0;
-		// force of infection on the tensor cores: large models (the matrix is streamed from
-		// L2 each step; the particle's populations and counts move to global memory to make
-		// room for the operand ring)
+		// force of infection on the tensor cores, batched over the particles: every particle
+		// advances one step at a time and the contraction is one product over the batch per
+		// step (sim_batched.cu); the default for large models
 		const int opt = option_fast_foi() != 0 ? option_fast_foi() : m->tuned_foi;
+		const bool can_bx = allow_tc && batched_supported(m->dev) &&
+		                    batched_step_smem(m->dev, tnrows) <= limit;
+		if (can_bx && (opt == 3 || (opt == 0 && m->A >= 300))) {
+			q->bd.batched = 1;
+			q->state_global = false;
+			q->bd.m_in_smem = 0;
+		}
+		// force of infection on the tensor cores, one particle per CTA: large models (the
+		// matrix is streamed from L2 each step; the particle's populations and counts move to
+		// global memory to make room for the operand ring)
 		const bool can_tc = allow_tc && m->dev.tc_image != nullptr && fast_pick_threads(m->dev) == 640;
-		const bool want_tc = opt == 2 || (opt == 0 && m->A >= 300);
-		if (can_tc && want_tc) {
+		const bool want_tc = opt == 2 || (opt == 0 && m->A >= 300 && !can_bx);
+		if (!q->bd.batched && can_tc && want_tc) {
 			// the transition counts stay on chip when they fit beside the operand ring
 			for (int tn_on_chip = 1; tn_on_chip >= 0 && !q->bd.foi_tc; tn_on_chip--) {
 				const size_t base = fast_smem_bytes(m->dev, nslots, false, q->bd.nefoi_stage, true, tnrows, ps, tn_on_chip != 0);
@@ -717,7 +727,7 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 		const int forced = option_fast_ctas();
 		const int pref = forced != 0 ? 0 : m->tuned_ctas;
 		const bool asked = forced >= 2 || pref >= 2;
-		if (allow_ctas && !q->bd.foi_tc && forced != 1 && pref != 1 && fast_pick_threads(m->dev) == 640) {
+		if (allow_ctas && !q->bd.foi_tc && !q->bd.batched && forced != 1 && pref != 1 && fast_pick_threads(m->dev) == 640) {
 			const int kmax = std::min(forced >= 2 ? forced : 4, fast_ctas_max(m->G));
 			const int kmin = asked ? 2 : 3;
 			auto fit = [&](size_t bytes) { return (int)std::min<size_t>((size_t)kmax, kSmemPerSM / (bytes + 1024)); };
@@ -767,6 +777,12 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 	Layout wk;
 	const size_t PW = b->form == BEEP_FORM_FAST ? 0 : (size_t)P;   // the fast form keeps its state on chip
 	const size_t w_gs = wk.add(q->state_global ? fast_gstate_stride(m->dev) * (size_t)P : 0);
+	const bool bx = q->bd.batched != 0;
+	const size_t w_bxp = wk.add(bx ? (q->bd.pop_single ? 1 : 2) * 4 * popsz * (size_t)P : 0),
+	             w_bxi = wk.add(bx ? 2 * 4 * agsz * (size_t)P : 0), w_bxy = wk.add(bx ? 4 * agsz * (size_t)P : 0),
+	             w_bxs = wk.add(bx ? 4 * (size_t)q->bd.nslots * P : 0),
+	             w_bxk = wk.add(bx ? 8 * (size_t)batched_step_threads() * P : 0),
+	             w_bxw = wk.add(bx ? 4 * (size_t)nsteps : 0);
 	size_t w_pa = wk.add(4 * popsz * PW), w_pb = wk.add(4 * popsz * PW), w_tn = wk.add(traj ? 0 : 4 * tnsz * PW),
 	       w_im = wk.add(8 * agsz * PW), w_id = wk.add(8 * agsz * PW), w_di = wk.add(8 * agsz * PW),
 	       w_nmi = wk.add(8 * agsz * PW), w_acc = wk.add(8 * (size_t)nscored * PW);
@@ -795,6 +811,14 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 	bd.Imap = (double *)(dw + w_im); bd.Idiag = (double *)(dw + w_id); bd.dinf = (double *)(dw + w_di);
 	bd.NMI = (double *)(dw + w_nmi); bd.obs_acc = (double *)(dw + w_acc);
 	bd.gstate = q->state_global ? (void *)(dw + w_gs) : nullptr;
+	if (bx) {
+		bd.bx_pop = (int32_t *)(dw + w_bxp);
+		bd.bx_ic = (float *)(dw + w_bxi);
+		bd.bx_y = (float *)(dw + w_bxy);
+		bd.bx_slot = (float *)(dw + w_bxs);
+		bd.bx_kahan = (float2 *)(dw + w_bxk);
+		bd.bx_work = (int32_t *)(dw + w_bxw);
+	}
 	bd.gstate_stride = q->state_global ? fast_gstate_stride(m->dev) : 0;
 	bd.status = (int32_t *)(dout + q->u_st);
 	bd.L = b->L_out ? (double *)(dout + q->u_L) : nullptr;
@@ -826,9 +850,11 @@ beep_status beep_batch_upload(beep_batch *q)
 beep_status beep_batch_launch(beep_batch *q)
 {
 	if (!q) return fail(BEEP_BAD_INPUT, "null batch");
+	q->bd.sampler_limit = option_sampler_limit();   // batches kept across calls follow the current option
 	CUDA_TRY(cudaMemsetAsync(q->bd.status, 0, 4 * (size_t)q->bd.P, q->m->stream));
-	int le = q->b.form == BEEP_FORM_FAST ? launch_sim_fast(q->m->dev, q->bd, q->m->stream)
-	                                     : launch_sim_plain(q->m->dev, q->bd, q->m->stream);
+	int le = q->b.form != BEEP_FORM_FAST ? launch_sim_plain(q->m->dev, q->bd, q->m->stream)
+	         : q->bd.batched              ? launch_sim_batched(q->m->dev, q->bd, q->m->sms, q->m->stream)
+	                                      : launch_sim_fast(q->m->dev, q->bd, q->m->stream);
 	if (le != 0) return fail(BEEP_DEVICE_ERROR, std::string("kernel launch: ") + cudaGetErrorString((cudaError_t)le));
 	q->pending = true;
 	return BEEP_OK;
@@ -889,7 +915,11 @@ beep_status beep_batch_time(beep_batch *q, int32_t iters, double *ms_per_launch)
 	return BEEP_OK;
 }
 
-int32_t beep_batch_launches(const beep_batch *q) { return q ? 1 : 0; }
+int32_t beep_batch_launches(const beep_batch *q)
+{
+	if (!q) return 0;
+	return q->bd.batched ? batched_launches(q->b.tf - q->b.ti) : 1;
+}
 
 beep_status beep_batch_run_graph(beep_batch *q)
 {
@@ -952,8 +982,9 @@ beep_status beep_autotune(beep_model *m, const beep_sim_batch *b, int32_t *chose
 	double best = 1e300;
 	int best_foi = 1, best_ctas = 1;
 	// candidates (force of infection path, particles per SM): SIMT with one, SIMT with
-	// as many as fit (up to four), tensor cores (one)
-	const int cands[3][2] = {{1, 1}, {1, 4}, {2, 1}};
+	// as many as fit (up to four), tensor cores (one particle per CTA), tensor cores
+	// batched over the particles (step-synchronous)
+	const int cands[4][2] = {{1, 1}, {1, 4}, {2, 1}, {3, 1}};
 	for (const auto &c : cands) {
 		m->tuned_foi = c[0];
 		m->tuned_ctas = c[1];
@@ -961,7 +992,8 @@ beep_status beep_autotune(beep_model *m, const beep_sim_batch *b, int32_t *chose
 		beep_status st = beep_batch_create(m, &t, &q);
 		if (st != BEEP_OK) { m->tuned_foi = saved_foi; m->tuned_ctas = saved_ctas; return st; }
 		const int got = beep_batch_ctas_per_sm(q);
-		if (beep_batch_foi_path(q) != c[0] || (c[1] == 1) != (got == 1)) {   // not available for this model
+		const bool layout_ok = c[0] == 3 ? got == 0 : (c[1] == 1) == (got == 1);
+		if (beep_batch_foi_path(q) != c[0] || !layout_ok) {   // not available for this model
 			beep_batch_destroy(q);
 			continue;
 		}
@@ -985,12 +1017,13 @@ beep_status beep_autotune(beep_model *m, const beep_sim_batch *b, int32_t *chose
 int32_t beep_batch_foi_path(const beep_batch *q)
 {
 	if (!q || q->b.form != BEEP_FORM_FAST) return 0;
-	return q->bd.foi_tc ? 2 : 1;
+	return q->bd.batched ? 3 : q->bd.foi_tc ? 2 : 1;
 }
 
 int32_t beep_batch_ctas_per_sm(const beep_batch *q)
 {
 	if (!q || q->b.form != BEEP_FORM_FAST) return 0;
+	if (q->bd.batched) return 0;                  // particles are not pinned to SMs in the step-synchronous layout
 	return q->bd.nt == kDualThreads ? q->bd.ctas : 1;
 }
 

@@ -48,7 +48,7 @@ __host__ __device__ inline uint32_t kmajor_offset(int r, int k, int R)
 }
 
 // chunking of a model with A areas: nct target chunks of tw targets (a
-// multiple of 8, <= 256), nkc source chunks of kChunkK sources
+// multiple of 16, <= 256), nkc source chunks of kChunkK sources
 struct Geom {
 	int A, NS, nct, tw, nkc;
 	__host__ __device__ int kpad() const { return nkc * kChunkK; }
@@ -75,7 +75,7 @@ __host__ __device__ inline Geom geometry(int A, int NS)
 	g.A = A;
 	g.NS = NS;
 	g.nct = (A + 255) / 256;
-	g.tw = ((A + g.nct - 1) / g.nct + 7) / 8 * 8;
+	g.tw = ((A + g.nct - 1) / g.nct + 15) / 16 * 16;   // a multiple of 16: valid N for M = 64 and M = 128
 	g.nkc = (A + kChunkK - 1) / kChunkK;
 	return g;
 }

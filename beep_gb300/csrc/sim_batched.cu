@@ -1,0 +1,567 @@
+// Fast form, step-synchronous layout: every particle of the batch advances one
+// step at a time, so that the area-mixing contraction of the force of
+// infection (src/state.cc:164-219, 223-290) is one dense product over the
+// whole batch per step, on the tensor cores:
+//
+//   Y[(p,st,a)][t] = sum_c I[(p,st,a)][c] * M[c][t]       [P*NS*G x A] . [A x A]
+//
+// Per step two kernels run on the model's stream:
+//   bx_foi   the product, one CTA per 128 rows (particle, strain, age):
+//            tcgen05.mma kind::f16 with M = 128 rows, N = the target chunks
+//            of the model's matrix image (foi_tc.cuh: three BF16 pieces
+//            Mh + Mm + Ml of M[c][t], K-major, streamed from L2 by bulk
+//            copies), K = sources in chunks of 32.  The counts are split
+//            into two BF16 pieces Ih + Il (exact below 65536) while the CTA
+//            stages them into shared memory, and the five products
+//            Ih.Mh, Ih.Mm, Ih.Ml, Il.Mh, Il.Mm accumulate in FP32 in tensor
+//            memory (the dropped Il.Ml is below 2^-24 of each term).
+//   bx_step  per particle (CTAs take particles from a counter): the strain
+//            shift, NMI, transition means, keyed FP32 draws and population
+//            update per column (c, dp), with the same arithmetic and the same
+//            variate streams as the fast kernel of sim_fast.cuh; the next
+//            step's infectious counts; then the step's observation terms.
+// The particles' populations, infectious counts, contraction, observation
+// slots and compensated log-likelihood partials stay in global memory (L2)
+// between steps; bx_init sets them up and bx_final reduces L in FP64.
+#include <algorithm>
+
+#include "sim_fast.cuh"
+
+namespace beep {
+namespace {
+
+constexpr int kBxRows = 128;          // MMA M: rows (particle, strain, age) per product CTA
+constexpr int kBxThreads = 256;       // threads of a product CTA
+constexpr int kBxK = tc::kChunkK;     // sources per chunk (the matrix image's chunking)
+constexpr int kBxStages = 2;
+constexpr int kBxStepThreads = kDualThreads;
+constexpr int kMaxC = 8;              // compartments held in registers per column
+
+__device__ __forceinline__ uint32_t idesc_m128(int n)
+{
+	return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kBxRows >> 4) << 24);
+}
+
+struct BxGeom {
+	int nct, tw, nkc;
+	uint32_t a_piece, b_bytes, stage;   // bytes: one A piece (128 x 32 BF16), the B chunks of all targets, a stage
+};
+
+__host__ __device__ inline BxGeom bx_geometry(int A, int NS)
+{
+	const tc::Geom g = tc::geometry(A, NS);
+	BxGeom x;
+	x.nct = g.nct;
+	x.tw = g.tw;
+	x.nkc = g.nkc;
+	x.a_piece = (uint32_t)kBxRows * kBxK * 2;
+	x.b_bytes = (uint32_t)g.nct * g.chunk_bytes();
+	x.stage = (2 * x.a_piece + x.b_bytes + 127) & ~127u;
+	return x;
+}
+
+// ---------------------------------------------------------------------------
+// the product Y = I . M for one tile of 128 rows
+
+__global__ void __launch_bounds__(kBxThreads, 1) bx_foi(const ModelDev m, const BatchDev b, int cur)
+{
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	__shared__ uint64_t full[kBxStages], aready[kBxStages], empty[kBxStages], done;
+	__shared__ uint32_t tslot;
+	__shared__ int abort_flag;
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const int A = m.A, G = m.G;
+	const int rows = b.P * m.NS * G;
+	const int r0 = blockIdx.x * kBxRows;
+	const BxGeom x = bx_geometry(A, m.NS);
+	const tc::Geom g = tc::geometry(A, m.NS);
+	const float *Ic = b.bx_ic + (size_t)cur * rows * A;
+	unsigned char *stage0 = smem_raw;
+	uint32_t tcols = 32;
+	while (tcols < (uint32_t)(x.nct * x.tw)) tcols <<= 1;
+	if (warp == 0) tc::tmem_alloc(&tslot, tcols);
+	if (tid == 0) {
+		abort_flag = 0;
+		for (int s = 0; s < kBxStages; s++) {
+			tc::mbar_init(&full[s], 1);
+			tc::mbar_init(&aready[s], kBxThreads);
+			tc::mbar_init(&empty[s], 1);
+		}
+		tc::mbar_init(&done, 1);
+		tc::fence_mbar_init();
+	}
+	tc::tc_before_sync();
+	__syncthreads();
+	tc::tc_after_sync();
+	const uint32_t taddr = tslot;
+	uint32_t pending = 0, pend_par = 0;           // thread 0: stages with a bulk load in flight, and its phase parity
+	// thread 0: the matrix chunks of source chunk kc (every target chunk) into stage s
+	auto load_b = [&](int kc, int s) {
+		unsigned char *dst = stage0 + (size_t)s * x.stage + 2 * x.a_piece;
+		tc::mbar_expect_tx(&full[s], x.b_bytes);
+		for (int ct = 0; ct < x.nct; ct++) {
+			const unsigned char *src = m.tc_image + (size_t)(ct * x.nkc + kc) * g.chunk_bytes();
+			for (int pc = 0; pc < tc::kPieces; pc++)
+				tc::bulk_load(dst + (size_t)ct * g.chunk_bytes() + pc * g.piece_bytes(), src + pc * g.piece_bytes(),
+				              g.piece_bytes(), &full[s]);
+		}
+		pending |= 1u << s;
+		pend_par = (pend_par & ~(1u << s)) | ((uint32_t)((kc / kBxStages) & 1) << s);
+	};
+	const uint32_t id = idesc_m128(x.tw);
+	const uint32_t albo = (uint32_t)kBxRows * 16, blbo = (uint32_t)x.tw * 16;
+	for (int kc = 0; kc < x.nkc; kc++) {
+		const int s = kc % kBxStages;
+		const uint32_t use = (uint32_t)(kc / kBxStages);
+		unsigned char *st = stage0 + (size_t)s * x.stage;
+		if (kc >= kBxStages && !tc::mbar_wait(&empty[s], (use - 1) & 1u)) atomicExch(&abort_flag, 1);
+		if (*(volatile int *)&abort_flag) break;
+		if (tid == 0) load_b(kc, s);
+		// counts of rows r0.. for sources kc*32.. as two BF16 pieces, K-major core-matrix layout
+		for (int idx = tid; idx < kBxRows * kBxK; idx += kBxThreads) {
+			const int rr = idx % kBxRows, kk = idx / kBxRows;
+			const int r = r0 + rr, c = kc * kBxK + kk;
+			float v = 0.f;
+			if (r < rows && c < A) {
+				const int gi = r / G, a = r - gi * G;
+				v = Ic[((size_t)gi * A + c) * G + a];
+			}
+			const __nv_bfloat16 h = __float2bfloat16_rn(v);
+			const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
+			const uint32_t o = tc::kmajor_offset(rr, kk, kBxRows);
+			*(__nv_bfloat16 *)(st + o) = h;
+			*(__nv_bfloat16 *)(st + x.a_piece + o) = l;
+		}
+		tc::fence_async_smem();
+		asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(&aready[s])) : "memory");
+		if (tid == 0) {
+			bool ok = tc::mbar_wait(&aready[s], use & 1u) && tc::mbar_wait(&full[s], use & 1u);
+			if (ok) {
+				pending &= ~(1u << s);
+				tc::tc_after_sync();
+				const uint32_t sa = tc::smem_u32(st);
+#pragma unroll
+				for (int ks = 0; ks < kBxK / 16; ks++) {
+					const uint64_t ah = tc::sdesc(sa + (uint32_t)(ks * 2) * albo, albo, 128);
+					const uint64_t al = tc::sdesc(sa + x.a_piece + (uint32_t)(ks * 2) * albo, albo, 128);
+					for (int ct = 0; ct < x.nct; ct++) {
+						const uint32_t bb = sa + 2 * x.a_piece + (uint32_t)ct * g.chunk_bytes() + (uint32_t)(ks * 2) * blbo;
+						const uint64_t bh = tc::sdesc(bb, blbo, 128);
+						const uint64_t bm = tc::sdesc(bb + g.piece_bytes(), blbo, 128);
+						const uint64_t bl = tc::sdesc(bb + 2 * g.piece_bytes(), blbo, 128);
+						const uint32_t d = taddr + (uint32_t)(ct * x.tw);
+						tc::mma_bf16(d, ah, bh, id, !(kc == 0 && ks == 0));
+						tc::mma_bf16(d, ah, bm, id, true);
+						tc::mma_bf16(d, ah, bl, id, true);
+						tc::mma_bf16(d, al, bh, id, true);
+						tc::mma_bf16(d, al, bm, id, true);
+					}
+				}
+				tc::mma_commit(&empty[s]);
+			} else {
+				atomicExch(&abort_flag, 1);
+			}
+		}
+	}
+	if (tid == 0) {
+		if (!*(volatile int *)&abort_flag) tc::mma_commit(&done);
+		// loads still in flight (only after a timeout) land before the CTA exits
+		for (int s = 0; s < kBxStages; s++)
+			if (pending & (1u << s)) tc::mbar_wait(&full[s], (pend_par >> s) & 1u);
+	}
+	__syncthreads();
+	const bool ok = !*(volatile int *)&abort_flag && tc::mbar_wait(&done, 0);
+	tc::tc_after_sync();
+	if (ok) {
+		// rows of warp quarter q: lanes 32q..32q+31; the two warps of a quarter split the column groups
+		const int q = warp & 3, half = warp >> 2;
+		const int rr = q * 32 + lane, r = r0 + rr;
+		const int gi = r / G, a = r - gi * G;
+		float *Y = b.bx_y + (size_t)gi * A * G + a;
+		const int ngrp = (x.nct * x.tw) / 16;
+		for (int gp = half; gp < ngrp; gp += kBxThreads / 128) {
+			float v[16];
+			tc::tmem_ld16(taddr + ((uint32_t)(q * 32) << 16) + (uint32_t)(gp * 16), v);
+			if (r < rows) {
+#pragma unroll
+				for (int i = 0; i < 16; i++) {
+					const int t = gp * 16 + i;
+					if (t < A) Y[(size_t)t * G] = v[i];
+				}
+			}
+		}
+	} else if (tid == 0) {
+		for (int r = r0; r < r0 + kBxRows && r < rows; r += G) atomicCAS(b.status + r / (G * m.NS), 0, BEEP_TIMEOUT);
+	}
+	tc::tc_before_sync();
+	__syncthreads();
+	if (warp == 0) {
+		tc::tc_after_sync();
+		tc::tmem_dealloc(taddr, tcols);
+	}
+}
+
+// ---------------------------------------------------------------------------
+// per-particle kernels
+
+struct BxTabs {
+	Tabs tb;
+	GroupDir dir;
+};
+
+__device__ __forceinline__ Tabs bx_tabs(const BatchDev &b, int p)
+{
+	const GroupDir dir = b.dirs[b.group_of ? b.group_of[p] : 0];
+	const float *fp = b.fpool32;
+	Tabs tb;
+	tb.rate = fp + dir.transrate; tb.sus = fp + dir.susceptibility; tb.inf = fp + dir.infectivity;
+	tb.beta_rows = fp + dir.beta_rows; tb.areafactor = fp + dir.areafactor; tb.Ntime = fp + dir.Ntime;
+	tb.geo = fp + dir.geo_spline; tb.efoi_spline = fp + dir.efoi_spline; tb.efoi_age = fp + dir.efoi_agedist;
+	tb.obs_spline = fp + dir.obs_spline;
+	tb.beta_row_of = b.ipool + dir.beta_row_of; tb.efoi_ref = b.ipool + dir.efoi_ref;
+	tb.efoi_mult = dir.efoi_mult >= 0 ? fp + dir.efoi_mult : nullptr;
+	tb.tm_mult = dir.tm_mult >= 0 ? fp + dir.tm_mult : nullptr;
+	return tb;
+}
+
+// populations of particle p (buffer k of the pair, or the single buffer), layout [comp][col]
+__device__ __forceinline__ int32_t *bx_pop(const ModelDev &m, const BatchDev &b, int p, int k)
+{
+	const size_t popsz = (size_t)m.C * m.A * m.DP;
+	return b.bx_pop + ((size_t)(b.pop_single ? 0 : k) * b.P + p) * popsz;
+}
+
+// start populations, infectious counts of the first step, cleared slots and partial sums
+__global__ void __launch_bounds__(256) bx_init(const ModelDev m, const BatchDev b)
+{
+	const int p = blockIdx.x, tid = threadIdx.x;
+	const int A = m.A, G = m.G, DP = m.DP, DPS = m.DPS, C = m.C, NS = m.NS, ncol = A * DP, popsz = C * ncol;
+	int32_t *pop = bx_pop(m, b, p, 0);
+	for (int k = tid; k < popsz; k += blockDim.x) {
+		const int dp = k % DP, co = (k / DP) % C, c = k / (DP * C);
+		pop[co * ncol + c * DP + dp] = b.ti == 0 ? m.pop_init[k] : b.pop_in[(size_t)p * popsz + k];
+	}
+	__syncthreads();
+	const Tabs tb = bx_tabs(b, p);
+	float *Ic = b.bx_ic + (size_t)p * NS * A * G;          // buffer 0 holds the counts of step ti
+	for (int idx = tid; idx < NS * A * G; idx += blockDim.x) {
+		const int a = idx % G, c = (idx / G) % A, st = idx / (G * A);
+		float v = 0.f;
+		for (int co = 0; co < C; co++) {
+			const float inf = tb.inf[co];
+			if (inf != 0.f)
+				for (int dp = 0; dp < DPS; dp++)
+					if (m.dp_age[dp] == a) v += inf * (float)pop[co * ncol + c * DP + st * DPS + dp];
+		}
+		Ic[idx] = v;
+	}
+	for (int k = tid; k < b.nslots; k += blockDim.x) b.bx_slot[(size_t)p * b.nslots + k] = 0.f;
+	for (int k = tid; k < kBxStepThreads; k += blockDim.x) b.bx_kahan[(size_t)p * kBxStepThreads + k] = make_float2(0.f, 0.f);
+	if (p == 0)
+		for (int k = tid; k < b.tf - b.ti; k += blockDim.x) b.bx_work[k] = 0;
+}
+
+// one step of every particle (CTAs take particles in turn from the step's counter)
+template <int MG, int MB>
+__global__ void __launch_bounds__(kBxStepThreads, MB) bx_step(const ModelDev m, const BatchDev b, int sett)
+{
+	constexpr int NT = kBxStepThreads;
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	__shared__ int next_p;
+	const int tid = threadIdx.x;
+	const int A = m.A, G = m.G, DP = m.DP, NS = m.NS, DPS = m.DPS, C = m.C, T = m.T;
+	const int ncol = A * DP, popsz = C * ncol, tnsz = T * ncol;
+	const int tnrows = b.tn_full ? T : m.tn_rows;
+	const int nsteps = b.tf - b.ti, s_rel = sett - b.ti;
+	const int cur = s_rel & 1;
+	const int rows_ic = b.P * NS * A * G;
+	// shared memory: the step's counts of the observed transitions, the step's table
+	// slices, the particle's rates and the model's small tables
+	size_t off = 0;
+	auto take = [&](size_t bytes) { unsigned char *q = smem_raw + off; off += (bytes + 15) & ~(size_t)15; return q; };
+	int32_t *tn = (int32_t *)take(4 * (size_t)tnrows * ncol);
+	float *be = (float *)take(4 * (size_t)NS * A);
+	float *et = (float *)take(4 * (size_t)NS * A);
+	float *Nm = (float *)take(4 * (size_t)G * G);
+	float *rate = (float *)take(4 * (size_t)T * DP);
+	float *sus = (float *)take(4 * (size_t)DP);
+	float *inf = (float *)take(4 * (size_t)C);
+	float *rcp = (float *)take(4 * 64);
+	float *lnfact = (float *)take(4 * 32);
+	int32_t *from = (int32_t *)take(4 * (size_t)T);
+	int32_t *to = (int32_t *)take(4 * (size_t)T);
+	int32_t *trow = (int32_t *)take(4 * (size_t)T);
+	int32_t *age = (int32_t *)take(4 * (size_t)DPS);
+	float *Icn = m.dp_age_unique ? nullptr : (float *)take(4 * (size_t)NS * A * G);
+	float *dgeo = (float *)take(16);
+	for (int k = tid; k < T; k += NT) {
+		from[k] = m.trans_from[k];
+		to[k] = m.trans_to[k];
+		trow[k] = b.tn_full ? k : m.tn_row[k];
+	}
+	for (int k = tid; k < DPS; k += NT) age[k] = m.dp_age[k];
+	for (int k = tid; k < 64; k += NT) rcp[k] = k == 0 ? 0.f : 1.f / (float)k;
+	for (int k = tid; k < 32; k += NT) lnfact[k] = c_lnfact[k];
+	const int itr = m.infection_trans;
+	const int inf_from = m.trans_from[itr];
+	const float dt = (float)m.dt;
+	const uint32_t lim = b.sampler_limit ? b.sampler_limit : 65536u;
+	const float *Ic_all = b.bx_ic + (size_t)cur * rows_ic;
+	float *Icn_all = b.bx_ic + (size_t)(cur ^ 1) * rows_ic;
+	for (;;) {
+		__syncthreads();                            // the previous particle is finished with shared memory
+		if (tid == 0) next_p = atomicAdd(b.bx_work + s_rel, 1);
+		__syncthreads();
+		const int p = next_p;
+		if (p >= b.P) break;
+		const Tabs tb = bx_tabs(b, p);
+		const uint32_t stream = b.stream_of ? b.stream_of[p] : (uint32_t)p;
+		int32_t *status = b.status + p;
+		int32_t *pc = bx_pop(m, b, p, cur), *pn = bx_pop(m, b, p, cur ^ 1);
+		const float *Ic = Ic_all + (size_t)p * NS * A * G;
+		const float *Y = b.bx_y + (size_t)p * NS * A * G;
+		float *Icp = Icn_all + (size_t)p * NS * A * G;
+		float *slot = b.bx_slot + (size_t)p * b.nslots;
+		for (int k = tid; k < T * DP; k += NT) rate[k] = tb.rate[k];
+		for (int k = tid; k < DP; k += NT) sus[k] = tb.sus[k];
+		for (int k = tid; k < C; k += NT) inf[k] = tb.inf[k];
+		for (int i = tid; i < NS * A; i += NT) {
+			const int c = i % A;
+			be[i] = __ldg(tb.beta_rows + (size_t)__ldg(tb.beta_row_of + i) * m.S + sett) *
+			        __ldg(tb.areafactor + (size_t)(sett / m.div_per_time) * A + c);
+			float e = __ldg(tb.efoi_spline + (size_t)__ldg(tb.efoi_ref + i) * m.S + sett) * m.inv_popsize_f;
+			if (tb.efoi_mult) e *= __ldg(tb.efoi_mult + ((size_t)sett * A + c) * NS + i / A);
+			et[i] = e;
+		}
+		for (int k = tid; k < G * G; k += NT) Nm[k] = __ldg(tb.Ntime + (size_t)sett * G * G + k);
+		if (tid == 0) dgeo[0] = __ldg(tb.geo + sett);
+		if (Icn)
+			for (int k = tid; k < NS * A * G; k += NT) Icn[k] = 0.f;
+		if (NS > 1) {
+			// strain shift of the susceptible population (src/state.cc:392-401)
+			for (int idx = tid; idx < A * DPS; idx += NT) {
+				const int dp = idx % DPS, c = idx / DPS;
+				int32_t *sp = pc + inf_from * ncol + c * DP;
+				int32_t sum = 0;
+				for (int st = 1; st < NS; st++) { sum += sp[DPS * st + dp]; sp[DPS * st + dp] = 0; }
+				sp[dp] += sum;
+			}
+		}
+		__syncthreads();
+		float2 kah = b.bx_kahan[(size_t)p * NT + tid];
+		float Lsum = kah.x, Lcmp = kah.y;
+		const float d = dgeo[0], omd = 1.f - d;
+		// ---- per column (c, dp): NMI, means, draws, population update, next infectious count
+		for (int col = tid; col < ncol; col += NT) {
+			const int c = col / DP, dp = col - c * DP;
+			const int st = dp / DPS, dpl = dp - st * DPS, a = age[dpl];
+			int32_t pv[kMaxC];
+#pragma unroll
+			for (int co = 0; co < kMaxC; co++) pv[co] = co < C ? pc[co * ncol + col] : 0;
+			if (b.pop_traj)
+#pragma unroll
+				for (int co = 0; co < kMaxC; co++)
+					if (co < C) b.pop_traj[((size_t)p * nsteps + s_rel) * popsz + ((size_t)c * C + co) * DP + dp] = pv[co];
+			U4 inv{0, 0, 0, 0};
+			uint32_t inv_call = 0xffffffffu;
+			float minf = 0.f;
+			{
+				int32_t su = 0;
+#pragma unroll
+				for (int co = 0; co < kMaxC; co++) su = co == inf_from ? pv[co] : su;
+				// the infection transition's source of strain st is read at its strain-0 column
+				const float popu = st == 0 ? (float)su : (float)pc[inf_from * ncol + c * DP + dpl];
+				if (popu > 0.f) {
+					const float fac = m.M_factor_f[c], dg = m.M_diag_f[c];
+					const float *Icc = Ic + (st * A + c) * G, *Yc = Y + (st * A + c) * G;
+					const float *N = Nm + a * G;
+					float nmi = 0.f;
+#pragma unroll
+					for (int aa = 0; aa < MG; aa++) {
+						if (aa < G) {
+							const float id = __ldg(Icc + aa) * dg;
+							nmi = fmaf(N[aa], (id + __ldg(Yc + aa)) * d + fac * id * omd, nmi);
+						}
+					}
+					nmi = fmaxf(nmi, 0.f);
+					const int sc = st * A + c;
+					const float eage = __ldg(tb.efoi_age + (size_t)__ldg(tb.efoi_ref + sc) * G + a);
+					minf = dt * popu * sus[dp] * (be[sc] * nmi + et[sc] * eage);
+				}
+			}
+			float mv[kMaxT];
+#pragma unroll
+			for (int tr = 0; tr < kMaxT; tr++) {
+				mv[tr] = 0.f;
+				if (tr < T) {
+					if (tr == itr) mv[tr] = minf;
+					else {
+						int32_t pf = 0;
+#pragma unroll
+						for (int co = 0; co < kMaxC; co++) pf = co == from[tr] ? pv[co] : pf;
+						const float popu = (float)pf;
+						mv[tr] = popu <= 0.f ? 0.f : dt * popu * rate[tr * DP + dp];
+					}
+					if (tb.tm_mult) mv[tr] *= __ldg(tb.tm_mult + ((size_t)sett * A + c) * T * DP + tr * DP + dp);
+				}
+			}
+			for (int tr = 0; tr < T; tr++) {
+				float mean = mv[0];
+#pragma unroll
+				for (int k = 1; k < kMaxT; k++) mean = tr == k ? mv[k] : mean;
+				int32_t n = 0;
+				if (mean > 0.f) {
+					if (mean > 1.0e9f) atomicCAS(status, 0, BEEP_COUNT_OVERFLOW);
+					else {
+						n = poisson_fp32(mean, b.k0, b.k1, (uint32_t)col, (uint32_t)tr, (uint32_t)sett, stream, inv, inv_call,
+						                 rcp, lnfact, lim);
+						if (n < 0) { atomicCAS(status, 0, BEEP_TIMEOUT); n = 0; }
+					}
+				} else if (mean != mean) atomicCAS(status, 0, BEEP_NAN_RATE);
+				const int row = trow[tr];
+				if (row >= 0) tn[row * ncol + col] = n;
+				if (b.tn_traj) b.tn_traj[((size_t)p * nsteps + s_rel) * tnsz + ((size_t)c * T + tr) * DP + dp] = n;
+				if (n != 0) {
+					const int f = from[tr], t2 = to[tr];
+#pragma unroll
+					for (int co = 0; co < kMaxC; co++) {
+						if (co == f) pv[co] -= n;
+						if (co == t2) pv[co] += n;
+					}
+				}
+			}
+			float iv = 0.f;
+#pragma unroll
+			for (int co = 0; co < kMaxC; co++) {
+				if (co < C) {
+					pn[co * ncol + col] = pv[co];
+					if (inf[co] != 0.f) iv = fmaf(inf[co], (float)pv[co], iv);
+				}
+			}
+			if (Icn) atomicAdd(Icn + (st * A + c) * G + a, iv);
+			else Icp[(st * A + c) * G + a] = iv;
+		}
+		__syncthreads();
+		// ---- observation sums of the step (completed ones -> log-density)
+		const int a0 = b.step_ptr[s_rel], a1 = b.step_ptr[s_rel + 1];
+		for (int k = a0 + tid; k < a1; k += NT) {
+			const int4 t0 = __ldg(b.tasks + 2 * k), t1 = __ldg(b.tasks + 2 * k + 1);
+			const float fac = __int_as_float(t1.x);
+			const int spl = t1.y;
+			const float w = spl < 0 ? fac : fac * tb.obs_spline[(size_t)spl * m.S + sett];
+			const int nc = t0.w & 0x7fffffff;
+			float v = slot[t0.x];
+			if (nc > 0) {
+				const int cell = t0.z;
+				v = fmaf(w, cell >= 0 ? (float)tn[cell] : (float)pc[-1 - cell], v);
+			}
+			for (int i = 1; i < nc; i++) {
+				const int cell = __ldg((b.tn_full ? m.obs_cells_full : m.obs_cells_f) + t1.z + i);
+				v = fmaf(w, cell >= 0 ? (float)tn[cell] : (float)pc[-1 - cell], v);
+			}
+			if (t0.w < 0) {                  // the observation's last step: log-density
+				const float lp = obs_lp_fast(v, t0.y, m);
+				v = 0.f;
+				const float y = lp - Lcmp;      // Kahan
+				const float tt = Lsum + y;
+				Lcmp = (tt - Lsum) - y;
+				Lsum = tt;
+			}
+			slot[t0.x] = v;
+		}
+		if (Lsum != kah.x || Lcmp != kah.y) b.bx_kahan[(size_t)p * NT + tid] = make_float2(Lsum, Lcmp);
+		if (Icn) {
+			__syncthreads();
+			for (int k = tid; k < NS * A * G; k += NT) Icp[k] = Icn[k];
+		}
+	}
+}
+
+// L per particle (FP64 reduction of the threads' compensated partial sums) and final populations
+__global__ void __launch_bounds__(256) bx_final(const ModelDev m, const BatchDev b)
+{
+	__shared__ double red[8];
+	const int p = blockIdx.x, tid = threadIdx.x;
+	const int A = m.A, DP = m.DP, C = m.C, ncol = A * DP, popsz = C * ncol;
+	if (b.L) {
+		double S = 0.0;
+		for (int k = tid; k < kBxStepThreads; k += blockDim.x) {
+			const float2 v = b.bx_kahan[(size_t)p * kBxStepThreads + k];
+			S += (double)v.x - (double)v.y;
+		}
+		for (int o = 16; o > 0; o >>= 1) S += __shfl_xor_sync(0xffffffffu, S, o);
+		if ((tid & 31) == 0) red[tid >> 5] = S;
+		__syncthreads();
+		if (tid == 0) {
+			double t = 0.0;
+			for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+			if (t != t) atomicCAS(b.status + p, 0, BEEP_NAN_RATE);
+			b.L[p] = t;
+		}
+	}
+	if (b.pop_out) {
+		const int32_t *pf = bx_pop(m, b, p, (b.tf - b.ti) & 1);
+		for (int k = tid; k < popsz; k += blockDim.x) {
+			const int dp = k % DP, co = (k / DP) % C, c = k / (DP * C);
+			b.pop_out[(size_t)p * popsz + k] = pf[co * ncol + c * DP + dp];
+		}
+	}
+}
+
+template <int MG, int MB>
+int launch_steps(const ModelDev &m, const BatchDev &b, size_t smem_step, int sms, cudaStream_t st)
+{
+	auto kstep = bx_step<MG, MB>;
+	cudaError_t e = cudaFuncSetAttribute(kstep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_step);
+	if (e != cudaSuccess) return (int)e;
+	const BxGeom x = bx_geometry(m.A, m.NS);
+	const size_t smem_foi = (size_t)kBxStages * x.stage;
+	e = cudaFuncSetAttribute(bx_foi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_foi);
+	if (e != cudaSuccess) return (int)e;
+	const int rows = b.P * m.NS * m.G;
+	const int ntile = (rows + kBxRows - 1) / kBxRows;
+	const int grid = std::min(b.P, sms * MB);
+	bx_init<<<b.P, 256, 0, st>>>(m, b);
+	for (int s = b.ti; s < b.tf; s++) {
+		bx_foi<<<ntile, kBxThreads, smem_foi, st>>>(m, b, (s - b.ti) & 1);
+		kstep<<<grid, kBxStepThreads, smem_step, st>>>(m, b, s);
+	}
+	bx_final<<<b.P, 256, 0, st>>>(m, b);
+	return (int)cudaGetLastError();
+}
+
+}  // namespace
+
+bool batched_supported(const ModelDev &m)
+{
+	return m.tc_image != nullptr && tc::supported(m.A, m.NS) && m.C <= kMaxC && m.T <= kMaxT && m.G <= 16 &&
+	       (size_t)kBxStages * bx_geometry(m.A, m.NS).stage <= 227 * 1024;
+}
+
+size_t batched_step_smem(const ModelDev &m, int tnrows)
+{
+	auto r = [](size_t x) { return (x + 15) & ~(size_t)15; };
+	const size_t A = m.A, G = m.G, DP = m.DP, NS = m.NS, C = m.C, T = m.T, DPS = m.DPS;
+	return r(4 * (size_t)tnrows * A * DP) + 2 * r(4 * NS * A) + r(4 * G * G) + r(4 * T * DP) + r(4 * DP) + r(4 * C) +
+	       r(4 * 64) + r(4 * 32) + 3 * r(4 * T) + r(4 * DPS) + (m.dp_age_unique ? 0 : r(4 * NS * A * G)) + 16;
+}
+
+int batched_step_threads() { return kBxStepThreads; }
+
+int batched_prepare() { return prepare_constants(); }
+
+int batched_launches(int nsteps) { return 2 * nsteps + 2; }
+
+int launch_sim_batched(const ModelDev &m, const BatchDev &b, int sms, void *stream)
+{
+	if (b.P == 0) return 0;
+	if (!batched_supported(m) || !b.bx_pop || b.mode != 0) return (int)cudaErrorInvalidValue;
+	const int e0 = prepare_constants();
+	if (e0 != 0) return e0;
+	const size_t smem = batched_step_smem(m, b.tn_full ? m.T : m.tn_rows);
+	cudaStream_t st = (cudaStream_t)stream;
+	return m.G <= 4 ? launch_steps<4, 4>(m, b, smem, sms, st) : m.G <= 8 ? launch_steps<8, 4>(m, b, smem, sms, st)
+	     : m.G <= 12 ? launch_steps<12, 3>(m, b, smem, sms, st) : launch_steps<16, 3>(m, b, smem, sms, st);
+}
+
+}  // namespace beep

@@ -30,6 +30,7 @@ int fast_prepare()
 {
 	int e = prepare_constants();
 	if (e == 0) e = fast_chain_prepare();
+	if (e == 0) e = batched_prepare();
 	return e != 0 ? e : fast_ctas_prepare();
 }
 

@@ -32,7 +32,7 @@ def built():
 def test_count_overflow_is_reported(built, form):
     b, m, tabs, seed = load("c0_sim")
     dm = capi.DeviceModel(m)
-    big = capi.Tables({k: (v * 1e9 if k == "g0.beta_rows" else v) for k, v in b.items()}, "g0.")
+    big = capi.Tables({k: (v * 1e15 if k == "g0.beta_rows" else v) for k, v in b.items()}, "g0.")
     with pytest.raises(capi.BeepError) as e:
         dm.simulate(capi.Batch(m, [big], 4, seed, form=form))
     assert e.value.status == 7, e.value
@@ -62,14 +62,16 @@ def test_mbp_thinning_iteration_limit_is_reported(built):
     """The coupled MBP proposal's binomial thinning (BTRS) under the same limit."""
     b, m, tabs, seed = load("c0_mbp")
     dm = capi.DeviceModel(m)
-    ch = capi.MbpChains(dm, 4)
-    ch.initialise(tabs[:1], seed, group_of=np.zeros(4, np.int32))
-    # a proposal whose means are well below the current ones: every coupled cell thins
-    low = capi.Tables({k: (v * 0.5 if k == "g0.beta_rows" else v) for k, v in b.items()}, "g0.")
+    ch = capi.MbpChains(dm, 16)
+    ch.initialise(tabs[:1], seed, group_of=np.zeros(16, np.int32))
+    # a proposal whose infection means are a little below the current ones: the coupled
+    # infection counts are thinned with p near 0.9 (q = 0.1), by BTRS wherever n q >= 10
+    # (a steeper cut would let the proposal fall behind, p drop and inversion take over)
+    low = capi.Tables({k: (v * 0.9 if k == "g0.beta_rows" else v) for k, v in b.items()}, "g0.")
     capi.set_option("sampler_iteration_limit", 1)
     try:
         with pytest.raises(capi.BeepError) as e:
-            ch.propose([low], seed + 1, group_of=np.zeros(4, np.int32))
+            ch.propose([low], seed + 1, group_of=np.zeros(16, np.int32))
         assert e.value.status == 4, e.value
     finally:
         capi.set_option("sampler_iteration_limit", 0)

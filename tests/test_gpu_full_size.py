@@ -5,8 +5,10 @@ fixtures:
 * the plain FP64 form against the oracle, bit for bit: transition counts and
   populations identical, log-likelihood within 1e-12 relative
   (src/state.cc:596-638, src/obsmodel.cc:22-58);
-* the fast form (FP32 SIMT force of infection and tensor-core force of
-  infection, each forced) against the plain FP64 form as distributions, on
+* the fast form (FP32 SIMT force of infection, tensor-core force of infection
+  per particle, and tensor cores batched over the particles in the
+  step-synchronous layout, each forced) against the plain FP64 form as
+  distributions, on
   independent variate streams: two-sample Kolmogorov-Smirnov and
   Anderson-Darling tests on the final epidemic size, the day of peak
   incidence and the log-likelihood, and every area's attack rate within
@@ -120,7 +122,7 @@ def plain_samples(built):
 
 
 @pytest.mark.parametrize("kind", ["abc_smc", "precision"])
-@pytest.mark.parametrize("foi", [capi.FOI_SIMT, capi.FOI_TENSOR])
+@pytest.mark.parametrize("foi", [capi.FOI_SIMT, capi.FOI_TENSOR, capi.FOI_BATCHED])
 def test_fast_form_distribution_at_full_size(plain_samples, kind, foi):
     w, m, t_true = workload(kind)
     capi.set_option("fast_foi", foi)
