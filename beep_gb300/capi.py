@@ -260,6 +260,8 @@ def lib():
                   "beep_batch_destroy"):
             getattr(L, f).argtypes = [C.c_void_p]
         L.beep_batch_time.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]
+        L.beep_batch_time_split.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.beep_batch_time_split.restype = C.c_int32
         L.beep_batch_run_graph.argtypes = [C.c_void_p]
         L.beep_batch_run_graph.restype = C.c_int32
         L.beep_autotune.argtypes = [C.c_void_p, C.POINTER(SimBatch), C.POINTER(C.c_int32)]
@@ -467,6 +469,12 @@ class DeviceBatch:
         ms = C.c_double()
         check(lib().beep_batch_time(self.h, iters, C.byref(ms)))
         return ms.value
+
+    def time_split(self, iters: int):
+        """(ms per launch, of which ms in the per-step tensor-core products) -- step-synchronous layout."""
+        ms, prod = C.c_double(), C.c_double()
+        check(lib().beep_batch_time_split(self.h, iters, C.byref(ms), C.byref(prod)))
+        return ms.value, prod.value
 
     def bytes(self):
         a, b = C.c_int64(), C.c_int64()

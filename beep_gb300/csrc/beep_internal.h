@@ -114,7 +114,8 @@ struct BatchDev {
 	float *bx_ic;                       // [2][P][NS][A][G] infectious counts of the step / the next step
 	float *bx_y;                        // [P][NS][A][G] area-mixing contraction of the step's counts
 	float *bx_slot;                     // [P][nslots] observation accumulators
-	float2 *bx_kahan;                   // [P][step threads] compensated log-likelihood partial sums
+	float2 *bx_kahan;                   // [P][observation threads] compensated log-likelihood partial sums
+	int32_t *bx_tn;                     // [P][observed transitions][A*DP] counts of the step
 	int32_t *bx_work;                   // [tf-ti] particle counters of the step kernels
 	int32_t ctas;                       // fast form, nt == kDualThreads: CTAs resident per SM (2..4)
 };
@@ -146,9 +147,10 @@ int launch_sim_fast_chain_ctas(const ModelDev &m, const BatchDev &b, size_t smem
 // step-synchronous fast form (sim_batched.cu)
 bool batched_supported(const ModelDev &m);
 size_t batched_step_smem(const ModelDev &m, int tnrows);
-int batched_step_threads();
+int batched_obs_threads();
 int batched_prepare();                           // constant tables of sim_batched.cu
 int batched_launches(int nsteps);                // kernel launches of one batch run
-int launch_sim_batched(const ModelDev &m, const BatchDev &b, int sms, void *stream);
+// events: null, or 2 * (tf - ti) cudaEvent_t recorded around each step's product kernel
+int launch_sim_batched(const ModelDev &m, const BatchDev &b, int sms, void *stream, void *events = nullptr);
 
 }  // namespace beep

@@ -781,7 +781,8 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 	const size_t w_bxp = wk.add(bx ? (q->bd.pop_single ? 1 : 2) * 4 * popsz * (size_t)P : 0),
 	             w_bxi = wk.add(bx ? 2 * 4 * agsz * (size_t)P : 0), w_bxy = wk.add(bx ? 4 * agsz * (size_t)P : 0),
 	             w_bxs = wk.add(bx ? 4 * (size_t)q->bd.nslots * P : 0),
-	             w_bxk = wk.add(bx ? 8 * (size_t)batched_step_threads() * P : 0),
+	             w_bxk = wk.add(bx ? 8 * (size_t)batched_obs_threads() * P : 0),
+	             w_bxt = wk.add(bx ? 4 * (size_t)(q->bd.tn_full ? m->T : m->dev.tn_rows) * m->A * m->DP * P : 0),
 	             w_bxw = wk.add(bx ? 4 * (size_t)nsteps : 0);
 	size_t w_pa = wk.add(4 * popsz * PW), w_pb = wk.add(4 * popsz * PW), w_tn = wk.add(traj ? 0 : 4 * tnsz * PW),
 	       w_im = wk.add(8 * agsz * PW), w_id = wk.add(8 * agsz * PW), w_di = wk.add(8 * agsz * PW),
@@ -817,6 +818,7 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 		bd.bx_y = (float *)(dw + w_bxy);
 		bd.bx_slot = (float *)(dw + w_bxs);
 		bd.bx_kahan = (float2 *)(dw + w_bxk);
+		bd.bx_tn = (int32_t *)(dw + w_bxt);
 		bd.bx_work = (int32_t *)(dw + w_bxw);
 	}
 	bd.gstate_stride = q->state_global ? fast_gstate_stride(m->dev) : 0;
@@ -912,6 +914,44 @@ beep_status beep_batch_time(beep_batch *q, int32_t iters, double *ms_per_launch)
 	float ms = 0;
 	CUDA_TRY(cudaEventElapsedTime(&ms, q->ev0, q->ev1));
 	*ms_per_launch = (double)ms / iters;
+	return BEEP_OK;
+}
+
+beep_status beep_batch_time_split(beep_batch *q, int32_t iters, double *ms_per_launch, double *ms_product)
+{
+	if (!q || iters <= 0 || !ms_per_launch || !ms_product) return fail(BEEP_BAD_INPUT, "bad argument");
+	if (!q->bd.batched) {
+		*ms_product = 0.0;
+		return beep_batch_time(q, iters, ms_per_launch);
+	}
+	cudaStream_t s = q->m->stream;
+	const int nsteps = q->b.tf - q->b.ti;
+	if (q->ev_split.size() != (size_t)(2 * nsteps)) {
+		for (cudaEvent_t e : q->ev_split) cudaEventDestroy(e);
+		q->ev_split.assign(2 * (size_t)nsteps, nullptr);
+		for (auto &e : q->ev_split) CUDA_TRY(cudaEventCreate(&e));
+	}
+	double tot = 0.0, prod = 0.0;
+	for (int k = 0; k < iters; k++) {
+		CUDA_TRY(cudaStreamSynchronize(s));
+		q->bd.sampler_limit = option_sampler_limit();
+		CUDA_TRY(cudaMemsetAsync(q->bd.status, 0, 4 * (size_t)q->bd.P, s));
+		CUDA_TRY(cudaEventRecord(q->ev0, s));
+		const int le = launch_sim_batched(q->m->dev, q->bd, q->m->sms, s, q->ev_split.data());
+		if (le != 0) return fail(BEEP_DEVICE_ERROR, std::string("kernel launch: ") + cudaGetErrorString((cudaError_t)le));
+		CUDA_TRY(cudaEventRecord(q->ev1, s));
+		CUDA_TRY(cudaEventSynchronize(q->ev1));
+		float ms = 0;
+		CUDA_TRY(cudaEventElapsedTime(&ms, q->ev0, q->ev1));
+		tot += ms;
+		for (int j = 0; j < nsteps; j++) {
+			CUDA_TRY(cudaEventElapsedTime(&ms, q->ev_split[2 * j], q->ev_split[2 * j + 1]));
+			prod += ms;
+		}
+	}
+	q->pending = true;
+	*ms_per_launch = tot / iters;
+	*ms_product = prod / iters;
 	return BEEP_OK;
 }
 
@@ -1046,6 +1086,7 @@ beep_status beep_batch_destroy(beep_batch *q)
 	q->out_dev.release();
 	if (q->ev0) cudaEventDestroy(q->ev0);
 	if (q->ev1) cudaEventDestroy(q->ev1);
+	for (cudaEvent_t e : q->ev_split) cudaEventDestroy(e);
 	if (q->graph_exec) cudaGraphExecDestroy(q->graph_exec);
 	if (q->graph) cudaGraphDestroy(q->graph);
 	delete q;

@@ -134,6 +134,7 @@ struct beep_batch {
 	cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 	bool pending = false;
 	bool state_global = false;   // fast form keeps particle state in global memory
+	std::vector<cudaEvent_t> ev_split;   // beep_batch_time_split: around each step's product kernel
 	// CUDA graph of upload + status reset + kernel + download (beep_batch_run_graph)
 	cudaGraph_t graph = nullptr;
 	cudaGraphExec_t graph_exec = nullptr;

@@ -34,7 +34,11 @@ constexpr int kBxRows = 128;          // MMA M: rows (particle, strain, age) per
 constexpr int kBxThreads = 256;       // threads of a product CTA
 constexpr int kBxK = tc::kChunkK;     // sources per chunk (the matrix image's chunking)
 constexpr int kBxStages = 2;
-constexpr int kBxStepThreads = kDualThreads;
+constexpr int kBxUnits = kBxRows * kBxK / 8 / kBxThreads;   // 16-byte units of a chunk's A pieces per thread
+static_assert(kBxUnits * kBxThreads * 8 == kBxRows * kBxK && kBxThreads == 2 * kBxRows, "A-operand staging split");
+constexpr int kBxStepThreads = 256;   // threads of a step CTA
+constexpr int kBxChunk = 512;         // columns per work item of the step kernel (two passes)
+constexpr int kBxObsThreads = 128;    // threads of an observation CTA (one particle)
 constexpr int kMaxC = 8;              // compartments held in registers per column
 
 __device__ __forceinline__ uint32_t idesc_m128(int n)
@@ -108,6 +112,11 @@ __global__ void __launch_bounds__(kBxThreads, 1) bx_foi(const ModelDev m, const 
 		pending |= 1u << s;
 		pend_par = (pend_par & ~(1u << s)) | ((uint32_t)((kc / kBxStages) & 1) << s);
 	};
+	// this thread's row of the tile (the same for every chunk) and its counts' base
+	const int rr = tid & (kBxRows - 1);
+	const bool my_row = r0 + rr < rows;
+	const int my_gi = (r0 + rr) / G, my_a = (r0 + rr) - my_gi * G;
+	const float *my_src = Ic + ((size_t)my_gi * A) * G + my_a;
 	const uint32_t id = idesc_m128(x.tw);
 	const uint32_t albo = (uint32_t)kBxRows * 16, blbo = (uint32_t)x.tw * 16;
 	for (int kc = 0; kc < x.nkc; kc++) {
@@ -117,20 +126,28 @@ __global__ void __launch_bounds__(kBxThreads, 1) bx_foi(const ModelDev m, const 
 		if (kc >= kBxStages && !tc::mbar_wait(&empty[s], (use - 1) & 1u)) atomicExch(&abort_flag, 1);
 		if (*(volatile int *)&abort_flag) break;
 		if (tid == 0) load_b(kc, s);
-		// counts of rows r0.. for sources kc*32.. as two BF16 pieces, K-major core-matrix layout
-		for (int idx = tid; idx < kBxRows * kBxK; idx += kBxThreads) {
-			const int rr = idx % kBxRows, kk = idx / kBxRows;
-			const int r = r0 + rr, c = kc * kBxK + kk;
-			float v = 0.f;
-			if (r < rows && c < A) {
-				const int gi = r / G, a = r - gi * G;
-				v = Ic[((size_t)gi * A + c) * G + a];
+		// counts of rows r0.. for sources kc*32.. as two BF16 pieces, K-major core-matrix layout:
+		// each thread takes one row and 8 consecutive sources per unit (one 16-byte row of a
+		// core matrix per piece), its loads all in flight before the conversion
+#pragma unroll
+		for (int u = 0; u < kBxUnits; u++) {
+			const int kg = (tid >> 7) + 2 * u;            // sources kg*8 .. kg*8+7 of the chunk
+			const int c0 = kc * kBxK + kg * 8;
+			float v[8];
+#pragma unroll
+			for (int i = 0; i < 8; i++) v[i] = (my_row && c0 + i < A) ? __ldg(my_src + (size_t)(c0 + i) * G) : 0.f;
+			uint32_t hw[4], lw[4];
+#pragma unroll
+			for (int i = 0; i < 4; i++) {
+				const __nv_bfloat16 h0 = __float2bfloat16_rn(v[2 * i]), h1 = __float2bfloat16_rn(v[2 * i + 1]);
+				const __nv_bfloat16 l0 = __float2bfloat16_rn(v[2 * i] - __bfloat162float(h0));
+				const __nv_bfloat16 l1 = __float2bfloat16_rn(v[2 * i + 1] - __bfloat162float(h1));
+				hw[i] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+				lw[i] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
 			}
-			const __nv_bfloat16 h = __float2bfloat16_rn(v);
-			const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
-			const uint32_t o = tc::kmajor_offset(rr, kk, kBxRows);
-			*(__nv_bfloat16 *)(st + o) = h;
-			*(__nv_bfloat16 *)(st + x.a_piece + o) = l;
+			const uint32_t o = tc::kmajor_offset(rr, kg * 8, kBxRows);
+			*(uint4 *)(st + o) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+			*(uint4 *)(st + x.a_piece + o) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
 		}
 		tc::fence_async_smem();
 		asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(&aready[s])) : "memory");
@@ -175,7 +192,7 @@ __global__ void __launch_bounds__(kBxThreads, 1) bx_foi(const ModelDev m, const 
 	if (ok) {
 		// rows of warp quarter q: lanes 32q..32q+31; the two warps of a quarter split the column groups
 		const int q = warp & 3, half = warp >> 2;
-		const int rr = q * 32 + lane, r = r0 + rr;
+		const int r = r0 + q * 32 + lane;
 		const int gi = r / G, a = r - gi * G;
 		float *Y = b.bx_y + (size_t)gi * A * G + a;
 		const int ngrp = (x.nct * x.tw) / 16;
@@ -204,11 +221,6 @@ __global__ void __launch_bounds__(kBxThreads, 1) bx_foi(const ModelDev m, const 
 // ---------------------------------------------------------------------------
 // per-particle kernels
 
-struct BxTabs {
-	Tabs tb;
-	GroupDir dir;
-};
-
 __device__ __forceinline__ Tabs bx_tabs(const BatchDev &b, int p)
 {
 	const GroupDir dir = b.dirs[b.group_of ? b.group_of[p] : 0];
@@ -231,7 +243,23 @@ __device__ __forceinline__ int32_t *bx_pop(const ModelDev &m, const BatchDev &b,
 	return b.bx_pop + ((size_t)(b.pop_single ? 0 : k) * b.P + p) * popsz;
 }
 
-// start populations, infectious counts of the first step, cleared slots and partial sums
+// strain shift of the susceptible population before a step (src/state.cc:392-401): the
+// susceptibles of strains 1.. join strain 0's, whose pool every strain's infection draws on
+__device__ __forceinline__ void strain_shift(const ModelDev &m, int32_t *pop, int tid, int nt)
+{
+	const int A = m.A, DP = m.DP, DPS = m.DPS, NS = m.NS, ncol = A * DP;
+	const int inf_from = m.trans_from[m.infection_trans];
+	for (int idx = tid; idx < A * DPS; idx += nt) {
+		const int dp = idx % DPS, c = idx / DPS;
+		int32_t *sp = pop + inf_from * ncol + c * DP;
+		int32_t sum = 0;
+		for (int st = 1; st < NS; st++) { sum += sp[DPS * st + dp]; sp[DPS * st + dp] = 0; }
+		sp[dp] += sum;
+	}
+}
+
+// start populations (and the first step's strain shift), infectious counts of the first
+// step, cleared slots and partial sums, the steps' work counters
 __global__ void __launch_bounds__(256) bx_init(const ModelDev m, const BatchDev b)
 {
 	const int p = blockIdx.x, tid = threadIdx.x;
@@ -242,6 +270,10 @@ __global__ void __launch_bounds__(256) bx_init(const ModelDev m, const BatchDev 
 		pop[co * ncol + c * DP + dp] = b.ti == 0 ? m.pop_init[k] : b.pop_in[(size_t)p * popsz + k];
 	}
 	__syncthreads();
+	if (NS > 1) {
+		strain_shift(m, pop, tid, blockDim.x);
+		__syncthreads();
+	}
 	const Tabs tb = bx_tabs(b, p);
 	float *Ic = b.bx_ic + (size_t)p * NS * A * G;          // buffer 0 holds the counts of step ti
 	for (int idx = tid; idx < NS * A * G; idx += blockDim.x) {
@@ -254,20 +286,24 @@ __global__ void __launch_bounds__(256) bx_init(const ModelDev m, const BatchDev 
 					if (m.dp_age[dp] == a) v += inf * (float)pop[co * ncol + c * DP + st * DPS + dp];
 		}
 		Ic[idx] = v;
+		if (!m.dp_age_unique) Ic[(size_t)b.P * NS * A * G + idx] = 0.f;   // the first step's accumulation target
 	}
 	for (int k = tid; k < b.nslots; k += blockDim.x) b.bx_slot[(size_t)p * b.nslots + k] = 0.f;
-	for (int k = tid; k < kBxStepThreads; k += blockDim.x) b.bx_kahan[(size_t)p * kBxStepThreads + k] = make_float2(0.f, 0.f);
+	for (int k = tid; k < kBxObsThreads; k += blockDim.x) b.bx_kahan[(size_t)p * kBxObsThreads + k] = make_float2(0.f, 0.f);
 	if (p == 0)
 		for (int k = tid; k < b.tf - b.ti; k += blockDim.x) b.bx_work[k] = 0;
 }
 
-// one step of every particle (CTAs take particles in turn from the step's counter)
+// One step of every particle: CTAs take work items (particle p, column chunk k) from
+// the step's counter.  Per column (c, dp): NMI, the transition means, the keyed draws
+// and the population update, then the column's infectious count for the next step;
+// the counts of observed transitions go to the step's count buffer.
 template <int MG, int MB>
 __global__ void __launch_bounds__(kBxStepThreads, MB) bx_step(const ModelDev m, const BatchDev b, int sett)
 {
 	constexpr int NT = kBxStepThreads;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
-	__shared__ int next_p;
+	__shared__ int next_item, cur_group;
 	const int tid = threadIdx.x;
 	const int A = m.A, G = m.G, DP = m.DP, NS = m.NS, DPS = m.DPS, C = m.C, T = m.T;
 	const int ncol = A * DP, popsz = C * ncol, tnsz = T * ncol;
@@ -275,11 +311,11 @@ __global__ void __launch_bounds__(kBxStepThreads, MB) bx_step(const ModelDev m, 
 	const int nsteps = b.tf - b.ti, s_rel = sett - b.ti;
 	const int cur = s_rel & 1;
 	const int rows_ic = b.P * NS * A * G;
-	// shared memory: the step's counts of the observed transitions, the step's table
-	// slices, the particle's rates and the model's small tables
+	const int nchunk = (ncol + kBxChunk - 1) / kBxChunk, nitem = b.P * nchunk;
+	// shared memory: the step's table slices of the current parameter set, its rates and
+	// the model's small tables
 	size_t off = 0;
 	auto take = [&](size_t bytes) { unsigned char *q = smem_raw + off; off += (bytes + 15) & ~(size_t)15; return q; };
-	int32_t *tn = (int32_t *)take(4 * (size_t)tnrows * ncol);
 	float *be = (float *)take(4 * (size_t)NS * A);
 	float *et = (float *)take(4 * (size_t)NS * A);
 	float *Nm = (float *)take(4 * (size_t)G * G);
@@ -292,7 +328,6 @@ __global__ void __launch_bounds__(kBxStepThreads, MB) bx_step(const ModelDev m, 
 	int32_t *to = (int32_t *)take(4 * (size_t)T);
 	int32_t *trow = (int32_t *)take(4 * (size_t)T);
 	int32_t *age = (int32_t *)take(4 * (size_t)DPS);
-	float *Icn = m.dp_age_unique ? nullptr : (float *)take(4 * (size_t)NS * A * G);
 	float *dgeo = (float *)take(16);
 	for (int k = tid; k < T; k += NT) {
 		from[k] = m.trans_from[k];
@@ -302,6 +337,7 @@ __global__ void __launch_bounds__(kBxStepThreads, MB) bx_step(const ModelDev m, 
 	for (int k = tid; k < DPS; k += NT) age[k] = m.dp_age[k];
 	for (int k = tid; k < 64; k += NT) rcp[k] = k == 0 ? 0.f : 1.f / (float)k;
 	for (int k = tid; k < 32; k += NT) lnfact[k] = c_lnfact[k];
+	if (tid == 0) cur_group = -1;
 	const int itr = m.infection_trans;
 	const int inf_from = m.trans_from[itr];
 	const float dt = (float)m.dt;
@@ -309,50 +345,45 @@ __global__ void __launch_bounds__(kBxStepThreads, MB) bx_step(const ModelDev m, 
 	const float *Ic_all = b.bx_ic + (size_t)cur * rows_ic;
 	float *Icn_all = b.bx_ic + (size_t)(cur ^ 1) * rows_ic;
 	for (;;) {
-		__syncthreads();                            // the previous particle is finished with shared memory
-		if (tid == 0) next_p = atomicAdd(b.bx_work + s_rel, 1);
+		__syncthreads();                            // the previous item is finished with shared memory
+		if (tid == 0) next_item = atomicAdd(b.bx_work + s_rel, 1);
 		__syncthreads();
-		const int p = next_p;
-		if (p >= b.P) break;
+		const int item = next_item;
+		if (item >= nitem) break;
+		const int p = item / nchunk, k = item - p * nchunk;
+		const int grp = b.group_of ? b.group_of[p] : 0;
 		const Tabs tb = bx_tabs(b, p);
+		if (grp != cur_group) {                     // the parameter set's rates and slices (kept while it repeats)
+			for (int j = tid; j < T * DP; j += NT) rate[j] = tb.rate[j];
+			for (int j = tid; j < DP; j += NT) sus[j] = tb.sus[j];
+			for (int j = tid; j < C; j += NT) inf[j] = tb.inf[j];
+			for (int i = tid; i < NS * A; i += NT) {
+				const int c = i % A;
+				be[i] = __ldg(tb.beta_rows + (size_t)__ldg(tb.beta_row_of + i) * m.S + sett) *
+				        __ldg(tb.areafactor + (size_t)(sett / m.div_per_time) * A + c);
+				float e = __ldg(tb.efoi_spline + (size_t)__ldg(tb.efoi_ref + i) * m.S + sett) * m.inv_popsize_f;
+				if (tb.efoi_mult) e *= __ldg(tb.efoi_mult + ((size_t)sett * A + c) * NS + i / A);
+				et[i] = e;
+			}
+			for (int j = tid; j < G * G; j += NT) Nm[j] = __ldg(tb.Ntime + (size_t)sett * G * G + j);
+			if (tid == 0) {
+				dgeo[0] = __ldg(tb.geo + sett);
+				cur_group = grp;
+			}
+			__syncthreads();
+		}
 		const uint32_t stream = b.stream_of ? b.stream_of[p] : (uint32_t)p;
 		int32_t *status = b.status + p;
-		int32_t *pc = bx_pop(m, b, p, cur), *pn = bx_pop(m, b, p, cur ^ 1);
+		const int32_t *pc = bx_pop(m, b, p, cur);
+		int32_t *pn = bx_pop(m, b, p, cur ^ 1);
 		const float *Ic = Ic_all + (size_t)p * NS * A * G;
 		const float *Y = b.bx_y + (size_t)p * NS * A * G;
 		float *Icp = Icn_all + (size_t)p * NS * A * G;
-		float *slot = b.bx_slot + (size_t)p * b.nslots;
-		for (int k = tid; k < T * DP; k += NT) rate[k] = tb.rate[k];
-		for (int k = tid; k < DP; k += NT) sus[k] = tb.sus[k];
-		for (int k = tid; k < C; k += NT) inf[k] = tb.inf[k];
-		for (int i = tid; i < NS * A; i += NT) {
-			const int c = i % A;
-			be[i] = __ldg(tb.beta_rows + (size_t)__ldg(tb.beta_row_of + i) * m.S + sett) *
-			        __ldg(tb.areafactor + (size_t)(sett / m.div_per_time) * A + c);
-			float e = __ldg(tb.efoi_spline + (size_t)__ldg(tb.efoi_ref + i) * m.S + sett) * m.inv_popsize_f;
-			if (tb.efoi_mult) e *= __ldg(tb.efoi_mult + ((size_t)sett * A + c) * NS + i / A);
-			et[i] = e;
-		}
-		for (int k = tid; k < G * G; k += NT) Nm[k] = __ldg(tb.Ntime + (size_t)sett * G * G + k);
-		if (tid == 0) dgeo[0] = __ldg(tb.geo + sett);
-		if (Icn)
-			for (int k = tid; k < NS * A * G; k += NT) Icn[k] = 0.f;
-		if (NS > 1) {
-			// strain shift of the susceptible population (src/state.cc:392-401)
-			for (int idx = tid; idx < A * DPS; idx += NT) {
-				const int dp = idx % DPS, c = idx / DPS;
-				int32_t *sp = pc + inf_from * ncol + c * DP;
-				int32_t sum = 0;
-				for (int st = 1; st < NS; st++) { sum += sp[DPS * st + dp]; sp[DPS * st + dp] = 0; }
-				sp[dp] += sum;
-			}
-		}
-		__syncthreads();
-		float2 kah = b.bx_kahan[(size_t)p * NT + tid];
-		float Lsum = kah.x, Lcmp = kah.y;
+		int32_t *tn = b.bx_tn + (size_t)p * tnrows * ncol;
 		const float d = dgeo[0], omd = 1.f - d;
+		const int col1 = min(ncol, (k + 1) * kBxChunk);
 		// ---- per column (c, dp): NMI, means, draws, population update, next infectious count
-		for (int col = tid; col < ncol; col += NT) {
+		for (int col = k * kBxChunk + tid; col < col1; col += NT) {
 			const int c = col / DP, dp = col - c * DP;
 			const int st = dp / DPS, dpl = dp - st * DPS, a = age[dpl];
 			int32_t pv[kMaxC];
@@ -408,7 +439,7 @@ __global__ void __launch_bounds__(kBxStepThreads, MB) bx_step(const ModelDev m, 
 			for (int tr = 0; tr < T; tr++) {
 				float mean = mv[0];
 #pragma unroll
-				for (int k = 1; k < kMaxT; k++) mean = tr == k ? mv[k] : mean;
+				for (int kk = 1; kk < kMaxT; kk++) mean = tr == kk ? mv[kk] : mean;
 				int32_t n = 0;
 				if (mean > 0.f) {
 					if (mean > 1.0e9f) atomicCAS(status, 0, BEEP_COUNT_OVERFLOW);
@@ -438,41 +469,60 @@ __global__ void __launch_bounds__(kBxStepThreads, MB) bx_step(const ModelDev m, 
 					if (inf[co] != 0.f) iv = fmaf(inf[co], (float)pv[co], iv);
 				}
 			}
-			if (Icn) atomicAdd(Icn + (st * A + c) * G + a, iv);
-			else Icp[(st * A + c) * G + a] = iv;
+			if (m.dp_age_unique) Icp[(st * A + c) * G + a] = iv;
+			else atomicAdd(Icp + (st * A + c) * G + a, iv);   // cleared by the step's observation kernel
 		}
-		__syncthreads();
-		// ---- observation sums of the step (completed ones -> log-density)
-		const int a0 = b.step_ptr[s_rel], a1 = b.step_ptr[s_rel + 1];
-		for (int k = a0 + tid; k < a1; k += NT) {
-			const int4 t0 = __ldg(b.tasks + 2 * k), t1 = __ldg(b.tasks + 2 * k + 1);
-			const float fac = __int_as_float(t1.x);
-			const int spl = t1.y;
-			const float w = spl < 0 ? fac : fac * tb.obs_spline[(size_t)spl * m.S + sett];
-			const int nc = t0.w & 0x7fffffff;
-			float v = slot[t0.x];
-			if (nc > 0) {
-				const int cell = t0.z;
-				v = fmaf(w, cell >= 0 ? (float)tn[cell] : (float)pc[-1 - cell], v);
-			}
-			for (int i = 1; i < nc; i++) {
-				const int cell = __ldg((b.tn_full ? m.obs_cells_full : m.obs_cells_f) + t1.z + i);
-				v = fmaf(w, cell >= 0 ? (float)tn[cell] : (float)pc[-1 - cell], v);
-			}
-			if (t0.w < 0) {                  // the observation's last step: log-density
-				const float lp = obs_lp_fast(v, t0.y, m);
-				v = 0.f;
-				const float y = lp - Lcmp;      // Kahan
-				const float tt = Lsum + y;
-				Lcmp = (tt - Lsum) - y;
-				Lsum = tt;
-			}
-			slot[t0.x] = v;
+	}
+}
+
+// The step's observation terms of particle p (completed observations -> log-density,
+// compensated per thread), then the next step's strain shift; with several dp per age
+// the next infectious counts are accumulated by atomics, so the buffer the step after
+// next accumulates into is cleared here.
+__global__ void __launch_bounds__(kBxObsThreads) bx_obs(const ModelDev m, const BatchDev b, int sett)
+{
+	const int p = blockIdx.x, tid = threadIdx.x;
+	const int A = m.A, G = m.G, NS = m.NS, ncol = A * m.DP;
+	const int tnrows = b.tn_full ? m.T : m.tn_rows;
+	const int s_rel = sett - b.ti, cur = s_rel & 1;
+	const Tabs tb = bx_tabs(b, p);
+	const int32_t *pc = bx_pop(m, b, p, cur);
+	const int32_t *tn = b.bx_tn + (size_t)p * tnrows * ncol;
+	float *slot = b.bx_slot + (size_t)p * b.nslots;
+	float2 kah = b.bx_kahan[(size_t)p * kBxObsThreads + tid];
+	float Lsum = kah.x, Lcmp = kah.y;
+	const int a0 = b.step_ptr[s_rel], a1 = b.step_ptr[s_rel + 1];
+	for (int k = a0 + tid; k < a1; k += kBxObsThreads) {
+		const int4 t0 = __ldg(b.tasks + 2 * k), t1 = __ldg(b.tasks + 2 * k + 1);
+		const float fac = __int_as_float(t1.x);
+		const int spl = t1.y;
+		const float w = spl < 0 ? fac : fac * tb.obs_spline[(size_t)spl * m.S + sett];
+		const int nc = t0.w & 0x7fffffff;
+		float v = slot[t0.x];
+		if (nc > 0) {
+			const int cell = t0.z;
+			v = fmaf(w, cell >= 0 ? (float)tn[cell] : (float)pc[-1 - cell], v);
 		}
-		if (Lsum != kah.x || Lcmp != kah.y) b.bx_kahan[(size_t)p * NT + tid] = make_float2(Lsum, Lcmp);
-		if (Icn) {
-			__syncthreads();
-			for (int k = tid; k < NS * A * G; k += NT) Icp[k] = Icn[k];
+		for (int i = 1; i < nc; i++) {
+			const int cell = __ldg((b.tn_full ? m.obs_cells_full : m.obs_cells_f) + t1.z + i);
+			v = fmaf(w, cell >= 0 ? (float)tn[cell] : (float)pc[-1 - cell], v);
+		}
+		if (t0.w < 0) {                  // the observation's last step: log-density
+			const float lp = obs_lp_fast(v, t0.y, m);
+			v = 0.f;
+			const float y = lp - Lcmp;      // Kahan
+			const float tt = Lsum + y;
+			Lcmp = (tt - Lsum) - y;
+			Lsum = tt;
+		}
+		slot[t0.x] = v;
+	}
+	if (Lsum != kah.x || Lcmp != kah.y) b.bx_kahan[(size_t)p * kBxObsThreads + tid] = make_float2(Lsum, Lcmp);
+	if (sett + 1 < b.tf) {
+		if (NS > 1) strain_shift(m, bx_pop(m, b, p, cur ^ 1), tid, kBxObsThreads);
+		if (!m.dp_age_unique) {
+			float *Ic = b.bx_ic + (size_t)cur * b.P * NS * A * G + (size_t)p * NS * A * G;
+			for (int k = tid; k < NS * A * G; k += kBxObsThreads) Ic[k] = 0.f;
 		}
 	}
 }
@@ -485,8 +535,8 @@ __global__ void __launch_bounds__(256) bx_final(const ModelDev m, const BatchDev
 	const int A = m.A, DP = m.DP, C = m.C, ncol = A * DP, popsz = C * ncol;
 	if (b.L) {
 		double S = 0.0;
-		for (int k = tid; k < kBxStepThreads; k += blockDim.x) {
-			const float2 v = b.bx_kahan[(size_t)p * kBxStepThreads + k];
+		for (int k = tid; k < kBxObsThreads; k += blockDim.x) {
+			const float2 v = b.bx_kahan[(size_t)p * kBxObsThreads + k];
 			S += (double)v.x - (double)v.y;
 		}
 		for (int o = 16; o > 0; o >>= 1) S += __shfl_xor_sync(0xffffffffu, S, o);
@@ -509,7 +559,7 @@ __global__ void __launch_bounds__(256) bx_final(const ModelDev m, const BatchDev
 }
 
 template <int MG, int MB>
-int launch_steps(const ModelDev &m, const BatchDev &b, size_t smem_step, int sms, cudaStream_t st)
+int launch_steps(const ModelDev &m, const BatchDev &b, size_t smem_step, int sms, cudaStream_t st, cudaEvent_t *ev)
 {
 	auto kstep = bx_step<MG, MB>;
 	cudaError_t e = cudaFuncSetAttribute(kstep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_step);
@@ -520,11 +570,15 @@ int launch_steps(const ModelDev &m, const BatchDev &b, size_t smem_step, int sms
 	if (e != cudaSuccess) return (int)e;
 	const int rows = b.P * m.NS * m.G;
 	const int ntile = (rows + kBxRows - 1) / kBxRows;
-	const int grid = std::min(b.P, sms * MB);
+	const int ncol = m.A * m.DP, nitem = b.P * ((ncol + kBxChunk - 1) / kBxChunk);
+	const int grid = std::min(nitem, sms * MB);
 	bx_init<<<b.P, 256, 0, st>>>(m, b);
 	for (int s = b.ti; s < b.tf; s++) {
+		if (ev) cudaEventRecord(ev[2 * (s - b.ti)], st);
 		bx_foi<<<ntile, kBxThreads, smem_foi, st>>>(m, b, (s - b.ti) & 1);
+		if (ev) cudaEventRecord(ev[2 * (s - b.ti) + 1], st);
 		kstep<<<grid, kBxStepThreads, smem_step, st>>>(m, b, s);
+		bx_obs<<<b.P, kBxObsThreads, 0, st>>>(m, b, s);
 	}
 	bx_final<<<b.P, 256, 0, st>>>(m, b);
 	return (int)cudaGetLastError();
@@ -538,30 +592,31 @@ bool batched_supported(const ModelDev &m)
 	       (size_t)kBxStages * bx_geometry(m.A, m.NS).stage <= 227 * 1024;
 }
 
-size_t batched_step_smem(const ModelDev &m, int tnrows)
+size_t batched_step_smem(const ModelDev &m, int)
 {
 	auto r = [](size_t x) { return (x + 15) & ~(size_t)15; };
 	const size_t A = m.A, G = m.G, DP = m.DP, NS = m.NS, C = m.C, T = m.T, DPS = m.DPS;
-	return r(4 * (size_t)tnrows * A * DP) + 2 * r(4 * NS * A) + r(4 * G * G) + r(4 * T * DP) + r(4 * DP) + r(4 * C) +
-	       r(4 * 64) + r(4 * 32) + 3 * r(4 * T) + r(4 * DPS) + (m.dp_age_unique ? 0 : r(4 * NS * A * G)) + 16;
+	return 2 * r(4 * NS * A) + r(4 * G * G) + r(4 * T * DP) + r(4 * DP) + r(4 * C) + r(4 * 64) + r(4 * 32) +
+	       3 * r(4 * T) + r(4 * DPS) + 16;
 }
 
-int batched_step_threads() { return kBxStepThreads; }
+int batched_obs_threads() { return kBxObsThreads; }
 
 int batched_prepare() { return prepare_constants(); }
 
-int batched_launches(int nsteps) { return 2 * nsteps + 2; }
+int batched_launches(int nsteps) { return 3 * nsteps + 2; }
 
-int launch_sim_batched(const ModelDev &m, const BatchDev &b, int sms, void *stream)
+int launch_sim_batched(const ModelDev &m, const BatchDev &b, int sms, void *stream, void *events)
 {
 	if (b.P == 0) return 0;
 	if (!batched_supported(m) || !b.bx_pop || b.mode != 0) return (int)cudaErrorInvalidValue;
 	const int e0 = prepare_constants();
 	if (e0 != 0) return e0;
-	const size_t smem = batched_step_smem(m, b.tn_full ? m.T : m.tn_rows);
+	const size_t smem = batched_step_smem(m, 0);
 	cudaStream_t st = (cudaStream_t)stream;
-	return m.G <= 4 ? launch_steps<4, 4>(m, b, smem, sms, st) : m.G <= 8 ? launch_steps<8, 4>(m, b, smem, sms, st)
-	     : m.G <= 12 ? launch_steps<12, 3>(m, b, smem, sms, st) : launch_steps<16, 3>(m, b, smem, sms, st);
+	cudaEvent_t *ev = (cudaEvent_t *)events;
+	return m.G <= 4 ? launch_steps<4, 6>(m, b, smem, sms, st, ev) : m.G <= 8 ? launch_steps<8, 6>(m, b, smem, sms, st, ev)
+	     : m.G <= 12 ? launch_steps<12, 5>(m, b, smem, sms, st, ev) : launch_steps<16, 5>(m, b, smem, sms, st, ev);
 }
 
 }  // namespace beep

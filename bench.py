@@ -47,6 +47,18 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def tensor_peak():
+    """Dense BF16 tensor throughput (TFLOP/s): the measured sustained figure for a
+    kernel timed inside a long run, else the fallback."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        v = d.get("bf16_tflops_sustained") or d.get("bf16_tflops")
+        if v:
+            return float(v), "measured sustained"
+    return 1700.0, "fallback"
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle samples during a timed region."""
 
@@ -216,16 +228,29 @@ def run_serving(nreq: int, rate: float, seed: int, budget_bytes: int, inflight: 
     srv.close()
     lat = np.array([s["done_s"] - s["submit_s"] for s in st])
     wait = np.array([s["admit_s"] - s["submit_s"] for s in st])
+    svc = np.array([s["gpu_end_s"] - s["gpu_start_s"] for s in st])
     span = max(s["done_s"] for s in st) - min(s["submit_s"] for s in st)
     busy = sorted((s["gpu_start_s"], s["gpu_end_s"]) for s in st)
     overlap = sum(1 for a, b in zip(busy, busy[1:]) if b[0] < a[1])
     for r in reqs:
         assert r["batch"].L is None or np.all(np.isfinite(r["batch"].L))
     units = sum(r["units"] for r in reqs)
+    errs = []
+    for r in [r for r in reqs if r["kind"] == capi.REQ_LIKELIHOOD][:3]:
+        dmr = capi.DeviceModel(r["model"])
+        e = fast_loglik_error(dmr, r["model"], r["batch"].tables, np.arange(4) % len(r["batch"].tables), 4, seed)
+        dmr.close()
+        errs.append(e["max_rel_err_vs_fp64_of_own_trajectory"])
+    errs = [e for e in errs if e is not None]
     return {
+        "loglik_vs_fp64": {"requests": len(errs), "particles_each": 4,
+                           "max_rel_err_vs_fp64_of_own_trajectory": float(max(errs)) if errs else None,
+                           "tolerance": 1e-6},
         "requests": nreq, "arrival_rate_per_s": rate, "max_inflight": inflight, "hbm_budget_gb": budget_bytes / 2**30,
         "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
         "queue_wait_p50_ms": float(np.percentile(wait, 50) * 1e3),
+        "queue_wait_p99_ms": float(np.percentile(wait, 99) * 1e3),
+        "service_p50_ms": float(np.percentile(svc, 50) * 1e3), "service_p99_ms": float(np.percentile(svc, 99) * 1e3),
         "throughput": units / span, "unit": "particle.area.group.steps/s",
         "loglik_evals_per_s": sum(r["particles"] for r in reqs) / span, "makespan_s": span,
         "overlapping_request_pairs": overlap,
@@ -251,22 +276,62 @@ def fp64_loglik_of_trajectory(m, transnum):
     """The observation log-likelihood of one transition-count trajectory
     [S][A][T][DP] in FP64 (ObservationModel::calculate with normal
     observations, src/obsmodel.cc:22-58,245-305): every observation's count is an
-    exact integer sum over its steps and cells, then its normal log-density."""
+    exact integer sum over its steps and cells -- transition counts, or the
+    populations at each step's start rebuilt from the start populations and the
+    counts (update_pop, src/state.cc:460-485) -- then its normal log-density.
+    None for models with other observation models or censored values."""
     a = m.arr
     S = transnum.shape[0]
+    if (a["obs_model"] > 1).any() or (a["obs_value_kind"] != 0).any() or m.nstrain != 1:
+        return None                                   # Poisson / negative binomial / censored: not handled here
     tn = transnum.reshape(S, -1).astype(np.int64)
     cum = np.vstack([np.zeros((1, tn.shape[1]), np.int64), np.cumsum(tn, 0)])
     ptr, cells = a["obs_cell_ptr"], a["obs_cells"]
     si, sf = a["obs_sett_i"], a["obs_sett_f"]
-    if (cells < 0).any() or (a["obs_model"] != 0).any() or (a["obs_value_kind"] != 0).any():
-        return None                                   # population or non-normal observations: not handled here
     obs_of_cell = np.repeat(np.arange(m.nobs), np.diff(ptr))
-    per_cell = cum[sf[obs_of_cell], cells] - cum[si[obs_of_cell], cells]
     v = np.zeros(m.nobs)
-    np.add.at(v, obs_of_cell, per_cell.astype(np.float64))
+    tm = cells >= 0
+    if tm.any():
+        oc = obs_of_cell[tm]
+        np.add.at(v, oc, (cum[sf[oc], cells[tm]] - cum[si[oc], cells[tm]]).astype(np.float64))
+    if (~tm).any():
+        A, C, T, DP = m.narea, m.ncomp, m.ntrans, m.ndemocatpos
+        frm, to = a["trans_from"], a["trans_to"]
+        t4 = transnum.astype(np.int64)                            # [S][A][T][DP]
+        flow = np.zeros((S, A, C, DP), np.int64)
+        for tr in range(T):
+            flow[:, :, frm[tr], :] -= t4[:, :, tr, :]
+            flow[:, :, to[tr], :] += t4[:, :, tr, :]
+        pop0 = np.rint(a["pop_init"]).astype(np.int64).reshape(1, A, C, DP)
+        pops = (pop0 + np.vstack([np.zeros((1, A, C, DP), np.int64), np.cumsum(flow, 0)[:-1]])).reshape(S, -1)
+        cpp = np.vstack([np.zeros((1, pops.shape[1]), np.int64), np.cumsum(pops, 0)])
+        oc = obs_of_cell[~tm]
+        pc = -1 - cells[~tm]
+        np.add.at(v, oc, (cpp[sf[oc], pc] - cpp[si[oc], pc]).astype(np.float64))
     v = np.maximum(v * a["obs_factor"], 0.0)
     var = a["obs_sd"] ** 2
     return float(np.sum(-0.5 * np.log(2 * np.pi * var) - (a["obs_value"] - v) ** 2 / (2 * var)))
+
+
+def fast_loglik_error(dm, m, tabs, group_of, n: int, seed: int):
+    """The fast form's log-likelihood against FP64 on n particles: each fast
+    trajectory scored in FP64 on the host (largest relative error), and, on
+    the same particles and streams, the share that kept the FP64 form's
+    trajectory and their largest L difference."""
+    from beep_gb300 import capi
+    go = None if group_of is None else group_of[:n]
+    tb = tabs[:n] if len(tabs) > 1 else tabs
+    res = {}
+    for f in (capi.FORM_FAST, capi.FORM_PLAIN_FP64):
+        res[f] = dm.simulate(capi.Batch(m, tb, n, seed, group_of=go, want_transnum=True, form=f))
+    fa, pl = res[capi.FORM_FAST], res[capi.FORM_PLAIN_FP64]
+    same = np.array([np.array_equal(fa.transnum[k], pl.transnum[k]) for k in range(n)])
+    rel = np.abs(fa.L - pl.L) / np.abs(pl.L)
+    l64 = [fp64_loglik_of_trajectory(m, fa.transnum[k]) for k in range(n)]
+    own = [abs(fa.L[k] - l64[k]) / abs(l64[k]) for k in range(n) if l64[k] is not None]
+    return {"particles": n, "identical_trajectories": float(same.mean()),
+            "max_rel_err_identical": float(rel[same].max()) if same.any() else None,
+            "max_rel_err_vs_fp64_of_own_trajectory": float(max(own)) if own else None, "tolerance": 1e-6}
 
 
 def run_particle_filter(reps: int, seed: int, N: int = 256, section_steps: int = 28):
@@ -295,6 +360,7 @@ def run_particle_filter(reps: int, seed: int, N: int = 256, section_steps: int =
     dm = capi.DeviceModel(m)
     out = {"workload": "pmcmc_pf_10x3", "particles": N, "steps": S, "sections": len(sections),
            "timing": "host wall clock per estimate (beep_pf_loglik)"}
+    out["loglik_vs_fp64"] = fast_loglik_error(dm, m, [t], None, 32, seed)
     for form, name in ((capi.FORM_FAST, "fast"), (capi.FORM_PLAIN_FP64, "plain_fp64")):
         for k in range(2):                                   # warm-up
             dm.pf_loglik(t, N, seed + k, 5, 1.0, sections, form=form)
@@ -372,6 +438,18 @@ def run_mbp_chains(sweeps: int, seed: int, nchain: int = 128, plain_sweeps: int 
                 x["L"] = np.where(ok, res[i], x["L"])
                 acc.append(ok.mean())
             times.append(time.perf_counter() - t0)
+        if form == capi.FORM_FAST:
+            # the chains' log-likelihoods against FP64 scoring of their own current trajectories
+            x = models[-1]
+            errs = []
+            for c in range(min(8, nchain)):
+                tn_c, _ = x["ch"].read_state(c)
+                l64 = fp64_loglik_of_trajectory(x["m"], tn_c)
+                if l64 is not None:
+                    errs.append(abs(x["L"][c] - l64) / abs(l64))
+            out["loglik_vs_fp64"] = {"model": f"{x['m'].narea}x{x['m'].nage}", "chains": len(errs),
+                                     "max_rel_err_vs_fp64_of_own_trajectory": float(max(errs)) if errs else None,
+                                     "tolerance": 1e-6}
         for x in models:
             x["ch"].close()
             x["dm"].close()
@@ -384,6 +462,139 @@ def run_mbp_chains(sweeps: int, seed: int, nchain: int = 128, plain_sweeps: int 
                 "units_per_sweep": units, "data": "synthetic, weekly hospital populations",
                 "timing": "host wall clock per sweep (4 concurrent model streams, proposals + FP64 acceptance)"})
     return out
+
+
+def run_precision(seed: int, P: int = 1024, steps: int = 3, warmup: int = 1, plain_particles: int = 304):
+    """The 350-area x 10-age PMCMC batch (1460 steps, 1024 particles of one
+    parameter set): the fast form in its automatic layout (tensor cores batched
+    over the particles), the plain FP64 form on a subset, the fast form's
+    log-likelihood error against FP64, and the tensor roofline of the per-step
+    force-of-infection products."""
+    from beep_gb300 import capi
+    w, m, tabs, group_of = build_workload("precision", P, seed)
+    dm = capi.DeviceModel(m)
+    db = capi.DeviceBatch(dm, capi.Batch(m, tabs, P, seed, group_of=group_of, form=capi.FORM_FAST))
+    db.upload()
+    db.time(warmup)
+    ms, ms_prod = db.time_split(steps)
+    units = P * m.narea * m.nage * m.ndivision
+    out = {"workload": WORKLOADS["precision"]["name"], "particles": P, "areas": m.narea, "ages": m.nage,
+           "steps": m.ndivision, "observations": m.nobs,
+           "fast": {"value": units / (ms / 1e3), "unit": METRIC, "ms_per_step": ms,
+                    "loglik_evals_per_s": P / (ms / 1e3), "launches": db.launches(),
+                    "foi": {1: "fp32-simt", 2: "tensor-core per particle", 3: "tensor-core batched"}[db.foi_path()]}}
+    if db.foi_path() == 3 and ms_prod > 0:
+        # useful work of the area contraction: 2 flops per (source, target) pair per (particle, strain, age) row
+        useful = 2.0 * P * m.nstrain * m.nage * m.narea * m.narea * m.ndivision
+        tp, tkind = tensor_peak()
+        ach = useful / (ms_prod / 1e3) / 1e12
+        out["foi_products"] = {"ms_per_step": ms_prod, "share_of_step": ms_prod / ms, "useful_flops_per_launch": useful,
+                               "roofline": {"bound": "tensor", "achieved": ach, "peak": tp, "unit": "TFLOP/s",
+                                            "frac": ach / tp, "peak_kind": tkind,
+                                            "note": "useful flops of the contraction over the product kernels' "
+                                                    "time; the kernels issue five split-BF16 products on padded "
+                                                    "tiles"}}
+    db.close()
+    Pp = min(P, plain_particles)
+    pb = capi.DeviceBatch(dm, capi.Batch(m, tabs, Pp, seed, group_of=group_of[:Pp], form=capi.FORM_PLAIN_FP64))
+    pb.upload()
+    pb.time(1)
+    pms = pb.time(1)
+    pb.close()
+    out["plain_fp64"] = {"value": Pp * m.narea * m.nage * m.ndivision / (pms / 1e3), "unit": METRIC,
+                         "ms_per_step": pms, "particles": Pp, "loglik_evals_per_s": Pp / (pms / 1e3)}
+    out["fast_over_plain_loglik_evals"] = out["fast"]["loglik_evals_per_s"] / out["plain_fp64"]["loglik_evals_per_s"]
+    out["loglik_vs_fp64"] = fast_loglik_error(dm, m, tabs, group_of, 12, seed)
+    dm.close()
+    return out, (w, m, tabs)
+
+
+def run_serving_precision(nreq: int, seed: int, model, tables, plain_evals_per_s: float, rate: float = 200.0):
+    """The serving form on the 350-area x 10-age model: likelihood requests of
+    uneven particle counts (log-uniform in [64, 1024]) arriving at `rate` per
+    second, admitted as memory and slots free up and run side by side.  Reports
+    log-likelihood evaluations per second over the makespan and their ratio to
+    the plain FP64 form's."""
+    from beep_gb300 import capi
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for k in range(nreq):
+        P = int(np.exp(rng.uniform(np.log(64), np.log(1024))))
+        reqs.append(capi.Batch(model, tables, P, seed + k, group_of=np.zeros(P, np.int32), form=capi.FORM_FAST))
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
+    srv = capi.Server(200 << 30, 8)
+    t0 = time.perf_counter()
+    tickets = []
+    for k, b in enumerate(reqs):
+        dt = arrivals[k] - (time.perf_counter() - t0)
+        if dt > 0:
+            time.sleep(dt)
+        tickets.append(srv.submit(model, b, capi.REQ_LIKELIHOOD))
+    for t in tickets:
+        srv.wait(t)
+    st = [srv.stats(t) for t in tickets]
+    srv.close()
+    span = max(x["done_s"] for x in st) - min(x["submit_s"] for x in st)
+    lat = np.array([x["done_s"] - x["submit_s"] for x in st])
+    svc = np.array([x["gpu_end_s"] - x["gpu_start_s"] for x in st])
+    evals = sum(len(b.L) for b in reqs)
+    assert all(np.all(np.isfinite(b.L)) for b in reqs)
+    return {"requests": nreq, "arrival_rate_per_s": rate, "particles_total": int(evals),
+            "loglik_evals_per_s": evals / span, "makespan_s": span,
+            "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "service_p50_ms": float(np.percentile(svc, 50) * 1e3),
+            "serving_over_plain_loglik_evals": evals / span / plain_evals_per_s,
+            "note": "serving-form log-likelihood evaluations/s over the plain FP64 form's on the same model"}
+
+
+def issue_roofline(kind: str, P: int, t_dev: float, clocks: dict):
+    """The fast kernel's instruction-issue roofline: warp instructions per launch
+    (per-particle count of the committed ncu capture of the workload, times the
+    particles) over the SMs' issue capacity in the timed region -- 4 schedulers
+    per SM, one warp instruction per cycle each, at the median SM clock sampled
+    during the timing.  The kernel keeps its state on chip, so this, not HBM,
+    is the bound that applies."""
+    import re
+    f = os.path.join(ROOT, "profiles", "sim_fast_abc_smc.md" if kind == "abc_smc" else "sim_fast_precision.md")
+    if not os.path.exists(f):
+        return None
+    mt = re.search(r"warp_instructions_per_particle:\s*([0-9.eE+]+)", open(f).read())
+    if not mt:
+        return None
+    try:
+        import torch
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+    except Exception:
+        sms = 152
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    inst = float(mt.group(1)) * P
+    achieved = inst / t_dev
+    peak = sms * 4 * mhz * 1e6
+    return {"bound": "issue", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "T warp-instructions/s",
+            "frac": achieved / peak, "sms": sms, "sm_mhz": mhz,
+            "warp_instructions_per_launch": inst, "source": os.path.relpath(f, ROOT)}
+
+
+def run_abc_weights(seed: int, n: int = 16384, reps: int = 3):
+    """beep_abcsmc_weights at the ABC-SMC generation's size: n new against n
+    previous particles, three parameters (host wall clock per call, host
+    arrays in and out)."""
+    from beep_gb300 import capi
+    rng = np.random.default_rng(seed)
+    lo, hi = np.array([1.5, 2.0, 3.0]), np.array([4.0, 6.0, 8.0])
+    tl = rng.uniform(lo, hi, (n, 3))
+    wl = rng.uniform(0.2, 2.0, n)
+    tn = np.clip(tl[rng.integers(0, n, n)] + rng.normal(0, 0.2, (n, 3)), lo, hi)
+    ic = np.linalg.inv(np.cov(tl.T, aweights=wl))
+    lp = np.full(n, -np.log(np.prod(hi - lo)))
+    capi.abcsmc_weights(tn, lp, tl, wl, ic, 1.3)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        w = capi.abcsmc_weights(tn, lp, tl, wl, ic, 1.3)
+    dt = (time.perf_counter() - t0) / reps
+    assert np.all(np.isfinite(w))
+    return {"new": n, "previous": n, "parameters": 3, "ms_per_call": dt * 1e3, "pairs_per_s": n * n / dt,
+            "timing": "host wall clock per call (host arrays in and out)"}
 
 
 def max_over_ranks(dist, *times):
@@ -482,7 +693,8 @@ def workload_config(kind, m, P, note=None):
 def run_ours(args, rank, ws, dist):
     from beep_gb300 import build as bbuild, capi
     bbuild.build()
-    capi.set_option("fast_foi", {"auto": capi.FOI_AUTO, "simt": capi.FOI_SIMT, "tensor": capi.FOI_TENSOR}[args.foi])
+    capi.set_option("fast_foi", {"auto": capi.FOI_AUTO, "simt": capi.FOI_SIMT, "tensor": capi.FOI_TENSOR,
+                                 "batched": capi.FOI_BATCHED}[args.foi])
     capi.set_option("fast_ctas_per_sm", args.ctas)
     P = args.particles or WORKLOADS[args.workload]["particles"]
     seed = args.seed + 7919 * rank
@@ -538,22 +750,9 @@ def run_ours(args, rank, ws, dist):
     if form == capi.FORM_FAST and args.plain_particles > 0 and rank == 0:
         traj_bytes = 4 * m.ndivision * m.narea * m.ntrans * m.ndemocatpos
         na = int(max(8, min(32, 2e9 // traj_bytes, P)))
-        res = {}
-        for f in (capi.FORM_FAST, capi.FORM_PLAIN_FP64):
-            res[f] = dm.simulate(capi.Batch(m, tabs[:na] if len(tabs) > 1 else tabs, na, seed, group_of=group_of[:na],
-                                            want_transnum=True, form=f))
-        fa, pl = res[capi.FORM_FAST], res[capi.FORM_PLAIN_FP64]
-        same = np.array([np.array_equal(fa.transnum[k], pl.transnum[k]) for k in range(na)])
-        rel = np.abs(fa.L - pl.L) / np.abs(pl.L)
-        # every fast trajectory scored in FP64 on the host: the error of the FP32 evaluation
-        l64 = [fp64_loglik_of_trajectory(m, fa.transnum[k]) for k in range(na)]
-        own = [abs(fa.L[k] - l64[k]) / abs(l64[k]) for k in range(na) if l64[k] is not None]
-        acc = {"particles": na, "identical_trajectories": float(same.mean()),
-               "max_rel_err_identical": float(rel[same].max()) if same.any() else None,
-               "max_rel_err_vs_fp64_of_own_trajectory": float(max(own)) if own else None,
-               "tolerance": 1e-6,
-               "note": "particles whose FP32 draws crossed a near tie follow another trajectory; each fast "
-                       "trajectory is also scored in FP64 on the host"}
+        acc = fast_loglik_error(dm, m, tabs, group_of, na, seed)
+        acc["note"] = ("particles whose FP32 draws crossed a near tie follow another trajectory; each fast "
+                       "trajectory is also scored in FP64 on the host")
     if rank != 0:
         return
     hbm, hbm_kind = peaks()
@@ -568,6 +767,17 @@ def run_ours(args, rank, ws, dist):
     serving = None
     if args.serve_requests > 0 and ws == 1:
         serving = run_serving(args.serve_requests, 200.0, args.seed + 4242, 200 << 30, 8)
+        if args.serve_sustained > 0:
+            serving["sustainable_rate"] = run_serving(args.serve_sustained, args.sustained_rate, args.seed + 4343,
+                                                      200 << 30, 8)
+    precision = serving_precision = None
+    if args.precision_particles > 0 and ws == 1 and args.workload == "abc_smc":
+        precision, (_, pm, ptabs) = run_precision(args.seed + 2, args.precision_particles,
+                                                  plain_particles=args.precision_plain_particles)
+        if args.serve_precision > 0:
+            serving_precision = run_serving_precision(args.serve_precision, args.seed + 5151, pm, ptabs,
+                                                      precision["plain_fp64"]["loglik_evals_per_s"])
+    weights = run_abc_weights(args.seed + 31) if ws == 1 else None
     cpu = None
     if not args.no_cpu:
         nthreads = os.cpu_count() or 1
@@ -580,7 +790,8 @@ def run_ours(args, rank, ws, dist):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.form == "fast" else "f64",
         "data": "synthetic", "config": workload_config(args.workload, m, P),
         "form": args.form,
-        "foi": {0: None, 1: "fp32-simt", 2: "tensor-core split-bf16"}[db.foi_path()],
+        "foi": {0: None, 1: "fp32-simt", 2: "tensor-core split-bf16 (per particle)",
+                3: "tensor-core split-bf16 batched over particles (step-synchronous)"}[db.foi_path()],
         "particles_per_sm": db.ctas_per_sm(),
         "plain_fp64": plain,
         "loglik_vs_fp64": acc,
@@ -592,10 +803,20 @@ def run_ours(args, rank, ws, dist):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_kind": hbm_kind, "traffic": traffic,
                      "algorithmic_bytes": f"{BYTES_PER_UNIT} B x {units} units per launch"},
+        "issue_roofline": issue_roofline(args.workload, P, t_dev, clocks) if args.form == "fast" else None,
         "cpu_baseline": cpu,
+        "precision_350x10": precision,
+        "serving_350x10": serving_precision,
         "serving": serving,
         "mbp_chains": mbp,
         "particle_filter": pf,
+        "abc_smc_weights": weights,
+        "loglik_vs_fp64_by_config": {
+            "C0_pf_10x3": pf.get("loglik_vs_fp64") if pf else None,
+            "C1_abc_smc_150x4": acc,
+            "C2_precision_350x10": precision.get("loglik_vs_fp64") if precision else None,
+            "C3_mbp_350x10": mbp.get("loglik_vs_fp64") if mbp else None,
+            "C4_serving": serving.get("loglik_vs_fp64") if serving else None},
     }
     print(json.dumps(line))
     db.close()
@@ -617,7 +838,7 @@ def main():
     ap.add_argument("--ctas", type=int, default=0, choices=[0, 1, 2, 3, 4],
                     help="particles (CTAs) per SM of the fast form: 0 = automatic, 1 = one, 2..4 = at most that many "
                          "(library option fast_ctas_per_sm)")
-    ap.add_argument("--foi", default="auto", choices=["auto", "simt", "tensor"],
+    ap.add_argument("--foi", default="auto", choices=["auto", "simt", "tensor", "batched"],
                     help="force of infection of the fast form (library option fast_foi)")
     ap.add_argument("--plain-particles", type=int, default=1024)
     ap.add_argument("--plain-steps", type=int, default=0, help="time the plain form over this many steps (0: all)")
@@ -625,8 +846,16 @@ def main():
                     help="sweeps of the MBP-chain workload (4 x 128 chains of uneven size) after the main measurement")
     ap.add_argument("--pf-estimates", type=int, default=10,
                     help="particle-filter likelihood estimates (256 particles, 10 x 3 model) per form after the main measurement")
-    ap.add_argument("--serve-requests", type=int, default=32,
+    ap.add_argument("--serve-requests", type=int, default=160,
                     help="requests of the serving stream (Poisson arrivals at 200/s) after the main measurement")
+    ap.add_argument("--serve-sustained", type=int, default=16,
+                    help="requests of the same stream at a rate the GPU sustains (latency without queueing)")
+    ap.add_argument("--sustained-rate", type=float, default=1.0)
+    ap.add_argument("--precision-particles", type=int, default=1024,
+                    help="particles of the 350x10 precision batch run after the main measurement (0: skip)")
+    ap.add_argument("--precision-plain-particles", type=int, default=152)
+    ap.add_argument("--serve-precision", type=int, default=24,
+                    help="350x10 likelihood requests through the server (serving form vs plain form)")
     args = ap.parse_args()
     rank, ws, dist = dist_setup(args)
     if args.impl == "reference":

@@ -202,6 +202,13 @@ BEEP_API beep_status beep_batch_launch(beep_batch *batch);
 BEEP_API beep_status beep_batch_download(beep_batch *batch);
 BEEP_API beep_status beep_batch_time(beep_batch *batch, int32_t iters, double *ms_per_launch);
 BEEP_API int32_t beep_batch_launches(const beep_batch *batch);   /* kernels per launch */
+/* beep_batch_time with the step-synchronous fast form's time split: the mean
+ * device time per launch and, of it, the time of the per-step tensor-core
+ * products of the force of infection (CUDA events around each product kernel;
+ * 0 for the other layouts).  A measurement aid with no counterpart in the
+ * reference. */
+BEEP_API beep_status beep_batch_time_split(beep_batch *batch, int32_t iters, double *ms_per_launch,
+                                           double *ms_product);
 /* bytes moved host->device by beep_batch_upload and device->host by beep_batch_download */
 BEEP_API beep_status beep_batch_bytes(const beep_batch *batch, int64_t *h2d, int64_t *d2h);
 BEEP_API beep_status beep_batch_destroy(beep_batch *batch);
@@ -211,19 +218,23 @@ BEEP_API beep_status beep_batch_destroy(beep_batch *batch);
 BEEP_API beep_status beep_batch_run_graph(beep_batch *batch);
 /* Autotuner of the fast form for a model: times every kernel layout the
  * model supports -- force of infection on FP32 SIMT (one or several particles
- * per SM) or on the tensor cores -- on a sample of the given batch (up to 8
- * particles per SM, up to 60 steps) and records the fastest on the model;
- * later batches of the model use it while the options fast_foi and
- * fast_ctas_per_sm are automatic (when several particles per SM won, each
- * batch still takes one per SM if it is too small to fill the SMs several
- * deep).  *chosen (may be NULL) receives the force of infection path (1 =
- * FP32 SIMT, 2 = tensor cores). */
+ * per SM), on the tensor cores one particle per CTA, or on the tensor cores
+ * batched over the particles (step-synchronous layout) -- on a sample of the
+ * given batch (up to 8 particles per SM, up to 60 steps) and records the
+ * fastest on the model; later batches of the model use it while the options
+ * fast_foi and fast_ctas_per_sm are automatic (when several particles per SM
+ * won, each batch still takes one per SM if it is too small to fill the SMs
+ * several deep).  *chosen (may be NULL) receives the force of infection path
+ * (1 = FP32 SIMT, 2 = tensor cores per particle, 3 = tensor cores batched). */
 BEEP_API beep_status beep_autotune(beep_model *model, const beep_sim_batch *batch, int32_t *chosen);
 /* Force-of-infection path the fast form of this batch runs: 1 = FP32 SIMT,
- * 2 = tensor cores; 0 for the plain form. */
+ * 2 = tensor cores one particle per CTA, 3 = tensor cores batched over the
+ * particles (every particle advances one step at a time; per step one product
+ * [particles x strains x ages, areas] . [areas, areas] and one step kernel);
+ * 0 for the plain form. */
 BEEP_API int32_t beep_batch_foi_path(const beep_batch *batch);
 /* Particles (CTAs) resident per SM that the fast form of this batch is laid
- * out for: 1..4; 0 for the plain form. */
+ * out for: 1..4; 0 for the plain form and the step-synchronous layout. */
 BEEP_API int32_t beep_batch_ctas_per_sm(const beep_batch *batch);
 
 /* Bootstrap particle filter of PMCMC (PMCMC::obs_prob + bootstrap,
@@ -271,7 +282,12 @@ BEEP_API beep_status beep_pf_loglik(beep_model *model, const beep_pf_request *re
  * with normalise != 0 the weights are divided by their mean
  * (normalise_particle_weights, src/abcsmc.cc:275-283).  The pairwise kernel
  * terms are computed in FP32 on the GPU and summed with compensation; the
- * per-particle sums, the prior factor and the normalisation are FP64. */
+ * per-particle sums, the prior factor and the normalisation are FP64.
+ * The form is evaluated as |L^T d|^2 with L L^T = inv_cov / size^2 when
+ * inv_cov is positive definite (as given otherwise); sums are kept as
+ * log-sum-exp, so they never underflow, and new particles far from every
+ * previous one are summed again in FP64.  Errors: BEEP_BAD_INPUT for
+ * negative or NaN previous weights or all of them zero. */
 BEEP_API beep_status beep_abcsmc_weights(int32_t nvar, int32_t nnew, const double *theta_new,
                                          const double *logprior_new, int32_t nlast, const double *theta_last,
                                          const double *w_last, const double *inv_cov, double size,
@@ -279,10 +295,16 @@ BEEP_API beep_status beep_abcsmc_weights(int32_t nvar, int32_t nnew, const doubl
 
 /* Library options (process-wide; no counterpart in the reference):
  *   "fast_foi"  force of infection of the fast form: 0 = automatic (tensor
- *               cores for models of 300 to 512 areas with one or two strains,
- *               FP32 SIMT otherwise), 1 = FP32 SIMT, 2 = tensor cores wherever
- *               supported (64 to 512 areas, one or two strains, more than 256
- *               area x group columns).
+ *               cores batched over the particles for models of 300 to 512
+ *               areas with one or two strains, FP32 SIMT otherwise), 1 = FP32
+ *               SIMT, 2 = tensor cores one particle per CTA wherever supported
+ *               (64 to 512 areas, one or two strains, more than 256 area x
+ *               group columns), 3 = tensor cores batched over the particles
+ *               (step-synchronous layout; 64 to 512 areas, one or two strains,
+ *               at most 8 compartments and 8 transitions, 16 ages).
+ *   "sampler_iteration_limit"  rejection iterations of the PTRS / BTRS
+ *               samplers before a draw gives up with BEEP_TIMEOUT: 0 = the
+ *               default 65536, or 1..65536 (lowered only to test that status).
  *   "fast_ctas_per_sm"  particles resident per SM in the fast form, for models
  *               of more than 256 area x group columns: 0 = automatic (several
  *               when at least three particles' state fits the SM's shared

@@ -25,8 +25,12 @@
 // 0..K-1 form the previous generation (weights 0.5 + 0.1 (j mod 7)), rows
 // K..K+N-1 are the new samples; BEEP's own inputs need nsample and ngeneration.
 //
+// With pred=DIR predn=K (BEEP's mode=prediction with modifications) it loads the
+// posterior samples DIR/sample0..K-1 and simulates each from the modifications'
+// start to the end, as the reference's prediction mode does.
+//
 // usage: ref_harness out=FILE [npart=N] [ntraj=N] [seed=S] [pf=0|1] [theta=FILE] [mbp=N] [sampledir=DIR]
-//                    [abcw=N abck=K] -- <BEEP key=value...>
+//                    [abcw=N abck=K] [pred=DIR predn=K] -- <BEEP key=value...>
 
 #include <cmath>
 #include <cstdint>
@@ -387,15 +391,20 @@ int main(int argc, char **argv)
 	g_replay.narea = A; g_replay.ntrans = T; g_replay.ndp = DP; g_replay.ndiv = S;
 	B.i("seed_words", {(int32_t)g_replay.k0, (int32_t)g_replay.k1});
 	B.scalar_i("ngroup", ngroup);
+	{
+		std::vector<int32_t> names;
+		for (const auto &par : model.param) {
+			for (char ch : par.name) names.push_back((int32_t)(unsigned char)ch);
+			names.push_back('\n');
+		}
+		B.i("param_names", names);
+	}
 	B.scalar_i("npart", npart);
 	B.scalar_i("ntraj", ntraj);
 
-	for (int gidx = 0; gidx < ngroup; gidx++) {
-		std::string gp = "g" + std::to_string(gidx) + ".";
-		B.d(gp + "theta", thetas[gidx]);
-		State state(details, data, model, obsmodel);
-		state.set_param(thetas[gidx]);
-		{
+	// the tables State::set_param produced for parameter set theta (beep_param_tables), and in
+	// prediction mode the model modifications' multipliers (ModelMod, src/model.cc:1446-1585)
+	auto dump_tables = [&](const std::string &gp, const State &state, const std::vector<double> &theta) {
 			std::vector<double> v;
 			for (unsigned tr = 0; tr < T; tr++) {
 				if (state.transrate[tr].size() == DP) for (unsigned dp = 0; dp < DP; dp++) v.push_back(state.transrate[tr][dp]);
@@ -404,7 +413,7 @@ int main(int argc, char **argv)
 			B.d(gp + "transrate", v, {T, DP});
 			B.d(gp + "susceptibility", state.susceptibility);
 			std::vector<double> inf(C);
-			for (unsigned co = 0; co < C; co++) inf[co] = thetas[gidx][model.comp[co].infectivity_param];
+			for (unsigned co = 0; co < C; co++) inf[co] = theta[model.comp[co].infectivity_param];
 			B.d(gp + "infectivity", inf);
 			// beta rows, deduplicated by content (the reference copies one row per R-spline to its areas, src/model.cc:1339-1345)
 			std::vector<std::vector<double>> rows;
@@ -441,7 +450,25 @@ int main(int argc, char **argv)
 			std::vector<double> os;
 			for (auto spl : spline_rows) os.insert(os.end(), state.disc_spline[spl].begin(), state.disc_spline[spl].end());
 			B.d(gp + "obs_spline", os, {spline_rows.size(), S});
+		if (details.mode == PREDICTION) {
+			std::vector<double> em, tm;
+			for (unsigned s = 0; s < S; s++)
+				for (unsigned c = 0; c < A; c++) {
+					for (unsigned st = 0; st < NS; st++) em.push_back(model.modelmod.efoi_mult[s][c][st]);
+					for (unsigned tr = 0; tr < T; tr++)
+						for (unsigned dp = 0; dp < DP; dp++) tm.push_back(model.modelmod.transmean_mult[s][c][tr][dp]);
+				}
+			B.d(gp + "efoi_mult", em, {S, A, NS});
+			B.d(gp + "transmean_mult", tm, {S, A, T, DP});
 		}
+	};
+
+	for (int gidx = 0; gidx < ngroup; gidx++) {
+		std::string gp = "g" + std::to_string(gidx) + ".";
+		B.d(gp + "theta", thetas[gidx]);
+		State state(details, data, model, obsmodel);
+		state.set_param(thetas[gidx]);
+		dump_tables(gp, state, thetas[gidx]);
 
 		std::vector<double> Lfull(npart), Lsec;
 		std::vector<int32_t> tnum, popt;
@@ -559,6 +586,44 @@ int main(int argc, char **argv)
 		int nt = std::min(ntraj, npart);
 		B.i(gp + "transnum", tnum, {(uint64_t)nt, S, A, T, DP});
 		B.i(gp + "pop", popt, {(uint64_t)nt, S, A, C, DP});
+	}
+	if (opt.count("pred")) {
+		// Prediction (Simulate::model_modification, src/simulate.cc:142-165): each posterior
+		// sample <pred>/sample<k> is loaded (State::load, src/state.cc:743-808) and simulated
+		// from the modifications' start to the end (State::simulate(ti, tf)) under the
+		// model's modifications, on stream 7000 + k.
+		const std::string dir = opt["pred"] + "/";
+		const int K = opt.count("predn") ? atoi(opt["predn"].c_str()) : 1;
+		const unsigned ti = model.modelmod.pred_start * details.division_per_time;
+		B.scalar_i("pred.n", K);
+		B.scalar_i("pred.ti", (int32_t)ti);
+		State st(details, data, model, obsmodel);
+		for (int k = 0; k < K; k++) {
+			const std::string pk = "pred" + std::to_string(k) + ".";
+			st.load(dir + "sample" + std::to_string(k), S);
+			B.d(pk + "theta", st.paramval);
+			dump_tables(pk, st, st.paramval);
+			std::vector<int32_t> p0, tn, p1;
+			for (unsigned c = 0; c < A; c++)
+				for (unsigned co = 0; co < C; co++)
+					for (unsigned dp = 0; dp < DP; dp++) p0.push_back((int32_t)st.pop[ti][c][co][dp]);
+			g_replay.mbp = false; g_replay.st = &st; g_replay.stream = 7000u + k;
+			g_replay.sett = ti; g_replay.c = 0; g_replay.tr = 0; g_replay.dp = 0;
+			g_replay.active = true;
+			st.simulate(ti, S);
+			g_replay.active = false;
+			for (unsigned s2 = ti; s2 < S; s2++)
+				for (unsigned c = 0; c < A; c++)
+					for (unsigned tr = 0; tr < T; tr++)
+						for (unsigned dp = 0; dp < DP; dp++) tn.push_back((int32_t)st.transnum[s2][c][tr][dp]);
+			for (unsigned c = 0; c < A; c++)
+				for (unsigned co = 0; co < C; co++)
+					for (unsigned dp = 0; dp < DP; dp++) p1.push_back((int32_t)st.pop[S][c][co][dp]);
+			B.i(pk + "pop_ti", p0, {A, C, DP});
+			B.i(pk + "transnum", tn, {(uint64_t)(S - ti), A, T, DP});
+			B.i(pk + "pop_end", p1, {A, C, DP});
+			B.i(pk + "stream", {(int32_t)(7000 + k)});
+		}
 	}
 	if (opt.count("mbp")) {
 		// MBP chains (src/mbp.cc:252-361,460-491, src/state.cc:812-826).  Chain k

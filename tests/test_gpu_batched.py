@@ -65,7 +65,7 @@ def test_batched_follows_fp64_trajectories(built, case):
     P = 40
     g = dm.simulate(capi.Batch(m, tabs, P, 9, want_transnum=True, want_pop=True))
     db = _batched(dm, m, tabs, P, 9, want_transnum=True, want_pop=True)
-    assert db.launches() == 2 * m.ndivision + 2
+    assert db.launches() == 3 * m.ndivision + 2          # per step: product, step kernel, observations
     f = db.run()
     db.close()
     same = np.array([np.array_equal(f.transnum[p], g.transnum[p]) for p in range(P)])
