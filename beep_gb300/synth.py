@@ -61,6 +61,9 @@ class Workload:
     # R factor values/priors as TOML strings, and the exposed seeds of each strain
     # [NS][A][G] (the susceptibles start in the first strain)
     strains: Optional[dict] = None
+    # model modifications of the reference's prediction mode (TOML `modification`): dicts
+    # of its keys, e.g. {"type": "beta_fac", "start": "36", "end": "50", "factor": "0.5"}
+    modifications: List[dict] = dataclasses.field(default_factory=list)
     # prior ranges (inference modes)
     R_prior: tuple = (0.5, 4.0)
     sigma_inv_prior: tuple = (2.0, 6.0)
@@ -259,6 +262,11 @@ def write_beep_inputs(w: Workload, outdir: str, obs_values: Optional[dict] = Non
                          f'param="{names}", '
                          f'value="{"|".join(_fmt(v) for v in mm["val"])}", '
                          f'prior="{"|".join(f"Fixed({_fmt(v)})" for v in mm["val"])}"}},')
+        lines.append("]")
+    if w.modifications:
+        lines.append("modification = [")
+        for mod in w.modifications:
+            lines.append("{" + ", ".join(f'{k}="{v}"' for k, v in mod.items()) + "},")
         lines.append("]")
     lines.append("data_tables = [")
     for tab in tables:

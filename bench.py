@@ -846,7 +846,7 @@ def main():
                     help="sweeps of the MBP-chain workload (4 x 128 chains of uneven size) after the main measurement")
     ap.add_argument("--pf-estimates", type=int, default=10,
                     help="particle-filter likelihood estimates (256 particles, 10 x 3 model) per form after the main measurement")
-    ap.add_argument("--serve-requests", type=int, default=160,
+    ap.add_argument("--serve-requests", type=int, default=128,
                     help="requests of the serving stream (Poisson arrivals at 200/s) after the main measurement")
     ap.add_argument("--serve-sustained", type=int, default=16,
                     help="requests of the same stream at a rate the GPU sustains (latency without queueing)")

@@ -616,9 +616,18 @@ int main(int argc, char **argv)
 				for (unsigned c = 0; c < A; c++)
 					for (unsigned tr = 0; tr < T; tr++)
 						for (unsigned dp = 0; dp < DP; dp++) tn.push_back((int32_t)st.transnum[s2][c][tr][dp]);
-			for (unsigned c = 0; c < A; c++)
+			// the populations after the last step (State::simulate updates them only up to
+			// the last step's start): update_pop's arithmetic on the last step's counts
+			for (unsigned c = 0; c < A; c++) {
+				auto pe = st.pop[S - 1][c];
+				for (unsigned tr = 0; tr < T; tr++)
+					for (unsigned dp = 0; dp < DP; dp++) {
+						const double num = st.transnum[S - 1][c][tr][dp];
+						if (num != 0) { pe[model.trans[tr].from][dp] -= num; pe[model.trans[tr].to][dp] += num; }
+					}
 				for (unsigned co = 0; co < C; co++)
-					for (unsigned dp = 0; dp < DP; dp++) p1.push_back((int32_t)st.pop[S][c][co][dp]);
+					for (unsigned dp = 0; dp < DP; dp++) p1.push_back((int32_t)pe[co][dp]);
+			}
 			B.i(pk + "pop_ti", p0, {A, C, DP});
 			B.i(pk + "transnum", tn, {(uint64_t)(S - ti), A, T, DP});
 			B.i(pk + "pop_end", p1, {A, C, DP});

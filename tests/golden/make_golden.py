@@ -171,6 +171,56 @@ def make_fixture(name, w: synth.Workload, npart, ntraj, seed, pf=False, theta_ro
         shutil.rmtree(work, ignore_errors=True)
 
 
+def make_prediction_fixture(name, w: synth.Workload, ngroup, npart, seed):
+    """Prediction with model modifications (the reference's mode=prediction,
+    src/simulate.cc:142-165, src/model.cc:1446-1585): posterior samples are the
+    reference's own trajectories of ngroup parameter rows x npart particles
+    (run without modifications), written as BEEP sample files by
+    beep_gb300.samples; the reference then loads each sample and simulates it
+    from the modifications' start to the end.  The bundle also holds a full
+    simulation of the workload's own parameter values under the modifications
+    (g0.*) with the multiplier tables."""
+    from beep_gb300 import samples
+    if ONLY is not None and name not in ONLY:
+        return
+    work = tempfile.mkdtemp(prefix=f"golden_{name}_")
+    try:
+        toml = synth.write_beep_inputs(w, work)
+        b0 = run_harness(work, toml, os.path.join(work, "b0.bnd"), 1, 1, seed + 1, "abcsmc")
+        synth.write_beep_inputs(w, work, obs_values=obs_values_from(b0, w))
+        # posterior samples: ngroup parameter rows around the workload's values, npart trajectories each
+        base = b0["g0.theta"]
+        rows = mbp_theta_rows(base, (ngroup + 1) // 2, w.seed)[:ngroup]
+        theta = os.path.join(work, "theta.csv")
+        with open(theta, "w") as f:
+            for row in rows:
+                f.write(",".join(repr(float(x)) for x in row) + "\n")
+        bs = run_harness(work, toml, os.path.join(work, "bs.bnd"), npart, npart, seed + 2, "abcsmc", theta=theta)
+        names = bytes(bs["param_names"].astype(np.uint8)).decode().split("\n")[:-1]
+        sdir = os.path.join(work, "samples")
+        os.makedirs(sdir)
+        dims = [int(x) for x in bs["dims"]]
+        period, S = dims[7], dims[6]
+        times = samples.division_times(period, S, start=0.0)
+        k = 0
+        for g in range(ngroup):
+            for p in range(npart):
+                # EF is written as 0: State::save prints doubles %g-style and State::load's number
+                # parser rejects the exponent form an EF above 1e6 takes (the prediction does not use it)
+                samples.write_sample(sdir, k, 0.0, names, bs[f"g{g}.theta"], bs[f"g{g}.transnum"][p], times)
+                k += 1
+        out = os.path.join(HERE, f"{name}.bnd")
+        cmd = [HARNESS, f"out={out}", "npart=4", "ntraj=2", f"seed={seed}", "pf=0", f"pred={sdir}",
+               f"predn={ngroup * npart}", "--", f"inputfile={os.path.basename(toml)}", "mode=prediction",
+               f"prediction_end={w.days}"]   # the inference horizon: the splines keep their knots
+        r = subprocess.run(cmd, cwd=work, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"harness failed:\n{r.stdout}\n{r.stderr}")
+        print(f"{name}: {os.path.getsize(out) / 1e3:.0f} kB")
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("BEEP_REF_DIR") or os.path.join(os.path.dirname(ROOT), "reference"))
@@ -218,6 +268,16 @@ def main():
     make_fixture("c0_mbp", c0, npart=1, ntraj=0, seed=20260003, mbp=4)
     # ABC-SMC importance weights: 40 previous-generation samples, 24 new ones
     make_fixture("c0_abcw", c0, npart=1, ntraj=0, seed=20260004, abcw=(24, 40))
+    # prediction with model modifications: a transition-rate factor on some areas, a beta
+    # factor over a window, an external-FOI factor (src/model.cc:1495-1580); the time-varying
+    # tables of the features workload (covariates, stepped age mixing, external FOI)
+    pw = synth.seir_hd_features(seed=20260107, days=60, name="pred")
+    pw.modifications = [
+        {"type": "trans_rate_fac", "trans": "E->I", "start": "30", "factor": "0.6", "geo_filt": "area:A1|A3"},
+        {"type": "beta_fac", "start": "36", "end": "50", "factor": "0.5"},
+        {"type": "efoi_fac", "start": "30", "factor": "2.5", "geo_filt": "area:A0|A2|A4"},
+    ]
+    make_prediction_fixture("pred_sim", pw, ngroup=2, npart=2, seed=0x9E7D)
 
 
 if __name__ == "__main__":

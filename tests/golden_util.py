@@ -8,7 +8,7 @@ import numpy as np
 from beep_gb300 import bundle, capi
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-FIXTURES = ["tiny_sim", "oneage_sim", "c0_sim", "strain_sim", "obsmodel_sim", "features_sim"]
+FIXTURES = ["tiny_sim", "oneage_sim", "c0_sim", "strain_sim", "obsmodel_sim", "features_sim", "pred_sim"]
 PF_FIXTURES = ["tiny_pf", "c0_pf", "features_pf"]
 MBP_FIXTURES = ["tiny_mbp", "c0_mbp"]
 MBP_VARIANTS = 3   # 0 INF_DIF_UPDATE, 1 INF_UPDATE, 2 INF_DIF_UPDATE with SIMU cells
@@ -19,6 +19,20 @@ def load(name):
     m, tabs = capi.load_model_bundle(b)
     seed = int(np.uint32(b["seed_words"][0])) | (int(np.uint32(b["seed_words"][1])) << 32)
     return b, m, tabs, seed
+
+
+def prediction_runs(b):
+    """The loaded-sample prediction runs of a prediction fixture: per sample k its
+    tables (with the modifications' multipliers), start step, start populations
+    [A][C][DP], stream, and the reference's counts [S-ti][A][T][DP] and final
+    populations."""
+    ti = int(b["pred.ti"][0])
+    out = []
+    for k in range(int(b["pred.n"][0])):
+        p = f"pred{k}."
+        out.append(dict(tables=capi.Tables(b, p), ti=ti, pop_ti=b[p + "pop_ti"], stream=int(b[p + "stream"][0]),
+                        transnum=b[p + "transnum"], pop_end=b[p + "pop_end"]))
+    return out
 
 
 def checksums(transnum, pop):

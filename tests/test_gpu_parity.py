@@ -216,3 +216,27 @@ def test_negative_binomial_observations_match_oracle(built):
     assert same.mean() >= 0.6, same.mean()
     np.testing.assert_allclose(f.L[same], g.L[same], rtol=1e-6)
     dm.close()
+
+
+def test_prediction_from_loaded_samples_matches_reference(built):
+    """The reference's prediction mode on samples written by beep_gb300.samples
+    (State::load, then State::simulate from the modifications' start under the
+    modification multipliers, src/simulate.cc:142-165, src/state.cc:415,446-453):
+    the plain form, started from the loaded populations, gives the reference's
+    counts and final populations bit for bit; the fast form follows them."""
+    from golden_util import prediction_runs
+    b, m, tabs, seed = load("pred_sim")
+    dm = capi.DeviceModel(m)
+    runs = prediction_runs(b)
+    for r in runs:
+        g = dm.simulate(capi.Batch(m, [r["tables"]], 1, seed, ti=r["ti"], pop_in=r["pop_ti"][None],
+                                   stream_of=[r["stream"]], want_transnum=True, want_pop=True))
+        assert np.array_equal(g.transnum[0], r["transnum"])
+        assert np.array_equal(g.pop[0], r["pop_end"])
+    same = 0
+    for r in runs:
+        f = dm.simulate(capi.Batch(m, [r["tables"]], 1, seed, ti=r["ti"], pop_in=r["pop_ti"][None],
+                                   stream_of=[r["stream"]], want_transnum=True, form=capi.FORM_FAST))
+        same += int(np.array_equal(f.transnum[0], r["transnum"]))
+    assert same >= len(runs) // 2, same
+    dm.close()

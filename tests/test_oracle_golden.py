@@ -84,3 +84,22 @@ def test_oracle_particle_filter_matches_reference(name):
     np.testing.assert_allclose(L, b["g0.pf.L_section"], rtol=L_RTOL, atol=1e-12)
     np.testing.assert_allclose(lls, b["g0.pf.obprob_section"], rtol=L_RTOL, atol=1e-12)
     np.testing.assert_allclose(ll, b["g0.pf.obprob"][0], rtol=L_RTOL)
+
+
+def test_oracle_prediction_from_loaded_samples_matches_reference():
+    """The reference's prediction mode (src/simulate.cc:142-165): posterior
+    samples written by beep_gb300.samples, loaded by State::load and simulated
+    from the modifications' start under the model modifications (transition-rate,
+    beta and external-FOI factors, src/model.cc:1495-1580).  The oracle, started
+    from the loaded populations with the same tables and stream, gives the same
+    counts and final populations."""
+    from golden_util import prediction_runs
+    b, m, tabs, seed = load("pred_sim")
+    runs = prediction_runs(b)
+    assert runs and runs[0]["ti"] > 0
+    for r in runs:
+        bt = capi.Batch(m, [r["tables"]], 1, seed, ti=r["ti"], pop_in=r["pop_ti"][None], stream_of=[r["stream"]],
+                        want_transnum=True, want_pop=True)
+        oracle_simulate(m, bt)
+        assert np.array_equal(bt.transnum[0], r["transnum"])
+        assert np.array_equal(bt.pop[0], r["pop_end"])
