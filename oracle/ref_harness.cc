@@ -62,6 +62,8 @@
 #include "utils.hh"
 #include "timers.hh"
 
+#include "beep_binding.hh"
+
 extern "C" {
 #include "beep_rng_ref.h"
 }
@@ -309,77 +311,19 @@ int main(int argc, char **argv)
 	             (int32_t)details.period, (int32_t)details.division_per_time});
 	B.scalar_d("dt", double(details.period) / details.ndivision);
 	B.scalar_d("popsize", (double)data.popsize);
-	std::vector<int32_t> tf(T), tt(T);
-	for (unsigned tr = 0; tr < T; tr++) { tf[tr] = model.trans[tr].from; tt[tr] = model.trans[tr].to; }
-	B.i("trans_from", tf); B.i("trans_to", tt);
-	B.scalar_i("infection_trans", (int32_t)model.infection_trans);
-	std::vector<int32_t> dpage(DPS);
-	for (unsigned dp = 0; dp < DPS; dp++) dpage[dp] = data.democatpos[dp][0];
-	B.i("democatpos_age", dpage);
-	{
-		std::vector<double> diag(A), val, fac(A);
-		std::vector<int32_t> rowptr(A + 1, 0), to;
-		for (unsigned c = 0; c < A; c++) {
-			diag[c] = data.genQ.M.diag[c];
-			fac[c] = data.genQ.factor[c];
-			for (unsigned j = 0; j < data.genQ.M.to[c].size(); j++) {
-				to.push_back(data.genQ.M.to[c][j]);
-				val.push_back(data.genQ.M.val[c][j]);
-			}
-			rowptr[c + 1] = (int32_t)to.size();
-		}
-		B.d("M_diag", diag); B.i("M_rowptr", rowptr); B.i("M_to", to); B.d("M_val", val); B.d("M_factor", fac);
-	}
-	{
-		std::vector<double> pi((size_t)A * C * DP);
-		for (unsigned c = 0; c < A; c++)
-			for (unsigned co = 0; co < C; co++)
-				for (unsigned dp = 0; dp < DP; dp++) pi[((size_t)c * C + co) * DP + dp] = data.area[c].pop_init[co][dp];
-		B.d("pop_init", pi, {A, C, DP});
-	}
-	// observations; cells in the order the reference visits them (src/obsmodel.cc:74-109)
-	std::map<unsigned, int32_t> spline_row;
-	std::vector<unsigned> spline_rows;
-	{
-		unsigned nobs = data.nobs;
-		std::vector<int32_t> si(nobs), sf(nobs), kind(nobs), mdl(nobs), fspl(nobs), cptr(nobs + 1, 0), cells;
-		std::vector<double> val(nobs), sd(nobs), shape(nobs), thr(nobs), fac(nobs);
-		for (unsigned i = 0; i < nobs; i++) {
-			const auto &ob = data.obs[i];
-			si[i] = ob.sett_i; sf[i] = ob.sett_f;
-			kind[i] = ob.value == UNKNOWN ? 1 : (ob.value == THRESH ? 2 : 0);
-			val[i] = ob.value; sd[i] = ob.sd; shape[i] = ob.shape;
-			thr[i] = data.datatable[ob.datatable].threshold;
-			fac[i] = ob.factor; mdl[i] = (int32_t)ob.obsmodel;
-			if (ob.factor_spline == UNSET) fspl[i] = -1;
-			else {
-				if (!spline_row.count(ob.factor_spline)) {
-					spline_row[ob.factor_spline] = (int32_t)spline_rows.size();
-					spline_rows.push_back(ob.factor_spline);
-				}
-				fspl[i] = spline_row[ob.factor_spline];
-			}
-			struct K { unsigned c, kind, x, dp; int32_t cell; };
-			std::vector<K> ks;
-			const auto &dtab = data.datatable[ob.datatable];
-			for (auto c : ob.area)
-				for (auto dp : ob.dp_sel) {
-					for (auto tr : dtab.translist) ks.push_back({c, 0, tr, dp, (int32_t)((c * T + tr) * DP + dp)});
-					for (auto co : dtab.complist) ks.push_back({c, 1, co, dp, (int32_t)(-1 - (int32_t)((c * C + co) * DP + dp))});
-				}
-			std::stable_sort(ks.begin(), ks.end(), [](const K &a, const K &b) {
-				if (a.c != b.c) return a.c < b.c;
-				if (a.kind != b.kind) return a.kind < b.kind;
-				if (a.x != b.x) return a.x < b.x;
-				return a.dp < b.dp;
-			});
-			for (auto &k : ks) cells.push_back(k.cell);
-			cptr[i + 1] = (int32_t)cells.size();
-		}
-		B.i("obs_sett_i", si); B.i("obs_sett_f", sf); B.i("obs_value_kind", kind); B.d("obs_value", val);
-		B.i("obs_model", mdl); B.d("obs_sd", sd); B.d("obs_shape", shape); B.d("obs_threshold", thr);
-		B.d("obs_factor", fac); B.i("obs_factor_spline", fspl); B.i("obs_cell_ptr", cptr); B.i("obs_cells", cells);
-	}
+	// the model through the binding a BEEP maintainer adds (beep_gb300/binding): the bundle
+	// holds exactly what it packs for beep_model_create
+	const beep_binding::ModelPack mp(details, data, model);
+	B.i("trans_from", mp.trans_from); B.i("trans_to", mp.trans_to);
+	B.scalar_i("infection_trans", mp.desc.infection_trans);
+	B.i("democatpos_age", mp.democatpos_age);
+	B.d("M_diag", mp.M_diag); B.i("M_rowptr", mp.M_rowptr); B.i("M_to", mp.M_to); B.d("M_val", mp.M_val);
+	B.d("M_factor", mp.M_factor);
+	B.d("pop_init", mp.pop_init, {A, C, DP});
+	B.i("obs_sett_i", mp.obs_sett_i); B.i("obs_sett_f", mp.obs_sett_f); B.i("obs_value_kind", mp.obs_value_kind);
+	B.d("obs_value", mp.obs_value); B.i("obs_model", mp.obs_model); B.d("obs_sd", mp.obs_sd);
+	B.d("obs_shape", mp.obs_shape); B.d("obs_threshold", mp.obs_threshold); B.d("obs_factor", mp.obs_factor);
+	B.i("obs_factor_spline", mp.obs_factor_spline); B.i("obs_cell_ptr", mp.obs_cell_ptr); B.i("obs_cells", mp.obs_cells);
 	if (pf) {
 		std::vector<int32_t> sti, stf;
 		for (unsigned s = 0; s < obsmodel.nsection; s++) { sti.push_back(obsmodel.section_ti[s]); stf.push_back(obsmodel.section_tf[s]); }
@@ -405,61 +349,22 @@ int main(int argc, char **argv)
 	// the tables State::set_param produced for parameter set theta (beep_param_tables), and in
 	// prediction mode the model modifications' multipliers (ModelMod, src/model.cc:1446-1585)
 	auto dump_tables = [&](const std::string &gp, const State &state, const std::vector<double> &theta) {
-			std::vector<double> v;
-			for (unsigned tr = 0; tr < T; tr++) {
-				if (state.transrate[tr].size() == DP) for (unsigned dp = 0; dp < DP; dp++) v.push_back(state.transrate[tr][dp]);
-				else for (unsigned dp = 0; dp < DP; dp++) v.push_back(0.0);   // infection transition: no rate
-			}
-			B.d(gp + "transrate", v, {T, DP});
-			B.d(gp + "susceptibility", state.susceptibility);
-			std::vector<double> inf(C);
-			for (unsigned co = 0; co < C; co++) inf[co] = theta[model.comp[co].infectivity_param];
-			B.d(gp + "infectivity", inf);
-			// beta rows, deduplicated by content (the reference copies one row per R-spline to its areas, src/model.cc:1339-1345)
-			std::vector<std::vector<double>> rows;
-			std::vector<int32_t> rowof(NS * A);
-			for (unsigned st = 0; st < NS; st++)
-				for (unsigned c = 0; c < A; c++) {
-					const auto &r = state.beta[st][c];
-					unsigned k = 0;
-					while (k < rows.size() && rows[k] != r) k++;
-					if (k == rows.size()) rows.push_back(r);
-					rowof[st * A + c] = (int32_t)k;
-				}
-			std::vector<double> br;
-			for (auto &r : rows) br.insert(br.end(), r.begin(), r.end());
-			B.d(gp + "beta_rows", br, {rows.size(), S});
-			B.i(gp + "beta_row_of", rowof, {NS, A});
-			std::vector<double> af;
-			for (unsigned t = 0; t < details.period; t++) af.insert(af.end(), state.areafactor[t].begin(), state.areafactor[t].end());
-			B.d(gp + "areafactor", af, {details.period, A});
-			std::vector<double> nt;
-			for (unsigned s = 0; s < S; s++) for (unsigned a = 0; a < G; a++) nt.insert(nt.end(), state.Ntime[s][a].begin(), state.Ntime[s][a].end());
-			B.d(gp + "Ntime", nt, {S, G, G});
-			B.d(gp + "geo_spline", state.disc_spline[model.geo_spline_ref]);
-			std::vector<double> es, ea;
-			for (auto &info : model.efoispline_info) {
-				es.insert(es.end(), state.disc_spline[info.spline_ref].begin(), state.disc_spline[info.spline_ref].end());
-				ea.insert(ea.end(), info.efoi_agedist.begin(), info.efoi_agedist.end());
-			}
-			B.d(gp + "efoi_spline", es, {model.efoispline_info.size(), S});
-			B.d(gp + "efoi_agedist", ea, {model.efoispline_info.size(), G});
-			std::vector<int32_t> er;
-			for (unsigned st = 0; st < NS; st++) for (unsigned c = 0; c < A; c++) er.push_back(model.efoi_spl_ref[st][c]);
-			B.i(gp + "efoi_ref", er, {NS, A});
-			std::vector<double> os;
-			for (auto spl : spline_rows) os.insert(os.end(), state.disc_spline[spl].begin(), state.disc_spline[spl].end());
-			B.d(gp + "obs_spline", os, {spline_rows.size(), S});
-		if (details.mode == PREDICTION) {
-			std::vector<double> em, tm;
-			for (unsigned s = 0; s < S; s++)
-				for (unsigned c = 0; c < A; c++) {
-					for (unsigned st = 0; st < NS; st++) em.push_back(model.modelmod.efoi_mult[s][c][st]);
-					for (unsigned tr = 0; tr < T; tr++)
-						for (unsigned dp = 0; dp < DP; dp++) tm.push_back(model.modelmod.transmean_mult[s][c][tr][dp]);
-				}
-			B.d(gp + "efoi_mult", em, {S, A, NS});
-			B.d(gp + "transmean_mult", tm, {S, A, T, DP});
+		const beep_binding::TablePack tp(mp, details, data, model, state, theta);
+		B.d(gp + "transrate", tp.transrate, {T, DP});
+		B.d(gp + "susceptibility", tp.susceptibility);
+		B.d(gp + "infectivity", tp.infectivity);
+		B.d(gp + "beta_rows", tp.beta_rows, {(uint64_t)tp.tables.nbeta_row, S});
+		B.i(gp + "beta_row_of", tp.beta_row_of, {NS, A});
+		B.d(gp + "areafactor", tp.areafactor, {details.period, A});
+		B.d(gp + "Ntime", tp.Ntime, {S, G, G});
+		B.d(gp + "geo_spline", tp.geo_spline);
+		B.d(gp + "efoi_spline", tp.efoi_spline, {(uint64_t)tp.tables.nefoi, S});
+		B.d(gp + "efoi_agedist", tp.efoi_agedist, {(uint64_t)tp.tables.nefoi, G});
+		B.i(gp + "efoi_ref", tp.efoi_ref, {NS, A});
+		B.d(gp + "obs_spline", tp.obs_spline, {(uint64_t)tp.tables.nobs_spline, S});
+		if (!tp.efoi_mult.empty()) {
+			B.d(gp + "efoi_mult", tp.efoi_mult, {S, A, NS});
+			B.d(gp + "transmean_mult", tp.transmean_mult, {S, A, T, DP});
 		}
 	};
 

@@ -125,7 +125,7 @@ ONLY = None   # fixture names to (re)generate (--only); None: all
 
 
 def make_fixture(name, w: synth.Workload, npart, ntraj, seed, pf=False, theta_rows=None, keep_dir=None, pfn=0,
-                 mbp=0, samples=False, abcw=None):
+                 mbp=0, samples=False, abcw=None, outdir=HERE):
     if ONLY is not None and name not in ONLY:
         return
     work = tempfile.mkdtemp(prefix=f"golden_{name}_")
@@ -150,7 +150,7 @@ def make_fixture(name, w: synth.Workload, npart, ntraj, seed, pf=False, theta_ro
             with open(theta, "w") as f:
                 for row in mbp_theta_rows(base, nrow_pairs, w.seed):
                     f.write(",".join(repr(float(x)) for x in row) + "\n")
-        out = os.path.join(HERE, f"{name}.bnd")
+        out = os.path.join(outdir, f"{name}.bnd")
         sdir = os.path.join(work, "samples") if samples else None
         if sdir:
             os.makedirs(sdir)
@@ -163,7 +163,7 @@ def make_fixture(name, w: synth.Workload, npart, ntraj, seed, pf=False, theta_ro
         if sdir:
             # the reference's own sample files of the sampled lineage
             for f in sorted(os.listdir(sdir)):
-                shutil.copy(os.path.join(sdir, f), os.path.join(HERE, f"{name}_{f}"))
+                shutil.copy(os.path.join(sdir, f), os.path.join(outdir, f"{name}_{f}"))
         if keep_dir:
             shutil.copytree(work, os.path.join(keep_dir, name), dirs_exist_ok=True)
         print(f"{name}: {os.path.getsize(out) / 1e3:.0f} kB")
