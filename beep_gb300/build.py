@@ -28,6 +28,7 @@ UNITS = {
     "sim_plain.cu": ["--fmad=false"],
     "sim_fast.cu": [],
     "sim_fast_ctas.cu": [],
+    "sim_fast_wide.cu": [],
     "sim_batched.cu": [],
     "noalloc.cu": [],
     "pf.cu": [],

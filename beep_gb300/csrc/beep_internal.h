@@ -62,6 +62,7 @@ struct BatchDev {
 	const int32_t *ipool;
 	const int32_t *group_of;            // [P] or null
 	const uint32_t *stream_of;          // [P] or null
+	const uint2 *key_of;                // [P] Philox key (seed words) of each particle, or null: (k0, k1) for all
 	const int32_t *pop_in;              // [P][A][C][DP] or null (ti == 0)
 	// scored observations and their per-step activity
 	int32_t nscored;
@@ -144,6 +145,11 @@ int fast_ctas_max(int G);                        // most 320-thread CTAs per SM 
 int launch_sim_fast_ctas(const ModelDev &m, const BatchDev &b, size_t smem, void *stream);   // sim_fast_ctas.cu
 int fast_chain_ctas_prepare();                   // constant tables of mbp_fast_ctas.cu
 int launch_sim_fast_chain_ctas(const ModelDev &m, const BatchDev &b, size_t smem, void *stream);   // mbp_fast_ctas.cu
+// fast form for models with more than 8 transitions or 16 age groups (sim_fast_wide.cu)
+bool fast_wide_needed(const ModelDev &m);
+bool fast_wide_supported(const ModelDev &m);   // up to 16 transitions and 20 age groups
+int fast_wide_prepare();
+int launch_sim_fast_wide(const ModelDev &m, const BatchDev &b, size_t smem, void *stream);
 // step-synchronous fast form (sim_batched.cu)
 bool batched_supported(const ModelDev &m);
 size_t batched_step_smem(const ModelDev &m, int tnrows);

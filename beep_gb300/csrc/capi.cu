@@ -514,6 +514,7 @@ beep_status stage_inputs(beep_batch *q)
 	       o_f32 = in.add(fast ? 4 * pk.fsize : 0),
 	       o_i = in.add(4 * pk.i.size()), o_go = in.add(b->group_of ? 4 * (size_t)P : 0),
 	       o_so = in.add(b->stream_of ? 4 * (size_t)P : 0), o_pin = in.add(b->ti > 0 && !q->device_io ? 4 * popsz * P : 0),
+	       o_key = in.add(8 * q->keys.size()),
 	       o_sc = in.add(4 * q->scored.size()), o_sp = in.add(4 * q->step_ptr.size()),
 	       o_sobs = in.add(4 * q->step_obs.size()), o_tasks = in.add(4 * q->tasks.size());
 	CUDA_TRY(q->in_host.reserve(in.size));
@@ -525,6 +526,7 @@ beep_status stage_inputs(beep_batch *q)
 	if (!pk.i.empty()) memcpy(h + o_i, pk.i.data(), 4 * pk.i.size());
 	if (b->group_of) memcpy(h + o_go, b->group_of, 4 * (size_t)P);
 	if (b->stream_of) memcpy(h + o_so, b->stream_of, 4 * (size_t)P);
+	if (!q->keys.empty()) memcpy(h + o_key, q->keys.data(), 8 * q->keys.size());
 	if (b->ti > 0 && !q->device_io) memcpy(h + o_pin, b->pop_in, 4 * popsz * P);
 	if (!q->scored.empty()) memcpy(h + o_sc, q->scored.data(), 4 * q->scored.size());
 	memcpy(h + o_sp, q->step_ptr.data(), 4 * q->step_ptr.size());
@@ -571,6 +573,7 @@ beep_status stage_inputs(beep_batch *q)
 	bd.ipool = (const int32_t *)(di + o_i);
 	bd.group_of = b->group_of ? (const int32_t *)(di + o_go) : nullptr;
 	bd.stream_of = b->stream_of ? (const uint32_t *)(di + o_so) : nullptr;
+	bd.key_of = q->keys.empty() ? nullptr : (const uint2 *)(di + o_key);
 	bd.pop_in = b->ti > 0 && !q->device_io ? (const int32_t *)(di + o_pin) : nullptr;
 	bd.scored = (const int32_t *)(di + o_sc);
 	bd.step_ptr = (const int32_t *)(di + o_sp);
@@ -594,7 +597,7 @@ beep_status beep_batch_create(beep_model *m, const beep_sim_batch *b, beep_batch
 }  // extern "C"
 
 beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, bool device_io, beep_batch **out,
-                                        bool device_traj, bool allow_tc, bool allow_ctas)
+                                        bool device_traj, bool allow_tc, bool allow_ctas, const std::vector<uint2> *keys)
 {
 	// a count trajectory is written: to the batch's output (transnum_out), or to a
 	// device buffer the caller sets in bd.tn_traj before each launch (device_traj)
@@ -604,10 +607,12 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 	beep_status st = check_batch(m, b, device_io);
 	if (st != BEEP_OK) return st;
 	CUDA_TRY(cudaSetDevice(m->device));
+	if (keys && keys->size() != (size_t)b->nparticle) return fail(BEEP_BAD_INPUT, "one key per particle");
 	beep_batch *q = new beep_batch();
 	q->m = m;
 	q->b = *b;
 	q->device_io = device_io;
+	if (keys) q->keys = *keys;
 	const int P = b->nparticle;
 	const size_t popsz = (size_t)m->A * m->C * m->DP, tnsz = (size_t)m->A * m->T * m->DP;
 	const size_t agsz = (size_t)m->NS * m->A * m->G;
@@ -679,18 +684,23 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 		q->bd.pop_single = (!m->dev.pop_obs && m->NS == 1 && !b->pop_traj_out) ? 1 : 0;
 		const int tnrows = q->bd.tn_full ? m->T : m->dev.tn_rows;
 		const bool ps = q->bd.pop_single != 0;
-		q->state_global = fast_smem_bytes(m->dev, nslots, false, q->bd.nefoi_stage, false, tnrows, ps) > limit;
-		if (fast_smem_bytes(m->dev, nslots, false, q->bd.nefoi_stage, true, tnrows, ps) > limit || m->NS * m->A > 640 ||
-		    m->G * m->G > 640 || m->T > 8) {
+		// models with more than 8 transitions or 16 age groups: the wide instantiation,
+		// one 640-thread CTA per SM with the FOI on FP32 SIMT (sim_fast_wide.cu)
+		const bool wide = fast_wide_needed(m->dev);
+		const int nt0 = wide ? 640 : 0;
+		q->state_global = fast_smem_bytes(m->dev, nslots, false, q->bd.nefoi_stage, false, tnrows, ps, false, nt0) > limit;
+		if (fast_smem_bytes(m->dev, nslots, false, q->bd.nefoi_stage, true, tnrows, ps, false, nt0) > limit ||
+		    m->NS * m->A > 640 || m->G * m->G > 640 || (wide && !fast_wide_supported(m->dev))) {
 			delete q;
-			return fail(BEEP_BAD_INPUT, "model too large for the fast form (observation slots or tables exceed shared memory, or more than 8 transitions)");
+			return fail(BEEP_BAD_INPUT, "model too large for the fast form (observation slots or tables exceed shared memory, or more than 16 transitions or 20 age groups)");
 		}
-		q->bd.m_in_smem = fast_smem_bytes(m->dev, nslots, true, q->bd.nefoi_stage, q->state_global, tnrows, ps) <= limit ? 1 : 0;
+		if (wide) q->bd.nt = 640;
+		q->bd.m_in_smem = fast_smem_bytes(m->dev, nslots, true, q->bd.nefoi_stage, q->state_global, tnrows, ps, false, nt0) <= limit ? 1 : 0;
 		// force of infection on the tensor cores, batched over the particles: every particle
 		// advances one step at a time and the contraction is one product over the batch per
 		// step (sim_batched.cu); the default for large models
 		const int opt = option_fast_foi() != 0 ? option_fast_foi() : m->tuned_foi;
-		const bool can_bx = allow_tc && batched_supported(m->dev) &&
+		const bool can_bx = allow_tc && !wide && batched_supported(m->dev) &&
 		                    batched_step_smem(m->dev, tnrows) <= limit;
 		if (can_bx && (opt == 3 || (opt == 0 && m->A >= 300))) {
 			q->bd.batched = 1;
@@ -700,7 +710,7 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 		// force of infection on the tensor cores, one particle per CTA: large models (the
 		// matrix is streamed from L2 each step; the particle's populations and counts move to
 		// global memory to make room for the operand ring)
-		const bool can_tc = allow_tc && m->dev.tc_image != nullptr && fast_pick_threads(m->dev) == 640;
+		const bool can_tc = allow_tc && !wide && m->dev.tc_image != nullptr && fast_pick_threads(m->dev) == 640;
 		const bool want_tc = opt == 2 || (opt == 0 && m->A >= 300 && !can_bx);
 		if (!q->bd.batched && can_tc && want_tc) {
 			// the transition counts stay on chip when they fit beside the operand ring
@@ -727,7 +737,8 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 		const int forced = option_fast_ctas();
 		const int pref = forced != 0 ? 0 : m->tuned_ctas;
 		const bool asked = forced >= 2 || pref >= 2;
-		if (allow_ctas && !q->bd.foi_tc && !q->bd.batched && forced != 1 && pref != 1 && fast_pick_threads(m->dev) == 640) {
+		if (allow_ctas && !wide && !q->bd.foi_tc && !q->bd.batched && forced != 1 && pref != 1 &&
+		    fast_pick_threads(m->dev) == 640) {
 			const int kmax = std::min(forced >= 2 ? forced : 4, fast_ctas_max(m->G));
 			const int kmin = asked ? 2 : 3;
 			auto fit = [&](size_t bytes) { return (int)std::min<size_t>((size_t)kmax, kSmemPerSM / (bytes + 1024)); };

@@ -129,6 +129,7 @@ struct beep_batch {
 	size_t in_size = 0, out_size = 0;
 	size_t o_f = 0, u_st = 0, u_L = 0, u_po = 0, u_tn = 0, u_pt = 0;
 	std::vector<beep::GroupDir> dirs;
+	std::vector<uint2> keys;           // per-particle Philox keys (requests packed into one batch), or empty
 	std::vector<int32_t> scored, step_ptr, step_obs, slot_of, tasks;
 	beep::BatchDev bd{};
 	cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -151,8 +152,11 @@ namespace beep {
 // each launch.
 // allow_tc = false keeps the fast form's force of infection on FP32 SIMT;
 // allow_ctas = false keeps it at one particle per SM.
+// keys (may be null): one Philox key per particle, for batches that pack the
+// particles of requests with different seeds.
 beep_status batch_create_internal(beep_model *m, const beep_sim_batch *b, bool device_io, beep_batch **out,
-                                  bool device_traj = false, bool allow_tc = true, bool allow_ctas = true);
+                                  bool device_traj = false, bool allow_tc = true, bool allow_ctas = true,
+                                  const std::vector<uint2> *keys = nullptr);
 // beep_batch_download in two halves: the device->host copy enqueued on the
 // model's stream, and (once that copy completed) the status check and the
 // copy into the caller's arrays.

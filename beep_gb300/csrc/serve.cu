@@ -8,9 +8,14 @@
 //     run and their device footprint fits the budget -- first fit, holding back
 //     the room the oldest waiting request needs, so that later small requests
 //     may start early but never starve it,
-//   * creates each admitted request's device model and batch and enqueues its
-//     copies and kernel on the model's own non-blocking stream, so kernels of
-//     different requests run side by side on the SMs they leave free.
+//   * packs queued simulation requests of the same model (the same model
+//     description), form, step range and outputs into one batch: their
+//     parameter sets, streams and per-particle keys (each request's seed) are
+//     concatenated, so one launch serves them all and each particle draws
+//     exactly what it draws alone;
+//   * creates each admitted request's (or pack's) device model and batch and
+//     enqueues its copies and kernel on the model's own non-blocking stream, so
+//     kernels of different requests run side by side on the SMs they leave free.
 // Device memory of finished requests is released only while nothing runs (or
 // when the oldest request is waiting for that memory): releasing device or
 // pinned memory synchronises the whole device and would stall the kernels of
@@ -53,7 +58,30 @@ struct Req {
 	beep_status status = BEEP_OK;
 	std::string err;
 	double t_submit = 0, t_admit = 0, t_done = 0, g_start = -1, g_end = -1;
+	// a pack: the requests run as one batch (the first is the leader, which holds the
+	// device model and batch), and the concatenated inputs and outputs of that batch
+	std::vector<Req *> members;
+	beep_sim_batch pbatch{};
+	std::vector<beep_param_tables> pgroups;
+	std::vector<int32_t> pgroup_of, ppop_in, ppop_out;
+	std::vector<uint32_t> pstream_of;
+	std::vector<uint2> pkeys;
+	std::vector<double> pL;
 };
+
+constexpr int32_t kPackParticles = 32768;   // particles of one packed batch, at most
+
+// Requests that can share one batch: simulation kinds of the same model description
+// (the caller's own arrays), form, step range and outputs; no trajectory outputs.
+bool packable(const Req *a, const Req *b)
+{
+	if (a->kind == BEEP_REQ_PF_LIKELIHOOD || b->kind == BEEP_REQ_PF_LIKELIHOOD) return false;
+	if (memcmp(&a->desc, &b->desc, sizeof(beep_model_desc)) != 0) return false;
+	const beep_sim_batch &x = a->batch, &y = b->batch;
+	return x.form == y.form && x.ti == y.ti && x.tf == y.tf && (x.pop_in != nullptr) == (y.pop_in != nullptr) &&
+	       !x.transnum_out && !y.transnum_out && !x.pop_traj_out && !y.pop_traj_out &&
+	       (x.L_out != nullptr) == (y.L_out != nullptr) && (x.pop_out != nullptr) == (y.pop_out != nullptr);
+}
 
 size_t rup(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -186,7 +214,39 @@ void start_request(beep_server *s, Req *r)
 		return;
 	}
 	beep_status st = beep_model_create(&r->desc, &r->m);
-	if (st == BEEP_OK) st = beep_batch_create(r->m, &r->batch, &r->q);
+	if (st == BEEP_OK && r->members.size() > 1) {
+		// one batch for the pack: parameter sets, group and stream indices, keys and
+		// start populations of the members one after another
+		beep_sim_batch &pb = r->pbatch;
+		pb = r->batch;
+		int32_t P = 0;
+		const size_t popsz = (size_t)r->desc.narea * r->desc.ncomp * r->desc.ndemocatpos;
+		for (Req *x : r->members) {
+			const beep_sim_batch &b = x->batch;
+			const int32_t goff = (int32_t)r->pgroups.size();
+			for (int g = 0; g < b.ngroup; g++) r->pgroups.push_back(b.groups[g]);
+			for (int p = 0; p < b.nparticle; p++) {
+				r->pgroup_of.push_back((b.group_of ? b.group_of[p] : 0) + goff);
+				r->pstream_of.push_back(b.stream_of ? b.stream_of[p] : (uint32_t)p);
+				r->pkeys.push_back(make_uint2((uint32_t)b.seed, (uint32_t)(b.seed >> 32)));
+			}
+			if (b.pop_in) r->ppop_in.insert(r->ppop_in.end(), b.pop_in, b.pop_in + popsz * b.nparticle);
+			P += b.nparticle;
+		}
+		r->pL.assign(pb.L_out ? (size_t)P : 0, 0.0);
+		r->ppop_out.assign(pb.pop_out ? popsz * P : 0, 0);
+		pb.nparticle = P;
+		pb.ngroup = (int32_t)r->pgroups.size();
+		pb.groups = r->pgroups.data();
+		pb.group_of = r->pgroup_of.data();
+		pb.stream_of = r->pstream_of.data();
+		pb.pop_in = pb.pop_in ? r->ppop_in.data() : nullptr;
+		pb.L_out = pb.L_out ? r->pL.data() : nullptr;
+		pb.pop_out = pb.pop_out ? r->ppop_out.data() : nullptr;
+		st = batch_create_internal(r->m, &pb, false, &r->q, false, true, true, &r->pkeys);
+	} else if (st == BEEP_OK) {
+		st = beep_batch_create(r->m, &r->batch, &r->q);
+	}
 	if (st == BEEP_OK) {
 		cudaStream_t str = r->m->stream;
 		cudaError_t e = cudaEventCreate(&r->ev_start);
@@ -214,6 +274,37 @@ void finish_request(beep_server *s, Req *r, cudaError_t ev_state)
 	if (ev_state != cudaSuccess) {
 		r->status = BEEP_DEVICE_ERROR;
 		r->err = cudaGetErrorString(ev_state);
+	} else if (r->members.size() > 1) {
+		// the pack's outputs, member by member: statuses, L and final populations
+		beep_batch *q = r->q;
+		q->pending = false;
+		const char *ho = (const char *)q->out_host.ptr;
+		const int32_t *pst = (const int32_t *)(ho + q->u_st);
+		const double *L = (const double *)(ho + q->u_L);
+		const int32_t *pop = (const int32_t *)(ho + q->u_po);
+		const size_t popsz = (size_t)r->desc.narea * r->desc.ncomp * r->desc.ndemocatpos;
+		size_t off = 0;
+		for (Req *x : r->members) {
+			const beep_sim_batch &b = x->batch;
+			for (int p = 0; p < b.nparticle && x->status == BEEP_OK; p++)
+				if (pst[off + p] != 0) {
+					x->status = (beep_status)pst[off + p];
+					x->err = "particle " + std::to_string(p) + " failed on the device";
+				}
+			if (x->status == BEEP_OK) {
+				if (b.L_out) memcpy(b.L_out, L + off, 8 * (size_t)b.nparticle);
+				if (b.pop_out) memcpy(b.pop_out, pop + off * popsz, 4 * popsz * b.nparticle);
+			}
+			off += (size_t)b.nparticle;
+		}
+		float a = 0, bt = 0;
+		if (cudaEventElapsedTime(&a, s->ev0, r->ev_start) == cudaSuccess &&
+		    cudaEventElapsedTime(&bt, s->ev0, r->ev_end) == cudaSuccess) {
+			for (Req *x : r->members) {
+				x->g_start = a * 1e-3;
+				x->g_end = bt * 1e-3;
+			}
+		}
 	} else {
 		beep_status st = batch_download_finish(r->q);
 		if (st != BEEP_OK) {
@@ -248,6 +339,12 @@ void worker_main(beep_server *s)
 			lk.lock();
 			r->t_done = s->now();
 			r->state = 2;
+			for (Req *x : r->members) {
+				if (x == r) continue;
+				if (r->status != BEEP_OK && x->status == BEEP_OK) { x->status = r->status; x->err = r->err; }
+				x->t_done = r->t_done;
+				x->state = 2;
+			}
 			s->used -= r->bytes;
 			s->held += r->bytes;
 			s->graveyard.push_back(r);
@@ -284,6 +381,25 @@ void worker_main(beep_server *s)
 			s->queue.erase(s->queue.begin() + k);
 			r->state = 1;
 			r->t_admit = s->now();
+			// later queued requests that can share its batch (within the budget and the pack size)
+			r->members.assign(1, r);
+			int32_t npack = r->batch.nparticle;
+			size_t est = r->est;
+			for (size_t j = k; j < s->queue.size();) {
+				Req *x = s->queue[j];
+				if (packable(r, x) && npack + x->batch.nparticle <= kPackParticles &&
+				    (s->used + s->held + reserve + est + x->est <= s->budget || alone)) {
+					s->queue.erase(s->queue.begin() + j);
+					x->state = 1;
+					x->t_admit = r->t_admit;
+					r->members.push_back(x);
+					npack += x->batch.nparticle;
+					est += x->est;
+				} else {
+					j++;
+				}
+			}
+			r->est = est;
 			s->used += r->est;
 			lk.unlock();
 			start_request(s, r);

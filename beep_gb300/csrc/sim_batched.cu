@@ -373,6 +373,7 @@ __global__ void __launch_bounds__(kBxStepThreads, MB) bx_step(const ModelDev m, 
 			__syncthreads();
 		}
 		const uint32_t stream = b.stream_of ? b.stream_of[p] : (uint32_t)p;
+		const uint32_t k0 = b.key_of ? b.key_of[p].x : b.k0, k1 = b.key_of ? b.key_of[p].y : b.k1;
 		int32_t *status = b.status + p;
 		const int32_t *pc = bx_pop(m, b, p, cur);
 		int32_t *pn = bx_pop(m, b, p, cur ^ 1);
@@ -444,7 +445,7 @@ __global__ void __launch_bounds__(kBxStepThreads, MB) bx_step(const ModelDev m, 
 				if (mean > 0.f) {
 					if (mean > 1.0e9f) atomicCAS(status, 0, BEEP_COUNT_OVERFLOW);
 					else {
-						n = poisson_fp32(mean, b.k0, b.k1, (uint32_t)col, (uint32_t)tr, (uint32_t)sett, stream, inv, inv_call,
+						n = poisson_fp32(mean, k0, k1, (uint32_t)col, (uint32_t)tr, (uint32_t)sett, stream, inv, inv_call,
 						                 rcp, lnfact, lim);
 						if (n < 0) { atomicCAS(status, 0, BEEP_TIMEOUT); n = 0; }
 					}

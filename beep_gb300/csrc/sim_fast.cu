@@ -31,6 +31,7 @@ int fast_prepare()
 	int e = prepare_constants();
 	if (e == 0) e = fast_chain_prepare();
 	if (e == 0) e = batched_prepare();
+	if (e == 0) e = fast_wide_prepare();
 	return e != 0 ? e : fast_ctas_prepare();
 }
 
@@ -65,10 +66,14 @@ int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream)
 {
 	if (b.P == 0) return 0;
 	if (b.mode != 0) return launch_sim_fast_chain(m, b, stream);
-	if (m.G > 16 || m.T > kMaxT) return (int)cudaErrorInvalidValue;
 	const int nt = b.nt > 0 ? b.nt : pick_threads(m);
 	size_t smem = fast_smem_bytes(m, b.nslots, b.m_in_smem != 0, b.nefoi_stage, b.gstate != nullptr,
 	                              b.tn_full ? m.T : m.tn_rows, b.pop_single != 0, b.tn_smem != 0, nt);
+	if (fast_wide_needed(m)) {
+		const int e = fast_prepare();
+		if (e != 0) return e;
+		return launch_sim_fast_wide(m, b, smem, stream);
+	}
 	if (b.foi_tc) {
 		if (!m.tc_image || pick_threads(m) != 640 || b.tc_smem_off < smem) return (int)cudaErrorInvalidValue;
 		smem = b.tc_smem_off + fast_tc_smem_bytes(m);

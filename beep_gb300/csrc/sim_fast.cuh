@@ -44,7 +44,9 @@ namespace beep {
 namespace {
 
 constexpr int kFastThreads = 640;   // largest CTA; smaller models use 128 or 256 threads
-constexpr int kMaxT = 8;            // transitions per model in the fast form
+constexpr int kMaxT = 8;            // transitions per model in the fast form's usual instantiations
+constexpr int kWideT = 16;          // transitions in the wide instantiation (one 640-thread CTA per SM)
+constexpr int kWideG = 20;          // age groups in the wide instantiation
 
 __constant__ float c_lnfact[32];   // log k!, k < 32
 
@@ -494,7 +496,9 @@ __device__ __forceinline__ int32_t binomial_fp32(float p, int32_t n, uint32_t k0
 // chains; two of 256 or four of 128 threads for small models.
 constexpr int min_ctas(int nt) { return nt >= 640 ? 1 : nt >= 256 ? 2 : 4; }
 
-template <int NT, int MG, bool TC, bool CH = false, int MB = min_ctas(NT)>
+// MT: the most transitions the per-column mean registers hold (kMaxT, or kWideT
+// for models with more transitions)
+template <int NT, int MG, bool TC, bool CH = false, int MB = min_ctas(NT), int MT = kMaxT>
 __global__ void __launch_bounds__(NT, MB) sim_fast_kernel(const ModelDev m, const BatchDev b)
 {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -508,6 +512,7 @@ __global__ void __launch_bounds__(NT, MB) sim_fast_kernel(const ModelDev m, cons
 	const int lda = ms_lda(A);
 	const GroupDir dir = b.dirs[b.group_of ? b.group_of[p] : 0];
 	const uint32_t stream = b.stream_of ? b.stream_of[p] : (uint32_t)p;
+	const uint32_t k0 = b.key_of ? b.key_of[p].x : b.k0, k1 = b.key_of ? b.key_of[p].y : b.k1;   // the particle's key
 	Tabs tb;
 	{
 		const float *fp = b.fpool32;
@@ -705,9 +710,9 @@ __global__ void __launch_bounds__(NT, MB) sim_fast_kernel(const ModelDev m, cons
 					minf = dt * popu * s.sus[dp] * (be[sc] * nmi + et[sc] * eage);
 				}
 			}
-			float mv[kMaxT];
+			float mv[MT];
 #pragma unroll
-			for (int tr = 0; tr < kMaxT; tr++) {
+			for (int tr = 0; tr < MT; tr++) {
 				mv[tr] = 0.f;
 				if (tr < T) {
 					if (tr == itr) mv[tr] = minf;
@@ -724,7 +729,7 @@ __global__ void __launch_bounds__(NT, MB) sim_fast_kernel(const ModelDev m, cons
 			for (int tr = 0; tr < T; tr++) {
 				float mean = mv[0];
 #pragma unroll
-				for (int k = 1; k < kMaxT; k++) mean = tr == k ? mv[k] : mean;
+				for (int k = 1; k < MT; k++) mean = tr == k ? mv[k] : mean;
 				int32_t n = 0;
 				if constexpr (CH) {
 					const size_t tcell = (size_t)tr * ncol + col, step_cells = (size_t)T * ncol;
@@ -747,17 +752,17 @@ __global__ void __launch_bounds__(NT, MB) sim_fast_kernel(const ModelDev m, cons
 						if (mean > 0.f) {
 							if (mean > 1.0e9f) atomicCAS(status, 0, BEEP_COUNT_OVERFLOW);
 							else if (b.simu_all || (b.simu && b.simu[((size_t)p * m.S + sett) * A + c])) {
-								n = poisson_fp32(mean, b.k0, b.k1, (uint32_t)col, (uint32_t)tr, (uint32_t)sett, stream, inv,
+								n = poisson_fp32(mean, k0, k1, (uint32_t)col, (uint32_t)tr, (uint32_t)sett, stream, inv,
 								                 inv_call, s.rcp, s.lnfact, lim);
 							} else {                       // coupled to the current state (src/mbp.cc:293-305)
 								const int32_t ni = b.ch_tn[ci];
 								const float ri = b.ch_mean_f[ci];
 								if (mean > ri) {
-									n = poisson_fp32(mean - ri, b.k0, b.k1, (uint32_t)col, (uint32_t)tr, (uint32_t)sett,
+									n = poisson_fp32(mean - ri, k0, k1, (uint32_t)col, (uint32_t)tr, (uint32_t)sett,
 									                 stream, inv, inv_call, s.rcp, s.lnfact, lim);
 									if (n >= 0) n += ni;
 								} else if (mean == ri) n = ni;
-								else n = binomial_fp32(mean / ri, ni, b.k0, b.k1, (uint32_t)col, (uint32_t)tr, (uint32_t)sett,
+								else n = binomial_fp32(mean / ri, ni, k0, k1, (uint32_t)col, (uint32_t)tr, (uint32_t)sett,
 								                       stream, lim);
 							}
 							if (n < 0) { atomicCAS(status, 0, BEEP_TIMEOUT); n = 0; }
@@ -769,7 +774,7 @@ __global__ void __launch_bounds__(NT, MB) sim_fast_kernel(const ModelDev m, cons
 				if (mean > 0.f) {
 					if (mean > 1.0e9f) atomicCAS(status, 0, BEEP_COUNT_OVERFLOW);
 					else {
-						n = poisson_fp32(mean, b.k0, b.k1, (uint32_t)col, (uint32_t)tr, (uint32_t)sett, stream, inv, inv_call,
+						n = poisson_fp32(mean, k0, k1, (uint32_t)col, (uint32_t)tr, (uint32_t)sett, stream, inv, inv_call,
 						                 s.rcp, s.lnfact, lim);
 						if (n < 0) { atomicCAS(status, 0, BEEP_TIMEOUT); n = 0; }
 					}

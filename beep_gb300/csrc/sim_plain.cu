@@ -98,6 +98,7 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 	const int nsteps = b.tf - b.ti;
 	const GroupDir dir = b.dirs[b.group_of ? b.group_of[p] : 0];
 	const uint32_t stream = b.stream_of ? b.stream_of[p] : (uint32_t)p;
+	const uint32_t k0 = b.key_of ? b.key_of[p].x : b.k0, k1 = b.key_of ? b.key_of[p].y : b.k1;   // the particle's key
 	const double *fp = b.fpool;
 	const int32_t *ip = b.ipool;
 	const double *transrate = fp + dir.transrate, *sus = fp + dir.susceptibility, *infectivity = fp + dir.infectivity;
@@ -282,16 +283,16 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 				else {
 					const uint32_t col = (uint32_t)(c * DP + dp);
 					if (mode == 0 || b.simu_all || (b.simu && b.simu[((size_t)p * m.S + sett) * A + c])) {
-						n = poisson_fp64(mean, b.k0, b.k1, col, (uint32_t)tr, (uint32_t)sett, stream, lim);
+						n = poisson_fp64(mean, k0, k1, col, (uint32_t)tr, (uint32_t)sett, stream, lim);
 					} else {                        // coupled to the current state (src/mbp.cc:293-305)
 						const size_t ci = chs(cs_i, sett) * tnsz + cell;
 						const int32_t ni = b.ch_tn[ci];
 						const double ri = b.ch_mean[ci];
 						if (mean > ri) {
-							n = poisson_fp64(mean - ri, b.k0, b.k1, col, (uint32_t)tr, (uint32_t)sett, stream, lim);
+							n = poisson_fp64(mean - ri, k0, k1, col, (uint32_t)tr, (uint32_t)sett, stream, lim);
 							if (n >= 0) n += ni;
 						} else if (mean == ri) n = ni;
-						else n = binomial_fp64(mean / ri, ni, b.k0, b.k1, col, (uint32_t)tr, (uint32_t)sett, stream, lim);
+						else n = binomial_fp64(mean / ri, ni, k0, k1, col, (uint32_t)tr, (uint32_t)sett, stream, lim);
 					}
 					if (n < 0) { set_status(status, BEEP_TIMEOUT); n = 0; }
 				}

@@ -64,6 +64,9 @@ class Workload:
     # model modifications of the reference's prediction mode (TOML `modification`): dicts
     # of its keys, e.g. {"type": "beta_fac", "start": "36", "end": "50", "factor": "0.5"}
     modifications: List[dict] = dataclasses.field(default_factory=list)
+    # Erlang stages of the latent and infectious periods: E1..Ek and I1..Ik, each with
+    # an exponential residence of mean sigma_inv / k (gamma_inv / k) -- 4k + 2 transitions
+    stages: int = 1
     # prior ranges (inference modes)
     R_prior: tuple = (0.5, 4.0)
     sigma_inv_prior: tuple = (2.0, 6.0)
@@ -73,6 +76,19 @@ class Workload:
     @property
     def ndivision(self) -> int:
         return self.days * self.steps_per_day
+
+    def e_names(self) -> List[str]:
+        return ["E"] if self.stages == 1 else [f"E{i + 1}" for i in range(self.stages)]
+
+    def i_names(self) -> List[str]:
+        return ["I"] if self.stages == 1 else [f"I{i + 1}" for i in range(self.stages)]
+
+    def comp_names(self) -> List[str]:
+        return ["S"] + self.e_names() + self.i_names() + ["H", "R", "D"]
+
+    def cases_transition(self) -> str:
+        """The observed E->I transition (the last latent stage into the first infectious one)."""
+        return f"{self.e_names()[-1]}->{self.i_names()[0]}"
 
     def age_names(self) -> List[str]:
         return [f"age{a}" for a in range(self.nage)]
@@ -150,7 +166,8 @@ def write_beep_inputs(w: Workload, outdir: str, obs_values: Optional[dict] = Non
         with open(os.path.join(data, "geo_mixing_matrix.csv"), "w") as f:
             for c in range(A):
                 f.write(",".join(_fmt(v) for v in w.geo[c]) + "\n")
-    comps = ["S", "E", "I", "H", "R", "D"]
+    comps = w.comp_names()
+    e_first = w.e_names()[0]
     with open(os.path.join(data, "init_pop.csv"), "w") as f:
         if w.strains is None:
             f.write("area," + ("age," if G > 1 else "") + "compartment,population\n")
@@ -159,7 +176,7 @@ def write_beep_inputs(w: Workload, outdir: str, obs_values: Optional[dict] = Non
                     for co in comps:
                         if co == "S":
                             v = int(w.pop[c, a] - w.seed_E[c, a])
-                        elif co == "E":
+                        elif co == e_first:
                             v = int(w.seed_E[c, a])
                         else:
                             v = 0
@@ -173,7 +190,7 @@ def write_beep_inputs(w: Workload, outdir: str, obs_values: Optional[dict] = Non
                         for co in comps:
                             if co == "S":
                                 v = int(w.pop[c, a] - seeds[:, c, a].sum()) if st == 0 else 0
-                            elif co == "E":
+                            elif co == e_first:
                                 v = int(seeds[st, c, a])
                             else:
                                 v = 0
@@ -231,17 +248,33 @@ def write_beep_inputs(w: Workload, outdir: str, obs_values: Optional[dict] = Non
     lines += [
         "comps = [",
         '{name="S"},',
-        f'{{name="E", dist="Exp", mean_value="{_fmt(w.sigma_inv)}", mean_prior="Uniform({w.sigma_inv_prior[0]},{w.sigma_inv_prior[1]})"}},',
-        f'{{name="I", dist="Exp", mean_value="{_fmt(w.gamma_inv)}", inf_value="1", mean_prior="Uniform({w.gamma_inv_prior[0]},{w.gamma_inv_prior[1]})"}},',
+    ]
+    k = w.stages
+    en, iname = w.e_names(), w.i_names()
+    for e in en:
+        lines.append(f'{{name="{e}", dist="Exp", mean_value="{_fmt(w.sigma_inv / k)}", '
+                     f'mean_prior="Uniform({_fmt(w.sigma_inv_prior[0] / k)},{_fmt(w.sigma_inv_prior[1] / k)})"}},'
+                     if k > 1 else
+                     f'{{name="E", dist="Exp", mean_value="{_fmt(w.sigma_inv)}", mean_prior="Uniform({w.sigma_inv_prior[0]},{w.sigma_inv_prior[1]})"}},')
+    for i in iname:
+        lines.append(f'{{name="{i}", dist="Exp", mean_value="{_fmt(w.gamma_inv / k)}", inf_value="1", '
+                     f'mean_prior="Uniform({_fmt(w.gamma_inv_prior[0] / k)},{_fmt(w.gamma_inv_prior[1] / k)})"}},'
+                     if k > 1 else
+                     f'{{name="I", dist="Exp", mean_value="{_fmt(w.gamma_inv)}", inf_value="1", mean_prior="Uniform({w.gamma_inv_prior[0]},{w.gamma_inv_prior[1]})"}},')
+    lines += [
         f'{{name="H", dist="Exp", mean_value="{_fmt(w.h_mean)}", mean_prior="Uniform({w.h_mean_prior[0]},{w.h_mean_prior[1]})"}},',
         '{name="R"},',
         '{name="D"}',
         "]",
         "trans = [",
-        '{from="S", to="E", infection="yes"},',
-        '{from="E", to="I"},',
-        f'{{from="I", to="H", prob_value="{_fmt(w.p_H)}", prob_prior="Dir(1)"}},',
-        '{from="I", to="R", prob_value="*", prob_prior="Dir(1)"},',
+        f'{{from="S", to="{en[0]}", infection="yes"}},',
+    ]
+    chain = en + iname
+    for a_, b_ in zip(chain, chain[1:]):
+        lines.append(f'{{from="{a_}", to="{b_}"}},')
+    lines += [
+        f'{{from="{iname[-1]}", to="H", prob_value="{_fmt(w.p_H)}", prob_prior="Dir(1)"}},',
+        f'{{from="{iname[-1]}", to="R", prob_value="*", prob_prior="Dir(1)"}},',
         f'{{from="H", to="D", prob_value="{_fmt(w.p_D)}", prob_prior="Dir(1)"}},',
         '{from="H", to="R", prob_value="*", prob_prior="Dir(1)"}',
         "]",
@@ -284,7 +317,7 @@ def data_tables(w: Workload) -> List[dict]:
     tabs = []
     if w.obs_kind == "cases_deaths":
         tabs.append(dict(file="cases.csv", times=list(range(0, w.days)), columns=areas,
-                         toml=dict(type="transition", observation="E->I", timestep="1", obsmodel="normal load",
+                         toml=dict(type="transition", observation=w.cases_transition(), timestep="1", obsmodel="normal load",
                                    geo_dep="area", file="cases.csv")))
         tabs.append(dict(file="deaths.csv", times=list(range(0, w.days - 6, 7)), columns=areas,
                          toml=dict(type="transition", observation="H->D", timestep="7", obsmodel="normal load",
@@ -292,7 +325,7 @@ def data_tables(w: Workload) -> List[dict]:
     elif w.obs_kind == "cases_age":
         for a, an in enumerate(w.age_names()):
             tabs.append(dict(file=f"cases_{an}.csv", times=list(range(0, w.days)), columns=areas,
-                             toml=dict(type="transition", observation="E->I", timestep="1", obsmodel="normal load",
+                             toml=dict(type="transition", observation=w.cases_transition(), timestep="1", obsmodel="normal load",
                                        geo_dep="area", democats_filt=f"age:{an}", file=f"cases_{an}.csv")))
     elif w.obs_kind == "hosp_pop":
         tabs.append(dict(file="hosp.csv", times=list(range(0, w.days, 7)), columns=areas,
@@ -302,7 +335,7 @@ def data_tables(w: Workload) -> List[dict]:
         # every observation model the reference parses (src/inputs.cc:413-473) with
         # censored ('*' below the table's threshold) and missing ('.') entries
         tabs.append(dict(file="cases.csv", times=list(range(0, w.days)), columns=areas, sd_col=False,
-                         toml=dict(type="transition", observation="E->I", timestep="1", obsmodel="normal 10%",
+                         toml=dict(type="transition", observation=w.cases_transition(), timestep="1", obsmodel="normal 10%",
                                    geo_dep="area", file="cases.csv")))
         tabs.append(dict(file="deaths.csv", times=list(range(0, w.days - 6, 7)), columns=areas, sd_col=False,
                          censor_below=5, nodata_every=5,
@@ -313,7 +346,7 @@ def data_tables(w: Workload) -> List[dict]:
                          toml=dict(type="population", observation="H", obsmodel="normal 30",
                                    geo_dep="area", file="hosp.csv")))
         tabs.append(dict(file="cases_w.csv", times=list(range(0, w.days - 6, 7)), columns=areas, censor_below=20,
-                         toml=dict(type="transition", observation="E->I", timestep="7", obsmodel="normal load",
+                         toml=dict(type="transition", observation=w.cases_transition(), timestep="7", obsmodel="normal load",
                                    threshold="20", geo_dep="area", file="cases_w.csv")))
     else:
         raise ValueError(w.obs_kind)

@@ -143,7 +143,9 @@ enum beep_form {
 	BEEP_FORM_PLAIN_FP64 = 0, /* FP64 in the reference's summation order: bit-exact transnum/pop */
 	BEEP_FORM_FAST = 1        /* particle-resident, FP32 rates and draws on the same keyed streams,
 	                             exact integer observation sums, compensated FP32 log-densities
-	                             reduced in FP64 */
+	                             reduced in FP64; models of up to 16 transitions and 20 age
+	                             groups (beyond 8 transitions or 16 ages: one 640-thread CTA
+	                             per SM with the FOI on FP32 SIMT; MBP chains up to 8 and 16) */
 };
 
 /* One batch of particles advanced over steps [ti, tf): State::simulate(ti,tf)

@@ -278,6 +278,12 @@ def main():
         {"type": "efoi_fac", "start": "30", "factor": "2.5", "geo_filt": "area:A0|A2|A4"},
     ]
     make_prediction_fixture("pred_sim", pw, ngroup=2, npart=2, seed=0x9E7D)
+    # beyond the fast form's usual instantiations: 18 age groups and Erlang-staged latent
+    # and infectious periods (3 stages each: 10 compartments, 10 transitions)
+    ww = synth.seir_hd_small(seed=20260108, narea=5, nage=18, days=30, name="wide")
+    ww.stages = 3
+    ww.seed_E[:, :] = 20                       # exposed in every area and age: a visible epidemic in 30 days
+    make_fixture("wide_sim", ww, npart=8, ntraj=2, seed=0x31DE)
 
 
 if __name__ == "__main__":

@@ -8,7 +8,7 @@ import numpy as np
 from beep_gb300 import bundle, capi
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-FIXTURES = ["tiny_sim", "oneage_sim", "c0_sim", "strain_sim", "obsmodel_sim", "features_sim", "pred_sim"]
+FIXTURES = ["tiny_sim", "oneage_sim", "c0_sim", "strain_sim", "obsmodel_sim", "features_sim", "pred_sim", "wide_sim"]
 PF_FIXTURES = ["tiny_pf", "c0_pf", "features_pf"]
 MBP_FIXTURES = ["tiny_mbp", "c0_mbp"]
 MBP_VARIANTS = 3   # 0 INF_DIF_UPDATE, 1 INF_UPDATE, 2 INF_DIF_UPDATE with SIMU cells

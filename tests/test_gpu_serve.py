@@ -159,3 +159,37 @@ def test_particle_filter_requests_alone_and_in_the_mix():
     for t in tsim:
         srv.wait(t, 120.0)
     srv.close()
+
+
+@pytest.mark.parametrize("form", [capi.FORM_PLAIN_FP64, capi.FORM_FAST])
+def test_requests_of_one_model_are_packed_into_one_batch(form):
+    """Queued requests of the same model, form, step range and outputs run as
+    one batch: their parameter sets, streams and seeds are concatenated, and
+    each request gets what it gets alone -- the same counts and populations,
+    and L bit for bit in the plain form (within the fast form's 1e-6 where the
+    pack's size gives the fast kernel another layout)."""
+    m, tabs = synthetic(100, 4, 60, 4, 20260403)
+    rng = np.random.default_rng(7)
+    sizes = [40, 300, 17, 900, 64]
+    specs = []
+    for k, P in enumerate(sizes):
+        t = [tabs[j] for j in rng.permutation(len(tabs))[:2]]
+        specs.append((t, P, 500 + 31 * k, rng.integers(0, 2, P)))
+    dm = capi.DeviceModel(m)
+    alone = [dm.simulate(capi.Batch(m, t, P, sd, group_of=go, want_pop=True, form=form)) for t, P, sd, go in specs]
+    dm.close()
+    srv = capi.Server(16 << 30, 1)
+    bs = [capi.Batch(m, t, P, sd, group_of=go, want_pop=True, form=form) for t, P, sd, go in specs]
+    ts = [srv.submit(m, b, capi.REQ_LIKELIHOOD) for b in bs]
+    for t in ts:
+        srv.wait(t, 120.0)
+    st = [srv.stats(t) for t in ts]
+    spans = [(s["gpu_start_s"], s["gpu_end_s"]) for s in st]
+    assert len(set(spans)) < len(spans), spans          # at least two requests shared one batch
+    for b, ref in zip(bs, alone):
+        assert np.array_equal(b.pop, ref.pop)
+        if form == capi.FORM_PLAIN_FP64:
+            assert np.array_equal(b.L, ref.L)
+        else:
+            np.testing.assert_allclose(b.L, ref.L, rtol=1e-6)
+    srv.close()
