@@ -164,4 +164,58 @@ TablePack::TablePack(const ModelPack &mp, const Details &details, const Data &da
 	tables.transmean_mult = transmean_mult.empty() ? nullptr : transmean_mult.data();
 }
 
+PriorPack::PriorPack(const Details &details, const Model &model)
+{
+	const unsigned np = model.param.size();
+	auto par_or_none = [&](unsigned p) { return p < np ? (int32_t)p : -1; };
+	gt_ptr.push_back(0);
+	lt_ptr.push_back(0);
+	for (unsigned th = 0; th < np; th++) {
+		const auto &par = model.param[th];
+		type.push_back((int32_t)par.priortype);
+		val1.push_back(par.val1);
+		val2.push_back(par.val2);
+		val1_param.push_back(par_or_none(par.val1_param));
+		val2_param.push_back(par_or_none(par.val2_param));
+		for (auto t2 : par.greaterthan) gt_param.push_back((int32_t)t2);
+		for (auto t2 : par.lessthan) lt_param.push_back((int32_t)t2);
+		gt_ptr.push_back((int32_t)gt_param.size());
+		lt_ptr.push_back((int32_t)lt_param.size());
+	}
+	dir_ptr.push_back(0);
+	for (const auto &dir : model.dirichlet) {
+		for (const auto &dp : dir.param) {
+			dir_param.push_back((int32_t)dp.th);
+			dir_frac.push_back(dp.frac);
+		}
+		dir_ptr.push_back((int32_t)dir_param.size());
+	}
+	// the consecutive spline points Model::spline_prior smooths (none when simulating)
+	if (details.siminf != SIMULATE)
+		for (const auto &spl : model.spline) {
+			if (spl.smoothtype == NOSMOOTH) continue;
+			for (unsigned i = 0; i + 1 < spl.p.size(); i++) {
+				const auto &a = spl.p[i], &b = spl.p[i + 1];
+				if (a.param == b.param || a.t == b.t) continue;
+				if (model.param[a.param].priortype == FIXED_PRIOR && model.param[b.param].priortype == FIXED_PRIOR) continue;
+				smooth_kind.push_back(spl.smoothtype == LOGSMOOTH ? 1 : 2);
+				smooth_par1.push_back((int32_t)a.param);
+				smooth_par2.push_back((int32_t)b.param);
+				smooth_mult1.push_back(a.multfac);
+				smooth_mult2.push_back(b.multfac);
+				smooth_value.push_back(a.smooth_value);
+			}
+		}
+	spec.nparam = (int32_t)np;
+	spec.type = type.data(); spec.val1 = val1.data(); spec.val2 = val2.data();
+	spec.val1_param = val1_param.data(); spec.val2_param = val2_param.data();
+	spec.gt_ptr = gt_ptr.data(); spec.gt_param = gt_param.data(); spec.lt_ptr = lt_ptr.data(); spec.lt_param = lt_param.data();
+	spec.ndirichlet = (int32_t)model.dirichlet.size();
+	spec.dir_ptr = dir_ptr.data(); spec.dir_param = dir_param.data(); spec.dir_frac = dir_frac.data();
+	spec.nsmooth = (int32_t)smooth_kind.size();
+	spec.smooth_kind = smooth_kind.data(); spec.smooth_par1 = smooth_par1.data(); spec.smooth_par2 = smooth_par2.data();
+	spec.smooth_mult1 = smooth_mult1.data(); spec.smooth_mult2 = smooth_mult2.data(); spec.smooth_value = smooth_value.data();
+	spec.ml_mode = details.mode == ML_INF ? 1 : 0;
+}
+
 }  // namespace beep_binding

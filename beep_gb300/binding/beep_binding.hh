@@ -62,6 +62,20 @@ struct TablePack {
 	TablePack &operator=(const TablePack &) = delete;
 };
 
+// The priors and bounds of BEEP's parameters (beep_prior_spec): Param's prior
+// type, hyperparameters and order constraints, the Dirichlet groups, and the
+// spline smoothing terms Model::spline_prior evaluates.
+struct PriorPack {
+	std::vector<int32_t> type, val1_param, val2_param, gt_ptr, gt_param, lt_ptr, lt_param, dir_ptr, dir_param,
+	    smooth_kind, smooth_par1, smooth_par2;
+	std::vector<double> val1, val2, dir_frac, smooth_mult1, smooth_mult2, smooth_value;
+	beep_prior_spec spec{};
+
+	PriorPack(const Details &details, const Model &model);
+	PriorPack(const PriorPack &) = delete;
+	PriorPack &operator=(const PriorPack &) = delete;
+};
+
 // State::simulate(ti, tf) + ObservationModel::calculate(_section) for nparticle
 // particles of one parameter set (particle p on variate stream p): pop_in
 // [nparticle][narea][ncomp][ndemocatpos] when ti > 0; L_out [nparticle],

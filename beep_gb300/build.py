@@ -33,6 +33,7 @@ UNITS = {
     "noalloc.cu": [],
     "pf.cu": [],
     "abc_weights.cu": [],
+    "prior.cu": [],
     "mbp.cu": [],
     "mbp_fast.cu": [],
     "mbp_fast_ctas.cu": [],

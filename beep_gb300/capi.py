@@ -41,6 +41,48 @@ class ModelDesc(C.Structure):
     ]
 
 
+class PriorSpec(C.Structure):
+    _fields_ = [
+        ("nparam", C.c_int32), ("type", _i32p), ("val1", _f64p), ("val2", _f64p), ("val1_param", _i32p),
+        ("val2_param", _i32p), ("gt_ptr", _i32p), ("gt_param", _i32p), ("lt_ptr", _i32p), ("lt_param", _i32p),
+        ("ndirichlet", C.c_int32), ("dir_ptr", _i32p), ("dir_param", _i32p), ("dir_frac", _f64p),
+        ("nsmooth", C.c_int32), ("smooth_kind", _i32p), ("smooth_par1", _i32p), ("smooth_par2", _i32p),
+        ("smooth_mult1", _f64p), ("smooth_mult2", _f64p), ("smooth_value", _f64p), ("ml_mode", C.c_int32),
+    ]
+
+
+PRIOR_INT_ARRAYS = ("type", "val1_param", "val2_param", "gt_ptr", "gt_param", "lt_ptr", "lt_param", "dir_ptr",
+                    "dir_param", "smooth_kind", "smooth_par1", "smooth_par2")
+PRIOR_F64_ARRAYS = ("val1", "val2", "dir_frac", "smooth_mult1", "smooth_mult2", "smooth_value")
+
+
+class Priors:
+    """A ``beep_prior_spec`` over arrays named as its fields (e.g. a bundle's ``prior.*``)."""
+
+    def __init__(self, arrays, prefix: str = "prior."):
+        self.arr = {}
+        self.st = PriorSpec()
+        for k in PRIOR_INT_ARRAYS:
+            self.arr[k] = np.ascontiguousarray(np.asarray(arrays.get(prefix + k, []), np.int32).reshape(-1))
+            setattr(self.st, k, self.arr[k].ctypes.data_as(_i32p))
+        for k in PRIOR_F64_ARRAYS:
+            self.arr[k] = np.ascontiguousarray(np.asarray(arrays.get(prefix + k, []), np.float64).reshape(-1))
+            setattr(self.st, k, self.arr[k].ctypes.data_as(_f64p))
+        self.st.nparam = int(self.arr["type"].size)
+        self.st.ndirichlet = int(self.arr["dir_ptr"].size) - 1 if self.arr["dir_ptr"].size else 0
+        self.st.nsmooth = int(self.arr["smooth_kind"].size)
+        self.st.ml_mode = int(np.asarray(arrays.get(prefix + "ml_mode", [0])).reshape(-1)[0])
+
+    def evaluate(self, theta):
+        """(log-prior [n], in bounds [n]) of parameter rows theta [n][nparam] (beep_log_prior)."""
+        th = np.ascontiguousarray(np.asarray(theta, np.float64).reshape(-1, self.st.nparam))
+        lp = np.zeros(th.shape[0])
+        ib = np.zeros(th.shape[0], np.int32)
+        check(lib().beep_log_prior(C.byref(self.st), th.shape[0], th.ctypes.data_as(_f64p), lp.ctypes.data_as(_f64p),
+                                   ib.ctypes.data_as(_i32p)))
+        return lp, ib.astype(bool)
+
+
 class ParamTables(C.Structure):
     _fields_ = [
         ("transrate", _f64p), ("susceptibility", _f64p), ("infectivity", _f64p),
@@ -281,6 +323,8 @@ def lib():
         L.beep_abcsmc_weights.argtypes = [C.c_int32, C.c_int32, _f64p, _f64p, C.c_int32, _f64p, _f64p, _f64p,
                                           C.c_double, C.c_int32, _f64p]
         L.beep_abcsmc_weights.restype = C.c_int32
+        L.beep_log_prior.argtypes = [C.POINTER(PriorSpec), C.c_int32, _f64p, _f64p, _i32p]
+        L.beep_log_prior.restype = C.c_int32
         L.beep_pf_loglik.argtypes = [C.c_void_p, C.POINTER(PFRequest)]
         L.beep_pf_loglik.restype = C.c_int32
         L.beep_set_option.argtypes = [C.c_char_p, C.c_int64]

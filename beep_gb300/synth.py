@@ -52,6 +52,8 @@ class Workload:
     p_D: float = 0.2
     R_bp: List[int] = dataclasses.field(default_factory=list)   # knot days, first 0 last days
     R_val: List[float] = dataclasses.field(default_factory=list)
+    R_smooth: Optional[float] = None          # smoothing sd of the R(t) knots (the reference's `smooth`)
+    R_smooth_type: str = ""                   # "log_smooth" or "smooth"
     efoi: float = 0.0
     covar: Optional[np.ndarray] = None        # [ncovar][A]
     covar_effect: List[float] = dataclasses.field(default_factory=list)
@@ -278,7 +280,8 @@ def write_beep_inputs(w: Workload, outdir: str, obs_values: Optional[dict] = Non
         f'{{from="H", to="D", prob_value="{_fmt(w.p_D)}", prob_prior="Dir(1)"}},',
         '{from="H", to="R", prob_value="*", prob_prior="Dir(1)"}',
         "]",
-        f'R_spline = [{{ value="{rval}", prior="{rprior}", bp="{bp}"}}]',
+        f'R_spline = [{{ value="{rval}", prior="{rprior}", bp="{bp}"' +
+        (f', smooth="{_fmt(w.R_smooth)}", smooth_type="{w.R_smooth_type}"' if w.R_smooth is not None else "") + "}]",
         f'efoi_spline = [{{ value="{_fmt(w.efoi)}"}}]',
     ]
     if w.covar is not None:

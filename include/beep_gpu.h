@@ -295,6 +295,49 @@ BEEP_API beep_status beep_abcsmc_weights(int32_t nvar, int32_t nnew, const doubl
                                          const double *w_last, const double *inv_cov, double size,
                                          int32_t normalise, double *w_out);
 
+/* Log-prior and bounds of parameter sets: Model::prior with its spline
+ * smoothing term (src/model.cc:1590-1706) and Model::inbounds
+ * (src/model.cc:2625-2669), on the host.  The prior types are the
+ * reference's PriorType in its order; a hyperparameter val1 / val2 equal to
+ * 999999999 (the reference's UNSET) is taken from parameter val1_param /
+ * val2_param, as Model::get_val1/get_val2 do.  The smoothing terms are the
+ * pairs of consecutive spline points that Model::spline_prior visits (points
+ * on different parameters and times, not both fixed), evaluated on the
+ * Dirichlet-corrected values (Model::dirichlet_correct, src/model.cc:2685-2695);
+ * none in simulation modes.  paramval is [nset][nparam]; inbounds_out[k] = 1
+ * when set k is inside the bounds, and logprior_out[k] is its log-prior
+ * (-inf outside the bounds or where a gamma density's argument is not
+ * positive). */
+typedef enum beep_prior_type {
+	BEEP_PRIOR_FIXED = 0,
+	BEEP_PRIOR_UNIFORM = 1,
+	BEEP_PRIOR_EXP = 2,
+	BEEP_PRIOR_NORMAL = 3,
+	BEEP_PRIOR_DIRICHLET = 4,
+	BEEP_PRIOR_DIRICHLET_ALPHA = 5,
+	BEEP_PRIOR_DIRICHLET_FLAT = 6,
+	BEEP_PRIOR_MDIRICHLET = 7
+} beep_prior_type;
+
+typedef struct beep_prior_spec {
+	int32_t nparam;
+	const int32_t *type;                      /* [nparam] beep_prior_type */
+	const double *val1, *val2;                /* [nparam] */
+	const int32_t *val1_param, *val2_param;   /* [nparam], -1 where unused */
+	const int32_t *gt_ptr, *gt_param;         /* [nparam+1] CSR: parameters each must be >= (Param::greaterthan) */
+	const int32_t *lt_ptr, *lt_param;         /* [nparam+1] CSR: parameters each must be <= (Param::lessthan) */
+	int32_t ndirichlet;
+	const int32_t *dir_ptr, *dir_param;       /* [ndirichlet+1] CSR: the members of each Dirichlet group */
+	const double *dir_frac;                   /* and their fractions */
+	int32_t nsmooth;
+	const int32_t *smooth_kind;               /* [nsmooth] 1 log-normal (log_smooth), 2 normal (smooth) */
+	const int32_t *smooth_par1, *smooth_par2; /* [nsmooth] the two points' parameters */
+	const double *smooth_mult1, *smooth_mult2, *smooth_value;   /* [nsmooth] their factors, the smoothing sd */
+	int32_t ml_mode;                          /* 1: the reference's maximum-likelihood mode (mode=map) */
+} beep_prior_spec;
+BEEP_API beep_status beep_log_prior(const beep_prior_spec *spec, int32_t nset, const double *paramval,
+                                    double *logprior_out, int32_t *inbounds_out);
+
 /* Library options (process-wide; no counterpart in the reference):
  *   "fast_foi"  force of infection of the fast form: 0 = automatic (tensor
  *               cores batched over the particles for models of 300 to 512

@@ -368,6 +368,49 @@ int main(int argc, char **argv)
 		}
 	};
 
+	// the priors through the binding, and the reference's own Model::prior / inbounds of
+	// every parameter row and of probe rows (each parameter in turn moved below its
+	// lower or above its upper uniform bound, or scaled by 1.1)
+	{
+		const beep_binding::PriorPack pp(details, model);
+		const uint64_t np = pp.type.size();
+		B.i("prior.type", pp.type); B.d("prior.val1", pp.val1); B.d("prior.val2", pp.val2);
+		B.i("prior.val1_param", pp.val1_param); B.i("prior.val2_param", pp.val2_param);
+		B.i("prior.gt_ptr", pp.gt_ptr); B.i("prior.gt_param", pp.gt_param);
+		B.i("prior.lt_ptr", pp.lt_ptr); B.i("prior.lt_param", pp.lt_param);
+		B.i("prior.dir_ptr", pp.dir_ptr); B.i("prior.dir_param", pp.dir_param); B.d("prior.dir_frac", pp.dir_frac);
+		B.i("prior.smooth_kind", pp.smooth_kind); B.i("prior.smooth_par1", pp.smooth_par1);
+		B.i("prior.smooth_par2", pp.smooth_par2); B.d("prior.smooth_mult1", pp.smooth_mult1);
+		B.d("prior.smooth_mult2", pp.smooth_mult2); B.d("prior.smooth_value", pp.smooth_value);
+		B.scalar_i("prior.ml_mode", pp.spec.ml_mode);
+		std::vector<double> rows, Pr;
+		std::vector<int32_t> inb;
+		for (const auto &th : thetas) {
+			std::vector<std::vector<double>> probes{th};
+			for (unsigned k = 0; k < np; k++) {
+				auto t2 = th;
+				if (model.param[k].priortype == UNIFORM_PRIOR) {
+					auto t3 = th;
+					t2[k] = model.param[k].val1 - 0.5;
+					t3[k] = model.param[k].val2 + 0.5;
+					probes.push_back(t3);
+				} else {
+					t2[k] = th[k] * 1.1;
+				}
+				probes.push_back(t2);
+			}
+			for (const auto &p : probes) {
+				rows.insert(rows.end(), p.begin(), p.end());
+				const bool ok = model.inbounds(p);
+				inb.push_back(ok ? 1 : 0);
+				Pr.push_back(ok ? model.prior(p) : 0.0);
+			}
+		}
+		B.d("prior.theta", rows, {(uint64_t)inb.size(), np});
+		B.i("prior.inbounds", inb);
+		B.d("prior.logprior", Pr);
+	}
+
 	for (int gidx = 0; gidx < ngroup; gidx++) {
 		std::string gp = "g" + std::to_string(gidx) + ".";
 		B.d(gp + "theta", thetas[gidx]);

@@ -121,6 +121,24 @@ def mbp_theta_rows(base, nchain, seed):
     return rows
 
 
+def prior_theta_rows(w: synth.Workload):
+    """Parameter rows for the prior fixture, made from the reference's own
+    values: the E, I and H durations and the R(t) knots scaled by U(0.8, 1.2)
+    (the reference's parameter order: E 1, I 2, H 4, R knots from 9)."""
+    def rows_of(base):
+        rng = np.random.default_rng(w.seed + 3)
+        rows = []
+        for _ in range(4):
+            t = np.array(base, np.float64)
+            for i in (1, 2, 4):
+                t[i] *= rng.uniform(0.8, 1.2)
+            for i in range(9, 9 + len(w.R_val)):
+                t[i] = min(3.9, max(0.6, t[i] * rng.uniform(0.8, 1.2)))
+            rows.append(t)
+        return rows
+    return rows_of
+
+
 ONLY = None   # fixture names to (re)generate (--only); None: all
 
 
@@ -136,6 +154,8 @@ def make_fixture(name, w: synth.Workload, npart, ntraj, seed, pf=False, theta_ro
         vals = obs_values_from(b0, w)
         synth.write_beep_inputs(w, work, obs_values=vals)
         theta = None
+        if callable(theta_rows):
+            theta_rows = theta_rows(b0["g0.theta"])
         if theta_rows is not None:
             theta = os.path.join(work, "theta.csv")
             with open(theta, "w") as f:
@@ -278,6 +298,11 @@ def main():
         {"type": "efoi_fac", "start": "30", "factor": "2.5", "geo_filt": "area:A0|A2|A4"},
     ]
     make_prediction_fixture("pred_sim", pw, ngroup=2, npart=2, seed=0x9E7D)
+    # priors and bounds: the reference's Model::prior and inbounds on parameter rows around the
+    # workload's values and on probe rows outside the bounds; log-normal smoothing of R(t)
+    pw2 = synth.seir_hd_features(seed=20260109, days=40, name="priors")
+    pw2.R_smooth, pw2.R_smooth_type = 0.3, "log_smooth"
+    make_fixture("prior_spec", pw2, npart=1, ntraj=0, seed=0x7A10, theta_rows=prior_theta_rows(pw2))
     # beyond the fast form's usual instantiations: 18 age groups and Erlang-staged latent
     # and infectious periods (3 stages each: 10 compartments, 10 transitions)
     ww = synth.seir_hd_small(seed=20260108, narea=5, nage=18, days=30, name="wide")
