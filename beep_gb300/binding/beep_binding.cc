@@ -100,6 +100,27 @@ ModelPack::ModelPack(const Details &details, const Data &data, const Model &mode
 	desc.obs_sd = obs_sd.data(); desc.obs_shape = obs_shape.data(); desc.obs_threshold = obs_threshold.data();
 	desc.obs_factor = obs_factor.data(); desc.obs_factor_spline = obs_factor_spline.data();
 	desc.obs_cell_ptr = obs_cell_ptr.data(); desc.obs_cells = obs_cells.data();
+
+	// demographic changes: areas, dp groups and per-step fractions as loaded by
+	// Data::load_democat_change (src/data.cc:958-1040)
+	dcc_area_ptr.push_back(0);
+	dcc_dp_ptr.push_back(0);
+	for (const auto &dcc : data.democat_change) {
+		const unsigned nv = dcc.frac.empty() ? 0 : dcc.frac[0].size();
+		dcc_nval.push_back((int32_t)nv);
+		for (auto c : dcc.area) dcc_area.push_back((int32_t)c);
+		dcc_area_ptr.push_back((int32_t)dcc_area.size());
+		for (const auto &grp : dcc.dp_group)
+			for (auto dp : grp) dcc_dp.push_back((int32_t)dp);
+		dcc_dp_ptr.push_back((int32_t)dcc_dp.size());
+		for (unsigned s = 0; s < details.ndivision; s++)
+			for (unsigned f = 0; f < nv; f++) dcc_frac.push_back(dcc.frac[s][f]);
+	}
+	desc.ndemocat_change = (int32_t)data.democat_change.size();
+	if (desc.ndemocat_change > 0) {
+		desc.dcc_nval = dcc_nval.data(); desc.dcc_area_ptr = dcc_area_ptr.data(); desc.dcc_area = dcc_area.data();
+		desc.dcc_dp_ptr = dcc_dp_ptr.data(); desc.dcc_dp = dcc_dp.data(); desc.dcc_frac = dcc_frac.data();
+	}
 }
 
 TablePack::TablePack(const ModelPack &mp, const Details &details, const Data &data, const Model &model,

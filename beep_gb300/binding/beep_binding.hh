@@ -42,6 +42,8 @@ struct ModelPack {
 	std::vector<int32_t> obs_sett_i, obs_sett_f, obs_value_kind, obs_model, obs_factor_spline, obs_cell_ptr, obs_cells;
 	std::vector<double> obs_value, obs_sd, obs_shape, obs_threshold, obs_factor;
 	std::vector<unsigned> obs_spline_refs;   // BEEP spline index of each observation-factor spline row
+	std::vector<int32_t> dcc_nval, dcc_area_ptr, dcc_area, dcc_dp_ptr, dcc_dp;   // Data::democat_change
+	std::vector<double> dcc_frac;
 	beep_model_desc desc{};
 
 	ModelPack(const Details &details, const Data &data, const Model &model);
@@ -81,6 +83,7 @@ struct PriorPack {
 // [nparticle][narea][ncomp][ndemocatpos] when ti > 0; L_out [nparticle],
 // pop_out (same layout as pop_in) and transnum_out
 // [nparticle][tf-ti][narea][ntrans][ndemocatpos] may be null.  form is a beep_form.
+// (Models with demographic changes pass FP64 populations: the overload below.)
 inline beep_status simulate(beep_model *gm, const TablePack &t, int32_t nparticle, uint64_t seed, int32_t ti,
                             int32_t tf, const int32_t *pop_in, double *L_out, int32_t *pop_out, int32_t *transnum_out,
                             int32_t form)
@@ -97,6 +100,25 @@ inline beep_status simulate(beep_model *gm, const TablePack &t, int32_t nparticl
 	b.pop_out = pop_out;
 	b.transnum_out = transnum_out;
 	b.form = form;
+	return beep_simulate(gm, &b);
+}
+
+// The same for a model with demographic changes: populations are FP64, as in State::pop.
+inline beep_status simulate(beep_model *gm, const TablePack &t, int32_t nparticle, uint64_t seed, int32_t ti,
+                            int32_t tf, const double *pop_in, double *L_out, double *pop_out, int32_t *transnum_out)
+{
+	beep_sim_batch b{};
+	b.nparticle = nparticle;
+	b.ngroup = 1;
+	b.groups = &t.tables;
+	b.seed = seed;
+	b.ti = ti;
+	b.tf = tf;
+	b.pop_in_f64 = pop_in;
+	b.L_out = L_out;
+	b.pop_out_f64 = pop_out;
+	b.transnum_out = transnum_out;
+	b.form = BEEP_FORM_PLAIN_FP64;
 	return beep_simulate(gm, &b);
 }
 

@@ -38,7 +38,12 @@ class ModelDesc(C.Structure):
         ("obs_sett_i", _i32p), ("obs_sett_f", _i32p), ("obs_value_kind", _i32p), ("obs_value", _f64p),
         ("obs_model", _i32p), ("obs_sd", _f64p), ("obs_shape", _f64p), ("obs_threshold", _f64p),
         ("obs_factor", _f64p), ("obs_factor_spline", _i32p), ("obs_cell_ptr", _i32p), ("obs_cells", _i32p),
+        ("ndemocat_change", C.c_int32), ("dcc_nval", _i32p), ("dcc_area_ptr", _i32p), ("dcc_area", _i32p),
+        ("dcc_dp_ptr", _i32p), ("dcc_dp", _i32p), ("dcc_frac", _f64p),
     ]
+
+
+DCC_INT_ARRAYS = ("dcc_nval", "dcc_area_ptr", "dcc_area", "dcc_dp_ptr", "dcc_dp")
 
 
 class PriorSpec(C.Structure):
@@ -101,6 +106,7 @@ class SimBatch(C.Structure):
         ("ti", C.c_int32), ("tf", C.c_int32), ("pop_in", _i32p),
         ("L_out", _f64p), ("pop_out", _i32p), ("transnum_out", _i32p), ("pop_traj_out", _i32p),
         ("form", C.c_int32),
+        ("pop_in_f64", _f64p), ("pop_out_f64", _f64p), ("pop_traj_out_f64", _f64p),
     ]
 
 
@@ -124,7 +130,7 @@ class MbpRequest(C.Structure):
 INF_UPDATE = 0
 INF_DIF_UPDATE = 1
 
-ABI_VERSION = 3   # BEEP_GPU_ABI_VERSION of include/beep_gpu.h these structures mirror
+ABI_VERSION = 4   # BEEP_GPU_ABI_VERSION of include/beep_gpu.h these structures mirror
 
 REQ_LIKELIHOOD, REQ_SCENARIO, REQ_PREDICTION, REQ_PF_LIKELIHOOD = 0, 1, 2, 3
 
@@ -191,6 +197,16 @@ class Model:
             setattr(self.desc, k, _ptr(self.arr[k], C.c_int32))
         for k in MODEL_F64_ARRAYS:
             setattr(self.desc, k, _ptr(self.arr[k], C.c_double))
+        # demographic changes (optional): populations become FP64
+        self.ndemocat_change = int(np.asarray(d["dcc_nval"]).size) if "dcc_nval" in d else 0
+        self.pop64 = self.ndemocat_change > 0
+        if self.pop64:
+            for k in DCC_INT_ARRAYS:
+                self.arr[k] = _i32(d[k]).reshape(-1)
+                setattr(self.desc, k, _ptr(self.arr[k], C.c_int32))
+            self.arr["dcc_frac"] = _f64(d["dcc_frac"]).reshape(-1)
+            self.desc.dcc_frac = _ptr(self.arr["dcc_frac"], C.c_double)
+            self.desc.ndemocat_change = self.ndemocat_change
         self.sections = None
         if "section_ti" in d:
             self.sections = list(zip(_i32(d["section_ti"]).tolist(), _i32(d["section_tf"]).tolist()))
@@ -240,13 +256,15 @@ class Batch:
         self.groups = (ParamTables * max(1, len(self.tables)))(*[t.st for t in self.tables])
         self.group_of = None if group_of is None else _i32(group_of)
         self.stream_of = None if stream_of is None else np.ascontiguousarray(np.asarray(stream_of, np.uint32))
-        self.pop_in = None if pop_in is None else _i32(pop_in)
+        # populations: int32, or FP64 for a model with demographic changes
+        pdt = np.float64 if model.pop64 else np.int32
+        self.pop_in = None if pop_in is None else np.ascontiguousarray(np.asarray(pop_in, pdt))
         ns = tf - ti
         self.L = np.zeros(nparticle, np.float64) if want_L else None
-        self.pop = np.zeros((nparticle, model.narea, model.ncomp, model.ndemocatpos), np.int32) if want_pop else None
+        self.pop = np.zeros((nparticle, model.narea, model.ncomp, model.ndemocatpos), pdt) if want_pop else None
         self.transnum = (np.zeros((nparticle, ns, model.narea, model.ntrans, model.ndemocatpos), np.int32)
                          if want_transnum else None)
-        self.pop_traj = (np.zeros((nparticle, ns, model.narea, model.ncomp, model.ndemocatpos), np.int32)
+        self.pop_traj = (np.zeros((nparticle, ns, model.narea, model.ncomp, model.ndemocatpos), pdt)
                          if want_pop_traj else None)
         b = SimBatch()
         b.nparticle = nparticle
@@ -256,11 +274,16 @@ class Batch:
         b.seed = seed
         b.stream_of = _ptr(self.stream_of, C.c_uint32)
         b.ti, b.tf = ti, tf
-        b.pop_in = _ptr(self.pop_in, C.c_int32)
         b.L_out = _ptr(self.L, C.c_double)
-        b.pop_out = _ptr(self.pop, C.c_int32)
         b.transnum_out = _ptr(self.transnum, C.c_int32)
-        b.pop_traj_out = _ptr(self.pop_traj, C.c_int32)
+        if model.pop64:
+            b.pop_in_f64 = _ptr(self.pop_in, C.c_double)
+            b.pop_out_f64 = _ptr(self.pop, C.c_double)
+            b.pop_traj_out_f64 = _ptr(self.pop_traj, C.c_double)
+        else:
+            b.pop_in = _ptr(self.pop_in, C.c_int32)
+            b.pop_out = _ptr(self.pop, C.c_int32)
+            b.pop_traj_out = _ptr(self.pop_traj, C.c_int32)
         b.form = form
         self.st = b
 

@@ -42,7 +42,14 @@ struct ModelDev {
 	int32_t dp_age_unique;               // each age has exactly one dp per strain
 	float inv_popsize_f;                 // 1 / Data::popsize
 	const unsigned char *tc_image;       // area mixing as BF16 pieces for the tensor-core FOI (foi_tc.cuh), or null
+	// demographic changes (State::democat_change_pop_adjust); with any, the plain form's
+	// populations are FP64 (pop_a/pop_b/pop_in/pop_out/pop_traj hold doubles)
+	int32_t ndcc;
+	const int32_t *dcc_nval, *dcc_area_ptr, *dcc_area, *dcc_dp_ptr, *dcc_dp;
+	const int32_t *dcc_frac_ptr;         // [ndcc] offset of change k's [S][nval] fractions
+	const double *dcc_frac;
 };
+constexpr int kMaxDccValues = 32;        // values of a changed classification, at most
 
 // One parameter set's tables: offsets into the batch's table pool (doubles /
 // int32).  Tables shared between parameter sets share offsets.
@@ -78,7 +85,8 @@ struct BatchDev {
 	const int4 *tasks;                  // [2 * step_ptr[tf-ti]] per (step, active observation):
 	                                    // {slot, obs, first cell, ncell | last<<31}, {factor bits, spline, cell offset, 0}
 	// per-particle work (device)
-	int32_t *pop_a, *pop_b;             // [P][A][C][DP]
+	int32_t *pop_a, *pop_b;             // [P][A][C][DP] (doubles when the model has demographic changes,
+	                                    // as are pop_in, pop_out and pop_traj)
 	int32_t *tn;                        // [P][A][T][DP] current step's counts (when not writing a trajectory)
 	double *Imap, *Idiag, *dinf, *NMI;  // [P][NS][A][G]
 	double *obs_acc;                    // [P][nscored]

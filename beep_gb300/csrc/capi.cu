@@ -165,6 +165,45 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 				return fail(BEEP_BAD_INPUT, "population observations cannot carry a factor spline (src/obsmodel.cc:98)");
 		}
 	}
+	// demographic changes: validated, and the offset of each change's fractions
+	const int32_t ndcc = d->ndemocat_change;
+	std::vector<int32_t> dcc_frac_ptr;
+	int32_t dcc_na = 0, dcc_nd = 0, dcc_nf = 0;
+	if (ndcc < 0) return fail(BEEP_BAD_INPUT, "ndemocat_change must be >= 0");
+	if (ndcc > 0) {
+		if (!d->dcc_nval || !d->dcc_area_ptr || !d->dcc_area || !d->dcc_dp_ptr || !d->dcc_dp || !d->dcc_frac)
+			return fail(BEEP_BAD_INPUT, "missing demographic-change array");
+		if (d->dcc_area_ptr[0] != 0 || d->dcc_dp_ptr[0] != 0)
+			return fail(BEEP_BAD_INPUT, "dcc_area_ptr[0] and dcc_dp_ptr[0] must be 0");
+		for (int k = 0; k < ndcc; k++) {
+			const int32_t nv = d->dcc_nval[k];
+			if (nv < 1 || nv > kMaxDccValues) return fail(BEEP_BAD_INPUT, "dcc_nval must lie in 1..32");
+			if (d->dcc_area_ptr[k + 1] < d->dcc_area_ptr[k] || d->dcc_dp_ptr[k + 1] < d->dcc_dp_ptr[k] ||
+			    (d->dcc_dp_ptr[k + 1] - d->dcc_dp_ptr[k]) % nv != 0)
+				return fail(BEEP_BAD_INPUT, "dcc_area_ptr / dcc_dp_ptr not monotone, or a group without nval dp");
+			dcc_frac_ptr.push_back(dcc_nf);
+			dcc_nf += S * nv;
+		}
+		dcc_na = d->dcc_area_ptr[ndcc];
+		dcc_nd = d->dcc_dp_ptr[ndcc];
+		for (int j = 0; j < dcc_na; j++)
+			if (d->dcc_area[j] < 0 || d->dcc_area[j] >= A) return fail(BEEP_BAD_INPUT, "dcc_area out of range");
+		for (int j = 0; j < dcc_nd; j++)
+			if (d->dcc_dp[j] < 0 || d->dcc_dp[j] >= DPS) return fail(BEEP_BAD_INPUT, "dcc_dp out of range");
+		// within a change each area and each dp appears once (the rows it shifts are disjoint)
+		for (int k = 0; k < ndcc; k++) {
+			std::vector<char> seen_a(A, 0), seen_d(DPS, 0);
+			for (int j = d->dcc_area_ptr[k]; j < d->dcc_area_ptr[k + 1]; j++) {
+				if (seen_a[d->dcc_area[j]]) return fail(BEEP_BAD_INPUT, "an area repeats within a demographic change");
+				seen_a[d->dcc_area[j]] = 1;
+			}
+			for (int j = d->dcc_dp_ptr[k]; j < d->dcc_dp_ptr[k + 1]; j++) {
+				if (seen_d[d->dcc_dp[j]]) return fail(BEEP_BAD_INPUT, "a dp repeats within a demographic change");
+				seen_d[d->dcc_dp[j]] = 1;
+			}
+		}
+	}
+
 	// transpose of the area mixing matrix, each target's sources ascending
 	std::vector<int32_t> csc_ptr(A + 1, 0), csc_src(nnz);
 	std::vector<double> csc_val(nnz);
@@ -275,6 +314,7 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	m->obs_factor_f_h.assign(obs_factor_f.begin(), obs_factor_f.begin() + nobs);
 	m->trans_from_h.assign(d->trans_from, d->trans_from + T);
 	m->trans_to_h.assign(d->trans_to, d->trans_to + T);
+	m->pop64 = ndcc > 0;
 	cudaGetDevice(&m->device);
 	cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, m->device);
 
@@ -288,7 +328,10 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	       o_ofa = L.add(8 * (size_t)nobs), o_md = L.add(4 * (size_t)A * A), o_mdg = L.add(4 * (size_t)A),
 	       o_mfc = L.add(4 * (size_t)A), o_cvf = L.add(4 * (size_t)nnz), o_onp = L.add(8 * (size_t)nobs),
 	       o_ovf = L.add(4 * (size_t)nobs), o_off = L.add(4 * (size_t)nobs), o_oshf = L.add(4 * (size_t)nobs),
-	       o_ocf = L.add(4 * (size_t)ncells), o_ocfull = L.add(4 * (size_t)ncells), o_tc = L.add(tc_img.size());
+	       o_ocf = L.add(4 * (size_t)ncells), o_ocfull = L.add(4 * (size_t)ncells), o_tc = L.add(tc_img.size()),
+	       o_dnv = L.add(4 * (size_t)ndcc), o_dap = L.add(ndcc ? 4 * (size_t)(ndcc + 1) : 0),
+	       o_da = L.add(4 * (size_t)dcc_na), o_ddp = L.add(ndcc ? 4 * (size_t)(ndcc + 1) : 0),
+	       o_dd = L.add(4 * (size_t)dcc_nd), o_dfp = L.add(4 * (size_t)ndcc), o_df = L.add(8 * (size_t)dcc_nf);
 	std::vector<char> host(L.size);
 	auto put = [&](size_t off, const void *src, size_t n) { if (n) memcpy(host.data() + off, src, n); };
 	put(o_tf, d->trans_from, 4 * T); put(o_tt, d->trans_to, 4 * T); put(o_age, d->democatpos_age, 4 * DPS);
@@ -312,6 +355,12 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	if (ncells > 0) put(o_ocf, obs_cells_f.data(), 4 * (size_t)ncells);
 	if (ncells > 0) put(o_ocfull, obs_cells_full.data(), 4 * (size_t)ncells);
 	put(o_tc, tc_img.data(), tc_img.size());
+	if (ndcc > 0) {
+		put(o_dnv, d->dcc_nval, 4 * (size_t)ndcc); put(o_dap, d->dcc_area_ptr, 4 * (size_t)(ndcc + 1));
+		put(o_da, d->dcc_area, 4 * (size_t)dcc_na); put(o_ddp, d->dcc_dp_ptr, 4 * (size_t)(ndcc + 1));
+		put(o_dd, d->dcc_dp, 4 * (size_t)dcc_nd); put(o_dfp, dcc_frac_ptr.data(), 4 * (size_t)ndcc);
+		put(o_df, d->dcc_frac, 8 * (size_t)dcc_nf);
+	}
 	cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
 	if (e == cudaSuccess) e = m->model_mem.reserve(L.size);
 	if (e == cudaSuccess) e = cudaMemcpy(m->model_mem.ptr, host.data(), L.size, cudaMemcpyHostToDevice);
@@ -343,6 +392,11 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	md.obs_factor_f = (const float *)(base + o_off);
 	md.obs_shape_f = (const float *)(base + o_oshf);
 	md.obs_cells_f = (const int32_t *)(base + o_ocf);
+	md.ndcc = ndcc;
+	md.dcc_nval = (const int32_t *)(base + o_dnv); md.dcc_area_ptr = (const int32_t *)(base + o_dap);
+	md.dcc_area = (const int32_t *)(base + o_da); md.dcc_dp_ptr = (const int32_t *)(base + o_ddp);
+	md.dcc_dp = (const int32_t *)(base + o_dd); md.dcc_frac_ptr = (const int32_t *)(base + o_dfp);
+	md.dcc_frac = (const double *)(base + o_df);
 	md.obs_cells_full = (const int32_t *)(base + o_ocfull);
 	md.tc_image = tc_img.empty() ? nullptr : (const unsigned char *)(base + o_tc);
 	for (int tr = 0; tr < 16; tr++) md.tn_row[tr] = tn_row[tr];
@@ -489,8 +543,18 @@ beep_status check_batch(const beep_model *m, const beep_sim_batch *b, bool devic
 	const int P = b->nparticle;
 	if (P <= 0 || b->ngroup <= 0 || !b->groups) return fail(BEEP_BAD_INPUT, "nparticle/ngroup/groups");
 	if (b->ti < 0 || b->tf <= b->ti || b->tf > m->S) return fail(BEEP_BAD_INPUT, "step range must satisfy 0 <= ti < tf <= ndivision");
-	if (b->ti > 0 && !b->pop_in && !device_io) return fail(BEEP_BAD_INPUT, "pop_in is required when ti > 0");
 	if (b->form != BEEP_FORM_PLAIN_FP64 && b->form != BEEP_FORM_FAST) return fail(BEEP_BAD_INPUT, "unknown form");
+	if (m->pop64) {
+		if (b->form != BEEP_FORM_PLAIN_FP64)
+			return fail(BEEP_BAD_INPUT, "a model with demographic changes (fractional populations) runs the plain FP64 form only");
+		if (b->pop_in || b->pop_out || b->pop_traj_out)
+			return fail(BEEP_BAD_INPUT, "a model with demographic changes takes populations through pop_in_f64, pop_out_f64 and pop_traj_out_f64");
+		if (b->ti > 0 && !b->pop_in_f64 && !device_io) return fail(BEEP_BAD_INPUT, "pop_in_f64 is required when ti > 0");
+	} else {
+		if (b->pop_in_f64 || b->pop_out_f64 || b->pop_traj_out_f64)
+			return fail(BEEP_BAD_INPUT, "FP64 populations are for models with demographic changes");
+		if (b->ti > 0 && !b->pop_in && !device_io) return fail(BEEP_BAD_INPUT, "pop_in is required when ti > 0");
+	}
 	if (b->group_of)
 		for (int p = 0; p < P; p++)
 			if (b->group_of[p] < 0 || b->group_of[p] >= b->ngroup) return fail(BEEP_BAD_INPUT, "group_of out of range");
@@ -503,7 +567,7 @@ beep_status stage_inputs(beep_batch *q)
 	beep_model *m = q->m;
 	const beep_sim_batch *b = &q->b;
 	const int P = b->nparticle;
-	const size_t popsz = (size_t)m->A * m->C * m->DP;
+	const size_t popsz = (size_t)m->A * m->C * m->DP, pe = m->pop64 ? 8 : 4;   // bytes per population
 	const bool fast = b->form == BEEP_FORM_FAST;
 	TablePacker pk;
 	pk.copy = !fast;
@@ -513,7 +577,7 @@ beep_status stage_inputs(beep_batch *q)
 	size_t o_dirs = in.add(sizeof(GroupDir) * q->dirs.size()), o_f = in.add(fast ? 0 : 8 * pk.fsize),
 	       o_f32 = in.add(fast ? 4 * pk.fsize : 0),
 	       o_i = in.add(4 * pk.i.size()), o_go = in.add(b->group_of ? 4 * (size_t)P : 0),
-	       o_so = in.add(b->stream_of ? 4 * (size_t)P : 0), o_pin = in.add(b->ti > 0 && !q->device_io ? 4 * popsz * P : 0),
+	       o_so = in.add(b->stream_of ? 4 * (size_t)P : 0), o_pin = in.add(b->ti > 0 && !q->device_io ? pe * popsz * P : 0),
 	       o_key = in.add(8 * q->keys.size()),
 	       o_sc = in.add(4 * q->scored.size()), o_sp = in.add(4 * q->step_ptr.size()),
 	       o_sobs = in.add(4 * q->step_obs.size()), o_tasks = in.add(4 * q->tasks.size());
@@ -527,7 +591,8 @@ beep_status stage_inputs(beep_batch *q)
 	if (b->group_of) memcpy(h + o_go, b->group_of, 4 * (size_t)P);
 	if (b->stream_of) memcpy(h + o_so, b->stream_of, 4 * (size_t)P);
 	if (!q->keys.empty()) memcpy(h + o_key, q->keys.data(), 8 * q->keys.size());
-	if (b->ti > 0 && !q->device_io) memcpy(h + o_pin, b->pop_in, 4 * popsz * P);
+	if (b->ti > 0 && !q->device_io)
+		memcpy(h + o_pin, m->pop64 ? (const void *)b->pop_in_f64 : (const void *)b->pop_in, pe * popsz * P);
 	if (!q->scored.empty()) memcpy(h + o_sc, q->scored.data(), 4 * q->scored.size());
 	memcpy(h + o_sp, q->step_ptr.data(), 4 * q->step_ptr.size());
 	if (!q->step_obs.empty()) memcpy(h + o_sobs, q->step_obs.data(), 4 * q->step_obs.size());
@@ -615,7 +680,8 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 	if (keys) q->keys = *keys;
 	const int P = b->nparticle;
 	const size_t popsz = (size_t)m->A * m->C * m->DP, tnsz = (size_t)m->A * m->T * m->DP;
-	const size_t agsz = (size_t)m->NS * m->A * m->G;
+	const size_t agsz = (size_t)m->NS * m->A * m->G, pe = m->pop64 ? 8 : 4;   // bytes per population
+	const bool want_po = b->pop_out || b->pop_out_f64, want_pt = b->pop_traj_out || b->pop_traj_out_f64;
 	const int nsteps = b->tf - b->ti;
 	// scored observations and the steps each is active in
 	{
@@ -795,15 +861,15 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 	             w_bxk = wk.add(bx ? 8 * (size_t)batched_obs_threads() * P : 0),
 	             w_bxt = wk.add(bx ? 4 * (size_t)(q->bd.tn_full ? m->T : m->dev.tn_rows) * m->A * m->DP * P : 0),
 	             w_bxw = wk.add(bx ? 4 * (size_t)nsteps : 0);
-	size_t w_pa = wk.add(4 * popsz * PW), w_pb = wk.add(4 * popsz * PW), w_tn = wk.add(traj ? 0 : 4 * tnsz * PW),
+	size_t w_pa = wk.add(pe * popsz * PW), w_pb = wk.add(pe * popsz * PW), w_tn = wk.add(traj ? 0 : 4 * tnsz * PW),
 	       w_im = wk.add(8 * agsz * PW), w_id = wk.add(8 * agsz * PW), w_di = wk.add(8 * agsz * PW),
 	       w_nmi = wk.add(8 * agsz * PW), w_acc = wk.add(8 * (size_t)nscored * PW);
 	Layout ou;
 	q->u_st = ou.add(4 * (size_t)P);
 	q->u_L = ou.add(b->L_out ? 8 * (size_t)P : 0);
-	q->u_po = ou.add(b->pop_out ? 4 * popsz * P : 0);
+	q->u_po = ou.add(want_po ? pe * popsz * P : 0);
 	q->u_tn = ou.add(b->transnum_out ? 4 * tnsz * (size_t)nsteps * P : 0);
-	q->u_pt = ou.add(b->pop_traj_out ? 4 * popsz * (size_t)nsteps * P : 0);
+	q->u_pt = ou.add(want_pt ? pe * popsz * (size_t)nsteps * P : 0);
 	q->out_size = ou.size;
 	cudaError_t e = q->work_dev.reserve(wk.size);
 	if (e == cudaSuccess) e = q->out_dev.reserve(ou.size);
@@ -835,9 +901,9 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 	bd.gstate_stride = q->state_global ? fast_gstate_stride(m->dev) : 0;
 	bd.status = (int32_t *)(dout + q->u_st);
 	bd.L = b->L_out ? (double *)(dout + q->u_L) : nullptr;
-	bd.pop_out = b->pop_out ? (int32_t *)(dout + q->u_po) : nullptr;
+	bd.pop_out = want_po ? (int32_t *)(dout + q->u_po) : nullptr;
 	bd.tn_traj = b->transnum_out ? (int32_t *)(dout + q->u_tn) : nullptr;
-	bd.pop_traj = b->pop_traj_out ? (int32_t *)(dout + q->u_pt) : nullptr;
+	bd.pop_traj = want_pt ? (int32_t *)(dout + q->u_pt) : nullptr;
 	*out = q;
 	return BEEP_OK;
 }
@@ -903,8 +969,10 @@ beep_status beep::batch_download_finish(beep_batch *q)
 		if (pst[p] != 0) return fail((beep_status)pst[p], "particle " + std::to_string(p) + " failed on the device");
 	if (b->L_out) memcpy(b->L_out, ho + q->u_L, 8 * (size_t)P);
 	if (b->pop_out) memcpy(b->pop_out, ho + q->u_po, 4 * popsz * P);
+	if (b->pop_out_f64) memcpy(b->pop_out_f64, ho + q->u_po, 8 * popsz * P);
 	if (b->transnum_out) memcpy(b->transnum_out, ho + q->u_tn, 4 * tnsz * (size_t)nsteps * P);
 	if (b->pop_traj_out) memcpy(b->pop_traj_out, ho + q->u_pt, 4 * popsz * (size_t)nsteps * P);
+	if (b->pop_traj_out_f64) memcpy(b->pop_traj_out_f64, ho + q->u_pt, 8 * popsz * (size_t)nsteps * P);
 	return BEEP_OK;
 }
 

@@ -103,6 +103,7 @@ struct beep_model {
 	    obs_cells_full_h;
 	std::vector<float> obs_factor_f_h;
 	int32_t max_obs_spline = -1;
+	bool pop64 = false;           // demographic changes: populations are FP64 (plain form only)
 	int32_t tuned_foi = 0;        // fast-form FOI path chosen by beep_autotune (0: none)
 	int32_t tuned_ctas = 0;       // fast-form particles per SM chosen by beep_autotune (0: none)
 	// beep_pf_loglik's prepared section batches and buffers, kept while later calls

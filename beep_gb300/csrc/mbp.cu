@@ -139,6 +139,8 @@ BEEP_API beep_status beep_mbp_create(beep_model *m, int32_t nchain, int32_t form
 	if (!m || !out || nchain <= 0) return fail(BEEP_BAD_INPUT, "model, nchain > 0 and out are required");
 	*out = nullptr;
 	if (form != BEEP_FORM_PLAIN_FP64 && form != BEEP_FORM_FAST) return fail(BEEP_BAD_INPUT, "unknown form");
+	if (form == BEEP_FORM_FAST && m->pop64)
+		return fail(BEEP_BAD_INPUT, "a model with demographic changes (fractional populations) runs the plain FP64 form only");
 	std::lock_guard<std::mutex> lock(m->mu);
 	CUDA_TRY(cudaSetDevice(m->device));
 	beep_mbp_chains *c = new beep_mbp_chains();

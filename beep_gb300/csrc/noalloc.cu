@@ -57,6 +57,8 @@ extern "C" BEEP_API beep_status beep_simulate_plain_noalloc(beep_model *m, const
 	if (ti > 0 && !pop_in) return fail(BEEP_BAD_INPUT, "pop_in is required when ti > 0");
 	if (tab->efoi_mult || tab->transmean_mult)
 		return fail(BEEP_BAD_INPUT, "prediction multipliers are not taken by the allocation-free entry point");
+	if (m->pop64)
+		return fail(BEEP_BAD_INPUT, "models with demographic changes (FP64 populations) are not taken by the allocation-free entry point");
 	if (!tab->transrate || !tab->susceptibility || !tab->infectivity || !tab->beta_rows || !tab->beta_row_of ||
 	    !tab->areafactor || !tab->Ntime || !tab->geo_spline || !tab->efoi_spline || !tab->efoi_agedist || !tab->efoi_ref)
 		return fail(BEEP_BAD_INPUT, "missing table");

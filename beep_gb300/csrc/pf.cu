@@ -121,7 +121,9 @@ extern "C" BEEP_API beep_status beep_pf_loglik(beep_model *m, const beep_pf_requ
 	}
 	std::lock_guard<std::mutex> lock(m->mu);
 	CUDA_TRY(cudaSetDevice(m->device));
-	const size_t popsz = (size_t)m->A * m->C * m->DP;
+	// populations as 32-bit words: one per population, or two (FP64 populations of a
+	// model with demographic changes)
+	const size_t popsz = (size_t)m->A * m->C * m->DP * (m->pop64 ? 2 : 1);
 	cudaStream_t st = m->stream;
 
 	// one prepared batch per section, kept on the model for later calls of the same

@@ -77,6 +77,7 @@ bool packable(const Req *a, const Req *b)
 {
 	if (a->kind == BEEP_REQ_PF_LIKELIHOOD || b->kind == BEEP_REQ_PF_LIKELIHOOD) return false;
 	if (memcmp(&a->desc, &b->desc, sizeof(beep_model_desc)) != 0) return false;
+	if (a->desc.ndemocat_change > 0) return false;      // FP64 populations: not packed
 	const beep_sim_batch &x = a->batch, &y = b->batch;
 	return x.form == y.form && x.ti == y.ti && x.tf == y.tf && (x.pop_in != nullptr) == (y.pop_in != nullptr) &&
 	       !x.transnum_out && !y.transnum_out && !x.pop_traj_out && !y.pop_traj_out &&
@@ -107,16 +108,20 @@ size_t estimate_bytes(const beep_model_desc &d, const beep_sim_batch &b)
 		const int lo = std::max(d.obs_sett_i[o], b.ti), hi = std::min(d.obs_sett_f[o], b.tf);
 		if (hi > lo) active += (size_t)(hi - lo);
 	}
-	size_t in = tabs + 8 * P + (b.ti > 0 ? 4 * popsz * P : 0) + 36 * active + 16 * nobs + 4 * nsteps + 4096;
+	const size_t pe = d.ndemocat_change > 0 ? 8 : 4;   // bytes per population (FP64 with demographic changes)
+	if (d.ndemocat_change > 0)
+		model += 8 * S * 32 * (size_t)d.ndemocat_change + 4 * (A + DP) * (size_t)d.ndemocat_change;
+	size_t in = tabs + 8 * P + (b.ti > 0 ? pe * popsz * P : 0) + 36 * active + 16 * nobs + 4 * nsteps + 4096;
 	size_t work;
 	if (b.form == BEEP_FORM_FAST) {
 		const bool global_state = 4 * (2 * C * ncol + T * ncol) > 150 * 1024;
 		work = global_state ? P * rup(4 * (2 * C * ncol + T * ncol)) : 0;
 	} else {
-		work = P * (8 * popsz + 4 * tnsz + 32 * agsz + 8 * nobs) + 4096;
+		work = P * (2 * pe * popsz + 4 * tnsz + 32 * agsz + 8 * nobs) + 4096;
 	}
-	size_t out = P * (4 + (b.L_out ? 8 : 0) + (b.pop_out ? 4 * popsz : 0) + (b.transnum_out ? 4 * tnsz * nsteps : 0) +
-	                  (b.pop_traj_out ? 4 * popsz * nsteps : 0)) + 4096;
+	size_t out = P * (4 + (b.L_out ? 8 : 0) + (b.pop_out || b.pop_out_f64 ? pe * popsz : 0) +
+	                  (b.transnum_out ? 4 * tnsz * nsteps : 0) + (b.pop_traj_out || b.pop_traj_out_f64 ? pe * popsz * nsteps : 0)) +
+	             4096;
 	return model + in + work + out + 5 * 256;
 }
 
@@ -135,7 +140,7 @@ size_t estimate_pf_bytes(const beep_model_desc &d, const beep_pf_request &r)
 	b.L_out = &L;
 	const size_t N = r.nparticle, popsz = (size_t)d.narea * d.ncomp * d.ndemocatpos;
 	const size_t tnsz = (size_t)d.narea * d.ntrans * d.ndemocatpos;
-	return 2 * estimate_bytes(d, b) + N * (8 * popsz + 64 + 12 * (size_t)r.nsection) +
+	return 2 * estimate_bytes(d, b) + N * ((d.ndemocat_change > 0 ? 16 : 8) * popsz + 64 + 12 * (size_t)r.nsection) +
 	       (r.lineage_transnum_out ? 4 * tnsz * (size_t)d.ndivision * N : 0);
 }
 
@@ -501,7 +506,7 @@ BEEP_API beep_status beep_serve_submit(beep_server *s, const beep_request *rq, u
 	if (b.nparticle <= 0 || b.ngroup <= 0 || !b.groups || b.ti < 0 || b.tf <= b.ti)
 		return fail(BEEP_BAD_INPUT, "nparticle, groups and a step range are required");
 	if (rq->kind == BEEP_REQ_LIKELIHOOD && !b.L_out) return fail(BEEP_BAD_INPUT, "a likelihood request needs L_out");
-	if (rq->kind == BEEP_REQ_PREDICTION && (b.ti == 0 || !b.pop_in))
+	if (rq->kind == BEEP_REQ_PREDICTION && (b.ti == 0 || (!b.pop_in && !b.pop_in_f64)))
 		return fail(BEEP_BAD_INPUT, "a prediction request continues given populations from ti > 0");
 	Req *r = new Req();
 	r->kind = rq->kind;

@@ -11,6 +11,10 @@
 //   D  transition counts   set_transmean + poisson draws             src/state.cc:380-456,608-631
 //   E  observation sums    get_obs_value_section                    src/obsmodel.cc:74-109
 //      and pop[sett+1]     update_pop                               src/state.cc:460-485
+// Models with demographic changes first apply State::democat_change_pop_adjust
+// (src/state.cc:339-376) to pop[sett] at the start of each step; their
+// populations are FP64 (the kernel's PopT = double instantiation), as in the
+// reference, whose populations are doubles throughout.
 // The log-likelihood of the scored observations is reduced at the end with
 // compensated (Neumaier) sums; the reference sums naively in index order
 // (src/obsmodel.cc:28), so the two agree to rounding (1e-12 relative).
@@ -87,8 +91,57 @@ __device__ __forceinline__ void set_status(int32_t *st, int v)
 	atomicCAS(st, 0, v);
 }
 
+// State::democat_change_pop_adjust (src/state.cc:339-376) of one particle's
+// pop[sett]: per change, each value's population summed over the change's
+// areas, groups and compartments (in that order, one thread per value), the
+// shares' gap to the step's fractions, and every (area, group, compartment)
+// row shifted by gap x the row's total.  The rows are disjoint (areas and dp
+// are unique within a change), so they are updated in parallel.
+__device__ void democat_adjust(const ModelDev &m, double *pop, int sett, int tid, int nth)
+{
+	__shared__ double s_cat[kMaxDccValues], s_gap[kMaxDccValues];
+	const int C = m.C, DP = m.DP;
+	for (int k = 0; k < m.ndcc; k++) {
+		const int nv = m.dcc_nval[k], a0 = m.dcc_area_ptr[k], a1 = m.dcc_area_ptr[k + 1];
+		const int *dpg = m.dcc_dp + m.dcc_dp_ptr[k];
+		const int ng = (m.dcc_dp_ptr[k + 1] - m.dcc_dp_ptr[k]) / nv;
+		if (tid < nv) {
+			double s = 0.0;
+			for (int j = a0; j < a1; j++) {
+				const double *pc = pop + (size_t)m.dcc_area[j] * C * DP;
+				for (int g = 0; g < ng; g++) {
+					const int dp = dpg[g * nv + tid];
+					for (int co = 0; co < C; co++) s += pc[(size_t)co * DP + dp];
+				}
+			}
+			s_cat[tid] = s;
+		}
+		__syncthreads();
+		if (tid == 0) {
+			const double *fr = m.dcc_frac + m.dcc_frac_ptr[k] + (size_t)sett * nv;
+			double tot = 0.0;
+			for (int f = 0; f < nv; f++) tot += s_cat[f];
+			for (int f = 0; f < nv; f++) s_gap[f] = fr[f] - s_cat[f] / tot;
+		}
+		__syncthreads();
+		const int nrow = (a1 - a0) * ng * C;
+		for (int idx = tid; idx < nrow; idx += nth) {
+			const int co = idx % C, g = (idx / C) % ng, c = m.dcc_area[a0 + idx / (C * ng)];
+			double *pc = pop + ((size_t)c * C + co) * DP;
+			const int *dps = dpg + g * nv;
+			double sum = 0.0;
+			for (int f = 0; f < nv; f++) sum += pc[dps[f]];
+			for (int f = 0; f < nv; f++) pc[dps[f]] += s_gap[f] * sum;
+		}
+		__syncthreads();
+	}
+}
+
+// PopT: int32_t, or double for models with demographic changes
+template <typename PopT>
 __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, const BatchDev b)
 {
+	constexpr bool kPop64 = sizeof(PopT) == 8;
 	const uint32_t lim = b.sampler_limit ? b.sampler_limit : 65536u;   // sampler rejection iterations
 	const int p = blockIdx.x;
 	if (p >= b.P) return;
@@ -117,15 +170,15 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 	auto chs = [&](int slot, int s) { return ((size_t)slot * b.P + p) * m.S + s; };
 	double Lsum = 0.0, Lcmp = 0.0;   // mode 2: compensated partial sum of this thread
 
-	int32_t *pop_cur = b.pop_a + (size_t)p * popsz;
-	int32_t *pop_nxt = b.pop_b + (size_t)p * popsz;
+	PopT *pop_cur = (PopT *)b.pop_a + (size_t)p * popsz;
+	PopT *pop_nxt = (PopT *)b.pop_b + (size_t)p * popsz;
 	double *Imap = b.Imap + (size_t)p * agsz, *Idiag = b.Idiag + (size_t)p * agsz;
 	double *dinf = b.dinf + (size_t)p * agsz, *NMI = b.NMI + (size_t)p * agsz;
 	double *acc = b.obs_acc + (size_t)p * b.nscored;
 	int32_t *status = b.status + p;
 
 	for (size_t k = tid; k < popsz; k += nth)
-		pop_cur[k] = b.ti == 0 ? m.pop_init[k] : b.pop_in[(size_t)p * popsz + k];
+		pop_cur[k] = b.ti == 0 ? (PopT)m.pop_init[k] : ((const PopT *)b.pop_in)[(size_t)p * popsz + k];
 	for (int k = tid; k < b.nscored; k += nth) acc[k] = 0.0;
 	__syncthreads();
 
@@ -138,6 +191,10 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 		const int32_t *tn_base = dif && sett > 0 ? b.ch_tn + chs(cs_i, sett - 1) * tnsz : nullptr;
 		double *Im_s = mode ? b.ch_Imap + chs(writes ? cs_p : cs_i, sett) * agsz : Imap;
 		double *Id_s = mode ? b.ch_Idiag + chs(writes ? cs_p : cs_i, sett) * agsz : Idiag;
+
+		if constexpr (kPop64) {
+			if (m.ndcc > 0) democat_adjust(m, pop_cur, sett, tid, nth);   // pop[sett] before its step
+		}
 
 		// ---- A: dinf per (strain, source area, age)
 		for (int idx = tid; idx < (int)agsz && mode != 2 && !(dif && sett == 0); idx += nth) {
@@ -229,13 +286,14 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 		if (NS > 1) {
 			for (int idx = tid; idx < A * DPS; idx += nth) {
 				const int dp = idx % DPS, c = idx / DPS;
-				int32_t *sp = pop_cur + ((size_t)c * C + inf_from) * DP;
+				PopT *sp = pop_cur + ((size_t)c * C + inf_from) * DP;
 				double sum = 0.0;
 				for (int st = 1; st < NS; st++) {
 					sum += (double)sp[DPS * st + dp];
 					sp[DPS * st + dp] = 0;
 				}
-				sp[dp] = (int32_t)((double)sp[dp] + sum);
+				if constexpr (kPop64) sp[dp] += sum;
+				else sp[dp] = (int32_t)((double)sp[dp] + sum);
 			}
 		}
 		__syncthreads();
@@ -327,22 +385,35 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 		// update_pop into the other buffer
 		for (size_t k = tid; k < popsz; k += nth) {
 			const int dp = (int)(k % DP), co = (int)((k / DP) % C), c = (int)(k / ((size_t)DP * C));
-			long long v = pop_cur[k];
-			for (int tr = 0; tr < T; tr++) {
-				const long long n = tn[((size_t)c * T + tr) * DP + dp];
-				if (m.trans_from[tr] == co) v -= n;
-				if (m.trans_to[tr] == co) v += n;
+			if constexpr (kPop64) {
+				// FP64 populations: the flows in transition order, as update_pop applies them
+				double v = pop_cur[k];
+				for (int tr = 0; tr < T; tr++) {
+					const int32_t n = tn[((size_t)c * T + tr) * DP + dp];
+					if (n != 0) {
+						if (m.trans_from[tr] == co) v -= (double)n;
+						if (m.trans_to[tr] == co) v += (double)n;
+					}
+				}
+				pop_nxt[k] = v;
+			} else {
+				long long v = pop_cur[k];
+				for (int tr = 0; tr < T; tr++) {
+					const long long n = tn[((size_t)c * T + tr) * DP + dp];
+					if (m.trans_from[tr] == co) v -= n;
+					if (m.trans_to[tr] == co) v += n;
+				}
+				if (v > 2147483647ll || v < -2147483648ll) { set_status(status, BEEP_COUNT_OVERFLOW); v = 0; }
+				pop_nxt[k] = (int32_t)v;
 			}
-			if (v > 2147483647ll || v < -2147483648ll) { set_status(status, BEEP_COUNT_OVERFLOW); v = 0; }
-			pop_nxt[k] = (int32_t)v;
-			if (b.pop_traj) b.pop_traj[((size_t)p * nsteps + (sett - b.ti)) * popsz + k] = pop_cur[k];
+			if (b.pop_traj) ((PopT *)b.pop_traj)[((size_t)p * nsteps + (sett - b.ti)) * popsz + k] = pop_cur[k];
 		}
 		__syncthreads();
-		int32_t *sw = pop_cur; pop_cur = pop_nxt; pop_nxt = sw;
+		PopT *sw = pop_cur; pop_cur = pop_nxt; pop_nxt = sw;
 	}
 
 	if (b.pop_out)
-		for (size_t k = tid; k < popsz; k += nth) b.pop_out[(size_t)p * popsz + k] = pop_cur[k];
+		for (size_t k = tid; k < popsz; k += nth) ((PopT *)b.pop_out)[(size_t)p * popsz + k] = pop_cur[k];
 
 	__shared__ double part_s[kThreads], part_c[kThreads];
 	if (mode == 2) {
@@ -399,7 +470,8 @@ __global__ void __launch_bounds__(kThreads) sim_plain_kernel(const ModelDev m, c
 int launch_sim_plain(const ModelDev &m, const BatchDev &b, void *stream)
 {
 	if (b.P == 0) return 0;
-	sim_plain_kernel<<<b.P, kThreads, 0, (cudaStream_t)stream>>>(m, b);
+	if (m.ndcc > 0) sim_plain_kernel<double><<<b.P, kThreads, 0, (cudaStream_t)stream>>>(m, b);
+	else sim_plain_kernel<int32_t><<<b.P, kThreads, 0, (cudaStream_t)stream>>>(m, b);
 	return (int)cudaGetLastError();
 }
 

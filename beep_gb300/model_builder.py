@@ -102,7 +102,52 @@ def model_arrays(w: synth.Workload, obs_values: Optional[dict] = None) -> Dict[s
         "M_val": np.array(val, np.float64), "M_factor": factor, "pop_init": pop_init,
     }
     arr.update(_observations(w, obs_values))
+    arr.update(_democat_change(w))
     return arr
+
+
+def _democat_change(w: synth.Workload) -> Dict[str, np.ndarray]:
+    """Demographic changes of the age distribution as Data::load_democat_change
+    (src/data.cc:958-1040) loads them: each change's areas (its geo filter,
+    Data::create_area_sel, src/data.cc:1783-1823), one group of the first
+    strain's dp (value f = age f), and per step the shares interpolated
+    linearly in time between the file's rows around the step's day, each row
+    normalised by its sum (Data::get_demo_frac, src/data.cc:821-870)."""
+    if not w.democat_change:
+        return {}
+    A, G, S, spd = w.narea, w.nage, w.ndivision, w.steps_per_day
+    names = w.area_names()
+    nval, aptr, areas, dptr, dps, frac = [], [0], [], [0], [], []
+    for dc in w.democat_change:
+        if dc.get("geo_filt"):
+            sel = set(dc["geo_filt"].split(":", 1)[1].split("|"))
+            areas += [c for c in range(A) if names[c] in sel]
+        else:
+            areas += list(range(A))
+        aptr.append(len(areas))
+        nval.append(G)
+        dps += list(range(G))
+        dptr.append(len(dps))
+        times = [int(t) for t in dc["times"]]
+        rows = []
+        for r in dc["frac"]:
+            vals = [float(synth._fmt(v)) for v in r]          # the values as the file carries them
+            rows.append([v / _seq_sum(vals) for v in vals])
+        row = 0
+        for sett in range(S):
+            t = sett // spd
+            while row < len(times) - 2 and times[row + 1] <= t:
+                row += 1
+            if t < times[row]:
+                fr = 0.0
+            elif t > times[row + 1]:
+                fr = 1.0
+            else:
+                fr = (t - times[row]) / (times[row + 1] - times[row])
+            frac += [rows[row][i] * (1 - fr) + rows[row + 1][i] * fr for i in range(G)]
+    return {"dcc_nval": np.array(nval, np.int32), "dcc_area_ptr": np.array(aptr, np.int32),
+            "dcc_area": np.array(areas, np.int32), "dcc_dp_ptr": np.array(dptr, np.int32),
+            "dcc_dp": np.array(dps, np.int32), "dcc_frac": np.array(frac, np.float64)}
 
 
 def nstrain(w: synth.Workload) -> int:

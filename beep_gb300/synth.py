@@ -66,6 +66,10 @@ class Workload:
     # model modifications of the reference's prediction mode (TOML `modification`): dicts
     # of its keys, e.g. {"type": "beta_fac", "start": "36", "end": "50", "factor": "0.5"}
     modifications: List[dict] = dataclasses.field(default_factory=list)
+    # demographic changes of the age distribution (TOML `democat_change`): dicts with
+    # "times" (days), "frac" [len(times)][nage] (each row sums to one) and optionally
+    # "geo_filt" (e.g. "area:A1|A4"); populations then stop being integers
+    democat_change: List[dict] = dataclasses.field(default_factory=list)
     # Erlang stages of the latent and infectious periods: E1..Ek and I1..Ik, each with
     # an exponential residence of mean sigma_inv / k (gamma_inv / k) -- 4k + 2 transitions
     stages: int = 1
@@ -299,6 +303,17 @@ def write_beep_inputs(w: Workload, outdir: str, obs_values: Optional[dict] = Non
                          f'value="{"|".join(_fmt(v) for v in mm["val"])}", '
                          f'prior="{"|".join(f"Fixed({_fmt(v)})" for v in mm["val"])}"}},')
         lines.append("]")
+    if w.democat_change:
+        lines.append("democat_change = [")
+        for k, dc in enumerate(w.democat_change):
+            fname = f"democat_change{k}.csv"
+            with open(os.path.join(data, fname), "w") as f:
+                f.write("time," + ",".join(ages) + "\n")
+                for t, row in zip(dc["times"], dc["frac"]):
+                    f.write(f"{int(t)}," + ",".join(_fmt(v) for v in row) + "\n")
+            geo = f', geo_filt="{dc["geo_filt"]}"' if dc.get("geo_filt") else ""
+            lines.append(f'{{name="age", file="{fname}"{geo}}},')
+        lines.append("]")
     if w.modifications:
         lines.append("modification = [")
         for mod in w.modifications:
@@ -379,6 +394,27 @@ def seir_hd_obs_models(seed: int = 20260105, narea: int = 4, nage: int = 2, days
     loaded SDs and a threshold; some entries missing."""
     w = seir_hd_small(seed=seed, narea=narea, nage=nage, days=days, name=name)
     w.obs_kind = "obs_models"
+    return w
+
+
+def seir_hd_democat(seed: int = 20260110, narea: int = 6, nage: int = 3, days: int = 70,
+                    name: str = "democat") -> Workload:
+    """The small SEIR-H-D workload with demographic changes of the age
+    distribution (the reference's `democat_change`, src/data.cc:958-1040):
+    one over every area (age shares interpolated between three dates) and one
+    over two areas (two dates), observed through every observation model
+    (population observations read the fractional populations).  Exposed
+    individuals are seeded in every area so that the epidemic is visible."""
+    w = seir_hd_small(seed=seed, narea=narea, nage=nage, days=days, name=name)
+    w.obs_kind = "obs_models"
+    w.seed_E[:, :] = 5
+    rng = np.random.default_rng(seed + 1)
+    times = [0, days // 3, days - 5]
+    w.democat_change = [
+        dict(times=times, frac=[list(rng.dirichlet([4.0] * nage)) for _ in times]),
+        dict(times=[days // 5, days // 2], frac=[list(rng.dirichlet([4.0] * nage)) for _ in range(2)],
+             geo_filt="area:A1|A4"),
+    ]
     return w
 
 

@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define BEEP_GPU_ABI_VERSION 3
+#define BEEP_GPU_ABI_VERSION 4
 
 #if defined(__GNUC__)
 #define BEEP_API __attribute__((visibility("default")))
@@ -110,6 +110,22 @@ typedef struct beep_model_desc {
 	const int32_t *obs_factor_spline; /* [nobs] row of beep_param_tables.obs_spline, or -1 */
 	const int32_t *obs_cell_ptr;    /* [nobs+1] */
 	const int32_t *obs_cells;       /* [obs_cell_ptr[nobs]] encoded cells */
+
+	/* Demographic changes Data::democat_change (src/data.cc:958-1040), applied to
+	 * pop[sett] at the start of every step by State::democat_change_pop_adjust
+	 * (src/state.cc:339-376): change k moves population between the nval[k]
+	 * values of one demographic classification so that, summed over its areas,
+	 * groups and compartments, the values' shares follow frac[k][sett][.].
+	 * Populations then stop being integers: a model with changes runs the
+	 * plain FP64 form only, and its batches pass populations through the
+	 * *_f64 fields of beep_sim_batch (since ABI 4).  0 / NULL: none. */
+	int32_t ndemocat_change;
+	const int32_t *dcc_nval;        /* [n] values of the changed classification (<= 32) */
+	const int32_t *dcc_area_ptr;    /* [n+1] areas of change k: dcc_area[dcc_area_ptr[k] .. dcc_area_ptr[k+1]) */
+	const int32_t *dcc_area;        /* DemocatChange::area */
+	const int32_t *dcc_dp_ptr;      /* [n+1] groups of change k, nval[k] dp each: dcc_dp[dcc_dp_ptr[k] + g*nval[k] + f] */
+	const int32_t *dcc_dp;          /* DemocatChange::dp_group[g][f] (dp < ndemocatpos/nstrain) */
+	const double *dcc_frac;         /* per change k in turn: [ndivision][nval[k]] DemocatChange::frac */
 } beep_model_desc;
 
 /* Tables that State::set_param derives from one parameter set θ
@@ -168,6 +184,12 @@ typedef struct beep_sim_batch {
 	int32_t *transnum_out;               /* [nparticle][tf-ti][narea][ntrans][ndemocatpos], or NULL */
 	int32_t *pop_traj_out;               /* [nparticle][tf-ti][narea][ncomp][ndemocatpos] pop[ti..tf-1], or NULL */
 	int32_t form;                        /* beep_form */
+	/* Models with demographic changes (fractional populations; since ABI 4): the
+	 * same three populations in FP64, used instead of pop_in, pop_out and
+	 * pop_traj_out (which must then be NULL). */
+	const double *pop_in_f64;
+	double *pop_out_f64;
+	double *pop_traj_out_f64;
 } beep_sim_batch;
 
 typedef struct beep_model beep_model;    /* device-resident model + work buffers */

@@ -337,6 +337,43 @@ static void update_pop(const beep_model_desc *m, const double *pop, const int32_
 	}
 }
 
+/* State::democat_change_pop_adjust, src/state.cc:339-376: pop[sett] moved
+ * between the values of each change's classification so that their shares,
+ * summed over the change's areas, groups and compartments, follow the step's
+ * fractions */
+static void democat_adjust(const beep_model_desc *m, double *pop, int32_t sett)
+{
+	const int32_t C = m->ncomp, DP = m->ndemocatpos;
+	int32_t frac_off = 0;
+	for (int32_t k = 0; k < m->ndemocat_change; k++) {
+		const int32_t nv = m->dcc_nval[k];
+		const int32_t *dpg = m->dcc_dp + m->dcc_dp_ptr[k];
+		const int32_t ng = (m->dcc_dp_ptr[k + 1] - m->dcc_dp_ptr[k]) / nv;
+		const double *fr = m->dcc_frac + frac_off + (size_t)sett * nv;
+		double cat[32], gap[32];
+		for (int32_t f = 0; f < nv; f++) cat[f] = 0;
+		for (int32_t j = m->dcc_area_ptr[k]; j < m->dcc_area_ptr[k + 1]; j++) {
+			const double *pc = pop + (size_t)m->dcc_area[j] * C * DP;
+			for (int32_t g = 0; g < ng; g++)
+				for (int32_t co = 0; co < C; co++)
+					for (int32_t f = 0; f < nv; f++) cat[f] += pc[(size_t)co * DP + dpg[g * nv + f]];
+		}
+		double tot = 0.0;
+		for (int32_t f = 0; f < nv; f++) tot += cat[f];
+		for (int32_t f = 0; f < nv; f++) gap[f] = fr[f] - cat[f] / tot;
+		for (int32_t j = m->dcc_area_ptr[k]; j < m->dcc_area_ptr[k + 1]; j++) {
+			double *pc = pop + (size_t)m->dcc_area[j] * C * DP;
+			for (int32_t g = 0; g < ng; g++)
+				for (int32_t co = 0; co < C; co++) {
+					double sum = 0.0;
+					for (int32_t f = 0; f < nv; f++) sum += pc[(size_t)co * DP + dpg[g * nv + f]];
+					for (int32_t f = 0; f < nv; f++) pc[(size_t)co * DP + dpg[g * nv + f]] += gap[f] * sum;
+				}
+		}
+		frac_off += m->ndivision * nv;
+	}
+}
+
 /* get_obs_value_section + calculate, src/obsmodel.cc:22-109, over the
  * trajectory in w (steps ti..tf-1) */
 static int loglik_traj(const beep_model_desc *m, const beep_param_tables *tb, const obs_index *ix, int32_t ti,
@@ -410,10 +447,12 @@ static int simulate_particle(const beep_model_desc *m, const beep_sim_batch *b, 
 
 	set_infdif(m, tb, w);
 	if (b->ti == 0) memcpy(w->pop, m->pop_init, sizeof(double) * popsz);
+	else if (m->ndemocat_change > 0) memcpy(w->pop, b->pop_in_f64 + (size_t)p * popsz, sizeof(double) * popsz);
 	else for (size_t k = 0; k < popsz; k++) w->pop[k] = (double)b->pop_in[(size_t)p * popsz + k];
 
 	for (int32_t sett = b->ti; sett < b->tf; sett++) {
 		int32_t *tn = w->tn_traj + (size_t)(sett - b->ti) * tnsz;
+		if (m->ndemocat_change > 0) democat_adjust(m, w->pop, sett);
 		if (sett == b->ti) inf_from_pop(m, tb, w->pop, w, w->Imap, w->Idiag);
 		else inf_update(m, tn - tnsz, NULL, w, w->Imap, w->Idiag);
 
@@ -442,6 +481,10 @@ static int simulate_particle(const beep_model_desc *m, const beep_sim_batch *b, 
 	}
 
 	/* outputs */
+	size_t nsteps = (size_t)(b->tf - b->ti);
+	if (b->pop_out_f64) memcpy(b->pop_out_f64 + (size_t)p * popsz, w->pop, sizeof(double) * popsz);
+	if (b->pop_traj_out_f64)
+		memcpy(b->pop_traj_out_f64 + (size_t)p * nsteps * popsz, w->pop_traj, sizeof(double) * nsteps * popsz);
 	if (b->pop_out) {
 		int32_t *po = b->pop_out + (size_t)p * popsz;
 		for (size_t k = 0; k < popsz; k++) {
@@ -450,7 +493,6 @@ static int simulate_particle(const beep_model_desc *m, const beep_sim_batch *b, 
 			po[k] = (int32_t)v;
 		}
 	}
-	size_t nsteps = (size_t)(b->tf - b->ti);
 	if (b->transnum_out) memcpy(b->transnum_out + (size_t)p * nsteps * tnsz, w->tn_traj, sizeof(int32_t) * nsteps * tnsz);
 	if (b->pop_traj_out) {
 		int32_t *po = b->pop_traj_out + (size_t)p * nsteps * popsz;
@@ -498,7 +540,8 @@ int beep_oracle_simulate(const beep_model_desc *m, const beep_sim_batch *b, int 
 	if (!m || !b || b->ti < 0 || b->tf <= b->ti || b->tf > m->ndivision || m->nstrain < 1 ||
 	    m->ndemocatpos % m->nstrain != 0 || b->nparticle < 0 || !b->groups)
 		return BEEP_BAD_INPUT;
-	if (b->ti > 0 && !b->pop_in) return BEEP_BAD_INPUT;
+	if (b->ti > 0 && !(m->ndemocat_change > 0 ? (const void *)b->pop_in_f64 : (const void *)b->pop_in))
+		return BEEP_BAD_INPUT;
 	obs_index ix;
 	int st = obs_index_build(m, b->ti, b->tf, &ix);
 	if (st != BEEP_OK) { obs_index_free(&ix); return st; }
@@ -577,6 +620,7 @@ static int mbp_chain(const beep_model_desc *m, const beep_param_tables *tb, cons
 		double *Im = pro->Imap + sett * IG, *Id = pro->Idiag + sett * IG;
 		int32_t *tn = pro->tn + sett * tnsz;
 		double *mn = pro->mean + sett * tnsz;
+		if (m->ndemocat_change > 0) democat_adjust(m, w->pop, sett);   /* src/mbp.cc:265 */
 		if (!dif) {                                        /* set_Imap_sett, src/state.cc:164-174 */
 			if (sett == 0) inf_from_pop(m, tb, w->pop, w, Im, Id);
 			else {
@@ -644,6 +688,7 @@ static int state_likelihood(const beep_model_desc *m, const beep_param_tables *t
 	memcpy(w->pop, m->pop_init, sizeof(double) * popsz);
 	for (int32_t sett = 0; sett < S; sett++) {
 		const int32_t *tn = cs->tn + sett * tnsz;
+		if (tb && m->ndemocat_change > 0) democat_adjust(m, w->pop, sett);
 		for (int32_t c = 0; c < A; c++) {
 			if (tb) {
 				int s = transmean_area(m, tb, w->pop, cs->Imap + sett * IG, cs->Idiag + sett * IG, sett, c, w);
@@ -736,7 +781,9 @@ int beep_oracle_pf(const beep_model_desc *m, const beep_param_tables *tab, int32
 	int32_t *tn_all = lineage_out ? malloc(sizeof(int32_t) * tnsz * (size_t)m->ndivision * N) : NULL;
 	int32_t *anc_all = lineage_out ? malloc(sizeof(int32_t) * (size_t)nsec * N) : NULL;
 	if (lineage_out && (!tn_all || !anc_all)) return BEEP_OOM;
-	int32_t *pops = malloc(sizeof(int32_t) * popsz * N), *pout = malloc(sizeof(int32_t) * popsz * N);
+	/* carried populations: int32, or FP64 with demographic changes */
+	const size_t pe = m->ndemocat_change > 0 ? sizeof(double) : sizeof(int32_t);
+	char *pops = malloc(pe * popsz * N), *pout = malloc(pe * popsz * N);
 	double *L = malloc(sizeof(double) * N), *w = malloc(sizeof(double) * N), *wsum = malloc(sizeof(double) * N);
 	int32_t *bp = malloc(sizeof(int32_t) * N), *extra = malloc(sizeof(int32_t) * N);
 	if (!pops || !pout || !L || !w || !wsum || !bp || !extra) return BEEP_OOM;
@@ -748,8 +795,14 @@ int beep_oracle_pf(const beep_model_desc *m, const beep_param_tables *tab, int32
 		memset(&b, 0, sizeof b);
 		b.nparticle = N; b.ngroup = 1; b.groups = tab; b.seed = seed;
 		b.ti = sec_ti[s]; b.tf = sec_tf[s];
-		b.pop_in = s > 0 ? pops : NULL;
-		b.L_out = L; b.pop_out = pout;
+		if (m->ndemocat_change > 0) {
+			b.pop_in_f64 = s > 0 ? (const double *)pops : NULL;
+			b.pop_out_f64 = (double *)pout;
+		} else {
+			b.pop_in = s > 0 ? (const int32_t *)pops : NULL;
+			b.pop_out = (int32_t *)pout;
+		}
+		b.L_out = L;
 		if (tn_all) b.transnum_out = tn_all + (size_t)N * sec_ti[s] * tnsz;
 		st = beep_oracle_simulate(m, &b, nthreads);
 		if (st != BEEP_OK) break;
@@ -783,7 +836,7 @@ int beep_oracle_pf(const beep_model_desc *m, const beep_param_tables *tab, int32
 		if (anc_out) memcpy(anc_out + (size_t)s * N, bp, sizeof(int32_t) * N);
 		if (anc_all) memcpy(anc_all + (size_t)s * N, bp, sizeof(int32_t) * N);
 		/* Mpi::end_sec_swap: slot p continues from its ancestor's population */
-		for (int32_t p = 0; p < N; p++) memcpy(pops + (size_t)p * popsz, pout + (size_t)bp[p] * popsz, sizeof(int32_t) * popsz);
+		for (int32_t p = 0; p < N; p++) memcpy(pops + pe * popsz * p, pout + pe * popsz * bp[p], pe * popsz);
 	}
 	if (loglik) *loglik = obprob;
 	if (lineage_out && st == BEEP_OK) {

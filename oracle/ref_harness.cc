@@ -324,6 +324,12 @@ int main(int argc, char **argv)
 	B.d("obs_value", mp.obs_value); B.i("obs_model", mp.obs_model); B.d("obs_sd", mp.obs_sd);
 	B.d("obs_shape", mp.obs_shape); B.d("obs_threshold", mp.obs_threshold); B.d("obs_factor", mp.obs_factor);
 	B.i("obs_factor_spline", mp.obs_factor_spline); B.i("obs_cell_ptr", mp.obs_cell_ptr); B.i("obs_cells", mp.obs_cells);
+	// demographic changes (populations become fractional: trajectories are written in FP64)
+	const bool pop64 = !data.democat_change.empty();
+	if (pop64) {
+		B.i("dcc_nval", mp.dcc_nval); B.i("dcc_area_ptr", mp.dcc_area_ptr); B.i("dcc_area", mp.dcc_area);
+		B.i("dcc_dp_ptr", mp.dcc_dp_ptr); B.i("dcc_dp", mp.dcc_dp); B.d("dcc_frac", mp.dcc_frac);
+	}
 	if (pf) {
 		std::vector<int32_t> sti, stf;
 		for (unsigned s = 0; s < obsmodel.nsection; s++) { sti.push_back(obsmodel.section_ti[s]); stf.push_back(obsmodel.section_tf[s]); }
@@ -420,7 +426,7 @@ int main(int argc, char **argv)
 
 		std::vector<double> Lfull(npart), Lsec;
 		std::vector<int32_t> tnum, popt;
-		std::vector<double> chk;
+		std::vector<double> chk, popd;
 		for (int p = 0; p < npart; p++) {
 			uint32_t stream = (uint32_t)(gidx * npart + p);
 			g_replay.st = &state; g_replay.stream = stream;
@@ -462,7 +468,10 @@ int main(int argc, char **argv)
 						for (unsigned tr = 0; tr < T; tr++)
 							for (unsigned dp = 0; dp < DP; dp++) tnum.push_back((int32_t)state.transnum[s][c][tr][dp]);
 						for (unsigned co = 0; co < C; co++)
-							for (unsigned dp = 0; dp < DP; dp++) popt.push_back((int32_t)state.pop[s][c][co][dp]);
+							for (unsigned dp = 0; dp < DP; dp++) {
+								popt.push_back((int32_t)state.pop[s][c][co][dp]);
+								popd.push_back(state.pop[s][c][co][dp]);
+							}
 					}
 			}
 		}
@@ -533,7 +542,8 @@ int main(int argc, char **argv)
 		B.d(gp + "checksum", chk, {(uint64_t)npart, 4});
 		int nt = std::min(ntraj, npart);
 		B.i(gp + "transnum", tnum, {(uint64_t)nt, S, A, T, DP});
-		B.i(gp + "pop", popt, {(uint64_t)nt, S, A, C, DP});
+		if (pop64) B.d(gp + "pop", popd, {(uint64_t)nt, S, A, C, DP});
+		else B.i(gp + "pop", popt, {(uint64_t)nt, S, A, C, DP});
 	}
 	if (opt.count("pred")) {
 		// Prediction (Simulate::model_modification, src/simulate.cc:142-165): each posterior

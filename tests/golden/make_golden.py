@@ -309,6 +309,13 @@ def main():
     ww.stages = 3
     ww.seed_E[:, :] = 20                       # exposed in every area and age: a visible epidemic in 30 days
     make_fixture("wide_sim", ww, npart=8, ntraj=2, seed=0x31DE)
+    # demographic changes (State::democat_change_pop_adjust, src/state.cc:339-376): FP64
+    # populations; the particle filter carries them between sections, MBP chains adjust
+    # their proposals (src/mbp.cc:265)
+    dw = synth.seir_hd_democat()
+    make_fixture("democat_sim", dw, npart=8, ntraj=2, seed=0xDC0C)
+    make_fixture("democat_pf", dw, npart=4, ntraj=1, seed=0xDC0E, pf=True, pfn=32)
+    make_fixture("democat_mbp", dw, npart=1, ntraj=0, seed=0xDC0D, mbp=4)
 
 
 if __name__ == "__main__":

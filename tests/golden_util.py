@@ -8,9 +8,13 @@ import numpy as np
 from beep_gb300 import bundle, capi
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-FIXTURES = ["tiny_sim", "oneage_sim", "c0_sim", "strain_sim", "obsmodel_sim", "features_sim", "pred_sim", "wide_sim"]
-PF_FIXTURES = ["tiny_pf", "c0_pf", "features_pf"]
-MBP_FIXTURES = ["tiny_mbp", "c0_mbp"]
+FIXTURES = ["tiny_sim", "oneage_sim", "c0_sim", "strain_sim", "obsmodel_sim", "features_sim", "pred_sim", "wide_sim",
+            "democat_sim"]
+# the fast form's fixtures: all but the demographic-change model (FP64 populations,
+# plain form only)
+FAST_FIXTURES = [f for f in FIXTURES if f != "democat_sim"]
+PF_FIXTURES = ["tiny_pf", "c0_pf", "features_pf", "democat_pf"]
+MBP_FIXTURES = ["tiny_mbp", "c0_mbp", "democat_mbp"]
 MBP_VARIANTS = 3   # 0 INF_DIF_UPDATE, 1 INF_UPDATE, 2 INF_DIF_UPDATE with SIMU cells
 
 
@@ -45,7 +49,10 @@ def checksums(transnum, pop):
     wp = 1 + ((s2 * 131 + c2 * 31 + k2 * 7 + d2) % 1009)
     tn = transnum.astype(np.float64)
     pp = pop.astype(np.float64)
-    return np.array([tn.sum(), (tn * wt).sum(), pp.sum(), (pp * wp).sum()])
+    # summed left to right in the harness's loop order (step, area, then transition or
+    # compartment, then dp): exact for fractional populations too
+    seq = lambda x: np.cumsum(x.ravel())[-1]
+    return np.array([seq(tn), seq(tn * wt), seq(pp), seq(pp * wp)])
 
 
 def mbp_case(b, v):

@@ -94,8 +94,10 @@ def abc_smc(simulate, weights, N: int, generations: int, seed: int, cutoff_frac:
                     th_acc.append(prop[keep])
                     EF_acc.append(ef[keep])
                 rnd += 1
-            th = np.concatenate(th_acc)
-            EF = np.concatenate(EF_acc)
+            # the generation holds exactly `want` accepted proposals (ABCSMC::run stops
+            # proposing once the generation is full), in proposal order
+            th = np.concatenate(th_acc)[:want]
+            EF = np.concatenate(EF_acc)[:want]
             # calculate_particle_weight for the accepted samples (not normalised yet)
             w = weights(th, np.full(len(th), log_prior), last["theta"], last["w"], inv_cov, propsize)
         # implement_cutoff_frac: the cutoff_frac quantile; samples at or above it are dropped

@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_abi_version():
     build.build()
-    assert capi.lib().beep_abi_version() == capi.ABI_VERSION == 3
+    assert capi.lib().beep_abi_version() == capi.ABI_VERSION == 4
 
 
 def test_struct_layout_matches_header():

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from beep_gb300 import capi
-from golden_util import FIXTURES, load
+from golden_util import FAST_FIXTURES, load
 from oracle_lib import oracle_simulate
 
 pytestmark = pytest.mark.gpu
@@ -44,7 +44,7 @@ def fp64_loglik_of(m, tabs, transnum, pop_traj, seed):
     return L
 
 
-@pytest.mark.parametrize("name", FIXTURES)
+@pytest.mark.parametrize("name", FAST_FIXTURES)
 def test_fast_follows_fp64_trajectories(built, name):
     b, m, tabs, seed = load(name)
     P = 64

@@ -9,7 +9,10 @@ form give the same posterior means and variances within Monte Carlo error.
   oracle's, EF for EF.
 * PMCMC (src/pmcmc.cc:33-114, 180-268): 500 random-walk Metropolis-Hastings
   iterations on the 10-area x 3-age model, the likelihood estimated by the
-  bootstrap particle filter (256 particles, sections of 28 steps).  The
+  bootstrap particle filter (256 particles, sections of 28 steps) at inverse
+  temperature invT = 0.1 (the reference's tempered PMCMC, invT of src/pmcmc.cc:24,230-235:
+  at invT = 1 the estimate's standard deviation is ~30 nats with 256
+  particles and no chain of this length mixes; at 0.1 it is ~0.8).  The
   plain form's chain is the oracle's chain, iteration for iteration; the
   fast form's chain agrees in posterior mean (batch-means standard errors)
   and variance."""
@@ -55,8 +58,11 @@ def test_abc_smc_posteriors_agree(built):
     for k, g in runs.items():
         assert len(g[-1]["theta"]) == 2048
         assert final[k][2] > 200, (k, final[k][2])             # effective sample size
-        # the posterior contracted from the prior (R0 U(1.5,4), 1/sigma U(2,6), 1/gamma U(3,8))
-        assert np.all(final[k][1] < np.array([2.5, 4.0, 5.0]) ** 2 / 12), (k, final[k][1])
+        # the cut-off falls from generation to generation, and the posterior of R0 (the
+        # parameter daily cases identify; prior U(1.5, 4)) contracts to under 0.6 of the
+        # prior variance (two oracle runs of other seeds: 0.42-0.47)
+        assert all(a["EFcut"] > b["EFcut"] for a, b in zip(g, g[1:])), k
+        assert final[k][1][0] < 0.6 * 2.5 ** 2 / 12, (k, final[k][1])
     _agree(*final["plain"], *final["oracle"], "plain vs oracle")
     _agree(*final["fast"], *final["plain"], "fast vs plain")
     _agree(*final["fast"], *final["oracle"], "fast vs oracle")
@@ -78,8 +84,9 @@ def test_pmcmc_chains_agree(built):
     S = m.ndivision
     sections = [(a, min(a + 28, S)) for a in range(0, S, 28)]
     N = 256
+    invT = 0.1
     lo, hi = np.array([0.5, 2.0]), np.array([2.0, 6.0])          # R(t) scale, 1/sigma
-    step = np.array([0.03, 0.25])
+    step = np.array([0.06, 0.7])                                 # ~30% acceptance
 
     def tables(th):
         return capi.Tables(mb.param_tables(w, sigma_inv=float(th[1]), R_scale=float(th[0])))
@@ -87,10 +94,10 @@ def test_pmcmc_chains_agree(built):
     dm = capi.DeviceModel(m)
 
     def gpu_ll(form):
-        return lambda th, k: dm.pf_loglik(tables(th), N, 9000 + k, k, 1.0, sections, form=form)[0]
+        return lambda th, k: dm.pf_loglik(tables(th), N, 9000 + k, k, invT, sections, form=form)[0]
 
     def oracle_ll(th, k):
-        return oracle_pf(m, tables(th), N, 9000 + k, k, 1.0, sections)[0]
+        return oracle_pf(m, tables(th), N, 9000 + k, k, invT, sections)[0]
 
     th0 = np.array([1.0, 4.0])
     iters = 500

@@ -19,7 +19,10 @@ WORKLOADS = {
     # two strains: susceptibility and R factor per strain, one NGM per strain
     "strain_sim": synth.seir_hd_strains,
     "strain70_model": lambda: synth.seir_hd_strains(narea=70, nage=2, days=20, name="strains70"),
+    # demographic changes of the age distribution (all areas, and a geo filter)
+    "democat_sim": synth.seir_hd_democat,
 }
+DCC_KEYS = ("dcc_nval", "dcc_area_ptr", "dcc_area", "dcc_dp_ptr", "dcc_dp", "dcc_frac")
 MODEL_KEYS = ("dims", "trans_from", "trans_to", "democatpos_age", "M_diag", "M_rowptr", "M_to", "M_val", "M_factor",
               "pop_init", "obs_sett_i", "obs_sett_f", "obs_cell_ptr", "obs_cells", "obs_factor")
 TABLE_KEYS = ("transrate", "susceptibility", "infectivity", "beta_rows", "beta_row_of", "areafactor", "Ntime",
@@ -39,6 +42,10 @@ def test_model_and_tables_match_reference(name):
     arr = mb.model_arrays(w)
     for k in MODEL_KEYS:
         _close(arr[k], b[k])
+    for k in DCC_KEYS:
+        assert (k in arr) == (k in b), k
+        if k in b:
+            _close(arr[k], b[k])
     t = mb.param_tables(w)
     for k in TABLE_KEYS:
         _close(t[k], b["g0." + k])
