@@ -329,6 +329,10 @@ __global__ void __launch_bounds__(kBxStepThreads, MB) bx_step(const ModelDev m, 
 	int32_t *trow = (int32_t *)take(4 * (size_t)T);
 	int32_t *age = (int32_t *)take(4 * (size_t)DPS);
 	float *dgeo = (float *)take(16);
+	// each thread's column: populations and transition means, [row][thread] (the 32
+	// threads of a warp touch 32 consecutive words), indexed by compartment and transition
+	int32_t *cpv = (int32_t *)take(4 * (size_t)kMaxC * NT) + tid;
+	float *cmv = (float *)take(4 * (size_t)kMaxT * NT) + tid;
 	for (int k = tid; k < T; k += NT) {
 		from[k] = m.trans_from[k];
 		to[k] = m.trans_to[k];
@@ -387,22 +391,16 @@ __global__ void __launch_bounds__(kBxStepThreads, MB) bx_step(const ModelDev m, 
 		for (int col = k * kBxChunk + tid; col < col1; col += NT) {
 			const int c = col / DP, dp = col - c * DP;
 			const int st = dp / DPS, dpl = dp - st * DPS, a = age[dpl];
-			int32_t pv[kMaxC];
-#pragma unroll
-			for (int co = 0; co < kMaxC; co++) pv[co] = co < C ? pc[co * ncol + col] : 0;
+			for (int co = 0; co < C; co++) cpv[co * NT] = pc[co * ncol + col];
 			if (b.pop_traj)
-#pragma unroll
-				for (int co = 0; co < kMaxC; co++)
-					if (co < C) b.pop_traj[((size_t)p * nsteps + s_rel) * popsz + ((size_t)c * C + co) * DP + dp] = pv[co];
+				for (int co = 0; co < C; co++)
+					b.pop_traj[((size_t)p * nsteps + s_rel) * popsz + ((size_t)c * C + co) * DP + dp] = cpv[co * NT];
 			U4 inv{0, 0, 0, 0};
 			uint32_t inv_call = 0xffffffffu;
 			float minf = 0.f;
 			{
-				int32_t su = 0;
-#pragma unroll
-				for (int co = 0; co < kMaxC; co++) su = co == inf_from ? pv[co] : su;
 				// the infection transition's source of strain st is read at its strain-0 column
-				const float popu = st == 0 ? (float)su : (float)pc[inf_from * ncol + c * DP + dpl];
+				const float popu = st == 0 ? (float)cpv[inf_from * NT] : (float)pc[inf_from * ncol + c * DP + dpl];
 				if (popu > 0.f) {
 					const float fac = m.M_factor_f[c], dg = m.M_diag_f[c];
 					const float *Icc = Ic + (st * A + c) * G, *Yc = Y + (st * A + c) * G;
@@ -421,26 +419,19 @@ __global__ void __launch_bounds__(kBxStepThreads, MB) bx_step(const ModelDev m, 
 					minf = dt * popu * sus[dp] * (be[sc] * nmi + et[sc] * eage);
 				}
 			}
-			float mv[kMaxT];
-#pragma unroll
-			for (int tr = 0; tr < kMaxT; tr++) {
-				mv[tr] = 0.f;
-				if (tr < T) {
-					if (tr == itr) mv[tr] = minf;
-					else {
-						int32_t pf = 0;
-#pragma unroll
-						for (int co = 0; co < kMaxC; co++) pf = co == from[tr] ? pv[co] : pf;
-						const float popu = (float)pf;
-						mv[tr] = popu <= 0.f ? 0.f : dt * popu * rate[tr * DP + dp];
-					}
-					if (tb.tm_mult) mv[tr] *= __ldg(tb.tm_mult + ((size_t)sett * A + c) * T * DP + tr * DP + dp);
+			// every mean from the step's populations before any count is applied
+			for (int tr = 0; tr < T; tr++) {
+				float mv;
+				if (tr == itr) mv = minf;
+				else {
+					const float popu = (float)cpv[from[tr] * NT];
+					mv = popu <= 0.f ? 0.f : dt * popu * rate[tr * DP + dp];
 				}
+				if (tb.tm_mult) mv *= __ldg(tb.tm_mult + ((size_t)sett * A + c) * T * DP + tr * DP + dp);
+				cmv[tr * NT] = mv;
 			}
 			for (int tr = 0; tr < T; tr++) {
-				float mean = mv[0];
-#pragma unroll
-				for (int kk = 1; kk < kMaxT; kk++) mean = tr == kk ? mv[kk] : mean;
+				const float mean = cmv[tr * NT];
 				int32_t n = 0;
 				if (mean > 0.f) {
 					if (mean > 1.0e9f) atomicCAS(status, 0, BEEP_COUNT_OVERFLOW);
@@ -454,21 +445,15 @@ __global__ void __launch_bounds__(kBxStepThreads, MB) bx_step(const ModelDev m, 
 				if (row >= 0) tn[row * ncol + col] = n;
 				if (b.tn_traj) b.tn_traj[((size_t)p * nsteps + s_rel) * tnsz + ((size_t)c * T + tr) * DP + dp] = n;
 				if (n != 0) {
-					const int f = from[tr], t2 = to[tr];
-#pragma unroll
-					for (int co = 0; co < kMaxC; co++) {
-						if (co == f) pv[co] -= n;
-						if (co == t2) pv[co] += n;
-					}
+					cpv[from[tr] * NT] -= n;
+					cpv[to[tr] * NT] += n;
 				}
 			}
 			float iv = 0.f;
-#pragma unroll
-			for (int co = 0; co < kMaxC; co++) {
-				if (co < C) {
-					pn[co * ncol + col] = pv[co];
-					if (inf[co] != 0.f) iv = fmaf(inf[co], (float)pv[co], iv);
-				}
+			for (int co = 0; co < C; co++) {
+				const int32_t v = cpv[co * NT];
+				pn[co * ncol + col] = v;
+				if (inf[co] != 0.f) iv = fmaf(inf[co], (float)v, iv);
 			}
 			if (m.dp_age_unique) Icp[(st * A + c) * G + a] = iv;
 			else atomicAdd(Icp + (st * A + c) * G + a, iv);   // cleared by the step's observation kernel
@@ -598,7 +583,7 @@ size_t batched_step_smem(const ModelDev &m, int)
 	auto r = [](size_t x) { return (x + 15) & ~(size_t)15; };
 	const size_t A = m.A, G = m.G, DP = m.DP, NS = m.NS, C = m.C, T = m.T, DPS = m.DPS;
 	return 2 * r(4 * NS * A) + r(4 * G * G) + r(4 * T * DP) + r(4 * DP) + r(4 * C) + r(4 * 64) + r(4 * 32) +
-	       3 * r(4 * T) + r(4 * DPS) + 16;
+	       3 * r(4 * T) + r(4 * DPS) + 16 + 4 * (size_t)(kMaxC + kMaxT) * kBxStepThreads;
 }
 
 int batched_obs_threads() { return kBxObsThreads; }

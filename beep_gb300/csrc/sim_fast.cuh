@@ -100,16 +100,25 @@ __device__ __forceinline__ float ptrs_rhs(float k, float mean, float loglam, con
 }
 
 // FP32 Poisson draw on the keyed stream of the FP64 form (same counters/words).
+// The Philox blocks are computed by the warp's calling lanes together: when a
+// lane of the warp needs the inversion words of its column or the first PTRS
+// pair, every calling lane computes its own (same counters, so the same
+// values), instead of the warp issuing the block once for the inversion lanes
+// and again for the PTRS lanes.
 __device__ __forceinline__ int32_t poisson_fp32(float mean, uint32_t k0, uint32_t k1, uint32_t col, uint32_t tr,
                                                 uint32_t sett, uint32_t stream, U4 &inv, uint32_t &inv_call,
                                                 const float *rcp, const float *lnfact, uint32_t limit)
 {
-	if (mean < 10.f) {
-		const uint32_t call = tr >> 2;
-		if (inv_call != call) {
-			inv = philox10(U4{col, sett, stream, (PURPOSE_INV << 24) | call}, k0, k1);
-			inv_call = call;
-		}
+	const unsigned act = __activemask();
+	const bool big = mean >= 10.f;
+	const uint32_t call = tr >> 2;
+	if (__any_sync(act, !big && inv_call != call)) {
+		inv = philox10(U4{col, sett, stream, (PURPOSE_INV << 24) | call}, k0, k1);
+		inv_call = call;
+	}
+	U4 r0{0, 0, 0, 0};
+	if (__any_sync(act, big)) r0 = philox10(U4{col, sett, stream, (PURPOSE_PTRS << 24) | (tr << 16)}, k0, k1);
+	if (!big) {
 		const float u = u01_f(word_of(inv, tr & 3u));
 		float p = expf(-mean);
 		float F = p;
@@ -132,7 +141,7 @@ __device__ __forceinline__ int32_t poisson_fp32(float mean, uint32_t k0, uint32_
 	const float log_invalpha = __logf(invalpha);
 	const float two_a = 2.0f * a;
 	for (uint32_t it = 0; it < limit; it++) {
-		const U4 r = philox10(U4{col, sett, stream, (PURPOSE_PTRS << 24) | (tr << 16) | it}, k0, k1);
+		const U4 r = it == 0 ? r0 : philox10(U4{col, sett, stream, (PURPOSE_PTRS << 24) | (tr << 16) | it}, k0, k1);
 		const float U = u01_f(r.x) - 0.5f;
 		const float V = u01_f(r.y);
 		const float us = 0.5f - fabsf(U);

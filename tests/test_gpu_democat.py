@@ -69,8 +69,7 @@ def test_sections_carry_fp64_populations(built, model60):
     P, S = 16, m.ndivision
     dm = capi.DeviceModel(m)
     res = []
-    for sim in (dm.simulate, oracle_simulate):
-        run = (lambda b: sim(b)) if sim is dm.simulate else (lambda b: sim(m, b))
+    for run in (dm.simulate, lambda bt: oracle_simulate(m, bt)):
         a = run(capi.Batch(m, tabs, P, 5, ti=0, tf=S // 2, want_transnum=True, want_pop=True))
         b = run(capi.Batch(m, tabs, P, 5, ti=S // 2, tf=S, pop_in=a.pop, want_transnum=True, want_pop=True))
         res.append((a, b))
