@@ -12,7 +12,13 @@ reference oracle with oracle/Makefile.ref.  For each fixture:
      log-likelihoods, checksums and (for a few particles) full transition and
      population trajectories are saved as a bundle ``<name>.bnd``.
 
-usage: python tests/golden/make_golden.py [--ref REFERENCE_TREE]
+usage: python tests/golden/make_golden.py [--ref REFERENCE_TREE] [--only NAMES]
+                                         [--harness BINARY --outdir DIR]
+
+--harness runs another build of the harness (for instance the reference
+compiled with its own CMake flags, -mfma and the compiler's default FP
+contraction) and --outdir writes its bundles elsewhere, so that they can be
+compared with the committed ones.
 """
 from __future__ import annotations
 
@@ -140,12 +146,14 @@ def prior_theta_rows(w: synth.Workload):
 
 
 ONLY = None   # fixture names to (re)generate (--only); None: all
+OUTDIR = HERE  # where the bundles go (--outdir)
 
 
 def make_fixture(name, w: synth.Workload, npart, ntraj, seed, pf=False, theta_rows=None, keep_dir=None, pfn=0,
-                 mbp=0, samples=False, abcw=None, outdir=HERE):
+                 mbp=0, samples=False, abcw=None, outdir=None):
     if ONLY is not None and name not in ONLY:
         return
+    outdir = outdir or OUTDIR
     work = tempfile.mkdtemp(prefix=f"golden_{name}_")
     try:
         toml = synth.write_beep_inputs(w, work)
@@ -229,7 +237,7 @@ def make_prediction_fixture(name, w: synth.Workload, ngroup, npart, seed):
                 # parser rejects the exponent form an EF above 1e6 takes (the prediction does not use it)
                 samples.write_sample(sdir, k, 0.0, names, bs[f"g{g}.theta"], bs[f"g{g}.transnum"][p], times)
                 k += 1
-        out = os.path.join(HERE, f"{name}.bnd")
+        out = os.path.join(OUTDIR, f"{name}.bnd")
         cmd = [HARNESS, f"out={out}", "npart=4", "ntraj=2", f"seed={seed}", "pf=0", f"pred={sdir}",
                f"predn={ngroup * npart}", "--", f"inputfile={os.path.basename(toml)}", "mode=prediction",
                f"prediction_end={w.days}"]   # the inference horizon: the splines keep their knots
@@ -246,10 +254,18 @@ def main():
     ap.add_argument("--ref", default=os.environ.get("BEEP_REF_DIR") or os.path.join(os.path.dirname(ROOT), "reference"))
     ap.add_argument("--keep", default=None, help="keep the generated TOML/CSV inputs here")
     ap.add_argument("--only", default=None, help="comma-separated fixture names to (re)generate; default all")
+    ap.add_argument("--harness", default=None, help="a harness binary to run instead of oracle/_ref/ref_harness")
+    ap.add_argument("--outdir", default=None, help="write the bundles here instead of tests/golden")
     a = ap.parse_args()
-    global ONLY
+    global ONLY, HARNESS, OUTDIR
     ONLY = set(a.only.split(",")) if a.only else None
-    subprocess.run(["make", "-s", "-f", "oracle/Makefile.ref", f"REF={a.ref}", "-j8"], cwd=ROOT, check=True)
+    if a.outdir:
+        OUTDIR = os.path.abspath(a.outdir)
+        os.makedirs(OUTDIR, exist_ok=True)
+    if a.harness:
+        HARNESS = os.path.abspath(a.harness)
+    else:
+        subprocess.run(["make", "-s", "-f", "oracle/Makefile.ref", f"REF={a.ref}", "-j8"], cwd=ROOT, check=True)
 
     # tiny: 4 areas x 3 ages, 40 days at dt 0.25
     tiny = synth.seir_hd_small(seed=20260100, narea=4, nage=3, days=40, name="tiny")
