@@ -602,7 +602,7 @@ int launch_sim_batched(const ModelDev &m, const BatchDev &b, int sms, void *stre
 	cudaStream_t st = (cudaStream_t)stream;
 	cudaEvent_t *ev = (cudaEvent_t *)events;
 	return m.G <= 4 ? launch_steps<4, 6>(m, b, smem, sms, st, ev) : m.G <= 8 ? launch_steps<8, 6>(m, b, smem, sms, st, ev)
-	     : m.G <= 12 ? launch_steps<12, 5>(m, b, smem, sms, st, ev) : launch_steps<16, 5>(m, b, smem, sms, st, ev);
+	     : m.G <= 12 ? launch_steps<12, 6>(m, b, smem, sms, st, ev) : launch_steps<16, 5>(m, b, smem, sms, st, ev);
 }
 
 }  // namespace beep

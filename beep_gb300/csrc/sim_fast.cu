@@ -21,7 +21,7 @@ size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_
 	       (state_global && !tn_smem ? 0 : r(4 * (size_t)tnrows * ncol)) + 3 * r(4 * agsz) +
 	       r(4 * (size_t)nslots) + 3 * r(4 * T) + r(4 * DPS) + r(4 * C) + r(4 * T * DP) + r(4 * DP) + r(4 * 64) +
 	       r(4 * 32) + 2 * r(4 * NS * A) + r(4 * (size_t)nefoi_stage * G) + 2 * (2 * r(4 * NS * A) + r(4 * G * G)) +
-	       r(8) + r(4 * 2 * (size_t)(nt > 0 ? nt : pick_threads(m)));
+	       r(8) + r(4 * 2 * (size_t)(nt > 0 ? nt : pick_threads(m))) + (nt == kDualThreads ? r(4 * T * (size_t)nt) : 0);
 }
 
 int fast_threads() { return kFastThreads; }

@@ -82,6 +82,7 @@ struct FastSmem {
 	float *N0, *N1;       // [G][G] age mixing
 	float *dgeo;          // [2] geographic spline value
 	float *red;           // [2*NT]
+	float *mv;            // [T][NT] each thread's transition means (320-thread CTAs, whose registers are tight)
 };
 
 __host__ __device__ inline int ms_lda(int A) { return A + ((40 - A % 32) % 32); }
@@ -585,6 +586,7 @@ __global__ void __launch_bounds__(NT, MB) sim_fast_kernel(const ModelDev m, cons
 		s.N1 = (float *)take(4 * (size_t)G * G);
 		s.dgeo = (float *)take(4 * 2);
 		s.red = (float *)take(4 * 2 * (size_t)NT);
+		s.mv = NT == kDualThreads ? (float *)take(4 * (size_t)T * NT) : nullptr;
 	}
 	// tensor-core FOI (large models, 640 threads): chunk ring, stacked counts, barriers, tensor memory
 	__shared__ uint64_t tc_bars[2 * tc::kStages + 1];
@@ -719,26 +721,38 @@ __global__ void __launch_bounds__(NT, MB) sim_fast_kernel(const ModelDev m, cons
 					minf = dt * popu * s.sus[dp] * (be[sc] * nmi + et[sc] * eage);
 				}
 			}
-			float mv[MT];
-#pragma unroll
-			for (int tr = 0; tr < MT; tr++) {
-				mv[tr] = 0.f;
-				if (tr < T) {
-					if (tr == itr) mv[tr] = minf;
-					else {
-						const float popu = (float)pc[s.from[tr] * ncol + col];
-						mv[tr] = popu <= 0.f ? 0.f : dt * popu * s.rate[tr * DP + dp];
-					}
-					if (tb.tm_mult) mv[tr] *= __ldg(tb.tm_mult + ((size_t)sett * A + c) * T * DP + tr * DP + dp);
+			// the means: in registers, or (320-thread CTAs) in the thread's shared-memory column
+			constexpr bool kMvSmem = NT == kDualThreads;
+			float mv[kMvSmem ? 1 : MT];
+			float *mvs = s.mv + tid;
+			auto mean_of = [&](int tr) {
+				float v;
+				if (tr == itr) v = minf;
+				else {
+					const float popu = (float)pc[s.from[tr] * ncol + col];
+					v = popu <= 0.f ? 0.f : dt * popu * s.rate[tr * DP + dp];
 				}
+				if (tb.tm_mult) v *= __ldg(tb.tm_mult + ((size_t)sett * A + c) * T * DP + tr * DP + dp);
+				return v;
+			};
+			if constexpr (kMvSmem) {
+				for (int tr = 0; tr < T; tr++) mvs[tr * NT] = mean_of(tr);
+			} else {
+#pragma unroll
+				for (int tr = 0; tr < MT; tr++) mv[tr] = tr < T ? mean_of(tr) : 0.f;
 			}
 			if (pn != pc)
 				for (int co = 0; co < C; co++) pn[co * ncol + col] = pc[co * ncol + col];
 			// draws; the populations are updated after every mean was formed
 			for (int tr = 0; tr < T; tr++) {
-				float mean = mv[0];
+				float mean;
+				if constexpr (kMvSmem) {
+					mean = mvs[tr * NT];
+				} else {
+					mean = mv[0];
 #pragma unroll
-				for (int k = 1; k < MT; k++) mean = tr == k ? mv[k] : mean;
+					for (int k = 1; k < MT; k++) mean = tr == k ? mv[k] : mean;
+				}
 				int32_t n = 0;
 				if constexpr (CH) {
 					const size_t tcell = (size_t)tr * ncol + col, step_cells = (size_t)T * ncol;
