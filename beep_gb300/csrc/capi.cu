@@ -721,7 +721,9 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 		}
 		q->bd.nslots = nslots;
 		// one 32-byte task per (step, active observation), in step_obs order:
-		// {slot, obs, first cell, ncell | last<<31}, {factor bits, spline, cell offset, 0}
+		// {slot, obs, first cell, ncell | last<<31}, {factor bits, spline, cell offset, run}
+		// run: 1 when the cells are consecutive counts, 2 consecutive populations (the
+		// kernels then read them without the cell list), 0 otherwise
 		q->tasks.resize((size_t)8 * q->step_obs.size());
 		for (int s2 = 0; s2 < nsteps; s2++)
 			for (int k = q->step_ptr[s2]; k < q->step_ptr[s2 + 1]; k++) {
@@ -735,7 +737,17 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 				const std::vector<int32_t> &enc = traj ? m->obs_cells_full_h : m->obs_cells_f_h;
 				t[0] = q->slot_of[pos]; t[1] = o; t[2] = nc > 0 ? enc[c0] : 0;
 				t[3] = (int32_t)((uint32_t)nc | (last ? 0x80000000u : 0u));
-				t[4] = fbits; t[5] = m->obs_spline[o]; t[6] = c0; t[7] = 0;
+				int32_t run = 0;
+				if (nc > 1) {
+					const int32_t e0 = enc[c0];
+					bool up = e0 >= 0, down = e0 < 0;
+					for (int i = 1; i < nc && (up || down); i++) {
+						up = up && enc[c0 + i] == e0 + i;
+						down = down && enc[c0 + i] == e0 - i;
+					}
+					run = up ? 1 : down ? 2 : 0;
+				}
+				t[4] = fbits; t[5] = m->obs_spline[o]; t[6] = c0; t[7] = run;
 			}
 		const size_t limit = 227 * 1024;
 		int nefoi = 1 << 30;

@@ -39,16 +39,18 @@ static_assert(kBxUnits * kBxThreads * 8 == kBxRows * kBxK && kBxThreads == 2 * k
 constexpr int kBxStepThreads = 256;   // threads of a step CTA
 constexpr int kBxChunk = 512;         // columns per work item of the step kernel (two passes)
 constexpr int kBxObsThreads = 128;    // threads of an observation CTA (one particle)
-constexpr int kMaxC = 8;              // compartments held in registers per column
+constexpr int kMaxC = 8;              // compartments of a model in this layout, at most
 
 __device__ __forceinline__ uint32_t idesc_m128(int n)
 {
 	return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kBxRows >> 4) << 24);
 }
 
+// One product CTA computes one 128-row tile against one target chunk (tw columns of
+// the matrix): the grid is tiles x target chunks.
 struct BxGeom {
 	int nct, tw, nkc;
-	uint32_t a_piece, b_bytes, stage;   // bytes: one A piece (128 x 32 BF16), the B chunks of all targets, a stage
+	uint32_t a_piece, b_bytes, stage;   // bytes: one A piece (128 x 32 BF16), one target chunk's B pieces, a stage
 };
 
 __host__ __device__ inline BxGeom bx_geometry(int A, int NS)
@@ -59,7 +61,7 @@ __host__ __device__ inline BxGeom bx_geometry(int A, int NS)
 	x.tw = g.tw;
 	x.nkc = g.nkc;
 	x.a_piece = (uint32_t)kBxRows * kBxK * 2;
-	x.b_bytes = (uint32_t)g.nct * g.chunk_bytes();
+	x.b_bytes = g.chunk_bytes();
 	x.stage = (2 * x.a_piece + x.b_bytes + 127) & ~127u;
 	return x;
 }
@@ -76,13 +78,14 @@ __global__ void __launch_bounds__(kBxThreads, 1) bx_foi(const ModelDev m, const 
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const int A = m.A, G = m.G;
 	const int rows = b.P * m.NS * G;
-	const int r0 = blockIdx.x * kBxRows;
 	const BxGeom x = bx_geometry(A, m.NS);
+	const int ct = blockIdx.x % x.nct;            // the target chunk
+	const int r0 = (blockIdx.x / x.nct) * kBxRows;
 	const tc::Geom g = tc::geometry(A, m.NS);
 	const float *Ic = b.bx_ic + (size_t)cur * rows * A;
 	unsigned char *stage0 = smem_raw;
 	uint32_t tcols = 32;
-	while (tcols < (uint32_t)(x.nct * x.tw)) tcols <<= 1;
+	while (tcols < (uint32_t)x.tw) tcols <<= 1;
 	if (warp == 0) tc::tmem_alloc(&tslot, tcols);
 	if (tid == 0) {
 		abort_flag = 0;
@@ -99,16 +102,13 @@ __global__ void __launch_bounds__(kBxThreads, 1) bx_foi(const ModelDev m, const 
 	tc::tc_after_sync();
 	const uint32_t taddr = tslot;
 	uint32_t pending = 0, pend_par = 0;           // thread 0: stages with a bulk load in flight, and its phase parity
-	// thread 0: the matrix chunks of source chunk kc (every target chunk) into stage s
+	// thread 0: the matrix chunk (target chunk ct, source chunk kc) into stage s
 	auto load_b = [&](int kc, int s) {
 		unsigned char *dst = stage0 + (size_t)s * x.stage + 2 * x.a_piece;
 		tc::mbar_expect_tx(&full[s], x.b_bytes);
-		for (int ct = 0; ct < x.nct; ct++) {
-			const unsigned char *src = m.tc_image + (size_t)(ct * x.nkc + kc) * g.chunk_bytes();
-			for (int pc = 0; pc < tc::kPieces; pc++)
-				tc::bulk_load(dst + (size_t)ct * g.chunk_bytes() + pc * g.piece_bytes(), src + pc * g.piece_bytes(),
-				              g.piece_bytes(), &full[s]);
-		}
+		const unsigned char *src = m.tc_image + (size_t)(ct * x.nkc + kc) * g.chunk_bytes();
+		for (int pc = 0; pc < tc::kPieces; pc++)
+			tc::bulk_load(dst + pc * g.piece_bytes(), src + pc * g.piece_bytes(), g.piece_bytes(), &full[s]);
 		pending |= 1u << s;
 		pend_par = (pend_par & ~(1u << s)) | ((uint32_t)((kc / kBxStages) & 1) << s);
 	};
@@ -161,18 +161,15 @@ __global__ void __launch_bounds__(kBxThreads, 1) bx_foi(const ModelDev m, const 
 				for (int ks = 0; ks < kBxK / 16; ks++) {
 					const uint64_t ah = tc::sdesc(sa + (uint32_t)(ks * 2) * albo, albo, 128);
 					const uint64_t al = tc::sdesc(sa + x.a_piece + (uint32_t)(ks * 2) * albo, albo, 128);
-					for (int ct = 0; ct < x.nct; ct++) {
-						const uint32_t bb = sa + 2 * x.a_piece + (uint32_t)ct * g.chunk_bytes() + (uint32_t)(ks * 2) * blbo;
-						const uint64_t bh = tc::sdesc(bb, blbo, 128);
-						const uint64_t bm = tc::sdesc(bb + g.piece_bytes(), blbo, 128);
-						const uint64_t bl = tc::sdesc(bb + 2 * g.piece_bytes(), blbo, 128);
-						const uint32_t d = taddr + (uint32_t)(ct * x.tw);
-						tc::mma_bf16(d, ah, bh, id, !(kc == 0 && ks == 0));
-						tc::mma_bf16(d, ah, bm, id, true);
-						tc::mma_bf16(d, ah, bl, id, true);
-						tc::mma_bf16(d, al, bh, id, true);
-						tc::mma_bf16(d, al, bm, id, true);
-					}
+					const uint32_t bb = sa + 2 * x.a_piece + (uint32_t)(ks * 2) * blbo;
+					const uint64_t bh = tc::sdesc(bb, blbo, 128);
+					const uint64_t bm = tc::sdesc(bb + g.piece_bytes(), blbo, 128);
+					const uint64_t bl = tc::sdesc(bb + 2 * g.piece_bytes(), blbo, 128);
+					tc::mma_bf16(taddr, ah, bh, id, !(kc == 0 && ks == 0));
+					tc::mma_bf16(taddr, ah, bm, id, true);
+					tc::mma_bf16(taddr, ah, bl, id, true);
+					tc::mma_bf16(taddr, al, bh, id, true);
+					tc::mma_bf16(taddr, al, bm, id, true);
 				}
 				tc::mma_commit(&empty[s]);
 			} else {
@@ -195,14 +192,14 @@ __global__ void __launch_bounds__(kBxThreads, 1) bx_foi(const ModelDev m, const 
 		const int r = r0 + q * 32 + lane;
 		const int gi = r / G, a = r - gi * G;
 		float *Y = b.bx_y + (size_t)gi * A * G + a;
-		const int ngrp = (x.nct * x.tw) / 16;
+		const int ngrp = x.tw / 16;
 		for (int gp = half; gp < ngrp; gp += kBxThreads / 128) {
 			float v[16];
 			tc::tmem_ld16(taddr + ((uint32_t)(q * 32) << 16) + (uint32_t)(gp * 16), v);
 			if (r < rows) {
 #pragma unroll
 				for (int i = 0; i < 16; i++) {
-					const int t = gp * 16 + i;
+					const int t = ct * x.tw + gp * 16 + i;
 					if (t < A) Y[(size_t)t * G] = v[i];
 				}
 			}
@@ -485,13 +482,19 @@ __global__ void __launch_bounds__(kBxObsThreads) bx_obs(const ModelDev m, const 
 		const float w = spl < 0 ? fac : fac * tb.obs_spline[(size_t)spl * m.S + sett];
 		const int nc = t0.w & 0x7fffffff;
 		float v = slot[t0.x];
-		if (nc > 0) {
-			const int cell = t0.z;
-			v = fmaf(w, cell >= 0 ? (float)tn[cell] : (float)pc[-1 - cell], v);
-		}
-		for (int i = 1; i < nc; i++) {
-			const int cell = __ldg((b.tn_full ? m.obs_cells_full : m.obs_cells_f) + t1.z + i);
-			v = fmaf(w, cell >= 0 ? (float)tn[cell] : (float)pc[-1 - cell], v);
+		if (t1.w != 0) {                  // consecutive counts or populations: no cell list
+			const int32_t *src = t1.w == 1 ? tn + t0.z : pc + (-1 - t0.z);
+#pragma unroll 4
+			for (int i = 0; i < nc; i++) v = fmaf(w, (float)src[i], v);
+		} else {
+			if (nc > 0) {
+				const int cell = t0.z;
+				v = fmaf(w, cell >= 0 ? (float)tn[cell] : (float)pc[-1 - cell], v);
+			}
+			for (int i = 1; i < nc; i++) {
+				const int cell = __ldg((b.tn_full ? m.obs_cells_full : m.obs_cells_f) + t1.z + i);
+				v = fmaf(w, cell >= 0 ? (float)tn[cell] : (float)pc[-1 - cell], v);
+			}
 		}
 		if (t0.w < 0) {                  // the observation's last step: log-density
 			const float lp = obs_lp_fast(v, t0.y, m);
@@ -555,7 +558,7 @@ int launch_steps(const ModelDev &m, const BatchDev &b, size_t smem_step, int sms
 	e = cudaFuncSetAttribute(bx_foi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_foi);
 	if (e != cudaSuccess) return (int)e;
 	const int rows = b.P * m.NS * m.G;
-	const int ntile = (rows + kBxRows - 1) / kBxRows;
+	const int ntile = (rows + kBxRows - 1) / kBxRows * x.nct;   // (row tile, target chunk) pairs
 	const int ncol = m.A * m.DP, nitem = b.P * ((ncol + kBxChunk - 1) / kBxChunk);
 	const int grid = std::min(nitem, sms * MB);
 	bx_init<<<b.P, 256, 0, st>>>(m, b);

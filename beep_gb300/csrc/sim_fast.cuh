@@ -845,13 +845,19 @@ __global__ void __launch_bounds__(NT, MB) sim_fast_kernel(const ModelDev m, cons
 			const float w = spl < 0 ? fac : fac * tb.obs_spline[(size_t)spl * m.S + sett];
 			const int nc = t0.w & 0x7fffffff;
 			float v = s.slot[t0.x];
-			if (nc > 0) {
-				const int cell = t0.z;
-				v = fmaf(w, cell >= 0 ? (float)s.tn[cell] : (float)pc[-1 - cell], v);
-			}
-			for (int i = 1; i < nc; i++) {
-				const int cell = __ldg((b.tn_full ? m.obs_cells_full : m.obs_cells_f) + t1.z + i);
-				v = fmaf(w, cell >= 0 ? (float)s.tn[cell] : (float)pc[-1 - cell], v);
+			if (t1.w != 0) {                  // consecutive counts or populations: no cell list
+				const int32_t *src = t1.w == 1 ? s.tn + t0.z : pc + (-1 - t0.z);
+#pragma unroll 4
+				for (int i = 0; i < nc; i++) v = fmaf(w, (float)src[i], v);
+			} else {
+				if (nc > 0) {
+					const int cell = t0.z;
+					v = fmaf(w, cell >= 0 ? (float)s.tn[cell] : (float)pc[-1 - cell], v);
+				}
+				for (int i = 1; i < nc; i++) {
+					const int cell = __ldg((b.tn_full ? m.obs_cells_full : m.obs_cells_f) + t1.z + i);
+					v = fmaf(w, cell >= 0 ? (float)s.tn[cell] : (float)pc[-1 - cell], v);
+				}
 			}
 			if (t0.w < 0) {                  // the observation's last step: log-density
 				const float lp = obs_lp_fast(v, t0.y, m);
