@@ -126,6 +126,8 @@ struct BatchDev {
 	float2 *bx_kahan;                   // [P][observation threads] compensated log-likelihood partial sums
 	int32_t *bx_tn;                     // [P][observed transitions][A*DP] counts of the step
 	int32_t *bx_work;                   // [tf-ti] particle counters of the step kernels
+	unsigned char *bx_a;                // the next product's A operand: per (128-row tile, 32-source chunk) the
+	                                    // infectious counts as split BF16 (hi, lo) in K-major core matrices
 	int32_t ctas;                       // fast form, nt == kDualThreads: CTAs resident per SM (2..4)
 };
 
@@ -164,6 +166,7 @@ size_t batched_step_smem(const ModelDev &m, int tnrows);
 int batched_obs_threads();
 int batched_prepare();                           // constant tables of sim_batched.cu
 int batched_launches(int nsteps);                // kernel launches of one batch run
+size_t batched_a_bytes(const ModelDev &m, int P);  // bytes of BatchDev::bx_a
 // events: null, or 2 * (tf - ti) cudaEvent_t recorded around each step's product kernel
 int launch_sim_batched(const ModelDev &m, const BatchDev &b, int sms, void *stream, void *events = nullptr);
 

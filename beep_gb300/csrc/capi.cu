@@ -872,7 +872,8 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 	             w_bxs = wk.add(bx ? 4 * (size_t)q->bd.nslots * P : 0),
 	             w_bxk = wk.add(bx ? 8 * (size_t)batched_obs_threads() * P : 0),
 	             w_bxt = wk.add(bx ? 4 * (size_t)(q->bd.tn_full ? m->T : m->dev.tn_rows) * m->A * m->DP * P : 0),
-	             w_bxw = wk.add(bx ? 4 * (size_t)nsteps : 0);
+	             w_bxw = wk.add(bx ? 4 * (size_t)nsteps : 0),
+	             w_bxa = wk.add(bx ? batched_a_bytes(m->dev, P) : 0);
 	size_t w_pa = wk.add(pe * popsz * PW), w_pb = wk.add(pe * popsz * PW), w_tn = wk.add(traj ? 0 : 4 * tnsz * PW),
 	       w_im = wk.add(8 * agsz * PW), w_id = wk.add(8 * agsz * PW), w_di = wk.add(8 * agsz * PW),
 	       w_nmi = wk.add(8 * agsz * PW), w_acc = wk.add(8 * (size_t)nscored * PW);
@@ -909,6 +910,7 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 		bd.bx_kahan = (float2 *)(dw + w_bxk);
 		bd.bx_tn = (int32_t *)(dw + w_bxt);
 		bd.bx_work = (int32_t *)(dw + w_bxw);
+		bd.bx_a = (unsigned char *)(dw + w_bxa);
 	}
 	bd.gstate_stride = q->state_global ? fast_gstate_stride(m->dev) : 0;
 	bd.status = (int32_t *)(dout + q->u_st);

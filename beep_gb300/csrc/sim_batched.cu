@@ -69,10 +69,10 @@ __host__ __device__ inline BxGeom bx_geometry(int A, int NS)
 // ---------------------------------------------------------------------------
 // the product Y = I . M for one tile of 128 rows
 
-__global__ void __launch_bounds__(kBxThreads, 1) bx_foi(const ModelDev m, const BatchDev b, int cur)
+__global__ void __launch_bounds__(kBxThreads, 1) bx_foi(const ModelDev m, const BatchDev b)
 {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
-	__shared__ uint64_t full[kBxStages], aready[kBxStages], empty[kBxStages], done;
+	__shared__ uint64_t full[kBxStages], empty[kBxStages], done;
 	__shared__ uint32_t tslot;
 	__shared__ int abort_flag;
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -82,7 +82,6 @@ __global__ void __launch_bounds__(kBxThreads, 1) bx_foi(const ModelDev m, const 
 	const int ct = blockIdx.x % x.nct;            // the target chunk
 	const int r0 = (blockIdx.x / x.nct) * kBxRows;
 	const tc::Geom g = tc::geometry(A, m.NS);
-	const float *Ic = b.bx_ic + (size_t)cur * rows * A;
 	unsigned char *stage0 = smem_raw;
 	uint32_t tcols = 32;
 	while (tcols < (uint32_t)x.tw) tcols <<= 1;
@@ -91,7 +90,6 @@ __global__ void __launch_bounds__(kBxThreads, 1) bx_foi(const ModelDev m, const 
 		abort_flag = 0;
 		for (int s = 0; s < kBxStages; s++) {
 			tc::mbar_init(&full[s], 1);
-			tc::mbar_init(&aready[s], kBxThreads);
 			tc::mbar_init(&empty[s], 1);
 		}
 		tc::mbar_init(&done, 1);
@@ -102,83 +100,55 @@ __global__ void __launch_bounds__(kBxThreads, 1) bx_foi(const ModelDev m, const 
 	tc::tc_after_sync();
 	const uint32_t taddr = tslot;
 	uint32_t pending = 0, pend_par = 0;           // thread 0: stages with a bulk load in flight, and its phase parity
-	// thread 0: the matrix chunk (target chunk ct, source chunk kc) into stage s
-	auto load_b = [&](int kc, int s) {
-		unsigned char *dst = stage0 + (size_t)s * x.stage + 2 * x.a_piece;
-		tc::mbar_expect_tx(&full[s], x.b_bytes);
+	const int tile = blockIdx.x / x.nct;
+	// thread 0: the A block (tile, source chunk kc) and the matrix chunk (ct, kc) into stage s
+	auto load = [&](int kc, int s) {
+		unsigned char *dst = stage0 + (size_t)s * x.stage;
+		tc::mbar_expect_tx(&full[s], 2 * x.a_piece + x.b_bytes);
+		tc::bulk_load(dst, b.bx_a + ((size_t)tile * x.nkc + kc) * 2 * x.a_piece, 2 * x.a_piece, &full[s]);
 		const unsigned char *src = m.tc_image + (size_t)(ct * x.nkc + kc) * g.chunk_bytes();
 		for (int pc = 0; pc < tc::kPieces; pc++)
-			tc::bulk_load(dst + pc * g.piece_bytes(), src + pc * g.piece_bytes(), g.piece_bytes(), &full[s]);
+			tc::bulk_load(dst + 2 * x.a_piece + pc * g.piece_bytes(), src + pc * g.piece_bytes(), g.piece_bytes(),
+			              &full[s]);
 		pending |= 1u << s;
 		pend_par = (pend_par & ~(1u << s)) | ((uint32_t)((kc / kBxStages) & 1) << s);
 	};
-	// this thread's row of the tile (the same for every chunk) and its counts' base
-	const int rr = tid & (kBxRows - 1);
-	const bool my_row = r0 + rr < rows;
-	const int my_gi = (r0 + rr) / G, my_a = (r0 + rr) - my_gi * G;
-	const float *my_src = Ic + ((size_t)my_gi * A) * G + my_a;
 	const uint32_t id = idesc_m128(x.tw);
 	const uint32_t albo = (uint32_t)kBxRows * 16, blbo = (uint32_t)x.tw * 16;
-	for (int kc = 0; kc < x.nkc; kc++) {
-		const int s = kc % kBxStages;
-		const uint32_t use = (uint32_t)(kc / kBxStages);
-		unsigned char *st = stage0 + (size_t)s * x.stage;
-		if (kc >= kBxStages && !tc::mbar_wait(&empty[s], (use - 1) & 1u)) atomicExch(&abort_flag, 1);
-		if (*(volatile int *)&abort_flag) break;
-		if (tid == 0) load_b(kc, s);
-		// counts of rows r0.. for sources kc*32.. as two BF16 pieces, K-major core-matrix layout:
-		// each thread takes one row and 8 consecutive sources per unit (one 16-byte row of a
-		// core matrix per piece), its loads all in flight before the conversion
-#pragma unroll
-		for (int u = 0; u < kBxUnits; u++) {
-			const int kg = (tid >> 7) + 2 * u;            // sources kg*8 .. kg*8+7 of the chunk
-			const int c0 = kc * kBxK + kg * 8;
-			float v[8];
-#pragma unroll
-			for (int i = 0; i < 8; i++) v[i] = (my_row && c0 + i < A) ? __ldg(my_src + (size_t)(c0 + i) * G) : 0.f;
-			uint32_t hw[4], lw[4];
-#pragma unroll
-			for (int i = 0; i < 4; i++) {
-				const __nv_bfloat16 h0 = __float2bfloat16_rn(v[2 * i]), h1 = __float2bfloat16_rn(v[2 * i + 1]);
-				const __nv_bfloat16 l0 = __float2bfloat16_rn(v[2 * i] - __bfloat162float(h0));
-				const __nv_bfloat16 l1 = __float2bfloat16_rn(v[2 * i + 1] - __bfloat162float(h1));
-				hw[i] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
-				lw[i] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
-			}
-			const uint32_t o = tc::kmajor_offset(rr, kg * 8, kBxRows);
-			*(uint4 *)(st + o) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-			*(uint4 *)(st + x.a_piece + o) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
-		}
-		tc::fence_async_smem();
-		asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(&aready[s])) : "memory");
-		if (tid == 0) {
-			bool ok = tc::mbar_wait(&aready[s], use & 1u) && tc::mbar_wait(&full[s], use & 1u);
-			if (ok) {
-				pending &= ~(1u << s);
-				tc::tc_after_sync();
-				const uint32_t sa = tc::smem_u32(st);
-#pragma unroll
-				for (int ks = 0; ks < kBxK / 16; ks++) {
-					const uint64_t ah = tc::sdesc(sa + (uint32_t)(ks * 2) * albo, albo, 128);
-					const uint64_t al = tc::sdesc(sa + x.a_piece + (uint32_t)(ks * 2) * albo, albo, 128);
-					const uint32_t bb = sa + 2 * x.a_piece + (uint32_t)(ks * 2) * blbo;
-					const uint64_t bh = tc::sdesc(bb, blbo, 128);
-					const uint64_t bm = tc::sdesc(bb + g.piece_bytes(), blbo, 128);
-					const uint64_t bl = tc::sdesc(bb + 2 * g.piece_bytes(), blbo, 128);
-					tc::mma_bf16(taddr, ah, bh, id, !(kc == 0 && ks == 0));
-					tc::mma_bf16(taddr, ah, bm, id, true);
-					tc::mma_bf16(taddr, ah, bl, id, true);
-					tc::mma_bf16(taddr, al, bh, id, true);
-					tc::mma_bf16(taddr, al, bm, id, true);
-				}
-				tc::mma_commit(&empty[s]);
-			} else {
-				atomicExch(&abort_flag, 1);
-			}
-		}
-	}
 	if (tid == 0) {
-		if (!*(volatile int *)&abort_flag) tc::mma_commit(&done);
+		// every stage filled up front; a stage is refilled once its products are done
+		bool ok = true;
+		for (int kc = 0; kc < x.nkc && kc < kBxStages; kc++) load(kc, kc);
+		for (int kc = 0; kc < x.nkc && ok; kc++) {
+			const int s = kc % kBxStages;
+			const uint32_t use = (uint32_t)(kc / kBxStages);
+			ok = tc::mbar_wait(&full[s], use & 1u);
+			if (!ok) break;
+			pending &= ~(1u << s);
+			tc::tc_after_sync();
+			const uint32_t sa = tc::smem_u32(stage0 + (size_t)s * x.stage);
+#pragma unroll
+			for (int ks = 0; ks < kBxK / 16; ks++) {
+				const uint64_t ah = tc::sdesc(sa + (uint32_t)(ks * 2) * albo, albo, 128);
+				const uint64_t al = tc::sdesc(sa + x.a_piece + (uint32_t)(ks * 2) * albo, albo, 128);
+				const uint32_t bb = sa + 2 * x.a_piece + (uint32_t)(ks * 2) * blbo;
+				const uint64_t bh = tc::sdesc(bb, blbo, 128);
+				const uint64_t bm = tc::sdesc(bb + g.piece_bytes(), blbo, 128);
+				const uint64_t bl = tc::sdesc(bb + 2 * g.piece_bytes(), blbo, 128);
+				tc::mma_bf16(taddr, ah, bh, id, !(kc == 0 && ks == 0));
+				tc::mma_bf16(taddr, ah, bm, id, true);
+				tc::mma_bf16(taddr, ah, bl, id, true);
+				tc::mma_bf16(taddr, al, bh, id, true);
+				tc::mma_bf16(taddr, al, bm, id, true);
+			}
+			tc::mma_commit(&empty[s]);
+			if (kc + kBxStages < x.nkc) {
+				ok = tc::mbar_wait(&empty[s], use & 1u);
+				if (ok) load(kc + kBxStages, s);
+			}
+		}
+		if (ok) tc::mma_commit(&done);
+		else abort_flag = 1;
 		// loads still in flight (only after a timeout) land before the CTA exits
 		for (int s = 0; s < kBxStages; s++)
 			if (pending & (1u << s)) tc::mbar_wait(&full[s], (pend_par >> s) & 1u);
@@ -240,6 +210,45 @@ __device__ __forceinline__ int32_t *bx_pop(const ModelDev &m, const BatchDev &b,
 	return b.bx_pop + ((size_t)(b.pop_single ? 0 : k) * b.P + p) * popsz;
 }
 
+// The product's A operand for particle p: its rows (p, strain, age) of the infectious
+// counts Ic [NS][A][G], split into BF16 hi and lo = bf16(v - hi), written as the
+// 16-byte rows (8 consecutive sources) of the K-major core matrices of each
+// (128-row tile, 32-source chunk) block [hi piece][lo piece], so that the product
+// kernel bulk-loads a block per stage.  Slots of rows or sources beyond the batch
+// stay zero (the buffer is cleared before a run).
+__device__ void bx_pack_a(const ModelDev &m, const BatchDev &b, int p, const float *Ic, int tid, int nt)
+{
+	const int A = m.A, G = m.G, NS = m.NS;
+	const BxGeom x = bx_geometry(A, NS);
+	const int units = (A + 7) / 8, nrl = NS * G;
+	// adjacent threads take adjacent rows of one source unit: their loads are the
+	// contiguous ages of a source, their stores consecutive rows of a core matrix
+	for (int idx = tid; idx < nrl * units; idx += nt) {
+		const int u = idx / nrl, rl = idx - u * nrl;       // source unit, row (strain, age) of the particle
+		const int st = rl / G, a = rl - st * G;
+		const int row = p * NS * G + rl;
+		const int tile = row / kBxRows, rr = row - tile * kBxRows;
+		const int c0 = u * 8, kc = c0 / kBxK, kl = c0 - kc * kBxK;
+		const float *src = Ic + ((size_t)st * A) * G + a;
+		float v[8];
+#pragma unroll
+		for (int i = 0; i < 8; i++) v[i] = c0 + i < A ? src[(size_t)(c0 + i) * G] : 0.f;
+		uint32_t hw[4], lw[4];
+#pragma unroll
+		for (int i = 0; i < 4; i++) {
+			const __nv_bfloat16 h0 = __float2bfloat16_rn(v[2 * i]), h1 = __float2bfloat16_rn(v[2 * i + 1]);
+			const __nv_bfloat16 l0 = __float2bfloat16_rn(v[2 * i] - __bfloat162float(h0));
+			const __nv_bfloat16 l1 = __float2bfloat16_rn(v[2 * i + 1] - __bfloat162float(h1));
+			hw[i] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+			lw[i] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+		}
+		unsigned char *blk = b.bx_a + ((size_t)tile * x.nkc + kc) * 2 * x.a_piece;
+		const uint32_t o = tc::kmajor_offset(rr, kl, kBxRows);
+		*(uint4 *)(blk + o) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+		*(uint4 *)(blk + x.a_piece + o) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+	}
+}
+
 // strain shift of the susceptible population before a step (src/state.cc:392-401): the
 // susceptibles of strains 1.. join strain 0's, whose pool every strain's infection draws on
 __device__ __forceinline__ void strain_shift(const ModelDev &m, int32_t *pop, int tid, int nt)
@@ -285,6 +294,8 @@ __global__ void __launch_bounds__(256) bx_init(const ModelDev m, const BatchDev 
 		Ic[idx] = v;
 		if (!m.dp_age_unique) Ic[(size_t)b.P * NS * A * G + idx] = 0.f;   // the first step's accumulation target
 	}
+	__syncthreads();
+	bx_pack_a(m, b, p, Ic, tid, blockDim.x);                 // the first product's operand
 	for (int k = tid; k < b.nslots; k += blockDim.x) b.bx_slot[(size_t)p * b.nslots + k] = 0.f;
 	for (int k = tid; k < kBxObsThreads; k += blockDim.x) b.bx_kahan[(size_t)p * kBxObsThreads + k] = make_float2(0.f, 0.f);
 	if (p == 0)
@@ -508,6 +519,9 @@ __global__ void __launch_bounds__(kBxObsThreads) bx_obs(const ModelDev m, const 
 	}
 	if (Lsum != kah.x || Lcmp != kah.y) b.bx_kahan[(size_t)p * kBxObsThreads + tid] = make_float2(Lsum, Lcmp);
 	if (sett + 1 < b.tf) {
+		// the next product's operand from the counts the step kernel left for the next step
+		bx_pack_a(m, b, p, b.bx_ic + (size_t)(cur ^ 1) * b.P * NS * A * G + (size_t)p * NS * A * G, tid,
+		          kBxObsThreads);
 		if (NS > 1) strain_shift(m, bx_pop(m, b, p, cur ^ 1), tid, kBxObsThreads);
 		if (!m.dp_age_unique) {
 			float *Ic = b.bx_ic + (size_t)cur * b.P * NS * A * G + (size_t)p * NS * A * G;
@@ -561,10 +575,12 @@ int launch_steps(const ModelDev &m, const BatchDev &b, size_t smem_step, int sms
 	const int ntile = (rows + kBxRows - 1) / kBxRows * x.nct;   // (row tile, target chunk) pairs
 	const int ncol = m.A * m.DP, nitem = b.P * ((ncol + kBxChunk - 1) / kBxChunk);
 	const int grid = std::min(nitem, sms * MB);
+	e = cudaMemsetAsync(b.bx_a, 0, batched_a_bytes(m, b.P), st);   // padding rows and sources stay zero
+	if (e != cudaSuccess) return (int)e;
 	bx_init<<<b.P, 256, 0, st>>>(m, b);
 	for (int s = b.ti; s < b.tf; s++) {
 		if (ev) cudaEventRecord(ev[2 * (s - b.ti)], st);
-		bx_foi<<<ntile, kBxThreads, smem_foi, st>>>(m, b, (s - b.ti) & 1);
+		bx_foi<<<ntile, kBxThreads, smem_foi, st>>>(m, b);
 		if (ev) cudaEventRecord(ev[2 * (s - b.ti) + 1], st);
 		kstep<<<grid, kBxStepThreads, smem_step, st>>>(m, b, s);
 		bx_obs<<<b.P, kBxObsThreads, 0, st>>>(m, b, s);
@@ -594,6 +610,13 @@ int batched_obs_threads() { return kBxObsThreads; }
 int batched_prepare() { return prepare_constants(); }
 
 int batched_launches(int nsteps) { return 3 * nsteps + 2; }
+
+size_t batched_a_bytes(const ModelDev &m, int P)
+{
+	const BxGeom x = bx_geometry(m.A, m.NS);
+	const size_t tiles = ((size_t)P * m.NS * m.G + kBxRows - 1) / kBxRows;
+	return tiles * (size_t)x.nkc * 2 * x.a_piece;
+}
 
 int launch_sim_batched(const ModelDev &m, const BatchDev &b, int sms, void *stream, void *events)
 {
