@@ -65,16 +65,17 @@ def model_arrays(w: synth.Workload, obs_values: Optional[dict] = None) -> Dict[s
     to: List[int] = []
     val: List[float] = []
     geo = np.asarray(w.geo, np.float64) if A > 1 else np.ones((1, 1))
+    tp = total_pop.astype(np.float64)
     for c in range(A):
         d = float(geo[c, c])
-        tos = [i for i in range(A) if i != c and geo[c, i] != 0]
-        vs = [float(geo[c, i]) for i in tos]
-        s = d * float(total_pop[c])
-        for i, v in zip(tos, vs):
-            s += v * float(total_pop[i])
+        row = geo[c]
+        tos = np.flatnonzero((row != 0) & (np.arange(A) != c))
+        vs = row[tos]
+        # d*pop_c + sum_i v_i*pop_i, added left to right (cumsum is sequential)
+        s = float(np.cumsum(np.concatenate(([d * tp[c]], vs * tp[tos])))[-1])
         diag[c] = d / s
-        to += tos
-        val += [v / s for v in vs]
+        to += tos.tolist()
+        val += (vs / s).tolist()
         rowptr.append(len(to))
     factor = np.array([(1.0 / float(total_pop[c])) / diag[c] for c in range(A)])
 
@@ -176,11 +177,14 @@ def _observations(w: synth.Workload, obs_values: Optional[dict]) -> Dict[str, np
     G, T, C = w.nage, len(TRANS), len(COMPS)
     DP = G * nstrain(w)
     spd = w.steps_per_day
-    si, sf, vals, sds, kinds, models, thr, cptr, cells = [], [], [], [], [], [], [], [0], []
+    # per data column (all its rows at once): windows, cells, values, kinds, SDs
+    si, sf, vals, sds, kinds, models, thr, cells = [], [], [], [], [], [], [], []
+    ncell = []                                      # cells of each observation
     tr_of = {"E->I": 1, "H->D": 4}
     for tab in synth.data_tables(w):
         tt = tab["toml"]
-        nrow = len(tab["times"])
+        times = np.asarray(tab["times"], np.int64)
+        nrow = len(times)
         model, fixed_sd, percent = _obsmodel(tt["obsmodel"])
         threshold = float(tt["threshold"]) if "threshold" in tt else UNSET
         for ci, col in enumerate(tab["columns"]):
@@ -190,47 +194,54 @@ def _observations(w: synth.Workload, obs_values: Optional[dict]) -> Dict[str, np
                 dps = [dp for dp in range(DP) if dp % G == age]
             else:
                 dps = list(range(DP))
+            if tt["type"] == "transition":
+                step = int(tt["timestep"])
+                si.append(times * spd)
+                sf.append((times + step) * spd)
+                tr = tr_of[tt["observation"]]
+                row_cells = [(c * T + tr) * DP + dp for dp in dps]
+            else:
+                si.append(times * spd)
+                sf.append(times * spd + 1)
+                co = COMPS.index(tt["observation"])
+                row_cells = [-1 - ((c * C + co) * DP + dp) for dp in dps]
+            cells.append(np.tile(np.asarray(row_cells, np.int64), nrow))
+            ncell.append(np.full(nrow, len(dps), np.int64))
             ov = obs_values.get(tab["file"], {}).get(col) if obs_values else None
-            col_vals, col_kinds, col_sds = [], [], []
-            for r, t in enumerate(tab["times"]):
-                if tt["type"] == "transition":
-                    step = int(tt["timestep"])
-                    si.append(t * spd)
-                    sf.append((t + step) * spd)
-                    tr = tr_of[tt["observation"]]
-                    cells += [(c * T + tr) * DP + dp for dp in dps]
-                else:
-                    si.append(t * spd)
-                    sf.append(t * spd + 1)
-                    co = COMPS.index(tt["observation"])
-                    cells += [-1 - ((c * C + co) * DP + dp) for dp in dps]
-                cptr.append(len(cells))
-                kind, v, sd = OBSVAL_VALUE, 1.0 if not tab.get("sd_col", True) else 0.0, 1.0
-                if ov is not None:
-                    nd = tab.get("nodata_every")
-                    v, sd = float(ov[0][r]), (float(ov[1][r]) if ov[1] is not None else 1.0)
-                    if nd and (r + ci) % nd == 0:
-                        kind, v = OBSVAL_UNKNOWN, UNKNOWN
-                    elif tab.get("censor_below") is not None and v < tab["censor_below"]:
-                        kind, v = OBSVAL_THRESH, THRESH
-                    v = v if kind != OBSVAL_VALUE else float(int(v))
-                col_vals.append(v)
-                col_kinds.append(kind)
-                col_sds.append(sd)
+            kind = np.full(nrow, OBSVAL_VALUE, np.int64)
+            if ov is None:
+                v = np.full(nrow, 1.0 if not tab.get("sd_col", True) else 0.0)
+                sd = np.ones(nrow)
+            else:
+                v = np.asarray(ov[0], np.float64)[:nrow].copy()
+                sd = np.asarray(ov[1], np.float64)[:nrow].copy() if ov[1] is not None else np.ones(nrow)
+                r = np.arange(nrow)
+                nd = tab.get("nodata_every")
+                unknown = (r + ci) % nd == 0 if nd else np.zeros(nrow, bool)
+                cens = (~unknown & (v < tab["censor_below"]) if tab.get("censor_below") is not None
+                        else np.zeros(nrow, bool))
+                kind[unknown], kind[cens] = OBSVAL_UNKNOWN, OBSVAL_THRESH
+                v = np.where(unknown, UNKNOWN, np.where(cens, THRESH, np.trunc(v)))
             # standard deviations by observation model
-            vmax = max([v for v, k in zip(col_vals, col_kinds) if k == OBSVAL_VALUE], default=0.0)
-            for v, k, sd in zip(col_vals, col_kinds, col_sds):
-                if model == OBS_POISSON:
-                    sd = UNSET
-                elif percent is not None:
-                    sd = (v * (1 - EPSILON_FACTOR) + vmax * EPSILON_FACTOR) * 0.01 * percent
-                elif fixed_sd is not None:
-                    sd = fixed_sd
-                vals.append(v)
-                kinds.append(k)
-                sds.append(sd)
-                models.append(model)
-                thr.append(threshold)
+            valued = v[kind == OBSVAL_VALUE]
+            vmax = float(valued.max()) if valued.size else 0.0
+            if model == OBS_POISSON:
+                sd = np.full(nrow, UNSET)
+            elif percent is not None:
+                sd = (v * (1 - EPSILON_FACTOR) + vmax * EPSILON_FACTOR) * 0.01 * percent
+            elif fixed_sd is not None:
+                sd = np.full(nrow, fixed_sd)
+            vals.append(v)
+            kinds.append(kind)
+            sds.append(sd)
+            models.append(np.full(nrow, model, np.int64))
+            thr.append(np.full(nrow, threshold))
+    cat = lambda xs, dt: np.concatenate(xs).astype(dt) if xs else np.zeros(0, dt)
+    si, sf, vals, sds, kinds, models, thr = (cat(si, np.int32), cat(sf, np.int32), cat(vals, np.float64),
+                                              cat(sds, np.float64), cat(kinds, np.int32), cat(models, np.int32),
+                                              cat(thr, np.float64))
+    cptr = np.concatenate([[0], np.cumsum(cat(ncell, np.int64))]).astype(np.int32)
+    cells = cat(cells, np.int32)
     n = len(si)
     return {
         "obs_sett_i": np.array(si, np.int32), "obs_sett_f": np.array(sf, np.int32),

@@ -846,11 +846,12 @@ def main():
                     help="sweeps of the MBP-chain workload (4 x 128 chains of uneven size) after the main measurement")
     ap.add_argument("--pf-estimates", type=int, default=10,
                     help="particle-filter likelihood estimates (256 particles, 10 x 3 model) per form after the main measurement")
-    ap.add_argument("--serve-requests", type=int, default=128,
+    ap.add_argument("--serve-requests", type=int, default=512,
                     help="requests of the serving stream (Poisson arrivals at 200/s) after the main measurement")
-    ap.add_argument("--serve-sustained", type=int, default=16,
+    ap.add_argument("--serve-sustained", type=int, default=64,
                     help="requests of the same stream at a rate the GPU sustains (latency without queueing)")
-    ap.add_argument("--sustained-rate", type=float, default=1.0)
+    ap.add_argument("--sustained-rate", type=float, default=4.0,
+                    help="arrivals per second of that phase (about 2/3 of the rate the server completes)")
     ap.add_argument("--precision-particles", type=int, default=1024,
                     help="particles of the 350x10 precision batch run after the main measurement (0: skip)")
     ap.add_argument("--precision-plain-particles", type=int, default=152)
