@@ -37,7 +37,6 @@ constexpr int kBxStages = 2;
 constexpr int kBxUnits = kBxRows * kBxK / 8 / kBxThreads;   // 16-byte units of a chunk's A pieces per thread
 static_assert(kBxUnits * kBxThreads * 8 == kBxRows * kBxK && kBxThreads == 2 * kBxRows, "A-operand staging split");
 constexpr int kBxStepThreads = 256;   // threads of a step CTA
-constexpr int kBxChunk = 512;         // columns per work item of the step kernel (two passes)
 constexpr int kBxObsThreads = 128;    // threads of an observation CTA (one particle)
 constexpr int kMaxC = 8;              // compartments of a model in this layout, at most
 
@@ -307,7 +306,7 @@ __global__ void __launch_bounds__(256) bx_init(const ModelDev m, const BatchDev 
 // and the population update, then the column's infectious count for the next step;
 // the counts of observed transitions go to the step's count buffer.
 template <int MG, int MB>
-__global__ void __launch_bounds__(kBxStepThreads, MB) bx_step(const ModelDev m, const BatchDev b, int sett)
+__global__ void __launch_bounds__(kBxStepThreads, MB) bx_step(const ModelDev m, const BatchDev b, int sett, int chunk)
 {
 	constexpr int NT = kBxStepThreads;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -319,7 +318,7 @@ __global__ void __launch_bounds__(kBxStepThreads, MB) bx_step(const ModelDev m, 
 	const int nsteps = b.tf - b.ti, s_rel = sett - b.ti;
 	const int cur = s_rel & 1;
 	const int rows_ic = b.P * NS * A * G;
-	const int nchunk = (ncol + kBxChunk - 1) / kBxChunk, nitem = b.P * nchunk;
+	const int nchunk = (ncol + chunk - 1) / chunk, nitem = b.P * nchunk;
 	// shared memory: the step's table slices of the current parameter set, its rates and
 	// the model's small tables
 	size_t off = 0;
@@ -394,9 +393,9 @@ __global__ void __launch_bounds__(kBxStepThreads, MB) bx_step(const ModelDev m, 
 		float *Icp = Icn_all + (size_t)p * NS * A * G;
 		int32_t *tn = b.bx_tn + (size_t)p * tnrows * ncol;
 		const float d = dgeo[0], omd = 1.f - d;
-		const int col1 = min(ncol, (k + 1) * kBxChunk);
+		const int col1 = min(ncol, (k + 1) * chunk);
 		// ---- per column (c, dp): NMI, means, draws, population update, next infectious count
-		for (int col = k * kBxChunk + tid; col < col1; col += NT) {
+		for (int col = k * chunk + tid; col < col1; col += NT) {
 			const int c = col / DP, dp = col - c * DP;
 			const int st = dp / DPS, dpl = dp - st * DPS, a = age[dpl];
 			for (int co = 0; co < C; co++) cpv[co * NT] = pc[co * ncol + col];
@@ -486,36 +485,57 @@ __global__ void __launch_bounds__(kBxObsThreads) bx_obs(const ModelDev m, const 
 	float2 kah = b.bx_kahan[(size_t)p * kBxObsThreads + tid];
 	float Lsum = kah.x, Lcmp = kah.y;
 	const int a0 = b.step_ptr[s_rel], a1 = b.step_ptr[s_rel + 1];
-	for (int k = a0 + tid; k < a1; k += kBxObsThreads) {
-		const int4 t0 = __ldg(b.tasks + 2 * k), t1 = __ldg(b.tasks + 2 * k + 1);
-		const float fac = __int_as_float(t1.x);
-		const int spl = t1.y;
+	// one task ahead: the next task's record, slot and first cell are loaded before the
+	// current one is summed (the observations active at a step have distinct slots); each
+	// task's sum and the thread's log-density sum keep their order
+	auto first_of = [&](const int4 &q0) {
+		const int cell = q0.z;
+		return (q0.w & 0x7fffffff) > 0 ? (cell >= 0 ? (float)tn[cell] : (float)pc[-1 - cell]) : 0.f;
+	};
+	int k = a0 + tid;
+	int4 n0 = make_int4(0, 0, 0, 0), n1 = make_int4(0, 0, 0, 0);
+	float nv = 0.f, nf = 0.f;
+	if (k < a1) {
+		n0 = __ldg(b.tasks + 2 * k);
+		n1 = __ldg(b.tasks + 2 * k + 1);
+		nv = slot[n0.x];
+		nf = first_of(n0);
+	}
+	for (; k < a1; k += kBxObsThreads) {
+		const int4 q0 = n0, q1 = n1;
+		float x = nv;
+		const float f = nf;
+		const int kn = k + kBxObsThreads;
+		if (kn < a1) {
+			n0 = __ldg(b.tasks + 2 * kn);
+			n1 = __ldg(b.tasks + 2 * kn + 1);
+			nv = slot[n0.x];
+			nf = first_of(n0);
+		}
+		const float fac = __int_as_float(q1.x);
+		const int spl = q1.y;
 		const float w = spl < 0 ? fac : fac * tb.obs_spline[(size_t)spl * m.S + sett];
-		const int nc = t0.w & 0x7fffffff;
-		float v = slot[t0.x];
-		if (t1.w != 0) {                  // consecutive counts or populations: no cell list
-			const int32_t *src = t1.w == 1 ? tn + t0.z : pc + (-1 - t0.z);
+		const int nc = q0.w & 0x7fffffff;
+		if (nc > 0) x = fmaf(w, f, x);
+		if (q1.w != 0) {                  // consecutive counts or populations: no cell list
+			const int32_t *src = q1.w == 1 ? tn + q0.z : pc + (-1 - q0.z);
 #pragma unroll 4
-			for (int i = 0; i < nc; i++) v = fmaf(w, (float)src[i], v);
+			for (int i = 1; i < nc; i++) x = fmaf(w, (float)src[i], x);
 		} else {
-			if (nc > 0) {
-				const int cell = t0.z;
-				v = fmaf(w, cell >= 0 ? (float)tn[cell] : (float)pc[-1 - cell], v);
-			}
 			for (int i = 1; i < nc; i++) {
-				const int cell = __ldg((b.tn_full ? m.obs_cells_full : m.obs_cells_f) + t1.z + i);
-				v = fmaf(w, cell >= 0 ? (float)tn[cell] : (float)pc[-1 - cell], v);
+				const int cell = __ldg((b.tn_full ? m.obs_cells_full : m.obs_cells_f) + q1.z + i);
+				x = fmaf(w, cell >= 0 ? (float)tn[cell] : (float)pc[-1 - cell], x);
 			}
 		}
-		if (t0.w < 0) {                  // the observation's last step: log-density
-			const float lp = obs_lp_fast(v, t0.y, m);
-			v = 0.f;
+		if (q0.w < 0) {                  // the observation's last step: log-density
+			const float lp = obs_lp_fast(x, q0.y, m);
+			x = 0.f;
 			const float y = lp - Lcmp;      // Kahan
 			const float tt = Lsum + y;
 			Lcmp = (tt - Lsum) - y;
 			Lsum = tt;
 		}
-		slot[t0.x] = v;
+		slot[q0.x] = x;
 	}
 	if (Lsum != kah.x || Lcmp != kah.y) b.bx_kahan[(size_t)p * kBxObsThreads + tid] = make_float2(Lsum, Lcmp);
 	if (sett + 1 < b.tf) {
@@ -573,8 +593,18 @@ int launch_steps(const ModelDev &m, const BatchDev &b, size_t smem_step, int sms
 	if (e != cudaSuccess) return (int)e;
 	const int rows = b.P * m.NS * m.G;
 	const int ntile = (rows + kBxRows - 1) / kBxRows * x.nct;   // (row tile, target chunk) pairs
-	const int ncol = m.A * m.DP, nitem = b.P * ((ncol + kBxChunk - 1) / kBxChunk);
-	const int grid = std::min(nitem, sms * MB);
+	// columns per work item: a multiple of the CTA's threads (a particle's columns then take
+	// the same passes whatever the multiple), as large as leaves six items per CTA of the
+	// grid -- each item costs two barriers, a counter and (parameter set per particle) the
+	// reload of the step's table slices
+	const int ncol = m.A * m.DP, grid0 = sms * MB;
+	int chunk = kBxStepThreads;
+	for (int c2 = 2 * kBxStepThreads; c2 < ncol + kBxStepThreads; c2 += kBxStepThreads) {
+		if ((long long)b.P * ((ncol + c2 - 1) / c2) < 6LL * grid0) break;
+		chunk = c2;
+	}
+	const int nitem = b.P * ((ncol + chunk - 1) / chunk);
+	const int grid = std::min(nitem, grid0);
 	e = cudaMemsetAsync(b.bx_a, 0, batched_a_bytes(m, b.P), st);   // padding rows and sources stay zero
 	if (e != cudaSuccess) return (int)e;
 	bx_init<<<b.P, 256, 0, st>>>(m, b);
@@ -582,7 +612,7 @@ int launch_steps(const ModelDev &m, const BatchDev &b, size_t smem_step, int sms
 		if (ev) cudaEventRecord(ev[2 * (s - b.ti)], st);
 		bx_foi<<<ntile, kBxThreads, smem_foi, st>>>(m, b);
 		if (ev) cudaEventRecord(ev[2 * (s - b.ti) + 1], st);
-		kstep<<<grid, kBxStepThreads, smem_step, st>>>(m, b, s);
+		kstep<<<grid, kBxStepThreads, smem_step, st>>>(m, b, s, chunk);
 		bx_obs<<<b.P, kBxObsThreads, 0, st>>>(m, b, s);
 	}
 	bx_final<<<b.P, 256, 0, st>>>(m, b);
