@@ -327,6 +327,8 @@ def lib():
         L.beep_batch_time.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]
         L.beep_batch_time_split.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.beep_batch_time_split.restype = C.c_int32
+        L.beep_batch_time_kernels.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double), _f64p]
+        L.beep_batch_time_kernels.restype = C.c_int32
         L.beep_batch_run_graph.argtypes = [C.c_void_p]
         L.beep_batch_run_graph.restype = C.c_int32
         L.beep_autotune.argtypes = [C.c_void_p, C.POINTER(SimBatch), C.POINTER(C.c_int32)]
@@ -542,6 +544,13 @@ class DeviceBatch:
         ms, prod = C.c_double(), C.c_double()
         check(lib().beep_batch_time_split(self.h, iters, C.byref(ms), C.byref(prod)))
         return ms.value, prod.value
+
+    def time_kernels(self, iters: int):
+        """(ms per launch, [ms in the products, the step kernels, the observation kernels]) --
+        step-synchronous layout (zeros otherwise)."""
+        ms, k3 = C.c_double(), np.zeros(3)
+        check(lib().beep_batch_time_kernels(self.h, iters, C.byref(ms), k3.ctypes.data_as(_f64p)))
+        return ms.value, k3
 
     def bytes(self):
         a, b = C.c_int64(), C.c_int64()

@@ -167,7 +167,8 @@ int batched_obs_threads();
 int batched_prepare();                           // constant tables of sim_batched.cu
 int batched_launches(int nsteps);                // kernel launches of one batch run
 size_t batched_a_bytes(const ModelDev &m, int P);  // bytes of BatchDev::bx_a
-// events: null, or 2 * (tf - ti) cudaEvent_t recorded around each step's product kernel
+// events: null, or 4 * (tf - ti) cudaEvent_t: per step before the product kernel, between it and
+// the step kernel, between that and the observation kernel, and after it
 int launch_sim_batched(const ModelDev &m, const BatchDev &b, int sms, void *stream, void *events = nullptr);
 
 }  // namespace beep

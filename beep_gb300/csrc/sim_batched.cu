@@ -609,11 +609,14 @@ int launch_steps(const ModelDev &m, const BatchDev &b, size_t smem_step, int sms
 	if (e != cudaSuccess) return (int)e;
 	bx_init<<<b.P, 256, 0, st>>>(m, b);
 	for (int s = b.ti; s < b.tf; s++) {
-		if (ev) cudaEventRecord(ev[2 * (s - b.ti)], st);
+		cudaEvent_t *e4 = ev ? ev + 4 * (s - b.ti) : nullptr;   // before and after each of the step's kernels
+		if (e4) cudaEventRecord(e4[0], st);
 		bx_foi<<<ntile, kBxThreads, smem_foi, st>>>(m, b);
-		if (ev) cudaEventRecord(ev[2 * (s - b.ti) + 1], st);
+		if (e4) cudaEventRecord(e4[1], st);
 		kstep<<<grid, kBxStepThreads, smem_step, st>>>(m, b, s, chunk);
+		if (e4) cudaEventRecord(e4[2], st);
 		bx_obs<<<b.P, kBxObsThreads, 0, st>>>(m, b, s);
+		if (e4) cudaEventRecord(e4[3], st);
 	}
 	bx_final<<<b.P, 256, 0, st>>>(m, b);
 	return (int)cudaGetLastError();

@@ -260,16 +260,31 @@ def run_serving(nreq: int, rate: float, seed: int, budget_bytes: int, inflight: 
     }
 
 
-def profile_traffic(kind: str, P: int):
-    """DRAM bytes per launch of the fast kernel, from the committed ncu
-    summary of the workload (captured on a smaller particle count and scaled
-    by the particles, the part of the traffic that grows with them)."""
+def profile_file(kind: str, batched: bool) -> str:
+    """The committed ncu summary of the workload's dominant kernel: the
+    particle-resident fast kernel (one launch = the whole horizon), or the
+    step kernel of the step-synchronous layout (one launch = one step)."""
+    if batched:
+        return os.path.join(ROOT, "profiles", "bx_step_abc_smc.md" if kind == "abc_smc" else "bx_step_precision.md")
+    return os.path.join(ROOT, "profiles", "sim_fast_abc_smc.md" if kind == "abc_smc" else "sim_fast_precision.md")
+
+
+def profile_figure(kind: str, batched: bool, key: str):
+    """A per-particle figure of that summary (per particle and launch), or None."""
     import re
-    f = os.path.join(ROOT, "profiles", "sim_fast_abc_smc.md" if kind == "abc_smc" else "sim_fast_precision.md")
+    f = profile_file(kind, batched)
     if not os.path.exists(f):
         return None
-    m = re.search(r"dram_bytes_per_particle:\s*([0-9.]+)", open(f).read())
-    return float(m.group(1)) * P if m else None
+    m = re.search(key + r":\s*([0-9.eE+]+)", open(f).read())
+    return float(m.group(1)) if m else None
+
+
+def profile_traffic(kind: str, P: int, batched: bool = False):
+    """DRAM bytes per launch of the dominant kernel, from the committed ncu
+    summary of the workload (captured on a smaller particle count and scaled
+    by the particles, the part of the traffic that grows with them)."""
+    v = profile_figure(kind, batched, "dram_bytes_per_particle")
+    return v * P if v is not None else None
 
 
 def fp64_loglik_of_trajectory(m, transnum):
@@ -476,7 +491,9 @@ def run_precision(seed: int, P: int = 1024, steps: int = 3, warmup: int = 1, pla
     db = capi.DeviceBatch(dm, capi.Batch(m, tabs, P, seed, group_of=group_of, form=capi.FORM_FAST))
     db.upload()
     db.time(warmup)
-    ms, ms_prod = db.time_split(steps)
+    ms = db.time(steps)
+    _, k3 = db.time_kernels(1)         # the three kernels' shares, from a separate run with events
+    ms_prod = k3[0]
     units = P * m.narea * m.nage * m.ndivision
     out = {"workload": WORKLOADS["precision"]["name"], "particles": P, "areas": m.narea, "ages": m.nage,
            "steps": m.ndivision, "observations": m.nobs,
@@ -494,6 +511,10 @@ def run_precision(seed: int, P: int = 1024, steps: int = 3, warmup: int = 1, pla
                                             "note": "useful flops of the contraction over the product kernels' "
                                                     "time; the kernels issue five split-BF16 products on padded "
                                                     "tiles"}}
+    if db.foi_path() == 3:
+        out["kernel_split"] = {"product_ms": k3[0], "step_ms": k3[1], "observation_ms": k3[2],
+                               "note": "device time per batch run in each of the step's three kernels (CUDA events)"}
+        out["step_kernel_issue_roofline"] = issue_roofline("precision", P, k3[1] / 1e3 / m.ndivision, None, True)
     db.close()
     Pp = min(P, plain_particles)
     pb = capi.DeviceBatch(dm, capi.Batch(m, tabs, Pp, seed, group_of=group_of[:Pp], form=capi.FORM_PLAIN_FP64))
@@ -547,27 +568,25 @@ def run_serving_precision(nreq: int, seed: int, model, tables, plain_evals_per_s
             "note": "serving-form log-likelihood evaluations/s over the plain FP64 form's on the same model"}
 
 
-def issue_roofline(kind: str, P: int, t_dev: float, clocks: dict):
-    """The fast kernel's instruction-issue roofline: warp instructions per launch
-    (per-particle count of the committed ncu capture of the workload, times the
-    particles) over the SMs' issue capacity in the timed region -- 4 schedulers
-    per SM, one warp instruction per cycle each, at the median SM clock sampled
-    during the timing.  The kernel keeps its state on chip, so this, not HBM,
-    is the bound that applies."""
-    import re
-    f = os.path.join(ROOT, "profiles", "sim_fast_abc_smc.md" if kind == "abc_smc" else "sim_fast_precision.md")
-    if not os.path.exists(f):
+def issue_roofline(kind: str, P: int, t_dev: float, clocks: dict, batched: bool = False):
+    """The dominant kernel's instruction-issue roofline: warp instructions per
+    launch (per-particle count of the committed ncu capture of the workload,
+    times the particles) over the SMs' issue capacity during the launch -- 4
+    schedulers per SM, one warp instruction per cycle each, at the median SM
+    clock sampled during the timing.  t_dev is the launch's duration.  The
+    kernels are bound by their sampler arithmetic, so this, not HBM, is the
+    bound that applies."""
+    per = profile_figure(kind, batched, "warp_instructions_per_particle")
+    if per is None:
         return None
-    mt = re.search(r"warp_instructions_per_particle:\s*([0-9.eE+]+)", open(f).read())
-    if not mt:
-        return None
+    f = profile_file(kind, batched)
     try:
         import torch
         sms = torch.cuda.get_device_properties(0).multi_processor_count
     except Exception:
         sms = 152
     mhz = (clocks or {}).get("sm_mhz") or 2070.0
-    inst = float(mt.group(1)) * P
+    inst = per * P
     achieved = inst / t_dev
     peak = sms * 4 * mhz * 1e6
     return {"bound": "issue", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "T warp-instructions/s",
@@ -756,8 +775,19 @@ def run_ours(args, rank, ws, dist):
     if rank != 0:
         return
     hbm, hbm_kind = peaks()
-    achieved = BYTES_PER_UNIT * units / t_dev / 1e9
-    traffic = profile_traffic(args.workload, P) if args.form == "fast" else None
+    batched = db.foi_path() == 3
+    if batched:
+        # the dominant kernel of the step-synchronous layout is the step kernel: one launch =
+        # one step of every particle, timed by CUDA events around each launch
+        _, k3 = db.time_kernels(1)
+        t_kernel = k3[1] / 1e3 / m.ndivision
+        units_launch = P * m.narea * m.nage
+        kernels = {"product_ms": k3[0], "step_ms": k3[1], "observation_ms": k3[2],
+                   "note": "device time per batch run in each of the step's three kernels (CUDA events)"}
+    else:
+        t_kernel, units_launch, kernels = t_dev, units, None
+    achieved = BYTES_PER_UNIT * units_launch / t_kernel / 1e9
+    traffic = profile_traffic(args.workload, P, batched) if args.form == "fast" else None
     mbp = None
     if args.mbp_sweeps > 0 and ws == 1:
         mbp = run_mbp_chains(args.mbp_sweeps, args.seed + 99)
@@ -802,8 +832,11 @@ def run_ours(args, rank, ws, dist):
         "gpu_launches": args.steps * db.launches(),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_kind": hbm_kind, "traffic": traffic,
-                     "algorithmic_bytes": f"{BYTES_PER_UNIT} B x {units} units per launch"},
-        "issue_roofline": issue_roofline(args.workload, P, t_dev, clocks) if args.form == "fast" else None,
+                     "kernel": "bx_step (one step of every particle)" if batched else "sim_fast_kernel (whole horizon)",
+                     "algorithmic_bytes": f"{BYTES_PER_UNIT} B x {units_launch} units per launch"},
+        "issue_roofline": (issue_roofline(args.workload, P, t_kernel, clocks, batched) if args.form == "fast"
+                           else None),
+        "kernel_split": kernels,
         "cpu_baseline": cpu,
         "precision_350x10": precision,
         "serving_350x10": serving_precision,

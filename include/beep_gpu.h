@@ -231,6 +231,11 @@ BEEP_API int32_t beep_batch_launches(const beep_batch *batch);   /* kernels per 
  * products of the force of infection (CUDA events around each product kernel;
  * 0 for the other layouts).  A measurement aid with no counterpart in the
  * reference. */
+/* The same split over the three kernels of each step: ms_kernels[0] the products,
+ * [1] the step kernels (means, draws, populations), [2] the observation kernels;
+ * all 0 for the other layouts. */
+BEEP_API beep_status beep_batch_time_kernels(beep_batch *batch, int32_t iters, double *ms_per_launch,
+                                             double *ms_kernels);
 BEEP_API beep_status beep_batch_time_split(beep_batch *batch, int32_t iters, double *ms_per_launch,
                                            double *ms_product);
 /* bytes moved host->device by beep_batch_upload and device->host by beep_batch_download */
