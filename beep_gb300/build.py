@@ -37,6 +37,7 @@ UNITS = {
     "mbp.cu": [],
     "mbp_fast.cu": [],
     "mbp_fast_ctas.cu": [],
+    "mbp_fused.cu": [],
     "serve.cu": [],
 }
 

@@ -359,6 +359,7 @@ def lib():
         for f in ("beep_mbp_initialise", "beep_mbp_propose"):
             getattr(L, f).argtypes = [C.c_void_p, C.POINTER(MbpRequest)]
         L.beep_mbp_set_state.argtypes = [C.c_void_p, C.POINTER(MbpRequest), _i32p]
+        L.beep_mbp_propose_fused.argtypes = [C.c_int32, C.POINTER(C.c_void_p), C.POINTER(MbpRequest)]
         L.beep_mbp_set_state.restype = C.c_int32
         L.beep_mbp_accept.argtypes = [C.c_void_p, C.POINTER(C.c_uint8)]
         L.beep_mbp_state_likelihood.argtypes = [C.c_void_p, C.POINTER(MbpRequest), _f64p]
@@ -647,6 +648,19 @@ class MbpChains:
         r, keep = self._request(tables, seed, group_of, stream_of, inf_update, simu)
         check(lib().beep_mbp_propose(self.h, C.byref(r)))
         return keep["L"]
+
+    @staticmethod
+    def propose_fused(sets: Sequence["MbpChains"], requests: Sequence[dict]) -> list:
+        """Mbp::mbp of the chains of several chain sets (different models) in one
+        persistent launch (beep_mbp_propose_fused).  requests[k] holds set k's
+        propose() arguments (tables, seed, group_of, stream_of, inf_update, simu);
+        returns each set's proposal log-likelihoods."""
+        built = [c._request(q["tables"], q["seed"], q.get("group_of"), q.get("stream_of"),
+                            q.get("inf_update", INF_DIF_UPDATE), q.get("simu")) for c, q in zip(sets, requests)]
+        hs = (C.c_void_p * len(sets))(*[c.h for c in sets])
+        rs = (MbpRequest * len(sets))(*[r for r, _ in built])
+        check(lib().beep_mbp_propose_fused(len(sets), hs, rs))
+        return [keep["L"] for _, keep in built]
 
     def accept(self, accept) -> None:
         a = np.ascontiguousarray(np.asarray(accept, np.uint8))

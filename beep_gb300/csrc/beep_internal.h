@@ -135,7 +135,7 @@ struct BatchDev {
 int launch_sim_plain(const ModelDev &m, const BatchDev &b, void *stream);   // sim_plain.cu
 int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream);    // sim_fast.cu
 size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_stage, bool state_global, int tnrows,
-                       bool pop_single, bool tn_smem = false, int nt = 0);
+                       bool pop_single, bool tn_smem = false, int nt = 0, int mg = 0);   // mg: age stride (0: G to 4s)
 size_t fast_gstate_stride(const ModelDev &m);
 size_t fast_tc_smem_bytes(const ModelDev &m);   // shared memory of the tensor-core FOI
 int fast_pick_threads(const ModelDev &m);        // threads per CTA of the fast kernel for this model
@@ -155,6 +155,13 @@ int fast_ctas_max(int G);                        // most 320-thread CTAs per SM 
 int launch_sim_fast_ctas(const ModelDev &m, const BatchDev &b, size_t smem, void *stream);   // sim_fast_ctas.cu
 int fast_chain_ctas_prepare();                   // constant tables of mbp_fast_ctas.cu
 int launch_sim_fast_chain_ctas(const ModelDev &m, const BatchDev &b, size_t smem, void *stream);   // mbp_fast_ctas.cu
+// MBP chains of several models in one persistent launch (mbp_fused.cu): n chain batches (mode 1),
+// items in array order; counter: one device int32 the launch zeroes and counts on
+constexpr int kMaxFusedSets = 8;
+bool fused_supported(const ModelDev &m);
+int fused_mg(const ModelDev *m, int n);          // age stride of a fused launch over these models
+size_t fused_smem_bytes(const ModelDev &m, const BatchDev &b, int mg);
+int launch_sim_fast_chain_fused(const ModelDev *m, const BatchDev *b, int n, int32_t *counter, int sms, void *stream);
 // fast form for models with more than 8 transitions or 16 age groups (sim_fast_wide.cu)
 bool fast_wide_needed(const ModelDev &m);
 bool fast_wide_supported(const ModelDev &m);   // up to 16 transitions and 20 age groups

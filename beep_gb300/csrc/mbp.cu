@@ -15,6 +15,7 @@
 // bit under the keyed variate stream.
 #include <algorithm>
 #include <cuda_runtime.h>
+#include <numeric>
 
 #include <cmath>
 #include <cstring>
@@ -39,6 +40,7 @@ struct beep_mbp_chains {
 	beep_batch *q[2] = {nullptr, nullptr};
 	int32_t q_ngroup[2] = {0, 0};
 	bool q_go[2] = {false, false}, q_so[2] = {false, false};
+	DevBuf fused_ctr;                    // work counter of fused launches led by this set
 };
 
 namespace {
@@ -55,19 +57,24 @@ void to_fast_layout(const beep_mbp_chains *c, const int32_t *src, int32_t *dst)
 					dst[((size_t)s * T + t) * ncol + (size_t)a * DP + dp] = src[(((size_t)s * A + a) * T + t) * DP + dp];
 }
 
-// One launch of the chain kernel over every chain: mode 1 writes the
-// non-current slot (simu_all: State::simulate), mode 3 rebuilds the
-// non-current slot from its counts, mode 2 scores the current one.
-beep_status run_chains(beep_mbp_chains *c, const beep_mbp_request *r, int mode, bool simu_all, double *Li_out)
+beep_status check_request(const beep_mbp_chains *c, const beep_mbp_request *r, int mode, bool simu_all)
 {
-	beep_model *m = c->m;
 	if (!r || !r->groups || r->ngroup <= 0) return fail(BEEP_BAD_INPUT, "the request needs parameter tables");
 	if (r->inf_update != BEEP_INF_UPDATE && r->inf_update != BEEP_INF_DIF_UPDATE)
 		return fail(BEEP_BAD_INPUT, "unknown inf_update");
 	if (mode == 2 || (mode == 1 && !simu_all))
 		if (!c->initialised) return fail(BEEP_BAD_INPUT, "chains are not initialised");
-	std::lock_guard<std::mutex> lock(m->mu);
-	CUDA_TRY(cudaSetDevice(m->device));
+	return BEEP_OK;
+}
+
+// The chain batch of a request, staged, with its inputs (tables, current
+// slots, SIMU mask) enqueued on the model's stream: mode 1 writes the
+// non-current slot (simu_all: State::simulate), mode 3 rebuilds the
+// non-current slot from its counts, mode 2 scores the current one.  The
+// caller holds the model's lock, with its device current.
+beep_status prepare_chains(beep_mbp_chains *c, const beep_mbp_request *r, int mode, bool simu_all, beep_batch **out)
+{
+	beep_model *m = c->m;
 	const int P = c->nchain;
 	beep_sim_batch b{};
 	b.nparticle = P; b.ngroup = r->ngroup; b.groups = r->groups; b.group_of = r->group_of;
@@ -99,18 +106,17 @@ beep_status run_chains(beep_mbp_chains *c, const beep_mbp_request *r, int mode, 
 		c->q_go[slot] = b.group_of != nullptr;
 		c->q_so[slot] = b.stream_of != nullptr;
 	}
-	auto done = [&](beep_status s) { return s; };
 	const bool mask = mode == 1 && !simu_all && r->simu;
 	Layout L;
 	const size_t o_cur = L.add((size_t)P), o_simu = L.add(mask ? (size_t)P * m->S * m->A : 0),
 	             o_li = L.add(8 * (size_t)P);
 	cudaError_t e = c->aux.reserve(L.size);
-	if (e != cudaSuccess) return done(fail(BEEP_OOM, std::string("chain buffers: ") + cudaGetErrorString(e)));
+	if (e != cudaSuccess) return fail(BEEP_OOM, std::string("chain buffers: ") + cudaGetErrorString(e));
 	char *d = (char *)c->aux.ptr;
 	e = cudaMemcpyAsync(d + o_cur, c->cur.data(), (size_t)P, cudaMemcpyHostToDevice, m->stream);
 	if (e == cudaSuccess && mask)
 		e = cudaMemcpyAsync(d + o_simu, r->simu, (size_t)P * m->S * m->A, cudaMemcpyHostToDevice, m->stream);
-	if (e != cudaSuccess) return done(fail(BEEP_DEVICE_ERROR, cudaGetErrorString(e)));
+	if (e != cudaSuccess) return fail(BEEP_DEVICE_ERROR, cudaGetErrorString(e));
 	BatchDev &bd = q->bd;
 	bd.mode = mode;
 	bd.inf_dif = r->inf_update == BEEP_INF_DIF_UPDATE ? 1 : 0;
@@ -121,13 +127,28 @@ beep_status run_chains(beep_mbp_chains *c, const beep_mbp_request *r, int mode, 
 	bd.ch_mean_f = c->mean_f;
 	bd.Li = (double *)(d + o_li);
 	st = beep_batch_upload(q);
-	if (st == BEEP_OK) st = beep_batch_launch(q);
+	if (st == BEEP_OK) *out = q;
+	return st;
+}
+
+// One launch of the chain kernel over every chain (prepare_chains' modes).
+beep_status run_chains(beep_mbp_chains *c, const beep_mbp_request *r, int mode, bool simu_all, double *Li_out)
+{
+	beep_status st = check_request(c, r, mode, simu_all);
+	if (st != BEEP_OK) return st;
+	beep_model *m = c->m;
+	std::lock_guard<std::mutex> lock(m->mu);
+	CUDA_TRY(cudaSetDevice(m->device));
+	beep_batch *q = nullptr;
+	st = prepare_chains(c, r, mode, simu_all, &q);
+	if (st != BEEP_OK) return st;
+	st = beep_batch_launch(q);
 	if (st == BEEP_OK) st = beep_batch_download(q);   // waits; checks every chain's status
 	if (st == BEEP_OK && mode == 2) {
-		e = cudaMemcpy(Li_out, bd.Li, 8 * (size_t)P, cudaMemcpyDeviceToHost);
+		const cudaError_t e = cudaMemcpy(Li_out, q->bd.Li, 8 * (size_t)c->nchain, cudaMemcpyDeviceToHost);
 		if (e != cudaSuccess) st = fail(BEEP_DEVICE_ERROR, cudaGetErrorString(e));
 	}
-	return done(st);
+	return st;
 }
 
 }  // namespace
@@ -183,6 +204,7 @@ BEEP_API beep_status beep_mbp_destroy(beep_mbp_chains *c)
 		if (q) beep_batch_destroy(q);
 	c->traj.release();
 	c->aux.release();
+	c->fused_ctr.release();
 	delete c;
 	return BEEP_OK;
 }
@@ -228,6 +250,91 @@ BEEP_API beep_status beep_mbp_propose(beep_mbp_chains *c, const beep_mbp_request
 {
 	if (!c) return fail(BEEP_BAD_INPUT, "null chains");
 	return run_chains(c, r, 1, false, nullptr);
+}
+
+BEEP_API beep_status beep_mbp_propose_fused(int32_t nset, beep_mbp_chains *const *sets,
+                                            const beep_mbp_request *requests)
+{
+	if (nset <= 0 || nset > kMaxFusedSets || !sets || !requests)
+		return fail(BEEP_BAD_INPUT, "1 to " + std::to_string(kMaxFusedSets) + " chain sets, one request each");
+	for (int k = 0; k < nset; k++) {
+		const beep_mbp_chains *c = sets[k];
+		if (!c) return fail(BEEP_BAD_INPUT, "null chains");
+		if (c->form != BEEP_FORM_FAST) return fail(BEEP_BAD_INPUT, "a fused launch takes fast-form chains");
+		if (c->m->device != sets[0]->m->device) return fail(BEEP_BAD_INPUT, "the chain sets are on different devices");
+		if (!fused_supported(c->m->dev))
+			return fail(BEEP_BAD_INPUT, "a fused launch takes models of at most 8 transitions and 16 age groups");
+		for (int j = 0; j < k; j++)
+			if (sets[j] == c) return fail(BEEP_BAD_INPUT, "a chain set appears twice");
+		beep_status st = check_request(c, &requests[k], 1, false);
+		if (st != BEEP_OK) return st;
+	}
+	// every model once, locked in address order
+	std::vector<beep_model *> models;
+	for (int k = 0; k < nset; k++) models.push_back(sets[k]->m);
+	std::sort(models.begin(), models.end());
+	models.erase(std::unique(models.begin(), models.end()), models.end());
+	std::vector<std::unique_lock<std::mutex>> locks;
+	for (beep_model *m : models) locks.emplace_back(m->mu);
+	CUDA_TRY(cudaSetDevice(sets[0]->m->device));
+	// launch order: the sets whose chains cost most first (steps x columns x transitions)
+	std::vector<int> order(nset);
+	std::iota(order.begin(), order.end(), 0);
+	auto cost = [&](int k) {
+		const beep_model *m = sets[k]->m;
+		return (double)m->S * m->A * m->DP * m->T;
+	};
+	std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost(x) > cost(y); });
+	beep_mbp_chains *lead = sets[order[0]];
+	cudaStream_t st0 = lead->m->stream;
+	// on an error once work is enqueued: wait for it, so that no copy is left in flight
+	auto drain = [&](beep_status s) {
+		for (beep_model *m : models) cudaStreamSynchronize(m->stream);
+		return s;
+	};
+	std::vector<beep_batch *> qs(nset, nullptr);
+	for (int i = 0; i < nset; i++) {
+		const int k = order[i];
+		beep_status st = prepare_chains(sets[k], &requests[k], 1, false, &qs[k]);
+		if (st != BEEP_OK) return drain(st);
+	}
+	// the other models' inputs are on their own streams: complete before the launch on st0
+	for (beep_model *m : models)
+		if (m->stream != st0 && cudaStreamSynchronize(m->stream) != cudaSuccess)
+			return drain(fail(BEEP_DEVICE_ERROR, "chain inputs"));
+	ModelDev md[kMaxFusedSets];
+	BatchDev bd[kMaxFusedSets];
+	for (int i = 0; i < nset; i++) {
+		md[i] = sets[order[i]]->m->dev;
+		bd[i] = qs[order[i]]->bd;
+		bd[i].sampler_limit = option_sampler_limit();
+	}
+	// one shared-memory layout per set at the launch's thread count and age stride: the
+	// area-mixing matrix is read from L2 where its copy no longer fits
+	const int mg = fused_mg(md, nset);
+	const size_t limit = 227 * 1024;
+	for (int i = 0; i < nset; i++) {
+		if (bd[i].m_in_smem && fused_smem_bytes(md[i], bd[i], mg) > limit) bd[i].m_in_smem = 0;
+		if (fused_smem_bytes(md[i], bd[i], mg) > limit)
+			return drain(fail(BEEP_BAD_INPUT, "a model's chain state exceeds the shared memory of a fused launch"));
+	}
+	cudaError_t e = lead->fused_ctr.reserve(256);
+	for (int i = 0; i < nset && e == cudaSuccess; i++)
+		e = cudaMemsetAsync(bd[i].status, 0, 4 * (size_t)bd[i].P, st0);
+	if (e != cudaSuccess) return drain(fail(BEEP_DEVICE_ERROR, cudaGetErrorString(e)));
+	const int le = launch_sim_fast_chain_fused(md, bd, nset, (int32_t *)lead->fused_ctr.ptr, lead->m->sms, st0);
+	if (le != 0)
+		return drain(fail(BEEP_DEVICE_ERROR, std::string("kernel launch: ") + cudaGetErrorString((cudaError_t)le)));
+	for (int k = 0; k < nset && e == cudaSuccess; k++)
+		e = cudaMemcpyAsync(qs[k]->out_host.ptr, qs[k]->out_dev.ptr, qs[k]->out_size, cudaMemcpyDeviceToHost, st0);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(st0);
+	if (e != cudaSuccess) return drain(fail(BEEP_DEVICE_ERROR, cudaGetErrorString(e)));
+	beep_status st = BEEP_OK;
+	for (int k = 0; k < nset; k++) {              // statuses and L of every set
+		const beep_status sk = batch_download_finish(qs[k]);
+		if (st == BEEP_OK) st = sk;
+	}
+	return st;
 }
 
 BEEP_API beep_status beep_mbp_accept(beep_mbp_chains *c, const uint8_t *accept)

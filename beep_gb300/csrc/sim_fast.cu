@@ -12,11 +12,11 @@ static int pick_threads(const ModelDev &m)
 }
 
 size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_stage, bool state_global,
-                       int tnrows, bool pop_single, bool tn_smem, int nt)
+                       int tnrows, bool pop_single, bool tn_smem, int nt, int mg)
 {
 	auto r = [](size_t x) { return (x + 15) & ~(size_t)15; };
 	const size_t A = m.A, G = m.G, DP = m.DP, NS = m.NS, C = m.C, T = m.T, DPS = m.DPS;
-	const size_t agsz = NS * A * (size_t)((m.G + 3) & ~3), ncol = A * DP;
+	const size_t agsz = NS * A * (size_t)(mg > 0 ? mg : (m.G + 3) & ~3), ncol = A * DP;
 	return (m_in_smem ? r(4 * A * ms_lda(m.A)) : 0) + (state_global ? 0 : (pop_single ? 1 : 2) * r(4 * C * ncol)) +
 	       (state_global && !tn_smem ? 0 : r(4 * (size_t)tnrows * ncol)) + 3 * r(4 * agsz) +
 	       r(4 * (size_t)nslots) + 3 * r(4 * T) + r(4 * DPS) + r(4 * C) + r(4 * T * DP) + r(4 * DP) + r(4 * 64) +

@@ -506,13 +506,13 @@ __device__ __forceinline__ int32_t binomial_fp32(float p, int32_t n, uint32_t k0
 // chains; two of 256 or four of 128 threads for small models.
 constexpr int min_ctas(int nt) { return nt >= 640 ? 1 : nt >= 256 ? 2 : 4; }
 
-// MT: the most transitions the per-column mean registers hold (kMaxT, or kWideT
-// for models with more transitions)
-template <int NT, int MG, bool TC, bool CH = false, int MB = min_ctas(NT), int MT = kMaxT>
-__global__ void __launch_bounds__(NT, MB) sim_fast_kernel(const ModelDev m, const BatchDev b)
+// One particle (or MBP chain) p of a batch over its whole step range, run by
+// the NT threads of a CTA.  MT: the most transitions the per-column mean
+// registers hold (kMaxT, or kWideT for models with more transitions).
+template <int NT, int MG, bool TC, bool CH, int MT>
+__device__ __forceinline__ void sim_fast_body(const ModelDev &m, const BatchDev &b, const int p)
 {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
-	const int p = blockIdx.x;
 	if (p >= b.P) return;
 	const int tid = threadIdx.x;
 	const int A = m.A, G = m.G, DP = m.DP, NS = m.NS, DPS = m.DPS, C = m.C, T = m.T;
@@ -930,6 +930,13 @@ __global__ void __launch_bounds__(NT, MB) sim_fast_kernel(const ModelDev m, cons
 			}
 		}
 	}
+}
+
+// One CTA per particle (or MBP chain): CTA p runs particle p.
+template <int NT, int MG, bool TC, bool CH = false, int MB = min_ctas(NT), int MT = kMaxT>
+__global__ void __launch_bounds__(NT, MB) sim_fast_kernel(const ModelDev m, const BatchDev b)
+{
+	sim_fast_body<NT, MG, TC, CH, MT>(m, b, blockIdx.x);
 }
 
 // log k! for k < 32 in this translation unit's constant memory, once (before

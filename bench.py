@@ -396,8 +396,11 @@ def run_mbp_chains(sweeps: int, seed: int, nchain: int = 128, plain_sweeps: int 
     80x4, 200x6 and 350x10 (areas x ages, dt 0.5, 200 days, weekly hospital
     populations).  A sweep is one coupled proposal per chain (parameters
     perturbed by a factor exp(N(0, 0.05)) per parameter), the FP64 acceptance
-    ratio exp(L' - L) (uniform priors, invT = 1) and the accept step.  The four
-    models' proposals run concurrently (one host thread and stream each)."""
+    ratio exp(L' - L) (uniform priors, invT = 1) and the accept step.  The fast
+    form proposes every chain of the four models in one fused persistent launch
+    (beep_mbp_propose_fused); it is also timed with the four models' proposals
+    as concurrent launches (one host thread and stream each), as the plain FP64
+    form runs."""
     import threading
     from beep_gb300 import capi, model_builder as mb, synth
     rng = np.random.default_rng(seed)
@@ -416,36 +419,48 @@ def run_mbp_chains(sweeps: int, seed: int, nchain: int = 128, plain_sweeps: int 
         m = capi.Model(arr)
         th = np.stack([rng.uniform(2.2, 2.8, nchain), rng.uniform(3.6, 4.4, nchain), rng.uniform(4.5, 5.5, nchain)], 1)
         props = []
-        for k in range(sweeps + plain_sweeps):
+        for k in range(2 * sweeps + plain_sweeps):
             tp = th * np.exp(rng.normal(0, 0.05, th.shape))
             props.append([capi.Tables(t) for t in mb.param_tables_batch(w, tp[:, 0], tp[:, 1], tp[:, 2])])
         t0 = [capi.Tables(t) for t in mb.param_tables_batch(w, th[:, 0], th[:, 1], th[:, 2])]
         models.append(dict(w=w, m=m, t0=t0, props=props, units=nchain * A * G * m.ndivision))
     units = sum(x["units"] for x in models)
     out = {}
-    for form, nsw in ((capi.FORM_FAST, sweeps), (capi.FORM_PLAIN_FP64, plain_sweeps)):
+    runs = (("fast", capi.FORM_FAST, sweeps, True), ("fast_separate_launches", capi.FORM_FAST, sweeps, False),
+            ("plain_fp64", capi.FORM_PLAIN_FP64, plain_sweeps, False))
+    base = 0
+    for name, form, nsw, fused in runs:
         if nsw <= 0:
             continue
         for x in models:
-            x["dm"] = capi.DeviceModel(x["m"])
-            x["ch"] = capi.MbpChains(x["dm"], nchain, form=form)
-            x["L"] = x["ch"].initialise(x["t0"], seed, stream_of=np.arange(nchain), group_of=np.arange(nchain))
+            if x.get("form") != form:
+                if "ch" in x:
+                    x["ch"].close()
+                    x["dm"].close()
+                x["dm"] = capi.DeviceModel(x["m"])
+                x["ch"] = capi.MbpChains(x["dm"], nchain, form=form)
+                x["L"] = x["ch"].initialise(x["t0"], seed, stream_of=np.arange(nchain), group_of=np.arange(nchain))
+                x["form"] = form
         acc = []
         times = []
-        base = 0 if form == capi.FORM_FAST else sweeps
         for k in range(nsw):
+            reqs = [dict(tables=x["props"][base + k], seed=seed, group_of=np.arange(nchain),
+                         stream_of=np.arange(nchain) + (base + k + 1) * nchain, inf_update=capi.INF_DIF_UPDATE)
+                    for x in models]
             res = {}
 
             def work(i, x):
-                res[i] = x["ch"].propose(x["props"][base + k], seed, group_of=np.arange(nchain),
-                                         stream_of=np.arange(nchain) + (k + 1) * nchain,
-                                         inf_update=capi.INF_DIF_UPDATE)
+                res[i] = x["ch"].propose(**reqs[i])
             t0 = time.perf_counter()
-            th_ = [threading.Thread(target=work, args=(i, x)) for i, x in enumerate(models)]
-            for t in th_:
-                t.start()
-            for t in th_:
-                t.join()
+            if fused:
+                for i, L in enumerate(capi.MbpChains.propose_fused([x["ch"] for x in models], reqs)):
+                    res[i] = L
+            else:
+                th_ = [threading.Thread(target=work, args=(i, x)) for i, x in enumerate(models)]
+                for t in th_:
+                    t.start()
+                for t in th_:
+                    t.join()
             for i, x in enumerate(models):
                 al = np.minimum(1.0, np.exp(np.clip(res[i] - x["L"], -700, 0)))
                 ok = rng.random(nchain) < al
@@ -453,7 +468,8 @@ def run_mbp_chains(sweeps: int, seed: int, nchain: int = 128, plain_sweeps: int 
                 x["L"] = np.where(ok, res[i], x["L"])
                 acc.append(ok.mean())
             times.append(time.perf_counter() - t0)
-        if form == capi.FORM_FAST:
+        base += nsw
+        if fused:
             # the chains' log-likelihoods against FP64 scoring of their own current trajectories
             x = models[-1]
             errs = []
@@ -465,17 +481,19 @@ def run_mbp_chains(sweeps: int, seed: int, nchain: int = 128, plain_sweeps: int 
             out["loglik_vs_fp64"] = {"model": f"{x['m'].narea}x{x['m'].nage}", "chains": len(errs),
                                      "max_rel_err_vs_fp64_of_own_trajectory": float(max(errs)) if errs else None,
                                      "tolerance": 1e-6}
-        for x in models:
+        t = statistics.mean(times)
+        out[name] = {"value": units / t, "unit": "chain.area.group.steps/s", "ms_per_sweep": t * 1e3, "sweeps": nsw,
+                     "acceptance": float(np.mean(acc)),
+                     "launches_per_sweep": 1 if fused else len(models)}
+    for x in models:
+        if "ch" in x:
             x["ch"].close()
             x["dm"].close()
-        t = statistics.mean(times)
-        out["fast" if form == capi.FORM_FAST else "plain_fp64"] = {
-            "value": units / t, "unit": "chain.area.group.steps/s", "ms_per_sweep": t * 1e3, "sweeps": nsw,
-            "acceptance": float(np.mean(acc))}
     out.update({"workload": "mbp_chains_uneven", "chains": 4 * nchain,
                 "models": [f"{A}x{G}" for (A, G) in synth.MBP_SIZES], "steps": models[0]["m"].ndivision,
                 "units_per_sweep": units, "data": "synthetic, weekly hospital populations",
-                "timing": "host wall clock per sweep (4 concurrent model streams, proposals + FP64 acceptance)"})
+                "timing": "host wall clock per sweep (proposals of every chain + FP64 acceptance); fast: one "
+                          "fused persistent launch per sweep; separate launches / plain: 4 concurrent model streams"})
     return out
 
 

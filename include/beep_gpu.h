@@ -434,6 +434,19 @@ BEEP_API beep_status beep_mbp_set_state(beep_mbp_chains *chains, const beep_mbp_
  * n' = n + Poisson(m'-m) (m' > m), n (m' = m) or Binomial(n, m'/m) (m' < m)
  * from the keyed stream of the chain; a SIMU cell draws Poisson(m'). */
 BEEP_API beep_status beep_mbp_propose(beep_mbp_chains *chains, const beep_mbp_request *request);
+/* Mbp::mbp (src/mbp.cc:252-330) for the chains of up to 8 chain sets of
+ * different models (uneven areas, ages and horizons) at once, in ONE
+ * persistent kernel launch: requests[k] is set k's proposal request, as for
+ * beep_mbp_propose.  One 640-thread CTA per SM takes chains from a work
+ * counter, the sets whose chains cost most first.  Each chain's counts are
+ * those beep_mbp_propose gives for its set (the same keyed streams and
+ * arithmetic); a set whose own launch runs fewer threads per chain can differ
+ * in the last FP32 bits of L (its observation terms are summed over another
+ * split of threads).  The sets must be fast-form, initialised, distinct and
+ * on one device, with models of at most 8 transitions and 16 age groups.
+ * The reference updates its chains one after another (Mbp::mcmc_updates, src/mbp.cc:34-98). */
+BEEP_API beep_status beep_mbp_propose_fused(int32_t nset, beep_mbp_chains *const *sets,
+                                            const beep_mbp_request *requests);
 /* Mbp::swap_initial_propose_state (src/mbp.cc:241-246) for every chain with
  * accept[k] != 0: its last proposal becomes its current state. */
 BEEP_API beep_status beep_mbp_accept(beep_mbp_chains *chains, const uint8_t *accept);
