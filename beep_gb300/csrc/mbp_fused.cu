@@ -30,6 +30,8 @@ struct FusedChains {
 	ModelDev m[kMaxFusedSets];
 	BatchDev b[kMaxFusedSets];
 };
+// one kernel parameter: within the 32764 bytes a launch takes (CUDA 12.1 and later)
+static_assert(sizeof(FusedChains) <= 32764, "the fused launch descriptor exceeds the kernel parameter limit");
 
 template <int MG>
 __global__ void __launch_bounds__(kFusedThreads, 1) sim_fast_fused_kernel(const __grid_constant__ FusedChains f)
