@@ -129,13 +129,38 @@ struct BatchDev {
 	unsigned char *bx_a;                // the next product's A operand: per (128-row tile, 32-source chunk) the
 	                                    // infectious counts as split BF16 (hi, lo) in K-major core matrices
 	int32_t ctas;                       // fast form, nt == kDualThreads: CTAs resident per SM (2..4)
+	int32_t pd;                         // fast form, small models and batches: the draws of a step one per
+	                                    // (transition, column) thread (latency: the GPU is not full)
 };
+
+#if defined(__CUDACC__)
+// Raises a kernel's dynamic shared-memory limit (a per-kernel attribute) to the most the
+// device allows beside the kernel's static shared memory, and checks that `need` fits.
+// Every host thread sets the same value, so that concurrent launches of one kernel with
+// different sizes (requests served from several threads) do not undercut each other.
+template <typename K>
+inline cudaError_t allow_dynamic_smem(K kern, size_t need)
+{
+	cudaFuncAttributes fa;
+	cudaError_t e = cudaFuncGetAttributes(&fa, (const void *)kern);
+	if (e != cudaSuccess) return e;
+	int dev = 0, optin = 0;
+	e = cudaGetDevice(&dev);
+	if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+	if (e != cudaSuccess) return e;
+	const long long lim = (long long)optin - (long long)fa.sharedSizeBytes;
+	if ((long long)need > lim) return cudaErrorInvalidValue;
+	return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim);
+}
+#endif
 
 // launchers
 int launch_sim_plain(const ModelDev &m, const BatchDev &b, void *stream);   // sim_plain.cu
 int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream);    // sim_fast.cu
 size_t fast_smem_bytes(const ModelDev &m, int nslots, bool m_in_smem, int nefoi_stage, bool state_global, int tnrows,
-                       bool pop_single, bool tn_smem = false, int nt = 0, int mg = 0);   // mg: age stride (0: G to 4s)
+                       bool pop_single, bool tn_smem = false, int nt = 0, int mg = 0,    // mg: age stride (0: G to 4s)
+                       bool pd = false);                                                 // pd: draws per (transition, column)
+bool fast_pd_fits(const ModelDev &m, int nt);    // the draws of a step fit two passes of nt threads
 size_t fast_gstate_stride(const ModelDev &m);
 size_t fast_tc_smem_bytes(const ModelDev &m);   // shared memory of the tensor-core FOI
 int fast_pick_threads(const ModelDev &m);        // threads per CTA of the fast kernel for this model
@@ -143,6 +168,7 @@ int fast_pick_threads(const ModelDev &m);        // threads per CTA of the fast 
 int option_fast_foi();                           // 0 automatic, 1 FP32 SIMT, 2 tensor cores per particle,
                                                  // 3 tensor cores batched over the particles (step-synchronous)
 int option_fast_ctas();                          // 0 automatic, 1, or 2..4: particles (CTAs) per SM, at most
+int option_parallel_draws();                     // 0 automatic, 1 never, 2 where the draws fit
 uint32_t option_sampler_limit();                 // 0 (65536) or the rejection-iteration limit of the samplers
 constexpr int kDualThreads = 320;                // threads per CTA with several particles per SM
 constexpr size_t kSmemPerSM = 228 * 1024;        // shared memory per SM (each resident CTA reserves 1 KB)

@@ -36,6 +36,7 @@ thread_local std::string g_err;
 std::atomic<int> g_fast_foi{0};
 std::atomic<int> g_fast_ctas{0};
 std::atomic<uint32_t> g_sampler_limit{0};
+std::atomic<int> g_parallel_draws{0};
 
 beep_status fail(beep_status s, const std::string &msg)
 {
@@ -80,6 +81,11 @@ beep_status beep_set_option(const char *name, int64_t value)
 	if (std::string(name) == "fast_ctas_per_sm") {
 		if (value < 0 || value > 4) return fail(BEEP_BAD_INPUT, "fast_ctas_per_sm must be 0 (automatic) or 1..4");
 		g_fast_ctas.store((int)value);
+		return BEEP_OK;
+	}
+	if (std::string(name) == "fast_parallel_draws") {
+		if (value < 0 || value > 2) return fail(BEEP_BAD_INPUT, "fast_parallel_draws must be 0 (automatic), 1 (never) or 2");
+		g_parallel_draws.store((int)value);
 		return BEEP_OK;
 	}
 	if (std::string(name) == "sampler_iteration_limit") {
@@ -861,6 +867,13 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 				q->bd.m_in_smem = (size_t)k * (s1 + 1024) <= kSmemPerSM ? 1 : 0;
 			}
 		}
+		// small models in batches too small to fill the GPU (at most four particles per SM):
+		// a step's draws one per (transition, column) thread, which shortens the step's
+		// sequential chain of draws per thread (the particle filter's sections are this case)
+		const int popt = option_parallel_draws();
+		const int nt_run = q->bd.nt > 0 ? q->bd.nt : fast_pick_threads(m->dev);
+		q->bd.pd = !wide && !q->bd.foi_tc && !q->bd.batched && fast_pd_fits(m->dev, nt_run) && popt != 1 &&
+		           (popt == 2 || (long long)P <= 4LL * std::max(1, m->sms)) ? 1 : 0;
 	}
 	auto bail = [&](beep_status s) { beep_batch_destroy(q); return s; };
 	if (b->form == BEEP_FORM_FAST && fast_prepare() != 0) return bail(fail(BEEP_DEVICE_ERROR, "constant tables"));
@@ -1109,20 +1122,43 @@ beep_status beep_autotune(beep_model *m, const beep_sim_batch *b, int32_t *chose
 {
 	if (!m || !b) return fail(BEEP_BAD_INPUT, "null argument");
 	if (b->form != BEEP_FORM_FAST) return fail(BEEP_BAD_INPUT, "the autotuner chooses among fast-form kernels");
-	// a sample of the batch: its first particles over the first steps of its range
-	beep_sim_batch t = *b;
+	// the sample: the batch's particles up to 64 per SM over a window of up to 90 steps in
+	// the middle of its range, started from the populations a run of the first steps leaves
+	// there -- the layouts' costs shift as an epidemic grows (draws of larger means, fixed
+	// per-step costs weighing less), and a window at the start favoured the
+	// particle-resident layouts (398 against 379 ms per 16384-particle generation of the
+	// 150-area x 4-age ABC-SMC workload)
 	int dev_sms = 152;
 	cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, m->device);
-	// (two waves of the four-per-SM layout: every candidate fills the SMs alike)
-	t.nparticle = std::min(b->nparticle, 8 * dev_sms);
-	t.tf = std::min(b->tf, b->ti + 60);
+	beep_sim_batch t = *b;
+	t.nparticle = std::min(b->nparticle, 64 * dev_sms);
 	t.L_out = nullptr;
 	t.pop_out = nullptr;
+	t.pop_out_f64 = nullptr;
 	t.transnum_out = nullptr;
 	t.pop_traj_out = nullptr;
+	t.pop_traj_out_f64 = nullptr;
+	if (t.ti > 0 && !t.pop_in) return fail(BEEP_BAD_INPUT, "pop_in is required when ti > 0");
+	const int range = b->tf - b->ti, win = std::min(range, 90), t0 = b->ti + (range - win) / 2;
+	std::vector<int32_t> pop_mid;
+	if (t0 > b->ti) {
+		beep_sim_batch pre = t;
+		pre.tf = t0;
+		pop_mid.resize((size_t)t.nparticle * m->A * m->C * m->DP);
+		pre.pop_out = pop_mid.data();
+		beep_batch *q = nullptr;
+		beep_status st = beep_batch_create(m, &pre, &q);
+		if (st == BEEP_OK) st = beep_batch_upload(q);
+		if (st == BEEP_OK) st = beep_batch_launch(q);
+		if (st == BEEP_OK) st = beep_batch_download(q);
+		if (q) beep_batch_destroy(q);
+		if (st != BEEP_OK) return st;
+		t.ti = t0;
+		t.pop_in = pop_mid.data();
+	}
+	t.tf = t0 + win;
 	std::vector<double> L(t.nparticle);
 	t.L_out = L.data();
-	if (t.ti > 0 && !t.pop_in) return fail(BEEP_BAD_INPUT, "pop_in is required when ti > 0");
 	const int saved_foi = m->tuned_foi, saved_ctas = m->tuned_ctas;
 	double best = 1e300;
 	int best_foi = 1, best_ctas = 1;
@@ -1145,7 +1181,7 @@ beep_status beep_autotune(beep_model *m, const beep_sim_batch *b, int32_t *chose
 		double ms = 0;
 		st = beep_batch_upload(q);
 		if (st == BEEP_OK) st = beep_batch_time(q, 1, &ms);      // warm-up
-		if (st == BEEP_OK) st = beep_batch_time(q, 2, &ms);
+		if (st == BEEP_OK) st = beep_batch_time(q, 1, &ms);
 		beep_batch_destroy(q);
 		if (st != BEEP_OK) { m->tuned_foi = saved_foi; m->tuned_ctas = saved_ctas; return st; }
 		if (ms < best) { best = ms; best_foi = c[0]; best_ctas = c[1]; }
@@ -1228,3 +1264,4 @@ int beep::option_fast_foi() { return g_fast_foi.load(); }
 int beep::option_fast_ctas() { return g_fast_ctas.load(); }
 
 uint32_t beep::option_sampler_limit() { return g_sampler_limit.load(); }
+int beep::option_parallel_draws() { return g_parallel_draws.load(); }

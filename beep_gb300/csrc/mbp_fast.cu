@@ -21,7 +21,7 @@ int launch_chain_nt(const ModelDev &m, const BatchDev &b, size_t smem, cudaStrea
 {
 	auto kern = m.G <= 4 ? sim_fast_kernel<NT, 4, false, true> : m.G <= 8 ? sim_fast_kernel<NT, 8, false, true>
 	          : m.G <= 12 ? sim_fast_kernel<NT, 12, false, true> : sim_fast_kernel<NT, 16, false, true>;
-	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	cudaError_t e = allow_dynamic_smem(kern, smem);
 	if (e != cudaSuccess) return (int)e;
 	kern<<<b.P, NT, smem, st>>>(m, b);
 	return (int)cudaGetLastError();

@@ -88,7 +88,7 @@ int launch_sim_fast_chain_fused(const ModelDev *m, const BatchDev *b, int n, int
 	if (f.nitem == 0) return 0;
 	auto kern = mg <= 4 ? sim_fast_fused_kernel<4> : mg <= 8 ? sim_fast_fused_kernel<8>
 	          : mg <= 12 ? sim_fast_fused_kernel<12> : sim_fast_fused_kernel<16>;
-	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	cudaError_t e = allow_dynamic_smem(kern, smem);
 	if (e != cudaSuccess) return (int)e;
 	cudaStream_t st = (cudaStream_t)stream;
 	e = cudaMemsetAsync(counter, 0, sizeof(int32_t), st);

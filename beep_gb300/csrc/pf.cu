@@ -33,14 +33,25 @@ namespace beep {
 namespace {
 
 constexpr int kBootThreads = 1024;
+constexpr int kBootSmemN = 8192;   // particles whose cumulative sums and placement fit shared memory
 
+// The sequential parts (cumulative sums, placement) read and write one slot after another:
+// their arrays are in shared memory for N <= kBootSmemN (launched with 16 N bytes of dynamic
+// shared memory), where a load after a store to another slot does not wait for global
+// memory; larger filters use the global scratch arrays.
 __global__ void __launch_bounds__(kBootThreads) pf_bootstrap(const double *L, int N, double invT, uint32_t k0,
                                                             uint32_t k1, uint32_t rstream, int sec, double *w,
-                                                            double *wsum, int32_t *sel, int32_t *bp, int32_t *extra,
-                                                            double *ob_sec, int32_t *anc, int32_t *status)
+                                                            double *wsum_g, int32_t *sel, int32_t *bp_g,
+                                                            int32_t *extra_g, double *ob_sec, int32_t *anc,
+                                                            int32_t *status)
 {
+	extern __shared__ __align__(16) unsigned char boot_smem[];
 	__shared__ double red[kBootThreads];
 	__shared__ double s_sum;
+	const bool sm = N <= kBootSmemN;
+	double *wsum = sm ? (double *)boot_smem : wsum_g;
+	int32_t *bp = sm ? (int32_t *)(boot_smem + 8 * (size_t)N) : bp_g;
+	int32_t *extra = sm ? (int32_t *)(boot_smem + 12 * (size_t)N) : extra_g;
 	const int tid = threadIdx.x;
 	double mx = -1000000000.0;                       // -LARGE, src/pmcmc.cc:223
 	for (int p = tid; p < N; p += kBootThreads) mx = fmax(mx, L[p]);
@@ -89,8 +100,10 @@ __global__ void __launch_bounds__(kBootThreads) pf_bootstrap(const double *L, in
 			if (bp[p] == -1) bp[p] = extra[--ne];
 	}
 	__syncthreads();
-	if (anc)
-		for (int p = tid; p < N; p += kBootThreads) anc[p] = bp[p];
+	for (int p = tid; p < N; p += kBootThreads) {
+		if (sm) bp_g[p] = bp[p];
+		if (anc) anc[p] = bp[p];
+	}
 }
 
 __global__ void pf_gather(int32_t *dst, const int32_t *src, const int32_t *bp, int N, int popsz)
@@ -184,6 +197,10 @@ extern "C" BEEP_API beep_status beep_pf_loglik(beep_model *m, const beep_pf_requ
 	std::string err;
 	auto bail = [&](beep_status s, const std::string &msg) { status = s; err = msg; };
 	if (cudaMemsetAsync(pst, 0, 4, st) != cudaSuccess) bail(BEEP_DEVICE_ERROR, "memset");
+	// the bootstrap's cumulative sums and placement in shared memory (16 N bytes) where they fit
+	const size_t boot_smem = N <= kBootSmemN ? 16 * (size_t)N : 0;
+	if (status == BEEP_OK && allow_dynamic_smem(pf_bootstrap, boot_smem) != cudaSuccess)
+		bail(BEEP_DEVICE_ERROR, "bootstrap shared memory");
 	for (int k = 0; k < ns && status == BEEP_OK; k++) {
 		beep_batch *b = q[k];
 		if (beep_batch_upload(b) != BEEP_OK) { bail(BEEP_DEVICE_ERROR, beep_last_error()); break; }
@@ -193,7 +210,7 @@ extern "C" BEEP_API beep_status beep_pf_loglik(beep_model *m, const beep_pf_requ
 		// section k's counts of every slot: [slot][step - ti][cell] at N * ti cells in
 		if (lineage) b->bd.tn_traj = (int32_t *)(d + o_tn) + (size_t)N * r->section_ti[k] * tnsz;
 		if (beep_batch_launch(b) != BEEP_OK) { bail(BEEP_DEVICE_ERROR, beep_last_error()); break; }
-		pf_bootstrap<<<1, kBootThreads, 0, st>>>(Lall + (size_t)k * N, N, r->invT, (uint32_t)r->seed,
+		pf_bootstrap<<<1, kBootThreads, boot_smem, st>>>(Lall + (size_t)k * N, N, r->invT, (uint32_t)r->seed,
 		                                         (uint32_t)(r->seed >> 32), r->resample_stream, k,
 		                                         (double *)(d + o_w), (double *)(d + o_ws), (int32_t *)(d + o_sel),
 		                                         (int32_t *)(d + o_bp), (int32_t *)(d + o_ex), obsec,

@@ -585,11 +585,11 @@ template <int MG, int MB>
 int launch_steps(const ModelDev &m, const BatchDev &b, size_t smem_step, int sms, cudaStream_t st, cudaEvent_t *ev)
 {
 	auto kstep = bx_step<MG, MB>;
-	cudaError_t e = cudaFuncSetAttribute(kstep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_step);
+	cudaError_t e = allow_dynamic_smem(kstep, smem_step);
 	if (e != cudaSuccess) return (int)e;
 	const BxGeom x = bx_geometry(m.A, m.NS);
 	const size_t smem_foi = (size_t)kBxStages * x.stage;
-	e = cudaFuncSetAttribute(bx_foi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_foi);
+	e = allow_dynamic_smem(bx_foi, smem_foi);
 	if (e != cudaSuccess) return (int)e;
 	const int rows = b.P * m.NS * m.G;
 	const int ntile = (rows + kBxRows - 1) / kBxRows * x.nct;   // (row tile, target chunk) pairs

@@ -83,6 +83,7 @@ struct FastSmem {
 	float *dgeo;          // [2] geographic spline value
 	float *red;           // [2*NT]
 	float *mv;            // [T][NT] each thread's transition means (320-thread CTAs, whose registers are tight)
+	float *pm;            // [T][ncol] the step's transition means (draws per (transition, column)), or null
 };
 
 __host__ __device__ inline int ms_lda(int A) { return A + ((40 - A % 32) % 32); }
@@ -509,7 +510,7 @@ constexpr int min_ctas(int nt) { return nt >= 640 ? 1 : nt >= 256 ? 2 : 4; }
 // One particle (or MBP chain) p of a batch over its whole step range, run by
 // the NT threads of a CTA.  MT: the most transitions the per-column mean
 // registers hold (kMaxT, or kWideT for models with more transitions).
-template <int NT, int MG, bool TC, bool CH, int MT>
+template <int NT, int MG, bool TC, bool CH, int MT, bool PD = false>
 __device__ __forceinline__ void sim_fast_body(const ModelDev &m, const BatchDev &b, const int p)
 {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -587,6 +588,7 @@ __device__ __forceinline__ void sim_fast_body(const ModelDev &m, const BatchDev 
 		s.dgeo = (float *)take(4 * 2);
 		s.red = (float *)take(4 * 2 * (size_t)NT);
 		s.mv = NT == kDualThreads ? (float *)take(4 * (size_t)T * NT) : nullptr;
+		s.pm = PD ? (float *)take(4 * (size_t)T * ncol) : nullptr;
 	}
 	// tensor-core FOI (large models, 640 threads): chunk ring, stacked counts, barriers, tensor memory
 	__shared__ uint64_t tc_bars[2 * tc::kStages + 1];
@@ -694,6 +696,82 @@ __device__ __forceinline__ void sim_fast_body(const ModelDev &m, const BatchDev 
 
 		// ---- A: per column (c, dp): NMI, means, draws, next population and infectious count
 		const float d = s.dgeo[sb], omd = 1.f - d;
+		if constexpr (PD) {
+		// ---- A, small models: the means of every column, then one draw per (transition,
+		//      column) -- the draws of a column run on T threads at once instead of one after
+		//      another on one -- then every column's next infectious count
+		for (int col = tid; col < ncol; col += NT) {
+			const int c = col / DP, dp = col - c * DP;
+			const int st = dp / DPS, dpl = dp - st * DPS, a = s.age[dpl];
+			float minf = 0.f;
+			{
+				const float popu = (float)pc[inf_from * ncol + c * DP + dpl];
+				if (popu > 0.f) {
+					const float fac = m.M_factor_f[c], dg = m.M_diag_f[c];
+					const float *Ic = Ic_cur + (st * A + c) * MG, *Im = s.Imap + (st * A + c) * MG;
+					const float *N = Nm + a * G;
+					float nmi = 0.f;
+#pragma unroll
+					for (int aa = 0; aa < MG; aa++) {
+						if (aa < G) {
+							const float id = Ic[aa] * dg;
+							nmi = fmaf(N[aa], (id + Im[aa]) * d + fac * id * omd, nmi);
+						}
+					}
+					nmi = fmaxf(nmi, 0.f);
+					const int sc = st * A + c;
+					const float eage = b.nefoi_stage ? s.eage[s.eref[sc] * G + a] : __ldg(tb.efoi_age + (size_t)s.eref[sc] * G + a);
+					minf = dt * popu * s.sus[dp] * (be[sc] * nmi + et[sc] * eage);
+				}
+			}
+			for (int tr = 0; tr < T; tr++) {
+				float v;
+				if (tr == itr) v = minf;
+				else {
+					const float popu = (float)pc[s.from[tr] * ncol + col];
+					v = popu <= 0.f ? 0.f : dt * popu * s.rate[tr * DP + dp];
+				}
+				if (tb.tm_mult) v *= __ldg(tb.tm_mult + ((size_t)sett * A + c) * T * DP + tr * DP + dp);
+				s.pm[tr * ncol + col] = v;
+			}
+			if (pn != pc)
+				for (int co = 0; co < C; co++) pn[co * ncol + col] = pc[co * ncol + col];
+		}
+		__syncthreads();
+		for (int idx = tid; idx < T * ncol; idx += NT) {
+			const int tr = idx / ncol, col = idx - tr * ncol;
+			const float mean = s.pm[idx];
+			U4 inv{0, 0, 0, 0};
+			uint32_t inv_call = 0xffffffffu;
+			int32_t n = 0;
+			if (mean > 0.f) {
+				if (mean > 1.0e9f) atomicCAS(status, 0, BEEP_COUNT_OVERFLOW);
+				else {
+					n = poisson_fp32(mean, k0, k1, (uint32_t)col, (uint32_t)tr, (uint32_t)sett, stream, inv, inv_call,
+					                 s.rcp, s.lnfact, lim);
+					if (n < 0) { atomicCAS(status, 0, BEEP_TIMEOUT); n = 0; }
+				}
+			} else if (mean != mean) atomicCAS(status, 0, BEEP_NAN_RATE);
+			const int row = s.trow[tr];
+			if (row >= 0) s.tn[row * ncol + col] = n;
+			if (n != 0) {                                // integer updates: their order does not matter
+				atomicSub(pn + s.from[tr] * ncol + col, n);
+				atomicAdd(pn + s.to[tr] * ncol + col, n);
+			}
+		}
+		__syncthreads();
+		for (int col = tid; col < ncol; col += NT) {
+			const int c = col / DP, dp = col - c * DP;
+			const int st = dp / DPS, dpl = dp - st * DPS, a = s.age[dpl];
+			float iv = 0.f;
+			for (int co = 0; co < C; co++) {
+				const float inf = s.inf[co];
+				if (inf != 0.f) iv = fmaf(inf, (float)pn[co * ncol + col], iv);
+			}
+			if (m.dp_age_unique) Ic_nxt[(st * A + c) * MG + a] = iv;
+			else atomicAdd(Ic_nxt + (st * A + c) * MG + a, iv);
+		}
+		} else {
 		for (int col = tid; col < ncol; col += NT) {
 			const int c = col / DP, dp = col - c * DP;
 			const int st = dp / DPS, dpl = dp - st * DPS, a = s.age[dpl];
@@ -818,6 +896,7 @@ __device__ __forceinline__ void sim_fast_body(const ModelDev &m, const BatchDev 
 			if (m.dp_age_unique) Ic_nxt[(st * A + c) * MG + a] = iv;
 			else atomicAdd(Ic_nxt + (st * A + c) * MG + a, iv);
 		}
+		}
 		if (sett + 1 < b.tf) slice_store<NT>(m, tb, s, nxt, sb ^ 1, sett + 1, tid);
 		__syncthreads();
 
@@ -932,11 +1011,12 @@ __device__ __forceinline__ void sim_fast_body(const ModelDev &m, const BatchDev 
 	}
 }
 
-// One CTA per particle (or MBP chain): CTA p runs particle p.
-template <int NT, int MG, bool TC, bool CH = false, int MB = min_ctas(NT), int MT = kMaxT>
+// One CTA per particle (or MBP chain): CTA p runs particle p.  PD: the draws of a step
+// one per (transition, column) thread (small models, fast_parallel_draws).
+template <int NT, int MG, bool TC, bool CH = false, int MB = min_ctas(NT), int MT = kMaxT, bool PD = false>
 __global__ void __launch_bounds__(NT, MB) sim_fast_kernel(const ModelDev m, const BatchDev b)
 {
-	sim_fast_body<NT, MG, TC, CH, MT>(m, b, blockIdx.x);
+	sim_fast_body<NT, MG, TC, CH, MT, PD>(m, b, blockIdx.x);
 }
 
 // log k! for k < 32 in this translation unit's constant memory, once (before

@@ -12,7 +12,7 @@ template <int MG, int MB>
 int launch_mb(const ModelDev &m, const BatchDev &b, size_t smem, cudaStream_t st)
 {
 	auto kern = sim_fast_kernel<kDualThreads, MG, false, false, MB>;
-	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	cudaError_t e = allow_dynamic_smem(kern, smem);
 	if (e != cudaSuccess) return (int)e;
 	kern<<<b.P, kDualThreads, smem, st>>>(m, b);
 	return (int)cudaGetLastError();

@@ -12,7 +12,7 @@ template <int MG>
 int launch_w(const ModelDev &m, const BatchDev &b, size_t smem, cudaStream_t st)
 {
 	auto kern = sim_fast_kernel<640, MG, false, false, 1, kWideT>;
-	cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	cudaError_t e = allow_dynamic_smem(kern, smem);
 	if (e != cudaSuccess) return (int)e;
 	kern<<<b.P, 640, smem, st>>>(m, b);
 	return (int)cudaGetLastError();

@@ -739,6 +739,14 @@ def run_ours(args, rank, ws, dist):
     dm = capi.DeviceModel(m, device=int(os.environ.get("LOCAL_RANK", "0")) if ws > 1 else 0)
     form = capi.FORM_FAST if args.form == "fast" else capi.FORM_PLAIN_FP64
     batch = capi.Batch(m, tabs, P, seed, group_of=group_of, stream_of=np.arange(P) + rank * P, form=form)
+    # the layout (force-of-infection path, particles per SM) chosen by the library's autotuner on
+    # a sample of this batch, unless forced by the options
+    tuned = None
+    if form == capi.FORM_FAST and args.foi == "auto" and args.ctas == 0 and not args.no_autotune:
+        t0 = time.perf_counter()
+        path = dm.autotune(batch)
+        tuned = {"foi_path": path, "seconds": time.perf_counter() - t0,
+                 "sample": "up to 64 particles per SM over 90 steps mid-horizon, each fast-form layout timed"}
     db = capi.DeviceBatch(dm, batch)
     h2d, d2h = db.bytes()
     db.upload()
@@ -841,6 +849,7 @@ def run_ours(args, rank, ws, dist):
         "foi": {0: None, 1: "fp32-simt", 2: "tensor-core split-bf16 (per particle)",
                 3: "tensor-core split-bf16 batched over particles (step-synchronous)"}[db.foi_path()],
         "particles_per_sm": db.ctas_per_sm(),
+        "autotuner": tuned,
         "plain_fp64": plain,
         "loglik_vs_fp64": acc,
         "loglik_evals_per_s": P * ws / t_dev,
@@ -891,6 +900,8 @@ def main():
                          "(library option fast_ctas_per_sm)")
     ap.add_argument("--foi", default="auto", choices=["auto", "simt", "tensor", "batched"],
                     help="force of infection of the fast form (library option fast_foi)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="skip the autotuner: the fast form's layout follows the library's static rules")
     ap.add_argument("--plain-particles", type=int, default=1024)
     ap.add_argument("--plain-steps", type=int, default=0, help="time the plain form over this many steps (0: all)")
     ap.add_argument("--mbp-sweeps", type=int, default=3,

@@ -249,7 +249,9 @@ BEEP_API beep_status beep_batch_run_graph(beep_batch *batch);
  * model supports -- force of infection on FP32 SIMT (one or several particles
  * per SM), on the tensor cores one particle per CTA, or on the tensor cores
  * batched over the particles (step-synchronous layout) -- on a sample of the
- * given batch (up to 8 particles per SM, up to 60 steps) and records the
+ * given batch (up to 64 particles per SM over a window of up to 90 steps in
+ * the middle of its range, started from the populations its first steps
+ * leave there) and records the
  * fastest on the model; later batches of the model use it while the options
  * fast_foi and fast_ctas_per_sm are automatic (when several particles per SM
  * won, each batch still takes one per SM if it is too small to fill the SMs
@@ -384,6 +386,12 @@ BEEP_API beep_status beep_log_prior(const beep_prior_spec *spec, int32_t nset, c
  *               finish sooner than one, else one), 1 = one (640-thread CTAs),
  *               2..4 = at most that many (320-thread CTAs; at most 3 above 8
  *               ages; the particles' state may then move to global memory).
+ *   "fast_parallel_draws"  the fast form's draws of a step one per (transition,
+ *               column) thread instead of a column's transitions one after
+ *               another on one thread: 0 = automatic (models whose draws fit
+ *               two passes of the CTA, in batches of at most four particles
+ *               per SM, where a step's latency sets the time), 1 = never,
+ *               2 = wherever the draws fit.  The draws are the same.
  * Unknown names or values give BEEP_BAD_INPUT. */
 BEEP_API beep_status beep_set_option(const char *name, int64_t value);
 

@@ -58,6 +58,31 @@ def test_fast_follows_fp64_trajectories(built, name):
     dm.close()
 
 
+@pytest.fixture
+def draws_option(built):
+    yield capi.set_option
+    capi.set_option("fast_parallel_draws", 0)
+
+
+@pytest.mark.parametrize("name", ["tiny_sim", "c0_sim", "strain_sim", "obsmodel_sim", "features_sim", "pred_sim", "oneage_sim"])
+def test_parallel_draws_give_the_same_trajectories(draws_option, name):
+    """Small models: a step's draws one per (transition, column) thread draw the
+    same keyed variates from the same means as the column threads drawing their
+    transitions one after another, so counts, populations and log-likelihoods are
+    identical (population updates are integer atomics, whose order does not
+    matter)."""
+    b, m, tabs, seed = load(name)
+    dm = capi.DeviceModel(m)
+    res = []
+    for opt in (1, 2):
+        draws_option("fast_parallel_draws", opt)
+        r = dm.simulate(capi.Batch(m, tabs, 24, seed, want_transnum=True, want_pop=True, form=capi.FORM_FAST))
+        res.append((r.transnum.copy(), r.pop.copy(), r.L.copy()))
+    for a, c in zip(*res):
+        assert np.array_equal(a, c)
+    dm.close()
+
+
 def test_fast_loglik_matches_fp64_of_same_trajectory(built):
     b, m, tabs, seed = load("tiny_sim")
     P = 16
