@@ -222,19 +222,37 @@ def run_serving(nreq: int, rate: float, seed: int, budget_bytes: int, inflight: 
         if dt > 0:
             time.sleep(dt)
         tickets.append(srv.submit(r["model"], r["batch"], r["kind"]))
-    for t in tickets:
-        srv.wait(t)
-    st = [srv.stats(t) for t in tickets]
+    failed = []
+    for k, t in enumerate(tickets):
+        try:
+            srv.wait(t)
+        except capi.BeepError as e:
+            # a failed request is reported (and run again alone), the stream's figures are over the others
+            r = reqs[k]
+            failed.append({"request": k, "kind": r["kind"], "size": r["size"], "particles": r["particles"],
+                           "error": str(e)})
+    ok = [k for k in range(len(tickets)) if all(f["request"] != k for f in failed)]
+    st = [srv.stats(tickets[k]) for k in ok]
     srv.close()
+    for f in failed:
+        r = reqs[f["request"]]
+        dmr = capi.DeviceModel(r["model"])
+        try:
+            out = dmr.simulate(r["batch"])
+            f["alone"] = "ok" if out.L is None or np.all(np.isfinite(out.L)) else "non-finite L"
+        except capi.BeepError as e:
+            f["alone"] = str(e)
+        dmr.close()
+    reqs_ok = [reqs[k] for k in ok]
     lat = np.array([s["done_s"] - s["submit_s"] for s in st])
     wait = np.array([s["admit_s"] - s["submit_s"] for s in st])
     svc = np.array([s["gpu_end_s"] - s["gpu_start_s"] for s in st])
     span = max(s["done_s"] for s in st) - min(s["submit_s"] for s in st)
     busy = sorted((s["gpu_start_s"], s["gpu_end_s"]) for s in st)
     overlap = sum(1 for a, b in zip(busy, busy[1:]) if b[0] < a[1])
-    for r in reqs:
+    for r in reqs_ok:
         assert r["batch"].L is None or np.all(np.isfinite(r["batch"].L))
-    units = sum(r["units"] for r in reqs)
+    units = sum(r["units"] for r in reqs_ok)
     errs = []
     for r in [r for r in reqs if r["kind"] == capi.REQ_LIKELIHOOD][:3]:
         dmr = capi.DeviceModel(r["model"])
@@ -252,8 +270,9 @@ def run_serving(nreq: int, rate: float, seed: int, budget_bytes: int, inflight: 
         "queue_wait_p99_ms": float(np.percentile(wait, 99) * 1e3),
         "service_p50_ms": float(np.percentile(svc, 50) * 1e3), "service_p99_ms": float(np.percentile(svc, 99) * 1e3),
         "throughput": units / span, "unit": "particle.area.group.steps/s",
-        "loglik_evals_per_s": sum(r["particles"] for r in reqs) / span, "makespan_s": span,
+        "loglik_evals_per_s": sum(r["particles"] for r in reqs_ok) / span, "makespan_s": span,
         "overlapping_request_pairs": overlap,
+        "failed_requests": failed,
         "kinds": {k: sum(1 for r in reqs if r["kind"] == i) for i, k in enumerate(("likelihood", "scenario",
                                                                                    "prediction"))},
         "form": "fast", "data": "synthetic, generated per request",
@@ -569,10 +588,28 @@ def run_serving_precision(nreq: int, seed: int, model, tables, plain_evals_per_s
         if dt > 0:
             time.sleep(dt)
         tickets.append(srv.submit(model, b, capi.REQ_LIKELIHOOD))
-    for t in tickets:
-        srv.wait(t)
-    st = [srv.stats(t) for t in tickets]
+    failed = []
+    for k, t in enumerate(tickets):
+        try:
+            srv.wait(t)
+        except capi.BeepError as e:
+            # a failed request is reported (and run again alone), the stream's figures are over the others
+            r = reqs[k]
+            failed.append({"request": k, "kind": r["kind"], "size": r["size"], "particles": r["particles"],
+                           "error": str(e)})
+    ok = [k for k in range(len(tickets)) if all(f["request"] != k for f in failed)]
+    st = [srv.stats(tickets[k]) for k in ok]
     srv.close()
+    for f in failed:
+        r = reqs[f["request"]]
+        dmr = capi.DeviceModel(r["model"])
+        try:
+            out = dmr.simulate(r["batch"])
+            f["alone"] = "ok" if out.L is None or np.all(np.isfinite(out.L)) else "non-finite L"
+        except capi.BeepError as e:
+            f["alone"] = str(e)
+        dmr.close()
+    reqs_ok = [reqs[k] for k in ok]
     span = max(x["done_s"] for x in st) - min(x["submit_s"] for x in st)
     lat = np.array([x["done_s"] - x["submit_s"] for x in st])
     svc = np.array([x["gpu_end_s"] - x["gpu_start_s"] for x in st])
