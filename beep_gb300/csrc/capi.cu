@@ -369,7 +369,12 @@ beep_status beep_model_create(const beep_model_desc *d, beep_model **out)
 	}
 	cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
 	if (e == cudaSuccess) e = m->model_mem.reserve(L.size);
-	if (e == cudaSuccess) e = cudaMemcpy(m->model_mem.ptr, host.data(), L.size, cudaMemcpyHostToDevice);
+	// on the model's stream, waited for: a cudaMemcpy from pageable memory may return
+	// before its last bytes land, and the model's (non-blocking) stream would not wait for
+	// the legacy stream's copy
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(m->model_mem.ptr, host.data(), L.size, cudaMemcpyHostToDevice, m->stream);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
 	if (e != cudaSuccess) {
 		beep_model_destroy(m);
 		return fail(e == cudaErrorMemoryAllocation ? BEEP_OOM : BEEP_DEVICE_ERROR, std::string("model upload: ") + cudaGetErrorString(e));

@@ -236,7 +236,10 @@ BEEP_API beep_status beep_mbp_set_state(beep_mbp_chains *c, const beep_mbp_reque
 				to_fast_layout(c, src, tmp.data());
 				src = tmp.data();
 			}
-			CUDA_TRY(cudaMemcpy(c->tn + off, src, 4 * per, cudaMemcpyHostToDevice));
+			// on the model's stream (the chain kernels' stream), completed before the
+			// host buffer is reused
+			CUDA_TRY(cudaMemcpyAsync(c->tn + off, src, 4 * per, cudaMemcpyHostToDevice, c->m->stream));
+			CUDA_TRY(cudaStreamSynchronize(c->m->stream));
 		}
 	}
 	beep_status st = run_chains(c, r, 3, false, nullptr);

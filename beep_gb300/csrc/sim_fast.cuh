@@ -1030,6 +1030,9 @@ inline int prepare_constants()
 	float lf[32];
 	for (int k = 0; k < 32; k++) lf[k] = (float)std::lgamma((double)k + 1.0);
 	cudaError_t e = cudaMemcpyToSymbol(c_lnfact, lf, sizeof lf);
+	// a copy from pageable memory may return before its bytes land, and the kernels run on
+	// non-blocking streams that do not wait for the legacy stream: wait for it here
+	if (e == cudaSuccess) e = cudaStreamSynchronize(cudaStreamLegacy);
 	if (e != cudaSuccess) return (int)e;
 	done = true;
 	return 0;
