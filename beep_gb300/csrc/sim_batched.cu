@@ -5,21 +5,26 @@
 //
 //   Y[(p,st,a)][t] = sum_c I[(p,st,a)][c] * M[c][t]       [P*NS*G x A] . [A x A]
 //
-// Per step two kernels run on the model's stream:
-//   bx_foi   the product, one CTA per 128 rows (particle, strain, age):
-//            tcgen05.mma kind::f16 with M = 128 rows, N = the target chunks
-//            of the model's matrix image (foi_tc.cuh: three BF16 pieces
-//            Mh + Mm + Ml of M[c][t], K-major, streamed from L2 by bulk
-//            copies), K = sources in chunks of 32.  The counts are split
-//            into two BF16 pieces Ih + Il (exact below 65536) while the CTA
-//            stages them into shared memory, and the five products
-//            Ih.Mh, Ih.Mm, Ih.Ml, Il.Mh, Il.Mm accumulate in FP32 in tensor
-//            memory (the dropped Il.Ml is below 2^-24 of each term).
-//   bx_step  per particle (CTAs take particles from a counter): the strain
-//            shift, NMI, transition means, keyed FP32 draws and population
+// Per step three kernels run on the model's stream:
+//   bx_foi   the product, one CTA per (128-row tile of (particle, strain,
+//            age) rows, target chunk): tcgen05.mma kind::f16 with M = 128
+//            rows, N = the chunk's targets of the model's matrix image
+//            (foi_tc.cuh: three BF16 pieces Mh + Mm + Ml of M[c][t],
+//            K-major), K = sources in chunks of 32; thread 0 keeps two
+//            stages full with bulk copies of the A block and the matrix chunk.
+//            The counts are split into two BF16 pieces Ih + Il (exact below
+//            65536) when the previous step's observation kernel packs them,
+//            and the five products Ih.Mh, Ih.Mm, Ih.Ml, Il.Mh, Il.Mm
+//            accumulate in FP32 in tensor memory (the dropped Il.Ml is below
+//            2^-24 of each term).
+//   bx_step  CTAs take (particle, column chunk) items from the step's counter:
+//            NMI, transition means, keyed FP32 draws and the population
 //            update per column (c, dp), with the same arithmetic and the same
-//            variate streams as the fast kernel of sim_fast.cuh; the next
-//            step's infectious counts; then the step's observation terms.
+//            variate streams as the fast kernel of sim_fast.cuh, and the
+//            next step's infectious counts.
+//   bx_obs   one CTA per particle: the step's observation terms (completed
+//            observations -> compensated log-density sums), the next
+//            product's A operand and the next step's strain shift.
 // The particles' populations, infectious counts, contraction, observation
 // slots and compensated log-likelihood partials stay in global memory (L2)
 // between steps; bx_init sets them up and bx_final reduces L in FP64.
