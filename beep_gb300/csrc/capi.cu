@@ -879,6 +879,11 @@ beep_status beep::batch_create_internal(beep_model *m, const beep_sim_batch *b, 
 		const int nt_run = q->bd.nt > 0 ? q->bd.nt : fast_pick_threads(m->dev);
 		q->bd.pd = !wide && !q->bd.foi_tc && !q->bd.batched && fast_pd_fits(m->dev, nt_run) && popt != 1 &&
 		           (popt == 2 || (long long)P <= 4LL * std::max(1, m->sms)) ? 1 : 0;
+		// one pass of 256 threads over the draws instead of two of 128, where the batch
+		// leaves room for the larger CTAs (two per SM)
+		if (q->bd.pd && popt != 2 && nt_run == 128 && (long long)m->T * m->A * m->DP > 128 &&
+		    (long long)P <= 2LL * std::max(1, m->sms))
+			q->bd.nt = 256;
 	}
 	auto bail = [&](beep_status s) { beep_batch_destroy(q); return s; };
 	if (b->form == BEEP_FORM_FAST && fast_prepare() != 0) return bail(fail(BEEP_DEVICE_ERROR, "constant tables"));

@@ -101,6 +101,9 @@ beep_status prepare_chains(beep_mbp_chains *c, const beep_mbp_request *r, int mo
 		c->q[slot] = nullptr;
 		st = batch_create_internal(m, &b, false, &q, false, false, true);
 		if (st != BEEP_OK) return st;
+		// the chain kernels draw per column thread, in the model's own CTA size
+		q->bd.pd = 0;
+		if (q->b.form == BEEP_FORM_FAST && q->bd.nt == 256 && fast_pick_threads(m->dev) == 128) q->bd.nt = 0;
 		c->q[slot] = q;
 		c->q_ngroup[slot] = b.ngroup;
 		c->q_go[slot] = b.group_of != nullptr;

@@ -89,7 +89,9 @@ int launch_sim_fast(const ModelDev &m, const BatchDev &b, void *stream)
 		if (!m.tc_image || pick_threads(m) != 640 || b.tc_smem_off < smem) return (int)cudaErrorInvalidValue;
 		smem = b.tc_smem_off + fast_tc_smem_bytes(m);
 	}
-	if (nt != pick_threads(m) && (nt != kDualThreads || b.foi_tc)) return (int)cudaErrorInvalidValue;
+	// (256 threads for a 128-thread model: its draws in one pass, parallel-draw batches)
+	if (nt != pick_threads(m) && (nt != kDualThreads || b.foi_tc) && !(pd && nt == 256))
+		return (int)cudaErrorInvalidValue;
 	{
 		const int e = fast_prepare();
 		if (e != 0) return e;
