@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(kBxStepThreads, MB) bx_step(const ModelDev m, 
 {
 	constexpr int NT = kBxStepThreads;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
-	__shared__ int next_item, cur_group;
+	__shared__ int next_item, cur_group, reload;
 	const int tid = threadIdx.x;
 	const int A = m.A, G = m.G, DP = m.DP, NS = m.NS, DPS = m.DPS, C = m.C, T = m.T;
 	const int ncol = A * DP, popsz = C * ncol, tnsz = T * ncol;
@@ -362,14 +362,24 @@ __global__ void __launch_bounds__(kBxStepThreads, MB) bx_step(const ModelDev m, 
 	float *Icn_all = b.bx_ic + (size_t)(cur ^ 1) * rows_ic;
 	for (;;) {
 		__syncthreads();                            // the previous item is finished with shared memory
-		if (tid == 0) next_item = atomicAdd(b.bx_work + s_rel, 1);
+		if (tid == 0) {
+			// the next item, and whether its parameter set's tables must be loaded: decided
+			// by one thread before the barrier, so that every thread takes the same branch
+			// (the tables' barrier below is reached by all threads or by none)
+			const int it = atomicAdd(b.bx_work + s_rel, 1);
+			next_item = it;
+			if (it < nitem) {
+				const int g = b.group_of ? b.group_of[it / nchunk] : 0;
+				reload = g != cur_group;
+				cur_group = g;
+			}
+		}
 		__syncthreads();
 		const int item = next_item;
 		if (item >= nitem) break;
 		const int p = item / nchunk, k = item - p * nchunk;
-		const int grp = b.group_of ? b.group_of[p] : 0;
 		const Tabs tb = bx_tabs(b, p);
-		if (grp != cur_group) {                     // the parameter set's rates and slices (kept while it repeats)
+		if (reload) {                               // the parameter set's rates and slices (kept while it repeats)
 			for (int j = tid; j < T * DP; j += NT) rate[j] = tb.rate[j];
 			for (int j = tid; j < DP; j += NT) sus[j] = tb.sus[j];
 			for (int j = tid; j < C; j += NT) inf[j] = tb.inf[j];
@@ -382,10 +392,7 @@ __global__ void __launch_bounds__(kBxStepThreads, MB) bx_step(const ModelDev m, 
 				et[i] = e;
 			}
 			for (int j = tid; j < G * G; j += NT) Nm[j] = __ldg(tb.Ntime + (size_t)sett * G * G + j);
-			if (tid == 0) {
-				dgeo[0] = __ldg(tb.geo + sett);
-				cur_group = grp;
-			}
+			if (tid == 0) dgeo[0] = __ldg(tb.geo + sett);
 			__syncthreads();
 		}
 		const uint32_t stream = b.stream_of ? b.stream_of[p] : (uint32_t)p;
