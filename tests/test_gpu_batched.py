@@ -75,6 +75,29 @@ def test_batched_follows_fp64_trajectories(built, case):
     dm.close()
 
 
+def test_batched_parameter_set_per_particle(built):
+    """ABC-SMC-like batch: every particle has its own parameter set (R0, 1/sigma,
+    1/gamma from the priors), so the step kernel reloads a set's rates and table
+    slices at nearly every work item; the particles follow the FP64 form's
+    trajectories under their own sets."""
+    from beep_gb300 import model_builder as mb, synth
+    w = synth.seir_hd_small(seed=20260209, narea=100, nage=3, days=60, name="mid_groups")
+    m = capi.Model(mb.model_arrays(w))
+    P = 48
+    R0, si, gi = synth.abc_smc_priors(np.random.default_rng(5), P)
+    tabs = [capi.Tables(t) for t in mb.param_tables_batch(w, R0, si, gi)]
+    go = np.arange(P)
+    dm = capi.DeviceModel(m)
+    g = dm.simulate(capi.Batch(m, tabs, P, 31, group_of=go, want_transnum=True, want_pop=True))
+    db = _batched(dm, m, tabs, P, 31, group_of=go, want_transnum=True, want_pop=True)
+    f = db.run()
+    db.close()
+    same = np.array([np.array_equal(f.transnum[p], g.transnum[p]) for p in range(P)])
+    assert same.mean() >= 0.6, same.mean()
+    np.testing.assert_allclose(f.L[same], g.L[same], rtol=L_RTOL_FAST)
+    dm.close()
+
+
 def test_batched_uneven_tile_and_particle_counts(built):
     """Particle counts whose rows (particle x age) do not fill the last
     128-row tile, and more particles than the step kernel's CTAs (particles
