@@ -121,15 +121,35 @@ __device__ __forceinline__ int32_t poisson_fp32(float mean, uint32_t k0, uint32_
 	U4 r0{0, 0, 0, 0};
 	if (__any_sync(act, big)) r0 = philox10(U4{col, sett, stream, (PURPOSE_PTRS << 24) | (tr << 16)}, k0, k1);
 	if (!big) {
+		// sequential search of the FP32 CDF: the smallest k with u <= F(k), or the k at
+		// which adding p(k) no longer changes F (the FP32 tail is exhausted), at most 63.
+		// kInvTerms terms per pass: the same products and sums in the same order as one
+		// term per pass, so the same k, with fewer of the loop's passes and branches
+		constexpr int kInvTerms = 2;
 		const float u = u01_f(word_of(inv, tr & 3u));
 		float p = expf(-mean);
 		float F = p;
 		int32_t k = 0;
-		while (u > F && k < 63) {
+		if (!(u > F)) return 0;
+		while (k <= 63 - kInvTerms) {
+			float pt[kInvTerms], Ft[kInvTerms];
+#pragma unroll
+			for (int j = 0; j < kInvTerms; j++) {
+				pt[j] = (j == 0 ? p : pt[j - 1]) * mean * rcp[k + 1 + j];
+				Ft[j] = (j == 0 ? F : Ft[j - 1]) + pt[j];
+			}
+#pragma unroll
+			for (int j = 0; j < kInvTerms; j++)       // exhausted at k + 1 + j, or u <= F(k + 1 + j)
+				if (Ft[j] == (j == 0 ? F : Ft[j - 1]) || !(u > Ft[j])) return k + 1 + j;
+			k += kInvTerms;
+			p = pt[kInvTerms - 1];
+			F = Ft[kInvTerms - 1];
+		}
+		while (u > F && k < 63) {                      // the last terms, one at a time
 			k++;
 			p = p * mean * rcp[k];
 			const float Fn = F + p;
-			if (Fn == F) break;          // FP32 tail exhausted
+			if (Fn == F) break;
 			F = Fn;
 		}
 		return k;
