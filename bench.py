@@ -12,6 +12,14 @@ step is one full simulation + log-likelihood of every particle.
           parameter tables into pinned memory, host->device copy, kernels,
           device->host copy of the log-likelihoods, every step (the device
           work of a step replayed as one CUDA graph).
+The layout of the fast form is the one the library's autotuner picks on a
+sample of the batch (``--no-autotune``: its static rules).  After the main
+line's figures the bench measures, on the same GPU, the 350-area x 10-age
+precision batch, the serving engine (a 350x10 likelihood stream and the mixed
+serving stream at 200 and 4 requests/s), the MBP chains of uneven size (one
+fused launch per sweep, and as four launches), the particle filter (one, and
+sixteen at once), the ABC-SMC weights, the plain FP64 form and the fast form's
+log-likelihood error against FP64 per configuration.
 
 ``--impl reference`` times the reference's CPU algorithm for the same
 workload on this host's cores (the oracle restatement, all threads, a bounded
